@@ -1,0 +1,1130 @@
+/*
+ * imd_oracle.c -- CPU restatement of IMD's force / neighbour-list / NVE / CG
+ * hot path (itapmd/imd, src/imd_forces_nbl.c, src/potaccess.h,
+ * src/imd_potential.c, src/imd_geom_3d.c, src/imd_comm_force_3d.c,
+ * src/imd_fix_cells_3d.c, src/imd_integrate.c, src/imd_cg.c,
+ * src/cg_utils.h).
+ *
+ * TEST INFRASTRUCTURE ONLY: the checker for the GPU library and the timed
+ * CPU baseline.  Never linked into the product.
+ *
+ * Build with -ffp-contract=off: the reference is compiled without fused
+ * multiply-add, and r^2 / table-index / cell-index bits depend on it.
+ */
+#include "imd_oracle.h"
+
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define OMIN(a, b) ((a) < (b) ? (a) : (b))
+#define OMAX(a, b) ((a) > (b) ? (a) : (b))
+#define SQR(a) ((a) * (a))
+
+/* ------------------------------------------------------------------------ */
+/* tables                                                                    */
+/* ------------------------------------------------------------------------ */
+
+static int alloc_info(orc_table_t *pt, int ncols) {
+  pt->ncols = ncols;
+  pt->maxsteps = 0;
+  pt->begin = (double *)calloc(ncols, sizeof(double));
+  pt->end = (double *)calloc(ncols, sizeof(double));
+  pt->step = (double *)calloc(ncols, sizeof(double));
+  pt->invstep = (double *)calloc(ncols, sizeof(double));
+  pt->len = (int *)calloc(ncols, sizeof(int));
+  pt->table = NULL;
+  return (pt->begin && pt->end && pt->step && pt->invstep && pt->len) ? 0 : 1;
+}
+
+void orc_free_table(orc_table_t *pt) {
+  free(pt->begin);
+  free(pt->end);
+  free(pt->step);
+  free(pt->invstep);
+  free(pt->len);
+  free(pt->table);
+  memset(pt, 0, sizeof(*pt));
+}
+
+/* init_threepoint (src/imd_potential.c:1256-1272): continue the last
+ * interpolation polynomial into rows len and len+1. */
+static void threepoint(orc_table_t *pt) {
+  int nc = pt->ncols;
+  for (int col = 0; col < nc; col++) {
+    double *y = pt->table + col;
+    int n = pt->len[col];
+    if (n < 3) continue;
+    y[n * nc] = 3 * y[(n - 1) * nc] - 3 * y[(n - 2) * nc] + y[(n - 3) * nc];
+    y[(n + 1) * nc] =
+        6 * y[(n - 1) * nc] - 8 * y[(n - 2) * nc] + 3 * y[(n - 3) * nc];
+  }
+}
+
+/* format 1 (src/imd_potential.c:297-376): lines "r2 v_0 ... v_{ncols-1}",
+ * end = r2 of the last nonzero value, len = its row + 1, shift by the value
+ * of the last row. */
+static int read_format1(orc_table_t *pt, FILE *in, int radial, double *cellsz,
+                        char *err, int errlen) {
+  int nc = pt->ncols, npot = 0, cap = 50;
+  double r2 = 0.0, r2_start = 0.0, val;
+  pt->table = (double *)malloc((size_t)nc * cap * sizeof(double));
+  for (;;) {
+    if (npot == cap) {
+      cap += 50;
+      pt->table = (double *)realloc(pt->table, (size_t)nc * cap * sizeof(double));
+    }
+    if (1 != fscanf(in, "%lf", &r2)) break;
+    if (npot == 0) r2_start = r2;
+    for (int i = 0; i < nc; i++) {
+      if (1 != fscanf(in, "%lf", &val)) {
+        snprintf(err, errlen, "Line incomplete in potential file.");
+        return 1;
+      }
+      pt->table[npot * nc + i] = val;
+      if (val != 0.0) {
+        pt->end[i] = r2;
+        pt->len[i] = npot + 1;
+      }
+    }
+    npot++;
+  }
+  if (npot < 2) {
+    snprintf(err, errlen, "table too short");
+    return 1;
+  }
+  double r2_step = (r2 - r2_start) / (npot - 1);
+  pt->maxsteps = cap;
+  for (int i = 0; i < nc; i++) {
+    pt->begin[i] = r2_start;
+    pt->step[i] = r2_step;
+    pt->invstep[i] = 1.0 / r2_step;
+    double delta = pt->table[(npot - 1) * nc + i];
+    if (radial && delta != 0.0)
+      for (int k = 0; k < npot; k++) pt->table[k * nc + i] -= delta;
+    if (radial) *cellsz = OMAX(*cellsz, pt->end[i]);
+  }
+  pt->table = (double *)realloc(pt->table, (size_t)nc * (cap + 2) * sizeof(double));
+  for (int k = npot; k < cap + 2; k++)
+    for (int i = 0; i < nc; i++) pt->table[k * nc + i] = 0.0;
+  return 0;
+}
+
+/* format 2 (src/imd_potential.c:394-462): per column "begin end step", then
+ * len values per column; shift radial columns by their last value. */
+static int read_format2(orc_table_t *pt, FILE *in, int radial, double *cellsz,
+                        char *err, int errlen) {
+  int nc = pt->ncols;
+  for (int i = 0; i < nc; i++) {
+    if (3 != fscanf(in, "%lf %lf %lf", &pt->begin[i], &pt->end[i], &pt->step[i])) {
+      snprintf(err, errlen, "Info line corrupt.");
+      return 1;
+    }
+    if (radial) *cellsz = OMAX(*cellsz, pt->end[i]);
+    pt->invstep[i] = 1.0 / pt->step[i];
+    double numstep = 1 + (pt->end[i] - pt->begin[i]) / pt->step[i];
+    pt->len[i] = (int)(numstep + 0.49);
+    pt->maxsteps = OMAX(pt->maxsteps, pt->len[i]);
+  }
+  size_t tsize = (size_t)nc * (pt->maxsteps + 2);
+  pt->table = (double *)calloc(tsize, sizeof(double));
+  for (int i = 0; i < nc; i++)
+    for (int k = 0; k < pt->len[i]; k++) {
+      double val;
+      if (1 != fscanf(in, "%lf", &val)) {
+        snprintf(err, errlen, "wrong format in potential file.");
+        return 1;
+      }
+      pt->table[k * nc + i] = val;
+    }
+  if (radial)
+    for (int i = 0; i < nc; i++) {
+      double delta = pt->table[(pt->len[i] - 1) * nc + i];
+      if (delta != 0.0)
+        for (int k = 0; k < pt->len[i]; k++) pt->table[k * nc + i] -= delta;
+    }
+  return 0;
+}
+
+/* read_pot_table (src/imd_potential.c:161-282): header "#F fmt ncols" ...
+ * "#E"; no header means the build's default format. */
+int orc_read_table(orc_table_t *pt, const char *fname, int ncols, int radial,
+                   int default_format, double *cellsz, char *err, int errlen) {
+  char buf[1024];
+  int have_header = 0, have_format = 0, end_header = 0;
+  int format = default_format, size = ncols;
+  FILE *in = fopen(fname, "r");
+  if (!in) {
+    snprintf(err, errlen, "Could not open potential file %s", fname);
+    return 1;
+  }
+  do {
+    if (!fgets(buf, sizeof buf, in)) {
+      snprintf(err, errlen, "Unexpected end of file in %s", fname);
+      fclose(in);
+      return 1;
+    }
+    if (buf[0] == '#') {
+      have_header = 1;
+      end_header = (buf[1] == 'E');
+      if (buf[1] == 'F') {
+        if (2 != sscanf(buf + 2, "%d%d", &format, &size)) {
+          snprintf(err, errlen, "Corrupted format header line in file %s", fname);
+          fclose(in);
+          return 1;
+        }
+        if (size != ncols) {
+          snprintf(err, errlen, "Wrong number of data columns in file %s", fname);
+          fclose(in);
+          return 1;
+        }
+        if (format != 1 && format != 2) {
+          snprintf(err, errlen, "Unrecognized format specified for file %s", fname);
+          fclose(in);
+          return 1;
+        }
+        have_format = 1;
+      }
+    } else if (have_header) {
+      snprintf(err, errlen, "Corrupted header in file %s", fname);
+      fclose(in);
+      return 1;
+    } else {
+      end_header = 1;
+    }
+  } while (!end_header);
+  if (have_header && !have_format) {
+    snprintf(err, errlen, "Format not specified in header of file %s", fname);
+    fclose(in);
+    return 1;
+  }
+  if (!have_header) rewind(in);
+  if (alloc_info(pt, ncols)) {
+    fclose(in);
+    return 1;
+  }
+  int rc = (format == 1) ? read_format1(pt, in, radial, cellsz, err, errlen)
+                         : read_format2(pt, in, radial, cellsz, err, errlen);
+  fclose(in);
+  if (rc) return rc;
+  threepoint(pt);
+  return 0;
+}
+
+int orc_make_table(orc_table_t *pt, int ncols, const double *begin,
+                   const double *end, const double *step, const double *vals,
+                   const int *len, int radial, double *cellsz) {
+  if (alloc_info(pt, ncols)) return 1;
+  for (int i = 0; i < ncols; i++) {
+    pt->begin[i] = begin[i];
+    pt->end[i] = end[i];
+    pt->step[i] = step[i];
+    pt->invstep[i] = 1.0 / step[i];
+    pt->len[i] = len[i];
+    pt->maxsteps = OMAX(pt->maxsteps, len[i]);
+    if (radial) *cellsz = OMAX(*cellsz, end[i]);
+  }
+  pt->table = (double *)calloc((size_t)ncols * (pt->maxsteps + 2), sizeof(double));
+  long off = 0;
+  for (int i = 0; i < ncols; i++) {
+    for (int k = 0; k < len[i]; k++) pt->table[k * ncols + i] = vals[off + k];
+    off += len[i];
+  }
+  if (radial)
+    for (int i = 0; i < ncols; i++) {
+      double delta = pt->table[(len[i] - 1) * ncols + i];
+      if (delta != 0.0)
+        for (int k = 0; k < len[i]; k++) pt->table[k * ncols + i] -= delta;
+    }
+  threepoint(pt);
+  return 0;
+}
+
+/* shared index computation of PAIR_INT2/VAL_FUNC2/DERIV_FUNC2
+ * (src/potaccess.h:323-345) */
+static inline void tab_row(const orc_table_t *pt, int col, int inc, double r2,
+                           double *chi, double *istep, double *p0, double *p1,
+                           double *p2, int *is_short) {
+  double r2a = OMIN(r2, pt->end[col]);
+  r2a = r2a - pt->begin[col];
+  if (r2a < 0) {
+    r2a = 0;
+    *is_short = 1;
+  }
+  *istep = pt->invstep[col];
+  r2a = r2a * (*istep);
+  int k = (int)r2a;
+  *chi = r2a - k;
+  const double *ptr = pt->table + (long)k * inc + col;
+  *p0 = ptr[0];
+  *p1 = ptr[inc];
+  *p2 = ptr[2 * inc];
+}
+
+void orc_pair_int2(const orc_table_t *pt, int col, int inc, double r2,
+                   double *pot, double *grad, int *is_short) {
+  double chi, istep, p0, p1, p2;
+  tab_row(pt, col, inc, r2, &chi, &istep, &p0, &p1, &p2, is_short);
+  double dv = p1 - p0;
+  double d2v = p2 - 2 * p1 + p0;
+  *pot = p0 + chi * dv + 0.5 * chi * (chi - 1) * d2v;
+  *grad = 2 * istep * (dv + (chi - 0.5) * d2v);
+}
+
+double orc_val_func2(const orc_table_t *pt, int col, int inc, double r2,
+                     int *is_short) {
+  double chi, istep, p0, p1, p2;
+  tab_row(pt, col, inc, r2, &chi, &istep, &p0, &p1, &p2, is_short);
+  double dv = p1 - p0;
+  double d2v = p2 - 2 * p1 + p0;
+  return p0 + chi * dv + 0.5 * chi * (chi - 1) * d2v;
+}
+
+double orc_deriv_func2(const orc_table_t *pt, int col, int inc, double r2,
+                       int *is_short) {
+  double chi, istep, p0, p1, p2;
+  tab_row(pt, col, inc, r2, &chi, &istep, &p0, &p1, &p2, is_short);
+  double dv = p1 - p0;
+  double d2v = p2 - 2 * p1 + p0;
+  return 2 * istep * (dv + (chi - 0.5) * d2v);
+}
+
+void orc_pair_int2_batch(const orc_table_t *pt, int col, int inc, int n,
+                         const double *r2, double *pot, double *grad) {
+  int is_short = 0;
+  for (int i = 0; i < n; i++) orc_pair_int2(pt, col, inc, r2[i], pot + i, grad + i, &is_short);
+}
+
+/* ------------------------------------------------------------------------ */
+/* system set-up                                                             */
+/* ------------------------------------------------------------------------ */
+
+int orc_init(orc_sys_t *s, int n) {
+  /* keep caller-set parameters, reset everything else */
+  s->n = n;
+  s->number = (int *)calloc(n, sizeof(int));
+  s->type = (int *)calloc(n, sizeof(int));
+  s->mass = (double *)calloc(n, sizeof(double));
+  s->x = (double *)calloc(3 * (size_t)n, sizeof(double));
+  s->p = (double *)calloc(3 * (size_t)n, sizeof(double));
+  s->f = (double *)calloc(3 * (size_t)n, sizeof(double));
+  s->epot = (double *)calloc(n, sizeof(double));
+  s->eam_rho = (double *)calloc(n, sizeof(double));
+  s->eam_df = (double *)calloc(n, sizeof(double));
+  s->nbl_pos = (double *)calloc(3 * (size_t)n, sizeof(double));
+  s->old_x = (double *)calloc(3 * (size_t)n, sizeof(double));
+  s->cg_g = (double *)calloc(3 * (size_t)n, sizeof(double));
+  s->cg_h = (double *)calloc(3 * (size_t)n, sizeof(double));
+  s->order = (int *)calloc(n, sizeof(int));
+  s->tl = (int *)calloc((size_t)n + 1, sizeof(int));
+  s->next = 0;
+  s->next_cap = 0;
+  s->ex = NULL;
+  s->etype = s->esrc = s->eowner = NULL;
+  s->eshift = s->ef = s->eepot = s->erho = s->edf = NULL;
+  s->tb = NULL;
+  s->nb_cap = s->nb_len = 0;
+  s->have_valid_nbl = 0;
+  s->nbl_count = s->nfc = 0;
+  s->cell_start = s->cell_cnt = s->cell_atoms = NULL;
+  s->real_cells = s->cnbrs = NULL;
+  s->old_alphamin = 0.1; /* static in linmin, src/imd_cg.c:99 */
+  s->nactive = 3L * n;
+  if (s->linmin_maxsteps <= 0) s->linmin_maxsteps = 100;
+  if (s->linmin_tol <= 0) s->linmin_tol = 0.0002;
+  if (s->linmin_dmax <= 0) s->linmin_dmax = 0.01;
+  if (s->linmin_dmin <= 0) s->linmin_dmin = 0.001;
+  if (s->cg_glimit <= 0) s->cg_glimit = 100;
+  if (s->cg_zeps <= 0) s->cg_zeps = 1e-10;
+  return (s->number && s->type && s->x && s->p && s->f && s->tl) ? 0 : 1;
+}
+
+void orc_free(orc_sys_t *s) {
+  free(s->number); free(s->type); free(s->mass); free(s->x); free(s->p);
+  free(s->f); free(s->epot); free(s->eam_rho); free(s->eam_df);
+  free(s->nbl_pos); free(s->old_x); free(s->cg_g); free(s->cg_h);
+  free(s->order); free(s->tl); free(s->tb); free(s->ex); free(s->etype);
+  free(s->esrc); free(s->eowner); free(s->eshift); free(s->ef);
+  free(s->eepot); free(s->erho); free(s->edf); free(s->cell_start);
+  free(s->cell_cnt); free(s->cell_atoms); free(s->real_cells); free(s->cnbrs);
+  orc_free_table(&s->pair);
+  orc_free_table(&s->rho);
+  orc_free_table(&s->embed);
+}
+
+/* vec_prod (src/imd_geom_3d.c:36-43) */
+static void vec_prod(const double *u, const double *v, double *w) {
+  w[0] = u[1] * v[2] - u[2] * v[1];
+  w[1] = u[2] * v[0] - u[0] * v[2];
+  w[2] = u[0] * v[1] - u[1] * v[0];
+}
+static inline double sprod(const double *a, const double *b) {
+  return a[0] * b[0] + a[1] * b[1] + a[2] * b[2];
+}
+
+/* make_box (src/imd_geom_3d.c:52-106), init_cells with NBLIST
+ * (:113-200; margin added once :122-126) and make_cell_lists with AR
+ * (:823-947). */
+int orc_setup_geometry(orc_sys_t *s) {
+  vec_prod(s->box[1], s->box[2], s->tbox[0]);
+  vec_prod(s->box[2], s->box[0], s->tbox[1]);
+  vec_prod(s->box[0], s->box[1], s->tbox[2]);
+  s->volume = sprod(s->box[0], s->tbox[0]);
+  if (s->volume == 0) return 1;
+  for (int a = 0; a < 3; a++)
+    for (int c = 0; c < 3; c++) s->tbox[a][c] /= s->volume;
+  for (int a = 0; a < 3; a++) s->height[a] = 1.0 / sprod(s->tbox[a], s->tbox[a]);
+
+  s->cellsz = SQR(sqrt((double)s->cellsz) + s->nbl_margin);
+  for (int a = 0; a < 3; a++) {
+    double scale = sqrt(1.0 * s->cellsz / s->height[a]);
+    s->gdim[a] = (int)(1.0 / scale);
+    if (s->gdim[a] < 1) return 2; /* "global_cell_dim too small" */
+    s->cdim[a] = s->gdim[a] + 2;
+  }
+  int cx = s->cdim[0], cy = s->cdim[1], cz = s->cdim[2];
+  s->nallcells = cx * cy * cz;
+  s->nreal_cells = s->gdim[0] * s->gdim[1] * s->gdim[2];
+  s->real_cells = (int *)malloc(sizeof(int) * s->nreal_cells);
+  s->cnbrs = (int *)malloc(sizeof(int) * 14 * s->nreal_cells);
+  int l = 0;
+  for (int i = 1; i < cx - 1; i++)
+    for (int j = 1; j < cy - 1; j++)
+      for (int k = 1; k < cz - 1; k++) {
+        int np = i * cy * cz + j * cz + k;
+        int *nq = s->cnbrs + 14 * l;
+        s->real_cells[l] = np;
+        nq[0] = np;
+        int nn = 1;
+        for (int a = 0; a <= 1; a++)
+          for (int b = -a; b <= 1; b++)
+            for (int c = (a == 0 ? -b : -a); c <= 1; c++) {
+              int r = i + a, t2 = j + b, u = k + c;
+              int qq = r * cy * cz + t2 * cz + u;
+              if (qq == np) continue;
+              int gr = r - 1, gs = t2 - 1, gt = u - 1;
+              int px = (gr < 0) ? -1 : (gr > s->gdim[0] - 1) ? 1 : 0;
+              int py = (gs < 0) ? -1 : (gs > s->gdim[1] - 1) ? 1 : 0;
+              int pz = (gt < 0) ? -1 : (gt > s->gdim[2] - 1) ? 1 : 0;
+              if ((s->pbc[0] == 1 || px == 0) && (s->pbc[1] == 1 || py == 0) &&
+                  (s->pbc[2] == 1 || pz == 0))
+                nq[nn] = qq;
+              else
+                nq[nn] = -1;
+              nn++;
+            }
+        l++;
+      }
+  s->cell_start = (int *)calloc(s->nallcells + 1, sizeof(int));
+  s->cell_cnt = (int *)calloc(s->nallcells, sizeof(int));
+  return 0;
+}
+
+/* cell_coord (src/imd_geom_3d.c:1054-1074) */
+static void cell_coord(const orc_sys_t *s, const double *x, int *c) {
+  for (int a = 0; a < 3; a++) {
+    int v = (int)(s->gdim[a] * (x[0] * s->tbox[a][0] + x[1] * s->tbox[a][1] +
+                                x[2] * s->tbox[a][2]));
+    if (v >= s->gdim[a]) v = s->gdim[a] - 1;
+    else if (v < 0) v = 0;
+    c[a] = v;
+  }
+}
+
+/* do_boundaries (src/imd_main_3d.c:1972-2010) */
+static void wrap_atom(const orc_sys_t *s, double *x) {
+  for (int a = 0; a < 3; a++) {
+    if (s->pbc[a] != 1) continue;
+    double i = -floor(x[0] * s->tbox[a][0] + x[1] * s->tbox[a][1] + x[2] * s->tbox[a][2]);
+    x[0] += i * s->box[a][0];
+    x[1] += i * s->box[a][1];
+    x[2] += i * s->box[a][2];
+  }
+}
+
+static void ensure_ext(orc_sys_t *s, int need) {
+  if (need <= s->next_cap) return;
+  int cap = need + need / 4 + 64;
+  s->ex = (double *)realloc(s->ex, sizeof(double) * 3 * cap);
+  s->eshift = (double *)realloc(s->eshift, sizeof(double) * 3 * cap);
+  s->ef = (double *)realloc(s->ef, sizeof(double) * 3 * cap);
+  s->etype = (int *)realloc(s->etype, sizeof(int) * cap);
+  s->esrc = (int *)realloc(s->esrc, sizeof(int) * cap);
+  s->eowner = (int *)realloc(s->eowner, sizeof(int) * cap);
+  s->eepot = (double *)realloc(s->eepot, sizeof(double) * cap);
+  s->erho = (double *)realloc(s->erho, sizeof(double) * cap);
+  s->edf = (double *)realloc(s->edf, sizeof(double) * cap);
+  s->next_cap = cap;
+}
+
+/* One buffer-cell copy, copy_cell (src/imd_comm_force_3d.c:726-778):
+ * the atoms of cell `from` (in order) get ghost images in cell `to`. */
+static void copy_cell_ext(orc_sys_t *s, int from, int to, const double *v,
+                          int **lists, int *cnt, int *ncap) {
+  int nfrom = cnt[from];
+  for (int i = 0; i < nfrom; i++) {
+    int src = lists[from][i];
+    int g = s->next++;
+    ensure_ext(s, s->next);
+    for (int a = 0; a < 3; a++) {
+      s->eshift[3 * g + a] = v[a];
+      s->ex[3 * g + a] = s->ex[3 * src + a] + v[a];
+    }
+    s->etype[g] = s->etype[src];
+    s->esrc[g] = src;
+    s->eowner[g] = s->eowner[src];
+    if (cnt[to] == ncap[to]) {
+      ncap[to] = ncap[to] * 2 + 8;
+      lists[to] = (int *)realloc(lists[to], sizeof(int) * ncap[to]);
+    }
+    lists[to][cnt[to]++] = g;
+  }
+}
+
+/* fix_cells + send_cells(copy_cell) + make_nblist: wrap, bin, ghosts, list */
+int orc_rebuild(orc_sys_t *s) {
+  int n = s->n, cx = s->cdim[0], cy = s->cdim[1], cz = s->cdim[2];
+  int nall = s->nallcells;
+  int **lists = (int **)calloc(nall, sizeof(int *));
+  int *cnt = (int *)calloc(nall, sizeof(int));
+  int *ncap = (int *)calloc(nall, sizeof(int));
+  /* wrap and bin real atoms; in-cell order = atom index order */
+  for (int i = 0; i < n; i++) {
+    int c[3];
+    wrap_atom(s, s->x + 3 * i);
+    cell_coord(s, s->x + 3 * i, c);
+    int lin = (c[0] + 1) * cy * cz + (c[1] + 1) * cz + (c[2] + 1);
+    if (cnt[lin] == ncap[lin]) {
+      ncap[lin] = ncap[lin] * 2 + 8;
+      lists[lin] = (int *)realloc(lists[lin], sizeof(int) * ncap[lin]);
+    }
+    lists[lin][cnt[lin]++] = i;
+  }
+  /* ext arrays: reals first */
+  s->next = n;
+  ensure_ext(s, n);
+  for (int i = 0; i < n; i++) {
+    for (int a = 0; a < 3; a++) {
+      s->ex[3 * i + a] = s->x[3 * i + a];
+      s->eshift[3 * i + a] = 0.0;
+    }
+    s->etype[i] = s->type[i];
+    s->esrc[i] = -1;
+    s->eowner[i] = i;
+  }
+  /* ghost copies in send_cells order (src/imd_comm_force_3d.c:247-276,
+   * :288-296, :320-327, :351-358): z, then y, then x (east only, AR) */
+  double zero[3] = {0, 0, 0}, up[3], dn[3], no[3], so[3], ea[3];
+  for (int a = 0; a < 3; a++) {
+    up[a] = s->pbc[2] == 1 ? s->box[2][a] : 0.0;
+    dn[a] = s->pbc[2] == 1 ? -s->box[2][a] : 0.0;
+    no[a] = s->pbc[1] == 1 ? s->box[1][a] : 0.0;
+    so[a] = s->pbc[1] == 1 ? -s->box[1][a] : 0.0;
+    ea[a] = s->pbc[0] == 1 ? s->box[0][a] : 0.0;
+  }
+  (void)zero;
+#define LIN(i, j, k) ((i) * cy * cz + (j) * cz + (k))
+  for (int i = 1; i < cx - 1; i++)
+    for (int j = 1; j < cy - 1; j++) {
+      copy_cell_ext(s, LIN(i, j, 1), LIN(i, j, cz - 1), up, lists, cnt, ncap);
+      copy_cell_ext(s, LIN(i, j, cz - 2), LIN(i, j, 0), dn, lists, cnt, ncap);
+    }
+  for (int i = 1; i < cx - 1; i++)
+    for (int k = 0; k < cz; k++) {
+      copy_cell_ext(s, LIN(i, 1, k), LIN(i, cy - 1, k), no, lists, cnt, ncap);
+      copy_cell_ext(s, LIN(i, cy - 2, k), LIN(i, 0, k), so, lists, cnt, ncap);
+    }
+  for (int j = 0; j < cy; j++)
+    for (int k = 0; k < cz; k++)
+      copy_cell_ext(s, LIN(1, j, k), LIN(cx - 1, j, k), ea, lists, cnt, ncap);
+#undef LIN
+  /* CSR of cell contents */
+  s->cell_start[0] = 0;
+  for (int c = 0; c < nall; c++) {
+    s->cell_cnt[c] = cnt[c];
+    s->cell_start[c + 1] = s->cell_start[c] + cnt[c];
+  }
+  s->cell_atoms = (int *)realloc(s->cell_atoms, sizeof(int) * (s->cell_start[nall] + 1));
+  for (int c = 0; c < nall; c++) {
+    memcpy(s->cell_atoms + s->cell_start[c], lists[c], sizeof(int) * cnt[c]);
+    free(lists[c]);
+  }
+  free(lists);
+  free(cnt);
+  free(ncap);
+
+  /* make_nblist (src/imd_forces_nbl.c:136-273) */
+  for (int i = 0; i < 3 * n; i++) s->nbl_pos[i] = s->x[i];
+  if (s->nb_cap == 0) {
+    s->nb_cap = 64L * n + 1000;
+    s->tb = (int *)malloc(sizeof(int) * s->nb_cap);
+  }
+  long tn = 0;
+  int nn = 0;
+  s->tl[0] = 0;
+  for (int c = 0; c < s->nreal_cells; c++) {
+    int c1 = s->real_cells[c];
+    const int *nq = s->cnbrs + 14 * c;
+    for (int ii = 0; ii < s->cell_cnt[c1]; ii++) {
+      int i = s->cell_atoms[s->cell_start[c1] + ii];
+      double d1x = s->ex[3 * i], d1y = s->ex[3 * i + 1], d1z = s->ex[3 * i + 2];
+      for (int m = 0; m < 14; m++) {
+        int c2 = nq[m];
+        if (c2 < 0) continue;
+        int jstart = (c2 == c1) ? ii + 1 : 0;
+        for (int jj = jstart; jj < s->cell_cnt[c2]; jj++) {
+          int j = s->cell_atoms[s->cell_start[c2] + jj];
+          double dx = s->ex[3 * j] - d1x;
+          double dy = s->ex[3 * j + 1] - d1y;
+          double dz = s->ex[3 * j + 2] - d1z;
+          double r2 = dx * dx + dy * dy + dz * dz;
+          if (r2 < s->cellsz) {
+            if (tn == s->nb_cap) {
+              s->nb_cap = s->nb_cap * 3 / 2 + 1000;
+              s->tb = (int *)realloc(s->tb, sizeof(int) * s->nb_cap);
+            }
+            s->tb[tn++] = j;
+          }
+        }
+      }
+      s->order[nn] = i;
+      s->tl[++nn] = (int)tn;
+    }
+  }
+  s->nb_len = tn;
+  s->have_valid_nbl = 1;
+  s->nbl_count++;
+  return 0;
+}
+
+/* send_cells(copy_cell) on a valid list: refresh ghost positions in
+ * creation order so chained copies see their updated source. */
+static void refresh_ghosts(orc_sys_t *s) {
+  int n = s->n;
+  for (int i = 0; i < n; i++)
+    for (int a = 0; a < 3; a++) s->ex[3 * i + a] = s->x[3 * i + a];
+  for (int g = n; g < s->next; g++) {
+    int src = s->esrc[g];
+    for (int a = 0; a < 3; a++) s->ex[3 * g + a] = s->ex[3 * src + a] + s->eshift[3 * g + a];
+  }
+}
+
+/* calc_forces (src/imd_forces_nbl.c:281-1999), PAIR + EAM2 */
+int orc_calc_forces(orc_sys_t *s) {
+  int n = s->n, nt = s->ntypes, inc = nt * nt;
+  int eam = (s->interaction == ORC_EAM2);
+  if (!s->have_valid_nbl) orc_rebuild(s);
+  else refresh_ghosts(s);
+
+  s->tot_pot_energy = 0.0;
+  s->virial = 0.0;
+  s->nfc++;
+  for (int g = 0; g < s->next; g++) {
+    s->ef[3 * g] = s->ef[3 * g + 1] = s->ef[3 * g + 2] = 0.0;
+    s->eepot[g] = 0.0;
+    s->erho[g] = 0.0;
+  }
+  const double *ex = s->ex;
+  /* loop 1: pair + host electron density (:423-981) */
+  for (int nn = 0; nn < n; nn++) {
+    int i = s->order[nn];
+    double d1x = ex[3 * i], d1y = ex[3 * i + 1], d1z = ex[3 * i + 2];
+    double ffx = 0, ffy = 0, ffz = 0, ee = 0, eam_r = 0;
+    int it = s->etype[i];
+    for (int m = s->tl[nn]; m < s->tl[nn + 1]; m++) {
+      int j = s->tb[m];
+      double dx = ex[3 * j] - d1x, dy = ex[3 * j + 1] - d1y, dz = ex[3 * j + 2] - d1z;
+      double r2 = dx * dx + dy * dy + dz * dz;
+      int jt = s->etype[j];
+      int col = it * nt + jt, col2 = jt * nt + it;
+      if (r2 <= s->pair.end[col]) {
+        double pot, grad;
+        orc_pair_int2(&s->pair, col, inc, r2, &pot, &grad, &s->is_short);
+        s->tot_pot_energy += pot;
+        double fx = dx * grad, fy = dy * grad, fz = dz * grad;
+        s->ef[3 * j] -= fx;
+        s->ef[3 * j + 1] -= fy;
+        s->ef[3 * j + 2] -= fz;
+        ffx += fx;
+        ffy += fy;
+        ffz += fz;
+        pot *= 0.5;
+        ee += pot;
+        s->eepot[j] += pot;
+        s->virial -= r2 * grad;
+      }
+      if (eam) {
+        double rho_h = 0.0;
+        if (r2 < s->rho.end[col]) {
+          rho_h = orc_val_func2(&s->rho, col, inc, r2, &s->is_short);
+          eam_r += rho_h;
+        }
+        if (it == jt) {
+          if (r2 < s->rho.end[col]) s->erho[j] += rho_h;
+        } else {
+          if (r2 < s->rho.end[col2]) {
+            rho_h = orc_val_func2(&s->rho, col2, inc, r2, &s->is_short);
+            s->erho[j] += rho_h;
+          }
+        }
+      }
+    }
+    s->ef[3 * i] += ffx;
+    s->ef[3 * i + 1] += ffy;
+    s->ef[3 * i + 2] += ffz;
+    s->eepot[i] += ee;
+    if (eam) s->erho[i] += eam_r;
+  }
+  if (eam) {
+    /* send_forces(add_rho) (:1076): fold ghosts into sources, reverse order */
+    for (int g = s->next - 1; g >= n; g--) s->erho[s->esrc[g]] += s->erho[g];
+    /* embedding energy (:1079-1112) */
+    for (int nn = 0; nn < n; nn++) {
+      int i = s->order[nn];
+      double pot, df;
+      int idummy = 0;
+      orc_pair_int2(&s->embed, s->etype[i], nt, s->erho[i], &pot, &df, &idummy);
+      s->edf[i] = df;
+      s->eepot[i] += pot;
+      s->tot_pot_energy += pot;
+    }
+    /* send_cells(copy_dF) (:1115) */
+    for (int g = n; g < s->next; g++) s->edf[g] = s->edf[s->esrc[g]];
+    /* loop 2: EAM forces (:1117-1323) */
+    for (int nn = 0; nn < n; nn++) {
+      int i = s->order[nn];
+      double d1x = ex[3 * i], d1y = ex[3 * i + 1], d1z = ex[3 * i + 2];
+      double ffx = 0, ffy = 0, ffz = 0;
+      int it = s->etype[i];
+      for (int m = s->tl[nn]; m < s->tl[nn + 1]; m++) {
+        int j = s->tb[m];
+        double dx = ex[3 * j] - d1x, dy = ex[3 * j + 1] - d1y, dz = ex[3 * j + 2] - d1z;
+        double r2 = dx * dx + dy * dy + dz * dz;
+        int jt = s->etype[j];
+        int col1 = jt * nt + it, col2 = it * nt + jt;
+        if ((r2 < s->rho.end[col1]) || (r2 < s->rho.end[col2])) {
+          double rho_i_strich, rho_j_strich;
+          rho_i_strich = orc_deriv_func2(&s->rho, col1, inc, r2, &s->is_short);
+          if (col1 == col2)
+            rho_j_strich = rho_i_strich;
+          else
+            rho_j_strich = orc_deriv_func2(&s->rho, col2, inc, r2, &s->is_short);
+          double grad = 0.5 * (s->edf[i] * rho_j_strich + s->edf[j] * rho_i_strich);
+          double fx = dx * grad, fy = dy * grad, fz = dz * grad;
+          s->ef[3 * j] -= fx;
+          s->ef[3 * j + 1] -= fy;
+          s->ef[3 * j + 2] -= fz;
+          ffx += fx;
+          ffy += fy;
+          ffz += fz;
+          s->virial -= dx * fx + dy * fy + dz * fz;
+        }
+      }
+      s->ef[3 * i] += ffx;
+      s->ef[3 * i + 1] += ffy;
+      s->ef[3 * i + 2] += ffz;
+    }
+  }
+  /* send_forces(add_forces) (:1997) */
+  for (int g = s->next - 1; g >= n; g--) {
+    int src = s->esrc[g];
+    s->ef[3 * src] += s->ef[3 * g];
+    s->ef[3 * src + 1] += s->ef[3 * g + 1];
+    s->ef[3 * src + 2] += s->ef[3 * g + 2];
+    s->eepot[src] += s->eepot[g];
+  }
+  for (int i = 0; i < n; i++) {
+    s->f[3 * i] = s->ef[3 * i];
+    s->f[3 * i + 1] = s->ef[3 * i + 1];
+    s->f[3 * i + 2] = s->ef[3 * i + 2];
+    s->epot[i] = s->eepot[i];
+    if (eam) {
+      s->eam_rho[i] = s->erho[i];
+      s->eam_df[i] = s->edf[i];
+    }
+  }
+  return 0;
+}
+
+static inline double restr(const orc_sys_t *s, int t, int a) {
+  return s->restrictions ? s->restrictions[3 * t + a] : 1.0;
+}
+
+/* move_atoms_nve (src/imd_integrate.c:32-497), plain NVE branch */
+void orc_move_atoms_nve(orc_sys_t *s) {
+  double ekin = 0.0, fnorm = 0.0, fmax2 = 0.0;
+  double dt = s->timestep;
+  for (int nn = 0; nn < s->n; nn++) {
+    int i = s->order[nn];
+    double *p = s->p + 3 * i, *f = s->f + 3 * i, *x = s->x + 3 * i;
+    double kin1 = p[0] * p[0] + p[1] * p[1] + p[2] * p[2];
+    int t = s->type[i];
+    f[0] *= restr(s, t, 0);
+    f[1] *= restr(s, t, 1);
+    f[2] *= restr(s, t, 2);
+    fnorm += f[0] * f[0] + f[1] * f[1] + f[2] * f[2];
+    fmax2 = OMAX(SQR(f[0]), fmax2);
+    fmax2 = OMAX(SQR(f[1]), fmax2);
+    fmax2 = OMAX(SQR(f[2]), fmax2);
+    p[0] += dt * f[0];
+    p[1] += dt * f[1];
+    p[2] += dt * f[2];
+    double kin2 = p[0] * p[0] + p[1] * p[1] + p[2] * p[2];
+    ekin += (kin1 + kin2) / (4 * s->mass[i]);
+    double tmp = dt / s->mass[i];
+    x[0] += tmp * p[0];
+    x[1] += tmp * p[1];
+    x[2] += tmp * p[2];
+  }
+  s->tot_kin_energy = ekin;
+  s->fnorm = fnorm;
+  s->f_max2 = fmax2;
+}
+
+/* check_nblist (src/imd_forces_nbl.c:2007-2037) */
+void orc_check_nblist(orc_sys_t *s) {
+  double max1 = 0.0;
+  for (int i = 0; i < s->n; i++) {
+    double dx = s->x[3 * i] - s->nbl_pos[3 * i];
+    double dy = s->x[3 * i + 1] - s->nbl_pos[3 * i + 1];
+    double dz = s->x[3 * i + 2] - s->nbl_pos[3 * i + 2];
+    double r2 = dx * dx + dy * dy + dz * dz;
+    if (r2 > max1) max1 = r2;
+  }
+  if (max1 > SQR(0.5 * s->nbl_margin)) s->have_valid_nbl = 0;
+}
+
+int orc_nve_steps(orc_sys_t *s, int nsteps, double *epot_out, double *ekin_out) {
+  for (int st = 0; st < nsteps; st++) {
+    orc_calc_forces(s);
+    if (epot_out) epot_out[st] = s->tot_pot_energy;
+    orc_move_atoms_nve(s);
+    if (ekin_out) ekin_out[st] = s->tot_kin_energy;
+    orc_check_nblist(s);
+  }
+  return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* CG (src/imd_cg.c, src/cg_utils.h, move_atoms_cg src/imd_integrate.c:2881) */
+/* ------------------------------------------------------------------------ */
+
+static void move_atoms_cg(orc_sys_t *s, double alpha) {
+  for (int i = 0; i < 3 * s->n; i++) s->x[i] = s->old_x[i] + alpha * s->cg_h[i];
+}
+
+static void calc_fnorm(orc_sys_t *s) {
+  double t = 0.0;
+  for (int nn = 0; nn < s->n; nn++) {
+    int i = s->order[nn];
+    double *f = s->f + 3 * i;
+    int ty = s->type[i];
+    f[0] *= restr(s, ty, 0);
+    f[1] *= restr(s, ty, 1);
+    f[2] *= restr(s, ty, 2);
+    t += f[0] * f[0] + f[1] * f[1] + f[2] * f[2];
+  }
+  s->fnorm = t;
+}
+
+static void calc_fnorm_g_h(orc_sys_t *s) {
+  double t = 0.0, fm = 0.0;
+  for (int nn = 0; nn < s->n; nn++) {
+    int i = s->order[nn];
+    double *f = s->f + 3 * i;
+    int ty = s->type[i];
+    f[0] *= restr(s, ty, 0);
+    f[1] *= restr(s, ty, 1);
+    f[2] *= restr(s, ty, 2);
+    t += f[0] * f[0] + f[1] * f[1] + f[2] * f[2];
+    for (int a = 0; a < 3; a++) {
+      s->old_x[3 * i + a] = s->x[3 * i + a];
+      s->cg_h[3 * i + a] = f[a];
+      s->cg_g[3 * i + a] = f[a];
+    }
+    fm = OMAX(SQR(f[0]), fm);
+    fm = OMAX(SQR(f[1]), fm);
+    fm = OMAX(SQR(f[2]), fm);
+  }
+  s->fnorm = t;
+  s->f_max2 = fm;
+}
+
+static void cg_calcgamma(orc_sys_t *s) {
+  double gg = 0.0, dgg = 0.0;
+  for (int nn = 0; nn < s->n; nn++) {
+    int i = s->order[nn];
+    const double *g = s->cg_g + 3 * i, *f = s->f + 3 * i;
+    gg += g[0] * g[0] + g[1] * g[1] + g[2] * g[2];
+    if (s->cg_fr == 1) {
+      dgg += f[0] * f[0] + f[1] * f[1] + f[2] * f[2];
+    } else {
+      double tx = f[0] - g[0], ty = f[1] - g[1], tz = f[2] - g[2];
+      dgg += f[0] * tx + f[1] * ty + f[2] * tz;
+    }
+  }
+  s->cg_gamma = dgg / gg;
+}
+
+static void set_hg(orc_sys_t *s) {
+  double fm = 0.0;
+  for (int nn = 0; nn < s->n; nn++) {
+    int i = s->order[nn];
+    for (int a = 0; a < 3; a++) {
+      s->old_x[3 * i + a] = s->x[3 * i + a];
+      s->cg_g[3 * i + a] = s->f[3 * i + a];
+      s->cg_h[3 * i + a] = s->f[3 * i + a] + s->cg_gamma * s->cg_h[3 * i + a];
+    }
+    fm = OMAX(SQR(s->f[3 * i]), fm);
+    fm = OMAX(SQR(s->f[3 * i + 1]), fm);
+    fm = OMAX(SQR(s->f[3 * i + 2]), fm);
+  }
+  s->f_max2 = fm;
+}
+
+static double fonedim(orc_sys_t *s, double alpha) {
+  move_atoms_cg(s, alpha);
+  orc_check_nblist(s);
+  orc_calc_forces(s);
+  calc_fnorm(s);
+  return s->tot_pot_energy;
+}
+
+#define CGOLD 0.3819660
+#define GOLD 1.618034
+#define TINY 1.0e-20
+#define SHFT(a, b, c, d) \
+  (a) = (b);             \
+  (b) = (c);             \
+  (c) = (d);
+#define SIGN(a, b) ((b) >= 0.0 ? fabs(a) : -fabs(a))
+
+/* brent (src/cg_utils.h:34-114), IMD's variant: a=ax, b=bx, x=w=v=bx */
+static int brent(orc_sys_t *s, double ax, double bx, double cx, double fa,
+                 double fb, double fc, double *alphamin) {
+  (void)cx; (void)fa; (void)fc;
+  double a, b, etemp, fu, fv, fw, fx, p, q, r, tol1, tol2, u, v, w, x, xm;
+  double e = 0.0, d = 0.0, tol = s->linmin_tol;
+  a = ax;
+  b = bx;
+  x = w = v = bx;
+  fw = fv = fx = fb;
+  for (int iter = 1; iter <= s->linmin_maxsteps; iter++) {
+    xm = 0.5 * (a + b);
+    tol1 = tol * fabs(x) + s->cg_zeps;
+    tol2 = 2.0 * tol1;
+    if (fabs(x - xm) <= (tol2 - 0.5 * (b - a))) {
+      *alphamin = x;
+      return iter;
+    }
+    if (fabs(e) > tol1) {
+      r = (x - w) * (fx - fv);
+      q = (x - v) * (fx - fw);
+      p = (x - v) * q - (x - w) * r;
+      q = 2.0 * (q - r);
+      if (q > 0.0) p = -p;
+      q = fabs(q);
+      etemp = e;
+      e = d;
+      if (fabs(p) >= fabs(0.5 * q * etemp) || p <= q * (a - x) || p >= q * (b - x)) {
+        e = (x >= xm) ? (a - x) : (b - x);
+        d = CGOLD * e;
+      } else {
+        d = p / q;
+        u = x + d;
+        if ((u - a < tol2) || (b - u < tol2)) d = SIGN(tol1, xm - x);
+      }
+    } else {
+      e = (x >= xm) ? (a - x) : (b - x);
+      d = CGOLD * e;
+    }
+    u = ((fabs(d) >= tol1) ? (x + d) : (x + SIGN(tol1, d)));
+    fu = fonedim(s, u);
+    if (fu <= fx) {
+      if (u >= x) a = x;
+      else b = x;
+      SHFT(v, w, x, u)
+      SHFT(fv, fw, fx, fu)
+    } else {
+      if (u < x) a = u;
+      else b = u;
+      if ((fu <= fw) || (w == x)) {
+        v = w;
+        fv = fw;
+        w = u;
+        fw = fu;
+      } else if ((fu <= fv) || (v == x) || (v == w)) {
+        v = u;
+        fv = fu;
+      }
+    }
+  }
+  return -1; /* "Too many iterations in brent" */
+}
+
+/* mnbrak (src/cg_utils.h:119-194) */
+static int mnbrak(orc_sys_t *s, double *ax, double *bx, double *cx, double *fa,
+                  double *fb, double *fc) {
+  double ulim, u, r, q, fu, dum;
+  int ctf;
+  if (*fb > *fa) {
+    SHFT(dum, *ax, *bx, dum)
+    SHFT(dum, *fb, *fa, dum)
+  }
+  *cx = (*bx) + GOLD * (*bx - *ax);
+  if ((*bx - *ax) <= 1e-4) *cx = (*bx) + 0.05;
+  if (*cx < 0.0) *cx = (*bx) - 1.0 / GOLD * (*bx - *ax);
+  if (*cx >= 1.0) *cx = 1.0;
+  *fc = fonedim(s, *cx);
+  ctf = 1;
+  while (*fb >= *fc) {
+    r = (*bx - *ax) * (*fb - *fc);
+    q = (*bx - *cx) * (*fb - *fa);
+    u = (*bx) - ((*bx - *cx) * q - (*bx - *ax) * r) /
+                    (2.0 * SIGN(OMAX(fabs(q - r), TINY), q - r));
+    ulim = (*bx) + s->cg_glimit * (*cx - *bx);
+    if ((*bx - u) * (u - *cx) > 0.0) {
+      fu = fonedim(s, u);
+      ctf++;
+      if (fu < *fc) {
+        *ax = (*bx);
+        *bx = u;
+        *fa = (*fb);
+        *fb = fu;
+        return ctf;
+      } else if (fu > *fb) {
+        *cx = u;
+        *fc = fu;
+        return ctf;
+      }
+      u = (*cx) + GOLD * (*cx - *bx);
+      fu = fonedim(s, u);
+      ctf++;
+    } else if ((*cx - u) * (u - ulim) > 0.0) {
+      fu = fonedim(s, u);
+      ctf++;
+      if (fu < *fc) {
+        SHFT(*bx, *cx, u, *cx + GOLD * (*cx - *bx))
+        SHFT(*fb, *fc, fu, fonedim(s, u))
+        ctf++;
+      }
+    } else if ((u - ulim) * (ulim - *cx) >= 0.0) {
+      u = ulim;
+      fu = fonedim(s, u);
+      ctf++;
+    } else {
+      u = (*cx) + GOLD * (*cx - *bx);
+      fu = fonedim(s, u);
+      ctf++;
+    }
+    SHFT(*ax, *bx, *cx, u)
+    SHFT(*fa, *fb, *fc, fu)
+  }
+  return ctf;
+}
+
+/* linmin (src/imd_cg.c:96-200) */
+static int linmin(orc_sys_t *s) {
+  double alpha_a, alpha_b, alpha_c, fa, fb, fc, dum, alphamin = 0.0;
+  double f_max = sqrt(s->f_max2);
+  if (f_max > 100 * s->linmin_dmax)
+    alpha_b = s->linmin_dmax / f_max;
+  else if (s->old_alphamin < s->linmin_dmin)
+    alpha_b = 0.05;
+  else
+    alpha_b = 2.0 * s->old_alphamin;
+  alpha_c = 2.0 * alpha_b;
+  alpha_a = 0.0;
+  fa = s->old_cg_poteng;
+  fb = fonedim(s, alpha_b);
+  int iter1 = mnbrak(s, &alpha_a, &alpha_b, &alpha_c, &fa, &fb, &fc);
+  if (alpha_a > alpha_b) {
+    SHFT(dum, alpha_a, alpha_b, dum)
+    SHFT(dum, fa, fb, dum)
+  }
+  if (alpha_b > alpha_c) {
+    SHFT(dum, alpha_b, alpha_c, dum)
+    SHFT(dum, fb, fc, dum)
+  }
+  if (alpha_a > alpha_b) {
+    SHFT(dum, alpha_a, alpha_b, dum)
+    SHFT(dum, fa, fb, dum)
+  }
+  int iter2 = brent(s, alpha_a, alpha_b, alpha_c, fa, fb, fc, &alphamin);
+  if (iter2 < 0) return -1;
+  s->old_alphamin = alphamin;
+  return iter1 + iter2;
+}
+
+int orc_reset_cg(orc_sys_t *s) {
+  orc_calc_forces(s);
+  calc_fnorm_g_h(s);
+  s->cg_poteng = s->tot_pot_energy;
+  s->old_cg_poteng = s->cg_poteng;
+  return 0;
+}
+
+int orc_cg_step(orc_sys_t *s, int steps) {
+  if (s->cg_reset_int > 0 && 0 == steps % s->cg_reset_int) orc_reset_cg(s);
+  s->cg_poteng = s->tot_pot_energy;
+  s->old_cg_poteng = s->cg_poteng;
+  if (linmin(s) < 0) return -1;
+  cg_calcgamma(s);
+  set_hg(s);
+  return 0;
+}
+
+double orc_max_atom_force(const orc_sys_t *s) {
+  double m = 0.0;
+  for (int i = 0; i < s->n; i++) {
+    const double *f = s->f + 3 * i;
+    double v = f[0] * f[0] + f[1] * f[1] + f[2] * f[2];
+    if (v > m) m = v;
+  }
+  return sqrt(m);
+}
+
+/* main_loop with ensemble cg (src/imd_main_3d.c:140, :393, :760, :769),
+ * stopping on the max per-atom force. */
+int orc_cg_relax(orc_sys_t *s, double fmax, int maxsteps, double *fmax_out) {
+  orc_reset_cg(s);
+  double fm = orc_max_atom_force(s);
+  int steps = 0;
+  while (fm > fmax && steps < maxsteps) {
+    steps++;
+    if (orc_cg_step(s, steps) < 0) return -1;
+    fm = orc_max_atom_force(s);
+    orc_check_nblist(s);
+  }
+  if (fmax_out) *fmax_out = fm;
+  return steps;
+}
+
+/* neighbour pairs of the current list with ghost image shifts */
+long orc_pairs(const orc_sys_t *s, long cap, int *ni, int *nj, int *shift, double *r2) {
+  long cnt = 0;
+  int n = s->n;
+  for (int nn = 0; nn < n; nn++) {
+    int i = s->order[nn];
+    for (int m = s->tl[nn]; m < s->tl[nn + 1]; m++) {
+      int j = s->tb[m];
+      if (cnt < cap) {
+        ni[cnt] = s->number[i];
+        nj[cnt] = s->number[s->eowner[j]];
+        /* image shift in box vectors: solve from the position difference */
+        int o = s->eowner[j];
+        for (int a = 0; a < 3; a++) {
+          double d[3] = {s->ex[3 * j] - s->ex[3 * o], s->ex[3 * j + 1] - s->ex[3 * o + 1],
+                         s->ex[3 * j + 2] - s->ex[3 * o + 2]};
+          shift[3 * cnt + a] = (int)lround(sprod(d, s->tbox[a]));
+        }
+        double dx = s->ex[3 * j] - s->ex[3 * i], dy = s->ex[3 * j + 1] - s->ex[3 * i + 1],
+               dz = s->ex[3 * j + 2] - s->ex[3 * i + 2];
+        r2[cnt] = dx * dx + dy * dy + dz * dz;
+      }
+      cnt++;
+    }
+  }
+  return cnt;
+}

@@ -1,0 +1,155 @@
+/*
+ * imd_oracle.h -- CPU restatement of IMD's force / neighbour-list / NVE / CG
+ * hot path, used ONLY as the test checker and as the timed CPU baseline.
+ *
+ * This is test infrastructure.  Only tests/, __graft_entry__.smoke() and the
+ * cpu_baseline / reference arm of bench.py may load it.  The GPU library in
+ * imd_gb300/ never calls into it.
+ *
+ * Every routine restates the reference algorithm (itapmd/imd, plain C, FP64)
+ * and cites the file:line it follows.  Arithmetic order is kept where it
+ * decides bits (r^2, table index, cell index, wrap), and the file is built
+ * with -ffp-contract=off so that no multiply-add is fused.
+ *
+ * Parity pin: tests/golden/ holds outputs of the reference itself, built here
+ * from its own sources by oracle/Makefile (target `ref`) and driven by
+ * oracle/ref_harness.c; tests/test_oracle_golden.py checks this restatement
+ * against them.
+ */
+#ifndef IMD_ORACLE_H
+#define IMD_ORACLE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Function table, layout as pot_table_t (src/types.h:416-428):
+ * value of column `col` at row k is table[k*ncols + col]; two extra rows
+ * after maxsteps hold the extrapolation written by init_threepoint. */
+typedef struct {
+  int     ncols;
+  int     maxsteps;
+  double *begin, *end, *step, *invstep;
+  int    *len;
+  double *table;      /* (maxsteps + 2) * ncols */
+} orc_table_t;
+
+/* read_pot_table (src/imd_potential.c:161-282), formats 1 and 2
+ * (:297-376, :394-462) and init_threepoint (:1256-1272).
+ * `cellsz` is raised to the largest `end` of radial tables (:367, :406).
+ * Returns 0 on success, nonzero with a message in err on failure. */
+int  orc_read_table(orc_table_t *pt, const char *fname, int ncols, int radial,
+                    int default_format, double *cellsz, char *err, int errlen);
+/* Build a table from memory (format-2 semantics: begin/end/step per column,
+ * len[col] values each), including the radial shift and threepoint rows. */
+int  orc_make_table(orc_table_t *pt, int ncols, const double *begin,
+                    const double *end, const double *step, const double *vals,
+                    const int *len, int radial, double *cellsz);
+void orc_free_table(orc_table_t *pt);
+
+/* PAIR_INT2 / VAL_FUNC2 / DERIV_FUNC2 (src/potaccess.h:323-354, :465-495,
+ * :591-621). */
+void   orc_pair_int2(const orc_table_t *pt, int col, int inc, double r2,
+                     double *pot, double *grad, int *is_short);
+double orc_val_func2(const orc_table_t *pt, int col, int inc, double r2,
+                     int *is_short);
+double orc_deriv_func2(const orc_table_t *pt, int col, int inc, double r2,
+                       int *is_short);
+/* batch helpers for tests */
+void orc_pair_int2_batch(const orc_table_t *pt, int col, int inc, int n,
+                         const double *r2, double *pot, double *grad);
+
+enum { ORC_PAIR = 0, ORC_EAM2 = 1 };
+
+typedef struct {
+  /* ---- parameters (set by the caller before orc_init) ---- */
+  int    ntypes;
+  int    interaction;         /* ORC_PAIR or ORC_EAM2 */
+  double box[3][3];           /* box_x, box_y, box_z as rows */
+  int    pbc[3];
+  double nbl_margin;
+  double timestep;
+  double *restrictions;       /* 3*ntypes, 1.0 = free (NULL = all free) */
+  /* CG parameters (src/globals.h:711-719 defaults set by orc_init) */
+  int    linmin_maxsteps;
+  double linmin_tol, linmin_dmax, linmin_dmin, cg_glimit, cg_zeps;
+  int    cg_fr, cg_reset_int;
+
+  orc_table_t pair, rho, embed;
+  double cellsz;              /* neighbour-list radius^2 after init */
+
+  /* ---- atoms ---- */
+  int     n;
+  int    *number, *type;
+  double *mass;               /* n */
+  double *x, *p, *f;          /* 3n, atom-major */
+  double *epot, *eam_rho, *eam_df;  /* n */
+  double *nbl_pos;            /* 3n */
+
+  /* ---- derived geometry (make_box / init_cells) ---- */
+  double tbox[3][3], volume, height[3];
+  int    gdim[3], cdim[3];
+  int    nallcells, nreal_cells;
+  int   *real_cells;          /* buffered linear index, x-major */
+  int   *cnbrs;               /* 14 per real cell (-1 = none) */
+
+  /* ---- per-rebuild cell contents (ext numbering: real 0..n-1, ghosts) ---- */
+  int    *cell_start, *cell_cnt, *cell_atoms;   /* CSR over nallcells */
+  int     next, next_cap;
+  double *ex;                 /* 3*next positions (ghosts copied) */
+  int    *etype, *esrc, *eowner;  /* ghost source ext index / owning real atom */
+  double *eshift;             /* 3*next copy vector for ghosts */
+  double *ef, *eepot, *erho, *edf;  /* 3*next, next, next, next */
+  int    *order;              /* real atoms in list order (cell order) */
+
+  /* ---- neighbour list (make_nblist, CSR over `order`) ---- */
+  int    *tl;                 /* n+1 */
+  int    *tb;                 /* ext indices */
+  long    nb_cap, nb_len;
+  int     have_valid_nbl;
+  long    nbl_count, nfc;
+  int     is_short;
+
+  /* ---- results ---- */
+  double tot_pot_energy, virial, tot_kin_energy, fnorm, f_max2;
+
+  /* ---- CG state (src/imd_cg.c) ---- */
+  double *old_x, *cg_g, *cg_h;
+  double cg_gamma, cg_poteng, old_cg_poteng, old_alphamin;
+  long   nactive;
+} orc_sys_t;
+
+/* set defaults; allocate per-atom arrays for n atoms */
+int  orc_init(orc_sys_t *s, int n);
+void orc_free(orc_sys_t *s);
+/* make_box + init_cells + make_cell_lists (src/imd_geom_3d.c:52-426,
+ * :823-1044).  Call after box, tables (cellsz) and nbl_margin are set. */
+int  orc_setup_geometry(orc_sys_t *s);
+/* fix_cells + make_nblist (src/imd_fix_cells_3d.c:36, src/imd_forces_nbl.c:136) */
+int  orc_rebuild(orc_sys_t *s);
+/* calc_forces (src/imd_forces_nbl.c:281-1999), PAIR and EAM2 branches */
+int  orc_calc_forces(orc_sys_t *s);
+/* move_atoms_nve (src/imd_integrate.c:32-497) */
+void orc_move_atoms_nve(orc_sys_t *s);
+/* check_nblist (src/imd_forces_nbl.c:2007-2037) */
+void orc_check_nblist(orc_sys_t *s);
+/* one main_loop NVE step: calc_forces, move_atoms_nve, check_nblist */
+int  orc_nve_steps(orc_sys_t *s, int nsteps, double *epot_out, double *ekin_out);
+/* CG: reset_cg, cg_step (src/imd_cg.c:30-66) */
+int  orc_reset_cg(orc_sys_t *s);
+int  orc_cg_step(orc_sys_t *s, int steps);
+/* relax with CG until max per-atom |F| <= fmax (or maxsteps).
+ * Returns number of cg steps (>=0) or negative on error. */
+int  orc_cg_relax(orc_sys_t *s, double fmax, int maxsteps, double *fmax_out);
+double orc_max_atom_force(const orc_sys_t *s);
+
+/* neighbour pair set of the current list: per entry (number_i, number_j,
+ * image shift of j relative to i as 3 ints, r2).  Returns count; fills at
+ * most cap entries. */
+long orc_pairs(const orc_sys_t *s, long cap, int *ni, int *nj, int *shift,
+               double *r2);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,274 @@
+"""ctypes binding of the C oracle (oracle/liboracle.so).
+
+TEST INFRASTRUCTURE: only tests/, __graft_entry__.smoke() and the CPU
+baseline arm of bench.py import this module.  It is the checker, never the
+thing measured on the GPU and never called by imd_gb300.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "liboracle.so")
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+
+
+class Table(C.Structure):
+    _fields_ = [("ncols", C.c_int), ("maxsteps", C.c_int), ("begin", _dp), ("end", _dp),
+                ("step", _dp), ("invstep", _dp), ("len", _ip), ("table", _dp)]
+
+
+class Sys(C.Structure):
+    _fields_ = [
+        ("ntypes", C.c_int), ("interaction", C.c_int), ("box", (C.c_double * 3) * 3),
+        ("pbc", C.c_int * 3), ("nbl_margin", C.c_double), ("timestep", C.c_double),
+        ("restrictions", _dp), ("linmin_maxsteps", C.c_int), ("linmin_tol", C.c_double),
+        ("linmin_dmax", C.c_double), ("linmin_dmin", C.c_double), ("cg_glimit", C.c_double),
+        ("cg_zeps", C.c_double), ("cg_fr", C.c_int), ("cg_reset_int", C.c_int),
+        ("pair", Table), ("rho", Table), ("embed", Table), ("cellsz", C.c_double),
+        ("n", C.c_int), ("number", _ip), ("type", _ip), ("mass", _dp), ("x", _dp),
+        ("p", _dp), ("f", _dp), ("epot", _dp), ("eam_rho", _dp), ("eam_df", _dp),
+        ("nbl_pos", _dp), ("tbox", (C.c_double * 3) * 3), ("volume", C.c_double),
+        ("height", C.c_double * 3), ("gdim", C.c_int * 3), ("cdim", C.c_int * 3),
+        ("nallcells", C.c_int), ("nreal_cells", C.c_int), ("real_cells", _ip),
+        ("cnbrs", _ip), ("cell_start", _ip), ("cell_cnt", _ip), ("cell_atoms", _ip),
+        ("next", C.c_int), ("next_cap", C.c_int), ("ex", _dp), ("etype", _ip),
+        ("esrc", _ip), ("eowner", _ip), ("eshift", _dp), ("ef", _dp), ("eepot", _dp),
+        ("erho", _dp), ("edf", _dp), ("order", _ip), ("tl", _ip), ("tb", _ip),
+        ("nb_cap", C.c_long), ("nb_len", C.c_long), ("have_valid_nbl", C.c_int),
+        ("nbl_count", C.c_long), ("nfc", C.c_long), ("is_short", C.c_int),
+        ("tot_pot_energy", C.c_double), ("virial", C.c_double),
+        ("tot_kin_energy", C.c_double), ("fnorm", C.c_double), ("f_max2", C.c_double),
+        ("old_x", _dp), ("cg_g", _dp), ("cg_h", _dp), ("cg_gamma", C.c_double),
+        ("cg_poteng", C.c_double), ("old_cg_poteng", C.c_double),
+        ("old_alphamin", C.c_double), ("nactive", C.c_long)]
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            subprocess.run(["make", "-s", "-C", HERE, "liboracle.so"], check=True)
+        L = C.CDLL(LIB)
+        L.orc_read_table.argtypes = [C.POINTER(Table), C.c_char_p, C.c_int, C.c_int, C.c_int,
+                                     _dp, C.c_char_p, C.c_int]
+        L.orc_pair_int2_batch.argtypes = [C.POINTER(Table), C.c_int, C.c_int, C.c_int, _dp,
+                                          _dp, _dp]
+        L.orc_val_func2.argtypes = [C.POINTER(Table), C.c_int, C.c_int, C.c_double, _ip]
+        L.orc_val_func2.restype = C.c_double
+        L.orc_deriv_func2.argtypes = [C.POINTER(Table), C.c_int, C.c_int, C.c_double, _ip]
+        L.orc_deriv_func2.restype = C.c_double
+        for fn in ("orc_init",):
+            getattr(L, fn).argtypes = [C.POINTER(Sys), C.c_int]
+        for fn in ("orc_setup_geometry", "orc_rebuild", "orc_calc_forces", "orc_reset_cg"):
+            getattr(L, fn).argtypes = [C.POINTER(Sys)]
+        L.orc_move_atoms_nve.argtypes = [C.POINTER(Sys)]
+        L.orc_check_nblist.argtypes = [C.POINTER(Sys)]
+        L.orc_free.argtypes = [C.POINTER(Sys)]
+        L.orc_nve_steps.argtypes = [C.POINTER(Sys), C.c_int, _dp, _dp]
+        L.orc_cg_step.argtypes = [C.POINTER(Sys), C.c_int]
+        L.orc_cg_relax.argtypes = [C.POINTER(Sys), C.c_double, C.c_int, _dp]
+        L.orc_max_atom_force.argtypes = [C.POINTER(Sys)]
+        L.orc_max_atom_force.restype = C.c_double
+        L.orc_pairs.argtypes = [C.POINTER(Sys), C.c_long, _ip, _ip, _ip, _dp]
+        L.orc_pairs.restype = C.c_long
+        _lib = L
+    return _lib
+
+
+def _ptr(a: np.ndarray, t=C.c_double):
+    return a.ctypes.data_as(C.POINTER(t))
+
+
+class OracleTable:
+    """A potential table read by the oracle's restatement of read_pot_table."""
+
+    def __init__(self, path: str, ncols: int, radial: bool, default_format: int = 2):
+        self.t = Table()
+        self.cellsz = C.c_double(0.0)
+        err = C.create_string_buffer(512)
+        rc = lib().orc_read_table(C.byref(self.t), path.encode(), ncols, int(radial),
+                                  default_format, C.byref(self.cellsz), err, 512)
+        if rc:
+            raise IOError(err.value.decode())
+
+    def pair_int2(self, col: int, inc: int, r2: np.ndarray):
+        r2 = np.ascontiguousarray(r2, np.float64)
+        pot = np.empty_like(r2)
+        grad = np.empty_like(r2)
+        lib().orc_pair_int2_batch(C.byref(self.t), col, inc, len(r2), _ptr(r2), _ptr(pot),
+                                  _ptr(grad))
+        return pot, grad
+
+    def val(self, col: int, inc: int, r2: float) -> float:
+        s = C.c_int(0)
+        return lib().orc_val_func2(C.byref(self.t), col, inc, r2, C.byref(s))
+
+    def deriv(self, col: int, inc: int, r2: float) -> float:
+        s = C.c_int(0)
+        return lib().orc_deriv_func2(C.byref(self.t), col, inc, r2, C.byref(s))
+
+
+class OracleSystem:
+    """One simulation cell held by the oracle (atom-major arrays)."""
+
+    def __init__(self, box, x, types, mass, number, ntypes, tables, eam: bool,
+                 nbl_margin: float, timestep: float = 0.0, p=None, pbc=(1, 1, 1)):
+        L = lib()
+        self.s = s = Sys()
+        n = len(x)
+        s.ntypes = ntypes
+        s.interaction = 1 if eam else 0
+        for a in range(3):
+            for c in range(3):
+                s.box[a][c] = float(box[a][c])
+            s.pbc[a] = int(pbc[a])
+        s.nbl_margin = nbl_margin
+        s.timestep = timestep
+        cellsz = C.c_double(0.0)
+        err = C.create_string_buffer(512)
+        if eam:
+            pt, rt, et = tables
+            self._read(s.pair, pt, ntypes * ntypes, 1, cellsz, err)
+            self._read(s.rho, rt, ntypes * ntypes, 1, cellsz, err)
+            self._read(s.embed, et, ntypes, 0, cellsz, err)
+        else:
+            self._read(s.pair, tables[0], ntypes * ntypes, 1, cellsz, err)
+        if L.orc_init(C.byref(s), n):
+            raise MemoryError("oracle init")
+        s.cellsz = cellsz.value
+        self.n = n
+        self._copy_in(x, types, mass, number, p)
+        rc = L.orc_setup_geometry(C.byref(s))
+        if rc:
+            raise ValueError("oracle geometry set-up failed (%d)" % rc)
+
+    @staticmethod
+    def _read(t, path, ncols, radial, cellsz, err):
+        rc = lib().orc_read_table(C.byref(t), path.encode(), ncols, radial, 2,
+                                  C.byref(cellsz), err, 512)
+        if rc:
+            raise IOError(err.value.decode())
+
+    def _arr(self, name, shape, dtype=np.float64):
+        ptr = getattr(self.s, name)
+        return np.ctypeslib.as_array(ptr, shape=shape) if dtype == np.float64 else \
+            np.ctypeslib.as_array(C.cast(ptr, C.POINTER(C.c_int)), shape=shape)
+
+    def _copy_in(self, x, types, mass, number, p):
+        n = self.n
+        self._arr("x", (n, 3))[:] = x
+        self._arr("type", (n,), np.int32)[:] = types
+        self._arr("mass", (n,))[:] = mass
+        self._arr("number", (n,), np.int32)[:] = number
+        if p is not None:
+            self._arr("p", (n, 3))[:] = p
+
+    # views
+    @property
+    def x(self):
+        return self._arr("x", (self.n, 3))
+
+    @property
+    def p(self):
+        return self._arr("p", (self.n, 3))
+
+    @property
+    def f(self):
+        return self._arr("f", (self.n, 3))
+
+    @property
+    def epot(self):
+        return self._arr("epot", (self.n,))
+
+    @property
+    def rho(self):
+        return self._arr("eam_rho", (self.n,))
+
+    @property
+    def df(self):
+        return self._arr("eam_df", (self.n,))
+
+    @property
+    def epot_total(self):
+        return self.s.tot_pot_energy
+
+    @property
+    def virial(self):
+        return self.s.virial
+
+    @property
+    def ekin(self):
+        return self.s.tot_kin_energy
+
+    def calc_forces(self):
+        lib().orc_calc_forces(C.byref(self.s))
+
+    def invalidate(self):
+        self.s.have_valid_nbl = 0
+
+    def nve(self, nsteps: int):
+        ep = np.empty(nsteps)
+        ek = np.empty(nsteps)
+        lib().orc_nve_steps(C.byref(self.s), nsteps, _ptr(ep), _ptr(ek))
+        return ep, ek
+
+    def cg_relax(self, fmax: float, maxsteps: int = 100000):
+        fm = C.c_double(0.0)
+        st = lib().orc_cg_relax(C.byref(self.s), fmax, maxsteps, C.byref(fm))
+        return st, fm.value
+
+    def pairs(self):
+        """Canonical sorted pair keys and r2 of the current list."""
+        cnt = lib().orc_pairs(C.byref(self.s), 0, None, None, None, None)
+        ni = np.empty(cnt, np.int32)
+        nj = np.empty(cnt, np.int32)
+        sh = np.empty((cnt, 3), np.int32)
+        r2 = np.empty(cnt)
+        lib().orc_pairs(C.byref(self.s), cnt, _ptr(ni, C.c_int), _ptr(nj, C.c_int),
+                        _ptr(sh, C.c_int), _ptr(r2))
+        return canonical(ni, nj, sh, r2)
+
+    @property
+    def nfc(self):
+        return self.s.nfc
+
+    @property
+    def nbl_count(self):
+        return self.s.nbl_count
+
+    def close(self):
+        if self.s is not None:
+            lib().orc_free(C.byref(self.s))
+            self.s = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def canonical(ni, nj, shift, r2):
+    """Canonical unordered pair keys: (lo, hi, image shift of hi rel. lo),
+    sorted; r2 follows the same permutation."""
+    ni = np.asarray(ni, np.int64)
+    nj = np.asarray(nj, np.int64)
+    s = np.asarray(shift, np.int64).reshape(-1, 3)
+    flip = (ni > nj) | ((ni == nj) & (
+        (s[:, 0] < 0) | ((s[:, 0] == 0) & ((s[:, 1] < 0) | ((s[:, 1] == 0) & (s[:, 2] < 0))))))
+    lo = np.where(flip, nj, ni)
+    hi = np.where(flip, ni, nj)
+    s = np.where(flip[:, None], -s, s)
+    key = ((lo * (1 << 24) + hi) * 27 + (s[:, 0] + 1) * 9 + (s[:, 1] + 1) * 3 + (s[:, 2] + 1))
+    order = np.argsort(key, kind="stable")
+    return key[order], np.asarray(r2)[order]

@@ -1,0 +1,186 @@
+/*
+ * ref_harness.c -- driver linked against objects of the UNMODIFIED reference
+ * (itapmd/imd), compiled from its own sources by oracle/Makefile into
+ * oracle/_ref/.  Used only in the build container to write the golden
+ * vectors under tests/golden/ (tests/golden/make_golden.py) and to time the
+ * reference CPU build.  Never shipped, never linked into the product.
+ *
+ * It replaces IMD's main() (src/imd.c:31; compiled with -Dmain=imd_main so
+ * its globals stay defined there) with the same set-up sequence:
+ *   read_command_line / read_parameters (src/imd_param.c:3829, :3880)
+ *   setup_potentials (src/imd_potential.c:43)
+ *   generate_atoms / read_atoms (src/imd_generate.c:50, src/imd_io_3d.c:44)
+ *   maxwell (src/imd_main_3d.c:89)
+ * and then one of
+ *   forces  : calc_forces(0) and dump atoms, totals and the neighbour pairs
+ *   nve K   : K main_loop steps calc_forces / move_atoms / check_nblist
+ *   cg K F  : reset_cg, then cg_step until max per-atom |F| <= F
+ *   time K  : K NVE steps, print cpu seconds
+ */
+#include "imd.h"
+
+#include <time.h>
+
+extern int *tl, *tb, *cl_off, *cl_num;
+
+static void dump_state(const char *fname) {
+  FILE *out = fopen(fname, "w");
+  int k, i;
+  fprintf(out, "# number type mass x y z px py pz fx fy fz epot rho dF\n");
+  for (k = 0; k < NCELLS; k++) {
+    cell *p = CELLPTR(k);
+    for (i = 0; i < p->n; i++) {
+      double rho = 0.0, df = 0.0;
+#ifdef EAM2
+      rho = EAM_RHO(p, i);
+      df = EAM_DF(p, i);
+#endif
+      fprintf(out,
+              "%ld %d %.17e %.17e %.17e %.17e %.17e %.17e %.17e %.17e %.17e "
+              "%.17e %.17e %.17e %.17e\n",
+              (long)NUMMER(p, i), (int)SORTE(p, i), MASSE(p, i), ORT(p, i, X),
+              ORT(p, i, Y), ORT(p, i, Z), IMPULS(p, i, X), IMPULS(p, i, Y),
+              IMPULS(p, i, Z), KRAFT(p, i, X), KRAFT(p, i, Y), KRAFT(p, i, Z),
+              POTENG(p, i), rho, df);
+    }
+  }
+  fclose(out);
+}
+
+static void dump_box(const char *fname) {
+  FILE *out = fopen(fname, "w");
+  fprintf(out, "%.17e %.17e %.17e\n%.17e %.17e %.17e\n%.17e %.17e %.17e\n",
+          box_x.x, box_x.y, box_x.z, box_y.x, box_y.y, box_y.z, box_z.x,
+          box_z.y, box_z.z);
+  fprintf(out, "%d %d %d\n", global_cell_dim.x, global_cell_dim.y,
+          global_cell_dim.z);
+  fprintf(out, "%.17e\n", cellsz);
+  fclose(out);
+}
+
+/* neighbour pairs: owner numbers and image shift of j (ghost cells map back
+ * to the real cell they copy, same in-cell index; src/imd_comm_force_3d.c
+ * copy_cell keeps the order) */
+static void dump_pairs(const char *fname) {
+  FILE *out = fopen(fname, "w");
+  int c, i, n = 0;
+  int cdx = cell_dim.x, cdy = cell_dim.y, cdz = cell_dim.z;
+  for (c = 0; c < ncells; c++) {
+    cell *p = cell_array + cnbrs[c].np;
+    for (i = 0; i < p->n; i++) {
+      int m;
+      for (m = tl[n]; m < tl[n + 1]; m++) {
+        int cc = cl_num[tb[m]];
+        int j = tb[m] - cl_off[cc];
+        cell *q = cell_array + cc;
+        int bx = cc / (cdy * cdz), by = (cc / cdz) % cdy, bz = cc % cdz;
+        int sx = (bx == cdx - 1) ? 1 : (bx == 0 ? -1 : 0);
+        int sy = (by == cdy - 1) ? 1 : (by == 0 ? -1 : 0);
+        int sz = (bz == cdz - 1) ? 1 : (bz == 0 ? -1 : 0);
+        int rx = bx - sx * global_cell_dim.x, ry = by - sy * global_cell_dim.y,
+            rz = bz - sz * global_cell_dim.z;
+        cell *r = cell_array + (rx * cdy * cdz + ry * cdz + rz);
+        vektor d;
+        d.x = ORT(q, j, X) - ORT(p, i, X);
+        d.y = ORT(q, j, Y) - ORT(p, i, Y);
+        d.z = ORT(q, j, Z) - ORT(p, i, Z);
+        fprintf(out, "%ld %ld %d %d %d %.17e\n", (long)NUMMER(p, i),
+                (long)NUMMER(r, j), sx, sy, sz, SPROD(d, d));
+      }
+      n++;
+    }
+  }
+  fclose(out);
+}
+
+static double max_atom_force(void) {
+  int k, i;
+  double m = 0.0;
+  for (k = 0; k < NCELLS; k++) {
+    cell *p = CELLPTR(k);
+    for (i = 0; i < p->n; i++) {
+      double v = SQR(KRAFT(p, i, X)) + SQR(KRAFT(p, i, Y)) + SQR(KRAFT(p, i, Z));
+      if (v > m) m = v;
+    }
+  }
+  return sqrt(m);
+}
+
+int main(int argc, char **argv) {
+  char fname[600];
+  if (argc < 4) {
+    fprintf(stderr, "usage: %s param mode outprefix [steps] [fmax]\n", argv[0]);
+    return 2;
+  }
+  const char *mode = argv[2], *pre = argv[3];
+  int nsteps = (argc > 4) ? atoi(argv[4]) : 0;
+  char *cl[3] = {argv[0], "-p", argv[1]};
+  read_command_line(3, cl);
+  read_parameters(paramfilename, 1);
+  setup_potentials();
+  if ('_' == infilename[0]) generate_atoms(infilename);
+  else read_atoms(infilename);
+  if (0 == imdrestart) {
+    if (do_maxwell) maxwell(temperature);
+    do_maxwell = 0;
+  }
+  sprintf(fname, "%s.box", pre);
+  dump_box(fname);
+  sprintf(fname, "%s.state0", pre);
+  dump_state(fname);
+
+  if (0 == strcmp(mode, "forces")) {
+    calc_forces(0);
+    sprintf(fname, "%s.forces", pre);
+    dump_state(fname);
+    sprintf(fname, "%s.pairs", pre);
+    dump_pairs(fname);
+    sprintf(fname, "%s.totals", pre);
+    FILE *out = fopen(fname, "w");
+    fprintf(out, "%.17e %.17e %ld\n", tot_pot_energy, virial, (long)natoms);
+    fclose(out);
+  } else if (0 == strcmp(mode, "nve") || 0 == strcmp(mode, "time")) {
+    sprintf(fname, "%s.steps", pre);
+    FILE *out = fopen(fname, "w");
+    clock_t t0 = clock();
+    for (steps = 1; steps <= nsteps; steps++) {
+      calc_forces(steps);
+      double ep = tot_pot_energy;
+      move_atoms();
+      fprintf(out, "%d %.17e %.17e %ld\n", steps, ep, tot_kin_energy, (long)nbl_count);
+      check_nblist();
+    }
+    clock_t t1 = clock();
+    fclose(out);
+    if (0 == strcmp(mode, "time"))
+      printf("cpu_seconds %.6f atom_steps %ld\n", (double)(t1 - t0) / CLOCKS_PER_SEC,
+             (long)natoms * nsteps);
+    sprintf(fname, "%s.final", pre);
+    dump_state(fname);
+  }
+#ifdef CG
+  else if (0 == strcmp(mode, "cg")) {
+    double ftol = (argc > 5) ? atof(argv[5]) : 1e-4;
+    clock_t t0 = clock();
+    reset_cg();
+    double fm = max_atom_force();
+    int st = 0;
+    while (fm > ftol && st < nsteps) {
+      st++;
+      steps = st;
+      cg_step(st);
+      fm = max_atom_force();
+      check_nblist();
+    }
+    clock_t t1 = clock();
+    sprintf(fname, "%s.cg", pre);
+    FILE *out = fopen(fname, "w");
+    fprintf(out, "%d %ld %.17e %.17e %.6f\n", st, (long)nfc, tot_pot_energy, fm,
+            (double)(t1 - t0) / CLOCKS_PER_SEC);
+    fclose(out);
+    sprintf(fname, "%s.final", pre);
+    dump_state(fname);
+  }
+#endif
+  return 0;
+}

@@ -1,0 +1,236 @@
+"""Generate the golden vectors under tests/golden/ from the reference itself.
+
+Runs in the build container only (it needs the reference sources): builds
+the unmodified reference with oracle/Makefile (`make ref`), writes
+potential tables, parameter and configuration files in IMD's formats, runs
+oracle/_ref/<variant>/ref_harness on them and stores the outputs as small
+.npz fixtures next to this script, together with the table files the runs
+read.  Re-run with `python tests/golden/make_golden.py`.
+
+Fixtures (all sorted by atom number):
+  lj_pert     LJ fcc 10^3 (4000 atoms), positions perturbed, table format 2
+  lj_pert_f1  same system, table format 1
+  lj_nve      LJ fcc 10^3 from IMD's own _fcc generator + maxwell (seed 1,
+              T*=0.72), 200 NVE steps, dt 0.005, skin 0.3
+  cu_pert     Sutton-Chen Cu fcc 8^3 (2048 atoms), perturbed
+  cu_nve      Sutton-Chen Cu _fcc 8^3, 300 K, 100 NVE steps of 1 fs, skin 0.4
+  alloy_pert  binary Sutton-Chen Cu/Ni fcc 6^3 a0=3.57 (864 atoms)
+  tri_cg      strained (triclinic) Cu cell 3x4x3 with a vacancy and noise:
+              forces and a CG relaxation to max |F| <= 1e-4 eV/A
+"""
+from __future__ import annotations
+
+import hashlib
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+from imd_gb300 import workloads as wl  # noqa: E402
+
+ORACLE = os.path.join(ROOT, "oracle")
+
+
+def harness(variant: str) -> str:
+    return os.path.join(ORACLE, "_ref", variant, "ref_harness")
+
+
+def load_state(path: str) -> dict:
+    a = np.loadtxt(path, ndmin=2)
+    order = np.argsort(a[:, 0], kind="stable")
+    a = a[order]
+    return {"number": a[:, 0].astype(np.int32), "type": a[:, 1].astype(np.int32),
+            "mass": a[:, 2], "x": a[:, 3:6], "p": a[:, 6:9], "f": a[:, 9:12],
+            "epot": a[:, 12], "rho": a[:, 13], "df": a[:, 14]}
+
+
+def load_box(path: str):
+    lines = open(path).read().split("\n")
+    box = np.array([[float(v) for v in lines[i].split()] for i in range(3)])
+    gdim = np.array([int(v) for v in lines[3].split()], np.int32)
+    cellsz = float(lines[4])
+    return box, gdim, cellsz
+
+
+def canonical_pairs(path: str):
+    """Canonical unordered pair set: (lo, hi, shift of hi's image rel. lo, r2).
+    r2 is kept as computed by the reference (orientation does not change it
+    bitwise for the reference's own orientation; the key is the set)."""
+    a = np.loadtxt(path, ndmin=2)
+    ni, nj = a[:, 0].astype(np.int64), a[:, 1].astype(np.int64)
+    s = a[:, 2:5].astype(np.int64)
+    r2 = a[:, 5]
+    flip = (ni > nj) | ((ni == nj) & (
+        (s[:, 0] < 0) | ((s[:, 0] == 0) & ((s[:, 1] < 0) | ((s[:, 1] == 0) & (s[:, 2] < 0))))))
+    lo = np.where(flip, nj, ni)
+    hi = np.where(flip, ni, nj)
+    s = np.where(flip[:, None], -s, s)
+    key = ((lo * (1 << 24) + hi) * 27 + (s[:, 0] + 1) * 9 + (s[:, 1] + 1) * 3 + (s[:, 2] + 1))
+    order = np.argsort(key, kind="stable")
+    return key[order], r2[order]
+
+
+def pair_digest(key: np.ndarray, r2: np.ndarray) -> str:
+    h = hashlib.sha256()
+    h.update(np.ascontiguousarray(key, np.int64).tobytes())
+    h.update(np.ascontiguousarray(r2, np.float64).tobytes())
+    return h.hexdigest()
+
+
+def run(variant: str, param: str, mode: str, pre: str, *extra) -> None:
+    cmd = [harness(variant), param, mode, pre] + [str(e) for e in extra]
+    r = subprocess.run(cmd, cwd=os.path.dirname(param), capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("%s failed:\n%s\n%s" % (cmd, r.stdout[-2000:], r.stderr[-2000:]))
+
+
+def perturbed_config(sysobj, sigma: float, seed: int, path: str, remove=None,
+                     strain=None) -> None:
+    rng = np.random.default_rng(seed)
+    x = sysobj.x.copy()
+    box = sysobj.box.copy()
+    keep = np.ones(len(x), bool)
+    if remove is not None:
+        keep[remove] = False
+    if strain is not None:
+        m = np.eye(3) + strain
+        x = x @ m.T
+        box = box @ m.T
+    x = x + sigma * rng.standard_normal(x.shape)
+    wl.write_config(path, box, sysobj.number[keep], sysobj.types[keep],
+                    sysobj.mass[keep], x[keep])
+
+
+def main() -> None:
+    subprocess.run(["make", "-s", "-C", ORACLE, "ref"], check=True)
+    tmp = tempfile.mkdtemp(prefix="imdgold")
+    out = {}
+    # ---- tables (kept as fixtures: the runs read exactly these files) ----
+    lj2 = os.path.join(HERE, "lj.pt")
+    lj1 = os.path.join(HERE, "lj_f1.pt")
+    wl.lj_table(lj2, fmt=2)
+    wl.lj_table(lj1, npts=300, fmt=1)
+    cu = wl.sutton_chen_tables(os.path.join(HERE, "cu"), [wl.CU])
+    alloy = wl.sutton_chen_tables(os.path.join(HERE, "cuni"), [wl.CU, wl.NI])
+
+    def lj_param(path, coord, potfile, **kw):
+        tok = dict(coordname=coord, outfiles=os.path.join(tmp, "o"), ensemble="nve",
+                   ntypes=1, masses=1.0, pbc_dirs=[1, 1, 1], timestep=0.005,
+                   maxsteps=0, starttemp=0.0, seed=1, potfile=potfile,
+                   nbl_margin=0.3, eng_int=0, checkpt_int=100000000)
+        tok.update(kw)
+        wl.write_param(path, **tok)
+
+    def eam_param(path, coord, tabs, ntypes, masses, **kw):
+        tok = dict(coordname=coord, outfiles=os.path.join(tmp, "o"), ensemble="nve",
+                   ntypes=ntypes, masses=masses, pbc_dirs=[1, 1, 1],
+                   timestep=0.0982266, maxsteps=0, starttemp=0.0, seed=2,
+                   core_potential_file=tabs[0], **{"atomic_e-density_file": tabs[1]},
+                   embedding_energy_file=tabs[2], nbl_margin=0.4, eng_int=0,
+                   checkpt_int=100000000)
+        tok.update(kw)
+        wl.write_param(path, **tok)
+
+    def forces_case(name, variant, param):
+        pre = os.path.join(tmp, name)
+        run(variant, param, "forces", pre)
+        st = load_state(pre + ".forces")
+        box, gdim, cellsz = load_box(pre + ".box")
+        key, r2 = canonical_pairs(pre + ".pairs")
+        tot = np.loadtxt(pre + ".totals")
+        d = dict(box=box, gdim=gdim, cellsz=cellsz, epot_total=tot[0], virial=tot[1],
+                 npairs=len(key), pair_digest=pair_digest(key, r2), **st)
+        return d, key, r2
+
+    # ---- LJ perturbed, format 2 and format 1 ----
+    lj = wl.lj_fcc_system(10)
+    cfg = os.path.join(tmp, "lj_pert.cfg")
+    perturbed_config(lj, 0.05, 11, cfg)
+    p = os.path.join(tmp, "lj_pert.param")
+    lj_param(p, cfg, lj2, box_from_header=1)
+    out["lj_pert"], _, _ = forces_case("lj_pert", "nve_nbl", p)
+    p = os.path.join(tmp, "lj_pert_f1.param")
+    lj_param(p, cfg, lj1, box_from_header=1)
+    out["lj_pert_f1"], _, _ = forces_case("lj_pert_f1", "nve_nbl", p)
+
+    # ---- LJ NVE from IMD's own generator (config-1 set-up, shortened) ----
+    p = os.path.join(tmp, "lj_nve.param")
+    lj_param(p, "_fcc", lj2, box_param=[10, 10, 10], box_unit=lj.meta["a0"],
+             starttemp=0.72, seed=1)
+    pre = os.path.join(tmp, "lj_nve")
+    run("nve_nbl", p, "nve", pre, 200)
+    st0 = load_state(pre + ".state0")
+    stf = load_state(pre + ".final")
+    steps = np.loadtxt(pre + ".steps")
+    box, gdim, cellsz = load_box(pre + ".box")
+    out["lj_nve"] = dict(box=box, gdim=gdim, cellsz=cellsz, number=st0["number"],
+                         type=st0["type"], mass=st0["mass"], x0=st0["x"], p0=st0["p"],
+                         epot=steps[:, 1], ekin=steps[:, 2], nbl_count=steps[:, 3],
+                         x_final=stf["x"], p_final=stf["p"], dt=0.005, skin=0.3)
+
+    # ---- Cu perturbed ----
+    cus = wl.eam_fcc_system(8)
+    cfg = os.path.join(tmp, "cu_pert.cfg")
+    perturbed_config(cus, 0.1, 12, cfg)
+    p = os.path.join(tmp, "cu_pert.param")
+    eam_param(p, cfg, cu, 1, 63.546, box_from_header=1)
+    out["cu_pert"], _, _ = forces_case("cu_pert", "nve_nbl_eam", p)
+
+    # ---- Cu NVE (config-2 set-up at 8^3 cells, shortened) ----
+    p = os.path.join(tmp, "cu_nve.param")
+    eam_param(p, "_fcc", cu, 1, 63.546, box_param=[8, 8, 8], box_unit=3.615,
+              starttemp=0.0258520, seed=2)
+    pre = os.path.join(tmp, "cu_nve")
+    run("nve_nbl_eam", p, "nve", pre, 100)
+    st0 = load_state(pre + ".state0")
+    stf = load_state(pre + ".final")
+    steps = np.loadtxt(pre + ".steps")
+    box, gdim, cellsz = load_box(pre + ".box")
+    out["cu_nve"] = dict(box=box, gdim=gdim, cellsz=cellsz, number=st0["number"],
+                         type=st0["type"], mass=st0["mass"], x0=st0["x"], p0=st0["p"],
+                         epot=steps[:, 1], ekin=steps[:, 2], nbl_count=steps[:, 3],
+                         x_final=stf["x"], p_final=stf["p"], dt=0.0982266, skin=0.4)
+
+    # ---- binary alloy ----
+    als = wl.eam_fcc_system(6, a0=3.57, species=(wl.CU, wl.NI), type_seed=3)
+    cfg = os.path.join(tmp, "alloy.cfg")
+    perturbed_config(als, 0.08, 13, cfg)
+    p = os.path.join(tmp, "alloy.param")
+    eam_param(p, cfg, alloy, 2, [63.546, 58.69], box_from_header=1)
+    out["alloy_pert"], _, _ = forces_case("alloy_pert", "nve_nbl_eam", p)
+
+    # ---- small triclinic defect cell: forces + CG ----
+    x, box = wl.fcc(3, 4, 3, 3.615)
+    n = len(x)
+    tri = wl.System(box, x, np.zeros_like(x), np.zeros(n, np.int32),
+                    np.full(n, 63.546), np.arange(n, dtype=np.int32))
+    strain = np.array([[0.015, 0.01, -0.005], [0.0, -0.012, 0.008], [0.0, 0.0, 0.018]])
+    cfg = os.path.join(tmp, "tri.cfg")
+    perturbed_config(tri, 0.05, 14, cfg, remove=[17], strain=strain)
+    p = os.path.join(tmp, "tri.param")
+    eam_param(p, cfg, cu, 1, 63.546, box_from_header=1, ensemble="cg")
+    d, key, r2 = forces_case("tri", "cg_nbl_eam", p)
+    d["pair_key"] = key
+    d["pair_r2"] = r2
+    pre = os.path.join(tmp, "tri")
+    run("cg_nbl_eam", p, "cg", pre, 5000, 1e-4)
+    cg = np.loadtxt(pre + ".cg")
+    stf = load_state(pre + ".final")
+    d.update(cg_steps=int(cg[0]), cg_nfc=int(cg[1]), cg_epot=cg[2], cg_fmax=cg[3],
+             cg_x=stf["x"])
+    out["tri_cg"] = d
+
+    for name, d in out.items():
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **d)
+        print(name, {k: (v.shape if hasattr(v, "shape") and v.shape else v)
+                     for k, v in d.items() if k in ("npairs", "epot_total", "cg_steps",
+                                                    "cg_epot", "cg_nfc")})
+
+
+if __name__ == "__main__":
+    main()
