@@ -1,0 +1,348 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 force / neighbour-list / NVE path.
+
+Workload (one step = one main_loop NVE step): single-species Sutton-Chen Cu
+EAM2 in IMD eam2 table format (2000-point tables on r^2 from 1.5 A to 7.2 A,
+cubic taper over the last 0.3 A; F table 2000 points on [0, 400]), fcc
+a0 = 3.615 A, 40x40x40 cells = 256,000 atoms, mass 63.546 amu, periodic,
+Maxwell momenta at 300 K (seed 2), dt = 1 fs, skin 0.4 A, FP64.  Synthetic
+data, generated here deterministically.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line.  `value` is device-timed atom-steps/s with the state
+resident in HBM (CUDA events around every step, an L2-sized scratch write
+between steps outside the timed windows); `e2e` is the same metric through
+the C-ABI with host buffers: every step uploads positions and momenta from
+pinned host memory, runs calc_forces / move_atoms_nve / check_nblist and
+reads positions, momenta, forces and energies back.
+
+--impl reference times the reference's CPU algorithm for this path on the
+host cores: the C restatement in oracle/ (the reference itself is compiled
+only where its sources are, which the GPU host does not have), one process
+per core, a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = ("EAM atom-steps/s (FP32 vs FP64); defect CG relaxations/s learned vs plain")
+NCELL = 40
+A0 = 3.615
+DT_FS = 1.0
+SKIN = 0.4
+WORKLOAD = "sutton-chen Cu EAM2 NVE, fcc 40^3 = 256000 atoms, 300 K, dt 1 fs, skin 0.4 A"
+FORCE_BYTES_PER_ATOM = 56.0       # force kernel: read x (24) + 2F' (8), write F (24)
+STEP_BYTES_PER_ATOM = 232.0       # whole NVE EAM step, canonical count
+FLOPS_PER_PAIR = 66.0             # canonical FP64 flops per half-list pair within rc
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.samples = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except FileNotFoundError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.samples.append([v.strip() for v in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in self.samples if s[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for s in self.samples:
+            for k, nm in enumerate(names):
+                if len(s) > 5 + k and s[5 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(self.samples)}
+
+
+def workload_files(tmp: str):
+    from imd_gb300 import workloads as wl
+    return wl.sutton_chen_tables(os.path.join(tmp, "cu"), [wl.CU])
+
+
+def make_state():
+    from imd_gb300 import workloads as wl
+    return wl.eam_fcc_system(NCELL, a0=A0, T=300.0, seed=2)
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def committed_traffic(kernel: str):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(path) as f:
+            return json.load(f).get(kernel)
+    except Exception:
+        return None
+
+
+def cpu_sample(tabs, steps: int, cores: int = 1):
+    """The oracle (C restatement of the reference path) on the same workload,
+    `steps` NVE steps, in `cores` independent processes."""
+    import multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores) as pool:
+        res = pool.starmap(_cpu_worker, [(tabs, steps)] * cores)
+    n = res[0][0]
+    rate = sum(n * steps / t for n, t in res)
+    return rate, n
+
+
+def _cpu_worker(tabs, steps):
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    from imd_gb300 import workloads as wl
+    from oracle import OracleSystem
+    s = make_state()
+    o = OracleSystem(s.box, s.x, s.types, s.mass, s.number, 1, tabs, True, SKIN,
+                     timestep=DT_FS * wl.FS, p=s.p)
+    o.nve(1)   # first build outside the timed sample
+    t = time.perf_counter()
+    o.nve(steps)
+    return s.n, time.perf_counter() - t
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    tmp = tempfile.mkdtemp(prefix="imdbench")
+    tabs = workload_files(tmp)
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "liboracle.so"], check=True)
+    cores = os.cpu_count() or 1
+    steps = max(1, min(args.steps, 4))
+    # warm-up: one process, W steps (bounded)
+    _ = cpu_sample(tabs, 1, 1)
+    rate, n = cpu_sample(tabs, steps, cores)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": rate, "unit": "atom-steps/s",
+        "n_gpus": world, "steps": steps, "warmup": 1, "ms_per_step": 1e3 * n / (rate / cores),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "config": {"workload": WORKLOAD, "sample": "%d NVE steps per core" % steps},
+        "cpu_baseline": {"value": rate, "unit": "atom-steps/s", "cores": cores, "kind": "port",
+                         "sample": "%d independent processes x %d NVE steps of the 256000-atom "
+                                   "system (oracle/imd_oracle.c)" % (cores, steps)},
+        "e2e": {"value": rate, "unit": "atom-steps/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def run_ours(args, rank, world, local):
+    from imd_gb300 import api
+    from imd_gb300 import workloads as wl
+    api.set_device(local)
+    tmp = tempfile.mkdtemp(prefix="imdbench%d" % rank)
+    tabs = workload_files(tmp)
+    st = make_state()
+    dt = DT_FS * wl.FS
+    dist = None
+    if world > 1:
+        import torch.distributed as dist_mod
+        dist_mod.init_process_group("gloo")
+        dist = dist_mod
+
+    def barrier():
+        if dist:
+            dist.barrier()
+
+    def build(precision):
+        s = api.GpuSystem(1, api.EAM2, precision)
+        s.read_tables(tabs)
+        s.set_box(st.box, (1, 1, 1), SKIN)
+        s.set_atoms(st.number, st.types, st.mass, st.x, st.p)
+        return s
+
+    peaks, peak_kind = measured_peaks()
+    res = {}
+    for prec, name in ((api.FP64, "fp64"), (api.MIXED, "mixed")):
+        if name == "mixed" and args.no_mixed:
+            continue
+        s = build(prec)
+        s.nve_run(max(args.warmup, 3), dt, record=False)
+        s.set_profiling(True)
+        s.set_l2_flush(256 << 20)
+        barrier()
+        with ClockSampler(local) as clk:
+            ep, ek = s.nve_run(args.steps, dt)
+        barrier()
+        t = s.timing()
+        sc = s.scalars()
+        res[name] = dict(ms=t.ms_total, ms_force=t.ms_force, ms_density=t.ms_density,
+                         ms_integrate=t.ms_integrate, ms_rebuild=t.ms_rebuild,
+                         rebuilds=t.rebuilds, launches=t.kernel_launches,
+                         clocks=clk.summary(), etot=(ep + ek), nb=sc.nb_entries, sys=s)
+    r = res["fp64"]
+    ms_max = r["ms"]
+    if dist:
+        import torch
+        v = torch.tensor([ms_max], dtype=torch.float64)
+        dist.all_reduce(v, op=dist.ReduceOp.MAX)
+        ms_max = float(v[0])
+    n = st.n
+    value = n * args.steps * world / (ms_max * 1e-3)
+
+    # ---- end to end through the C-ABI with host buffers ----
+    s = r["sys"]
+    e2e_steps = min(args.steps, 20)
+    try:
+        import torch
+        xh = torch.empty((n, 3), dtype=torch.float64, pin_memory=True).numpy()
+        ph = torch.empty((n, 3), dtype=torch.float64, pin_memory=True).numpy()
+        fh = torch.empty((n, 3), dtype=torch.float64, pin_memory=True).numpy()
+        eh = torch.empty((n,), dtype=torch.float64, pin_memory=True).numpy()
+    except Exception:
+        xh, ph, fh, eh = (np.empty((n, 3)), np.empty((n, 3)), np.empty((n, 3)), np.empty(n))
+    s.get_state(xh, ph, fh, eh)
+    for _ in range(3):   # warm-up of the host path
+        s.put_state(xh, ph)
+        s.calc_forces(0)
+        s.move_atoms_nve(dt)
+        s.check_nblist()
+        s.get_state(xh, ph, fh, eh)
+    barrier()
+    t0 = time.perf_counter()
+    for k in range(e2e_steps):
+        s.put_state(xh, ph)
+        s.calc_forces(k)
+        s.move_atoms_nve(dt)
+        s.check_nblist()
+        s.get_state(xh, ph, fh, eh)
+    t_e2e = time.perf_counter() - t0
+    barrier()
+    e2e = n * e2e_steps * world / t_e2e
+
+    # ---- roofline of the dominant kernel (EAM force pass) ----
+    force_ms = r["ms_force"] / args.steps
+    achieved = FORCE_BYTES_PER_ATOM * n / (force_ms * 1e-3) / 1e9
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    fp64_peak = api.probe_fp64_peak()
+    pairs_rc = 67.0 * n  # half-list pairs within rc per atom for fcc Cu (6 shells, 134/2)
+    step_ms = r["ms"] / args.steps
+    fp64_achieved = FLOPS_PER_PAIR * pairs_rc / (step_ms * 1e-3) / 1e12
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "atom-steps/s", "n_gpus": world,
+        "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": step_ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD, "precision": "fp64", "atoms": n,
+                   "parallelism": "replicas" if world > 1 else "single",
+                   "l2": "256 MiB scratch write between timed steps (outside the windows)",
+                   "list_entries": r["nb"], "rebuilds_in_timed_steps": r["rebuilds"]},
+        "clocks": r["clocks"],
+        "e2e": {"value": e2e, "unit": "atom-steps/s", "h2d_bytes_per_step": 48 * n,
+                "d2h_bytes_per_step": 80 * n, "steps": e2e_steps},
+        "gpu_launches": int(r["launches"]),
+        "roofline": {"bound": "hbm", "kernel": "k_force64<EAM>", "achieved": achieved,
+                     "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": committed_traffic("k_force64"),
+                     "peak_kind": peak_kind,
+                     "bytes_per_atom": FORCE_BYTES_PER_ATOM,
+                     "fp64": {"achieved_tflops": fp64_achieved, "peak_tflops": fp64_peak,
+                              "frac": fp64_achieved / fp64_peak,
+                              "flops_per_step": FLOPS_PER_PAIR * pairs_rc,
+                              "peak_kind": "measured FMA probe"}},
+        "kernels_ms_per_step": {"density": r["ms_density"] / args.steps,
+                                "force": force_ms, "integrate": r["ms_integrate"] / args.steps,
+                                "rebuild": r["ms_rebuild"] / args.steps},
+        "energy_drift_per_atom": float((r["etot"][-1] - r["etot"][0]) / n),
+    }
+    if "mixed" in res:
+        m = res["mixed"]
+        mv = n * args.steps * world / (m["ms"] * 1e-3)
+        line["mixed"] = {"value": mv, "unit": "atom-steps/s", "speedup_vs_fp64": mv / value,
+                         "ms_per_step": m["ms"] / args.steps,
+                         "energy_drift_per_atom": float((m["etot"][-1] - m["etot"][0]) / n)}
+    if rank == 0 and not args.no_cpu:
+        try:
+            rate, _ = cpu_sample(tabs, args.cpu_steps, 1)
+            line["cpu_baseline"] = {"value": rate, "unit": "atom-steps/s", "cores": 1,
+                                    "kind": "port",
+                                    "sample": "%d NVE steps of the 256000-atom system on one "
+                                              "core (oracle/imd_oracle.c)" % args.cpu_steps}
+        except Exception as e:  # the measurement itself stays valid
+            line["cpu_baseline"] = {"value": None, "error": str(e)[:200]}
+    if rank == 0:
+        print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-steps", type=int, default=16)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-mixed", action="store_true")
+    args = ap.parse_args()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_ours(args, rank, world, local)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,305 @@
+"""Python host interface over the C-ABI of libimdgpu (include/imdgpu.h).
+
+Names and meaning follow IMD's own routines for this path (itapmd/imd):
+calc_forces (src/imd_forces_nbl.c:281), make_nblist (:136), check_nblist
+(:2007), deallocate_nblist (:56), estimate_nblist_size (:74),
+move_atoms_nve (src/imd_integrate.c:32), reset_cg / cg_step
+(src/imd_cg.c:30, :46).  The GPU library is the only implementation: if it
+cannot be loaded the constructor raises; there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIBPATH = os.path.join(HERE, "libimdgpu.so")
+
+PAIR, EAM2 = 0, 1
+FP64, MIXED = 0, 1
+TAB_PAIR, TAB_RHO, TAB_EMBED = 0, 1, 2
+WARN_SHORT = 1
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+
+
+class Scalars(C.Structure):
+    _fields_ = [("tot_pot_energy", C.c_double), ("virial", C.c_double),
+                ("tot_kin_energy", C.c_double), ("fnorm", C.c_double),
+                ("f_max2", C.c_double), ("max_atom_force", C.c_double),
+                ("nfc", C.c_long), ("nbl_count", C.c_long), ("nb_entries", C.c_long),
+                ("have_valid_nbl", C.c_int), ("gdim", C.c_int * 3), ("nghost", C.c_int),
+                ("max_cell_atoms", C.c_int), ("short_distance", C.c_int)]
+
+
+class Timing(C.Structure):
+    _fields_ = [("ms_total", C.c_double), ("ms_density", C.c_double),
+                ("ms_force", C.c_double), ("ms_integrate", C.c_double),
+                ("ms_rebuild", C.c_double), ("steps", C.c_int), ("rebuilds", C.c_int),
+                ("kernel_launches", C.c_long)]
+
+
+class IMDGPUError(RuntimeError):
+    pass
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    """Load libimdgpu.so (building it first if it is missing)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIBPATH):
+            from . import build
+            build.build()
+        L = C.CDLL(LIBPATH)
+        L.imdgpu_last_error.restype = C.c_char_p
+        L.imdgpu_version.restype = C.c_char_p
+        L.imdgpu_create.argtypes = [C.POINTER(C.c_void_p), C.c_int, C.c_int, C.c_int]
+        vp = C.c_void_p
+        L.imdgpu_destroy.argtypes = [vp]
+        L.imdgpu_set_precision.argtypes = [vp, C.c_int]
+        L.imdgpu_set_table.argtypes = [vp, C.c_int, C.c_int, C.c_int, _dp, _dp, _dp, _dp,
+                                       _ip, _dp]
+        L.imdgpu_read_table.argtypes = [vp, C.c_int, C.c_char_p, C.c_int, C.c_int]
+        L.imdgpu_set_box.argtypes = [vp, _dp, _ip, C.c_double, C.c_double]
+        L.imdgpu_set_restrictions.argtypes = [vp, _dp]
+        L.imdgpu_set_atoms.argtypes = [vp, C.c_int, _ip, _ip, _dp, _dp, _dp]
+        L.imdgpu_get_atoms.argtypes = [vp, _dp, _dp, _dp, _dp, _dp, _dp]
+        L.imdgpu_get_scalars.argtypes = [vp, C.POINTER(Scalars)]
+        L.imdgpu_calc_forces.argtypes = [vp, C.c_int]
+        L.imdgpu_make_nblist.argtypes = [vp]
+        L.imdgpu_check_nblist.argtypes = [vp]
+        L.imdgpu_deallocate_nblist.argtypes = [vp]
+        L.imdgpu_estimate_nblist_size.argtypes = [vp, C.POINTER(C.c_long)]
+        L.imdgpu_move_atoms_nve.argtypes = [vp, C.c_double]
+        L.imdgpu_nve_run.argtypes = [vp, C.c_int, C.c_double, _dp, _dp]
+        L.imdgpu_set_cg_params.argtypes = [vp, C.c_int, C.c_double, C.c_double, C.c_double,
+                                           C.c_double, C.c_double, C.c_int, C.c_int]
+        L.imdgpu_reset_cg.argtypes = [vp]
+        L.imdgpu_cg_step.argtypes = [vp, C.c_int]
+        L.imdgpu_cg_relax.argtypes = [vp, C.c_double, C.c_int, _ip, _dp]
+        L.imdgpu_get_pairs.argtypes = [vp, C.c_long, _ip, _ip, _ip, _dp,
+                                       C.POINTER(C.c_long)]
+        L.imdgpu_get_timing.argtypes = [vp, C.POINTER(Timing)]
+        L.imdgpu_set_profiling.argtypes = [vp, C.c_int]
+        L.imdgpu_device_count.argtypes = [_ip]
+        L.imdgpu_put_state.argtypes = [vp, _dp, _dp]
+        L.imdgpu_set_l2_flush.argtypes = [vp, C.c_long]
+        L.imdgpu_probe_fp64_peak.argtypes = [_dp]
+        L.imdgpu_set_device.argtypes = [C.c_int]
+        _lib = L
+    return _lib
+
+
+def _check(rc: int, what: str) -> int:
+    if rc < 0:
+        raise IMDGPUError("%s failed (%d): %s" % (what, rc, lib().imdgpu_last_error().decode()))
+    return rc
+
+
+def _p(a, t=C.c_double):
+    return None if a is None else a.ctypes.data_as(C.POINTER(t))
+
+
+def _f64(a, shape=None):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    return a if shape is None else a.reshape(shape)
+
+
+class GpuSystem:
+    """One simulation cell resident on the GPU.
+
+    Tables are IMD potential files (formats 1/2) or in-memory pot_table_t
+    arrays; the box, periodicity and list margin as IMD's parameters
+    box_x/y/z, pbc_dirs and nbl_margin."""
+
+    def __init__(self, ntypes: int = 1, interaction: int = EAM2, precision: int = FP64):
+        h = C.c_void_p()
+        _check(lib().imdgpu_create(C.byref(h), ntypes, interaction, precision), "imdgpu_create")
+        self.h = h
+        self.ntypes = ntypes
+        self.interaction = interaction
+        self.n = 0
+        self.last_rc = 0
+
+    # --- set-up ---------------------------------------------------------------
+    def read_tables(self, files, default_format: int = 2) -> None:
+        """files = (pair,) for PAIR or (pair, rho, embed) for EAM2."""
+        kinds = [(TAB_PAIR, 1)] if self.interaction == PAIR else \
+            [(TAB_PAIR, 1), (TAB_RHO, 1), (TAB_EMBED, 0)]
+        for (which, radial), f in zip(kinds, files):
+            _check(lib().imdgpu_read_table(self.h, which, f.encode(), radial, default_format),
+                   "imdgpu_read_table(%s)" % f)
+
+    def set_table(self, which, begin, end, step, length, table, maxsteps) -> None:
+        ncols = len(begin)
+        b, e, s = _f64(begin), _f64(end), _f64(step)
+        inv = 1.0 / s
+        ln = np.ascontiguousarray(length, np.int32)
+        t = _f64(table)
+        _check(lib().imdgpu_set_table(self.h, which, ncols, maxsteps, _p(b), _p(e), _p(s),
+                                      _p(inv), _p(ln, C.c_int), _p(t)), "imdgpu_set_table")
+
+    def set_box(self, box, pbc=(1, 1, 1), nbl_margin: float = 0.4, list_r2: float = 0.0) -> None:
+        b = _f64(box, (9,))
+        p = np.ascontiguousarray(pbc, np.int32)
+        _check(lib().imdgpu_set_box(self.h, _p(b), _p(p, C.c_int), nbl_margin, list_r2),
+               "imdgpu_set_box")
+
+    def set_restrictions(self, restr) -> None:
+        r = _f64(restr, (-1,))
+        _check(lib().imdgpu_set_restrictions(self.h, _p(r)), "imdgpu_set_restrictions")
+
+    def set_atoms(self, number, types, mass, x, p=None) -> None:
+        n = len(x)
+        num = np.ascontiguousarray(number, np.int32)
+        ty = np.ascontiguousarray(types, np.int32)
+        m = _f64(mass)
+        xx = _f64(x, (n * 3,))
+        pp = None if p is None else _f64(p, (n * 3,))
+        _check(lib().imdgpu_set_atoms(self.h, n, _p(num, C.c_int), _p(ty, C.c_int), _p(m),
+                                      _p(xx), _p(pp)), "imdgpu_set_atoms")
+        self.n = n
+
+    def put_state(self, x, p=None) -> None:
+        """Positions / momenta in caller order; x, p should be C-contiguous
+        float64 (pinned host memory gives direct DMA)."""
+        _check(lib().imdgpu_put_state(self.h, _p(x), _p(p)), "put_state")
+
+    def get_state(self, x=None, p=None, f=None, epot=None) -> None:
+        """Fill the given preallocated (n,3)/(n,) float64 arrays."""
+        _check(lib().imdgpu_get_atoms(self.h, _p(x), _p(p), _p(f), _p(epot), None, None),
+               "get_atoms")
+
+    def set_l2_flush(self, nbytes: int) -> None:
+        _check(lib().imdgpu_set_l2_flush(self.h, nbytes), "set_l2_flush")
+
+    def set_profiling(self, on: bool) -> None:
+        _check(lib().imdgpu_set_profiling(self.h, int(on)), "set_profiling")
+
+    def set_precision(self, precision: int) -> None:
+        _check(lib().imdgpu_set_precision(self.h, precision), "imdgpu_set_precision")
+
+    # --- the hot path -----------------------------------------------------------
+    def calc_forces(self, steps: int = 0) -> int:
+        self.last_rc = _check(lib().imdgpu_calc_forces(self.h, steps), "calc_forces")
+        return self.last_rc
+
+    def make_nblist(self) -> None:
+        _check(lib().imdgpu_make_nblist(self.h), "make_nblist")
+
+    def check_nblist(self) -> bool:
+        _check(lib().imdgpu_check_nblist(self.h), "check_nblist")
+        return bool(self.scalars().have_valid_nbl)
+
+    def deallocate_nblist(self) -> None:
+        _check(lib().imdgpu_deallocate_nblist(self.h), "deallocate_nblist")
+
+    def estimate_nblist_size(self) -> int:
+        n = C.c_long(0)
+        _check(lib().imdgpu_estimate_nblist_size(self.h, C.byref(n)), "estimate_nblist_size")
+        return n.value
+
+    def move_atoms_nve(self, timestep: float) -> None:
+        _check(lib().imdgpu_move_atoms_nve(self.h, timestep), "move_atoms_nve")
+
+    def nve_run(self, nsteps: int, timestep: float, record: bool = True):
+        ep = np.empty(nsteps) if record else None
+        ek = np.empty(nsteps) if record else None
+        self.last_rc = _check(lib().imdgpu_nve_run(self.h, nsteps, timestep, _p(ep), _p(ek)),
+                              "nve_run")
+        return ep, ek
+
+    # --- CG -------------------------------------------------------------------
+    def set_cg_params(self, linmin_maxsteps=100, linmin_tol=0.0002, linmin_dmax=0.01,
+                      linmin_dmin=0.001, cg_glimit=100.0, cg_zeps=1e-10, cg_fr=0,
+                      cg_reset_int=0) -> None:
+        _check(lib().imdgpu_set_cg_params(self.h, linmin_maxsteps, linmin_tol, linmin_dmax,
+                                          linmin_dmin, cg_glimit, cg_zeps, cg_fr,
+                                          cg_reset_int), "set_cg_params")
+
+    def reset_cg(self) -> None:
+        _check(lib().imdgpu_reset_cg(self.h), "reset_cg")
+
+    def cg_step(self, steps: int) -> None:
+        _check(lib().imdgpu_cg_step(self.h, steps), "cg_step")
+
+    def cg_relax(self, fmax: float = 1e-4, maxsteps: int = 100000):
+        st = C.c_int(0)
+        fm = C.c_double(0.0)
+        _check(lib().imdgpu_cg_relax(self.h, fmax, maxsteps, C.byref(st), C.byref(fm)),
+               "cg_relax")
+        return st.value, fm.value
+
+    # --- results ----------------------------------------------------------------
+    def scalars(self) -> Scalars:
+        s = Scalars()
+        _check(lib().imdgpu_get_scalars(self.h, C.byref(s)), "get_scalars")
+        return s
+
+    def get_atoms(self):
+        n = self.n
+        x = np.empty((n, 3))
+        p = np.empty((n, 3))
+        f = np.empty((n, 3))
+        e = np.empty(n)
+        rho = np.empty(n)
+        df = np.empty(n)
+        _check(lib().imdgpu_get_atoms(self.h, _p(x), _p(p), _p(f), _p(e), _p(rho), _p(df)),
+               "get_atoms")
+        return {"x": x, "p": p, "f": f, "epot": e, "rho": rho, "df": df}
+
+    def pairs(self):
+        cnt = C.c_long(0)
+        _check(lib().imdgpu_get_pairs(self.h, 0, None, None, None, None, C.byref(cnt)),
+               "get_pairs")
+        m = cnt.value
+        ni = np.empty(m, np.int32)
+        nj = np.empty(m, np.int32)
+        sh = np.empty((m, 3), np.int32)
+        r2 = np.empty(m)
+        _check(lib().imdgpu_get_pairs(self.h, m, _p(ni, C.c_int), _p(nj, C.c_int),
+                                      _p(sh, C.c_int), _p(r2), C.byref(cnt)), "get_pairs")
+        return ni, nj, sh, r2
+
+    def timing(self) -> Timing:
+        t = Timing()
+        _check(lib().imdgpu_get_timing(self.h, C.byref(t)), "get_timing")
+        return t
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            lib().imdgpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def set_device(device: int) -> None:
+    _check(lib().imdgpu_set_device(device), "set_device")
+
+
+def probe_fp64_peak() -> float:
+    """Measured FP64 FMA throughput of the current device in TFLOP/s."""
+    v = C.c_double(0.0)
+    _check(lib().imdgpu_probe_fp64_peak(C.byref(v)), "probe_fp64_peak")
+    return v.value
+
+
+def system_from_tables(files, box, number, types, mass, x, p=None, ntypes=1,
+                       interaction=EAM2, precision=FP64, nbl_margin=0.4, pbc=(1, 1, 1)):
+    """Convenience: a GpuSystem with tables, box and atoms set."""
+    s = GpuSystem(ntypes, interaction, precision)
+    s.read_tables(files)
+    s.set_box(box, pbc, nbl_margin)
+    s.set_atoms(number, types, mass, x, p)
+    return s

@@ -1,0 +1,240 @@
+// forces.cu -- pair and EAM2 force kernels of libimdgpu (sm_103a).
+//
+// FP64 path: the half neighbour list of make_nblist (IMD pair orientation,
+// src/imd_forces_nbl.c:136-273), one thread per real atom, partner updates
+// by FP64 atomics, exact (unfused) r^2 and table-index arithmetic so every
+// pair sees the same table row as the reference.  Two passes as
+// calc_forces (src/imd_forces_nbl.c:423-1323): density (rho), embedding
+// F(rho) per atom, then a fused pass that adds the pair force (loop 1's
+// PAIR branch) and the EAM force (loop 2) of each pair with one set of
+// atomics.
+#include "kernels.cuh"
+
+namespace imdgpu {
+
+// ---------------------------------------------------------------------------
+// ghosts: send_cells(copy_cell) (src/imd_comm_force_3d.c:247-358).  A ghost
+// copies its owner through the z, y, x copies in that order, so its position
+// is ((x + s_z box_z) + s_y box_y) + s_x box_x component-wise.
+// ---------------------------------------------------------------------------
+__global__ void k_ghost_pos(SysView v) {
+  const int ng = v.counters[0];
+  for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < ng; g += gridDim.x * blockDim.x)
+    v.pos[v.n + g] = ghost_image(v, v.pos[v.gowner[g]], v.gcode[g]);
+}
+
+// ---------------------------------------------------------------------------
+// density pass: loop 1 EAM branch (src/imd_forces_nbl.c:586-611, :907-918)
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(BS_FORCE) k_density64(SysView v, DevTable rho) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= v.n) return;
+  const double4 pi = v.pos[i];
+  const int it = (int)pi.w, nt = v.ntypes;
+  const int nn = v.nnb[i];
+  unsigned shortf = 0;
+  double eam_r = 0.0;
+  const uint32_t *nb = v.nbr + i;
+  for (int k = 0; k < nn; k++) {
+    const int j = (int)(__ldg(nb + (size_t)k * v.ncap) & NB_MASK);
+    const double4 pj = ldg4(&v.pos[j]);
+    const double dx = dsub(pj.x, pi.x), dy = dsub(pj.y, pi.y), dz = dsub(pj.z, pi.z);
+    const double r2 = r2_exact(dx, dy, dz);
+    const int jt = (int)pj.w;
+    const int col = it * nt + jt;
+    double rho_h = 0.0;
+    if (r2 < rho.end[col]) {
+      rho_h = val_func2(rho, col, r2, shortf);
+      eam_r += rho_h;
+    }
+    if (it == jt) {
+      if (r2 < rho.end[col]) atomicAdd(&v.rho[j], rho_h);
+    } else {
+      const int col2 = jt * nt + it;
+      if (r2 < rho.end[col2]) atomicAdd(&v.rho[j], val_func2(rho, col2, r2, shortf));
+    }
+  }
+  atomicAdd(&v.rho[i], eam_r);
+  if (shortf) atomicOr(v.status, ST_SHORT);
+}
+
+// send_forces(add_rho) (src/imd_forces_nbl.c:1076): ghosts into owners
+__global__ void k_fold_rho(SysView v) {
+  const int ng = v.counters[0];
+  for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < ng; g += gridDim.x * blockDim.x) {
+    const double r = v.rho[v.n + g];
+    if (r != 0.0) atomicAdd(&v.rho[v.gowner[g]], r);
+  }
+}
+
+// embedding energy (src/imd_forces_nbl.c:1079-1112): F(rho), EAM_DF = 2F'
+__global__ void __launch_bounds__(BS_VEC) k_embed(SysView v, DevTable emb, double *partial) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double e[1] = {0.0};
+  if (i < v.n) {
+    const int t = (int)v.pos[i].w;
+    unsigned dummy = 0;
+    double pot, grad;
+    pair_int2(emb, t, v.rho[i], pot, grad, dummy);
+    v.df[i] = grad;
+    atomicAdd(&v.frc[i].w, pot);
+    e[0] = pot;
+  }
+  block_sum_store<1, BS_VEC>(e, partial);
+}
+
+// send_cells(copy_dF) (src/imd_forces_nbl.c:1115)
+__global__ void k_ghost_df(SysView v) {
+  const int ng = v.counters[0];
+  for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < ng; g += gridDim.x * blockDim.x)
+    v.df[v.n + g] = v.df[v.gowner[g]];
+}
+
+// ---------------------------------------------------------------------------
+// force pass: loop 1 PAIR branch (src/imd_forces_nbl.c:490-584) fused with
+// loop 2 (:1117-1323).  Energy: each pair's pot goes to the total once and
+// half to each partner's per-atom energy (POTENG).  Virial as in the
+// reference: -r^2 grad for the pair part, -d.F for the EAM part.
+// ---------------------------------------------------------------------------
+template <bool EAM>
+__global__ void __launch_bounds__(BS_FORCE) k_force64(SysView v, DevTable pair, DevTable rho,
+                                                      double *partial) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double acc[2] = {0.0, 0.0};  // energy, virial
+  if (i < v.n) {
+    const double4 pi = v.pos[i];
+    const int it = (int)pi.w, nt = v.ntypes;
+    const int nn = v.nnb[i];
+    const double dfi = EAM ? v.df[i] : 0.0;
+    unsigned shortf = 0;
+    double ffx = 0.0, ffy = 0.0, ffz = 0.0, ee = 0.0;
+    const uint32_t *nb = v.nbr + i;
+    for (int k = 0; k < nn; k++) {
+      const int j = (int)(__ldg(nb + (size_t)k * v.ncap) & NB_MASK);
+      const double4 pj = ldg4(&v.pos[j]);
+      const double dx = dsub(pj.x, pi.x), dy = dsub(pj.y, pi.y), dz = dsub(pj.z, pi.z);
+      const double r2 = r2_exact(dx, dy, dz);
+      const int jt = (int)pj.w;
+      const int col = it * nt + jt;
+      double grad = 0.0, ehalf = 0.0;
+      bool have = false;
+      if (r2 <= pair.end[col]) {
+        double pot, gp;
+        pair_int2(pair, col, r2, pot, gp, shortf);
+        acc[0] += pot;
+        acc[1] -= r2 * gp;
+        ehalf = 0.5 * pot;
+        ee += ehalf;
+        grad = gp;
+        have = true;
+      }
+      if (EAM) {
+        const int col1 = jt * nt + it, col2 = col;
+        if ((r2 < rho.end[col1]) || (r2 < rho.end[col2])) {
+          const double ris = deriv_func2(rho, col1, r2, shortf);
+          const double rjs = (col1 == col2) ? ris : deriv_func2(rho, col2, r2, shortf);
+          const double dfj = __ldg(&v.df[j]);
+          const double ge = 0.5 * (dfi * rjs + dfj * ris);
+          acc[1] -= r2 * ge;
+          grad += ge;
+          have = true;
+        }
+      }
+      if (have) {
+        const double fx = dx * grad, fy = dy * grad, fz = dz * grad;
+        double *fj = &v.frc[j].x;
+        atomicAdd(fj + 0, -fx);
+        atomicAdd(fj + 1, -fy);
+        atomicAdd(fj + 2, -fz);
+        if (ehalf != 0.0) atomicAdd(fj + 3, ehalf);
+        ffx += fx;
+        ffy += fy;
+        ffz += fz;
+      }
+    }
+    double *fi = &v.frc[i].x;
+    atomicAdd(fi + 0, ffx);
+    atomicAdd(fi + 1, ffy);
+    atomicAdd(fi + 2, ffz);
+    atomicAdd(fi + 3, ee);
+    if (shortf) atomicOr(v.status, ST_SHORT);
+  }
+  block_sum_store<2, BS_FORCE>(acc, partial);
+}
+
+// send_forces(add_forces) (src/imd_forces_nbl.c:1997)
+__global__ void k_fold_force(SysView v) {
+  const int ng = v.counters[0];
+  for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < ng; g += gridDim.x * blockDim.x) {
+    const double4 f = v.frc[v.n + g];
+    if (f.x != 0.0 || f.y != 0.0 || f.z != 0.0 || f.w != 0.0) {
+      double *o = &v.frc[v.gowner[g]].x;
+      atomicAdd(o + 0, f.x);
+      atomicAdd(o + 1, f.y);
+      atomicAdd(o + 2, f.z);
+      atomicAdd(o + 3, f.w);
+    }
+  }
+}
+
+// energy / virial: fixed-order sum of block partials (the MPI_Allreduce of
+// 8 scalars, src/imd_forces_nbl.c:1975-1994, on one device)
+__global__ void k_finalize_forces(const double *pe, int ne, const double *pf, int nf,
+                                  DevScalars *sc) {
+  const int lane = threadIdx.x;
+  double e = 0.0, w = 0.0;
+  for (int b = lane; b < ne; b += 32) e += pe[b];
+  for (int b = lane; b < nf; b += 32) {
+    e += pf[2 * b];
+    w += pf[2 * b + 1];
+  }
+  e = warp_sum(e);
+  w = warp_sum(w);
+  if (lane == 0) {
+    sc->epot = e;
+    sc->virial = w;
+  }
+}
+
+static inline int nblk(long n, int bs) { return (int)((n + bs - 1) / bs); }
+
+int launch_forces(const SysView &v, const ForceTabs &t, DevScalars *sc, int mixed,
+                  cudaStream_t st, cudaEvent_t *ev) {
+  (void)mixed;
+  int launches = 0;
+  const int gblocks = nblk(v.gcap, BS_VEC) > 0 ? nblk(v.gcap, BS_VEC) : 1;
+  const size_t ext = (size_t)v.ncap + v.gcap;
+  cudaMemsetAsync(v.frc, 0, ext * sizeof(double4), st);
+  k_ghost_pos<<<gblocks, BS_VEC, 0, st>>>(v);
+  launches++;
+  const int nbf = nblk(v.n, BS_FORCE), nbe = nblk(v.n, BS_VEC);
+  double *pe = v.partial, *pf = v.partial + nbe;
+  if (t.eam) {
+    cudaMemsetAsync(v.rho, 0, ext * sizeof(double), st);
+    if (ev) cudaEventRecord(ev[0], st);
+    k_density64<<<nbf, BS_FORCE, 0, st>>>(v, t.rho);
+    if (ev) cudaEventRecord(ev[1], st);
+    k_fold_rho<<<gblocks, BS_VEC, 0, st>>>(v);
+    k_embed<<<nbe, BS_VEC, 0, st>>>(v, t.embed, pe);
+    k_ghost_df<<<gblocks, BS_VEC, 0, st>>>(v);
+    if (ev) cudaEventRecord(ev[2], st);
+    k_force64<true><<<nbf, BS_FORCE, 0, st>>>(v, t.pair, t.rho, pf);
+    if (ev) cudaEventRecord(ev[3], st);
+    launches += 5;
+  } else {
+    if (ev) {
+      cudaEventRecord(ev[0], st);
+      cudaEventRecord(ev[1], st);
+      cudaEventRecord(ev[2], st);
+    }
+    k_force64<false><<<nbf, BS_FORCE, 0, st>>>(v, t.pair, t.rho, pf);
+    if (ev) cudaEventRecord(ev[3], st);
+    launches += 1;
+  }
+  k_fold_force<<<gblocks, BS_VEC, 0, st>>>(v);
+  k_finalize_forces<<<1, 32, 0, st>>>(pe, t.eam ? nbe : 0, pf, nbf, sc);
+  launches += 2;
+  return launches;
+}
+
+}  // namespace imdgpu

@@ -1,0 +1,250 @@
+// internal.cuh -- device data layout and helpers shared by the kernels of
+// libimdgpu (sm_103a).
+//
+// Layout in HBM (one system, N atoms, G ghost atoms):
+//   * atoms are sorted by cell at every list build; cells are visited in
+//     Morton order, atoms inside a cell by their number (NUMMER), so the
+//     layout is a pure function of the positions;
+//   * "ext" arrays hold the N real atoms followed by the G buffer-cell
+//     copies (ghosts) of IMD's serial build (src/imd_comm_force_3d.c:247);
+//   * pos  double4 (x, y, z, type)    -- gathered per pair: one 32 B sector
+//     mom  double4 (px, py, pz, mass)
+//     frc  double4 (fx, fy, fz, epot) -- scattered by atomics per pair
+//   * the half neighbour list is column-major ELL: entry k of atom i at
+//     nbr[k * ncap_atoms + i], so consecutive threads read consecutive words.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace imdgpu {
+
+constexpr int MAXT = 4;              // atom types
+constexpr int MAXCOL = MAXT * MAXT;  // columns of pair / rho tables
+constexpr int CELLCAP = 256;         // atoms per cell supported by the builder
+constexpr int NB_SHIFT = 27;         // list entry: ext index (27 bits) | half-shell slot << 27
+constexpr uint32_t NB_MASK = (1u << NB_SHIFT) - 1u;
+
+// status bits (device status word)
+constexpr unsigned ST_SHORT = 1u;      // r^2 below a table begin
+constexpr unsigned ST_NBOVER = 2u;     // list entries beyond capacity
+constexpr unsigned ST_GHOSTOVER = 4u;  // ghost atoms beyond capacity
+constexpr unsigned ST_CELLOVER = 8u;   // atoms per cell beyond CELLCAP
+
+// One pot_table_t on the device.  `tri` holds, per column and row k, the
+// three table values the quadratic interpolation reads (rows k, k+1, k+2):
+// one aligned 32 B record per lookup instead of three strided loads.
+struct DevTable {
+  int ncols;
+  int rows;                 // maxsteps + 2
+  const double4 *tri;       // tri[col * rows + k] = (t[k], t[k+1], t[k+2], 0)
+  const float4 *trif;       // same in FP32 (mixed precision)
+  double begin[MAXCOL];
+  double end[MAXCOL];
+  double invstep[MAXCOL];
+};
+
+// Everything a kernel of one system needs, passed by value.
+struct SysView {
+  int n;                    // real atoms
+  int ncap;                 // capacity of real-atom arrays (list stride)
+  int gcap;                 // ghost capacity
+  int ntypes;
+  int nbcap;                // list entries per atom
+  int nreal_cells;
+  int nall_cells;
+  int cdim[3], gdim[3];
+  double box[3][3];
+  double tbox[3][3];
+  double cellvec[3][3];     // box rows / gdim
+  int pbc[3];
+  double cellsz;            // list radius^2
+  double skin2;             // (nbl_margin/2)^2
+  double restr[MAXT * 3];
+
+  double4 *pos, *mom, *frc, *ref;
+  double *rho, *df;
+  float4 *xl;               // mixed: cell-relative FP32 positions + type bits
+  int *number, *orig;
+  int *ecell;               // buffered cell id of every ext atom
+  int *gowner;              // ghost -> owning real slot
+  int *gcode;               // ghost -> packed image shift (sx+1) + 3(sy+1) + 9(sz+1)
+  uint32_t *nbr;            // ELL list
+  int *nnb;                 // entries per atom
+  int *cstart, *ccount;     // per buffered cell: first ext index, atoms
+  const int *cell_rank;     // buffered lin -> Morton rank of real cell (-1 for buffer)
+  const int *rank_lin;      // rank -> buffered lin
+  const int *hshell;        // 14 buffered lin per real rank (-1 none)
+  const int *bsrc;          // per buffer cell (enumerated): source real lin
+  const int *blin;          // per buffer cell: its lin
+  const int *bcode;         // per buffer cell: packed image shift
+  int nbuf;                 // number of buffer cells used
+  unsigned *status;
+  int *counters;            // [0] ghosts, [1] max entries per atom, [2] max cell atoms
+  double *partial;          // per-block partial sums
+};
+
+// ---------------------------------------------------------------------------
+// exact FP64 helpers: no contraction into FMA, so bits match the C oracle and
+// the reference built without fused multiply-add
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
+
+// r^2 = dx*dx + dy*dy + dz*dz, left to right (SPROD, src/makros.h:409)
+__device__ __forceinline__ double r2_exact(double dx, double dy, double dz) {
+  return dadd(dadd(dmul(dx, dx), dmul(dy, dy)), dmul(dz, dz));
+}
+
+// Table index of PAIR_INT2 / VAL_FUNC2 / DERIV_FUNC2 (src/potaccess.h:323-345)
+__device__ __forceinline__ int tab_index(double r2, double begin, double end,
+                                         double invstep, double &chi, unsigned &shortf) {
+  double r2a = r2 < end ? r2 : end;
+  r2a = dsub(r2a, begin);
+  if (r2a < 0) {
+    r2a = 0;
+    shortf = 1;
+  }
+  r2a = dmul(r2a, invstep);
+  int k = __double2int_rz(r2a);
+  chi = dsub(r2a, (double)k);
+  return k;
+}
+
+// PAIR_INT2 (src/potaccess.h:323-354): value and twice the derivative
+__device__ __forceinline__ void quad_vg(const double4 p, double chi, double istep,
+                                        double &pot, double &grad) {
+  double dv = dsub(p.y, p.x);
+  double d2v = dadd(dsub(p.z, dmul(2.0, p.y)), p.x);
+  pot = dadd(dadd(p.x, dmul(chi, dv)), dmul(dmul(dmul(0.5, chi), dsub(chi, 1.0)), d2v));
+  grad = dmul(dmul(2.0, istep), dadd(dv, dmul(dsub(chi, 0.5), d2v)));
+}
+// VAL_FUNC2 (:465-495)
+__device__ __forceinline__ double quad_v(const double4 p, double chi) {
+  double dv = dsub(p.y, p.x);
+  double d2v = dadd(dsub(p.z, dmul(2.0, p.y)), p.x);
+  return dadd(dadd(p.x, dmul(chi, dv)), dmul(dmul(dmul(0.5, chi), dsub(chi, 1.0)), d2v));
+}
+// DERIV_FUNC2 (:591-621)
+__device__ __forceinline__ double quad_g(const double4 p, double chi, double istep) {
+  double dv = dsub(p.y, p.x);
+  double d2v = dadd(dsub(p.z, dmul(2.0, p.y)), p.x);
+  return dmul(dmul(2.0, istep), dadd(dv, dmul(dsub(chi, 0.5), d2v)));
+}
+
+// read-only 32 B load (two 16 B non-coherent loads)
+__device__ __forceinline__ double4 ldg4(const double4 *p) {
+  const double2 a = __ldg(reinterpret_cast<const double2 *>(p));
+  const double2 b = __ldg(reinterpret_cast<const double2 *>(p) + 1);
+  return make_double4(a.x, a.y, b.x, b.y);
+}
+
+__device__ __forceinline__ double4 tab_load(const DevTable &t, int col, int k) {
+  return ldg4(&t.tri[(size_t)col * t.rows + k]);
+}
+
+__device__ __forceinline__ void pair_int2(const DevTable &t, int col, double r2, double &pot,
+                                          double &grad, unsigned &shortf) {
+  double chi;
+  int k = tab_index(r2, t.begin[col], t.end[col], t.invstep[col], chi, shortf);
+  quad_vg(tab_load(t, col, k), chi, t.invstep[col], pot, grad);
+}
+__device__ __forceinline__ double val_func2(const DevTable &t, int col, double r2,
+                                            unsigned &shortf) {
+  double chi;
+  int k = tab_index(r2, t.begin[col], t.end[col], t.invstep[col], chi, shortf);
+  return quad_v(tab_load(t, col, k), chi);
+}
+__device__ __forceinline__ double deriv_func2(const DevTable &t, int col, double r2,
+                                              unsigned &shortf) {
+  double chi;
+  int k = tab_index(r2, t.begin[col], t.end[col], t.invstep[col], chi, shortf);
+  return quad_g(tab_load(t, col, k), chi, t.invstep[col]);
+}
+
+// A ghost copies its owner through the z, y, x buffer copies of send_cells
+// (src/imd_comm_force_3d.c:247-358) in that order, so its position is
+// ((x + s_z box_z) + s_y box_y) + s_x box_x component-wise.
+__device__ __forceinline__ double4 ghost_image(const SysView &v, double4 p, int code) {
+  const int sx = code % 3 - 1, sy = (code / 3) % 3 - 1, sz = code / 9 - 1;
+  double c[3] = {p.x, p.y, p.z};
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+    double t = c[a];
+    if (sz) t = dadd(t, sz > 0 ? v.box[2][a] : -v.box[2][a]);
+    if (sy) t = dadd(t, sy > 0 ? v.box[1][a] : -v.box[1][a]);
+    if (sx) t = dadd(t, sx > 0 ? v.box[0][a] : -v.box[0][a]);
+    c[a] = t;
+  }
+  return make_double4(c[0], c[1], c[2], p.w);
+}
+
+// ---------------------------------------------------------------------------
+// FP32 variants (mixed precision): same index rule on r^2 computed in FP32
+// ---------------------------------------------------------------------------
+struct TabF {
+  float begin, end, invstep;
+};
+
+__device__ __forceinline__ int tab_index_f(float r2, float begin, float end, float invstep,
+                                           float &chi) {
+  float r2a = fminf(r2, end) - begin;
+  r2a = fmaxf(r2a, 0.0f) * invstep;
+  int k = __float2int_rz(r2a);
+  chi = r2a - (float)k;
+  return k;
+}
+__device__ __forceinline__ void quadf_vg(const float4 p, float chi, float istep, float &pot,
+                                         float &grad) {
+  float dv = p.y - p.x;
+  float d2v = p.z - 2.0f * p.y + p.x;
+  pot = p.x + chi * dv + 0.5f * chi * (chi - 1.0f) * d2v;
+  grad = 2.0f * istep * (dv + (chi - 0.5f) * d2v);
+}
+__device__ __forceinline__ float quadf_v(const float4 p, float chi) {
+  float dv = p.y - p.x;
+  float d2v = p.z - 2.0f * p.y + p.x;
+  return p.x + chi * dv + 0.5f * chi * (chi - 1.0f) * d2v;
+}
+__device__ __forceinline__ float quadf_g(const float4 p, float chi, float istep) {
+  float dv = p.y - p.x;
+  float d2v = p.z - 2.0f * p.y + p.x;
+  return 2.0f * istep * (dv + (chi - 0.5f) * d2v);
+}
+
+// ---------------------------------------------------------------------------
+// reductions
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ double warp_max(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+// Block-wide sum of K values per thread into out[blockIdx.x * K + k]
+// (deterministic: fixed shuffle tree, fixed warp order).
+template <int K, int BS>
+__device__ __forceinline__ void block_sum_store(double (&v)[K], double *out) {
+  __shared__ double sh[K][BS / 32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < K; k++) {
+    double s = warp_sum(v[k]);
+    if (lane == 0) sh[k][w] = s;
+  }
+  __syncthreads();
+  if (threadIdx.x < K) {
+    double s = 0.0;
+#pragma unroll
+    for (int i = 0; i < BS / 32; i++) s += sh[threadIdx.x][i];
+    out[(size_t)blockIdx.x * K + threadIdx.x] = s;
+  }
+}
+
+}  // namespace imdgpu

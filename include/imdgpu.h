@@ -1,0 +1,177 @@
+/*
+ * imdgpu.h -- C-ABI of the GB300 replacement for IMD's force, neighbour-list,
+ * NVE and CG hot path (itapmd/imd).
+ *
+ * Plain C types only: opaque handles, pointers and sizes.  Every function
+ * returns an int status (IMDGPU_OK = 0, > 0 recoverable, < 0 fatal; the
+ * message is in imdgpu_last_error()).  Kernels never trap; device-side
+ * problems (list or cell overflow, short distances, CG failures) are
+ * reported through status words that these calls read back.
+ *
+ * Data ownership follows the reference's calc_forces contract
+ * (src/imd_forces_nbl.c:281): the caller owns the atoms; the library keeps a
+ * device-resident, cell-sorted mirror, and copies in/out only on request.
+ * Atom arrays exchanged through this interface are in the caller's order
+ * (the order of imdgpu_set_atoms), atom-major (x[3*i+c]).
+ */
+#ifndef IMDGPU_H
+#define IMDGPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define IMDGPU_OK 0
+#define IMDGPU_WARN_SHORT 1       /* a pair closer than a table's begin (IMD: "Short distance") */
+#define IMDGPU_ERR_ARG (-1)
+#define IMDGPU_ERR_CUDA (-2)
+#define IMDGPU_ERR_NOMEM (-3)
+#define IMDGPU_ERR_GEOM (-4)      /* box too small for one cell of list radius */
+#define IMDGPU_ERR_TABLE (-5)
+#define IMDGPU_ERR_BRENT (-6)     /* "Too many iterations in brent" */
+#define IMDGPU_ERR_CELL (-7)      /* more atoms in one cell than supported */
+#define IMDGPU_ERR_STATE (-8)     /* call order (e.g. forces before atoms) */
+
+#define IMDGPU_PAIR 0             /* pair potential only (target imd_*_nbl) */
+#define IMDGPU_EAM2 1             /* pair + EAM2 (target imd_*_nbl_eam) */
+
+#define IMDGPU_FP64 0             /* all arithmetic in FP64 */
+#define IMDGPU_MIXED 1            /* pair/EAM arithmetic in FP32 on cell-relative
+                                     coordinates, FP64 positions/accumulation */
+
+#define IMDGPU_TAB_PAIR 0
+#define IMDGPU_TAB_RHO 1
+#define IMDGPU_TAB_EMBED 2
+
+typedef struct imdgpu_sys imdgpu_sys;
+
+/* Global results of the last calls; same meaning as IMD's globals
+ * (src/globals.h:405-412, :1444 onwards). */
+typedef struct {
+  double tot_pot_energy;   /* calc_forces */
+  double virial;           /* calc_forces */
+  double tot_kin_energy;   /* move_atoms_nve (half-step average) */
+  double fnorm;            /* sum |F|^2 (move_atoms_nve / calc_fnorm) */
+  double f_max2;           /* max squared force component */
+  double max_atom_force;   /* max per-atom |F| (CG stopping rule) */
+  long nfc;                /* force calls */
+  long nbl_count;          /* neighbour-list builds */
+  long nb_entries;         /* entries of the current list */
+  int have_valid_nbl;
+  int gdim[3];             /* global_cell_dim */
+  int nghost;              /* buffer-cell (ghost) atoms of the last build */
+  int max_cell_atoms;
+  int short_distance;      /* nonzero if a pair was below a table begin */
+} imdgpu_scalars;
+
+const char *imdgpu_last_error(void);
+const char *imdgpu_version(void);
+int imdgpu_device_count(int *count);
+/* select the CUDA device for systems created afterwards by this thread */
+int imdgpu_set_device(int device);
+
+/* Replaces IMD's implicit single global system (src/globals.h). */
+int imdgpu_create(imdgpu_sys **sys, int ntypes, int interaction, int precision);
+int imdgpu_destroy(imdgpu_sys *sys);
+/* precision may be switched between calls (the list is kept) */
+int imdgpu_set_precision(imdgpu_sys *sys, int precision);
+
+/* Upload one pot_table_t (src/types.h:416-428) exactly as IMD holds it
+ * after read_pot_table + init_threepoint (src/imd_potential.c:161-282,
+ * :1256-1272): value of column col at row k is table[k*ncols + col], with
+ * (maxsteps + 2) rows.  `which` is IMDGPU_TAB_*. */
+int imdgpu_set_table(imdgpu_sys *sys, int which, int ncols, int maxsteps,
+                     const double *begin, const double *end, const double *step,
+                     const double *invstep, const int *len, const double *table);
+/* Read an IMD potential file (formats 1 and 2, src/imd_potential.c:161-462)
+ * on the host and upload it.  radial as in read_pot_table. */
+int imdgpu_read_table(imdgpu_sys *sys, int which, const char *fname, int radial,
+                      int default_format);
+
+/* Box rows box_x, box_y, box_z (box[3*a+c]), periodicity, list margin
+ * (nbl_margin, src/globals.h:419).  list_r2 > 0 overrides the neighbour
+ * list radius^2 (IMD's cellsz after init_cells); 0 derives it as
+ * (sqrt(max radial table end) + nbl_margin)^2 like init_cells
+ * (src/imd_geom_3d.c:122-126). */
+int imdgpu_set_box(imdgpu_sys *sys, const double *box, const int *pbc, double nbl_margin,
+                   double list_r2);
+/* per-type restriction vectors (src/globals.h:206), 3*ntypes, 1 = free */
+int imdgpu_set_restrictions(imdgpu_sys *sys, const double *restr);
+
+/* Atoms: NUMMER, SORTE, MASSE, ORT (3n), IMPULS (3n, may be NULL). */
+int imdgpu_set_atoms(imdgpu_sys *sys, int n, const int *number, const int *type,
+                     const double *mass, const double *x, const double *p);
+/* Replace positions and momenta (caller order, 3n each; p may be NULL)
+ * without touching the neighbour list: the state IMD's cell arrays hand
+ * back to calc_forces each step when they live on the host. */
+int imdgpu_put_state(imdgpu_sys *sys, const double *x, const double *p);
+/* Copy state back (any pointer may be NULL): x, p, f (3n), epot (n),
+ * eam_rho, eam_df (n). */
+int imdgpu_get_atoms(imdgpu_sys *sys, double *x, double *p, double *f, double *epot,
+                     double *eam_rho, double *eam_df);
+int imdgpu_get_scalars(imdgpu_sys *sys, imdgpu_scalars *out);
+
+/* calc_forces (src/imd_forces_nbl.c:281-1999): fix_cells + make_nblist when
+ * the list is invalid, then pair / EAM2 forces, energies and virial. */
+int imdgpu_calc_forces(imdgpu_sys *sys, int steps);
+/* make_nblist (src/imd_forces_nbl.c:136-273): wrap, bin and rebuild now */
+int imdgpu_make_nblist(imdgpu_sys *sys);
+/* check_nblist (src/imd_forces_nbl.c:2007-2037) */
+int imdgpu_check_nblist(imdgpu_sys *sys);
+/* deallocate_nblist (src/imd_forces_nbl.c:56-64): drop the list */
+int imdgpu_deallocate_nblist(imdgpu_sys *sys);
+/* estimate_nblist_size (src/imd_forces_nbl.c:74-128): entries of a fresh list */
+int imdgpu_estimate_nblist_size(imdgpu_sys *sys, long *entries);
+/* move_atoms_nve (src/imd_integrate.c:32-497) */
+int imdgpu_move_atoms_nve(imdgpu_sys *sys, double timestep);
+/* nsteps of main_loop (src/imd_main_3d.c:155-870) for ensemble nve:
+ * calc_forces, move_atoms_nve, check_nblist, fully on the device.
+ * epot/ekin (may be NULL) receive tot_pot_energy and tot_kin_energy of every
+ * step. */
+int imdgpu_nve_run(imdgpu_sys *sys, int nsteps, double timestep, double *epot,
+                   double *ekin);
+
+/* CG (src/imd_cg.c): reset_cg (:30-38), cg_step (:46-66, linmin/mnbrak/brent
+ * of src/cg_utils.h:34-194), and a driver that stops on the max per-atom
+ * force (the threshold IMD parses as f_max_threshold, src/imd_param.c:850). */
+int imdgpu_set_cg_params(imdgpu_sys *sys, int linmin_maxsteps, double linmin_tol,
+                         double linmin_dmax, double linmin_dmin, double cg_glimit,
+                         double cg_zeps, int cg_fr, int cg_reset_int);
+int imdgpu_reset_cg(imdgpu_sys *sys);
+int imdgpu_cg_step(imdgpu_sys *sys, int steps);
+int imdgpu_cg_relax(imdgpu_sys *sys, double fmax, int maxsteps, int *steps_done,
+                    double *fmax_out);
+
+/* Neighbour pairs of the current list: NUMMER of both atoms, image shift of
+ * the second (3 ints, in box vectors) and r^2 as used for the list test.
+ * With cap == 0 only *count is set. */
+int imdgpu_get_pairs(imdgpu_sys *sys, long cap, int *ni, int *nj, int *shift,
+                     double *r2, long *count);
+
+/* Timing of the dominant kernels of the last nve_run (device ms, CUDA
+ * events on the system's stream). */
+typedef struct {
+  double ms_total;
+  double ms_density;
+  double ms_force;
+  double ms_integrate;
+  double ms_rebuild;
+  int steps;
+  int rebuilds;
+  long kernel_launches;
+} imdgpu_timing;
+int imdgpu_get_timing(imdgpu_sys *sys, imdgpu_timing *out);
+/* enable per-kernel event timing in nve_run (adds event records) */
+int imdgpu_set_profiling(imdgpu_sys *sys, int on);
+/* Between the steps of nve_run write `bytes` of scratch so that each timed
+ * step starts with a cold L2 (benchmarking); the write is outside the timed
+ * windows.  0 disables. */
+int imdgpu_set_l2_flush(imdgpu_sys *sys, long bytes);
+/* Measured FP64 FMA throughput of this device (TFLOP/s): a roofline
+ * denominator for the FP64 force kernels. */
+int imdgpu_probe_fp64_peak(double *tflops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
