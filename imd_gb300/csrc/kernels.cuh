@@ -34,4 +34,7 @@ constexpr int BS_VEC = 256;
 int launch_forces(const SysView &v, const ForceTabs &t, DevScalars *sc, int mixed,
                   cudaStream_t st, cudaEvent_t *ev = nullptr);
 
+// system.cu: message returned by imdgpu_last_error()
+void set_last_error(const char *msg);
+
 }  // namespace imdgpu

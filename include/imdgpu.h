@@ -171,6 +171,28 @@ int imdgpu_set_l2_flush(imdgpu_sys *sys, long bytes);
  * denominator for the FP64 force kernels. */
 int imdgpu_probe_fp64_peak(double *tflops);
 
+/* move_atoms_nve for callers that cannot allocate device memory.  No
+ * counterpart in the reference: IMD allocates everything itself.  Meant for
+ * host programs whose device memory all comes from their own pool or arena,
+ * or that must not meet the device synchronisation cudaMalloc/cudaFree can
+ * cause inside a time step: this call allocates nothing.  The caller passes
+ * its own device arrays, atom-major (x, p, f: 3n doubles; mass: n doubles;
+ * type: n ints; x_ref: 3n doubles or NULL, the positions of the last list
+ * build), host `restr` (3*ntypes, NULL = all free) and host `out` (4
+ * doubles: tot_kin_energy, fnorm, f_max2, max |x - x_ref|^2); stream may be
+ * NULL (default stream).  The kinetic-energy and norm partial sums go to a
+ * fixed file-scope device array of 2 MiB per device, so n is limited to
+ * 16,777,216 atoms (IMDGPU_ERR_ARG beyond).  The first call on each device
+ * looks up that array's device address (with the device current); make it
+ * before any stream capture.  All calls on a device share the array and
+ * leave their partial sums in it; each call overwrites every slot it reads,
+ * so nothing needs clearing, but calls that overlap on the GPU (two streams
+ * at once) race on it.  Returns after the results are in `out`. */
+int imdgpu_move_atoms_nve_noalloc(int n, int ntypes, double *x, double *p, double *f,
+                                  const double *mass, const int *type, const double *restr,
+                                  double timestep, const double *x_ref, double *out,
+                                  void *stream);
+
 #ifdef __cplusplus
 }
 #endif
