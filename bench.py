@@ -242,7 +242,7 @@ def run_ours(args, rank, world, local):
 
     # ---- end to end through the C-ABI with host buffers ----
     s = r["sys"]
-    e2e_steps = min(args.steps, 20)
+    e2e_steps = 0 if args.no_e2e else min(args.steps, 20)
     try:
         import torch
         xh = torch.empty((n, 3), dtype=torch.float64, pin_memory=True).numpy()
@@ -252,7 +252,7 @@ def run_ours(args, rank, world, local):
     except Exception:
         xh, ph, fh, eh = (np.empty((n, 3)), np.empty((n, 3)), np.empty((n, 3)), np.empty(n))
     s.get_state(xh, ph, fh, eh)
-    for _ in range(3):   # warm-up of the host path
+    for _ in range(3 if e2e_steps else 0):   # warm-up of the host path
         s.put_state(xh, ph)
         s.calc_forces(0)
         s.move_atoms_nve(dt)
@@ -268,7 +268,7 @@ def run_ours(args, rank, world, local):
         s.get_state(xh, ph, fh, eh)
     t_e2e = time.perf_counter() - t0
     barrier()
-    e2e = n * e2e_steps * world / t_e2e
+    e2e = n * e2e_steps * world / t_e2e if e2e_steps else None
 
     # ---- roofline of the dominant kernel (EAM force pass) ----
     force_ms = r["ms_force"] / args.steps
@@ -336,6 +336,7 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=16)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-mixed", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
     args = ap.parse_args()
     rank, world, local = dist_env()
     if args.impl == "reference":

@@ -63,6 +63,7 @@ def lib() -> C.CDLL:
         vp = C.c_void_p
         L.imdgpu_destroy.argtypes = [vp]
         L.imdgpu_set_precision.argtypes = [vp, C.c_int]
+        L.imdgpu_set_exact.argtypes = [vp, C.c_int]
         L.imdgpu_set_table.argtypes = [vp, C.c_int, C.c_int, C.c_int, _dp, _dp, _dp, _dp,
                                        _ip, _dp]
         L.imdgpu_read_table.argtypes = [vp, C.c_int, C.c_char_p, C.c_int, C.c_int]
@@ -181,6 +182,10 @@ class GpuSystem:
 
     def set_profiling(self, on: bool) -> None:
         _check(lib().imdgpu_set_profiling(self.h, int(on)), "set_profiling")
+
+    def set_exact(self, on: bool) -> None:
+        """IMD's unfused table arithmetic (bitwise table values) on/off."""
+        _check(lib().imdgpu_set_exact(self.h, int(on)), "set_exact")
 
     def set_precision(self, precision: int) -> None:
         _check(lib().imdgpu_set_precision(self.h, precision), "imdgpu_set_precision")

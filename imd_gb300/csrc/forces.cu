@@ -196,11 +196,199 @@ __global__ void k_finalize_forces(const double *pe, int ne, const double *pf, in
   }
 }
 
+// ---------------------------------------------------------------------------
+// fast FP64 kernels: coefficient-form tables with FMA, integer-domain cutoff
+// tests, one table index per pair when pair and rho share their grid, single
+// type specialisation, per-atom energy scatter only when requested.  Same
+// pairs and formulas as above; only rounding differs (~1e-16 relative).
+// ---------------------------------------------------------------------------
+template <bool NT1>
+__global__ void __launch_bounds__(BS_FORCE) k_density_fast(SysView v, DevTable rho) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= v.n) return;
+  const double4 pi = v.pos[i];
+  const int it = NT1 ? 0 : (int)pi.w, nt = v.ntypes;
+  const int nn = v.nnb[i];
+  bool shortf = false;
+  double eam_r = 0.0;
+  const uint32_t *__restrict__ nb = v.nbr + i;
+#pragma unroll 2
+  for (int k = 0; k < nn; k++) {
+    const int j = (int)(__ldg(nb + (size_t)k * v.ncap) & NB_MASK);
+    const double4 pj = ldg4(&v.pos[j]);
+    const double dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
+    const double r2 = fma(dx, dx, fma(dy, dy, dz * dz));
+    const int jt = NT1 ? 0 : (int)pj.w;
+    const int col = NT1 ? 0 : it * nt + jt;
+    double rho_h = 0.0;
+    if (lt_pos(r2, rho.end[col])) {
+      double chi;
+      const int kk = tab_index_fast(rho, col, r2, chi);
+      rho_h = poly_v(cv_load(rho, col, kk), chi);
+      eam_r += rho_h;
+      shortf |= lt_pos(r2, rho.begin[col]);
+    }
+    if (NT1 || it == jt) {
+      if (lt_pos(r2, rho.end[col])) atomicAdd(&v.rho[j], rho_h);
+    } else {
+      const int col2 = jt * nt + it;
+      if (lt_pos(r2, rho.end[col2])) {
+        double chi;
+        const int kk = tab_index_fast(rho, col2, r2, chi);
+        atomicAdd(&v.rho[j], poly_v(cv_load(rho, col2, kk), chi));
+        shortf |= lt_pos(r2, rho.begin[col2]);
+      }
+    }
+  }
+  atomicAdd(&v.rho[i], eam_r);
+  if (shortf) atomicOr(v.status, ST_SHORT);
+}
+
+template <bool NT1, bool EAM, bool EPOT, bool SAMEGRID>
+__global__ void __launch_bounds__(BS_FORCE) k_force_fast(SysView v, DevTable pair, DevTable rho,
+                                                         double *partial) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double acc[2] = {0.0, 0.0};  // energy, virial
+  if (i < v.n) {
+    const double4 pi = v.pos[i];
+    const int it = NT1 ? 0 : (int)pi.w, nt = v.ntypes;
+    const int nn = v.nnb[i];
+    const double dfi = EAM ? v.df[i] : 0.0;
+    bool shortf = false;
+    double ffx = 0.0, ffy = 0.0, ffz = 0.0, ee = 0.0, esum = 0.0, vir = 0.0;
+    const uint32_t *__restrict__ nb = v.nbr + i;
+#pragma unroll 2
+    for (int k = 0; k < nn; k++) {
+      const int j = (int)(__ldg(nb + (size_t)k * v.ncap) & NB_MASK);
+      const double4 pj = ldg4(&v.pos[j]);
+      const double dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
+      const double r2 = fma(dx, dx, fma(dy, dy, dz * dz));
+      const int jt = NT1 ? 0 : (int)pj.w;
+      const int col = NT1 ? 0 : it * nt + jt;
+      double grad = 0.0, ehalf = 0.0;
+      bool have = false;
+      int kk = 0;
+      double chi = 0.0;
+      if (le_pos(r2, pair.end[col])) {
+        kk = tab_index_fast(pair, col, r2, chi);
+        const double4 c = cv_load(pair, col, kk);
+        const double2 g = cg_load(pair, col, kk);
+        const double pot = poly_v(c, chi);
+        grad = poly_g(g, chi);
+        esum += pot;
+        if (EPOT) {
+          ehalf = 0.5 * pot;
+          ee += ehalf;
+        }
+        shortf |= lt_pos(r2, pair.begin[col]);
+        have = true;
+      }
+      if (EAM) {
+        const int col1 = NT1 ? 0 : jt * nt + it, col2 = col;
+        if (lt_pos(r2, rho.end[col1]) || lt_pos(r2, rho.end[col2])) {
+          double chi1 = chi;
+          int k1 = kk;
+          if (!(SAMEGRID && have)) k1 = tab_index_fast(rho, col1, r2, chi1);
+          const double ris = poly_g(cg_load(rho, col1, k1), chi1);
+          const double dfj = __ldg(&v.df[j]);
+          double ge;
+          if (NT1 || col1 == col2) {
+            ge = ris * (0.5 * (dfi + dfj));
+          } else {
+            double chi2 = chi;
+            int k2 = kk;
+            if (!(SAMEGRID && have)) k2 = tab_index_fast(rho, col2, r2, chi2);
+            const double rjs = poly_g(cg_load(rho, col2, k2), chi2);
+            ge = 0.5 * (dfi * rjs + dfj * ris);
+          }
+          grad += ge;
+          have = true;
+        }
+      }
+      if (have) {
+        const double fx = dx * grad, fy = dy * grad, fz = dz * grad;
+        double *fj = &v.frc[j].x;
+        atomicAdd(fj + 0, -fx);
+        atomicAdd(fj + 1, -fy);
+        atomicAdd(fj + 2, -fz);
+        if (EPOT) atomicAdd(fj + 3, ehalf);
+        ffx += fx;
+        ffy += fy;
+        ffz += fz;
+        vir = fma(-r2, grad, vir);
+      }
+    }
+    double *fi = &v.frc[i].x;
+    atomicAdd(fi + 0, ffx);
+    atomicAdd(fi + 1, ffy);
+    atomicAdd(fi + 2, ffz);
+    if (EPOT) atomicAdd(fi + 3, ee);
+    acc[0] = esum;
+    acc[1] = vir;
+    if (shortf) atomicOr(v.status, ST_SHORT);
+  }
+  block_sum_store<2, BS_FORCE>(acc, partial);
+}
+
+// embedding with the coefficient-form table
+__global__ void __launch_bounds__(BS_VEC) k_embed_fast(SysView v, DevTable emb, double *partial) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double e[1] = {0.0};
+  if (i < v.n) {
+    const int t = (int)v.pos[i].w;
+    double chi;
+    const int k = tab_index_fast(emb, t, v.rho[i], chi);
+    const double pot = poly_v(cv_load(emb, t, k), chi);
+    v.df[i] = poly_g(cg_load(emb, t, k), chi);
+    atomicAdd(&v.frc[i].w, pot);
+    e[0] = pot;
+  }
+  block_sum_store<1, BS_VEC>(e, partial);
+}
+
+template <bool NT1, bool EAM, bool EPOT>
+static void launch_force_fast(int samegrid, int nbf, cudaStream_t st, const SysView &v,
+                              const ForceTabs &t, double *pf) {
+  if (samegrid)
+    k_force_fast<NT1, EAM, EPOT, true><<<nbf, BS_FORCE, 0, st>>>(v, t.pair, t.rho, pf);
+  else
+    k_force_fast<NT1, EAM, EPOT, false><<<nbf, BS_FORCE, 0, st>>>(v, t.pair, t.rho, pf);
+}
+
+template <bool EAM, bool EPOT>
+static void launch_force_fast2(const ForceTabs &t, int nbf, cudaStream_t st, const SysView &v,
+                               double *pf) {
+  if (t.nt1)
+    launch_force_fast<true, EAM, EPOT>(t.samegrid, nbf, st, v, t, pf);
+  else
+    launch_force_fast<false, EAM, EPOT>(t.samegrid, nbf, st, v, t, pf);
+}
+
+static void launch_force_any(const ForceTabs &t, int nbf, cudaStream_t st, const SysView &v,
+                             double *pf) {
+  if (t.exact) {
+    if (t.eam) k_force64<true><<<nbf, BS_FORCE, 0, st>>>(v, t.pair, t.rho, pf);
+    else k_force64<false><<<nbf, BS_FORCE, 0, st>>>(v, t.pair, t.rho, pf);
+    return;
+  }
+  if (t.eam) {
+    if (t.epot) launch_force_fast2<true, true>(t, nbf, st, v, pf);
+    else launch_force_fast2<true, false>(t, nbf, st, v, pf);
+  } else {
+    if (t.epot) launch_force_fast2<false, true>(t, nbf, st, v, pf);
+    else launch_force_fast2<false, false>(t, nbf, st, v, pf);
+  }
+}
+
 static inline int nblk(long n, int bs) { return (int)((n + bs - 1) / bs); }
+
+void k_ghost_pos_launch(const SysView &v, int blocks, cudaStream_t st) {
+  k_ghost_pos<<<blocks, BS_VEC, 0, st>>>(v);
+}
 
 int launch_forces(const SysView &v, const ForceTabs &t, DevScalars *sc, int mixed,
                   cudaStream_t st, cudaEvent_t *ev) {
-  (void)mixed;
+  if (mixed) return launch_forces_mixed(v, t, sc, v.dff, st, ev);
   int launches = 0;
   const int gblocks = nblk(v.gcap, BS_VEC) > 0 ? nblk(v.gcap, BS_VEC) : 1;
   const size_t ext = (size_t)v.ncap + v.gcap;
@@ -212,13 +400,16 @@ int launch_forces(const SysView &v, const ForceTabs &t, DevScalars *sc, int mixe
   if (t.eam) {
     cudaMemsetAsync(v.rho, 0, ext * sizeof(double), st);
     if (ev) cudaEventRecord(ev[0], st);
-    k_density64<<<nbf, BS_FORCE, 0, st>>>(v, t.rho);
+    if (t.exact) k_density64<<<nbf, BS_FORCE, 0, st>>>(v, t.rho);
+    else if (t.nt1) k_density_fast<true><<<nbf, BS_FORCE, 0, st>>>(v, t.rho);
+    else k_density_fast<false><<<nbf, BS_FORCE, 0, st>>>(v, t.rho);
     if (ev) cudaEventRecord(ev[1], st);
     k_fold_rho<<<gblocks, BS_VEC, 0, st>>>(v);
-    k_embed<<<nbe, BS_VEC, 0, st>>>(v, t.embed, pe);
+    if (t.exact) k_embed<<<nbe, BS_VEC, 0, st>>>(v, t.embed, pe);
+    else k_embed_fast<<<nbe, BS_VEC, 0, st>>>(v, t.embed, pe);
     k_ghost_df<<<gblocks, BS_VEC, 0, st>>>(v);
     if (ev) cudaEventRecord(ev[2], st);
-    k_force64<true><<<nbf, BS_FORCE, 0, st>>>(v, t.pair, t.rho, pf);
+    launch_force_any(t, nbf, st, v, pf);
     if (ev) cudaEventRecord(ev[3], st);
     launches += 5;
   } else {
@@ -227,7 +418,7 @@ int launch_forces(const SysView &v, const ForceTabs &t, DevScalars *sc, int mixe
       cudaEventRecord(ev[1], st);
       cudaEventRecord(ev[2], st);
     }
-    k_force64<false><<<nbf, BS_FORCE, 0, st>>>(v, t.pair, t.rho, pf);
+    launch_force_any(t, nbf, st, v, pf);
     if (ev) cudaEventRecord(ev[3], st);
     launches += 1;
   }

@@ -34,14 +34,29 @@ constexpr unsigned ST_CELLOVER = 8u;   // atoms per cell beyond CELLCAP
 // One pot_table_t on the device.  `tri` holds, per column and row k, the
 // three table values the quadratic interpolation reads (rows k, k+1, k+2):
 // one aligned 32 B record per lookup instead of three strided loads.
+//
+// The fast kernels read the same quadratic in coefficient form: with
+// dv = p1 - p0 and d2v = p2 - 2 p1 + p0 of row k,
+//   value(chi) = A + chi (B + chi C),   A = p0, B = dv - d2v/2, C = d2v/2
+//   2 dV/dr2   = G0 + chi G1,           G0 = 2 istep B, G1 = 4 istep C
+// (algebraically IMD's p0 + chi dv + chi (chi-1) d2v / 2 and
+// 2 istep (dv + (chi - 1/2) d2v)), three FMAs instead of ~15 operations.
 struct DevTable {
   int ncols;
   int rows;                 // maxsteps + 2
   const double4 *tri;       // tri[col * rows + k] = (t[k], t[k+1], t[k+2], 0)
   const float4 *trif;       // same in FP32 (mixed precision)
+  const double4 *cv;        // (A, B, C, 0) per column and row
+  const double2 *cg;        // (G0, G1)
+  const float4 *cvf;        // FP32 copies for the mixed path
+  const float2 *cgf;
   double begin[MAXCOL];
   double end[MAXCOL];
   double invstep[MAXCOL];
+  double boff[MAXCOL];      // -begin * invstep
+  float fbegin[MAXCOL];
+  float fend[MAXCOL];
+  float finv[MAXCOL];
 };
 
 // Everything a kernel of one system needs, passed by value.
@@ -64,7 +79,8 @@ struct SysView {
 
   double4 *pos, *mom, *frc, *ref;
   double *rho, *df;
-  float4 *xl;               // mixed: cell-relative FP32 positions + type bits
+  float4 *xl;               // mixed: per atom FP32 (hi, lo) split of the position
+  float *dff;               // mixed: 2F' in FP32 (ext)
   int *number, *orig;
   int *ecell;               // buffered cell id of every ext atom
   int *gowner;              // ghost -> owning real slot
@@ -74,7 +90,8 @@ struct SysView {
   int *cstart, *ccount;     // per buffered cell: first ext index, atoms
   const int *cell_rank;     // buffered lin -> Morton rank of real cell (-1 for buffer)
   const int *rank_lin;      // rank -> buffered lin
-  const int *hshell;        // 14 buffered lin per real rank (-1 none)
+  const int *hshell;        // nshell buffered lin per real rank (-1 none): half or full shell
+  int nshell;               // 14 (half list, IMD's AR order) or 27 (full list)
   const int *bsrc;          // per buffer cell (enumerated): source real lin
   const int *blin;          // per buffer cell: its lin
   const int *bcode;         // per buffer cell: packed image shift
@@ -162,6 +179,37 @@ __device__ __forceinline__ double deriv_func2(const DevTable &t, int col, double
   int k = tab_index(r2, t.begin[col], t.end[col], t.invstep[col], chi, shortf);
   return quad_g(tab_load(t, col, k), chi, t.invstep[col]);
 }
+
+// ---------------------------------------------------------------------------
+// fast FP64 table access (FMA, coefficient form)
+// ---------------------------------------------------------------------------
+// r2 <= end / r2 < end for non-negative doubles, compared as integers so the
+// test does not occupy the FP64 pipe
+__device__ __forceinline__ bool le_pos(double a, double b) {
+  return __double_as_longlong(a) <= __double_as_longlong(b);
+}
+__device__ __forceinline__ bool lt_pos(double a, double b) {
+  return __double_as_longlong(a) < __double_as_longlong(b);
+}
+
+__device__ __forceinline__ int tab_index_fast(const DevTable &t, int col, double r2, double &chi) {
+  const double rm = fmin(r2, t.end[col]);
+  double r2a = fma(rm, t.invstep[col], t.boff[col]);
+  r2a = fmax(r2a, 0.0);
+  const int k = __double2int_rz(r2a);
+  chi = r2a - (double)k;
+  return k;
+}
+__device__ __forceinline__ double4 cv_load(const DevTable &t, int col, int k) {
+  return ldg4(&t.cv[(size_t)col * t.rows + k]);
+}
+__device__ __forceinline__ double2 cg_load(const DevTable &t, int col, int k) {
+  return __ldg(&t.cg[(size_t)col * t.rows + k]);
+}
+__device__ __forceinline__ double poly_v(const double4 c, double chi) {
+  return fma(chi, fma(chi, c.z, c.y), c.x);
+}
+__device__ __forceinline__ double poly_g(const double2 g, double chi) { return fma(chi, g.y, g.x); }
 
 // A ghost copies its owner through the z, y, x buffer copies of send_cells
 // (src/imd_comm_force_3d.c:247-358) in that order, so its position is

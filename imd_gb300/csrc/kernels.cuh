@@ -8,6 +8,10 @@ namespace imdgpu {
 struct ForceTabs {
   DevTable pair, rho, embed;
   int eam;
+  int nt1;       // single atom type
+  int samegrid;  // pair and rho columns share begin / end / step: one index per pair
+  int exact;     // IMD's unfused arithmetic (bitwise table values) instead of FMA form
+  int epot;      // scatter per-atom energies (POTENG) in the force pass
 };
 
 // Device-side scalars of one system (results + control).
@@ -33,6 +37,12 @@ constexpr int BS_VEC = 256;
 // ev (may be null): 4 events recorded around the density and force kernels.
 int launch_forces(const SysView &v, const ForceTabs &t, DevScalars *sc, int mixed,
                   cudaStream_t st, cudaEvent_t *ev = nullptr);
+
+// forces.cu: refresh ghost positions (send_cells(copy_cell))
+void k_ghost_pos_launch(const SysView &v, int blocks, cudaStream_t st);
+// mixed.cu: the FP32-force path over the full list
+int launch_forces_mixed(const SysView &v, const ForceTabs &t, DevScalars *sc, float *dff,
+                        cudaStream_t st, cudaEvent_t *ev);
 
 // system.cu: message returned by imdgpu_last_error()
 void set_last_error(const char *msg);

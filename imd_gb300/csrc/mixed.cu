@@ -1,0 +1,269 @@
+// mixed.cu -- FP32-force / FP64-accumulate path (IMDGPU_MIXED).
+//
+// Same physics as forces.cu (calc_forces PAIR + EAM2, src/imd_forces_nbl.c:
+// 423-1323) with the pair and EAM arithmetic in FP32:
+//   * positions stay FP64; every step each real and ghost atom is split into
+//     an FP32 high part and an FP32 residual (x = hi + lo to ~1e-14), so
+//     d = (hi_j - hi_i) + (lo_j - lo_i) is accurate to the last FP32 bit of d
+//     itself: the coordinates an FP32 pair sees are relative to the atom,
+//     never absolute box coordinates;
+//   * the list is the FULL list (every pair from both sides), so each thread
+//     owns its atom's sums: no atomics, no ghost fold;
+//   * per-atom sums of rho, force, energy and virial are kept as error-free
+//     (TwoSum) pairs of FP32 values and converted to FP64 once per atom; the
+//     block and device reductions are FP64;
+//   * the embedding function and the integrator stay FP64.
+#include <algorithm>
+
+#include "kernels.cuh"
+
+namespace imdgpu {
+
+struct __align__(16) SplitPos {
+  float4 hi;  // x, y, z, type (int bits)
+  float4 lo;  // residuals
+};
+
+// error-free accumulation: s + c carries the exact running sum to ~2^-48
+struct Acc {
+  float s, c;
+  __device__ __forceinline__ Acc() : s(0.f), c(0.f) {}
+  __device__ __forceinline__ void add(float x) {
+    const float t = s + x;
+    const float z = t - s;
+    c += (s - (t - z)) + (x - z);
+    s = t;
+  }
+  __device__ __forceinline__ double value() const { return (double)s + (double)c; }
+};
+
+__global__ void k_split(SysView v, SplitPos *sp) {
+  const int ne = v.n + v.counters[0];
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < ne; e += gridDim.x * blockDim.x) {
+    const double4 p = v.pos[e];
+    SplitPos o;
+    o.hi.x = (float)p.x;
+    o.hi.y = (float)p.y;
+    o.hi.z = (float)p.z;
+    o.hi.w = __int_as_float((int)p.w);
+    o.lo.x = (float)(p.x - (double)o.hi.x);
+    o.lo.y = (float)(p.y - (double)o.hi.y);
+    o.lo.z = (float)(p.z - (double)o.hi.z);
+    o.lo.w = 0.f;
+    sp[e] = o;
+  }
+}
+
+__device__ __forceinline__ SplitPos ldsp(const SplitPos *p) {
+  SplitPos o;
+  o.hi = __ldg(&p->hi);
+  o.lo = __ldg(&p->lo);
+  return o;
+}
+
+__device__ __forceinline__ int tab_index_f(const DevTable &t, int col, float r2, float &chi) {
+  float r2a = fmaf(fminf(r2, t.fend[col]), t.finv[col], -t.fbegin[col] * t.finv[col]);
+  r2a = fmaxf(r2a, 0.0f);
+  const int k = __float2int_rz(r2a);
+  chi = r2a - (float)k;
+  return k;
+}
+__device__ __forceinline__ float polyf_v(const DevTable &t, int col, int k, float chi) {
+  const float4 c = __ldg(&t.cvf[(size_t)col * t.rows + k]);
+  return fmaf(chi, fmaf(chi, c.z, c.y), c.x);
+}
+__device__ __forceinline__ float polyf_g(const DevTable &t, int col, int k, float chi) {
+  const float2 g = __ldg(&t.cgf[(size_t)col * t.rows + k]);
+  return fmaf(chi, g.y, g.x);
+}
+
+// rho_i = sum_j rho_{it,jt}(r_ij) over the full list (loop 1's eam_r)
+template <bool NT1>
+__global__ void __launch_bounds__(BS_FORCE) k_density_mixed(SysView v, DevTable rho,
+                                                            const SplitPos *sp) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= v.n) return;
+  const SplitPos a = sp[i];
+  const int it = NT1 ? 0 : __float_as_int(a.hi.w), nt = v.ntypes;
+  const int nn = v.nnb[i];
+  Acc r;
+  bool shortf = false;
+  const uint32_t *__restrict__ nb = v.nbr + i;
+#pragma unroll 4
+  for (int k = 0; k < nn; k++) {
+    const int j = (int)(__ldg(nb + (size_t)k * v.ncap) & NB_MASK);
+    const SplitPos b = ldsp(&sp[j]);
+    const float dx = (b.hi.x - a.hi.x) + (b.lo.x - a.lo.x);
+    const float dy = (b.hi.y - a.hi.y) + (b.lo.y - a.lo.y);
+    const float dz = (b.hi.z - a.hi.z) + (b.lo.z - a.lo.z);
+    const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+    const int col = NT1 ? 0 : it * nt + __float_as_int(b.hi.w);
+    if (r2 < rho.fend[col]) {
+      float chi;
+      const int kk = tab_index_f(rho, col, r2, chi);
+      r.add(polyf_v(rho, col, kk, chi));
+      shortf |= r2 < rho.fbegin[col];
+    }
+  }
+  v.rho[i] = r.value();
+  if (shortf) atomicOr(v.status, ST_SHORT);
+}
+
+// embedding in FP64 (per atom), F' also as FP32 for the pair kernel
+__global__ void __launch_bounds__(BS_VEC) k_embed_mixed(SysView v, DevTable emb, float *dff,
+                                                        double *partial) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double e[1] = {0.0};
+  if (i < v.n) {
+    const int t = (int)v.pos[i].w;
+    double chi;
+    const int k = tab_index_fast(emb, t, v.rho[i], chi);
+    const double pot = poly_v(cv_load(emb, t, k), chi);
+    const double df = poly_g(cg_load(emb, t, k), chi);
+    v.df[i] = df;
+    dff[i] = (float)df;
+    v.frc[i].w = pot;
+    e[0] = pot;
+  }
+  block_sum_store<1, BS_VEC>(e, partial);
+}
+
+__global__ void k_ghost_dff(SysView v, float *dff) {
+  const int ng = v.counters[0];
+  for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < ng; g += gridDim.x * blockDim.x)
+    dff[v.n + g] = dff[v.gowner[g]];
+}
+
+// forces over the full list: each directed pair adds d*grad to atom i and
+// half of the pair energy and virial
+template <bool NT1, bool EAM>
+__global__ void __launch_bounds__(BS_FORCE) k_force_mixed(SysView v, DevTable pair,
+                                                          DevTable rho, const SplitPos *sp,
+                                                          const float *dff, int pair_only_epot,
+                                                          double *partial) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double acc[2] = {0.0, 0.0};
+  if (i < v.n) {
+    const SplitPos a = sp[i];
+    const int it = NT1 ? 0 : __float_as_int(a.hi.w), nt = v.ntypes;
+    const int nn = v.nnb[i];
+    const float dfi = EAM ? dff[i] : 0.f;
+    Acc fx, fy, fz, ee, vir;
+    bool shortf = false;
+    const uint32_t *__restrict__ nb = v.nbr + i;
+#pragma unroll 4
+    for (int k = 0; k < nn; k++) {
+      const int j = (int)(__ldg(nb + (size_t)k * v.ncap) & NB_MASK);
+      const SplitPos b = ldsp(&sp[j]);
+      const float dx = (b.hi.x - a.hi.x) + (b.lo.x - a.lo.x);
+      const float dy = (b.hi.y - a.hi.y) + (b.lo.y - a.lo.y);
+      const float dz = (b.hi.z - a.hi.z) + (b.lo.z - a.lo.z);
+      const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+      const int jt = NT1 ? 0 : __float_as_int(b.hi.w);
+      const int col = NT1 ? 0 : it * nt + jt;
+      float grad = 0.f;
+      bool have = false;
+      if (r2 <= pair.fend[col]) {
+        float chi;
+        const int kk = tab_index_f(pair, col, r2, chi);
+        ee.add(0.5f * polyf_v(pair, col, kk, chi));
+        grad = polyf_g(pair, col, kk, chi);
+        shortf |= r2 < pair.fbegin[col];
+        have = true;
+      }
+      if (EAM) {
+        const int col1 = NT1 ? 0 : jt * nt + it, col2 = col;
+        if (r2 < rho.fend[col1] || r2 < rho.fend[col2]) {
+          float chi;
+          const int kk = tab_index_f(rho, col1, r2, chi);
+          const float ris = polyf_g(rho, col1, kk, chi);
+          float rjs = ris;
+          if (!NT1 && col1 != col2) {
+            const int k2 = tab_index_f(rho, col2, r2, chi);
+            rjs = polyf_g(rho, col2, k2, chi);
+          }
+          const float dfj = __ldg(&dff[j]);
+          grad += 0.5f * (dfi * rjs + dfj * ris);
+          have = true;
+        }
+      }
+      if (have) {
+        fx.add(dx * grad);
+        fy.add(dy * grad);
+        fz.add(dz * grad);
+        vir.add(-0.5f * r2 * grad);
+      }
+    }
+    const double e = ee.value();
+    double4 f = v.frc[i];  // .w holds the embedding energy
+    f.x = fx.value();
+    f.y = fy.value();
+    f.z = fz.value();
+    f.w += e;
+    v.frc[i] = f;
+    acc[0] = e;
+    acc[1] = vir.value();
+    if (shortf) atomicOr(v.status, ST_SHORT);
+  }
+  (void)pair_only_epot;
+  block_sum_store<2, BS_FORCE>(acc, partial);
+}
+
+__global__ void k_finalize_mixed(const double *pe, int ne, const double *pf, int nf,
+                                 DevScalars *sc) {
+  const int lane = threadIdx.x;
+  double e = 0.0, w = 0.0;
+  for (int b = lane; b < ne; b += 32) e += pe[b];
+  for (int b = lane; b < nf; b += 32) {
+    e += pf[2 * b];
+    w += pf[2 * b + 1];
+  }
+  e = warp_sum(e);
+  w = warp_sum(w);
+  if (lane == 0) {
+    sc->epot = e;
+    sc->virial = w;
+  }
+}
+
+static inline int nblk(long n, int bs) { return (int)((n + bs - 1) / bs); }
+
+int launch_forces_mixed(const SysView &v, const ForceTabs &t, DevScalars *sc, float *dff,
+                        cudaStream_t st, cudaEvent_t *ev) {
+  const int gblocks = std::max(1, nblk(v.gcap, BS_VEC));
+  const size_t ext = (size_t)v.ncap + v.gcap;
+  SplitPos *sp = reinterpret_cast<SplitPos *>(v.xl);
+  cudaMemsetAsync(v.frc, 0, (size_t)v.ncap * sizeof(double4), st);
+  k_ghost_pos_launch(v, gblocks, st);
+  k_split<<<nblk(ext, BS_VEC), BS_VEC, 0, st>>>(v, sp);
+  const int nbf = nblk(v.n, BS_FORCE), nbe = nblk(v.n, BS_VEC);
+  double *pe = v.partial, *pf = v.partial + nbe;
+  int launches = 4;
+  if (t.eam) {
+    if (ev) cudaEventRecord(ev[0], st);
+    if (t.nt1) k_density_mixed<true><<<nbf, BS_FORCE, 0, st>>>(v, t.rho, sp);
+    else k_density_mixed<false><<<nbf, BS_FORCE, 0, st>>>(v, t.rho, sp);
+    if (ev) cudaEventRecord(ev[1], st);
+    k_embed_mixed<<<nbe, BS_VEC, 0, st>>>(v, t.embed, dff, pe);
+    k_ghost_dff<<<gblocks, BS_VEC, 0, st>>>(v, dff);
+    if (ev) cudaEventRecord(ev[2], st);
+    if (t.nt1) k_force_mixed<true, true><<<nbf, BS_FORCE, 0, st>>>(v, t.pair, t.rho, sp, dff, 0, pf);
+    else k_force_mixed<false, true><<<nbf, BS_FORCE, 0, st>>>(v, t.pair, t.rho, sp, dff, 0, pf);
+    if (ev) cudaEventRecord(ev[3], st);
+    launches += 4;
+  } else {
+    if (ev) {
+      cudaEventRecord(ev[0], st);
+      cudaEventRecord(ev[1], st);
+      cudaEventRecord(ev[2], st);
+    }
+    if (t.nt1) k_force_mixed<true, false><<<nbf, BS_FORCE, 0, st>>>(v, t.pair, t.rho, sp, dff, 0, pf);
+    else k_force_mixed<false, false><<<nbf, BS_FORCE, 0, st>>>(v, t.pair, t.rho, sp, dff, 0, pf);
+    if (ev) cudaEventRecord(ev[3], st);
+    launches += 1;
+  }
+  k_finalize_mixed<<<1, 32, 0, st>>>(pe, t.eam ? nbe : 0, pf, nbf, sc);
+  return launches + 1;
+}
+
+}  // namespace imdgpu

@@ -63,6 +63,11 @@ struct imdgpu_sys {
   DevTable dtab[3];
   double4 *dtri[3] = {nullptr, nullptr, nullptr};
   float4 *dtrif[3] = {nullptr, nullptr, nullptr};
+  double4 *dcv[3] = {nullptr, nullptr, nullptr};
+  double2 *dcg[3] = {nullptr, nullptr, nullptr};
+  float4 *dcvf[3] = {nullptr, nullptr, nullptr};
+  float2 *dcgf[3] = {nullptr, nullptr, nullptr};
+  int exact = 0;
   double tab_cellsz = 0.0;
 
   bool have_box = false;
@@ -73,6 +78,8 @@ struct imdgpu_sys {
   int gdim[3] = {0, 0, 0}, cdim[3] = {0, 0, 0};
   int nreal_cells = 0, nall_cells = 0, nbuf = 0;
   bool geom_ready = false;
+  bool geom_full = false;     // full list (mixed precision) instead of IMD's half list
+  float *dff = nullptr;
   int *d_cell_rank = nullptr, *d_rank_lin = nullptr, *d_hshell = nullptr;
   int *d_bsrc = nullptr, *d_blin = nullptr, *d_bcode = nullptr;
   int *d_cstart = nullptr, *d_ccount = nullptr;
@@ -344,7 +351,8 @@ __global__ void k_rb_ghost_fill(SysView v, DevScalars *sc, const int *gstart) {
 }
 
 // make_nblist (src/imd_forces_nbl.c:136-273): half shell of 14 cells,
-// in-cell partners after i, r^2 < cellsz.  Stores NBL_POS.
+// in-cell partners after i, r^2 < cellsz.  With nshell == 27 the full list
+// (every partner from both sides) for the mixed path.  Stores NBL_POS.
 __global__ void __launch_bounds__(128) k_rb_build_half(SysView v, DevScalars *sc,
                                                         const int *slot_rank) {
   if (!sc->rebuild) return;
@@ -353,15 +361,17 @@ __global__ void __launch_bounds__(128) k_rb_build_half(SysView v, DevScalars *sc
   const double4 pi = v.pos[i];
   v.ref[i] = pi;
   const int r = slot_rank[i];
-  const int *hs = v.hshell + 14 * r;
+  const int *hs = v.hshell + (size_t)v.nshell * r;
+  const bool full = (v.nshell == 27);
   int cnt = 0;
-  for (int m = 0; m < 14; m++) {
+  for (int m = 0; m < v.nshell; m++) {
     const int c2 = hs[m];
     if (c2 < 0) continue;
     const int s = v.cstart[c2];
     const int e = min(s + v.ccount[c2], v.n + v.gcap);  // ghost overflow: stay in bounds
-    const int j0 = (m == 0) ? i + 1 : s;
+    const int j0 = (m == 0 && !full) ? i + 1 : s;
     for (int j = j0; j < e; j++) {
+      if (full && j == i) continue;
       const double4 pj = v.pos[j];
       const double r2 = r2_exact(dsub(pj.x, pi.x), dsub(pj.y, pi.y), dsub(pj.z, pi.z));
       if (r2 < v.cellsz) {
@@ -741,6 +751,8 @@ static SysView view(imdgpu_sys *s) {
   v.cell_rank = s->d_cell_rank;
   v.rank_lin = s->d_rank_lin;
   v.hshell = s->d_hshell;
+  v.nshell = s->geom_full ? 27 : 14;
+  v.dff = s->dff;
   v.bsrc = s->d_bsrc;
   v.blin = s->d_blin;
   v.bcode = s->d_bcode;
@@ -757,6 +769,17 @@ static ForceTabs ftabs(imdgpu_sys *s) {
   t.rho = s->dtab[1];
   t.embed = s->dtab[2];
   t.eam = (s->interaction == IMDGPU_EAM2);
+  t.nt1 = (s->ntypes == 1);
+  t.exact = s->exact;
+  t.epot = 1;
+  int same = s->have_tab[0] && s->have_tab[1];
+  if (same) {
+    const HostTable &a = s->htab[0], &b = s->htab[1];
+    for (int c = 0; c < a.ncols && same; c++)
+      for (int d = 0; d < b.ncols && same; d++)
+        same = (a.begin[c] == b.begin[d] && a.end[c] == b.end[d] && a.invstep[c] == b.invstep[d]);
+  }
+  t.samegrid = same;
   return t;
 }
 
@@ -818,31 +841,41 @@ static int setup_geometry(imdgpu_sys *s) {
     rank_lin[r] = mort[r].second;
     cell_rank[mort[r].second] = r;
   }
-  // half shell (AR order, src/imd_geom_3d.c:895-899) with pbc exclusion
-  std::vector<int> hshell(14 * s->nreal_cells, -1);
+  // half shell (AR order, src/imd_geom_3d.c:895-899) with pbc exclusion, or
+  // for the full list all 27 neighbour cells (own cell first)
+  s->geom_full = (s->precision == IMDGPU_MIXED);
+  const int ns = s->geom_full ? 27 : 14;
+  std::vector<int> hshell((size_t)ns * s->nreal_cells, -1);
   std::vector<char> used(s->nall_cells, 0);
   for (int r = 0; r < s->nreal_cells; r++) {
     const int lin = rank_lin[r];
     const int i = lin / (cy * cz), j = (lin / cz) % cy, k = lin % cz;
-    int *nq = hshell.data() + 14 * r;
+    int *nq = hshell.data() + (size_t)ns * r;
     nq[0] = lin;
     int nn = 1;
-    for (int a = 0; a <= 1; a++)
-      for (int b = -a; b <= 1; b++)
-        for (int c = (a == 0 ? -b : -a); c <= 1; c++) {
-          const int ri = i + a, si = j + b, ti = k + c;
-          const int qq = (ri * cy + si) * cz + ti;
-          if (qq == lin) continue;
-          const int px = (ri - 1 < 0) ? -1 : (ri - 1 > gx - 1) ? 1 : 0;
-          const int py = (si - 1 < 0) ? -1 : (si - 1 > gy - 1) ? 1 : 0;
-          const int pz = (ti - 1 < 0) ? -1 : (ti - 1 > gz - 1) ? 1 : 0;
-          if ((s->pbc[0] == 1 || px == 0) && (s->pbc[1] == 1 || py == 0) &&
-              (s->pbc[2] == 1 || pz == 0)) {
-            nq[nn] = qq;
-            used[qq] = 1;
-          }
-          nn++;
-        }
+    auto add = [&](int a, int b, int c) {
+      const int ri = i + a, si = j + b, ti = k + c;
+      const int qq = (ri * cy + si) * cz + ti;
+      if (qq == lin) return;
+      const int px = (ri - 1 < 0) ? -1 : (ri - 1 > gx - 1) ? 1 : 0;
+      const int py = (si - 1 < 0) ? -1 : (si - 1 > gy - 1) ? 1 : 0;
+      const int pz = (ti - 1 < 0) ? -1 : (ti - 1 > gz - 1) ? 1 : 0;
+      if ((s->pbc[0] == 1 || px == 0) && (s->pbc[1] == 1 || py == 0) &&
+          (s->pbc[2] == 1 || pz == 0)) {
+        nq[nn] = qq;
+        used[qq] = 1;
+      }
+      nn++;
+    };
+    if (s->geom_full) {
+      for (int a = -1; a <= 1; a++)
+        for (int b = -1; b <= 1; b++)
+          for (int c = -1; c <= 1; c++) add(a, b, c);
+    } else {
+      for (int a = 0; a <= 1; a++)
+        for (int b = -a; b <= 1; b++)
+          for (int c = (a == 0 ? -b : -a); c <= 1; c++) add(a, b, c);
+    }
   }
   // buffer cells referenced by some half shell
   std::vector<int> bsrc, blin, bcode;
@@ -871,7 +904,7 @@ static int setup_geometry(imdgpu_sys *s) {
   dfree(s->d_gstart);
   CK(dalloc(&s->d_cell_rank, s->nall_cells));
   CK(dalloc(&s->d_rank_lin, s->nreal_cells));
-  CK(dalloc(&s->d_hshell, 14 * (size_t)s->nreal_cells));
+  CK(dalloc(&s->d_hshell, (size_t)ns * s->nreal_cells));
   CK(dalloc(&s->d_bsrc, s->nbuf));
   CK(dalloc(&s->d_blin, s->nbuf));
   CK(dalloc(&s->d_bcode, s->nbuf));
@@ -904,6 +937,8 @@ static int alloc_ext(imdgpu_sys *s, int gcap) {
   dfree(s->ecell);
   dfree(s->gowner);
   dfree(s->gcode);
+  dfree(s->dff);
+  CK(dalloc(&s->dff, ext));
   CK(dalloc(&s->pos, ext));
   CK(dalloc(&s->frc, ext));
   CK(dalloc(&s->rho, ext));
@@ -943,7 +978,7 @@ static void estimate_caps(imdgpu_sys *s, int &nbcap, int &gcap) {
   const double rl = std::sqrt(s->cellsz);
   const double dens = s->n / std::fabs(s->volume);
   const double full = 4.18879 * rl * rl * rl * dens;
-  nbcap = (int)(0.5 * full * 1.6) + 32;
+  nbcap = (int)((s->geom_full ? 1.0 : 0.5) * full * 1.6) + 32;
   const double frac = (double)(s->nall_cells - s->nreal_cells) / s->nreal_cells;
   gcap = (int)(s->n * frac * 1.25) + 1024;
 }
@@ -1118,6 +1153,10 @@ int imdgpu_destroy(imdgpu_sys *s) {
   for (int k = 0; k < 3; k++) {
     dfree(s->dtri[k]);
     dfree(s->dtrif[k]);
+    dfree(s->dcv[k]);
+    dfree(s->dcg[k]);
+    dfree(s->dcvf[k]);
+    dfree(s->dcgf[k]);
   }
   dfree(s->d_cell_rank); dfree(s->d_rank_lin); dfree(s->d_hshell); dfree(s->d_bsrc);
   dfree(s->d_blin); dfree(s->d_bcode); dfree(s->d_cstart); dfree(s->d_ccount);
@@ -1129,7 +1168,7 @@ int imdgpu_destroy(imdgpu_sys *s) {
   dfree(s->nnb); dfree(s->status); dfree(s->counters); dfree(s->partial); dfree(s->dsc);
   dfree(s->dnbl); dfree(s->hist); dfree(s->oldx); dfree(s->cgg); dfree(s->cgh);
   dfree(s->toldx); dfree(s->tcgg); dfree(s->tcgh);
-  dfree(s->slot_of); dfree(s->d_in); dfree(s->d_out); dfree(s->flushbuf);
+  dfree(s->slot_of); dfree(s->d_in); dfree(s->d_out); dfree(s->flushbuf); dfree(s->dff);
   for (auto e : s->sev) cudaEventDestroy(e);
   if (s->hsc) cudaFreeHost(s->hsc);
   if (s->ev_made)
@@ -1139,11 +1178,25 @@ int imdgpu_destroy(imdgpu_sys *s) {
   return IMDGPU_OK;
 }
 
+int imdgpu_set_exact(imdgpu_sys *s, int on) {
+  if (!s) return fail(IMDGPU_ERR_ARG, "null system");
+  s->exact = on ? 1 : 0;
+  return IMDGPU_OK;
+}
+
 int imdgpu_set_precision(imdgpu_sys *s, int precision) {
   if (!s) return fail(IMDGPU_ERR_ARG, "null system");
   if (precision != IMDGPU_FP64 && precision != IMDGPU_MIXED)
     return fail(IMDGPU_ERR_ARG, "precision must be IMDGPU_FP64 or IMDGPU_MIXED");
-  s->precision = precision;
+  if (precision != s->precision) {
+    s->precision = precision;
+    if (s->geom_ready) {
+      // the two paths use different lists (half vs full): rebuild on next use
+      s->geom_ready = false;
+      int one = 1;
+      CK(cudaMemcpy(&s->dsc->rebuild, &one, sizeof(int), cudaMemcpyHostToDevice));
+    }
+  }
   return IMDGPU_OK;
 }
 
@@ -1161,22 +1214,58 @@ static int upload_table(imdgpu_sys *s, int which, HostTable &t) {
       tri[(size_t)c * rows + k] = make_double4(at(k), at(k + 1), at(k + 2), 0.0);
       trif[(size_t)c * rows + k] = make_float4((float)at(k), (float)at(k + 1), (float)at(k + 2), 0.f);
     }
+  // coefficient form (see DevTable): A, B, C and G0, G1 per row
+  std::vector<double4> cv((size_t)t.ncols * rows);
+  std::vector<double2> cg((size_t)t.ncols * rows);
+  std::vector<float4> cvf((size_t)t.ncols * rows);
+  std::vector<float2> cgf((size_t)t.ncols * rows);
+  for (int c = 0; c < t.ncols; c++)
+    for (int k = 0; k < rows; k++) {
+      const double4 q = tri[(size_t)c * rows + k];
+      const double dv = q.y - q.x, d2v = q.z - 2.0 * q.y + q.x;
+      const double A = q.x, B = dv - 0.5 * d2v, C = 0.5 * d2v;
+      const double G0 = 2.0 * t.invstep[c] * B, G1 = 4.0 * t.invstep[c] * C;
+      cv[(size_t)c * rows + k] = make_double4(A, B, C, 0.0);
+      cg[(size_t)c * rows + k] = make_double2(G0, G1);
+      cvf[(size_t)c * rows + k] = make_float4((float)A, (float)B, (float)C, 0.f);
+      cgf[(size_t)c * rows + k] = make_float2((float)G0, (float)G1);
+    }
   dfree(s->dtri[which]);
   dfree(s->dtrif[which]);
+  dfree(s->dcv[which]);
+  dfree(s->dcg[which]);
+  dfree(s->dcvf[which]);
+  dfree(s->dcgf[which]);
   CK(dalloc(&s->dtri[which], tri.size()));
   CK(dalloc(&s->dtrif[which], trif.size()));
+  CK(dalloc(&s->dcv[which], cv.size()));
+  CK(dalloc(&s->dcg[which], cg.size()));
+  CK(dalloc(&s->dcvf[which], cvf.size()));
+  CK(dalloc(&s->dcgf[which], cgf.size()));
   CK(cudaMemcpy(s->dtri[which], tri.data(), tri.size() * sizeof(double4), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(s->dtrif[which], trif.data(), trif.size() * sizeof(float4), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(s->dcv[which], cv.data(), cv.size() * sizeof(double4), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(s->dcg[which], cg.data(), cg.size() * sizeof(double2), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(s->dcvf[which], cvf.data(), cvf.size() * sizeof(float4), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(s->dcgf[which], cgf.data(), cgf.size() * sizeof(float2), cudaMemcpyHostToDevice));
   DevTable &d = s->dtab[which];
   memset(&d, 0, sizeof d);
   d.ncols = t.ncols;
   d.rows = rows;
   d.tri = s->dtri[which];
   d.trif = s->dtrif[which];
+  d.cv = s->dcv[which];
+  d.cg = s->dcg[which];
+  d.cvf = s->dcvf[which];
+  d.cgf = s->dcgf[which];
   for (int c = 0; c < t.ncols; c++) {
     d.begin[c] = t.begin[c];
     d.end[c] = t.end[c];
     d.invstep[c] = t.invstep[c];
+    d.boff[c] = -t.begin[c] * t.invstep[c];
+    d.fbegin[c] = (float)t.begin[c];
+    d.fend[c] = (float)t.end[c];
+    d.finv[c] = (float)t.invstep[c];
   }
   s->htab[which] = t;
   s->have_tab[which] = true;
@@ -1426,8 +1515,10 @@ int imdgpu_move_atoms_nve(imdgpu_sys *s, double timestep) {
 constexpr int EV_PER_STEP = 8;
 constexpr int CHUNK = 25;
 
-static int issue_nve_steps(imdgpu_sys *s, int k, double dt, int *istep, long &launches) {
+static int issue_nve_steps(imdgpu_sys *s, int k, double dt, int *istep, long &launches,
+                           bool last_chunk) {
   SysView v = view(s);
+  ForceTabs ft = ftabs(s);
   const int nb = nblk(s->n, BS_VEC);
   const bool prof = s->profiling || s->l2flush_bytes > 0;
   for (int st = 0; st < k; st++) {
@@ -1437,7 +1528,8 @@ static int issue_nve_steps(imdgpu_sys *s, int k, double dt, int *istep, long &la
     if (rc) return rc;
     launches += 11 + (s->nbuf ? 1 : 0);
     if (e) cudaEventRecord(e[1], s->st);
-    launches += launch_forces(v, ftabs(s), s->dsc, s->precision == IMDGPU_MIXED, s->st,
+    ft.epot = (last_chunk && st == k - 1) ? 1 : 0;  // POTENG of the final step only
+    launches += launch_forces(v, ft, s->dsc, s->precision == IMDGPU_MIXED, s->st,
                               e ? e + 2 : nullptr);
     if (e) cudaEventRecord(e[6], s->st);
     k_nve<<<nb, BS_VEC, 0, s->st>>>(v, dt, s->partial);
@@ -1517,7 +1609,7 @@ int imdgpu_nve_run(imdgpu_sys *s, int nsteps, double dt, double *epot, double *e
     CK(cudaMemcpyAsync(borig, s->orig, sizeof(int) * s->n, cudaMemcpyDeviceToDevice, s->st));
     CK(cudaMemsetAsync(s->status, 0, sizeof(unsigned), s->st));
     long chunk_launches = 0;
-    rc = issue_nve_steps(s, k, dt, istep, chunk_launches);
+    rc = issue_nve_steps(s, k, dt, istep, chunk_launches, done + k == nsteps);
     if (rc) break;
     CK(cudaMemcpyAsync(&s->status_host, s->status, sizeof(unsigned), cudaMemcpyDeviceToHost, s->st));
     CK(cudaStreamSynchronize(s->st));

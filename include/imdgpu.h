@@ -73,6 +73,10 @@ int imdgpu_set_device(int device);
 /* Replaces IMD's implicit single global system (src/globals.h). */
 int imdgpu_create(imdgpu_sys **sys, int ntypes, int interaction, int precision);
 int imdgpu_destroy(imdgpu_sys *sys);
+/* 1: evaluate tables with IMD's own unfused formulas (bitwise table values,
+ * parity mode); 0 (default): coefficient form with FMA, same results to
+ * ~1e-16 relative */
+int imdgpu_set_exact(imdgpu_sys *sys, int on);
 /* precision may be switched between calls (the list is kept) */
 int imdgpu_set_precision(imdgpu_sys *sys, int precision);
 

@@ -183,3 +183,67 @@ def test_bad_inputs_are_errors():
         s.calc_forces(0)
     with pytest.raises(api.IMDGPUError):
         s.set_atoms(g["number"][:10], g["type"][:10] + 3, g["mass"][:10], g["x"][:10])
+
+
+@pytest.mark.parametrize("name", ["cu_pert", "alloy_pert", "lj_pert"])
+def test_exact_mode_matches_reference(name):
+    """IMD's unfused table arithmetic (parity mode) also meets the bars."""
+    g = golden(name)
+    tab, eam, nt, skin = CASES[name]
+    s = gpu_system(g, tab, eam, nt, skin)
+    s.set_exact(True)
+    s.calc_forces(0)
+    a = s.get_atoms()
+    assert rel_rms(a["f"], g["f"]) < 1e-11
+    assert abs(s.scalars().tot_pot_energy - g["epot_total"]) <= 1e-12 * abs(g["epot_total"])
+
+
+@pytest.mark.parametrize("name", ["cu_pert", "alloy_pert", "lj_pert", "tri_cg"])
+def test_mixed_precision_force_error(name):
+    """FP32 pair/EAM arithmetic, FP64 accumulation: force RMS error within
+    1e-5 of the FP64 reference, energy within 1e-6 relative."""
+    from imd_gb300 import api
+    g = golden(name)
+    tab, eam, nt, skin = CASES[name]
+    s = gpu_system(g, tab, eam, nt, skin, precision=api.MIXED)
+    s.calc_forces(0)
+    a = s.get_atoms()
+    err = rel_rms(a["f"], g["f"])
+    assert err < 1e-5, err
+    de = abs(s.scalars().tot_pot_energy - g["epot_total"]) / abs(g["epot_total"])
+    assert de < 1e-6, de
+    np.testing.assert_allclose(a["epot"], g["epot"], rtol=0, atol=1e-5 * np.max(np.abs(g["epot"])))
+
+
+def test_mixed_nve_conserves_energy():
+    from imd_gb300 import api
+    g = golden("cu_nve")
+    gg = dict(g)
+    gg["x"] = g["x0"]
+    s = gpu_system(gg, "cu", 1, 1, 0.4, p=g["p0"], precision=api.MIXED)
+    ep, ek = s.nve_run(len(g["epot"]), float(g["dt"]))
+    et = ep + ek
+    n = len(g["x0"])
+    # same trajectory as the reference to the FP32 force error, and the total
+    # energy fluctuates like the FP64 run's
+    np.testing.assert_allclose(ep, g["epot"], rtol=1e-6)
+    ref = g["epot"] + g["ekin"]
+    assert np.max(np.abs(et - et[0])) / n < 2 * np.max(np.abs(ref - ref[0])) / n + 1e-7
+
+
+def test_precision_switch_keeps_state():
+    """Switching FP64 -> mixed -> FP64 rebuilds the matching list and gives
+    the FP64 forces again."""
+    from imd_gb300 import api
+    g = golden("cu_pert")
+    s = gpu_system(g, "cu", 1, 1, 0.4)
+    s.calc_forces(0)
+    f0 = s.get_atoms()["f"]
+    s.set_precision(api.MIXED)
+    s.calc_forces(0)
+    f1 = s.get_atoms()["f"]
+    s.set_precision(api.FP64)
+    s.calc_forces(0)
+    f2 = s.get_atoms()["f"]
+    assert rel_rms(f1, f0) < 1e-5
+    assert rel_rms(f2, f0) < 1e-13
