@@ -64,6 +64,7 @@ def lib() -> C.CDLL:
         L.imdgpu_destroy.argtypes = [vp]
         L.imdgpu_set_precision.argtypes = [vp, C.c_int]
         L.imdgpu_set_exact.argtypes = [vp, C.c_int]
+        L.imdgpu_set_graphs.argtypes = [vp, C.c_int]
         L.imdgpu_set_table.argtypes = [vp, C.c_int, C.c_int, C.c_int, _dp, _dp, _dp, _dp,
                                        _ip, _dp]
         L.imdgpu_read_table.argtypes = [vp, C.c_int, C.c_char_p, C.c_int, C.c_int]
@@ -182,6 +183,10 @@ class GpuSystem:
 
     def set_profiling(self, on: bool) -> None:
         _check(lib().imdgpu_set_profiling(self.h, int(on)), "set_profiling")
+
+    def set_graphs(self, on: bool) -> None:
+        """Replay NVE chunks from a captured CUDA graph (default on)."""
+        _check(lib().imdgpu_set_graphs(self.h, int(on)), "set_graphs")
 
     def set_exact(self, on: bool) -> None:
         """IMD's unfused table arithmetic (bitwise table values) on/off."""

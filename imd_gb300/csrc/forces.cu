@@ -255,7 +255,8 @@ __global__ void __launch_bounds__(BS_FORCE) k_force_fast(SysView v, DevTable pai
     const int nn = v.nnb[i];
     const double dfi = EAM ? v.df[i] : 0.0;
     bool shortf = false;
-    double ffx = 0.0, ffy = 0.0, ffz = 0.0, ee = 0.0, esum = 0.0, vir = 0.0;
+    // ng* = minus the gradient: the partner's force d * ng is used as is
+    double fnx = 0.0, fny = 0.0, fnz = 0.0, ee = 0.0, esum = 0.0, vir = 0.0;
     const uint32_t *__restrict__ nb = v.nbr + i;
 #pragma unroll 2
     for (int k = 0; k < nn; k++) {
@@ -265,16 +266,14 @@ __global__ void __launch_bounds__(BS_FORCE) k_force_fast(SysView v, DevTable pai
       const double r2 = fma(dx, dx, fma(dy, dy, dz * dz));
       const int jt = NT1 ? 0 : (int)pj.w;
       const int col = NT1 ? 0 : it * nt + jt;
-      double grad = 0.0, ehalf = 0.0;
+      double ngrad = 0.0, ehalf = 0.0;
       bool have = false;
       int kk = 0;
       double chi = 0.0;
       if (le_pos(r2, pair.end[col])) {
         kk = tab_index_fast(pair, col, r2, chi);
-        const double4 c = cv_load(pair, col, kk);
-        const double2 g = cg_load(pair, col, kk);
-        const double pot = poly_v(c, chi);
-        grad = poly_g(g, chi);
+        const double pot = poly_v(cv_load(pair, col, kk), chi);
+        ngrad = poly_g(cgn_load(pair, col, kk), chi);
         esum += pot;
         if (EPOT) {
           ehalf = 0.5 * pot;
@@ -289,39 +288,38 @@ __global__ void __launch_bounds__(BS_FORCE) k_force_fast(SysView v, DevTable pai
           double chi1 = chi;
           int k1 = kk;
           if (!(SAMEGRID && have)) k1 = tab_index_fast(rho, col1, r2, chi1);
-          const double ris = poly_g(cg_load(rho, col1, k1), chi1);
+          // rho.cgn holds -rho'/2
+          const double nris = poly_g(cgn_load(rho, col1, k1), chi1);
           const double dfj = __ldg(&v.df[j]);
-          double ge;
           if (NT1 || col1 == col2) {
-            ge = ris * (0.5 * (dfi + dfj));
+            ngrad = fma(nris, dfi + dfj, ngrad);
           } else {
             double chi2 = chi;
             int k2 = kk;
             if (!(SAMEGRID && have)) k2 = tab_index_fast(rho, col2, r2, chi2);
-            const double rjs = poly_g(cg_load(rho, col2, k2), chi2);
-            ge = 0.5 * (dfi * rjs + dfj * ris);
+            const double nrjs = poly_g(cgn_load(rho, col2, k2), chi2);
+            ngrad = fma(dfi, nrjs, fma(dfj, nris, ngrad));
           }
-          grad += ge;
           have = true;
         }
       }
       if (have) {
-        const double fx = dx * grad, fy = dy * grad, fz = dz * grad;
+        const double fx = dx * ngrad, fy = dy * ngrad, fz = dz * ngrad;
         double *fj = &v.frc[j].x;
-        atomicAdd(fj + 0, -fx);
-        atomicAdd(fj + 1, -fy);
-        atomicAdd(fj + 2, -fz);
+        atomicAdd(fj + 0, fx);
+        atomicAdd(fj + 1, fy);
+        atomicAdd(fj + 2, fz);
         if (EPOT) atomicAdd(fj + 3, ehalf);
-        ffx += fx;
-        ffy += fy;
-        ffz += fz;
-        vir = fma(-r2, grad, vir);
+        fnx += fx;
+        fny += fy;
+        fnz += fz;
+        vir = fma(r2, ngrad, vir);
       }
     }
     double *fi = &v.frc[i].x;
-    atomicAdd(fi + 0, ffx);
-    atomicAdd(fi + 1, ffy);
-    atomicAdd(fi + 2, ffz);
+    atomicAdd(fi + 0, -fnx);
+    atomicAdd(fi + 1, -fny);
+    atomicAdd(fi + 2, -fnz);
     if (EPOT) atomicAdd(fi + 3, ee);
     acc[0] = esum;
     acc[1] = vir;

@@ -48,6 +48,9 @@ struct DevTable {
   const float4 *trif;       // same in FP32 (mixed precision)
   const double4 *cv;        // (A, B, C, 0) per column and row
   const double2 *cg;        // (G0, G1)
+  const double2 *cgn;       // (-s G0, -s G1): negated gradient for the force pass
+                            // (s = 1 for pair tables, 1/2 for rho: the EAM
+                            // force term 0.5 (F'_i + F'_j) rho' needs rho'/2)
   const float4 *cvf;        // FP32 copies for the mixed path
   const float2 *cgf;
   double begin[MAXCOL];
@@ -192,12 +195,30 @@ __device__ __forceinline__ bool lt_pos(double a, double b) {
   return __double_as_longlong(a) < __double_as_longlong(b);
 }
 
+// floor(x) for 0 <= x < 2^21 from the bits of x (integer pipe only)
+__device__ __forceinline__ int ifloor_pos(double x) {
+  const int hi = __double2hiint(x);
+  const int e = (hi >> 20) - 1023;                 // unbiased exponent, < 0 for x < 1
+  const int m = (hi & 0xFFFFF) | 0x100000;         // top 21 bits of the significand
+  return m >> min(20 - e, 31);
+}
+// (double)k for 0 <= k < 2^21, assembled from bits (exact)
+__device__ __forceinline__ double small_int_to_double(int k) {
+  const int p = 31 - __clz(k | 1);
+  const int hi = ((1023 + p) << 20) | ((k << (20 - p)) & 0xFFFFF);
+  return k ? __hiloint2double(hi, 0) : 0.0;
+}
+
+// Table index of the fast path: r2a = (min(r2, end) - begin) * invstep as one
+// FMA; clamps, floor and int->double on the integer pipe, so only the FMA
+// and the final subtraction use the (slow) FP64 pipe.  chi = r2a - k is
+// exact.  Tables have fewer than 2^20 rows (checked at upload).
 __device__ __forceinline__ int tab_index_fast(const DevTable &t, int col, double r2, double &chi) {
-  const double rm = fmin(r2, t.end[col]);
+  const double rm = lt_pos(r2, t.end[col]) ? r2 : t.end[col];
   double r2a = fma(rm, t.invstep[col], t.boff[col]);
-  r2a = fmax(r2a, 0.0);
-  const int k = __double2int_rz(r2a);
-  chi = r2a - (double)k;
+  if (__double2hiint(r2a) < 0) r2a = 0.0;          // below begin (short distance)
+  const int k = ifloor_pos(r2a);
+  chi = r2a - small_int_to_double(k);
   return k;
 }
 __device__ __forceinline__ double4 cv_load(const DevTable &t, int col, int k) {
@@ -210,6 +231,35 @@ __device__ __forceinline__ double poly_v(const double4 c, double chi) {
   return fma(chi, fma(chi, c.z, c.y), c.x);
 }
 __device__ __forceinline__ double poly_g(const double2 g, double chi) { return fma(chi, g.y, g.x); }
+__device__ __forceinline__ double2 cgn_load(const DevTable &t, int col, int k) {
+  return __ldg(&t.cgn[(size_t)col * t.rows + k]);
+}
+
+// Per-atom FP32 split of an FP64 position: x = hi + lo to ~2^-48 relative.
+// The difference of two atoms, (hi_j - hi_i) + (lo_j - lo_i), is accurate to
+// the last FP32 bit of the difference itself.
+struct __align__(16) SplitPos {
+  float4 hi;  // x, y, z, type (int bits)
+  float4 lo;  // residuals
+};
+__device__ __forceinline__ SplitPos split_pos(const double4 p) {
+  SplitPos o;
+  o.hi.x = (float)p.x;
+  o.hi.y = (float)p.y;
+  o.hi.z = (float)p.z;
+  o.hi.w = __int_as_float((int)p.w);
+  o.lo.x = (float)(p.x - (double)o.hi.x);
+  o.lo.y = (float)(p.y - (double)o.hi.y);
+  o.lo.z = (float)(p.z - (double)o.hi.z);
+  o.lo.w = 0.f;
+  return o;
+}
+__device__ __forceinline__ SplitPos ldsp(const SplitPos *p) {
+  SplitPos o;
+  o.hi = __ldg(&p->hi);
+  o.lo = __ldg(&p->lo);
+  return o;
+}
 
 // A ghost copies its owner through the z, y, x buffer copies of send_cells
 // (src/imd_comm_force_3d.c:247-358) in that order, so its position is

@@ -19,11 +19,6 @@
 
 namespace imdgpu {
 
-struct __align__(16) SplitPos {
-  float4 hi;  // x, y, z, type (int bits)
-  float4 lo;  // residuals
-};
-
 // error-free accumulation: s + c carries the exact running sum to ~2^-48
 struct Acc {
   float s, c;
@@ -39,26 +34,8 @@ struct Acc {
 
 __global__ void k_split(SysView v, SplitPos *sp) {
   const int ne = v.n + v.counters[0];
-  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < ne; e += gridDim.x * blockDim.x) {
-    const double4 p = v.pos[e];
-    SplitPos o;
-    o.hi.x = (float)p.x;
-    o.hi.y = (float)p.y;
-    o.hi.z = (float)p.z;
-    o.hi.w = __int_as_float((int)p.w);
-    o.lo.x = (float)(p.x - (double)o.hi.x);
-    o.lo.y = (float)(p.y - (double)o.hi.y);
-    o.lo.z = (float)(p.z - (double)o.hi.z);
-    o.lo.w = 0.f;
-    sp[e] = o;
-  }
-}
-
-__device__ __forceinline__ SplitPos ldsp(const SplitPos *p) {
-  SplitPos o;
-  o.hi = __ldg(&p->hi);
-  o.lo = __ldg(&p->lo);
-  return o;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < ne; e += gridDim.x * blockDim.x)
+    sp[e] = split_pos(v.pos[e]);
 }
 
 __device__ __forceinline__ int tab_index_f(const DevTable &t, int col, float r2, float &chi) {

@@ -65,6 +65,7 @@ struct imdgpu_sys {
   float4 *dtrif[3] = {nullptr, nullptr, nullptr};
   double4 *dcv[3] = {nullptr, nullptr, nullptr};
   double2 *dcg[3] = {nullptr, nullptr, nullptr};
+  double2 *dcgn[3] = {nullptr, nullptr, nullptr};
   float4 *dcvf[3] = {nullptr, nullptr, nullptr};
   float2 *dcgf[3] = {nullptr, nullptr, nullptr};
   int exact = 0;
@@ -118,6 +119,12 @@ struct imdgpu_sys {
   long l2flush_bytes = 0;
   char *flushbuf = nullptr;
   std::vector<cudaEvent_t> sev;    // per-step event pool of nve_run
+
+  // CUDA graph of one full chunk of NVE steps, re-captured when buffers move
+  cudaGraphExec_t gexec = nullptr;
+  std::vector<uintptr_t> gkey;
+  int use_graph = 1;
+  long graph_launches = 0;
 
   long nfc = 0, nbl_count_host = 0;
   bool atoms_set = false;
@@ -350,6 +357,14 @@ __global__ void k_rb_ghost_fill(SysView v, DevScalars *sc, const int *gstart) {
   }
 }
 
+__global__ void k_rb_split(SysView v, DevScalars *sc) {
+  if (!sc->rebuild) return;
+  SplitPos *sp = reinterpret_cast<SplitPos *>(v.xl);
+  const int ne = v.n + v.counters[0];
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < ne; e += gridDim.x * blockDim.x)
+    sp[e] = split_pos(v.pos[e]);
+}
+
 // make_nblist (src/imd_forces_nbl.c:136-273): half shell of 14 cells,
 // in-cell partners after i, r^2 < cellsz.  With nshell == 27 the full list
 // (every partner from both sides) for the mixed path.  Stores NBL_POS.
@@ -363,6 +378,11 @@ __global__ void __launch_bounds__(128) k_rb_build_half(SysView v, DevScalars *sc
   const int r = slot_rank[i];
   const int *hs = v.hshell + (size_t)v.nshell * r;
   const bool full = (v.nshell == 27);
+  const SplitPos *sp = reinterpret_cast<const SplitPos *>(v.xl);
+  const SplitPos a = sp[i];
+  // FP32 distance decides all pairs outside a +-1e-5 band around the list
+  // radius; inside the band the exact FP64 r^2 of the reference decides
+  const float lo2 = (float)(v.cellsz * (1.0 - 1e-5)), hi2 = (float)(v.cellsz * (1.0 + 1e-5));
   int cnt = 0;
   for (int m = 0; m < v.nshell; m++) {
     const int c2 = hs[m];
@@ -372,9 +392,17 @@ __global__ void __launch_bounds__(128) k_rb_build_half(SysView v, DevScalars *sc
     const int j0 = (m == 0 && !full) ? i + 1 : s;
     for (int j = j0; j < e; j++) {
       if (full && j == i) continue;
-      const double4 pj = v.pos[j];
-      const double r2 = r2_exact(dsub(pj.x, pi.x), dsub(pj.y, pi.y), dsub(pj.z, pi.z));
-      if (r2 < v.cellsz) {
+      const SplitPos b = ldsp(&sp[j]);
+      const float dx = (b.hi.x - a.hi.x) + (b.lo.x - a.lo.x);
+      const float dy = (b.hi.y - a.hi.y) + (b.lo.y - a.lo.y);
+      const float dz = (b.hi.z - a.hi.z) + (b.lo.z - a.lo.z);
+      const float r2f = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+      bool in = r2f < lo2;
+      if (!in && r2f <= hi2) {
+        const double4 pj = v.pos[j];
+        in = r2_exact(dsub(pj.x, pi.x), dsub(pj.y, pi.y), dsub(pj.z, pi.z)) < v.cellsz;
+      }
+      if (in) {
         if (cnt < v.nbcap) v.nbr[(size_t)cnt * v.ncap + i] = (uint32_t)j | ((uint32_t)m << NB_SHIFT);
         cnt++;
       }
@@ -1004,6 +1032,7 @@ static int issue_rebuild(imdgpu_sys *s) {
                                        s->toldx, s->tcgg, s->tcgh, s->slot_of);
   k_rb_ghost_scan<<<1, 1024, 0, st>>>(v, sc, s->d_gstart);
   if (s->nbuf) k_rb_ghost_fill<<<s->nbuf, 64, 0, st>>>(v, sc, s->d_gstart);
+  k_rb_split<<<std::max(1, nblk((long)s->n + s->gcap, BS_VEC)), BS_VEC, 0, st>>>(v, sc);
   k_rb_build_half<<<nblk(s->n, 128), 128, 0, st>>>(v, sc, s->slot_rank);
   k_rb_done<<<1, 1, 0, st>>>(sc, s->dnbl);
   CK(cudaGetLastError());
@@ -1155,6 +1184,7 @@ int imdgpu_destroy(imdgpu_sys *s) {
     dfree(s->dtrif[k]);
     dfree(s->dcv[k]);
     dfree(s->dcg[k]);
+    dfree(s->dcgn[k]);
     dfree(s->dcvf[k]);
     dfree(s->dcgf[k]);
   }
@@ -1170,6 +1200,7 @@ int imdgpu_destroy(imdgpu_sys *s) {
   dfree(s->toldx); dfree(s->tcgg); dfree(s->tcgh);
   dfree(s->slot_of); dfree(s->d_in); dfree(s->d_out); dfree(s->flushbuf); dfree(s->dff);
   for (auto e : s->sev) cudaEventDestroy(e);
+  if (s->gexec) cudaGraphExecDestroy(s->gexec);
   if (s->hsc) cudaFreeHost(s->hsc);
   if (s->ev_made)
     for (int k = 0; k < 8; k++) cudaEventDestroy(s->ev[k]);
@@ -1217,6 +1248,10 @@ static int upload_table(imdgpu_sys *s, int which, HostTable &t) {
   // coefficient form (see DevTable): A, B, C and G0, G1 per row
   std::vector<double4> cv((size_t)t.ncols * rows);
   std::vector<double2> cg((size_t)t.ncols * rows);
+  std::vector<double2> cgn((size_t)t.ncols * rows);
+  const double gscale = (which == IMDGPU_TAB_RHO) ? -0.5 : -1.0;
+  if (t.maxsteps + 2 >= (1 << 20))
+    return fail(IMDGPU_ERR_TABLE, "tables with 2^20 or more rows are not supported");
   std::vector<float4> cvf((size_t)t.ncols * rows);
   std::vector<float2> cgf((size_t)t.ncols * rows);
   for (int c = 0; c < t.ncols; c++)
@@ -1227,6 +1262,7 @@ static int upload_table(imdgpu_sys *s, int which, HostTable &t) {
       const double G0 = 2.0 * t.invstep[c] * B, G1 = 4.0 * t.invstep[c] * C;
       cv[(size_t)c * rows + k] = make_double4(A, B, C, 0.0);
       cg[(size_t)c * rows + k] = make_double2(G0, G1);
+      cgn[(size_t)c * rows + k] = make_double2(gscale * G0, gscale * G1);
       cvf[(size_t)c * rows + k] = make_float4((float)A, (float)B, (float)C, 0.f);
       cgf[(size_t)c * rows + k] = make_float2((float)G0, (float)G1);
     }
@@ -1234,18 +1270,21 @@ static int upload_table(imdgpu_sys *s, int which, HostTable &t) {
   dfree(s->dtrif[which]);
   dfree(s->dcv[which]);
   dfree(s->dcg[which]);
+  dfree(s->dcgn[which]);
   dfree(s->dcvf[which]);
   dfree(s->dcgf[which]);
   CK(dalloc(&s->dtri[which], tri.size()));
   CK(dalloc(&s->dtrif[which], trif.size()));
   CK(dalloc(&s->dcv[which], cv.size()));
   CK(dalloc(&s->dcg[which], cg.size()));
+  CK(dalloc(&s->dcgn[which], cgn.size()));
   CK(dalloc(&s->dcvf[which], cvf.size()));
   CK(dalloc(&s->dcgf[which], cgf.size()));
   CK(cudaMemcpy(s->dtri[which], tri.data(), tri.size() * sizeof(double4), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(s->dtrif[which], trif.data(), trif.size() * sizeof(float4), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(s->dcv[which], cv.data(), cv.size() * sizeof(double4), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(s->dcg[which], cg.data(), cg.size() * sizeof(double2), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(s->dcgn[which], cgn.data(), cgn.size() * sizeof(double2), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(s->dcvf[which], cvf.data(), cvf.size() * sizeof(float4), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(s->dcgf[which], cgf.data(), cgf.size() * sizeof(float2), cudaMemcpyHostToDevice));
   DevTable &d = s->dtab[which];
@@ -1256,6 +1295,7 @@ static int upload_table(imdgpu_sys *s, int which, HostTable &t) {
   d.trif = s->dtrif[which];
   d.cv = s->dcv[which];
   d.cg = s->dcg[which];
+  d.cgn = s->dcgn[which];
   d.cvf = s->dcvf[which];
   d.cgf = s->dcgf[which];
   for (int c = 0; c < t.ncols; c++) {
@@ -1526,7 +1566,7 @@ static int issue_nve_steps(imdgpu_sys *s, int k, double dt, int *istep, long &la
     if (e) cudaEventRecord(e[0], s->st);
     int rc = issue_rebuild(s);
     if (rc) return rc;
-    launches += 11 + (s->nbuf ? 1 : 0);
+    launches += 12 + (s->nbuf ? 1 : 0);
     if (e) cudaEventRecord(e[1], s->st);
     ft.epot = (last_chunk && st == k - 1) ? 1 : 0;  // POTENG of the final step only
     launches += launch_forces(v, ft, s->dsc, s->precision == IMDGPU_MIXED, s->st,
@@ -1558,6 +1598,50 @@ static void accumulate_events(imdgpu_sys *s, int k) {
     s->timing.ms_force += f;
     s->timing.ms_integrate += in;
   }
+}
+
+// key of everything a captured chunk bakes in
+static std::vector<uintptr_t> graph_key(imdgpu_sys *s, double dt) {
+  double dtv = dt;
+  uintptr_t dtb;
+  memcpy(&dtb, &dtv, sizeof dtb);
+  return {(uintptr_t)s->pos, (uintptr_t)s->mom, (uintptr_t)s->frc, (uintptr_t)s->nbr,
+          (uintptr_t)s->xl, (uintptr_t)s->hist, (uintptr_t)s->flushbuf, (uintptr_t)s->oldx,
+          (uintptr_t)s->ncap, (uintptr_t)s->gcap, (uintptr_t)s->nbcap,
+          (uintptr_t)s->precision, (uintptr_t)s->exact, (uintptr_t)s->profiling,
+          (uintptr_t)s->l2flush_bytes, (uintptr_t)s->geom_full, (uintptr_t)s->nbuf, dtb};
+}
+
+// one full chunk (not the last) through a captured graph
+static int run_chunk_graph(imdgpu_sys *s, int k, double dt, int *istep, long &launches) {
+  auto key = graph_key(s, dt);
+  if (!s->gexec || key != s->gkey) {
+    if (s->gexec) {
+      cudaGraphExecDestroy(s->gexec);
+      s->gexec = nullptr;
+    }
+    cudaGraph_t g;
+    CK(cudaStreamBeginCapture(s->st, cudaStreamCaptureModeThreadLocal));
+    long l = 0;
+    int rc = issue_nve_steps(s, k, dt, istep, l, false);
+    cudaError_t e = cudaStreamEndCapture(s->st, &g);
+    if (rc) return rc;
+    if (e != cudaSuccess) return fail(IMDGPU_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+    e = cudaGraphInstantiate(&s->gexec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return fail(IMDGPU_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+    s->gkey = key;
+    s->graph_launches = l;
+  }
+  CK(cudaGraphLaunch(s->gexec, s->st));
+  launches += s->graph_launches;
+  return IMDGPU_OK;
+}
+
+int imdgpu_set_graphs(imdgpu_sys *s, int on) {
+  if (!s) return fail(IMDGPU_ERR_ARG, "null");
+  s->use_graph = on ? 1 : 0;
+  return IMDGPU_OK;
 }
 
 int imdgpu_nve_run(imdgpu_sys *s, int nsteps, double dt, double *epot, double *ekin) {
@@ -1609,7 +1693,13 @@ int imdgpu_nve_run(imdgpu_sys *s, int nsteps, double dt, double *epot, double *e
     CK(cudaMemcpyAsync(borig, s->orig, sizeof(int) * s->n, cudaMemcpyDeviceToDevice, s->st));
     CK(cudaMemsetAsync(s->status, 0, sizeof(unsigned), s->st));
     long chunk_launches = 0;
-    rc = issue_nve_steps(s, k, dt, istep, chunk_launches, done + k == nsteps);
+    const bool last = (done + k == nsteps);
+    // per-step event windows (profiling / L2 flush) are issued directly:
+    // timing events are not captured into the graph
+    if (s->use_graph && !prof && !last && k == CHUNK)
+      rc = run_chunk_graph(s, k, dt, istep, chunk_launches);
+    else
+      rc = issue_nve_steps(s, k, dt, istep, chunk_launches, last);
     if (rc) break;
     CK(cudaMemcpyAsync(&s->status_host, s->status, sizeof(unsigned), cudaMemcpyDeviceToHost, s->st));
     CK(cudaStreamSynchronize(s->st));

@@ -171,6 +171,9 @@ int imdgpu_set_profiling(imdgpu_sys *sys, int on);
  * step starts with a cold L2 (benchmarking); the write is outside the timed
  * windows.  0 disables. */
 int imdgpu_set_l2_flush(imdgpu_sys *sys, long bytes);
+/* nve_run replays each full chunk of 25 steps from a captured CUDA graph
+ * (default 1); 0 issues every launch from the host. */
+int imdgpu_set_graphs(imdgpu_sys *sys, int on);
 /* Measured FP64 FMA throughput of this device (TFLOP/s): a roofline
  * denominator for the FP64 force kernels. */
 int imdgpu_probe_fp64_peak(double *tflops);

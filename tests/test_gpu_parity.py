@@ -247,3 +247,21 @@ def test_precision_switch_keeps_state():
     f2 = s.get_atoms()["f"]
     assert rel_rms(f1, f0) < 1e-5
     assert rel_rms(f2, f0) < 1e-13
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_graph_replay_matches_direct_launches(precision):
+    """nve_run with chunks replayed from a captured CUDA graph follows the
+    same trajectory as with every launch issued from the host."""
+    g = golden("cu_nve")
+    gg = dict(g)
+    gg["x"] = g["x0"]
+    a = gpu_system(gg, "cu", 1, 1, 0.4, p=g["p0"], precision=precision)
+    b = gpu_system(gg, "cu", 1, 1, 0.4, p=g["p0"], precision=precision)
+    b.set_graphs(False)
+    dt = float(g["dt"])
+    ea, ka = a.nve_run(80, dt)
+    eb, kb = b.nve_run(80, dt)
+    np.testing.assert_allclose(ea, eb, rtol=1e-10)
+    np.testing.assert_allclose(ka, kb, rtol=1e-9)
+    assert a.scalars().nbl_count == b.scalars().nbl_count
