@@ -18,6 +18,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIBPATH = os.path.join(HERE, "libimdgpu.so")
 
 PAIR, EAM2 = 0, 1
+QUADRATIC, FOURPOINT, SPLINE = 0, 1, 2
 FP64, MIXED = 0, 1
 TAB_PAIR, TAB_RHO, TAB_EMBED = 0, 1, 2
 WARN_SHORT = 1
@@ -65,6 +66,8 @@ def lib() -> C.CDLL:
         L.imdgpu_set_precision.argtypes = [vp, C.c_int]
         L.imdgpu_set_exact.argtypes = [vp, C.c_int]
         L.imdgpu_set_graphs.argtypes = [vp, C.c_int]
+        L.imdgpu_set_interpolation.argtypes = [vp, C.c_int]
+        L.imdgpu_set_table2.argtypes = [vp, C.c_int, C.c_int, C.c_int, _dp]
         L.imdgpu_set_table.argtypes = [vp, C.c_int, C.c_int, C.c_int, _dp, _dp, _dp, _dp,
                                        _ip, _dp]
         L.imdgpu_read_table.argtypes = [vp, C.c_int, C.c_char_p, C.c_int, C.c_int]
@@ -94,6 +97,19 @@ def lib() -> C.CDLL:
         L.imdgpu_set_l2_flush.argtypes = [vp, C.c_long]
         L.imdgpu_probe_fp64_peak.argtypes = [_dp]
         L.imdgpu_set_device.argtypes = [C.c_int]
+        L.imdgpu_batch_set_cells.argtypes = [vp, C.c_int, _ip, _dp, _ip, _ip, _dp, _dp]
+        L.imdgpu_batch_set_margin.argtypes = [vp, C.c_double]
+        L.imdgpu_batch_relax.argtypes = [vp, C.c_double, C.c_int, C.c_int, _ip]
+        L.imdgpu_batch_results.argtypes = [vp, _dp, _dp, _ip, _ip, _ip]
+        L.imdgpu_batch_begin.argtypes = [vp, C.c_double, C.c_int]
+        L.imdgpu_batch_advance.argtypes = [vp, C.c_int, _ip, _ip]
+        L.imdgpu_batch_rebuilds.argtypes = [vp, C.POINTER(C.c_long)]
+        fp = C.POINTER(C.c_float)
+        L.imdgpu_ml_nparam.argtypes = []
+        L.imdgpu_ml_set_weights.argtypes = [vp, fp, C.c_int]
+        L.imdgpu_ml_get_weights.argtypes = [vp, fp, C.c_int]
+        L.imdgpu_ml_predict.argtypes = [vp, _dp]
+        L.imdgpu_ml_train_step.argtypes = [vp, _dp, C.c_double, _dp, fp]
         _lib = L
     return _lib
 
@@ -120,10 +136,12 @@ class GpuSystem:
     arrays; the box, periodicity and list margin as IMD's parameters
     box_x/y/z, pbc_dirs and nbl_margin."""
 
-    def __init__(self, ntypes: int = 1, interaction: int = EAM2, precision: int = FP64):
+    def __init__(self, ntypes: int = 1, interaction: int = EAM2, precision: int = FP64,
+                 interpolation: int = QUADRATIC):
         h = C.c_void_p()
         _check(lib().imdgpu_create(C.byref(h), ntypes, interaction, precision), "imdgpu_create")
         self.h = h
+        _check(lib().imdgpu_set_interpolation(h, interpolation), "set_interpolation")
         self.ntypes = ntypes
         self.interaction = interaction
         self.n = 0
@@ -277,6 +295,32 @@ class GpuSystem:
                                       _p(sh, C.c_int), _p(r2), C.byref(cnt)), "get_pairs")
         return ni, nj, sh, r2
 
+    # --- learned start ---------------------------------------------------------
+    def ml_set_weights(self, w) -> None:
+        w = np.ascontiguousarray(w, np.float32)
+        _check(lib().imdgpu_ml_set_weights(self.h, _p(w, C.c_float), len(w)), "ml_set_weights")
+
+    def ml_get_weights(self):
+        w = np.empty(lib().imdgpu_ml_nparam(), np.float32)
+        _check(lib().imdgpu_ml_get_weights(self.h, _p(w, C.c_float), len(w)), "ml_get_weights")
+        return w
+
+    def ml_predict(self):
+        """Predicted displacements (n,3), caller order, at the current positions."""
+        dx = np.empty((self.n, 3))
+        _check(lib().imdgpu_ml_predict(self.h, _p(dx)), "ml_predict")
+        return dx
+
+    def ml_train_step(self, target, lr: float = 0.0, want_grad: bool = False):
+        """Loss (and gradient) for per-atom target displacements; with lr > 0
+        one Adam step of the weights."""
+        t = _f64(target, (self.n * 3,))
+        loss = C.c_double(0.0)
+        g = np.empty(lib().imdgpu_ml_nparam(), np.float32) if want_grad else None
+        _check(lib().imdgpu_ml_train_step(self.h, _p(t), lr, C.byref(loss),
+                                          _p(g, C.c_float)), "ml_train_step")
+        return (loss.value, g) if want_grad else loss.value
+
     def timing(self) -> Timing:
         t = Timing()
         _check(lib().imdgpu_get_timing(self.h, C.byref(t)), "get_timing")
@@ -292,6 +336,65 @@ class GpuSystem:
             self.close()
         except Exception:
             pass
+
+
+class GpuBatch(GpuSystem):
+    """Many independent periodic cells relaxed together by IMD's CG, one
+    line-search state per cell on the device (imdgpu_batch_* in
+    include/imdgpu.h)."""
+
+    def set_cells(self, cells, nbl_margin: float = 0.4) -> None:
+        """cells: sequence of workloads.System (box, x, types, mass, number)."""
+        natoms = np.array([c.n for c in cells], np.int32)
+        boxes = np.ascontiguousarray(np.stack([np.asarray(c.box, np.float64) for c in cells]))
+        x = np.ascontiguousarray(np.concatenate([c.x for c in cells]), np.float64)
+        ty = np.ascontiguousarray(np.concatenate([c.types for c in cells]), np.int32)
+        m = np.ascontiguousarray(np.concatenate([c.mass for c in cells]), np.float64)
+        num = np.ascontiguousarray(np.concatenate([c.number for c in cells]), np.int32)
+        _check(lib().imdgpu_batch_set_margin(self.h, nbl_margin), "batch_set_margin")
+        _check(lib().imdgpu_batch_set_cells(self.h, len(cells), _p(natoms, C.c_int), _p(boxes),
+                                            _p(num, C.c_int), _p(ty, C.c_int), _p(m), _p(x)),
+               "batch_set_cells")
+        self.n = int(natoms.sum())
+        self.ncells = len(cells)
+        self.natoms = natoms
+
+    def relax(self, fmax: float = 1e-4, maxsteps: int = 100000, max_rounds: int = 1000000) -> int:
+        r = C.c_int(0)
+        _check(lib().imdgpu_batch_relax(self.h, fmax, maxsteps, max_rounds, C.byref(r)),
+               "batch_relax")
+        return r.value
+
+    def begin(self, fmax: float = 1e-4, maxsteps: int = 100000) -> None:
+        _check(lib().imdgpu_batch_begin(self.h, fmax, maxsteps), "batch_begin")
+
+    def advance(self, max_rounds: int):
+        nd = C.c_int(0)
+        r = C.c_int(0)
+        _check(lib().imdgpu_batch_advance(self.h, max_rounds, C.byref(nd), C.byref(r)),
+               "batch_advance")
+        return nd.value, r.value
+
+    def rebuilds(self) -> int:
+        n = C.c_long(0)
+        _check(lib().imdgpu_batch_rebuilds(self.h, C.byref(n)), "batch_rebuilds")
+        return n.value
+
+    def results(self):
+        k = self.ncells
+        e = np.empty(k)
+        fm = np.empty(k)
+        st = np.empty(k, np.int32)
+        nfc = np.empty(k, np.int32)
+        status = np.empty(k, np.int32)
+        _check(lib().imdgpu_batch_results(self.h, _p(e), _p(fm), _p(st, C.c_int),
+                                          _p(nfc, C.c_int), _p(status, C.c_int)), "batch_results")
+        return {"epot": e, "fmax": fm, "steps": st, "nfc": nfc, "status": status}
+
+    def positions(self):
+        x = np.empty((self.n, 3))
+        _check(lib().imdgpu_get_atoms(self.h, _p(x), None, None, None, None, None), "get_atoms")
+        return np.split(x, np.cumsum(self.natoms)[:-1])
 
 
 def set_device(device: int) -> None:

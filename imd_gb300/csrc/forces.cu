@@ -20,7 +20,10 @@ namespace imdgpu {
 __global__ void k_ghost_pos(SysView v) {
   const int ng = v.counters[0];
   for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < ng; g += gridDim.x * blockDim.x)
-    v.pos[v.n + g] = ghost_image(v, v.pos[v.gowner[g]], v.gcode[g]);
+  {
+    const int o = v.gowner[g];
+    v.pos[v.n + g] = ghost_image(v, v.pos[o], v.gcode[g], sys_of(v, o));
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -202,10 +205,10 @@ __global__ void k_finalize_forces(const double *pe, int ne, const double *pf, in
 // type specialisation, per-atom energy scatter only when requested.  Same
 // pairs and formulas as above; only rounding differs (~1e-16 relative).
 // ---------------------------------------------------------------------------
-template <bool NT1>
+template <bool NT1, bool CUB>
 __global__ void __launch_bounds__(BS_FORCE) k_density_fast(SysView v, DevTable rho) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= v.n) return;
+  if (i >= v.n || atom_idle(v, i)) return;
   const double4 pi = v.pos[i];
   const int it = NT1 ? 0 : (int)pi.w, nt = v.ntypes;
   const int nn = v.nnb[i];
@@ -224,7 +227,7 @@ __global__ void __launch_bounds__(BS_FORCE) k_density_fast(SysView v, DevTable r
     if (lt_pos(r2, rho.end[col])) {
       double chi;
       const int kk = tab_index_fast(rho, col, r2, chi);
-      rho_h = poly_v(cv_load(rho, col, kk), chi);
+      rho_h = poly_v<CUB>(cv_load(rho, col, kk), chi);
       eam_r += rho_h;
       shortf |= lt_pos(r2, rho.begin[col]);
     }
@@ -235,7 +238,7 @@ __global__ void __launch_bounds__(BS_FORCE) k_density_fast(SysView v, DevTable r
       if (lt_pos(r2, rho.end[col2])) {
         double chi;
         const int kk = tab_index_fast(rho, col2, r2, chi);
-        atomicAdd(&v.rho[j], poly_v(cv_load(rho, col2, kk), chi));
+        atomicAdd(&v.rho[j], poly_v<CUB>(cv_load(rho, col2, kk), chi));
         shortf |= lt_pos(r2, rho.begin[col2]);
       }
     }
@@ -244,12 +247,12 @@ __global__ void __launch_bounds__(BS_FORCE) k_density_fast(SysView v, DevTable r
   if (shortf) atomicOr(v.status, ST_SHORT);
 }
 
-template <bool NT1, bool EAM, bool EPOT, bool SAMEGRID>
+template <bool NT1, bool EAM, bool EPOT, bool SAMEGRID, bool CUB>
 __global__ void __launch_bounds__(BS_FORCE) k_force_fast(SysView v, DevTable pair, DevTable rho,
                                                          double *partial) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   double acc[2] = {0.0, 0.0};  // energy, virial
-  if (i < v.n) {
+  if (i < v.n && !atom_idle(v, i)) {
     const double4 pi = v.pos[i];
     const int it = NT1 ? 0 : (int)pi.w, nt = v.ntypes;
     const int nn = v.nnb[i];
@@ -272,8 +275,8 @@ __global__ void __launch_bounds__(BS_FORCE) k_force_fast(SysView v, DevTable pai
       double chi = 0.0;
       if (le_pos(r2, pair.end[col])) {
         kk = tab_index_fast(pair, col, r2, chi);
-        const double pot = poly_v(cv_load(pair, col, kk), chi);
-        ngrad = poly_g(cgn_load(pair, col, kk), chi);
+        const double pot = poly_v<CUB>(cv_load(pair, col, kk), chi);
+        ngrad = poly_g<CUB>(cgn_load(pair, col, kk), chi);
         esum += pot;
         if (EPOT) {
           ehalf = 0.5 * pot;
@@ -289,7 +292,7 @@ __global__ void __launch_bounds__(BS_FORCE) k_force_fast(SysView v, DevTable pai
           int k1 = kk;
           if (!(SAMEGRID && have)) k1 = tab_index_fast(rho, col1, r2, chi1);
           // rho.cgn holds -rho'/2
-          const double nris = poly_g(cgn_load(rho, col1, k1), chi1);
+          const double nris = poly_g<CUB>(cgn_load(rho, col1, k1), chi1);
           const double dfj = __ldg(&v.df[j]);
           if (NT1 || col1 == col2) {
             ngrad = fma(nris, dfi + dfj, ngrad);
@@ -297,7 +300,7 @@ __global__ void __launch_bounds__(BS_FORCE) k_force_fast(SysView v, DevTable pai
             double chi2 = chi;
             int k2 = kk;
             if (!(SAMEGRID && have)) k2 = tab_index_fast(rho, col2, r2, chi2);
-            const double nrjs = poly_g(cgn_load(rho, col2, k2), chi2);
+            const double nrjs = poly_g<CUB>(cgn_load(rho, col2, k2), chi2);
             ngrad = fma(dfi, nrjs, fma(dfj, nris, ngrad));
           }
           have = true;
@@ -321,6 +324,8 @@ __global__ void __launch_bounds__(BS_FORCE) k_force_fast(SysView v, DevTable pai
     atomicAdd(fi + 1, -fny);
     atomicAdd(fi + 2, -fnz);
     if (EPOT) atomicAdd(fi + 3, ee);
+    // energy share of the atom: its own half-list pairs (deterministic order)
+    if (!EPOT && v.eshare) atomicAdd(fi + 3, esum);
     acc[0] = esum;
     acc[1] = vir;
     if (shortf) atomicOr(v.status, ST_SHORT);
@@ -332,12 +337,12 @@ __global__ void __launch_bounds__(BS_FORCE) k_force_fast(SysView v, DevTable pai
 __global__ void __launch_bounds__(BS_VEC) k_embed_fast(SysView v, DevTable emb, double *partial) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   double e[1] = {0.0};
-  if (i < v.n) {
+  if (i < v.n && !atom_idle(v, i)) {
     const int t = (int)v.pos[i].w;
     double chi;
     const int k = tab_index_fast(emb, t, v.rho[i], chi);
-    const double pot = poly_v(cv_load(emb, t, k), chi);
-    v.df[i] = poly_g(cg_load(emb, t, k), chi);
+    const double pot = poly_v<true>(cv_load(emb, t, k), chi);
+    v.df[i] = poly_g<true>(cg_load(emb, t, k), chi);
     atomicAdd(&v.frc[i].w, pot);
     e[0] = pot;
   }
@@ -347,10 +352,14 @@ __global__ void __launch_bounds__(BS_VEC) k_embed_fast(SysView v, DevTable emb, 
 template <bool NT1, bool EAM, bool EPOT>
 static void launch_force_fast(int samegrid, int nbf, cudaStream_t st, const SysView &v,
                               const ForceTabs &t, double *pf) {
-  if (samegrid)
-    k_force_fast<NT1, EAM, EPOT, true><<<nbf, BS_FORCE, 0, st>>>(v, t.pair, t.rho, pf);
-  else
-    k_force_fast<NT1, EAM, EPOT, false><<<nbf, BS_FORCE, 0, st>>>(v, t.pair, t.rho, pf);
+  const bool cub = (t.pair.mode != TAB_QUADRATIC);
+  if (samegrid) {
+    if (cub) k_force_fast<NT1, EAM, EPOT, true, true><<<nbf, BS_FORCE, 0, st>>>(v, t.pair, t.rho, pf);
+    else k_force_fast<NT1, EAM, EPOT, true, false><<<nbf, BS_FORCE, 0, st>>>(v, t.pair, t.rho, pf);
+  } else {
+    if (cub) k_force_fast<NT1, EAM, EPOT, false, true><<<nbf, BS_FORCE, 0, st>>>(v, t.pair, t.rho, pf);
+    else k_force_fast<NT1, EAM, EPOT, false, false><<<nbf, BS_FORCE, 0, st>>>(v, t.pair, t.rho, pf);
+  }
 }
 
 template <bool EAM, bool EPOT>
@@ -364,7 +373,7 @@ static void launch_force_fast2(const ForceTabs &t, int nbf, cudaStream_t st, con
 
 static void launch_force_any(const ForceTabs &t, int nbf, cudaStream_t st, const SysView &v,
                              double *pf) {
-  if (t.exact) {
+  if (t.exact && t.pair.mode == TAB_QUADRATIC) {
     if (t.eam) k_force64<true><<<nbf, BS_FORCE, 0, st>>>(v, t.pair, t.rho, pf);
     else k_force64<false><<<nbf, BS_FORCE, 0, st>>>(v, t.pair, t.rho, pf);
     return;
@@ -398,12 +407,15 @@ int launch_forces(const SysView &v, const ForceTabs &t, DevScalars *sc, int mixe
   if (t.eam) {
     cudaMemsetAsync(v.rho, 0, ext * sizeof(double), st);
     if (ev) cudaEventRecord(ev[0], st);
-    if (t.exact) k_density64<<<nbf, BS_FORCE, 0, st>>>(v, t.rho);
-    else if (t.nt1) k_density_fast<true><<<nbf, BS_FORCE, 0, st>>>(v, t.rho);
-    else k_density_fast<false><<<nbf, BS_FORCE, 0, st>>>(v, t.rho);
+    const bool quad = (t.rho.mode == TAB_QUADRATIC);
+    if (t.exact && quad) k_density64<<<nbf, BS_FORCE, 0, st>>>(v, t.rho);
+    else if (t.nt1 && quad) k_density_fast<true, false><<<nbf, BS_FORCE, 0, st>>>(v, t.rho);
+    else if (t.nt1) k_density_fast<true, true><<<nbf, BS_FORCE, 0, st>>>(v, t.rho);
+    else if (quad) k_density_fast<false, false><<<nbf, BS_FORCE, 0, st>>>(v, t.rho);
+    else k_density_fast<false, true><<<nbf, BS_FORCE, 0, st>>>(v, t.rho);
     if (ev) cudaEventRecord(ev[1], st);
     k_fold_rho<<<gblocks, BS_VEC, 0, st>>>(v);
-    if (t.exact) k_embed<<<nbe, BS_VEC, 0, st>>>(v, t.embed, pe);
+    if (t.exact && t.embed.mode == TAB_QUADRATIC) k_embed<<<nbe, BS_VEC, 0, st>>>(v, t.embed, pe);
     else k_embed_fast<<<nbe, BS_VEC, 0, st>>>(v, t.embed, pe);
     k_ghost_df<<<gblocks, BS_VEC, 0, st>>>(v);
     if (ev) cudaEventRecord(ev[2], st);

@@ -41,18 +41,24 @@ constexpr unsigned ST_CELLOVER = 8u;   // atoms per cell beyond CELLCAP
 //   2 dV/dr2   = G0 + chi G1,           G0 = 2 istep B, G1 = 4 istep C
 // (algebraically IMD's p0 + chi dv + chi (chi-1) d2v / 2 and
 // 2 istep (dv + (chi - 1/2) d2v)), three FMAs instead of ~15 operations.
+// The 4-point and spline modes of IMD (src/potaccess.h:365-457) are cubic in
+// chi on each row: value = A + chi (B + chi (C + chi D)), 2 dV/dr2 =
+// G0 + chi (G1 + chi G2).  Quadratic rows have D = G2 = 0.
+constexpr int TAB_QUADRATIC = 0, TAB_FOURPOINT = 1, TAB_SPLINE = 2;
+
 struct DevTable {
   int ncols;
   int rows;                 // maxsteps + 2
+  int mode;                 // TAB_*
   const double4 *tri;       // tri[col * rows + k] = (t[k], t[k+1], t[k+2], 0)
   const float4 *trif;       // same in FP32 (mixed precision)
-  const double4 *cv;        // (A, B, C, 0) per column and row
-  const double2 *cg;        // (G0, G1)
-  const double2 *cgn;       // (-s G0, -s G1): negated gradient for the force pass
+  const double4 *cv;        // (A, B, C, D) per column and row
+  const double4 *cg;        // (G0, G1, G2, 0)
+  const double4 *cgn;       // -s (G0, G1, G2): negated gradient for the force pass
                             // (s = 1 for pair tables, 1/2 for rho: the EAM
                             // force term 0.5 (F'_i + F'_j) rho' needs rho'/2)
   const float4 *cvf;        // FP32 copies for the mixed path
-  const float2 *cgf;
+  const float4 *cgf;
   double begin[MAXCOL];
   double end[MAXCOL];
   double invstep[MAXCOL];
@@ -102,7 +108,35 @@ struct SysView {
   unsigned *status;
   int *counters;            // [0] ghosts, [1] max entries per atom, [2] max cell atoms
   double *partial;          // per-block partial sums
+
+  // batch of independent systems (null for a single system): system of each
+  // real atom, per-system box rows, reciprocal rows, cell grid, buffered
+  // grid and first global cell index, and a per-system "finished" flag
+  const int *atom_sys;
+  const double *sbox, *stbox;  // 9 per system
+  const int *sgdim, *scdim;    // 3 per system
+  const int *scoff;            // 1 per system
+  const int *sys_done;
+  double4 *wrap_oldx;          // batch CG: old_x moved with the wrap of x
+  int eshare;                  // force pass adds each atom's own pair energies to frc.w
 };
+
+// atoms of finished cells of a batch are skipped by the force passes
+__device__ __forceinline__ bool atom_idle(const SysView &v, int i) {
+  return v.sys_done && v.sys_done[v.atom_sys[i]];
+}
+
+// system of real atom i (0 for a single system)
+__device__ __forceinline__ int sys_of(const SysView &v, int i) {
+  return v.atom_sys ? v.atom_sys[i] : 0;
+}
+// box row a, component c of the system
+__device__ __forceinline__ double box_of(const SysView &v, int sys, int a, int c) {
+  return v.sbox ? v.sbox[9 * sys + 3 * a + c] : v.box[a][c];
+}
+__device__ __forceinline__ double tbox_of(const SysView &v, int sys, int a, int c) {
+  return v.stbox ? v.stbox[9 * sys + 3 * a + c] : v.tbox[a][c];
+}
 
 // ---------------------------------------------------------------------------
 // exact FP64 helpers: no contraction into FMA, so bits match the C oracle and
@@ -217,22 +251,29 @@ __device__ __forceinline__ int tab_index_fast(const DevTable &t, int col, double
   const double rm = lt_pos(r2, t.end[col]) ? r2 : t.end[col];
   double r2a = fma(rm, t.invstep[col], t.boff[col]);
   if (__double2hiint(r2a) < 0) r2a = 0.0;          // below begin (short distance)
-  const int k = ifloor_pos(r2a);
+  int k = ifloor_pos(r2a);
+  if (t.mode == TAB_FOURPOINT) k = max(k, 1);  // PAIR_INT3: rows k-1..k+2, k >= 1
   chi = r2a - small_int_to_double(k);
   return k;
 }
 __device__ __forceinline__ double4 cv_load(const DevTable &t, int col, int k) {
   return ldg4(&t.cv[(size_t)col * t.rows + k]);
 }
-__device__ __forceinline__ double2 cg_load(const DevTable &t, int col, int k) {
-  return __ldg(&t.cg[(size_t)col * t.rows + k]);
+__device__ __forceinline__ double4 cg_load(const DevTable &t, int col, int k) {
+  return ldg4(&t.cg[(size_t)col * t.rows + k]);
 }
+__device__ __forceinline__ double4 cgn_load(const DevTable &t, int col, int k) {
+  return ldg4(&t.cgn[(size_t)col * t.rows + k]);
+}
+// CUB: cubic rows (4-point / spline); quadratic rows skip the zero terms
+template <bool CUB = false>
 __device__ __forceinline__ double poly_v(const double4 c, double chi) {
-  return fma(chi, fma(chi, c.z, c.y), c.x);
+  return CUB ? fma(chi, fma(chi, fma(chi, c.w, c.z), c.y), c.x)
+             : fma(chi, fma(chi, c.z, c.y), c.x);
 }
-__device__ __forceinline__ double poly_g(const double2 g, double chi) { return fma(chi, g.y, g.x); }
-__device__ __forceinline__ double2 cgn_load(const DevTable &t, int col, int k) {
-  return __ldg(&t.cgn[(size_t)col * t.rows + k]);
+template <bool CUB = false>
+__device__ __forceinline__ double poly_g(const double4 g, double chi) {
+  return CUB ? fma(chi, fma(chi, g.z, g.y), g.x) : fma(chi, g.y, g.x);
 }
 
 // Per-atom FP32 split of an FP64 position: x = hi + lo to ~2^-48 relative.
@@ -264,15 +305,15 @@ __device__ __forceinline__ SplitPos ldsp(const SplitPos *p) {
 // A ghost copies its owner through the z, y, x buffer copies of send_cells
 // (src/imd_comm_force_3d.c:247-358) in that order, so its position is
 // ((x + s_z box_z) + s_y box_y) + s_x box_x component-wise.
-__device__ __forceinline__ double4 ghost_image(const SysView &v, double4 p, int code) {
+__device__ __forceinline__ double4 ghost_image(const SysView &v, double4 p, int code, int sys) {
   const int sx = code % 3 - 1, sy = (code / 3) % 3 - 1, sz = code / 9 - 1;
   double c[3] = {p.x, p.y, p.z};
 #pragma unroll
   for (int a = 0; a < 3; a++) {
     double t = c[a];
-    if (sz) t = dadd(t, sz > 0 ? v.box[2][a] : -v.box[2][a]);
-    if (sy) t = dadd(t, sy > 0 ? v.box[1][a] : -v.box[1][a]);
-    if (sx) t = dadd(t, sx > 0 ? v.box[0][a] : -v.box[0][a]);
+    if (sz) t = dadd(t, sz > 0 ? box_of(v, sys, 2, a) : -box_of(v, sys, 2, a));
+    if (sy) t = dadd(t, sy > 0 ? box_of(v, sys, 1, a) : -box_of(v, sys, 1, a));
+    if (sx) t = dadd(t, sx > 0 ? box_of(v, sys, 0, a) : -box_of(v, sys, 0, a));
     c[a] = t;
   }
   return make_double4(c[0], c[1], c[2], p.w);

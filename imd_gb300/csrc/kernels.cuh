@@ -1,6 +1,8 @@
 // kernels.cuh -- launchers shared between the translation units of libimdgpu.
 #pragma once
 
+#include <cuda_bf16.h>
+
 #include "internal.cuh"
 
 namespace imdgpu {
@@ -27,6 +29,26 @@ struct DevScalars {
   int pad;
 };
 
+// batched CG (batch.cu): vector operation a cell asks for in the next round
+enum { OP_NONE = 0, OP_MOVE = 1, OP_SETHG_MOVE = 2, OP_RESET_MOVE = 3, OP_IDLE = 4 };
+// program counter of the resumable linmin / mnbrak / brent
+enum {
+  PC_START, PC_AFTER_RESET, PC_LINMIN, PC_LINMIN_FB, PC_MNBRAK_FC, PC_MNBRAK_WHILE,
+  PC_MNBRAK_A, PC_MNBRAK_C, PC_MNBRAK_E, PC_MNBRAK_SHIFT, PC_MNBRAK_END, PC_BRENT_ITER,
+  PC_BRENT_FU, PC_AFTER_LINMIN, PC_DONE
+};
+struct CgParams {
+  double linmin_tol, linmin_dmax, linmin_dmin, cg_glimit, cg_zeps, fmax;
+  int linmin_maxsteps, maxsteps, cg_fr, pad;
+};
+struct CgSys {
+  double E, fnorm, fmax2, fatom2, gg, dgg;               // last evaluation (k_bt_reduce)
+  double alpha, gamma, old_alphamin, f_max2, cg_poteng, old_cg_poteng;
+  double ax, bx, cx, fa, fb, fc, u, fu, ulim;            // mnbrak
+  double a, b, x, w, v, fx, fw, fv, e, d;                // brent
+  int pc, op, pending, steps, nfc, status, iter, ctf;
+};
+
 constexpr int BS_FORCE = 128;
 constexpr int BS_VEC = 256;
 
@@ -43,6 +65,31 @@ void k_ghost_pos_launch(const SysView &v, int blocks, cudaStream_t st);
 // mixed.cu: the FP32-force path over the full list
 int launch_forces_mixed(const SysView &v, const ForceTabs &t, DevScalars *sc, float *dff,
                         cudaStream_t st, cudaEvent_t *ev);
+
+// batch.cu
+void launch_batch_round_pre(const SysView &v, CgSys *cs, int nsys, const CgParams &P,
+                            int *sys_done, double4 *oldx, double4 *g, double4 *h,
+                            unsigned long long *maxd, int *ndone, DevScalars *sc,
+                            double skin2, cudaStream_t st);
+void launch_batch_round_post(const SysView &v, const int *aoff, CgSys *cs, int nsys,
+                             const double4 *g, int cg_fr, cudaStream_t st);
+
+// learn.cu
+struct MlPair;
+size_t ml_smem_bytes();
+int ml_nparam();
+void launch_ml_pairs(const SysView &v, MlPair *pairs, int cap, int *count, cudaStream_t st);
+void launch_ml_forward(const MlPair *pairs, const int *np, const double *rho,
+                       const __nv_bfloat16 *wb, const float *wf, float *dxp, int blocks,
+                       cudaStream_t st);
+void launch_ml_loss(int n, const float *dxp, const float *target, float *dldx, double *loss,
+                    cudaStream_t st);
+void launch_ml_backward(const MlPair *pairs, const int *np, const double *rho,
+                        const __nv_bfloat16 *wb, const float *wf, const float *dldx,
+                        float *grad, int blocks, cudaStream_t st);
+void launch_ml_adam(float *w, __nv_bfloat16 *wb, const float *grad, float *m, float *vv, int n,
+                    float lr, int step, cudaStream_t st);
+void launch_ml_to_bf16(const float *w, __nv_bfloat16 *wb, int n, cudaStream_t st);
 
 // system.cu: message returned by imdgpu_last_error()
 void set_last_error(const char *msg);

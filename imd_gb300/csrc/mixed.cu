@@ -41,17 +41,18 @@ __global__ void k_split(SysView v, SplitPos *sp) {
 __device__ __forceinline__ int tab_index_f(const DevTable &t, int col, float r2, float &chi) {
   float r2a = fmaf(fminf(r2, t.fend[col]), t.finv[col], -t.fbegin[col] * t.finv[col]);
   r2a = fmaxf(r2a, 0.0f);
-  const int k = __float2int_rz(r2a);
+  int k = __float2int_rz(r2a);
+  if (t.mode == TAB_FOURPOINT) k = max(k, 1);
   chi = r2a - (float)k;
   return k;
 }
 __device__ __forceinline__ float polyf_v(const DevTable &t, int col, int k, float chi) {
   const float4 c = __ldg(&t.cvf[(size_t)col * t.rows + k]);
-  return fmaf(chi, fmaf(chi, c.z, c.y), c.x);
+  return fmaf(chi, fmaf(chi, fmaf(chi, c.w, c.z), c.y), c.x);
 }
 __device__ __forceinline__ float polyf_g(const DevTable &t, int col, int k, float chi) {
-  const float2 g = __ldg(&t.cgf[(size_t)col * t.rows + k]);
-  return fmaf(chi, g.y, g.x);
+  const float4 g = __ldg(&t.cgf[(size_t)col * t.rows + k]);
+  return fmaf(chi, fmaf(chi, g.z, g.y), g.x);
 }
 
 // rho_i = sum_j rho_{it,jt}(r_ij) over the full list (loop 1's eam_r)
@@ -59,7 +60,7 @@ template <bool NT1>
 __global__ void __launch_bounds__(BS_FORCE) k_density_mixed(SysView v, DevTable rho,
                                                             const SplitPos *sp) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= v.n) return;
+  if (i >= v.n || atom_idle(v, i)) return;
   const SplitPos a = sp[i];
   const int it = NT1 ? 0 : __float_as_int(a.hi.w), nt = v.ntypes;
   const int nn = v.nnb[i];
@@ -91,12 +92,12 @@ __global__ void __launch_bounds__(BS_VEC) k_embed_mixed(SysView v, DevTable emb,
                                                         double *partial) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   double e[1] = {0.0};
-  if (i < v.n) {
+  if (i < v.n && !atom_idle(v, i)) {
     const int t = (int)v.pos[i].w;
     double chi;
     const int k = tab_index_fast(emb, t, v.rho[i], chi);
-    const double pot = poly_v(cv_load(emb, t, k), chi);
-    const double df = poly_g(cg_load(emb, t, k), chi);
+    const double pot = poly_v<true>(cv_load(emb, t, k), chi);
+    const double df = poly_g<true>(cg_load(emb, t, k), chi);
     v.df[i] = df;
     dff[i] = (float)df;
     v.frc[i].w = pot;
@@ -120,7 +121,7 @@ __global__ void __launch_bounds__(BS_FORCE) k_force_mixed(SysView v, DevTable pa
                                                           double *partial) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   double acc[2] = {0.0, 0.0};
-  if (i < v.n) {
+  if (i < v.n && !atom_idle(v, i)) {
     const SplitPos a = sp[i];
     const int it = NT1 ? 0 : __float_as_int(a.hi.w), nt = v.ntypes;
     const int nn = v.nnb[i];

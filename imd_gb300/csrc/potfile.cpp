@@ -26,8 +26,59 @@ static void threepoint(HostTable &t) {
   }
 }
 
+// init_fourpoint (src/imd_potential.c:1171-1187)
+static void fourpoint(HostTable &t) {
+  const int nc = t.ncols;
+  for (int col = 0; col < nc; col++) {
+    double *y = t.table.data() + col;
+    const int n = t.len[col];
+    if (n < 4) continue;
+    y[n * nc] = 4 * y[(n - 1) * nc] - 6 * y[(n - 2) * nc] + 4 * y[(n - 3) * nc] - y[(n - 4) * nc];
+    y[(n + 1) * nc] =
+        10 * y[(n - 1) * nc] - 20 * y[(n - 2) * nc] + 15 * y[(n - 3) * nc] - 4 * y[(n - 4) * nc];
+  }
+}
+
+// init_spline (src/imd_potential.c:1197-1246): natural at the left end, zero
+// slope at the right end of radial functions, natural otherwise
+static void spline(HostTable &t, int radial) {
+  const int nc = t.ncols, size = t.maxsteps + 2;
+  t.table2.assign((size_t)nc * size, 0.0);
+  std::vector<double> u(size, 0.0);
+  for (int col = 0; col < nc; col++) {
+    double *y2 = t.table2.data() + col, *y = t.table.data() + col;
+    const int n = t.len[col];
+    const double step = t.step[col];
+    double p, qn, un;
+    y2[0] = u[0] = 0;
+    for (int i = 1; i < n - 1; i++) {
+      p = 0.5 * y2[(i - 1) * nc] + 2.0;
+      y2[i * nc] = -0.5 / p;
+      u[i] = (y[(i + 1) * nc] - 2 * y[i * nc] + y[(i - 1) * nc]) / step;
+      u[i] = (6.0 * u[i] / (2 * step) - 0.5 * u[i - 1]) / p;
+    }
+    if (radial) {
+      qn = 0.5;
+      un = (3.0 / step) * (y[(n - 2) * nc] - y[(n - 1) * nc]) / step;
+    } else {
+      qn = un = 0.0;
+    }
+    y2[(n - 1) * nc] = (un - qn * u[n - 2]) / (qn * y2[(n - 2) * nc] + 1.0);
+    for (int k = n - 2; k >= 0; k--) y2[k * nc] = y2[k * nc] * y2[(k + 1) * nc] + u[k];
+    y[n * nc] = 2 * y[(n - 1) * nc] - y[(n - 2) * nc] + step * step * y2[(n - 1) * nc];
+    y2[n * nc] = 2 * y2[(n - 1) * nc] - y2[(n - 2) * nc];
+  }
+}
+
+void init_interpolation(HostTable &t, int radial, int mode) {
+  t.mode = mode;
+  if (mode == 1) fourpoint(t);
+  else if (mode == 2) spline(t, radial);
+  else threepoint(t);
+}
+
 int read_table_file(const char *fname, int ncols, int radial, int default_format,
-                    HostTable &t, double &cellsz, std::string &err) {
+                    HostTable &t, double &cellsz, std::string &err, int mode) {
   FILE *in = std::fopen(fname, "r");
   if (!in) {
     err = std::string("Could not open potential file ") + fname;
@@ -161,7 +212,7 @@ int read_table_file(const char *fname, int ncols, int radial, int default_format
       err = std::string("column with fewer than 3 values in ") + fname;
       return 1;
     }
-  threepoint(t);
+  init_interpolation(t, radial, mode);
   t.radial = radial;
   return 0;
 }

@@ -51,6 +51,15 @@ static void dfree(T *&p) {
   p = nullptr;
 }
 
+// state of a batched relaxation in progress
+struct BatchRun {
+  CgParams P;
+  int rounds = 0;
+  int ndone = 0;
+  cudaGraphExec_t gx = nullptr;
+  std::vector<uintptr_t> gkey;
+};
+
 // ---------------------------------------------------------------------------
 // the system
 // ---------------------------------------------------------------------------
@@ -64,11 +73,13 @@ struct imdgpu_sys {
   double4 *dtri[3] = {nullptr, nullptr, nullptr};
   float4 *dtrif[3] = {nullptr, nullptr, nullptr};
   double4 *dcv[3] = {nullptr, nullptr, nullptr};
-  double2 *dcg[3] = {nullptr, nullptr, nullptr};
-  double2 *dcgn[3] = {nullptr, nullptr, nullptr};
+  double4 *dcg[3] = {nullptr, nullptr, nullptr};
+  double4 *dcgn[3] = {nullptr, nullptr, nullptr};
   float4 *dcvf[3] = {nullptr, nullptr, nullptr};
-  float2 *dcgf[3] = {nullptr, nullptr, nullptr};
+  float4 *dcgf[3] = {nullptr, nullptr, nullptr};
   int exact = 0;
+  int interp = 0;  // table interpolation of tables read from now on
+  std::vector<double> pending_table2[3];
   double tab_cellsz = 0.0;
 
   bool have_box = false;
@@ -120,6 +131,31 @@ struct imdgpu_sys {
   char *flushbuf = nullptr;
   std::vector<cudaEvent_t> sev;    // per-step event pool of nve_run
 
+  // batch of independent systems (batched CG); nsys == 0 for one system
+  int nsys = 0;
+  std::vector<int> h_aoff;           // nsys + 1 atom offsets
+  std::vector<double> h_boxes;       // 9 per system
+  int *d_atom_sys = nullptr, *d_aoff = nullptr, *d_sgdim = nullptr, *d_scdim = nullptr;
+  int *d_scoff = nullptr, *d_sys_done = nullptr, *d_ndone = nullptr;
+  double *d_sbox = nullptr, *d_stbox = nullptr;
+  CgSys *d_cs = nullptr;
+  unsigned long long *d_maxd = nullptr;
+  std::vector<int> h_sgdim;
+  BatchRun *brun = nullptr;
+  long batch_nbl0 = 0;
+
+  // learned start (learn.cu)
+  float *ml_w = nullptr, *ml_m = nullptr, *ml_v = nullptr, *ml_grad = nullptr;
+  __nv_bfloat16 *ml_wb = nullptr;
+  MlPair *ml_pairs = nullptr;
+  int ml_cap = 0;
+  int *ml_np = nullptr;
+  float *ml_dx = nullptr, *ml_target = nullptr, *ml_dldx = nullptr;
+  double *ml_loss = nullptr;
+  int ml_have = 0;
+  int ml_dx_cap = 0;
+  int ml_adam_step = 0;
+
   // CUDA graph of one full chunk of NVE steps, re-captured when buffers move
   cudaGraphExec_t gexec = nullptr;
   std::vector<uintptr_t> gkey;
@@ -158,29 +194,46 @@ __global__ void k_rb_wrap_bin(SysView v, DevScalars *sc, int *key, int *local, i
   if (!sc->rebuild) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= v.n) return;
+  const int sy = sys_of(v, i);
   double4 p = v.pos[i];
+  double sh[3] = {0.0, 0.0, 0.0};  // lattice shift applied (also to CG's old_x in a batch)
 #pragma unroll
   for (int a = 0; a < 3; a++) {
     if (v.pbc[a] != 1) continue;
-    const double s = dadd(dadd(dmul(p.x, v.tbox[a][0]), dmul(p.y, v.tbox[a][1])),
-                          dmul(p.z, v.tbox[a][2]));
+    const double s = dadd(dadd(dmul(p.x, tbox_of(v, sy, a, 0)), dmul(p.y, tbox_of(v, sy, a, 1))),
+                          dmul(p.z, tbox_of(v, sy, a, 2)));
     const double m = -floor(s);
-    p.x = dadd(p.x, dmul(m, v.box[a][0]));
-    p.y = dadd(p.y, dmul(m, v.box[a][1]));
-    p.z = dadd(p.z, dmul(m, v.box[a][2]));
+    if (m != 0.0) {
+      const double bx = box_of(v, sy, a, 0), by = box_of(v, sy, a, 1), bz = box_of(v, sy, a, 2);
+      p.x = dadd(p.x, dmul(m, bx));
+      p.y = dadd(p.y, dmul(m, by));
+      p.z = dadd(p.z, dmul(m, bz));
+      sh[0] += m * bx;
+      sh[1] += m * by;
+      sh[2] += m * bz;
+    }
   }
   v.pos[i] = p;
+  if (v.atom_sys && v.wrap_oldx && (sh[0] != 0.0 || sh[1] != 0.0 || sh[2] != 0.0)) {
+    double4 o = v.wrap_oldx[i];
+    o.x += sh[0];
+    o.y += sh[1];
+    o.z += sh[2];
+    v.wrap_oldx[i] = o;
+  }
   int c[3];
+  const int *gd = v.sgdim ? v.sgdim + 3 * sy : v.gdim;
+  const int *cd = v.scdim ? v.scdim + 3 * sy : v.cdim;
 #pragma unroll
   for (int a = 0; a < 3; a++) {
-    const double s = dadd(dadd(dmul(p.x, v.tbox[a][0]), dmul(p.y, v.tbox[a][1])),
-                          dmul(p.z, v.tbox[a][2]));
-    int q = __double2int_rz(dmul((double)v.gdim[a], s));
-    if (q >= v.gdim[a]) q = v.gdim[a] - 1;
+    const double s = dadd(dadd(dmul(p.x, tbox_of(v, sy, a, 0)), dmul(p.y, tbox_of(v, sy, a, 1))),
+                          dmul(p.z, tbox_of(v, sy, a, 2)));
+    int q = __double2int_rz(dmul((double)gd[a], s));
+    if (q >= gd[a]) q = gd[a] - 1;
     else if (q < 0) q = 0;
     c[a] = q;
   }
-  const int lin = ((c[0] + 1) * v.cdim[1] + (c[1] + 1)) * v.cdim[2] + (c[2] + 1);
+  const int lin = (v.scoff ? v.scoff[sy] : 0) + ((c[0] + 1) * cd[1] + (c[1] + 1)) * cd[2] + (c[2] + 1);
   const int r = v.cell_rank[lin];
   key[i] = r;
   local[i] = atomicAdd(&rcount[r], 1);
@@ -353,7 +406,7 @@ __global__ void k_rb_ghost_fill(SysView v, DevScalars *sc, const int *gstart) {
     v.gowner[g] = owner;
     v.gcode[g] = code;
     v.ecell[v.n + g] = lin;
-    v.pos[v.n + g] = ghost_image(v, v.pos[owner], code);
+    v.pos[v.n + g] = ghost_image(v, v.pos[owner], code, sys_of(v, owner));
   }
 }
 
@@ -788,6 +841,17 @@ static SysView view(imdgpu_sys *s) {
   v.status = s->status;
   v.counters = s->counters;
   v.partial = s->partial;
+  if (s->nsys > 0) {
+    v.atom_sys = s->d_atom_sys;
+    v.sbox = s->d_sbox;
+    v.stbox = s->d_stbox;
+    v.sgdim = s->d_sgdim;
+    v.scdim = s->d_scdim;
+    v.scoff = s->d_scoff;
+    v.sys_done = s->d_sys_done;
+    v.wrap_oldx = s->oldx;
+    v.eshare = 1;
+  }
   return v;
 }
 
@@ -955,6 +1019,162 @@ static int setup_geometry(imdgpu_sys *s) {
   return IMDGPU_OK;
 }
 
+// Geometry of a batch: make_box / init_cells / make_cell_lists per system,
+// concatenated into one global cell numbering (system-major, Morton order
+// inside each system), so the rebuild kernels of the single system serve all
+// systems at once and atoms never leave their system's slot range.
+static int setup_geometry_batch(imdgpu_sys *s) {
+  auto vp = [](const double *u, const double *v, double *w) {
+    w[0] = u[1] * v[2] - u[2] * v[1];
+    w[1] = u[2] * v[0] - u[0] * v[2];
+    w[2] = u[0] * v[1] - u[1] * v[0];
+  };
+  auto sp = [](const double *a, const double *b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; };
+  const int ns = s->nsys;
+  if (s->list_r2_override > 0) s->cellsz = s->list_r2_override;
+  else {
+    const double r = std::sqrt((double)s->tab_cellsz) + s->nbl_margin;
+    s->cellsz = r * r;
+  }
+  s->geom_full = (s->precision == IMDGPU_MIXED);
+  const int nsh = s->geom_full ? 27 : 14;
+  std::vector<double> tb(9 * (size_t)ns);
+  std::vector<int> gdim(3 * (size_t)ns), cdim(3 * (size_t)ns), coff(ns + 1, 0), roff(ns + 1, 0);
+  for (int q = 0; q < ns; q++) {
+    const double *B = &s->h_boxes[9 * (size_t)q];
+    double *T = &tb[9 * (size_t)q];
+    vp(B + 3, B + 6, T);
+    vp(B + 6, B, T + 3);
+    vp(B, B + 3, T + 6);
+    const double vol = sp(B, T);
+    if (vol == 0) return fail(IMDGPU_ERR_GEOM, "Box Edges are parallel (system " + std::to_string(q) + ")");
+    for (int k = 0; k < 9; k++) T[k] /= vol;
+    for (int a = 0; a < 3; a++) {
+      const double height = 1.0 / sp(T + 3 * a, T + 3 * a);
+      const double scale = std::sqrt(1.0 * s->cellsz / height);
+      gdim[3 * q + a] = (int)(1.0 / scale);
+      if (gdim[3 * q + a] < 1)
+        return fail(IMDGPU_ERR_GEOM, "system " + std::to_string(q) + " smaller than one list radius");
+      cdim[3 * q + a] = gdim[3 * q + a] + 2;
+    }
+    coff[q + 1] = coff[q] + cdim[3 * q] * cdim[3 * q + 1] * cdim[3 * q + 2];
+    roff[q + 1] = roff[q] + gdim[3 * q] * gdim[3 * q + 1] * gdim[3 * q + 2];
+  }
+  s->nall_cells = coff[ns];
+  s->nreal_cells = roff[ns];
+  std::vector<int> cell_rank(s->nall_cells, -1), rank_lin(s->nreal_cells);
+  std::vector<int> hshell((size_t)nsh * s->nreal_cells, -1);
+  std::vector<int> bsrc, blin, bcode;
+  for (int q = 0; q < ns; q++) {
+    const int gx = gdim[3 * q], gy = gdim[3 * q + 1], gz = gdim[3 * q + 2];
+    const int cx = cdim[3 * q], cy = cdim[3 * q + 1], cz = cdim[3 * q + 2];
+    std::vector<std::pair<uint64_t, int>> mort;
+    for (int i = 0; i < gx; i++)
+      for (int j = 0; j < gy; j++)
+        for (int k = 0; k < gz; k++) {
+          const uint64_t code = (uint64_t)spread3(i) << 2 | (uint64_t)spread3(j) << 1 | spread3(k);
+          mort.push_back({code, ((i + 1) * cy + (j + 1)) * cz + (k + 1)});
+        }
+    std::sort(mort.begin(), mort.end());
+    std::vector<char> used(cx * cy * cz, 0);
+    for (size_t r = 0; r < mort.size(); r++) {
+      const int gr = roff[q] + (int)r, lin = mort[r].second;
+      rank_lin[gr] = coff[q] + lin;
+      cell_rank[coff[q] + lin] = gr;
+      const int i = lin / (cy * cz), j = (lin / cz) % cy, k = lin % cz;
+      int *nq = hshell.data() + (size_t)nsh * gr;
+      nq[0] = coff[q] + lin;
+      int nn = 1;
+      auto add = [&](int a, int b, int c) {
+        const int qq = ((i + a) * cy + (j + b)) * cz + (k + c);
+        if (qq == lin) return;
+        nq[nn++] = coff[q] + qq;  // batches are periodic in all directions
+        used[qq] = 1;
+      };
+      if (s->geom_full) {
+        for (int a = -1; a <= 1; a++)
+          for (int b = -1; b <= 1; b++)
+            for (int c = -1; c <= 1; c++) add(a, b, c);
+      } else {
+        for (int a = 0; a <= 1; a++)
+          for (int b = -a; b <= 1; b++)
+            for (int c = (a == 0 ? -b : -a); c <= 1; c++) add(a, b, c);
+      }
+    }
+    for (int lin = 0; lin < cx * cy * cz; lin++) {
+      if (!used[lin] || cell_rank[coff[q] + lin] >= 0) continue;
+      const int i = lin / (cy * cz), j = (lin / cz) % cy, k = lin % cz;
+      const int sx = (i == cx - 1) ? 1 : (i == 0 ? -1 : 0);
+      const int sy = (j == cy - 1) ? 1 : (j == 0 ? -1 : 0);
+      const int sz = (k == cz - 1) ? 1 : (k == 0 ? -1 : 0);
+      const int ri = i - sx * gx, rj = j - sy * gy, rk = k - sz * gz;
+      blin.push_back(coff[q] + lin);
+      bsrc.push_back(coff[q] + (ri * cy + rj) * cz + rk);
+      bcode.push_back((sx + 1) + 3 * (sy + 1) + 9 * (sz + 1));
+    }
+  }
+  s->nbuf = (int)blin.size();
+  for (int a = 0; a < 3; a++) {
+    s->gdim[a] = gdim[a];
+    s->cdim[a] = cdim[a];
+    s->pbc[a] = 1;
+    for (int c = 0; c < 3; c++) {
+      s->box[a][c] = s->h_boxes[3 * a + c];
+      s->tbox[a][c] = tb[3 * a + c];
+    }
+  }
+  s->h_sgdim = gdim;
+  s->volume = 0;
+  for (int q = 0; q < ns; q++) {
+    const double *B = &s->h_boxes[9 * (size_t)q];
+    double w[3];
+    vp(B + 3, B + 6, w);
+    s->volume += std::fabs(sp(B, w));
+  }
+  int *ptrs_free[] = {s->d_cell_rank, s->d_rank_lin, s->d_hshell, s->d_bsrc, s->d_blin,
+                      s->d_bcode, s->d_cstart, s->d_ccount, s->d_rcount, s->d_rstart,
+                      s->d_gstart, s->d_sgdim, s->d_scdim, s->d_scoff, s->d_aoff};
+  for (int *p : ptrs_free)
+    if (p) cudaFree(p);
+  dfree(s->d_sbox);
+  dfree(s->d_stbox);
+  CK(dalloc(&s->d_cell_rank, s->nall_cells));
+  CK(dalloc(&s->d_rank_lin, s->nreal_cells));
+  CK(dalloc(&s->d_hshell, hshell.size()));
+  CK(dalloc(&s->d_bsrc, s->nbuf));
+  CK(dalloc(&s->d_blin, s->nbuf));
+  CK(dalloc(&s->d_bcode, s->nbuf));
+  CK(dalloc(&s->d_cstart, s->nall_cells));
+  CK(dalloc(&s->d_ccount, s->nall_cells));
+  CK(dalloc(&s->d_rcount, s->nreal_cells));
+  CK(dalloc(&s->d_rstart, s->nreal_cells));
+  CK(dalloc(&s->d_gstart, s->nbuf));
+  CK(dalloc(&s->d_sgdim, 3 * (size_t)ns));
+  CK(dalloc(&s->d_scdim, 3 * (size_t)ns));
+  CK(dalloc(&s->d_scoff, ns));
+  CK(dalloc(&s->d_aoff, ns + 1));
+  CK(dalloc(&s->d_sbox, 9 * (size_t)ns));
+  CK(dalloc(&s->d_stbox, 9 * (size_t)ns));
+  CK(cudaMemcpy(s->d_cell_rank, cell_rank.data(), sizeof(int) * cell_rank.size(), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(s->d_rank_lin, rank_lin.data(), sizeof(int) * rank_lin.size(), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(s->d_hshell, hshell.data(), sizeof(int) * hshell.size(), cudaMemcpyHostToDevice));
+  if (s->nbuf) {
+    CK(cudaMemcpy(s->d_bsrc, bsrc.data(), sizeof(int) * s->nbuf, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(s->d_blin, blin.data(), sizeof(int) * s->nbuf, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(s->d_bcode, bcode.data(), sizeof(int) * s->nbuf, cudaMemcpyHostToDevice));
+  }
+  CK(cudaMemcpy(s->d_sgdim, gdim.data(), sizeof(int) * gdim.size(), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(s->d_scdim, cdim.data(), sizeof(int) * cdim.size(), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(s->d_scoff, coff.data(), sizeof(int) * ns, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(s->d_aoff, s->h_aoff.data(), sizeof(int) * (ns + 1), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(s->d_sbox, s->h_boxes.data(), sizeof(double) * 9 * ns, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(s->d_stbox, tb.data(), sizeof(double) * 9 * ns, cudaMemcpyHostToDevice));
+  CK(cudaMemset(s->d_ccount, 0, sizeof(int) * s->nall_cells));
+  CK(cudaMemset(s->d_cstart, 0, sizeof(int) * s->nall_cells));
+  s->geom_ready = true;
+  return IMDGPU_OK;
+}
+
 static int alloc_ext(imdgpu_sys *s, int gcap) {
   const size_t ext = (size_t)s->ncap + gcap;
   dfree(s->pos);
@@ -1009,6 +1229,7 @@ static void estimate_caps(imdgpu_sys *s, int &nbcap, int &gcap) {
   nbcap = (int)((s->geom_full ? 1.0 : 0.5) * full * 1.6) + 32;
   const double frac = (double)(s->nall_cells - s->nreal_cells) / s->nreal_cells;
   gcap = (int)(s->n * frac * 1.25) + 1024;
+  if (s->nsys > 0) gcap = (int)(s->n * frac * 0.8) + 4096;  // refined by the first build
 }
 
 // issue the guarded rebuild sequence (no host synchronisation)
@@ -1088,7 +1309,7 @@ static int prepare(imdgpu_sys *s) {
     return fail(IMDGPU_ERR_STATE, "EAM2 needs rho and embedding tables");
   if (!s->have_box) return fail(IMDGPU_ERR_STATE, "box not set");
   if (!s->geom_ready) {
-    int rc = setup_geometry(s);
+    int rc = s->nsys > 0 ? setup_geometry_batch(s) : setup_geometry(s);
     if (rc) return rc;
     int nbcap, gcap;
     estimate_caps(s, nbcap, gcap);
@@ -1199,8 +1420,18 @@ int imdgpu_destroy(imdgpu_sys *s) {
   dfree(s->dnbl); dfree(s->hist); dfree(s->oldx); dfree(s->cgg); dfree(s->cgh);
   dfree(s->toldx); dfree(s->tcgg); dfree(s->tcgh);
   dfree(s->slot_of); dfree(s->d_in); dfree(s->d_out); dfree(s->flushbuf); dfree(s->dff);
+  dfree(s->ml_w); dfree(s->ml_m); dfree(s->ml_v); dfree(s->ml_grad); dfree(s->ml_wb);
+  dfree(s->ml_pairs); dfree(s->ml_np); dfree(s->ml_dx); dfree(s->ml_target); dfree(s->ml_dldx);
+  dfree(s->ml_loss);
+  dfree(s->d_atom_sys); dfree(s->d_aoff); dfree(s->d_sgdim); dfree(s->d_scdim); dfree(s->d_scoff);
+  dfree(s->d_sys_done); dfree(s->d_ndone); dfree(s->d_sbox); dfree(s->d_stbox); dfree(s->d_cs);
+  dfree(s->d_maxd);
   for (auto e : s->sev) cudaEventDestroy(e);
   if (s->gexec) cudaGraphExecDestroy(s->gexec);
+  if (s->brun) {
+    if (s->brun->gx) cudaGraphExecDestroy(s->brun->gx);
+    delete s->brun;
+  }
   if (s->hsc) cudaFreeHost(s->hsc);
   if (s->ev_made)
     for (int k = 0; k < 8; k++) cudaEventDestroy(s->ev[k]);
@@ -1245,26 +1476,61 @@ static int upload_table(imdgpu_sys *s, int which, HostTable &t) {
       tri[(size_t)c * rows + k] = make_double4(at(k), at(k + 1), at(k + 2), 0.0);
       trif[(size_t)c * rows + k] = make_float4((float)at(k), (float)at(k + 1), (float)at(k + 2), 0.f);
     }
-  // coefficient form (see DevTable): A, B, C and G0, G1 per row
+  // cubic coefficient rows (see DevTable) of IMD's three interpolations
   std::vector<double4> cv((size_t)t.ncols * rows);
-  std::vector<double2> cg((size_t)t.ncols * rows);
-  std::vector<double2> cgn((size_t)t.ncols * rows);
+  std::vector<double4> cg((size_t)t.ncols * rows);
+  std::vector<double4> cgn((size_t)t.ncols * rows);
+  std::vector<float4> cvf((size_t)t.ncols * rows);
+  std::vector<float4> cgf((size_t)t.ncols * rows);
   const double gscale = (which == IMDGPU_TAB_RHO) ? -0.5 : -1.0;
   if (t.maxsteps + 2 >= (1 << 20))
     return fail(IMDGPU_ERR_TABLE, "tables with 2^20 or more rows are not supported");
-  std::vector<float4> cvf((size_t)t.ncols * rows);
-  std::vector<float2> cgf((size_t)t.ncols * rows);
+  if (t.mode == 2 && t.table2.size() != t.table.size())
+    return fail(IMDGPU_ERR_TABLE, "spline table without second derivatives");
   for (int c = 0; c < t.ncols; c++)
     for (int k = 0; k < rows; k++) {
-      const double4 q = tri[(size_t)c * rows + k];
-      const double dv = q.y - q.x, d2v = q.z - 2.0 * q.y + q.x;
-      const double A = q.x, B = dv - 0.5 * d2v, C = 0.5 * d2v;
-      const double G0 = 2.0 * t.invstep[c] * B, G1 = 4.0 * t.invstep[c] * C;
-      cv[(size_t)c * rows + k] = make_double4(A, B, C, 0.0);
-      cg[(size_t)c * rows + k] = make_double2(G0, G1);
-      cgn[(size_t)c * rows + k] = make_double2(gscale * G0, gscale * G1);
-      cvf[(size_t)c * rows + k] = make_float4((float)A, (float)B, (float)C, 0.f);
-      cgf[(size_t)c * rows + k] = make_float2((float)G0, (float)G1);
+      auto y = [&](int kk) {
+        return (kk >= 0 && kk < rows) ? t.table[(size_t)kk * t.ncols + c] : 0.0;
+      };
+      const double is = t.invstep[c];
+      double A, B, C, D = 0.0, G0, G1, G2 = 0.0;
+      if (t.mode == 1) {  // PAIR_INT3 on rows k-1..k+2 (src/potaccess.h:365-410)
+        const double p0 = y(k - 1), p1 = y(k), p2 = y(k + 1), p3 = y(k + 2);
+        A = p1;
+        B = -p0 / 3.0 - 0.5 * p1 + p2 - p3 / 6.0;
+        C = 0.5 * p0 - p1 + 0.5 * p2;
+        D = (-p0 + 3.0 * p1 - 3.0 * p2 + p3) / 6.0;
+        G0 = 2.0 * is * B;
+        G1 = 4.0 * is * C;
+        G2 = 6.0 * is * D;
+      } else if (t.mode == 2) {  // PAIR_INT_SP (src/potaccess.h:421-457)
+        auto y2 = [&](int kk) {
+          return (kk >= 0 && kk < rows) ? t.table2[(size_t)kk * t.ncols + c] : 0.0;
+        };
+        const double p1 = y(k), p2 = y(k + 1), d21 = y2(k), d22 = y2(k + 1);
+        const double st = t.step[c], st6 = st / 6.0, s2 = st * st / 6.0;
+        A = p1;
+        B = (p2 - p1) + s2 * (-2.0 * d21 - d22);
+        C = 3.0 * s2 * d21;
+        D = s2 * (d22 - d21);
+        G0 = 2.0 * is * (p2 - p1) + 2.0 * st6 * (-d22 - 2.0 * d21);
+        G1 = 12.0 * st6 * d21;
+        G2 = 6.0 * st6 * (d22 - d21);
+      } else {  // PAIR_INT2 (src/potaccess.h:323-354)
+        const double4 q = tri[(size_t)c * rows + k];
+        const double dv = q.y - q.x, d2v = q.z - 2.0 * q.y + q.x;
+        A = q.x;
+        B = dv - 0.5 * d2v;
+        C = 0.5 * d2v;
+        G0 = 2.0 * is * B;
+        G1 = 4.0 * is * C;
+      }
+      const size_t o = (size_t)c * rows + k;
+      cv[o] = make_double4(A, B, C, D);
+      cg[o] = make_double4(G0, G1, G2, 0.0);
+      cgn[o] = make_double4(gscale * G0, gscale * G1, gscale * G2, 0.0);
+      cvf[o] = make_float4((float)A, (float)B, (float)C, (float)D);
+      cgf[o] = make_float4((float)G0, (float)G1, (float)G2, 0.f);
     }
   dfree(s->dtri[which]);
   dfree(s->dtrif[which]);
@@ -1283,14 +1549,15 @@ static int upload_table(imdgpu_sys *s, int which, HostTable &t) {
   CK(cudaMemcpy(s->dtri[which], tri.data(), tri.size() * sizeof(double4), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(s->dtrif[which], trif.data(), trif.size() * sizeof(float4), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(s->dcv[which], cv.data(), cv.size() * sizeof(double4), cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(s->dcg[which], cg.data(), cg.size() * sizeof(double2), cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(s->dcgn[which], cgn.data(), cgn.size() * sizeof(double2), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(s->dcg[which], cg.data(), cg.size() * sizeof(double4), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(s->dcgn[which], cgn.data(), cgn.size() * sizeof(double4), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(s->dcvf[which], cvf.data(), cvf.size() * sizeof(float4), cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(s->dcgf[which], cgf.data(), cgf.size() * sizeof(float2), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(s->dcgf[which], cgf.data(), cgf.size() * sizeof(float4), cudaMemcpyHostToDevice));
   DevTable &d = s->dtab[which];
   memset(&d, 0, sizeof d);
   d.ncols = t.ncols;
   d.rows = rows;
+  d.mode = t.mode;
   d.tri = s->dtri[which];
   d.trif = s->dtrif[which];
   d.cv = s->dcv[which];
@@ -1332,7 +1599,25 @@ int imdgpu_set_table(imdgpu_sys *s, int which, int ncols, int maxsteps, const do
   for (int c = 0; c < ncols; c++)
     if (len[c] + 1 > maxsteps + 1) return fail(IMDGPU_ERR_TABLE, "len exceeds maxsteps");
   t.table.assign(table, table + (size_t)ncols * (maxsteps + 2));
+  t.mode = s->interp;
+  if (t.mode == 2) {
+    // spline: second derivatives from imdgpu_set_table2, or computed here
+    if (s->pending_table2[which].size() == t.table.size()) t.table2 = s->pending_table2[which];
+    else return fail(IMDGPU_ERR_TABLE, "spline tables need imdgpu_set_table2 first");
+  }
   return upload_table(s, which, t);
+}
+
+int imdgpu_set_interpolation(imdgpu_sys *s, int mode) {
+  if (!s || mode < 0 || mode > 2) return fail(IMDGPU_ERR_ARG, "interpolation: 0, 1 or 2");
+  s->interp = mode;
+  return IMDGPU_OK;
+}
+
+int imdgpu_set_table2(imdgpu_sys *s, int which, int ncols, int maxsteps, const double *table2) {
+  if (!s || which < 0 || which > 2 || !table2) return fail(IMDGPU_ERR_ARG, "bad table2");
+  s->pending_table2[which].assign(table2, table2 + (size_t)ncols * (maxsteps + 2));
+  return IMDGPU_OK;
 }
 
 int imdgpu_read_table(imdgpu_sys *s, int which, const char *fname, int radial,
@@ -1342,7 +1627,7 @@ int imdgpu_read_table(imdgpu_sys *s, int which, const char *fname, int radial,
   HostTable t;
   std::string err;
   double dummy = 0.0;
-  if (read_table_file(fname, ncols, radial, default_format, t, dummy, err))
+  if (read_table_file(fname, ncols, radial, default_format, t, dummy, err, s->interp))
     return fail(IMDGPU_ERR_TABLE, err);
   return upload_table(s, which, t);
 }
@@ -2071,7 +2356,416 @@ int imdgpu_cg_relax(imdgpu_sys *s, double fmax, int maxsteps, int *steps_done,
   return IMDGPU_OK;
 }
 
-int imdgpu_get_pairs(imdgpu_sys *s, long cap, int *ni, int *nj, int *shift, double *r2,
+// ---------------------------------------------------------------------------
+// batched CG
+// ---------------------------------------------------------------------------
+int imdgpu_batch_set_cells(imdgpu_sys *s, int ncells, const int *natoms, const double *boxes,
+                           const int *number, const int *type, const double *mass,
+                           const double *x) {
+  if (!s || ncells < 1 || !natoms || !boxes) return fail(IMDGPU_ERR_ARG, "bad batch arguments");
+  std::vector<int> aoff(ncells + 1, 0);
+  for (int q = 0; q < ncells; q++) {
+    if (natoms[q] < 1) return fail(IMDGPU_ERR_ARG, "empty cell in batch");
+    aoff[q + 1] = aoff[q] + natoms[q];
+  }
+  s->nsys = ncells;
+  s->h_aoff = aoff;
+  s->h_boxes.assign(boxes, boxes + 9 * (size_t)ncells);
+  s->have_box = true;
+  s->geom_ready = false;
+  s->nbl_margin = s->nbl_margin > 0 ? s->nbl_margin : 0.4;
+  int rc = imdgpu_set_atoms(s, aoff[ncells], number, type, mass, x, nullptr);
+  if (rc) return rc;
+  std::vector<int> asys(aoff[ncells]);
+  for (int q = 0; q < ncells; q++)
+    for (int i = aoff[q]; i < aoff[q + 1]; i++) asys[i] = q;
+  dfree(s->d_atom_sys);
+  dfree(s->d_sys_done);
+  dfree(s->d_ndone);
+  dfree(s->d_cs);
+  dfree(s->d_maxd);
+  CK(dalloc(&s->d_atom_sys, asys.size()));
+  CK(dalloc(&s->d_sys_done, ncells));
+  CK(dalloc(&s->d_ndone, 1));
+  CK(dalloc(&s->d_cs, ncells));
+  CK(dalloc(&s->d_maxd, ncells));
+  CK(cudaMemcpy(s->d_atom_sys, asys.data(), sizeof(int) * asys.size(), cudaMemcpyHostToDevice));
+  CK(cudaMemset(s->d_sys_done, 0, sizeof(int) * ncells));
+  return IMDGPU_OK;
+}
+
+int imdgpu_batch_set_margin(imdgpu_sys *s, double nbl_margin) {
+  if (!s || nbl_margin < 0) return fail(IMDGPU_ERR_ARG, "bad margin");
+  s->nbl_margin = nbl_margin;
+  s->geom_ready = false;
+  return IMDGPU_OK;
+}
+
+static void issue_batch_round(imdgpu_sys *s, const CgParams &P) {
+  SysView v = view(s);
+  ForceTabs ft = ftabs(s);
+  ft.epot = 0;
+  launch_batch_round_pre(v, s->d_cs, s->nsys, P, s->d_sys_done, s->oldx, s->cgg, s->cgh,
+                         s->d_maxd, s->d_ndone, s->dsc, v.skin2, s->st);
+  issue_rebuild(s);
+  launch_forces(v, ft, s->dsc, s->precision == IMDGPU_MIXED, s->st);
+  launch_batch_round_post(v, s->d_aoff, s->d_cs, s->nsys, s->cgg, s->cg_fr, s->st);
+}
+
+
+int imdgpu_batch_begin(imdgpu_sys *s, double fmax, int maxsteps) {
+  if (!s || s->nsys < 1) return fail(IMDGPU_ERR_STATE, "imdgpu_batch_set_cells first");
+  int rc = prepare(s);
+  if (rc) return rc;
+  if ((rc = ensure_cg(s))) return rc;
+  const int ns = s->nsys;
+  std::vector<CgSys> init(ns);
+  for (auto &c : init) {
+    memset(&c, 0, sizeof c);
+    c.pc = PC_START;
+    c.op = OP_NONE;
+    c.old_alphamin = 0.1;  // static in linmin, src/imd_cg.c:99
+  }
+  CK(cudaMemcpy(s->d_cs, init.data(), sizeof(CgSys) * ns, cudaMemcpyHostToDevice));
+  CK(cudaMemset(s->d_sys_done, 0, sizeof(int) * ns));
+  CK(cudaMemset(s->d_ndone, 0, sizeof(int)));
+  CK(cudaMemset(s->cgg, 0, sizeof(double4) * s->ncap));
+  CK(cudaMemset(s->cgh, 0, sizeof(double4) * s->ncap));
+  CK(cudaMemset(s->oldx, 0, sizeof(double4) * s->ncap));
+  // first list: synchronous, sizes the buffers (with head-room for relaxation)
+  int one = 1;
+  CK(cudaMemcpy(&s->dsc->rebuild, &one, sizeof(int), cudaMemcpyHostToDevice));
+  rc = rebuild_sync(s);
+  if (rc) return rc;
+  {
+    int cnt[4];
+    CK(cudaMemcpy(cnt, s->counters, sizeof cnt, cudaMemcpyDeviceToHost));
+    if (s->nbcap < (int)(cnt[1] * 1.3) + 8) {
+      if ((rc = alloc_list(s, (int)(cnt[1] * 1.3) + 8))) return rc;
+      if ((rc = rebuild_sync(s))) return rc;
+    }
+  }
+  if (!s->brun) s->brun = new BatchRun();
+  BatchRun &B = *s->brun;
+  if (B.gx) cudaGraphExecDestroy(B.gx);
+  B = BatchRun();
+  CgParams &P = B.P;
+  memset(&P, 0, sizeof P);
+  P.linmin_tol = s->linmin_tol;
+  P.linmin_dmax = s->linmin_dmax;
+  P.linmin_dmin = s->linmin_dmin;
+  P.cg_glimit = s->cg_glimit;
+  P.cg_zeps = s->cg_zeps;
+  P.fmax = fmax;
+  P.linmin_maxsteps = s->linmin_maxsteps;
+  P.maxsteps = maxsteps;
+  P.cg_fr = s->cg_fr;
+  long nbl = 0;
+  CK(cudaMemcpy(&nbl, s->dnbl, sizeof(long), cudaMemcpyDeviceToHost));
+  s->batch_nbl0 = nbl;
+  return IMDGPU_OK;
+}
+
+// up to max_rounds more rounds (in chunks of 16); *ndone = finished cells
+int imdgpu_batch_advance(imdgpu_sys *s, int max_rounds, int *ndone_out, int *rounds_out) {
+  if (!s || !s->brun) return fail(IMDGPU_ERR_STATE, "imdgpu_batch_begin first");
+  BatchRun &B = *s->brun;
+  const CgParams &P = B.P;
+  const int ns = s->nsys;
+  const int R = 16;
+  const size_t n = s->n;
+  int rc = IMDGPU_OK;
+  // snapshot of everything a round changes, for replay after an overflow
+  double4 *b4[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+  double4 *live4[6] = {s->pos, s->mom, s->oldx, s->cgg, s->cgh, s->frc};
+  for (int k = 0; k < 6; k++) CK(dalloc(&b4[k], n));
+  int *bnum = nullptr, *borig = nullptr, *bdone = nullptr, *bnd = nullptr;
+  CgSys *bcs = nullptr;
+  CK(dalloc(&bnum, n));
+  CK(dalloc(&borig, n));
+  CK(dalloc(&bdone, ns));
+  CK(dalloc(&bnd, 1));
+  CK(dalloc(&bcs, ns));
+  int done_rounds = 0, replays = 0;
+  while (done_rounds < max_rounds && B.ndone < ns) {
+    live4[0] = s->pos;
+    live4[1] = s->mom;
+    live4[5] = s->frc;
+    for (int k = 0; k < 6; k++)
+      CK(cudaMemcpyAsync(b4[k], live4[k], sizeof(double4) * n, cudaMemcpyDeviceToDevice, s->st));
+    CK(cudaMemcpyAsync(bnum, s->number, sizeof(int) * n, cudaMemcpyDeviceToDevice, s->st));
+    CK(cudaMemcpyAsync(borig, s->orig, sizeof(int) * n, cudaMemcpyDeviceToDevice, s->st));
+    CK(cudaMemcpyAsync(bdone, s->d_sys_done, sizeof(int) * ns, cudaMemcpyDeviceToDevice, s->st));
+    CK(cudaMemcpyAsync(bnd, s->d_ndone, sizeof(int), cudaMemcpyDeviceToDevice, s->st));
+    CK(cudaMemcpyAsync(bcs, s->d_cs, sizeof(CgSys) * ns, cudaMemcpyDeviceToDevice, s->st));
+    CK(cudaMemsetAsync(s->status, 0, sizeof(unsigned), s->st));
+    std::vector<uintptr_t> key = {(uintptr_t)s->pos, (uintptr_t)s->nbr, (uintptr_t)s->xl,
+                                  (uintptr_t)s->nbcap, (uintptr_t)s->gcap,
+                                  (uintptr_t)s->precision, (uintptr_t)s->exact};
+    if (s->use_graph) {
+      if (!B.gx || key != B.gkey) {
+        if (B.gx) cudaGraphExecDestroy(B.gx);
+        B.gx = nullptr;
+        cudaGraph_t g;
+        CK(cudaStreamBeginCapture(s->st, cudaStreamCaptureModeThreadLocal));
+        for (int r = 0; r < R; r++) issue_batch_round(s, P);
+        cudaError_t e = cudaStreamEndCapture(s->st, &g);
+        if (e != cudaSuccess) return fail(IMDGPU_ERR_CUDA, std::string("batch graph capture: ") + cudaGetErrorString(e));
+        e = cudaGraphInstantiate(&B.gx, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return fail(IMDGPU_ERR_CUDA, std::string("batch graph instantiate: ") + cudaGetErrorString(e));
+        B.gkey = key;
+      }
+      CK(cudaGraphLaunch(B.gx, s->st));
+    } else {
+      for (int r = 0; r < R; r++) issue_batch_round(s, P);
+      CK(cudaGetLastError());
+    }
+    int nd = 0;
+    CK(cudaMemcpyAsync(&s->status_host, s->status, sizeof(unsigned), cudaMemcpyDeviceToHost, s->st));
+    CK(cudaMemcpyAsync(&nd, s->d_ndone, sizeof(int), cudaMemcpyDeviceToHost, s->st));
+    CK(cudaStreamSynchronize(s->st));
+    if (s->status_host & ST_CELLOVER) {
+      rc = fail(IMDGPU_ERR_CELL, "more than " + std::to_string(CELLCAP) + " atoms in one cell");
+      break;
+    }
+    if (s->status_host & (ST_NBOVER | ST_GHOSTOVER)) {
+      if (++replays > 8) {
+        rc = fail(IMDGPU_ERR_NOMEM, "list overflow persists in batch relaxation");
+        break;
+      }
+      int cnt[4];
+      CK(cudaMemcpy(cnt, s->counters, sizeof cnt, cudaMemcpyDeviceToHost));
+      if (s->status_host & ST_GHOSTOVER)
+        if ((rc = alloc_ext(s, (int)(cnt[3] * 1.25) + 4096))) break;
+      if (s->status_host & ST_NBOVER)
+        if ((rc = alloc_list(s, (int)(cnt[1] * 1.2) + 8))) break;
+      live4[0] = s->pos;
+      live4[1] = s->mom;
+      live4[5] = s->frc;
+      for (int k = 0; k < 6; k++)
+        CK(cudaMemcpy(live4[k], b4[k], sizeof(double4) * n, cudaMemcpyDeviceToDevice));
+      CK(cudaMemcpy(s->number, bnum, sizeof(int) * n, cudaMemcpyDeviceToDevice));
+      CK(cudaMemcpy(s->orig, borig, sizeof(int) * n, cudaMemcpyDeviceToDevice));
+      CK(cudaMemcpy(s->d_sys_done, bdone, sizeof(int) * ns, cudaMemcpyDeviceToDevice));
+      CK(cudaMemcpy(s->d_ndone, bnd, sizeof(int), cudaMemcpyDeviceToDevice));
+      CK(cudaMemcpy(s->d_cs, bcs, sizeof(CgSys) * ns, cudaMemcpyDeviceToDevice));
+      if ((rc = rebuild_sync(s))) break;
+      continue;
+    }
+    B.ndone = nd;
+    B.rounds += R;
+    done_rounds += R;
+  }
+  for (int k = 0; k < 6; k++) dfree(b4[k]);
+  dfree(bnum);
+  dfree(borig);
+  dfree(bdone);
+  dfree(bnd);
+  dfree(bcs);
+  if (rc) return rc;
+  if (ndone_out) *ndone_out = B.ndone;
+  if (rounds_out) *rounds_out = B.rounds;
+  return read_back(s);
+}
+
+int imdgpu_batch_relax(imdgpu_sys *s, double fmax, int maxsteps, int max_rounds,
+                       int *rounds_done) {
+  int rc = imdgpu_batch_begin(s, fmax, maxsteps);
+  if (rc) return rc;
+  int nd = 0, rounds = 0;
+  rc = imdgpu_batch_advance(s, max_rounds, &nd, &rounds);
+  if (rounds_done) *rounds_done = rounds;
+  return rc;
+}
+
+// rebuilds of the neighbour list since imdgpu_batch_begin
+int imdgpu_batch_rebuilds(imdgpu_sys *s, long *n) {
+  if (!s || !n) return fail(IMDGPU_ERR_ARG, "null");
+  long nbl = 0;
+  CK(cudaMemcpy(&nbl, s->dnbl, sizeof(long), cudaMemcpyDeviceToHost));
+  *n = nbl - s->batch_nbl0;
+  return IMDGPU_OK;
+}
+
+// per-cell results: energy, max |F|, CG steps, force calls, status
+// (0 converged, 1 not converged within the rounds, 2 brent failed, 3 control)
+int imdgpu_batch_results(imdgpu_sys *s, double *epot, double *fmax_out, int *steps, int *nfc,
+                         int *status) {
+  if (!s || s->nsys < 1) return fail(IMDGPU_ERR_STATE, "no batch");
+  std::vector<CgSys> cs(s->nsys);
+  CK(cudaMemcpy(cs.data(), s->d_cs, sizeof(CgSys) * s->nsys, cudaMemcpyDeviceToHost));
+  for (int q = 0; q < s->nsys; q++) {
+    if (epot) epot[q] = cs[q].E;
+    if (fmax_out) fmax_out[q] = std::sqrt(cs[q].fatom2);
+    if (steps) steps[q] = cs[q].steps;
+    if (nfc) nfc[q] = cs[q].nfc;
+    if (status) status[q] = cs[q].status ? cs[q].status : (cs[q].pc == PC_DONE ? 0 : 1);
+  }
+  return IMDGPU_OK;
+}
+
+// ---------------------------------------------------------------------------
+// learned start
+// ---------------------------------------------------------------------------
+namespace imdgpu {
+__global__ void k_gather_target(int n, const int *orig, const double *t, float *ts) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  const int o = orig[s];
+  ts[3 * s] = (float)t[3 * o];
+  ts[3 * s + 1] = (float)t[3 * o + 1];
+  ts[3 * s + 2] = (float)t[3 * o + 2];
+}
+__global__ void k_scatter_dx(int n, const int *orig, const float *dx, double *out) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  const int o = orig[s];
+  out[3 * o] = dx[3 * s];
+  out[3 * o + 1] = dx[3 * s + 1];
+  out[3 * o + 2] = dx[3 * s + 2];
+}
+// x += sign * dx for atoms whose system is selected (all when sel == null)
+__global__ void k_apply_dx(SysView v, const float *dx, double sign, const int *sel) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= v.n) return;
+  if (sel && !sel[v.atom_sys ? v.atom_sys[s] : 0]) return;
+  double4 x = v.pos[s];
+  x.x += sign * dx[3 * s];
+  x.y += sign * dx[3 * s + 1];
+  x.z += sign * dx[3 * s + 2];
+  v.pos[s] = x;
+}
+}  // namespace imdgpu
+
+static int ml_ensure(imdgpu_sys *s) {
+  const int np = ml_nparam();
+  if (!s->ml_w) {
+    CK(dalloc(&s->ml_w, np));
+    CK(dalloc(&s->ml_m, np));
+    CK(dalloc(&s->ml_v, np));
+    CK(dalloc(&s->ml_grad, np));
+    CK(dalloc(&s->ml_wb, np));
+    CK(dalloc(&s->ml_np, 1));
+    CK(dalloc(&s->ml_loss, 1));
+    CK(cudaMemset(s->ml_w, 0, sizeof(float) * np));
+    CK(cudaMemset(s->ml_m, 0, sizeof(float) * np));
+    CK(cudaMemset(s->ml_v, 0, sizeof(float) * np));
+  }
+  if (s->ml_dx_cap < s->ncap) {
+    dfree(s->ml_dx);
+    dfree(s->ml_target);
+    dfree(s->ml_dldx);
+    CK(dalloc(&s->ml_dx, 3 * (size_t)s->ncap));
+    CK(dalloc(&s->ml_target, 3 * (size_t)s->ncap));
+    CK(dalloc(&s->ml_dldx, 3 * (size_t)s->ncap));
+    s->ml_dx_cap = s->ncap;
+  }
+  return IMDGPU_OK;
+}
+
+// list + rho at the current positions, then the directed pairs within 5.5 A
+static int ml_prepare_pairs(imdgpu_sys *s) {
+  int rc = calc_forces_sync(s);
+  if (rc) return rc;
+  if ((rc = ml_ensure(s))) return rc;
+  long entries = 0;
+  {
+    std::vector<int> nn(s->n);
+    CK(cudaMemcpy(nn.data(), s->nnb, sizeof(int) * s->n, cudaMemcpyDeviceToHost));
+    for (int v : nn) entries += v;
+  }
+  const long need = 2 * entries + 64;
+  if (need > s->ml_cap) {
+    dfree(s->ml_pairs);
+    CK(cudaMalloc((void **)&s->ml_pairs, (size_t)need * 16));
+    s->ml_cap = (int)need;
+  }
+  CK(cudaMemsetAsync(s->ml_np, 0, sizeof(int), s->st));
+  launch_ml_pairs(view(s), s->ml_pairs, s->ml_cap, s->ml_np, s->st);
+  CK(cudaGetLastError());
+  return IMDGPU_OK;
+}
+
+static int ml_blocks() { return 152 * 8; }
+
+static int ml_forward(imdgpu_sys *s) {
+  CK(cudaMemsetAsync(s->ml_dx, 0, sizeof(float) * 3 * s->n, s->st));
+  launch_ml_forward(s->ml_pairs, s->ml_np, s->rho, s->ml_wb, s->ml_w, s->ml_dx, ml_blocks(), s->st);
+  CK(cudaGetLastError());
+  return IMDGPU_OK;
+}
+
+extern "C" {
+
+int imdgpu_ml_nparam(void) { return ml_nparam(); }
+
+int imdgpu_ml_set_weights(imdgpu_sys *s, const float *w, int n) {
+  if (!s || !w || n != ml_nparam()) return fail(IMDGPU_ERR_ARG, "weights: wrong size");
+  if (!s->atoms_set) return fail(IMDGPU_ERR_STATE, "atoms not set");
+  int rc = ml_ensure(s);
+  if (rc) return rc;
+  CK(cudaMemcpy(s->ml_w, w, sizeof(float) * n, cudaMemcpyHostToDevice));
+  CK(cudaMemset(s->ml_m, 0, sizeof(float) * n));
+  CK(cudaMemset(s->ml_v, 0, sizeof(float) * n));
+  launch_ml_to_bf16(s->ml_w, s->ml_wb, n, s->st);
+  CK(cudaStreamSynchronize(s->st));
+  s->ml_have = 1;
+  s->ml_adam_step = 0;
+  return IMDGPU_OK;
+}
+
+int imdgpu_ml_get_weights(imdgpu_sys *s, float *w, int n) {
+  if (!s || !w || n != ml_nparam() || !s->ml_w) return fail(IMDGPU_ERR_ARG, "weights: not set");
+  CK(cudaMemcpy(w, s->ml_w, sizeof(float) * n, cudaMemcpyDeviceToHost));
+  return IMDGPU_OK;
+}
+
+// predicted displacement of every atom (caller order) at the current positions
+int imdgpu_ml_predict(imdgpu_sys *s, double *dx) {
+  if (!s || !s->ml_have) return fail(IMDGPU_ERR_STATE, "no weights");
+  int rc = ml_prepare_pairs(s);
+  if (rc) return rc;
+  if ((rc = ml_forward(s))) return rc;
+  double *d = s->d_out;
+  k_scatter_dx<<<nblk(s->n, 256), 256, 0, s->st>>>(s->n, s->orig, s->ml_dx, d);
+  CK(cudaMemcpyAsync(dx, d, sizeof(double) * 3 * s->n, cudaMemcpyDeviceToHost, s->st));
+  CK(cudaStreamSynchronize(s->st));
+  return IMDGPU_OK;
+}
+
+// loss and parameter gradients for targets (caller order, 3n); with lr > 0
+// also one Adam step (learning rate lr)
+int imdgpu_ml_train_step(imdgpu_sys *s, const double *target, double lr, double *loss,
+                         float *grad_out) {
+  if (!s || !s->ml_have || !target) return fail(IMDGPU_ERR_STATE, "no weights / targets");
+  int rc = ml_prepare_pairs(s);
+  if (rc) return rc;
+  double *d = s->d_out;
+  CK(cudaMemcpyAsync(d, target, sizeof(double) * 3 * s->n, cudaMemcpyHostToDevice, s->st));
+  k_gather_target<<<nblk(s->n, 256), 256, 0, s->st>>>(s->n, s->orig, d, s->ml_target);
+  if ((rc = ml_forward(s))) return rc;
+  CK(cudaMemsetAsync(s->ml_loss, 0, sizeof(double), s->st));
+  launch_ml_loss(s->n, s->ml_dx, s->ml_target, s->ml_dldx, s->ml_loss, s->st);
+  const int np = ml_nparam();
+  CK(cudaMemsetAsync(s->ml_grad, 0, sizeof(float) * np, s->st));
+  launch_ml_backward(s->ml_pairs, s->ml_np, s->rho, s->ml_wb, s->ml_w, s->ml_dldx, s->ml_grad,
+                     ml_blocks(), s->st);
+  if (lr > 0) {
+    s->ml_adam_step++;
+    launch_ml_adam(s->ml_w, s->ml_wb, s->ml_grad, s->ml_m, s->ml_v, np, (float)lr,
+                   s->ml_adam_step, s->st);
+  }
+  CK(cudaGetLastError());
+  if (loss) CK(cudaMemcpyAsync(loss, s->ml_loss, sizeof(double), cudaMemcpyDeviceToHost, s->st));
+  if (grad_out) CK(cudaMemcpyAsync(grad_out, s->ml_grad, sizeof(float) * np, cudaMemcpyDeviceToHost, s->st));
+  CK(cudaStreamSynchronize(s->st));
+  return IMDGPU_OK;
+}
+
+}  // extern "C"
+
+extern "C" int imdgpu_get_pairs(imdgpu_sys *s, long cap, int *ni, int *nj, int *shift, double *r2,
                      long *count) {
   if (!s || !count) return fail(IMDGPU_ERR_ARG, "null");
   if (!s->geom_ready || s->nbcap == 0) return fail(IMDGPU_ERR_STATE, "no list");

@@ -220,3 +220,50 @@ def eam_fcc_system(ncell: int = 40, a0: float = 3.615, T: float = 300.0,
     mass = np.array([species[t].mass for t in types], np.float64)
     p = maxwell_momenta(mass, KB_EV * T, seed)
     return System(box, x, p, types, mass, np.arange(n, dtype=np.int32), {"a0": a0})
+
+
+def defect_cell(rng, a0: float = 3.615, nmin: int = 500, nmax: int = 20000,
+                nlim=(3, 18), species=CU, strain: float = 0.02, noise: float = 0.05,
+                dumbbell: float = 0.3) -> System:
+    """One cell of the batched-relaxation workload: an n1 x n2 x n3 fcc cell
+    (n_i in nlim) whose atom count follows a log-uniform target in
+    [nmin, nmax]; 1-4 defects, each a vacancy or a <100> dumbbell
+    interstitial (the site's atom replaced by two atoms at +-dumbbell*a0
+    along a random cube axis); a homogeneous deformation I + e with every
+    component of e uniform in +-strain (a triclinic box); Gaussian position
+    noise of `noise` Angstrom."""
+    lo, hi = nlim
+    while True:
+        target = math.exp(rng.uniform(math.log(nmin), math.log(nmax)))
+        n1, n2 = (int(v) for v in rng.integers(lo, hi + 1, size=2))
+        n3 = int(round(target / (4.0 * n1 * n2)))
+        if lo <= n3 <= hi:
+            break
+    x, box = fcc(n1, n2, n3, a0)
+    ndef = int(rng.integers(1, 5))
+    sites = rng.choice(len(x), size=ndef, replace=False)
+    keep = np.ones(len(x), bool)
+    extra = []
+    for site in sites:
+        if rng.integers(0, 2) == 0:
+            keep[site] = False
+        else:
+            d = np.zeros(3)
+            d[int(rng.integers(0, 3))] = dumbbell * a0
+            extra.append(x[site] + d)
+            x[site] = x[site] - d
+    x = np.concatenate([x[keep], np.array(extra).reshape(-1, 3)])
+    F = np.eye(3) + rng.uniform(-strain, strain, size=(3, 3))
+    x = x @ F.T
+    box = box @ F.T
+    x = x + noise * rng.standard_normal(x.shape)
+    n = len(x)
+    return System(box, x, np.zeros((n, 3)), np.zeros(n, np.int32),
+                  np.full(n, species.mass), np.arange(n, dtype=np.int32),
+                  {"dims": (n1, n2, n3), "defects": ndef})
+
+
+def defect_batch(ncells: int = 512, seed: int = 4, **kw) -> list:
+    """The batched CG workload: `ncells` independent defect cells (seeded)."""
+    rng = np.random.default_rng(seed)
+    return [defect_cell(rng, **kw) for _ in range(ncells)]

@@ -87,6 +87,16 @@ int imdgpu_set_precision(imdgpu_sys *sys, int precision);
 int imdgpu_set_table(imdgpu_sys *sys, int which, int ncols, int maxsteps,
                      const double *begin, const double *end, const double *step,
                      const double *invstep, const int *len, const double *table);
+/* Interpolation of tables uploaded from now on, as IMD's make targets
+ * select it: 0 = 3-point quadratic (default, src/potaccess.h:323),
+ * 1 = 4-point cubic (`4point`, :365), 2 = cubic spline (`spline`, :421). */
+#define IMDGPU_INTERP_QUADRATIC 0
+#define IMDGPU_INTERP_FOURPOINT 1
+#define IMDGPU_INTERP_SPLINE 2
+int imdgpu_set_interpolation(imdgpu_sys *sys, int mode);
+/* spline builds: pot_table_t.table2 of the next imdgpu_set_table(which) */
+int imdgpu_set_table2(imdgpu_sys *sys, int which, int ncols, int maxsteps,
+                      const double *table2);
 /* Read an IMD potential file (formats 1 and 2, src/imd_potential.c:161-462)
  * on the host and upload it.  radial as in read_pot_table. */
 int imdgpu_read_table(imdgpu_sys *sys, int which, const char *fname, int radial,
@@ -145,6 +155,48 @@ int imdgpu_reset_cg(imdgpu_sys *sys);
 int imdgpu_cg_step(imdgpu_sys *sys, int steps);
 int imdgpu_cg_relax(imdgpu_sys *sys, double fmax, int maxsteps, int *steps_done,
                     double *fmax_out);
+
+/* Batched CG: many independent periodic cells in one handle (create it with
+ * imdgpu_create, upload tables, then call imdgpu_batch_set_cells instead of
+ * imdgpu_set_box / imdgpu_set_atoms).  natoms[ncells]; boxes 9 per cell
+ * (rows box_x, box_y, box_z); atom arrays grouped by cell, caller order.
+ * Every cell runs IMD's CG (reset_cg, then cg_step = linmin/mnbrak/brent,
+ * cg_calcgamma, set_hg; src/imd_cg.c, src/cg_utils.h) until its max
+ * per-atom |F| <= fmax; one device thread per cell keeps the line-search
+ * state, all cells' force evaluations run together.  New: IMD relaxes one
+ * cell per process. */
+int imdgpu_batch_set_cells(imdgpu_sys *sys, int ncells, const int *natoms,
+                           const double *boxes, const int *number, const int *type,
+                           const double *mass, const double *x);
+int imdgpu_batch_set_margin(imdgpu_sys *sys, double nbl_margin);
+int imdgpu_batch_relax(imdgpu_sys *sys, double fmax, int maxsteps, int max_rounds,
+                       int *rounds_done);
+/* the same in two parts: set up (reset_cg state of every cell), then run up
+ * to max_rounds more rounds; *ndone = cells finished so far */
+int imdgpu_batch_begin(imdgpu_sys *sys, double fmax, int maxsteps);
+int imdgpu_batch_advance(imdgpu_sys *sys, int max_rounds, int *ndone, int *rounds);
+/* neighbour-list rebuilds since imdgpu_batch_begin */
+int imdgpu_batch_rebuilds(imdgpu_sys *sys, long *n);
+/* per cell: final energy, max |F|, CG steps, force calls (nfc), status
+ * (0 converged, 1 not converged, 2 "Too many iterations in brent") */
+int imdgpu_batch_results(imdgpu_sys *sys, double *epot, double *fmax, int *steps, int *nfc,
+                         int *status);
+
+/* Learned starting guess for CG (no counterpart in IMD).  Per directed pair
+ * (i, j) with r_ij < 5.5 A: x_ij = [16 Gaussian RBF(r_ij), rho_i/100] ->
+ * 64 -> 64 -> 1 (SiLU, BF16 weights, FP32 accumulation) = w_ij; predicted
+ * displacement dx_i = sum_j w_ij (r_j - r_i)/r_ij.  Weights: a flat FP32
+ * array of imdgpu_ml_nparam() values (W1[64][32] with inputs >= 17 zero,
+ * b1[64], W2[64][64], b2[64], W3[64], b3). */
+int imdgpu_ml_nparam(void);
+int imdgpu_ml_set_weights(imdgpu_sys *sys, const float *w, int n);
+int imdgpu_ml_get_weights(imdgpu_sys *sys, float *w, int n);
+/* dx (3n, caller order) at the current positions */
+int imdgpu_ml_predict(imdgpu_sys *sys, double *dx);
+/* loss = sum_i |dx_i - target_i|^2 / n and its gradient (grad may be NULL);
+ * lr > 0: one Adam step (beta 0.9 / 0.999) on the weights */
+int imdgpu_ml_train_step(imdgpu_sys *sys, const double *target, double lr, double *loss,
+                         float *grad);
 
 /* Neighbour pairs of the current list: NUMMER of both atoms, image shift of
  * the second (3 ints, in box vectors) and r^2 as used for the list test.

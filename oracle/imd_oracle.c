@@ -26,8 +26,13 @@
 /* tables                                                                    */
 /* ------------------------------------------------------------------------ */
 
+static int g_interp = ORC_QUADRATIC;
+void orc_set_interpolation(int mode) { g_interp = mode; }
+
 static int alloc_info(orc_table_t *pt, int ncols) {
   pt->ncols = ncols;
+  pt->table2 = NULL;
+  pt->mode = g_interp;
   pt->maxsteps = 0;
   pt->begin = (double *)calloc(ncols, sizeof(double));
   pt->end = (double *)calloc(ncols, sizeof(double));
@@ -39,6 +44,7 @@ static int alloc_info(orc_table_t *pt, int ncols) {
 }
 
 void orc_free_table(orc_table_t *pt) {
+  free(pt->table2);
   free(pt->begin);
   free(pt->end);
   free(pt->step);
@@ -60,6 +66,56 @@ static void threepoint(orc_table_t *pt) {
     y[(n + 1) * nc] =
         6 * y[(n - 1) * nc] - 8 * y[(n - 2) * nc] + 3 * y[(n - 3) * nc];
   }
+}
+
+/* init_fourpoint (src/imd_potential.c:1171-1187) */
+static void fourpoint(orc_table_t *pt) {
+  int nc = pt->ncols;
+  for (int col = 0; col < nc; col++) {
+    double *y = pt->table + col;
+    int n = pt->len[col];
+    if (n < 4) continue;
+    y[n * nc] = 4 * y[(n - 1) * nc] - 6 * y[(n - 2) * nc] + 4 * y[(n - 3) * nc] - y[(n - 4) * nc];
+    y[(n + 1) * nc] = 10 * y[(n - 1) * nc] - 20 * y[(n - 2) * nc] + 15 * y[(n - 3) * nc] -
+                      4 * y[(n - 4) * nc];
+  }
+}
+
+/* init_spline (src/imd_potential.c:1197-1246): natural spline at the left
+ * end; zero slope at the right end for radial functions, natural otherwise */
+static void spline(orc_table_t *pt, int radial) {
+  int nc = pt->ncols, size = pt->maxsteps + 2;
+  pt->table2 = (double *)calloc((size_t)nc * size, sizeof(double));
+  double *u = (double *)calloc(size, sizeof(double));
+  for (int col = 0; col < nc; col++) {
+    double *y2 = pt->table2 + col, *y = pt->table + col;
+    int n = pt->len[col];
+    double step = pt->step[col], p, qn, un;
+    y2[0] = u[0] = 0;
+    for (int i = 1; i < n - 1; i++) {
+      p = 0.5 * y2[(i - 1) * nc] + 2.0;
+      y2[i * nc] = -0.5 / p;
+      u[i] = (y[(i + 1) * nc] - 2 * y[i * nc] + y[(i - 1) * nc]) / step;
+      u[i] = (6.0 * u[i] / (2 * step) - 0.5 * u[i - 1]) / p;
+    }
+    if (radial) {
+      qn = 0.5;
+      un = (3.0 / step) * (y[(n - 2) * nc] - y[(n - 1) * nc]) / step;
+    } else {
+      qn = un = 0.0;
+    }
+    y2[(n - 1) * nc] = (un - qn * u[n - 2]) / (qn * y2[(n - 2) * nc] + 1.0);
+    for (int k = n - 2; k >= 0; k--) y2[k * nc] = y2[k * nc] * y2[(k + 1) * nc] + u[k];
+    y[n * nc] = 2 * y[(n - 1) * nc] - y[(n - 2) * nc] + SQR(step) * y2[(n - 1) * nc];
+    y2[n * nc] = 2 * y2[(n - 1) * nc] - y2[(n - 2) * nc];
+  }
+  free(u);
+}
+
+static void init_interp(orc_table_t *pt, int radial) {
+  if (pt->mode == ORC_FOURPOINT) fourpoint(pt);
+  else if (pt->mode == ORC_SPLINE) spline(pt, radial);
+  else threepoint(pt);
 }
 
 /* format 1 (src/imd_potential.c:297-376): lines "r2 v_0 ... v_{ncols-1}",
@@ -208,7 +264,7 @@ int orc_read_table(orc_table_t *pt, const char *fname, int ncols, int radial,
                          : read_format2(pt, in, radial, cellsz, err, errlen);
   fclose(in);
   if (rc) return rc;
-  threepoint(pt);
+  init_interp(pt, radial);
   return 0;
 }
 
@@ -237,7 +293,7 @@ int orc_make_table(orc_table_t *pt, int ncols, const double *begin,
       if (delta != 0.0)
         for (int k = 0; k < len[i]; k++) pt->table[k * ncols + i] -= delta;
     }
-  threepoint(pt);
+  init_interp(pt, radial);
   return 0;
 }
 
@@ -262,8 +318,8 @@ static inline void tab_row(const orc_table_t *pt, int col, int inc, double r2,
   *p2 = ptr[2 * inc];
 }
 
-void orc_pair_int2(const orc_table_t *pt, int col, int inc, double r2,
-                   double *pot, double *grad, int *is_short) {
+static void pair_int_q(const orc_table_t *pt, int col, int inc, double r2,
+                       double *pot, double *grad, int *is_short) {
   double chi, istep, p0, p1, p2;
   tab_row(pt, col, inc, r2, &chi, &istep, &p0, &p1, &p2, is_short);
   double dv = p1 - p0;
@@ -272,8 +328,8 @@ void orc_pair_int2(const orc_table_t *pt, int col, int inc, double r2,
   *grad = 2 * istep * (dv + (chi - 0.5) * d2v);
 }
 
-double orc_val_func2(const orc_table_t *pt, int col, int inc, double r2,
-                     int *is_short) {
+static double val_func_q(const orc_table_t *pt, int col, int inc, double r2,
+                         int *is_short) {
   double chi, istep, p0, p1, p2;
   tab_row(pt, col, inc, r2, &chi, &istep, &p0, &p1, &p2, is_short);
   double dv = p1 - p0;
@@ -281,13 +337,85 @@ double orc_val_func2(const orc_table_t *pt, int col, int inc, double r2,
   return p0 + chi * dv + 0.5 * chi * (chi - 1) * d2v;
 }
 
-double orc_deriv_func2(const orc_table_t *pt, int col, int inc, double r2,
-                       int *is_short) {
+static double deriv_func_q(const orc_table_t *pt, int col, int inc, double r2,
+                           int *is_short) {
   double chi, istep, p0, p1, p2;
   tab_row(pt, col, inc, r2, &chi, &istep, &p0, &p1, &p2, is_short);
   double dv = p1 - p0;
   double d2v = p2 - 2 * p1 + p0;
   return 2 * istep * (dv + (chi - 0.5) * d2v);
+}
+
+/* index of the 4-point and spline macros: r2a as for the quadratic one */
+static double r2a_of(const orc_table_t *pt, int col, double r2, int *is_short) {
+  double r2a = OMIN(r2, pt->end[col]);
+  r2a = r2a - pt->begin[col];
+  if (r2a < 0) {
+    r2a = 0;
+    *is_short = 1;
+  }
+  return r2a * pt->invstep[col];
+}
+
+/* PAIR_INT3 / VAL_FUNC3 / DERIV_FUNC3 (src/potaccess.h:365-410, :503-539,
+ * :630-666): cubic through rows k-1..k+2, k = max(floor, 1) */
+static void four_eval(const orc_table_t *pt, int col, int inc, double r2, double *pot,
+                      double *grad, int *is_short) {
+  double istep = pt->invstep[col];
+  double r2a = r2a_of(pt, col, r2, is_short);
+  int k = (int)r2a;
+  if (k < 1) k = 1;
+  double chi = r2a - k;
+  double fac0 = -(1.0 / 6.0) * chi * (chi - 1.0) * (chi - 2.0);
+  double fac1 = 0.5 * (chi * chi - 1.0) * (chi - 2.0);
+  double fac2 = -0.5 * chi * (chi + 1.0) * (chi - 2.0);
+  double fac3 = (1.0 / 6.0) * chi * (chi * chi - 1.0);
+  double dfac0 = -(1.0 / 6.0) * ((3.0 * chi - 6.0) * chi + 2.0);
+  double dfac1 = 0.5 * ((3.0 * chi - 4.0) * chi - 1.0);
+  double dfac2 = -0.5 * ((3.0 * chi - 2.0) * chi - 2.0);
+  double dfac3 = 1.0 / 6.0 * (3.0 * chi * chi - 1.0);
+  const double *ptr = pt->table + (long)(k - 1) * inc + col;
+  double p0 = ptr[0], p1 = ptr[inc], p2 = ptr[2 * inc], p3 = ptr[3 * inc];
+  if (pot) *pot = fac0 * p0 + fac1 * p1 + fac2 * p2 + fac3 * p3;
+  if (grad) *grad = 2 * istep * (dfac0 * p0 + dfac1 * p1 + dfac2 * p2 + dfac3 * p3);
+}
+
+/* PAIR_INT_SP / VAL_FUNC_SP / DERIV_FUNC_SP (src/potaccess.h:421-457,
+ * :547-582, :675-710) */
+static void spline_eval(const orc_table_t *pt, int col, int inc, double r2, double *pot,
+                        double *grad, int *is_short) {
+  double istep = pt->invstep[col], step = pt->step[col];
+  double r2a = r2a_of(pt, col, r2, is_short);
+  int k = (int)r2a;
+  double b = r2a - k, a = 1.0 - b;
+  k = k * inc + col;
+  double p1 = pt->table[k], d21 = pt->table2[k];
+  k += inc;
+  double p2 = pt->table[k], d22 = pt->table2[k];
+  double a2 = a * a - 1, b2 = b * b - 1, st6 = step / 6;
+  if (pot) *pot = a * p1 + b * p2 + (a * a2 * d21 + b * b2 * d22) * st6 * step;
+  if (grad) *grad = 2 * ((p2 - p1) * istep + ((3 * b2 + 2) * d22 - (3 * a2 + 2) * d21) * st6);
+}
+
+void orc_pair_int2(const orc_table_t *pt, int col, int inc, double r2, double *pot,
+                   double *grad, int *is_short) {
+  if (pt->mode == ORC_FOURPOINT) four_eval(pt, col, inc, r2, pot, grad, is_short);
+  else if (pt->mode == ORC_SPLINE) spline_eval(pt, col, inc, r2, pot, grad, is_short);
+  else pair_int_q(pt, col, inc, r2, pot, grad, is_short);
+}
+double orc_val_func2(const orc_table_t *pt, int col, int inc, double r2, int *is_short) {
+  double v;
+  if (pt->mode == ORC_FOURPOINT) four_eval(pt, col, inc, r2, &v, NULL, is_short);
+  else if (pt->mode == ORC_SPLINE) spline_eval(pt, col, inc, r2, &v, NULL, is_short);
+  else v = val_func_q(pt, col, inc, r2, is_short);
+  return v;
+}
+double orc_deriv_func2(const orc_table_t *pt, int col, int inc, double r2, int *is_short) {
+  double g;
+  if (pt->mode == ORC_FOURPOINT) four_eval(pt, col, inc, r2, NULL, &g, is_short);
+  else if (pt->mode == ORC_SPLINE) spline_eval(pt, col, inc, r2, NULL, &g, is_short);
+  else g = deriv_func_q(pt, col, inc, r2, is_short);
+  return g;
 }
 
 void orc_pair_int2_batch(const orc_table_t *pt, int col, int inc, int n,
@@ -903,11 +1031,11 @@ static double fonedim(orc_sys_t *s, double alpha) {
 /* brent (src/cg_utils.h:34-114), IMD's variant: a=ax, b=bx, x=w=v=bx */
 static int brent(orc_sys_t *s, double ax, double bx, double cx, double fa,
                  double fb, double fc, double *alphamin) {
-  (void)cx; (void)fa; (void)fc;
+  (void)fa; (void)fc;
   double a, b, etemp, fu, fv, fw, fx, p, q, r, tol1, tol2, u, v, w, x, xm;
   double e = 0.0, d = 0.0, tol = s->linmin_tol;
   a = ax;
-  b = bx;
+  b = s->cg_brent_full ? cx : bx;
   x = w = v = bx;
   fw = fv = fx = fb;
   for (int iter = 1; iter <= s->linmin_maxsteps; iter++) {

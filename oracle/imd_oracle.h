@@ -32,7 +32,16 @@ typedef struct {
   double *begin, *end, *step, *invstep;
   int    *len;
   double *table;      /* (maxsteps + 2) * ncols */
+  double *table2;     /* spline second derivatives (ORC_SPLINE only) */
+  int     mode;       /* ORC_QUADRATIC, ORC_FOURPOINT, ORC_SPLINE */
 } orc_table_t;
+
+/* interpolation of the tables: the default 3-point quadratic
+ * (src/potaccess.h:323-354), 4-point cubic (`4point` targets, :365-410) and
+ * cubic spline (`spline` targets, :421-457) */
+enum { ORC_QUADRATIC = 0, ORC_FOURPOINT = 1, ORC_SPLINE = 2 };
+/* set before reading tables: how read_pot_table initialises them */
+void orc_set_interpolation(int mode);
 
 /* read_pot_table (src/imd_potential.c:161-282), formats 1 and 2
  * (:297-376, :394-462) and init_threepoint (:1256-1272).
@@ -74,6 +83,8 @@ typedef struct {
   int    linmin_maxsteps;
   double linmin_tol, linmin_dmax, linmin_dmin, cg_glimit, cg_zeps;
   int    cg_fr, cg_reset_int;
+  int    cg_brent_full;       /* 1: brent over the whole bracket [a, c] (Numerical
+                                 Recipes); 0: IMD's [a, b] (src/cg_utils.h:45-46) */
 
   orc_table_t pair, rho, embed;
   double cellsz;              /* neighbour-list radius^2 after init */

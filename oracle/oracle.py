@@ -21,7 +21,15 @@ _ip = C.POINTER(C.c_int)
 
 class Table(C.Structure):
     _fields_ = [("ncols", C.c_int), ("maxsteps", C.c_int), ("begin", _dp), ("end", _dp),
-                ("step", _dp), ("invstep", _dp), ("len", _ip), ("table", _dp)]
+                ("step", _dp), ("invstep", _dp), ("len", _ip), ("table", _dp),
+                ("table2", _dp), ("mode", C.c_int)]
+
+QUADRATIC, FOURPOINT, SPLINE = 0, 1, 2
+
+
+def set_interpolation(mode: int) -> None:
+    """How tables read afterwards are initialised and interpolated."""
+    lib().orc_set_interpolation(mode)
 
 
 class Sys(C.Structure):
@@ -31,6 +39,7 @@ class Sys(C.Structure):
         ("restrictions", _dp), ("linmin_maxsteps", C.c_int), ("linmin_tol", C.c_double),
         ("linmin_dmax", C.c_double), ("linmin_dmin", C.c_double), ("cg_glimit", C.c_double),
         ("cg_zeps", C.c_double), ("cg_fr", C.c_int), ("cg_reset_int", C.c_int),
+        ("cg_brent_full", C.c_int),
         ("pair", Table), ("rho", Table), ("embed", Table), ("cellsz", C.c_double),
         ("n", C.c_int), ("number", _ip), ("type", _ip), ("mass", _dp), ("x", _dp),
         ("p", _dp), ("f", _dp), ("epot", _dp), ("eam_rho", _dp), ("eam_df", _dp),
@@ -81,6 +90,7 @@ def lib() -> C.CDLL:
         L.orc_max_atom_force.restype = C.c_double
         L.orc_pairs.argtypes = [C.POINTER(Sys), C.c_long, _ip, _ip, _ip, _dp]
         L.orc_pairs.restype = C.c_long
+        L.orc_set_interpolation.argtypes = [C.c_int]
         _lib = L
     return _lib
 

@@ -17,6 +17,10 @@ Fixtures (all sorted by atom number):
   alloy_pert  binary Sutton-Chen Cu/Ni fcc 6^3 a0=3.57 (864 atoms)
   tri_cg      strained (triclinic) Cu cell 3x4x3 with a vacancy and noise:
               forces and a CG relaxation to max |F| <= 1e-4 eV/A
+  cu_pert_spline, cu_pert_4point   cu_pert with IMD's spline / 4-point
+              table interpolation (targets with `spline`, `4point`)
+  defect_cg_spline  a defect cell of the batched-relaxation generator
+              (1005 atoms), CG to max |F| <= 1e-4 eV/A with spline tables
 """
 from __future__ import annotations
 
@@ -224,6 +228,27 @@ def main() -> None:
     d.update(cg_steps=int(cg[0]), cg_nfc=int(cg[1]), cg_epot=cg[2], cg_fmax=cg[3],
              cg_x=stf["x"])
     out["tri_cg"] = d
+
+    # ---- spline and 4-point interpolation ----
+    cfg = os.path.join(tmp, "cu_pert.cfg")
+    p = os.path.join(tmp, "cu_pert.param")
+    out["cu_pert_spline"], _, _ = forces_case("cu_pert_spline", "nve_nbl_eam_spline", p)
+    out["cu_pert_4point"], _, _ = forces_case("cu_pert_4point", "nve_nbl_eam_4point", p)
+    rng = np.random.default_rng(4)
+    cells = [wl.defect_cell(rng) for _ in range(3)]
+    dc = cells[2]
+    cfg = os.path.join(tmp, "defect.cfg")
+    wl.write_config(cfg, dc.box, dc.number, dc.types, dc.mass, dc.x)
+    p = os.path.join(tmp, "defect.param")
+    eam_param(p, cfg, cu, 1, 63.546, box_from_header=1, ensemble="cg")
+    d, _, _ = forces_case("defect", "cg_nbl_eam_spline", p)
+    pre = os.path.join(tmp, "defect")
+    run("cg_nbl_eam_spline", p, "cg", pre, 20000, 1e-4)
+    cg = np.loadtxt(pre + ".cg")
+    stf = load_state(pre + ".final")
+    d.update(cg_steps=int(cg[0]), cg_nfc=int(cg[1]), cg_epot=cg[2], cg_fmax=cg[3],
+             cg_x=stf["x"], cg_seconds=cg[4])
+    out["defect_cg_spline"] = d
 
     for name, d in out.items():
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **d)

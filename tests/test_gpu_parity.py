@@ -27,9 +27,9 @@ def rel_rms(a, b):
     return np.sqrt(np.mean((a - b) ** 2)) / np.sqrt(np.mean(b ** 2))
 
 
-def gpu_system(g, tab, eam, nt, skin, x=None, p=None, precision=0):
+def gpu_system(g, tab, eam, nt, skin, x=None, p=None, precision=0, interpolation=0):
     from imd_gb300 import api
-    s = api.GpuSystem(nt, api.EAM2 if eam else api.PAIR, precision)
+    s = api.GpuSystem(nt, api.EAM2 if eam else api.PAIR, precision, interpolation)
     s.read_tables(tables(tab), default_format=2 if eam else 1)
     s.set_box(g["box"], (1, 1, 1), skin)
     s.set_atoms(g["number"], g["type"], g["mass"], g["x"] if x is None else x, p)
@@ -265,3 +265,48 @@ def test_graph_replay_matches_direct_launches(precision):
     np.testing.assert_allclose(ea, eb, rtol=1e-10)
     np.testing.assert_allclose(ka, kb, rtol=1e-9)
     assert a.scalars().nbl_count == b.scalars().nbl_count
+
+
+# IMD's `spline` and `4point` table interpolations (reference built with
+# -DSPLINE / -DFOURPOINT): interpolation mode 2 / 1
+CUBIC = {"cu_pert_spline": 2, "cu_pert_4point": 1, "defect_cg_spline": 2}
+
+
+@pytest.mark.parametrize("name", list(CUBIC))
+def test_cubic_interpolation_forces_match_reference(name):
+    g = golden(name)
+    s = gpu_system(g, "cu", 1, 1, 0.4, interpolation=CUBIC[name])
+    assert s.calc_forces(0) == 0
+    a = s.get_atoms()
+    sc = s.scalars()
+    assert rel_rms(a["f"], g["f"]) < 1e-11
+    assert np.max(np.abs(a["epot"] - g["epot"])) <= 1e-11 * np.max(np.abs(g["epot"]))
+    assert abs(sc.tot_pot_energy - g["epot_total"]) <= 1e-12 * abs(g["epot_total"])
+    assert abs(sc.virial - g["virial"]) <= 1e-12 * abs(g["virial"])
+    assert np.max(np.abs(a["rho"] - g["rho"])) <= 1e-11 * np.max(g["rho"])
+    assert np.max(np.abs(a["df"] - g["df"])) <= 1e-11 * np.max(np.abs(g["df"]))
+
+
+@pytest.mark.parametrize("name", ["cu_pert_spline", "cu_pert_4point"])
+def test_cubic_interpolation_mixed_force_error(name):
+    from imd_gb300 import api
+    g = golden(name)
+    s = gpu_system(g, "cu", 1, 1, 0.4, precision=api.MIXED, interpolation=CUBIC[name])
+    s.calc_forces(0)
+    err = rel_rms(s.get_atoms()["f"], g["f"])
+    assert err < 1e-5, err
+    de = abs(s.scalars().tot_pot_energy - g["epot_total"]) / abs(g["epot_total"])
+    assert de < 1e-6, de
+
+
+def test_spline_cg_relaxation_matches_reference():
+    """With spline tables the forces are smooth and IMD's CG reaches
+    1e-4 eV/A on a defect cell; the device run ends at the reference's
+    energy."""
+    g = golden("defect_cg_spline")
+    s = gpu_system(g, "cu", 1, 1, 0.4, interpolation=2)
+    steps, fm = s.cg_relax(1e-4)
+    assert fm <= 1e-4
+    e = s.scalars().tot_pot_energy
+    assert abs(e - float(g["cg_epot"])) / len(g["x"]) <= 1e-6
+    assert 0.5 * int(g["cg_steps"]) <= steps <= 2 * int(g["cg_steps"]) + 3

