@@ -110,6 +110,9 @@ def lib() -> C.CDLL:
         L.imdgpu_ml_get_weights.argtypes = [vp, fp, C.c_int]
         L.imdgpu_ml_predict.argtypes = [vp, _dp]
         L.imdgpu_ml_train_step.argtypes = [vp, _dp, C.c_double, _dp, fp]
+        L.imdgpu_batch_ml_start.argtypes = [vp, _ip, _dp, _dp]
+        L.imdgpu_ml_get_adam.argtypes = [vp, fp, fp, _ip]
+        L.imdgpu_ml_set_adam.argtypes = [vp, fp, fp, C.c_int]
         _lib = L
     return _lib
 
@@ -305,6 +308,22 @@ class GpuSystem:
         _check(lib().imdgpu_ml_get_weights(self.h, _p(w, C.c_float), len(w)), "ml_get_weights")
         return w
 
+    def ml_get_adam(self):
+        """(m, v, step): the Adam state of the weights."""
+        k = lib().imdgpu_ml_nparam()
+        m = np.empty(k, np.float32)
+        v = np.empty(k, np.float32)
+        t = C.c_int(0)
+        _check(lib().imdgpu_ml_get_adam(self.h, _p(m, C.c_float), _p(v, C.c_float),
+                                        C.byref(t)), "ml_get_adam")
+        return m, v, t.value
+
+    def ml_set_adam(self, m, v, step: int) -> None:
+        m = np.ascontiguousarray(m, np.float32)
+        v = np.ascontiguousarray(v, np.float32)
+        _check(lib().imdgpu_ml_set_adam(self.h, _p(m, C.c_float), _p(v, C.c_float), int(step)),
+               "ml_set_adam")
+
     def ml_predict(self):
         """Predicted displacements (n,3), caller order, at the current positions."""
         dx = np.empty((self.n, 3))
@@ -374,6 +393,18 @@ class GpuBatch(GpuSystem):
         _check(lib().imdgpu_batch_advance(self.h, max_rounds, C.byref(nd), C.byref(r)),
                "batch_advance")
         return nd.value, r.value
+
+    def ml_start(self):
+        """Learned start (weights set with ml_set_weights): every cell keeps
+        its predicted positions where they lower its energy.  Returns
+        (used, e_start, e_pred) per cell."""
+        k = self.ncells
+        used = np.empty(k, np.int32)
+        e0 = np.empty(k)
+        e1 = np.empty(k)
+        _check(lib().imdgpu_batch_ml_start(self.h, _p(used, C.c_int), _p(e0), _p(e1)),
+               "batch_ml_start")
+        return used, e0, e1
 
     def rebuilds(self) -> int:
         n = C.c_long(0)

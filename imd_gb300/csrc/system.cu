@@ -155,6 +155,10 @@ struct imdgpu_sys {
   int ml_have = 0;
   int ml_dx_cap = 0;
   int ml_adam_step = 0;
+  double4 *ml_save = nullptr;      // batch learned start: positions by caller index
+  double *ml_ecell = nullptr;      // 2 per cell: energy at the start, at the prediction
+  int *ml_sel = nullptr;           // per cell: 1 = the prediction is kept
+  int ml_save_cap = 0, ml_cell_cap = 0;
 
   // CUDA graph of one full chunk of NVE steps, re-captured when buffers move
   cudaGraphExec_t gexec = nullptr;
@@ -1423,6 +1427,7 @@ int imdgpu_destroy(imdgpu_sys *s) {
   dfree(s->ml_w); dfree(s->ml_m); dfree(s->ml_v); dfree(s->ml_grad); dfree(s->ml_wb);
   dfree(s->ml_pairs); dfree(s->ml_np); dfree(s->ml_dx); dfree(s->ml_target); dfree(s->ml_dldx);
   dfree(s->ml_loss);
+  dfree(s->ml_save); dfree(s->ml_ecell); dfree(s->ml_sel);
   dfree(s->d_atom_sys); dfree(s->d_aoff); dfree(s->d_sgdim); dfree(s->d_scdim); dfree(s->d_scoff);
   dfree(s->d_sys_done); dfree(s->d_ndone); dfree(s->d_sbox); dfree(s->d_stbox); dfree(s->d_cs);
   dfree(s->d_maxd);
@@ -2636,6 +2641,46 @@ __global__ void k_apply_dx(SysView v, const float *dx, double sign, const int *s
   x.z += sign * dx[3 * s + 2];
   v.pos[s] = x;
 }
+// positions of the real atoms by caller index (save) and back for the atoms
+// of the cells whose flag is 0 (restore); the type in .w stays with the slot
+__global__ void k_save_by_orig(SysView v, double4 *save) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= v.n) return;
+  save[v.orig[s]] = v.pos[s];
+}
+__global__ void k_restore_by_orig(SysView v, const double4 *save, const int *keep) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= v.n) return;
+  if (keep[v.atom_sys[s]]) return;
+  const double4 o = save[v.orig[s]];
+  double4 x = v.pos[s];
+  x.x = o.x;
+  x.y = o.y;
+  x.z = o.z;
+  v.pos[s] = x;
+}
+// energy of every cell of a batch from the per-atom shares in frc.w, in a
+// fixed order (one block per cell)
+__global__ void __launch_bounds__(256) k_cell_energy(const double4 *frc, const int *aoff,
+                                                     double *e, int stride) {
+  const int c = blockIdx.x;
+  double acc = 0.0;
+  for (int i = aoff[c] + threadIdx.x; i < aoff[c + 1]; i += blockDim.x) acc += frc[i].w;
+  __shared__ double sh[8];
+  acc = warp_sum(acc);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double r = 0.0;
+    for (int k = 0; k < 8; k++) r += sh[k];
+    e[stride * c] = r;
+  }
+}
+// keep the prediction of a cell when its energy is below the start's
+__global__ void k_ml_select(const double *ecell, int nsys, int *keep) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < nsys) keep[c] = ecell[2 * c + 1] < ecell[2 * c] ? 1 : 0;
+}
 }  // namespace imdgpu
 
 static int ml_ensure(imdgpu_sys *s) {
@@ -2721,6 +2766,25 @@ int imdgpu_ml_get_weights(imdgpu_sys *s, float *w, int n) {
   return IMDGPU_OK;
 }
 
+int imdgpu_ml_get_adam(imdgpu_sys *s, float *m, float *v, int *step) {
+  if (!s || !s->ml_have) return fail(IMDGPU_ERR_STATE, "no weights");
+  const int np = ml_nparam();
+  if (m) CK(cudaMemcpy(m, s->ml_m, sizeof(float) * np, cudaMemcpyDeviceToHost));
+  if (v) CK(cudaMemcpy(v, s->ml_v, sizeof(float) * np, cudaMemcpyDeviceToHost));
+  if (step) *step = s->ml_adam_step;
+  return IMDGPU_OK;
+}
+
+int imdgpu_ml_set_adam(imdgpu_sys *s, const float *m, const float *v, int step) {
+  if (!s || !s->ml_have) return fail(IMDGPU_ERR_STATE, "no weights");
+  if (!m || !v || step < 0) return fail(IMDGPU_ERR_ARG, "adam state");
+  const int np = ml_nparam();
+  CK(cudaMemcpy(s->ml_m, m, sizeof(float) * np, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(s->ml_v, v, sizeof(float) * np, cudaMemcpyHostToDevice));
+  s->ml_adam_step = step;
+  return IMDGPU_OK;
+}
+
 // predicted displacement of every atom (caller order) at the current positions
 int imdgpu_ml_predict(imdgpu_sys *s, double *dx) {
   if (!s || !s->ml_have) return fail(IMDGPU_ERR_STATE, "no weights");
@@ -2760,6 +2824,61 @@ int imdgpu_ml_train_step(imdgpu_sys *s, const double *target, double lr, double 
   if (loss) CK(cudaMemcpyAsync(loss, s->ml_loss, sizeof(double), cudaMemcpyDeviceToHost, s->st));
   if (grad_out) CK(cudaMemcpyAsync(grad_out, s->ml_grad, sizeof(float) * np, cudaMemcpyDeviceToHost, s->st));
   CK(cudaStreamSynchronize(s->st));
+  return IMDGPU_OK;
+}
+
+// Learned start of a batch: energy of every cell at its current positions,
+// the predicted displacement, the energy at the displaced positions, and per
+// cell the better of the two (the prediction only where it lowers the
+// energy).  The neighbour list is rebuilt for the chosen positions by the
+// next calc_forces / imdgpu_batch_begin.
+int imdgpu_batch_ml_start(imdgpu_sys *s, int *used, double *e_start, double *e_pred) {
+  if (!s || s->nsys < 1) return fail(IMDGPU_ERR_STATE, "imdgpu_batch_set_cells first");
+  if (!s->ml_have) return fail(IMDGPU_ERR_STATE, "no weights");
+  if (s->brun) {
+    // a batch relaxation was begun on these cells: they may be marked done
+    CK(cudaMemset(s->d_sys_done, 0, sizeof(int) * s->nsys));
+  }
+  int rc = ml_prepare_pairs(s);  // forces, rho and the list at the start positions
+  if (rc) return rc;
+  const int ns = s->nsys;
+  if (s->ml_cell_cap < ns) {
+    dfree(s->ml_ecell);
+    dfree(s->ml_sel);
+    CK(dalloc(&s->ml_ecell, 2 * (size_t)ns));
+    CK(dalloc(&s->ml_sel, ns));
+    s->ml_cell_cap = ns;
+  }
+  if (s->ml_save_cap < s->n) {
+    dfree(s->ml_save);
+    CK(dalloc(&s->ml_save, s->n));
+    s->ml_save_cap = s->n;
+  }
+  SysView v = view(s);
+  k_cell_energy<<<ns, 256, 0, s->st>>>(s->frc, s->d_aoff, s->ml_ecell, 2);
+  if ((rc = ml_forward(s))) return rc;
+  k_save_by_orig<<<nblk(s->n, 256), 256, 0, s->st>>>(v, s->ml_save);
+  k_apply_dx<<<nblk(s->n, 256), 256, 0, s->st>>>(v, s->ml_dx, 1.0, nullptr);
+  CK(cudaGetLastError());
+  int one = 1;
+  CK(cudaMemcpyAsync(&s->dsc->rebuild, &one, sizeof(int), cudaMemcpyHostToDevice, s->st));
+  if ((rc = calc_forces_sync(s))) return rc;
+  v = view(s);
+  k_cell_energy<<<ns, 256, 0, s->st>>>(s->frc, s->d_aoff, s->ml_ecell + 1, 2);
+  k_ml_select<<<nblk(ns, 128), 128, 0, s->st>>>(s->ml_ecell, ns, s->ml_sel);
+  k_restore_by_orig<<<nblk(s->n, 256), 256, 0, s->st>>>(v, s->ml_save, s->ml_sel);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(&s->dsc->rebuild, &one, sizeof(int), cudaMemcpyHostToDevice, s->st));
+  std::vector<double> ec(2 * (size_t)ns);
+  std::vector<int> sel(ns);
+  CK(cudaMemcpyAsync(ec.data(), s->ml_ecell, sizeof(double) * 2 * ns, cudaMemcpyDeviceToHost, s->st));
+  CK(cudaMemcpyAsync(sel.data(), s->ml_sel, sizeof(int) * ns, cudaMemcpyDeviceToHost, s->st));
+  CK(cudaStreamSynchronize(s->st));
+  for (int c = 0; c < ns; c++) {
+    if (used) used[c] = sel[c];
+    if (e_start) e_start[c] = ec[2 * c];
+    if (e_pred) e_pred[c] = ec[2 * c + 1];
+  }
   return IMDGPU_OK;
 }
 

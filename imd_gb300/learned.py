@@ -1,0 +1,193 @@
+"""Learned starting guess for batched CG relaxation: data, training, use.
+
+No counterpart in IMD, which starts every relaxation from the positions it
+reads.  Every computation runs on the GPU through libimdgpu; this module is
+the host-side sequencing only:
+
+1. data: defect cells from the batched workload's generator are relaxed by
+   the plain batched CG (imdgpu_batch_*); the target of every atom is its
+   displacement, relaxed minus unrelaxed, unwrapped by the minimum image of
+   its cell's box;
+2. training: Adam on the per-pair MLP (imdgpu_ml_train_step: the project's
+   own forward, backward and Adam kernels), one step per group of
+   `batch_cells` cells; each group stays resident as one GpuBatch with its
+   atoms at the unrelaxed positions, and the model's weights and Adam state
+   move between the groups' handles;
+3. use: imdgpu_batch_ml_start moves every cell to its predicted start where
+   that lowers the cell's energy, and the plain batched CG finishes every
+   cell to the same force tolerance.
+"""
+from __future__ import annotations
+
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import api
+
+H, K1, NIN = 64, 32, 17
+OFF_W1 = 0
+OFF_B1 = OFF_W1 + H * K1
+OFF_W2 = OFF_B1 + H
+OFF_B2 = OFF_W2 + H * H
+OFF_W3 = OFF_B2 + H
+OFF_B3 = OFF_W3 + H
+NPARAM = OFF_B3 + 1
+
+# Table interpolation of the batched relaxations: IMD's `spline` target.  With
+# the default 3-point quadratic interpolation the force jumps by about
+# 1e-4 eV/A where a pair crosses a grid point of a 2000-point table (the
+# interpolant is continuous, its derivative is not), which is the size of
+# the 1e-4 eV/A stopping force, and CG then spends most of its force calls
+# in the last factor of two of the max force.
+BATCH_INTERPOLATION = api.SPLINE
+
+
+def init_weights(seed: int = 0) -> np.ndarray:
+    """Initial parameters in the layout of imdgpu_ml_set_weights: normal
+    weights scaled by 1/sqrt(fan-in) (inputs 17..31 of W1 are padding and
+    stay zero), zero biases, a small output layer so that the first
+    prediction is close to no displacement."""
+    rng = np.random.default_rng(seed)
+    w = np.zeros(NPARAM, np.float32)
+    w1 = rng.standard_normal((H, K1)) / np.sqrt(NIN)
+    w1[:, NIN:] = 0.0
+    w[OFF_W1:OFF_B1] = w1.ravel()
+    w[OFF_W2:OFF_B2] = (rng.standard_normal((H, H)) / np.sqrt(H)).ravel()
+    w[OFF_W3:OFF_B3] = 0.01 * rng.standard_normal(H)
+    return w
+
+
+def min_image(d: np.ndarray, box: np.ndarray) -> np.ndarray:
+    """Displacements d (n,3) reduced to the nearest image of the periodic
+    box whose rows are the box vectors."""
+    s = d @ np.linalg.inv(box)
+    s -= np.round(s)
+    return s @ box
+
+
+def make_batch(tables, cells, precision=api.FP64,
+               interpolation: int = BATCH_INTERPOLATION) -> api.GpuBatch:
+    b = api.GpuBatch(1, api.EAM2, precision, interpolation)
+    b.read_tables(tables)
+    b.set_cells(cells)
+    return b
+
+
+@dataclass
+class RelaxResult:
+    seconds: float
+    epot: np.ndarray
+    fmax: np.ndarray
+    nfc: np.ndarray
+    steps: np.ndarray
+    status: np.ndarray
+    rounds: int
+    used: np.ndarray | None = None
+    e_start: np.ndarray | None = None
+    e_pred: np.ndarray | None = None
+    positions: list = field(default_factory=list)
+
+    @property
+    def relaxations_per_s(self) -> float:
+        return len(self.epot) / self.seconds
+
+
+def relax(tables, cells, fmax: float = 1e-4, weights=None, precision=api.FP64,
+          keep_positions: bool = False, chunk_rounds: int = 4096,
+          interpolation: int = BATCH_INTERPOLATION) -> RelaxResult:
+    """Relax every cell with the batched CG, from the learned start when
+    `weights` are given.  The wall time covers the learned start (its two
+    force calls and the prediction) and the CG, not the upload of the cells.
+    Force calls per cell include the learned start's two."""
+    b = make_batch(tables, cells, precision, interpolation)
+    used = e0 = e1 = None
+    api.lib()
+    b.calc_forces(0)  # first list and geometry outside the timed region
+    t0 = time.perf_counter()
+    if weights is not None:
+        b.ml_set_weights(weights)
+        used, e0, e1 = b.ml_start()
+    b.begin(fmax)
+    rounds = 0
+    while True:
+        nd, rounds = b.advance(chunk_rounds)
+        if nd >= len(cells):
+            break
+        if rounds > 10_000_000:
+            raise RuntimeError("batched CG did not finish")
+    sec = time.perf_counter() - t0
+    r = b.results()
+    nfc = r["nfc"] + (2 if weights is not None else 0)
+    pos = b.positions() if keep_positions else []
+    b.close()
+    return RelaxResult(sec, r["epot"], r["fmax"], nfc, r["steps"], r["status"], rounds,
+                       used, e0, e1, pos)
+
+
+def targets(cells, relaxed_positions) -> list:
+    """Per cell (n,3) displacements relaxed - unrelaxed, minimum image."""
+    return [min_image(xr - c.x, np.asarray(c.box)) for c, xr in zip(cells, relaxed_positions)]
+
+
+class Trainer:
+    """Adam training of the per-pair MLP on resident groups of cells."""
+
+    def __init__(self, tables, cells, disp, batch_cells: int = 64, seed: int = 0,
+                 weights=None, interpolation: int = BATCH_INTERPOLATION):
+        self.groups = []
+        order = np.arange(len(cells))
+        for g0 in range(0, len(cells), batch_cells):
+            idx = order[g0:g0 + batch_cells]
+            gc = [cells[i] for i in idx]
+            b = make_batch(tables, gc, interpolation=interpolation)
+            t = np.ascontiguousarray(np.concatenate([disp[i] for i in idx]), np.float64)
+            self.groups.append((b, t))
+        self.w = init_weights(seed) if weights is None else np.asarray(weights, np.float32)
+        self.m = np.zeros(NPARAM, np.float32)
+        self.v = np.zeros(NPARAM, np.float32)
+        self.step = 0
+        self.rng = np.random.default_rng(seed + 1)
+        self.history = []
+
+    def _load(self, b):
+        b.ml_set_weights(self.w)
+        b.ml_set_adam(self.m, self.v, self.step)
+
+    def _store(self, b):
+        self.w = b.ml_get_weights()
+        self.m, self.v, self.step = b.ml_get_adam()
+
+    def epoch(self, lr: float = 1e-3) -> float:
+        """One pass over the groups in random order; mean loss before each
+        group's step."""
+        losses = []
+        if len(self.groups) == 1:
+            b, t = self.groups[0]
+            if self.step == 0:
+                self._load(b)
+            losses.append(b.ml_train_step(t, lr))
+            self._store(b)
+        else:
+            for gi in self.rng.permutation(len(self.groups)):
+                b, t = self.groups[gi]
+                self._load(b)
+                losses.append(b.ml_train_step(t, lr))
+                self._store(b)
+        m = float(np.mean(losses))
+        self.history.append(m)
+        return m
+
+    def loss(self) -> float:
+        """Mean loss over all groups at the current weights (no update)."""
+        out = []
+        for b, t in self.groups:
+            b.ml_set_weights(self.w)
+            out.append(b.ml_train_step(t, 0.0))
+        return float(np.mean(out))
+
+    def close(self):
+        for b, _ in self.groups:
+            b.close()
+        self.groups = []

@@ -1,0 +1,119 @@
+"""Train the learned CG start on the GPU and store its weights.
+
+    python -m imd_gb300.train_start [--train-cells 2048] [--epochs 20]
+        [--batch-cells 64] [--lr 1e-3] [--out imd_gb300/data/start_mlp.npz]
+        [--eval-cells 512]
+
+Training cells come from the batched-relaxation generator with seed 5, held-out
+cells with seed 6 (single-species Sutton-Chen Cu, 1-4 vacancies or <100>
+dumbbells per cell, +-2% strain, 0.05 A noise, 500-20,000 atoms).  Every
+training cell is relaxed by the plain batched CG to max |F| <= 1e-4 eV/A,
+512 cells per batch.  Its relaxed-minus-unrelaxed displacements are the
+targets.  Adam then trains the per-pair MLP on the device for `epochs`
+passes over groups of `batch_cells` cells.  The output file holds the FP32
+weights (`w`) and a record of the run; imd_gb300/learned.py and bench.py
+load it.  With --eval-cells > 0 the held-out cells are relaxed once plainly
+and once from the learned start, and the comparison is stored too.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+if os.path.dirname(HERE) not in sys.path:
+    sys.path.insert(0, os.path.dirname(HERE))
+
+from imd_gb300 import learned, workloads as wl  # noqa: E402
+
+DEFAULT_OUT = os.path.join(HERE, "data", "start_mlp.npz")
+
+
+def relax_targets(tabs, cells, chunk: int = 512):
+    """Plain batched CG of `cells` in batches of `chunk`; displacement targets."""
+    disp, stats = [], []
+    for c0 in range(0, len(cells), chunk):
+        part = cells[c0:c0 + chunk]
+        r = learned.relax(tabs, part, keep_positions=True)
+        bad = np.flatnonzero(r.status != 0)
+        if len(bad):
+            raise RuntimeError("plain CG did not converge for cells %s" % (bad + c0).tolist())
+        disp += learned.targets(part, r.positions)
+        stats.append({"cells": len(part), "seconds": r.seconds, "rounds": r.rounds,
+                      "nfc_mean": float(r.nfc.mean())})
+        print("relaxed %d/%d cells: %.1f s, %d rounds, %.0f force calls per cell"
+              % (c0 + len(part), len(cells), r.seconds, r.rounds, r.nfc.mean()), flush=True)
+    return disp, stats
+
+
+def evaluate(tabs, cells, w):
+    plain = learned.relax(tabs, cells)
+    ml = learned.relax(tabs, cells, weights=w)
+    n = np.array([c.n for c in cells])
+    de = (ml.epot - plain.epot) / n
+    return {
+        "cells": len(cells), "atoms": int(n.sum()),
+        "plain_relaxations_per_s": plain.relaxations_per_s,
+        "learned_relaxations_per_s": ml.relaxations_per_s,
+        "speedup": ml.relaxations_per_s / plain.relaxations_per_s,
+        "plain_nfc_mean": float(plain.nfc.mean()), "learned_nfc_mean": float(ml.nfc.mean()),
+        "plain_rounds": plain.rounds, "learned_rounds": ml.rounds,
+        "start_used": int(ml.used.sum()),
+        "final_energy_diff_ev_per_atom_max": float(np.abs(de).max()),
+        "final_energy_diff_ev_per_atom_mean": float(de.mean()),
+        "status_plain": np.bincount(plain.status, minlength=3).tolist(),
+        "status_learned": np.bincount(ml.status, minlength=3).tolist(),
+    }
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--train-cells", type=int, default=2048)
+    ap.add_argument("--epochs", type=int, default=20)
+    ap.add_argument("--batch-cells", type=int, default=64)
+    ap.add_argument("--lr", type=float, default=1e-3)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--eval-cells", type=int, default=512)
+    ap.add_argument("--out", default=DEFAULT_OUT)
+    a = ap.parse_args(argv)
+    tmp = tempfile.mkdtemp(prefix="imdtrain")
+    tabs = wl.sutton_chen_tables(os.path.join(tmp, "cu"), [wl.CU])
+    t0 = time.perf_counter()
+    train = wl.defect_batch(a.train_cells, seed=5)
+    disp, relax_stats = relax_targets(tabs, train)
+    t_data = time.perf_counter() - t0
+    t1 = time.perf_counter()
+    tr = learned.Trainer(tabs, train, disp, batch_cells=a.batch_cells, seed=a.seed)
+    loss0 = tr.loss()
+    for ep in range(a.epochs):
+        m = tr.epoch(a.lr)
+        print("epoch %d: mean loss %.6e" % (ep + 1, m), flush=True)
+    loss1 = tr.loss()
+    w = tr.w.copy()
+    steps = tr.step
+    tr.close()
+    t_train = time.perf_counter() - t1
+    # the same loss with zero displacement: mean |target|^2 per atom
+    zero = float(np.mean([np.mean(np.sum(d * d, axis=1)) for d in disp]))
+    rec = {"train_cells": a.train_cells, "train_atoms": int(sum(c.n for c in train)),
+           "epochs": a.epochs, "batch_cells": a.batch_cells, "lr": a.lr, "adam_steps": steps,
+           "loss_initial": loss0, "loss_final": loss1, "loss_zero_prediction": zero,
+           "loss_history": tr.history, "seconds_data": t_data, "seconds_train": t_train,
+           "relax_batches": relax_stats}
+    if a.eval_cells > 0:
+        held = wl.defect_batch(a.eval_cells, seed=6)
+        rec["eval"] = evaluate(tabs, held, w)
+        print(json.dumps(rec["eval"]), flush=True)
+    os.makedirs(os.path.dirname(os.path.abspath(a.out)), exist_ok=True)
+    np.savez(a.out, w=w, record=json.dumps(rec))
+    print("wrote %s (loss %.3e -> %.3e; zero prediction %.3e)" % (a.out, loss0, loss1, zero))
+
+
+if __name__ == "__main__":
+    main()

@@ -191,12 +191,25 @@ int imdgpu_batch_results(imdgpu_sys *sys, double *epot, double *fmax, int *steps
 int imdgpu_ml_nparam(void);
 int imdgpu_ml_set_weights(imdgpu_sys *sys, const float *w, int n);
 int imdgpu_ml_get_weights(imdgpu_sys *sys, float *w, int n);
+/* Adam first and second moments (imdgpu_ml_nparam() floats each) and step
+ * count; with the weights they carry one model's training state from one
+ * handle to another (imdgpu_ml_set_weights clears them). */
+int imdgpu_ml_get_adam(imdgpu_sys *sys, float *m, float *v, int *step);
+int imdgpu_ml_set_adam(imdgpu_sys *sys, const float *m, const float *v, int step);
 /* dx (3n, caller order) at the current positions */
 int imdgpu_ml_predict(imdgpu_sys *sys, double *dx);
 /* loss = sum_i |dx_i - target_i|^2 / n and its gradient (grad may be NULL);
  * lr > 0: one Adam step (beta 0.9 / 0.999) on the weights */
 int imdgpu_ml_train_step(imdgpu_sys *sys, const double *target, double lr, double *loss,
                          float *grad);
+/* Learned start of a batch (after imdgpu_batch_set_cells and
+ * imdgpu_ml_set_weights, before imdgpu_batch_begin): per cell the energy
+ * at the current positions (e_start), the energy after adding the predicted
+ * displacements (e_pred), and used[c] = (e_pred < e_start).  Cells with
+ * used[c] == 1 keep the displaced positions, the others go back to theirs;
+ * CG then relaxes every cell from its chosen start.  Two force calls.  Any
+ * output pointer may be NULL. */
+int imdgpu_batch_ml_start(imdgpu_sys *sys, int *used, double *e_start, double *e_pred);
 
 /* Neighbour pairs of the current list: NUMMER of both atoms, image shift of
  * the second (3 ints, in box vectors) and r^2 as used for the list test.
