@@ -104,6 +104,8 @@ def lib() -> C.CDLL:
         L.imdgpu_batch_begin.argtypes = [vp, C.c_double, C.c_int]
         L.imdgpu_batch_advance.argtypes = [vp, C.c_int, _ip, _ip]
         L.imdgpu_batch_rebuilds.argtypes = [vp, C.POINTER(C.c_long)]
+        L.imdgpu_batch_set_compaction.argtypes = [vp, C.c_int]
+        L.imdgpu_batch_positions.argtypes = [vp, _dp]
         fp = C.POINTER(C.c_float)
         L.imdgpu_ml_nparam.argtypes = []
         L.imdgpu_ml_set_weights.argtypes = [vp, fp, C.c_int]
@@ -423,9 +425,15 @@ class GpuBatch(GpuSystem):
         return {"epot": e, "fmax": fm, "steps": st, "nfc": nfc, "status": status}
 
     def positions(self):
+        """Current positions, one (n_c, 3) array per cell."""
         x = np.empty((self.n, 3))
-        _check(lib().imdgpu_get_atoms(self.h, _p(x), None, None, None, None, None), "get_atoms")
+        _check(lib().imdgpu_batch_positions(self.h, _p(x)), "batch_positions")
         return np.split(x, np.cumsum(self.natoms)[:-1])
+
+    def set_compaction(self, pct: int) -> None:
+        """Drop finished cells from the device once the unfinished ones hold
+        at most pct % of its atoms (0: never)."""
+        _check(lib().imdgpu_batch_set_compaction(self.h, int(pct)), "batch_set_compaction")
 
 
 def set_device(device: int) -> None:

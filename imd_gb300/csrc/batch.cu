@@ -21,7 +21,15 @@ namespace imdgpu {
 __device__ __forceinline__ double sgn(double a, double b) { return b >= 0.0 ? fabs(a) : -fabs(a); }
 
 // resumable linmin / mnbrak / brent of one cell
-__device__ void cg_machine(CgSys &S, const CgParams &P) {
+constexpr int SHORT_STEPS = 5;
+
+// short_last: the evaluation just consumed had a pair closer than a table's
+// first point (IMD's "Short distance").  Trial points of a line search may,
+// and CG usually gets out again.  SHORT_STEPS line searches in a row that end
+// on such a point without lowering the energy stop the cell with status 4:
+// the tables clamp there, energy and forces no longer match, and IMD's CG
+// stays there for good.
+__device__ void cg_machine(CgSys &S, const CgParams &P, bool short_last) {
   const double CGOLD = 0.3819660, GOLD = 1.618034, TINY = 1.0e-20;
   const double fres = S.E;  // result of the pending evaluation (energy at alpha)
   for (int guard = 0; guard < 64; guard++) {
@@ -31,6 +39,7 @@ __device__ void cg_machine(CgSys &S, const CgParams &P) {
         S.pc = PC_AFTER_RESET;
         return;
       case PC_AFTER_RESET:  // calc_fnorm_g_h done lazily by OP_RESET_MOVE
+        S.nshort = short_last ? 1 : 0;
         S.cg_poteng = fres;
         S.old_cg_poteng = fres;
         S.f_max2 = S.fmax2;
@@ -237,10 +246,18 @@ __device__ void cg_machine(CgSys &S, const CgParams &P) {
         S.pc = PC_BRENT_ITER;
         break;
       case PC_AFTER_LINMIN:  // cg_calcgamma + set_hg (applied with the next move)
+        S.nshort = (short_last && !(fres < S.old_cg_poteng)) ? S.nshort + 1 : 0;
+        if (S.nshort >= SHORT_STEPS) {
+          S.status = 4;
+          S.op = OP_IDLE;
+          S.pc = PC_DONE;
+          return;
+        }
         S.gamma = S.dgg / S.gg;
         S.f_max2 = S.fmax2;
         S.pending = OP_SETHG_MOVE;
         if (S.fatom2 <= P.fmax * P.fmax || S.steps >= P.maxsteps) {
+          if (S.fatom2 > P.fmax * P.fmax) S.status = 1;  // stopped by maxsteps
           S.pc = PC_DONE;
           break;
         }
@@ -261,12 +278,15 @@ __device__ void cg_machine(CgSys &S, const CgParams &P) {
   S.pc = PC_DONE;
 }
 
-__global__ void k_bt_control(CgSys *cs, int nsys, CgParams P, int *sys_done,
+__global__ void k_bt_control(CgSys *cs, int nsys, CgParams P, int *sys_done, int *sys_short,
                              unsigned long long *maxd, int *ndone) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= nsys) return;
   CgSys S = cs[s];
-  if (S.pc != PC_DONE) cg_machine(S, P);
+  // the flag of the last evaluation; the next force pass sets it afresh
+  const bool short_last = sys_short[s] != 0;
+  sys_short[s] = 0;
+  if (S.pc != PC_DONE) cg_machine(S, P, short_last);
   maxd[s] = 0ull;
   const int done = (S.pc == PC_DONE);
   if (done && !sys_done[s]) atomicAdd(ndone, 1);
@@ -380,10 +400,10 @@ __global__ void __launch_bounds__(256) k_bt_reduce(SysView v, const int *aoff, C
 static inline int nblk(long n, int bs) { return (int)((n + bs - 1) / bs); }
 
 void launch_batch_round_pre(const SysView &v, CgSys *cs, int nsys, const CgParams &P,
-                            int *sys_done, double4 *oldx, double4 *g, double4 *h,
-                            unsigned long long *maxd, int *ndone, DevScalars *sc,
+                            int *sys_done, int *sys_short, double4 *oldx, double4 *g,
+                            double4 *h, unsigned long long *maxd, int *ndone, DevScalars *sc,
                             double skin2, cudaStream_t st) {
-  k_bt_control<<<nblk(nsys, 128), 128, 0, st>>>(cs, nsys, P, sys_done, maxd, ndone);
+  k_bt_control<<<nblk(nsys, 128), 128, 0, st>>>(cs, nsys, P, sys_done, sys_short, maxd, ndone);
   k_bt_vec<<<nblk(v.n, BS_VEC), BS_VEC, 0, st>>>(v, cs, oldx, g, h, maxd);
   k_bt_flag<<<1, 1024, 0, st>>>(maxd, sys_done, nsys, skin2, sc);
 }

@@ -58,7 +58,7 @@ __global__ void __launch_bounds__(BS_FORCE) k_density64(SysView v, DevTable rho)
     }
   }
   atomicAdd(&v.rho[i], eam_r);
-  if (shortf) atomicOr(v.status, ST_SHORT);
+  if (shortf) flag_short(v, i);
 }
 
 // send_forces(add_rho) (src/imd_forces_nbl.c:1076): ghosts into owners
@@ -160,7 +160,7 @@ __global__ void __launch_bounds__(BS_FORCE) k_force64(SysView v, DevTable pair, 
     atomicAdd(fi + 1, ffy);
     atomicAdd(fi + 2, ffz);
     atomicAdd(fi + 3, ee);
-    if (shortf) atomicOr(v.status, ST_SHORT);
+    if (shortf) flag_short(v, i);
   }
   block_sum_store<2, BS_FORCE>(acc, partial);
 }
@@ -244,7 +244,7 @@ __global__ void __launch_bounds__(BS_FORCE) k_density_fast(SysView v, DevTable r
     }
   }
   atomicAdd(&v.rho[i], eam_r);
-  if (shortf) atomicOr(v.status, ST_SHORT);
+  if (shortf) flag_short(v, i);
 }
 
 template <bool NT1, bool EAM, bool EPOT, bool SAMEGRID, bool CUB>
@@ -328,7 +328,7 @@ __global__ void __launch_bounds__(BS_FORCE) k_force_fast(SysView v, DevTable pai
     if (!EPOT && v.eshare) atomicAdd(fi + 3, esum);
     acc[0] = esum;
     acc[1] = vir;
-    if (shortf) atomicOr(v.status, ST_SHORT);
+    if (shortf) flag_short(v, i);
   }
   block_sum_store<2, BS_FORCE>(acc, partial);
 }

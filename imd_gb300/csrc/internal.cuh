@@ -118,12 +118,20 @@ struct SysView {
   const int *scoff;            // 1 per system
   const int *sys_done;
   double4 *wrap_oldx;          // batch CG: old_x moved with the wrap of x
+  int *sys_short;              // batch: per-system flag, a pair below a table begin
   int eshare;                  // force pass adds each atom's own pair energies to frc.w
 };
 
 // atoms of finished cells of a batch are skipped by the force passes
 __device__ __forceinline__ bool atom_idle(const SysView &v, int i) {
   return v.sys_done && v.sys_done[v.atom_sys[i]];
+}
+
+// a pair of atom i closer than a table's first point (IMD's "Short
+// distance"): the status word, and in a batch the flag of i's system
+__device__ __forceinline__ void flag_short(const SysView &v, int i) {
+  atomicOr(v.status, ST_SHORT);
+  if (v.sys_short) atomicOr(&v.sys_short[v.atom_sys[i]], 1);
 }
 
 // system of real atom i (0 for a single system)

@@ -47,6 +47,7 @@ struct CgSys {
   double ax, bx, cx, fa, fb, fc, u, fu, ulim;            // mnbrak
   double a, b, x, w, v, fx, fw, fv, e, d;                // brent
   int pc, op, pending, steps, nfc, status, iter, ctf;
+  int nshort, pad;                                       // line searches ended short, in a row
 };
 
 constexpr int BS_FORCE = 128;
@@ -68,7 +69,8 @@ int launch_forces_mixed(const SysView &v, const ForceTabs &t, DevScalars *sc, fl
 
 // batch.cu
 void launch_batch_round_pre(const SysView &v, CgSys *cs, int nsys, const CgParams &P,
-                            int *sys_done, double4 *oldx, double4 *g, double4 *h,
+                            int *sys_done, int *sys_short, double4 *oldx, double4 *g,
+                            double4 *h,
                             unsigned long long *maxd, int *ndone, DevScalars *sc,
                             double skin2, cudaStream_t st);
 void launch_batch_round_post(const SysView &v, const int *aoff, CgSys *cs, int nsys,

@@ -84,7 +84,7 @@ __global__ void __launch_bounds__(BS_FORCE) k_density_mixed(SysView v, DevTable 
     }
   }
   v.rho[i] = r.value();
-  if (shortf) atomicOr(v.status, ST_SHORT);
+  if (shortf) flag_short(v, i);
 }
 
 // embedding in FP64 (per atom), F' also as FP32 for the pair kernel
@@ -181,7 +181,7 @@ __global__ void __launch_bounds__(BS_FORCE) k_force_mixed(SysView v, DevTable pa
     v.frc[i] = f;
     acc[0] = e;
     acc[1] = vir.value();
-    if (shortf) atomicOr(v.status, ST_SHORT);
+    if (shortf) flag_short(v, i);
   }
   (void)pair_only_epot;
   block_sum_store<2, BS_FORCE>(acc, partial);

@@ -58,6 +58,16 @@ struct BatchRun {
   int ndone = 0;
   cudaGraphExec_t gx = nullptr;
   std::vector<uintptr_t> gkey;
+  // Compaction: finished cells leave the device batch so that the rounds of
+  // the remaining cells cost what those cells cost.  cell_of maps a cell of
+  // the device batch to its cell of imdgpu_batch_set_cells; cells that left
+  // keep their final state here.
+  std::vector<int> cell_of;
+  std::vector<CgSys> final_cs;
+  std::vector<char> have_final;
+  std::vector<double> final_x;       // 3 per atom of imdgpu_batch_set_cells
+  int ndone_base = 0;                // finished cells no longer on the device
+  int compactions = 0;
 };
 
 // ---------------------------------------------------------------------------
@@ -136,12 +146,17 @@ struct imdgpu_sys {
   std::vector<int> h_aoff;           // nsys + 1 atom offsets
   std::vector<double> h_boxes;       // 9 per system
   int *d_atom_sys = nullptr, *d_aoff = nullptr, *d_sgdim = nullptr, *d_scdim = nullptr;
-  int *d_scoff = nullptr, *d_sys_done = nullptr, *d_ndone = nullptr;
+  int *d_scoff = nullptr, *d_sys_done = nullptr, *d_ndone = nullptr, *d_sys_short = nullptr;
   double *d_sbox = nullptr, *d_stbox = nullptr;
   CgSys *d_cs = nullptr;
   unsigned long long *d_maxd = nullptr;
   std::vector<int> h_sgdim;
   BatchRun *brun = nullptr;
+  // the cells as imdgpu_batch_set_cells received them (batch repacking)
+  int b0_ncells = 0;
+  std::vector<int> b0_aoff, b0_number, b0_type;
+  std::vector<double> b0_boxes, b0_mass;
+  int compact_pct = 50;            // compact when active atoms <= this % of the device batch
   long batch_nbl0 = 0;
 
   // learned start (learn.cu)
@@ -174,6 +189,12 @@ struct imdgpu_sys {
   cudaEvent_t ev[8];
   bool ev_made = false;
 };
+
+// every cell of a compacted batch back on the device (batched CG section,
+// inside the C-ABI block)
+extern "C" {
+static int batch_full(imdgpu_sys *s);
+}
 
 // ---------------------------------------------------------------------------
 // rebuild kernels (guarded by sc->rebuild)
@@ -762,6 +783,16 @@ __global__ void k_put_state(SysView v, const int *slot_of, const double *x, cons
   }
 }
 
+// batch repacking: slot order -> caller order and back
+__global__ void k_gather4(const double4 *src, const int *orig, int n, double4 *dst) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) dst[orig[i]] = src[i];
+}
+__global__ void k_scatter4(const double4 *src, const int *slot_of, int n, double4 *dst) {
+  const int o = blockIdx.x * blockDim.x + threadIdx.x;
+  if (o < n) dst[slot_of[o]] = src[o];
+}
+
 __global__ void k_iota(int *a, int n) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) a[i] = i;
@@ -854,6 +885,7 @@ static SysView view(imdgpu_sys *s) {
     v.scoff = s->d_scoff;
     v.sys_done = s->d_sys_done;
     v.wrap_oldx = s->oldx;
+    v.sys_short = s->d_sys_short;
     v.eshare = 1;
   }
   return v;
@@ -1428,6 +1460,7 @@ int imdgpu_destroy(imdgpu_sys *s) {
   dfree(s->ml_pairs); dfree(s->ml_np); dfree(s->ml_dx); dfree(s->ml_target); dfree(s->ml_dldx);
   dfree(s->ml_loss);
   dfree(s->ml_save); dfree(s->ml_ecell); dfree(s->ml_sel);
+  dfree(s->d_sys_short);
   dfree(s->d_atom_sys); dfree(s->d_aoff); dfree(s->d_sgdim); dfree(s->d_scdim); dfree(s->d_scoff);
   dfree(s->d_sys_done); dfree(s->d_ndone); dfree(s->d_sbox); dfree(s->d_stbox); dfree(s->d_cs);
   dfree(s->d_maxd);
@@ -1727,6 +1760,7 @@ int imdgpu_set_atoms(imdgpu_sys *s, int n, const int *number, const int *type,
 int imdgpu_get_atoms(imdgpu_sys *s, double *x, double *p, double *f, double *epot,
                      double *eam_rho, double *eam_df) {
   if (!s || !s->atoms_set) return fail(IMDGPU_ERR_STATE, "atoms not set");
+  if (int rcf = batch_full(s)) return rcf;
   const size_t n = s->n;
   double *host[6] = {x, p, f, epot, eam_rho, eam_df};
   const size_t off[6] = {0, 3 * n, 6 * n, 9 * n, 10 * n, 11 * n};
@@ -1744,6 +1778,7 @@ int imdgpu_get_atoms(imdgpu_sys *s, double *x, double *p, double *f, double *epo
 
 int imdgpu_put_state(imdgpu_sys *s, const double *x, const double *p) {
   if (!s || !s->atoms_set || !x) return fail(IMDGPU_ERR_STATE, "atoms not set");
+  if (int rcf = batch_full(s)) return rcf;
   const size_t n = s->n;
   CK(cudaMemcpyAsync(s->d_in, x, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, s->st));
   if (p) CK(cudaMemcpyAsync(s->d_in + 3 * n, p, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, s->st));
@@ -1786,14 +1821,18 @@ int imdgpu_get_scalars(imdgpu_sys *s, imdgpu_scalars *o) {
 int imdgpu_calc_forces(imdgpu_sys *s, int steps) {
   (void)steps;
   if (!s) return fail(IMDGPU_ERR_ARG, "null system");
-  int rc = calc_forces_sync(s);
+  int rc = batch_full(s);
+  if (rc) return rc;
+  rc = calc_forces_sync(s);
   if (rc) return rc;
   return (s->status_host & ST_SHORT) ? IMDGPU_WARN_SHORT : IMDGPU_OK;
 }
 
 int imdgpu_make_nblist(imdgpu_sys *s) {
   if (!s) return fail(IMDGPU_ERR_ARG, "null system");
-  int rc = prepare(s);
+  int rc = batch_full(s);
+  if (rc) return rc;
+  rc = prepare(s);
   if (rc) return rc;
   return rebuild_sync(s);
 }
@@ -2364,10 +2403,9 @@ int imdgpu_cg_relax(imdgpu_sys *s, double fmax, int maxsteps, int *steps_done,
 // ---------------------------------------------------------------------------
 // batched CG
 // ---------------------------------------------------------------------------
-int imdgpu_batch_set_cells(imdgpu_sys *s, int ncells, const int *natoms, const double *boxes,
-                           const int *number, const int *type, const double *mass,
-                           const double *x) {
-  if (!s || ncells < 1 || !natoms || !boxes) return fail(IMDGPU_ERR_ARG, "bad batch arguments");
+// the device side of imdgpu_batch_set_cells: cells, atoms and per-cell arrays
+static int batch_load(imdgpu_sys *s, int ncells, const int *natoms, const double *boxes,
+                      const int *number, const int *type, const double *mass, const double *x) {
   std::vector<int> aoff(ncells + 1, 0);
   for (int q = 0; q < ncells; q++) {
     if (natoms[q] < 1) return fail(IMDGPU_ERR_ARG, "empty cell in batch");
@@ -2389,13 +2427,221 @@ int imdgpu_batch_set_cells(imdgpu_sys *s, int ncells, const int *natoms, const d
   dfree(s->d_ndone);
   dfree(s->d_cs);
   dfree(s->d_maxd);
+  dfree(s->d_sys_short);
   CK(dalloc(&s->d_atom_sys, asys.size()));
+  CK(dalloc(&s->d_sys_short, ncells));
+  CK(cudaMemset(s->d_sys_short, 0, sizeof(int) * ncells));
   CK(dalloc(&s->d_sys_done, ncells));
   CK(dalloc(&s->d_ndone, 1));
   CK(dalloc(&s->d_cs, ncells));
   CK(dalloc(&s->d_maxd, ncells));
   CK(cudaMemcpy(s->d_atom_sys, asys.data(), sizeof(int) * asys.size(), cudaMemcpyHostToDevice));
   CK(cudaMemset(s->d_sys_done, 0, sizeof(int) * ncells));
+  return IMDGPU_OK;
+}
+
+// Repack the device batch to the cells of imdgpu_batch_set_cells with
+// keep[cell] != 0, carrying every cell's CG state: a cell still relaxing
+// keeps its positions, old_x, g, h, last forces and line-search state; a
+// finished cell keeps its final positions and results (on the host when it
+// leaves the device).  Compaction keeps the unfinished cells; restoring
+// keeps all.  Per-cell arithmetic does not depend on the other cells, so a
+// cell relaxes the same way with or without repacking, up to the rounding
+// of re-wrapped coordinates.
+static int batch_repack(imdgpu_sys *s, const std::vector<char> &keep) {
+  BatchRun &B = *s->brun;
+  const int ns = s->nsys, n = s->n;
+  std::vector<CgSys> cs(ns);
+  std::vector<int> done(ns);
+  CK(cudaStreamSynchronize(s->st));
+  CK(cudaMemcpy(cs.data(), s->d_cs, sizeof(CgSys) * ns, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(done.data(), s->d_sys_done, sizeof(int) * ns, cudaMemcpyDeviceToHost));
+  // pos, old_x, g, h, forces of every atom, by its index in the device batch
+  std::vector<double4> hv[5];
+  {
+    double4 *tmp = nullptr;
+    CK(dalloc(&tmp, 5 * (size_t)n));
+    const double4 *src[5] = {s->pos, s->oldx, s->cgg, s->cgh, s->frc};
+    for (int k = 0; k < 5; k++)
+      k_gather4<<<nblk(n, 256), 256, 0, s->st>>>(src[k], s->orig, n, tmp + (size_t)k * n);
+    CK(cudaGetLastError());
+    for (int k = 0; k < 5; k++) {
+      hv[k].resize(n);
+      CK(cudaMemcpyAsync(hv[k].data(), tmp + (size_t)k * n, sizeof(double4) * n,
+                         cudaMemcpyDeviceToHost, s->st));
+    }
+    CK(cudaStreamSynchronize(s->st));
+    dfree(tmp);
+  }
+  // cells finished on the device: final state to the host record
+  std::vector<int> cur_of(s->b0_ncells, -1);
+  for (int c = 0; c < ns; c++) {
+    const int o = B.cell_of[c];
+    cur_of[o] = c;
+    if (!done[c]) continue;
+    B.final_cs[o] = cs[c];
+    B.have_final[o] = 1;
+    for (int i = s->h_aoff[c]; i < s->h_aoff[c + 1]; i++) {
+      const size_t io = (size_t)s->b0_aoff[o] + (i - s->h_aoff[c]);
+      B.final_x[3 * io] = hv[0][i].x;
+      B.final_x[3 * io + 1] = hv[0][i].y;
+      B.final_x[3 * io + 2] = hv[0][i].z;
+    }
+  }
+  // the new batch
+  std::vector<int> cells, natoms, num, typ;
+  std::vector<double> boxes, mass, x;
+  std::vector<double4> nv[4];
+  std::vector<CgSys> ncs;
+  std::vector<int> ndone;
+  int base = 0;
+  for (int o = 0; o < s->b0_ncells; o++) {
+    if (!keep[o]) {
+      if (B.have_final[o]) base++;
+      continue;
+    }
+    const int c = cur_of[o];
+    const bool live = (c >= 0 && !done[c]);
+    if (!live && !B.have_final[o]) return fail(IMDGPU_ERR_STATE, "batch repack: cell has no state");
+    cells.push_back(o);
+    const int a0 = s->b0_aoff[o], na = s->b0_aoff[o + 1] - a0;
+    natoms.push_back(na);
+    boxes.insert(boxes.end(), s->b0_boxes.begin() + 9 * (size_t)o, s->b0_boxes.begin() + 9 * (size_t)o + 9);
+    for (int j = 0; j < na; j++) {
+      num.push_back(s->b0_number[a0 + j]);
+      typ.push_back(s->b0_type[a0 + j]);
+      mass.push_back(s->b0_mass[a0 + j]);
+      if (live) {
+        const int i = s->h_aoff[c] + j;
+        x.push_back(hv[0][i].x);
+        x.push_back(hv[0][i].y);
+        x.push_back(hv[0][i].z);
+        for (int k = 0; k < 4; k++) nv[k].push_back(hv[k + 1][i]);
+      } else {
+        for (int a = 0; a < 3; a++) x.push_back(B.final_x[3 * (size_t)(a0 + j) + a]);
+        for (int k = 0; k < 4; k++) nv[k].push_back(make_double4(0.0, 0.0, 0.0, 0.0));
+      }
+    }
+    ncs.push_back(live ? cs[c] : B.final_cs[o]);
+    ndone.push_back(live ? 0 : 1);
+  }
+  const int nc = (int)cells.size();
+  if (nc == 0) return fail(IMDGPU_ERR_STATE, "batch repack: no cells");
+  int rc = batch_load(s, nc, natoms.data(), boxes.data(), num.data(), typ.data(), mass.data(),
+                      x.data());
+  if (rc) return rc;
+  if ((rc = prepare(s))) return rc;
+  if ((rc = ensure_cg(s))) return rc;
+  const int nn = s->n;
+  // before the first build the device slot of every atom is its index
+  CK(cudaMemcpy(s->oldx, nv[0].data(), sizeof(double4) * nn, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(s->cgg, nv[1].data(), sizeof(double4) * nn, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(s->cgh, nv[2].data(), sizeof(double4) * nn, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(s->d_cs, ncs.data(), sizeof(CgSys) * nc, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(s->d_sys_done, ndone.data(), sizeof(int) * nc, cudaMemcpyHostToDevice));
+  int nd = 0;
+  for (int v : ndone) nd += v;
+  CK(cudaMemcpy(s->d_ndone, &nd, sizeof(int), cudaMemcpyHostToDevice));
+  int one = 1;
+  CK(cudaMemcpy(&s->dsc->rebuild, &one, sizeof(int), cudaMemcpyHostToDevice));
+  if ((rc = rebuild_sync(s))) return rc;
+  {
+    int cnt[4];
+    CK(cudaMemcpy(cnt, s->counters, sizeof cnt, cudaMemcpyDeviceToHost));
+    if (s->nbcap < (int)(cnt[1] * 1.3) + 8) {
+      if ((rc = alloc_list(s, (int)(cnt[1] * 1.3) + 8))) return rc;
+      if ((rc = rebuild_sync(s))) return rc;
+    }
+  }
+  // the last forces, which the next round's set_hg / reset reads, follow
+  // the atoms to their slots after the build
+  {
+    double4 *tmp = nullptr;
+    CK(dalloc(&tmp, nn));
+    CK(cudaMemcpy(tmp, nv[3].data(), sizeof(double4) * nn, cudaMemcpyHostToDevice));
+    k_scatter4<<<nblk(nn, 256), 256, 0, s->st>>>(tmp, s->slot_of, nn, s->frc);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(s->st));
+    dfree(tmp);
+  }
+  B.cell_of = cells;
+  B.ndone_base = base;
+  if (B.gx) cudaGraphExecDestroy(B.gx);
+  B.gx = nullptr;
+  B.gkey.clear();
+  B.compactions++;
+  return IMDGPU_OK;
+}
+
+// every cell of imdgpu_batch_set_cells back on the device (after compaction)
+static int batch_full(imdgpu_sys *s) {
+  if (!s || !s->brun || s->nsys == s->b0_ncells) return IMDGPU_OK;
+  std::vector<char> all(s->b0_ncells, 1);
+  return batch_repack(s, all);
+}
+
+int imdgpu_batch_set_cells(imdgpu_sys *s, int ncells, const int *natoms, const double *boxes,
+                           const int *number, const int *type, const double *mass,
+                           const double *x) {
+  if (!s || ncells < 1 || !natoms || !boxes || !number || !type || !mass || !x)
+    return fail(IMDGPU_ERR_ARG, "bad batch arguments");
+  std::vector<int> aoff(ncells + 1, 0);
+  for (int q = 0; q < ncells; q++) {
+    if (natoms[q] < 1) return fail(IMDGPU_ERR_ARG, "empty cell in batch");
+    aoff[q + 1] = aoff[q] + natoms[q];
+  }
+  const int n = aoff[ncells];
+  s->b0_ncells = ncells;
+  s->b0_aoff = aoff;
+  s->b0_boxes.assign(boxes, boxes + 9 * (size_t)ncells);
+  s->b0_number.assign(number, number + n);
+  s->b0_type.assign(type, type + n);
+  s->b0_mass.assign(mass, mass + n);
+  if (s->brun) {
+    if (s->brun->gx) cudaGraphExecDestroy(s->brun->gx);
+    delete s->brun;
+    s->brun = nullptr;
+  }
+  return batch_load(s, ncells, natoms, boxes, number, type, mass, x);
+}
+
+// Positions of every atom of imdgpu_batch_set_cells (3 per atom, its order),
+// wherever its cell is: on the device or finished and compacted away.
+int imdgpu_batch_positions(imdgpu_sys *s, double *x) {
+  if (!s || s->nsys < 1 || !x) return fail(IMDGPU_ERR_ARG, "no batch / null");
+  const int n = s->n;
+  std::vector<double> cur(3 * (size_t)n);
+  {
+    SysView v = view(s);
+    k_gather_out<<<nblk(n, 256), 256, 0, s->st>>>(v, s->d_out, nullptr, nullptr, nullptr,
+                                                   nullptr, nullptr);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(cur.data(), s->d_out, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost,
+                       s->st));
+    CK(cudaStreamSynchronize(s->st));
+  }
+  if (!s->brun || s->nsys == s->b0_ncells) {
+    memcpy(x, cur.data(), sizeof(double) * 3 * n);
+    return IMDGPU_OK;
+  }
+  const BatchRun &B = *s->brun;
+  for (int o = 0; o < s->b0_ncells; o++)
+    if (B.have_final[o])
+      memcpy(x + 3 * (size_t)s->b0_aoff[o], B.final_x.data() + 3 * (size_t)s->b0_aoff[o],
+             sizeof(double) * 3 * (s->b0_aoff[o + 1] - s->b0_aoff[o]));
+  for (int c = 0; c < s->nsys; c++) {
+    const int o = B.cell_of[c];
+    memcpy(x + 3 * (size_t)s->b0_aoff[o], cur.data() + 3 * (size_t)s->h_aoff[c],
+           sizeof(double) * 3 * (s->h_aoff[c + 1] - s->h_aoff[c]));
+  }
+  return IMDGPU_OK;
+}
+
+// compaction threshold: repack when the unfinished cells hold at most pct %
+// of the atoms on the device (0: never)
+int imdgpu_batch_set_compaction(imdgpu_sys *s, int pct) {
+  if (!s || pct < 0 || pct > 100) return fail(IMDGPU_ERR_ARG, "compaction percentage");
+  s->compact_pct = pct;
   return IMDGPU_OK;
 }
 
@@ -2410,8 +2656,8 @@ static void issue_batch_round(imdgpu_sys *s, const CgParams &P) {
   SysView v = view(s);
   ForceTabs ft = ftabs(s);
   ft.epot = 0;
-  launch_batch_round_pre(v, s->d_cs, s->nsys, P, s->d_sys_done, s->oldx, s->cgg, s->cgh,
-                         s->d_maxd, s->d_ndone, s->dsc, v.skin2, s->st);
+  launch_batch_round_pre(v, s->d_cs, s->nsys, P, s->d_sys_done, s->d_sys_short, s->oldx,
+                         s->cgg, s->cgh, s->d_maxd, s->d_ndone, s->dsc, v.skin2, s->st);
   issue_rebuild(s);
   launch_forces(v, ft, s->dsc, s->precision == IMDGPU_MIXED, s->st);
   launch_batch_round_post(v, s->d_aoff, s->d_cs, s->nsys, s->cgg, s->cg_fr, s->st);
@@ -2420,7 +2666,9 @@ static void issue_batch_round(imdgpu_sys *s, const CgParams &P) {
 
 int imdgpu_batch_begin(imdgpu_sys *s, double fmax, int maxsteps) {
   if (!s || s->nsys < 1) return fail(IMDGPU_ERR_STATE, "imdgpu_batch_set_cells first");
-  int rc = prepare(s);
+  int rc = batch_full(s);  // a compacted earlier run: every cell back
+  if (rc) return rc;
+  rc = prepare(s);
   if (rc) return rc;
   if ((rc = ensure_cg(s))) return rc;
   const int ns = s->nsys;
@@ -2433,6 +2681,7 @@ int imdgpu_batch_begin(imdgpu_sys *s, double fmax, int maxsteps) {
   }
   CK(cudaMemcpy(s->d_cs, init.data(), sizeof(CgSys) * ns, cudaMemcpyHostToDevice));
   CK(cudaMemset(s->d_sys_done, 0, sizeof(int) * ns));
+  CK(cudaMemset(s->d_sys_short, 0, sizeof(int) * ns));
   CK(cudaMemset(s->d_ndone, 0, sizeof(int)));
   CK(cudaMemset(s->cgg, 0, sizeof(double4) * s->ncap));
   CK(cudaMemset(s->cgh, 0, sizeof(double4) * s->ncap));
@@ -2465,6 +2714,11 @@ int imdgpu_batch_begin(imdgpu_sys *s, double fmax, int maxsteps) {
   P.linmin_maxsteps = s->linmin_maxsteps;
   P.maxsteps = maxsteps;
   P.cg_fr = s->cg_fr;
+  B.cell_of.resize(ns);
+  for (int c = 0; c < ns; c++) B.cell_of[c] = c;
+  B.final_cs.assign(ns, CgSys());
+  B.have_final.assign(ns, 0);
+  B.final_x.assign(3 * (size_t)s->n, 0.0);
   long nbl = 0;
   CK(cudaMemcpy(&nbl, s->dnbl, sizeof(long), cudaMemcpyDeviceToHost));
   s->batch_nbl0 = nbl;
@@ -2476,60 +2730,88 @@ int imdgpu_batch_advance(imdgpu_sys *s, int max_rounds, int *ndone_out, int *rou
   if (!s || !s->brun) return fail(IMDGPU_ERR_STATE, "imdgpu_batch_begin first");
   BatchRun &B = *s->brun;
   const CgParams &P = B.P;
-  const int ns = s->nsys;
   const int R = 16;
-  const size_t n = s->n;
   int rc = IMDGPU_OK;
-  // snapshot of everything a round changes, for replay after an overflow
+  // snapshot of everything a round changes, for replay after an overflow;
+  // sized for the batch as it is now (compaction only shrinks it)
+  const size_t n_alloc = s->n, ns_alloc = s->nsys;
   double4 *b4[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
-  double4 *live4[6] = {s->pos, s->mom, s->oldx, s->cgg, s->cgh, s->frc};
-  for (int k = 0; k < 6; k++) CK(dalloc(&b4[k], n));
-  int *bnum = nullptr, *borig = nullptr, *bdone = nullptr, *bnd = nullptr;
+  int *bnum = nullptr, *borig = nullptr, *bdone = nullptr, *bnd = nullptr, *bshort = nullptr;
   CgSys *bcs = nullptr;
-  CK(dalloc(&bnum, n));
-  CK(dalloc(&borig, n));
-  CK(dalloc(&bdone, ns));
-  CK(dalloc(&bnd, 1));
-  CK(dalloc(&bcs, ns));
+  auto release = [&]() {
+    for (int k = 0; k < 6; k++) dfree(b4[k]);
+    dfree(bnum);
+    dfree(borig);
+    dfree(bdone);
+    dfree(bnd);
+    dfree(bshort);
+    dfree(bcs);
+  };
+  bool ok = true;
+  for (int k = 0; k < 6; k++) ok = ok && dalloc(&b4[k], n_alloc) == cudaSuccess;
+  ok = ok && dalloc(&bnum, n_alloc) == cudaSuccess && dalloc(&borig, n_alloc) == cudaSuccess &&
+       dalloc(&bdone, ns_alloc) == cudaSuccess && dalloc(&bnd, 1) == cudaSuccess &&
+       dalloc(&bshort, ns_alloc) == cudaSuccess && dalloc(&bcs, ns_alloc) == cudaSuccess;
+  if (!ok) {
+    release();
+    return fail(IMDGPU_ERR_NOMEM, "batch snapshot buffers");
+  }
+#define CKR(call)                                                               \
+  do {                                                                          \
+    cudaError_t e_ = (call);                                                    \
+    if (e_ != cudaSuccess) {                                                    \
+      release();                                                                \
+      return fail(IMDGPU_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    }                                                                           \
+  } while (0)
   int done_rounds = 0, replays = 0;
-  while (done_rounds < max_rounds && B.ndone < ns) {
-    live4[0] = s->pos;
-    live4[1] = s->mom;
-    live4[5] = s->frc;
+  const int ncells0 = s->b0_ncells;
+  while (done_rounds < max_rounds && B.ndone < ncells0) {
+    const size_t n = s->n;
+    const int ns = s->nsys;
+    double4 *live4[6] = {s->pos, s->mom, s->oldx, s->cgg, s->cgh, s->frc};
     for (int k = 0; k < 6; k++)
-      CK(cudaMemcpyAsync(b4[k], live4[k], sizeof(double4) * n, cudaMemcpyDeviceToDevice, s->st));
-    CK(cudaMemcpyAsync(bnum, s->number, sizeof(int) * n, cudaMemcpyDeviceToDevice, s->st));
-    CK(cudaMemcpyAsync(borig, s->orig, sizeof(int) * n, cudaMemcpyDeviceToDevice, s->st));
-    CK(cudaMemcpyAsync(bdone, s->d_sys_done, sizeof(int) * ns, cudaMemcpyDeviceToDevice, s->st));
-    CK(cudaMemcpyAsync(bnd, s->d_ndone, sizeof(int), cudaMemcpyDeviceToDevice, s->st));
-    CK(cudaMemcpyAsync(bcs, s->d_cs, sizeof(CgSys) * ns, cudaMemcpyDeviceToDevice, s->st));
-    CK(cudaMemsetAsync(s->status, 0, sizeof(unsigned), s->st));
+      CKR(cudaMemcpyAsync(b4[k], live4[k], sizeof(double4) * n, cudaMemcpyDeviceToDevice, s->st));
+    CKR(cudaMemcpyAsync(bnum, s->number, sizeof(int) * n, cudaMemcpyDeviceToDevice, s->st));
+    CKR(cudaMemcpyAsync(borig, s->orig, sizeof(int) * n, cudaMemcpyDeviceToDevice, s->st));
+    CKR(cudaMemcpyAsync(bdone, s->d_sys_done, sizeof(int) * ns, cudaMemcpyDeviceToDevice, s->st));
+    CKR(cudaMemcpyAsync(bshort, s->d_sys_short, sizeof(int) * ns, cudaMemcpyDeviceToDevice, s->st));
+    CKR(cudaMemcpyAsync(bnd, s->d_ndone, sizeof(int), cudaMemcpyDeviceToDevice, s->st));
+    CKR(cudaMemcpyAsync(bcs, s->d_cs, sizeof(CgSys) * ns, cudaMemcpyDeviceToDevice, s->st));
+    CKR(cudaMemsetAsync(s->status, 0, sizeof(unsigned), s->st));
     std::vector<uintptr_t> key = {(uintptr_t)s->pos, (uintptr_t)s->nbr, (uintptr_t)s->xl,
                                   (uintptr_t)s->nbcap, (uintptr_t)s->gcap,
-                                  (uintptr_t)s->precision, (uintptr_t)s->exact};
+                                  (uintptr_t)s->precision, (uintptr_t)s->exact,
+                                  (uintptr_t)s->n, (uintptr_t)s->nsys, (uintptr_t)s->d_cs};
     if (s->use_graph) {
       if (!B.gx || key != B.gkey) {
         if (B.gx) cudaGraphExecDestroy(B.gx);
         B.gx = nullptr;
         cudaGraph_t g;
-        CK(cudaStreamBeginCapture(s->st, cudaStreamCaptureModeThreadLocal));
+        CKR(cudaStreamBeginCapture(s->st, cudaStreamCaptureModeThreadLocal));
         for (int r = 0; r < R; r++) issue_batch_round(s, P);
         cudaError_t e = cudaStreamEndCapture(s->st, &g);
-        if (e != cudaSuccess) return fail(IMDGPU_ERR_CUDA, std::string("batch graph capture: ") + cudaGetErrorString(e));
+        if (e != cudaSuccess) {
+          release();
+          return fail(IMDGPU_ERR_CUDA, std::string("batch graph capture: ") + cudaGetErrorString(e));
+        }
         e = cudaGraphInstantiate(&B.gx, g, 0);
         cudaGraphDestroy(g);
-        if (e != cudaSuccess) return fail(IMDGPU_ERR_CUDA, std::string("batch graph instantiate: ") + cudaGetErrorString(e));
+        if (e != cudaSuccess) {
+          release();
+          return fail(IMDGPU_ERR_CUDA, std::string("batch graph instantiate: ") + cudaGetErrorString(e));
+        }
         B.gkey = key;
       }
-      CK(cudaGraphLaunch(B.gx, s->st));
+      CKR(cudaGraphLaunch(B.gx, s->st));
     } else {
       for (int r = 0; r < R; r++) issue_batch_round(s, P);
-      CK(cudaGetLastError());
+      CKR(cudaGetLastError());
     }
     int nd = 0;
-    CK(cudaMemcpyAsync(&s->status_host, s->status, sizeof(unsigned), cudaMemcpyDeviceToHost, s->st));
-    CK(cudaMemcpyAsync(&nd, s->d_ndone, sizeof(int), cudaMemcpyDeviceToHost, s->st));
-    CK(cudaStreamSynchronize(s->st));
+    CKR(cudaMemcpyAsync(&s->status_host, s->status, sizeof(unsigned), cudaMemcpyDeviceToHost, s->st));
+    CKR(cudaMemcpyAsync(&nd, s->d_ndone, sizeof(int), cudaMemcpyDeviceToHost, s->st));
+    CKR(cudaStreamSynchronize(s->st));
     if (s->status_host & ST_CELLOVER) {
       rc = fail(IMDGPU_ERR_CELL, "more than " + std::to_string(CELLCAP) + " atoms in one cell");
       break;
@@ -2540,34 +2822,43 @@ int imdgpu_batch_advance(imdgpu_sys *s, int max_rounds, int *ndone_out, int *rou
         break;
       }
       int cnt[4];
-      CK(cudaMemcpy(cnt, s->counters, sizeof cnt, cudaMemcpyDeviceToHost));
+      CKR(cudaMemcpy(cnt, s->counters, sizeof cnt, cudaMemcpyDeviceToHost));
       if (s->status_host & ST_GHOSTOVER)
         if ((rc = alloc_ext(s, (int)(cnt[3] * 1.25) + 4096))) break;
       if (s->status_host & ST_NBOVER)
         if ((rc = alloc_list(s, (int)(cnt[1] * 1.2) + 8))) break;
-      live4[0] = s->pos;
-      live4[1] = s->mom;
-      live4[5] = s->frc;
+      double4 *back[6] = {s->pos, s->mom, s->oldx, s->cgg, s->cgh, s->frc};
       for (int k = 0; k < 6; k++)
-        CK(cudaMemcpy(live4[k], b4[k], sizeof(double4) * n, cudaMemcpyDeviceToDevice));
-      CK(cudaMemcpy(s->number, bnum, sizeof(int) * n, cudaMemcpyDeviceToDevice));
-      CK(cudaMemcpy(s->orig, borig, sizeof(int) * n, cudaMemcpyDeviceToDevice));
-      CK(cudaMemcpy(s->d_sys_done, bdone, sizeof(int) * ns, cudaMemcpyDeviceToDevice));
-      CK(cudaMemcpy(s->d_ndone, bnd, sizeof(int), cudaMemcpyDeviceToDevice));
-      CK(cudaMemcpy(s->d_cs, bcs, sizeof(CgSys) * ns, cudaMemcpyDeviceToDevice));
+        CKR(cudaMemcpy(back[k], b4[k], sizeof(double4) * n, cudaMemcpyDeviceToDevice));
+      CKR(cudaMemcpy(s->number, bnum, sizeof(int) * n, cudaMemcpyDeviceToDevice));
+      CKR(cudaMemcpy(s->orig, borig, sizeof(int) * n, cudaMemcpyDeviceToDevice));
+      CKR(cudaMemcpy(s->d_sys_done, bdone, sizeof(int) * ns, cudaMemcpyDeviceToDevice));
+      CKR(cudaMemcpy(s->d_sys_short, bshort, sizeof(int) * ns, cudaMemcpyDeviceToDevice));
+      CKR(cudaMemcpy(s->d_ndone, bnd, sizeof(int), cudaMemcpyDeviceToDevice));
+      CKR(cudaMemcpy(s->d_cs, bcs, sizeof(CgSys) * ns, cudaMemcpyDeviceToDevice));
       if ((rc = rebuild_sync(s))) break;
       continue;
     }
-    B.ndone = nd;
+    B.ndone = B.ndone_base + nd;
     B.rounds += R;
     done_rounds += R;
+    // compaction: the unfinished cells alone, once they hold few enough atoms
+    if (s->compact_pct > 0 && nd > 0 && nd < ns) {
+      std::vector<int> dn(ns);
+      CKR(cudaMemcpy(dn.data(), s->d_sys_done, sizeof(int) * ns, cudaMemcpyDeviceToHost));
+      long active = 0;
+      for (int c = 0; c < ns; c++)
+        if (!dn[c]) active += s->h_aoff[c + 1] - s->h_aoff[c];
+      if (active * 100 <= (long)s->compact_pct * (long)n) {
+        std::vector<char> keep(ncells0, 0);
+        for (int c = 0; c < ns; c++)
+          if (!dn[c]) keep[B.cell_of[c]] = 1;
+        if ((rc = batch_repack(s, keep))) break;
+      }
+    }
   }
-  for (int k = 0; k < 6; k++) dfree(b4[k]);
-  dfree(bnum);
-  dfree(borig);
-  dfree(bdone);
-  dfree(bnd);
-  dfree(bcs);
+#undef CKR
+  release();
   if (rc) return rc;
   if (ndone_out) *ndone_out = B.ndone;
   if (rounds_out) *rounds_out = B.rounds;
@@ -2594,18 +2885,30 @@ int imdgpu_batch_rebuilds(imdgpu_sys *s, long *n) {
 }
 
 // per-cell results: energy, max |F|, CG steps, force calls, status
-// (0 converged, 1 not converged within the rounds, 2 brent failed, 3 control)
+// (0 converged, 1 not converged within maxsteps or the rounds, 2 brent
+// failed, 3 control, 4 short distance)
 int imdgpu_batch_results(imdgpu_sys *s, double *epot, double *fmax_out, int *steps, int *nfc,
                          int *status) {
   if (!s || s->nsys < 1) return fail(IMDGPU_ERR_STATE, "no batch");
   std::vector<CgSys> cs(s->nsys);
   CK(cudaMemcpy(cs.data(), s->d_cs, sizeof(CgSys) * s->nsys, cudaMemcpyDeviceToHost));
-  for (int q = 0; q < s->nsys; q++) {
-    if (epot) epot[q] = cs[q].E;
-    if (fmax_out) fmax_out[q] = std::sqrt(cs[q].fatom2);
-    if (steps) steps[q] = cs[q].steps;
-    if (nfc) nfc[q] = cs[q].nfc;
-    if (status) status[q] = cs[q].status ? cs[q].status : (cs[q].pc == PC_DONE ? 0 : 1);
+  // per cell of imdgpu_batch_set_cells: on the device, or finished and
+  // compacted away
+  std::vector<CgSys> all;
+  if (s->brun && s->nsys != s->b0_ncells) {
+    const BatchRun &B = *s->brun;
+    all = B.final_cs;
+    for (int c = 0; c < s->nsys; c++) all[B.cell_of[c]] = cs[c];
+  } else {
+    all = cs;
+  }
+  for (int q = 0; q < (int)all.size(); q++) {
+    const CgSys &c = all[q];
+    if (epot) epot[q] = c.E;
+    if (fmax_out) fmax_out[q] = std::sqrt(c.fatom2);
+    if (steps) steps[q] = c.steps;
+    if (nfc) nfc[q] = c.nfc;
+    if (status) status[q] = c.status ? c.status : (c.pc == PC_DONE ? 0 : 1);
   }
   return IMDGPU_OK;
 }
@@ -2676,10 +2979,12 @@ __global__ void __launch_bounds__(256) k_cell_energy(const double4 *frc, const i
     e[stride * c] = r;
   }
 }
-// keep the prediction of a cell when its energy is below the start's
-__global__ void k_ml_select(const double *ecell, int nsys, int *keep) {
+// keep the prediction of a cell when its energy is below the start's and no
+// pair came closer than a table's first point (the tables clamp there, so
+// the energy is not the potential's)
+__global__ void k_ml_select(const double *ecell, const int *sys_short, int nsys, int *keep) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c < nsys) keep[c] = ecell[2 * c + 1] < ecell[2 * c] ? 1 : 0;
+  if (c < nsys) keep[c] = (ecell[2 * c + 1] < ecell[2 * c] && !sys_short[c]) ? 1 : 0;
 }
 }  // namespace imdgpu
 
@@ -2788,7 +3093,9 @@ int imdgpu_ml_set_adam(imdgpu_sys *s, const float *m, const float *v, int step) 
 // predicted displacement of every atom (caller order) at the current positions
 int imdgpu_ml_predict(imdgpu_sys *s, double *dx) {
   if (!s || !s->ml_have) return fail(IMDGPU_ERR_STATE, "no weights");
-  int rc = ml_prepare_pairs(s);
+  int rc = batch_full(s);
+  if (rc) return rc;
+  rc = ml_prepare_pairs(s);
   if (rc) return rc;
   if ((rc = ml_forward(s))) return rc;
   double *d = s->d_out;
@@ -2803,7 +3110,9 @@ int imdgpu_ml_predict(imdgpu_sys *s, double *dx) {
 int imdgpu_ml_train_step(imdgpu_sys *s, const double *target, double lr, double *loss,
                          float *grad_out) {
   if (!s || !s->ml_have || !target) return fail(IMDGPU_ERR_STATE, "no weights / targets");
-  int rc = ml_prepare_pairs(s);
+  int rc = batch_full(s);
+  if (rc) return rc;
+  rc = ml_prepare_pairs(s);
   if (rc) return rc;
   double *d = s->d_out;
   CK(cudaMemcpyAsync(d, target, sizeof(double) * 3 * s->n, cudaMemcpyHostToDevice, s->st));
@@ -2835,11 +3144,13 @@ int imdgpu_ml_train_step(imdgpu_sys *s, const double *target, double lr, double 
 int imdgpu_batch_ml_start(imdgpu_sys *s, int *used, double *e_start, double *e_pred) {
   if (!s || s->nsys < 1) return fail(IMDGPU_ERR_STATE, "imdgpu_batch_set_cells first");
   if (!s->ml_have) return fail(IMDGPU_ERR_STATE, "no weights");
+  int rc = batch_full(s);
+  if (rc) return rc;
   if (s->brun) {
     // a batch relaxation was begun on these cells: they may be marked done
     CK(cudaMemset(s->d_sys_done, 0, sizeof(int) * s->nsys));
   }
-  int rc = ml_prepare_pairs(s);  // forces, rho and the list at the start positions
+  rc = ml_prepare_pairs(s);  // forces, rho and the list at the start positions
   if (rc) return rc;
   const int ns = s->nsys;
   if (s->ml_cell_cap < ns) {
@@ -2860,12 +3171,14 @@ int imdgpu_batch_ml_start(imdgpu_sys *s, int *used, double *e_start, double *e_p
   k_save_by_orig<<<nblk(s->n, 256), 256, 0, s->st>>>(v, s->ml_save);
   k_apply_dx<<<nblk(s->n, 256), 256, 0, s->st>>>(v, s->ml_dx, 1.0, nullptr);
   CK(cudaGetLastError());
+  CK(cudaMemsetAsync(s->d_sys_short, 0, sizeof(int) * ns, s->st));
   int one = 1;
   CK(cudaMemcpyAsync(&s->dsc->rebuild, &one, sizeof(int), cudaMemcpyHostToDevice, s->st));
   if ((rc = calc_forces_sync(s))) return rc;
   v = view(s);
   k_cell_energy<<<ns, 256, 0, s->st>>>(s->frc, s->d_aoff, s->ml_ecell + 1, 2);
-  k_ml_select<<<nblk(ns, 128), 128, 0, s->st>>>(s->ml_ecell, ns, s->ml_sel);
+  k_ml_select<<<nblk(ns, 128), 128, 0, s->st>>>(s->ml_ecell, s->d_sys_short, ns, s->ml_sel);
+  CK(cudaMemsetAsync(s->d_sys_short, 0, sizeof(int) * ns, s->st));
   k_restore_by_orig<<<nblk(s->n, 256), 256, 0, s->st>>>(v, s->ml_save, s->ml_sel);
   CK(cudaGetLastError());
   CK(cudaMemcpyAsync(&s->dsc->rebuild, &one, sizeof(int), cudaMemcpyHostToDevice, s->st));

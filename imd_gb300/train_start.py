@@ -41,34 +41,44 @@ def relax_targets(tabs, cells, chunk: int = 512):
     for c0 in range(0, len(cells), chunk):
         part = cells[c0:c0 + chunk]
         r = learned.relax(tabs, part, keep_positions=True)
-        bad = np.flatnonzero(r.status != 0)
-        if len(bad):
-            raise RuntimeError("plain CG did not converge for cells %s" % (bad + c0).tolist())
-        disp += learned.targets(part, r.positions)
+        # cells that did not relax (status != 0) give no target
+        d = learned.targets(part, r.positions)
+        disp += [d[k] if r.status[k] == 0 else None for k in range(len(part))]
         stats.append({"cells": len(part), "seconds": r.seconds, "rounds": r.rounds,
-                      "nfc_mean": float(r.nfc.mean())})
+                      "nfc_mean": float(r.nfc.mean()),
+                      "status": np.bincount(r.status, minlength=5).tolist()})
         print("relaxed %d/%d cells: %.1f s, %d rounds, %.0f force calls per cell"
               % (c0 + len(part), len(cells), r.seconds, r.rounds, r.nfc.mean()), flush=True)
     return disp, stats
 
 
 def evaluate(tabs, cells, w):
+    """Held-out cells relaxed plainly and from the learned start."""
     plain = learned.relax(tabs, cells)
     ml = learned.relax(tabs, cells, weights=w)
     n = np.array([c.n for c in cells])
-    de = (ml.epot - plain.epot) / n
+    both = (plain.status == 0) & (ml.status == 0)
+    de = (ml.epot - plain.epot)[both] / n[both]
     return {
         "cells": len(cells), "atoms": int(n.sum()),
+        "plain_seconds": plain.seconds, "learned_seconds": ml.seconds,
         "plain_relaxations_per_s": plain.relaxations_per_s,
         "learned_relaxations_per_s": ml.relaxations_per_s,
         "speedup": ml.relaxations_per_s / plain.relaxations_per_s,
+        "plain_converged": int((plain.status == 0).sum()),
+        "learned_converged": int((ml.status == 0).sum()),
         "plain_nfc_mean": float(plain.nfc.mean()), "learned_nfc_mean": float(ml.nfc.mean()),
+        "plain_nfc_sum_atoms": float((plain.nfc * n).sum()),
+        "learned_nfc_sum_atoms": float((ml.nfc * n).sum()),
         "plain_rounds": plain.rounds, "learned_rounds": ml.rounds,
         "start_used": int(ml.used.sum()),
-        "final_energy_diff_ev_per_atom_max": float(np.abs(de).max()),
-        "final_energy_diff_ev_per_atom_mean": float(de.mean()),
-        "status_plain": np.bincount(plain.status, minlength=3).tolist(),
-        "status_learned": np.bincount(ml.status, minlength=3).tolist(),
+        "start_energy_gain_ev_per_atom_mean": float(((ml.e_start - ml.e_pred) / n)[ml.used == 1].mean())
+        if ml.used.any() else 0.0,
+        "final_energy_diff_ev_per_atom_max": float(np.abs(de).max()) if both.any() else None,
+        "final_energy_diff_ev_per_atom_mean": float(de.mean()) if both.any() else None,
+        "final_energy_within_1e-6": int((np.abs(de) <= 1e-6).sum()),
+        "status_plain": np.bincount(plain.status, minlength=5).tolist(),
+        "status_learned": np.bincount(ml.status, minlength=5).tolist(),
     }
 
 
@@ -87,6 +97,8 @@ def main(argv=None):
     t0 = time.perf_counter()
     train = wl.defect_batch(a.train_cells, seed=5)
     disp, relax_stats = relax_targets(tabs, train)
+    train = [c for c, d in zip(train, disp) if d is not None]
+    disp = [d for d in disp if d is not None]
     t_data = time.perf_counter() - t0
     t1 = time.perf_counter()
     tr = learned.Trainer(tabs, train, disp, batch_cells=a.batch_cells, seed=a.seed)
@@ -101,7 +113,8 @@ def main(argv=None):
     t_train = time.perf_counter() - t1
     # the same loss with zero displacement: mean |target|^2 per atom
     zero = float(np.mean([np.mean(np.sum(d * d, axis=1)) for d in disp]))
-    rec = {"train_cells": a.train_cells, "train_atoms": int(sum(c.n for c in train)),
+    rec = {"train_cells": a.train_cells, "train_cells_relaxed": len(train),
+           "train_atoms": int(sum(c.n for c in train)),
            "epochs": a.epochs, "batch_cells": a.batch_cells, "lr": a.lr, "adam_steps": steps,
            "loss_initial": loss0, "loss_final": loss1, "loss_zero_prediction": zero,
            "loss_history": tr.history, "seconds_data": t_data, "seconds_train": t_train,

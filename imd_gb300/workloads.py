@@ -224,14 +224,19 @@ def eam_fcc_system(ncell: int = 40, a0: float = 3.615, T: float = 300.0,
 
 def defect_cell(rng, a0: float = 3.615, nmin: int = 500, nmax: int = 20000,
                 nlim=(3, 18), species=CU, strain: float = 0.02, noise: float = 0.05,
-                dumbbell: float = 0.3) -> System:
+                dumbbell: float = 0.3, min_sep: float = 1.8) -> System:
     """One cell of the batched-relaxation workload: an n1 x n2 x n3 fcc cell
     (n_i in nlim) whose atom count follows a log-uniform target in
     [nmin, nmax]; 1-4 defects, each a vacancy or a <100> dumbbell
     interstitial (the site's atom replaced by two atoms at +-dumbbell*a0
-    along a random cube axis); a homogeneous deformation I + e with every
-    component of e uniform in +-strain (a triclinic box); Gaussian position
-    noise of `noise` Angstrom."""
+    along a random cube axis) at uniformly chosen sites; a homogeneous
+    deformation I + e with every component of e uniform in +-strain (a
+    triclinic box); Gaussian position noise of `noise` Angstrom.
+
+    Sites are drawn again when two defects would overlap: when an atom of a
+    dumbbell comes closer than `min_sep` to another atom (two dumbbells on
+    neighbouring sites can put two atoms 1 A apart, where the pair table is
+    below its first point and CG cannot move them apart)."""
     lo, hi = nlim
     while True:
         target = math.exp(rng.uniform(math.log(nmin), math.log(nmax)))
@@ -239,23 +244,43 @@ def defect_cell(rng, a0: float = 3.615, nmin: int = 500, nmax: int = 20000,
         n3 = int(round(target / (4.0 * n1 * n2)))
         if lo <= n3 <= hi:
             break
-    x, box = fcc(n1, n2, n3, a0)
+    x0, box0 = fcc(n1, n2, n3, a0)
     ndef = int(rng.integers(1, 5))
-    sites = rng.choice(len(x), size=ndef, replace=False)
-    keep = np.ones(len(x), bool)
-    extra = []
-    for site in sites:
-        if rng.integers(0, 2) == 0:
-            keep[site] = False
-        else:
-            d = np.zeros(3)
-            d[int(rng.integers(0, 3))] = dumbbell * a0
-            extra.append(x[site] + d)
-            x[site] = x[site] - d
-    x = np.concatenate([x[keep], np.array(extra).reshape(-1, 3)])
+    while True:
+        x = x0.copy()
+        sites = rng.choice(len(x), size=ndef, replace=False)
+        keep = np.ones(len(x), bool)
+        extra, moved = [], []
+        for site in sites:
+            if rng.integers(0, 2) == 0:
+                keep[site] = False
+            else:
+                d = np.zeros(3)
+                d[int(rng.integers(0, 3))] = dumbbell * a0
+                extra.append(x[site] + d)
+                x[site] = x[site] - d
+                moved.append(int(site))
+        x = np.concatenate([x[keep], np.array(extra).reshape(-1, 3)])
+        if not extra:
+            break
+        # dumbbell atoms: the displaced site atoms (kept) and the added ones
+        new_index = np.cumsum(keep) - 1
+        probe = np.concatenate([new_index[moved], len(x) - len(extra) + np.arange(len(extra))])
+        L = np.diag(box0)
+        ok = True
+        for i in probe:
+            d = x - x[i]
+            d -= L * np.round(d / L)
+            r2 = np.einsum("ij,ij->i", d, d)
+            r2[i] = np.inf
+            if r2.min() < min_sep * min_sep:
+                ok = False
+                break
+        if ok:
+            break
     F = np.eye(3) + rng.uniform(-strain, strain, size=(3, 3))
     x = x @ F.T
-    box = box @ F.T
+    box = box0 @ F.T
     x = x + noise * rng.standard_normal(x.shape)
     n = len(x)
     return System(box, x, np.zeros((n, 3)), np.zeros(n, np.int32),

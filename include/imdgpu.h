@@ -175,10 +175,25 @@ int imdgpu_batch_relax(imdgpu_sys *sys, double fmax, int maxsteps, int max_round
  * to max_rounds more rounds; *ndone = cells finished so far */
 int imdgpu_batch_begin(imdgpu_sys *sys, double fmax, int maxsteps);
 int imdgpu_batch_advance(imdgpu_sys *sys, int max_rounds, int *ndone, int *rounds);
+/* Compaction: once the unfinished cells hold at most pct % of the atoms on
+ * the device, the finished cells leave the device batch (their results and
+ * final positions stay with the handle), so that later rounds cost what the
+ * unfinished cells cost.  Default 50; 0 turns it off.  Calls that need every
+ * cell (imdgpu_batch_begin, imdgpu_get_atoms, imdgpu_calc_forces, the ml_
+ * calls) bring all cells back first.  New: IMD has no batches. */
+int imdgpu_batch_set_compaction(imdgpu_sys *sys, int pct);
+/* positions of every atom of imdgpu_batch_set_cells (3 per atom, in that
+ * order), whether or not its cell is still on the device */
+int imdgpu_batch_positions(imdgpu_sys *sys, double *x);
 /* neighbour-list rebuilds since imdgpu_batch_begin */
 int imdgpu_batch_rebuilds(imdgpu_sys *sys, long *n);
 /* per cell: final energy, max |F|, CG steps, force calls (nfc), status
- * (0 converged, 1 not converged, 2 "Too many iterations in brent") */
+ * (0 converged, 1 not converged within maxsteps or the rounds, 2 "Too many
+ * iterations in brent", 3 line-search control failure, 4 five line
+ * searches in a row ended, without lowering the energy, on a point with a
+ * pair closer than a table's first point (IMD's "Short distance"), where the
+ * tables clamp and energy and forces no longer match, so CG cannot leave
+ * it: the cell is stopped) */
 int imdgpu_batch_results(imdgpu_sys *sys, double *epot, double *fmax, int *steps, int *nfc,
                          int *status);
 

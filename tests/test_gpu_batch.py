@@ -71,3 +71,42 @@ def test_batch_mixed_precision_relaxes():
     n = np.array([c.n for c in cells])
     assert np.all(r64["status"] == 0)
     assert np.all(np.abs(rm["epot"] - r64["epot"]) / n <= 1e-6), (rm, r64)
+
+
+def test_compaction_keeps_every_cell_result():
+    """Finished cells leave the device batch (compaction at every chance with
+    pct = 100); every cell still ends at the energy of the uncompacted run,
+    positions() returns each cell's final positions (the oracle's energy of
+    them is the reported one) and bringing all cells back restores them."""
+    import oracle
+    from imd_gb300 import api, learned
+    from imd_gb300 import workloads as wl
+    from oracle import OracleSystem
+    rng = np.random.default_rng(13)
+    cells = [wl.defect_cell(rng, nmin=200, nmax=700, nlim=(3, 6)) for _ in range(6)]
+    out = {}
+    for pct in (0, 100):
+        b = api.GpuBatch(1, api.EAM2, api.FP64, api.SPLINE)
+        b.read_tables(tables("cu"))
+        b.set_cells(cells)
+        b.set_compaction(pct)
+        b.relax(1e-4)
+        out[pct] = (b.results(), b.positions(), b)
+    r0, _, _ = out[0]
+    r1, x1, b1 = out[100]
+    n = np.array([c.n for c in cells])
+    assert np.all(r0["status"] == 0) and np.all(r1["status"] == 0)
+    assert np.all(r1["fmax"] <= 1e-4)
+    assert np.all(np.abs(r1["epot"] - r0["epot"]) / n <= 1e-8), (r1["epot"] - r0["epot"]) / n
+    oracle.set_interpolation(oracle.SPLINE)
+    try:
+        for k, c in enumerate(cells):
+            o = OracleSystem(c.box, x1[k], c.types, c.mass, c.number, 1, tables("cu"), True, 0.4)
+            o.calc_forces()
+            assert abs(o.epot_total - r1["epot"][k]) <= 1e-10 * abs(o.epot_total)
+    finally:
+        oracle.set_interpolation(oracle.QUADRATIC)
+    # all cells back on the device: their energies at the final positions
+    b1.ml_set_weights(np.zeros(learned.NPARAM, np.float32))
+    used, e0, e1 = b1.ml_start()
+    assert np.allclose(e0, r1["epot"], rtol=1e-11, atol=0)

@@ -64,49 +64,88 @@ def _small_cells(seed, k, nmin=300, nmax=900):
     return [wl.defect_cell(rng, nmin=nmin, nmax=nmax, nlim=(3, 6)) for _ in range(k)]
 
 
+def _centroid_weights(b3):
+    """Weights whose pair output is the constant b3: dx_i = b3 sum_j unit(r_ij),
+    which moves a noisy atom towards (b3 > 0) or away from (b3 < 0) the
+    centre of its neighbours."""
+    from imd_gb300 import learned
+    w = np.zeros(learned.NPARAM, np.float32)
+    w[learned.OFF_B3] = b3
+    return w
+
+
+def _noisy_crystal(seed, dims=(4, 5, 4), noise=0.05):
+    """A defect-free Cu cell with Gaussian position noise."""
+    from imd_gb300 import workloads as wl
+    x, box = wl.fcc(*dims, 3.615)
+    x = x + noise * np.random.default_rng(seed).standard_normal(x.shape)
+    n = len(x)
+    return wl.System(box, x, np.zeros((n, 3)), np.zeros(n, np.int32), np.full(n, wl.CU.mass),
+                     np.arange(n, dtype=np.int32))
+
+
 def test_batch_ml_start_energies_and_gate():
     """imdgpu_batch_ml_start: e_start of every cell is the oracle's energy of
-    the cell, e_pred is the energy at start + predicted displacement, and
-    exactly the cells with e_pred < e_start keep the prediction."""
+    the cell, e_pred the oracle's energy at start + predicted displacement,
+    and exactly the cells with e_pred < e_start keep the prediction.  Moving
+    every atom towards the centre of its neighbours lowers the energy of a
+    noisy perfect crystal, so those cells keep it."""
     from imd_gb300 import api, learned
     from oracle import OracleSystem
-    cells = _small_cells(21, 4)
-    w = learned.init_weights(7)
-    w[learned.OFF_W3:learned.OFF_B3] *= 30.0  # displacements large enough to matter
-    b = learned.make_batch(tables("cu"), cells)
-    b.ml_set_weights(w)
-    # prediction at the start positions, cell by cell through single systems
-    pred = []
-    for c in cells:
-        s = api.system_from_tables(tables("cu"), c.box, c.number, c.types, c.mass, c.x)
-        s.ml_set_weights(w)
-        pred.append(s.ml_predict())
-        s.close()
+    cells = _small_cells(21, 2) + [_noisy_crystal(1), _noisy_crystal(2, (3, 6, 5))]
+    b = learned.make_batch(tables("cu"), cells, interpolation=api.QUADRATIC)
+    b.ml_set_weights(_centroid_weights(0.08))
+    pred = np.split(b.ml_predict(), np.cumsum(b.natoms)[:-1])
     used, e0, e1 = b.ml_start()
     xs = b.positions()
+    assert used[2] == 1 and used[3] == 1, (e0, e1)
     for k, c in enumerate(cells):
+        assert 0.005 < np.abs(pred[k]).max() < 0.5
         o = OracleSystem(c.box, c.x, c.types, c.mass, c.number, 1, tables("cu"), True, 0.4)
         o.calc_forces()
         assert abs(e0[k] - o.epot_total) <= 1e-12 * abs(o.epot_total)
-        o2 = OracleSystem(c.box, c.x + pred[k], c.types, c.mass, c.number, 1, tables("cu"),
-                          True, 0.4)
-        o2.calc_forces()
-        assert abs(e1[k] - o2.epot_total) <= 1e-9 * abs(o2.epot_total)
         assert used[k] == (e1[k] < e0[k])
-        expect = c.x + pred[k] if used[k] else c.x
-        d = learned.min_image(xs[k] - expect, np.asarray(c.box))
-        assert np.abs(d).max() < 1e-6, (k, used[k], np.abs(d).max())
+        ref = c.x + pred[k] if used[k] else c.x
+        d = learned.min_image(xs[k] - ref, np.asarray(c.box))
+        # the displacement is recomputed inside ml_start: FP32 sums in another order
+        assert np.abs(d).max() < (1e-6 if used[k] else 1e-12), (k, used[k], np.abs(d).max())
+        # energy at the predicted positions: exact positions where they were kept
+        o2 = OracleSystem(c.box, xs[k] if used[k] else c.x + pred[k], c.types, c.mass, c.number,
+                          1, tables("cu"), True, 0.4)
+        o2.calc_forces()
+        tol = 1e-11 if used[k] else 1e-7
+        assert abs(e1[k] - o2.epot_total) <= tol * abs(o2.epot_total), (k, e1[k], o2.epot_total)
+
+
+def _vacancy_cells(seed, k):
+    """Cells whose relaxation is local: a strained, noisy fcc cell (3-6 cubic
+    cells per side) with one vacancy."""
+    from imd_gb300 import workloads as wl
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(k):
+        dims = [int(v) for v in rng.integers(3, 7, size=3)]
+        x, box = wl.fcc(*dims, 3.615)
+        x = np.delete(x, int(rng.integers(len(x))), axis=0)
+        F = np.eye(3) + rng.uniform(-0.02, 0.02, size=(3, 3))
+        x = x @ F.T + 0.05 * rng.standard_normal(x.shape)
+        n = len(x)
+        out.append(wl.System(box @ F.T, x, np.zeros((n, 3)), np.zeros(n, np.int32),
+                             np.full(n, wl.CU.mass), np.arange(n, dtype=np.int32)))
+    return out
 
 
 def test_learned_start_beats_plain_cg():
-    """Train on displacements that the plain batched CG produced for small
-    defect cells, then relax held-out cells from the learned start: the
-    start lowers the energy of every held-out cell, CG needs fewer force
-    calls in total (the learned start's two included), and the final
-    energies equal plain CG's within 1e-6 eV/atom."""
+    """Train on displacements that the plain batched CG produced, then relax
+    held-out cells from the learned start: the start lowers every held-out
+    cell's energy, CG needs fewer force calls in total (the learned start's
+    two included), and every cell ends at plain CG's energy within
+    1e-6 eV/atom.  Cells with one vacancy: their relaxation is the removal
+    of the position noise plus the vacancy's small local field, what a
+    pair-additive displacement model can learn."""
     from imd_gb300 import learned
-    train = _small_cells(31, 24)
-    held = _small_cells(32, 8)
+    train = _vacancy_cells(31, 24)
+    held = _vacancy_cells(32, 8)
     plain_train = learned.relax(tables("cu"), train, keep_positions=True)
     assert np.all(plain_train.status == 0)
     disp = learned.targets(train, plain_train.positions)
