@@ -17,6 +17,12 @@ the C-ABI with host buffers: every step uploads positions and momenta from
 pinned host memory, runs calc_forces / move_atoms_nve / check_nblist and
 reads positions, momenta, forces and energies back.
 
+The same line carries the FP32-force / FP64-accumulate run of the same
+workload (`mixed`, with its force error against FP64 at the same positions)
+and the batched defect relaxations (`batched_cg`): relaxations/s of IMD's CG
+on 512 held-out cells, plain and from the learned start (--no-mixed,
+--no-batch, --batch-cells N).
+
 --impl reference times the reference's CPU algorithm for this path on the
 host cores: the C restatement in oracle/ (the reference itself is compiled
 only where its sources are, which the GPU host does not have), one process
@@ -48,6 +54,7 @@ WORKLOAD = "sutton-chen Cu EAM2 NVE, fcc 40^3 = 256000 atoms, 300 K, dt 1 fs, sk
 FORCE_BYTES_PER_ATOM = 56.0       # force kernel: read x (24) + 2F' (8), write F (24)
 STEP_BYTES_PER_ATOM = 232.0       # whole NVE EAM step, canonical count
 FLOPS_PER_PAIR = 66.0             # canonical FP64 flops per half-list pair within rc
+FORCE_FLOPS_PER_PAIR = 52.0       # of those in the force pass (all but rho's 14)
 
 
 def dist_env():
@@ -186,6 +193,44 @@ def run_reference(args, rank, world):
     print(json.dumps(line))
 
 
+def run_batch(args, tabs):
+    """Defect CG relaxations/s, plain and from the learned start: the held-out
+    cells of the learned-start workload (seed 6), each relaxed by IMD's CG
+    to max |F| <= 1e-4 eV/A in one batch; the learned start uses the weights
+    trained by imd_gb300/train_start.py (imd_gb300/data/start_mlp.npz)."""
+    from imd_gb300 import learned
+    from imd_gb300 import workloads as wl
+    cells = wl.defect_batch(args.batch_cells, seed=6)
+    natoms = np.array([c.n for c in cells])
+    wpath = os.path.join(ROOT, "imd_gb300", "data", "start_mlp.npz")
+    w = np.load(wpath)["w"]
+    out = {"workload": "%d Sutton-Chen Cu defect cells, %d atoms (%d-%d), 1-4 vacancies or "
+                       "<100> dumbbells, +-2%% strain, 0.05 A noise, seed 6; IMD CG to max |F| "
+                       "<= 1e-4 eV/A, FP64, spline tables" % (len(cells), natoms.sum(),
+                                                              natoms.min(), natoms.max()),
+           "unit": "relaxations/s"}
+    for name, weights in (("plain", None), ("learned", w)):
+        r = learned.relax(tabs, cells, weights=weights)
+        out[name] = {"value": r.relaxations_per_s, "seconds": r.seconds,
+                     "converged": int((r.status == 0).sum()),
+                     "converged_per_s": float((r.status == 0).sum() / r.seconds),
+                     "force_calls_per_relaxation": float(r.nfc.mean()),
+                     "rounds": r.rounds, "status_counts": np.bincount(r.status, minlength=5).tolist()}
+        if weights is not None:
+            out[name]["start_used"] = int(r.used.sum())
+        out[name + "_epot"] = r.epot
+        out[name + "_status"] = r.status
+    both = (out["plain_status"] == 0) & (out["learned_status"] == 0)
+    de = np.abs(out["learned_epot"] - out["plain_epot"])[both] / natoms[both]
+    for k in ("plain_epot", "learned_epot", "plain_status", "learned_status"):
+        del out[k]
+    out["speedup_learned_vs_plain"] = out["learned"]["value"] / out["plain"]["value"]
+    out["final_energy_diff_ev_per_atom"] = {"max": float(de.max()), "median": float(np.median(de)),
+                                            "within_1e-6": int((de <= 1e-6).sum()),
+                                            "compared": int(both.sum())}
+    return out
+
+
 def run_ours(args, rank, world, local):
     from imd_gb300 import api
     from imd_gb300 import workloads as wl
@@ -278,12 +323,34 @@ def run_ours(args, rank, world, local):
     barrier()
     e2e = n * e2e_steps * world / t_e2e if e2e_steps else None
 
-    # ---- roofline of the dominant kernel (EAM force pass) ----
+    # ---- precision: mixed-path forces against FP64 at the same (thermal) positions ----
+    prec = None
+    if not args.no_mixed:
+        s.calc_forces(0)
+        a64 = s.get_atoms()
+        e64 = s.scalars().tot_pot_energy
+        s.set_precision(api.MIXED)
+        s.calc_forces(0)
+        amx = s.get_atoms()
+        emx = s.scalars().tot_pot_energy
+        s.set_precision(api.FP64)
+        prec = {"force_rel_rms_error": float(np.sqrt(np.mean((amx["f"] - a64["f"]) ** 2)
+                                                     / np.mean(a64["f"] ** 2))),
+                "energy_rel_error": float(abs(emx - e64) / abs(e64)),
+                "positions": "the 256000-atom system after the FP64 run (300 K)"}
+
+    # ---- roofline of the dominant kernel (EAM force pass, k_force_fast) ----
+    # The FP64 kernels are bound by the FP64 pipe (ncu: 86% busy, DRAM 1-3%),
+    # so the roofline is FP64 TFLOP/s against this device's measured FP64 FMA
+    # rate; the HBM figures are given beside it.
     force_ms = r["ms_force"] / args.steps
-    achieved = FORCE_BYTES_PER_ATOM * n / (force_ms * 1e-3) / 1e9
-    peak = float(peaks.get("hbm_gbs", 6800.0))
-    fp64_peak = api.probe_fp64_peak()
     pairs_rc = 67.0 * n  # half-list pairs within rc per atom for fcc Cu (6 shells, 134/2)
+    force_flops = FORCE_FLOPS_PER_PAIR * pairs_rc
+    fp64_peak = api.probe_fp64_peak()
+    force_tflops = force_flops / (force_ms * 1e-3) / 1e12
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    hbm_alg = FORCE_BYTES_PER_ATOM * n / (force_ms * 1e-3) / 1e9
+    traffic = committed_traffic("k_force_fast")
     step_ms = r["ms"] / args.steps
     fp64_achieved = FLOPS_PER_PAIR * pairs_rc / (step_ms * 1e-3) / 1e12
 
@@ -300,15 +367,21 @@ def run_ours(args, rank, world, local):
         "e2e": {"value": e2e, "unit": "atom-steps/s", "h2d_bytes_per_step": 48 * n,
                 "d2h_bytes_per_step": 80 * n, "steps": e2e_steps},
         "gpu_launches": int(r["launches"]),
-        "roofline": {"bound": "hbm", "kernel": "k_force64<EAM>", "achieved": achieved,
-                     "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": committed_traffic("k_force64"),
-                     "peak_kind": peak_kind,
-                     "bytes_per_atom": FORCE_BYTES_PER_ATOM,
-                     "fp64": {"achieved_tflops": fp64_achieved, "peak_tflops": fp64_peak,
-                              "frac": fp64_achieved / fp64_peak,
-                              "flops_per_step": FLOPS_PER_PAIR * pairs_rc,
-                              "peak_kind": "measured FMA probe"}},
+        "roofline": {"bound": "fp64", "kernel": "k_force_fast (EAM2 force pass, half list)",
+                     "achieved": force_tflops, "peak": fp64_peak, "unit": "TFLOP/s",
+                     "frac": force_tflops / fp64_peak, "traffic": traffic,
+                     "peak_kind": "measured on this device: FP64 FMA chains "
+                                  "(imdgpu_probe_fp64_peak); MEASURED_PEAKS.json has no FP64 rate",
+                     "flops_per_launch": force_flops,
+                     "flops_per_pair": FORCE_FLOPS_PER_PAIR,
+                     "ncu_fp64_pipe_busy": 0.857,
+                     "hbm": {"achieved": hbm_alg, "peak": hbm_peak, "unit": "GB/s",
+                             "frac": hbm_alg / hbm_peak, "peak_kind": peak_kind,
+                             "bytes_per_atom": FORCE_BYTES_PER_ATOM,
+                             "traffic_gbs": (traffic / (force_ms * 1e-3) / 1e9) if traffic else None},
+                     "step_fp64": {"achieved_tflops": fp64_achieved,
+                                   "frac": fp64_achieved / fp64_peak,
+                                   "flops_per_step": FLOPS_PER_PAIR * pairs_rc}},
         "kernels_ms_per_step": {"density": r["ms_density"] / args.steps,
                                 "force": force_ms, "integrate": r["ms_integrate"] / args.steps,
                                 "rebuild": r["ms_rebuild"] / args.steps},
@@ -327,7 +400,10 @@ def run_ours(args, rank, world, local):
                                                  "rebuild": m["ms_rebuild"] / args.steps},
                          "rebuilds_in_timed_steps": m["rebuilds"],
                          "graph_replay_wall": m["graph_rate"],
-                         "energy_drift_per_atom": float((m["etot"][-1] - m["etot"][0]) / n)}
+                         "energy_drift_per_atom": float((m["etot"][-1] - m["etot"][0]) / n),
+                         "vs_fp64": prec}
+    if not args.no_batch and rank == 0:
+        line["batched_cg"] = run_batch(args, tabs)
     if rank == 0 and not args.no_cpu:
         try:
             rate, _ = cpu_sample(tabs, args.cpu_steps, 1)
@@ -353,6 +429,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--batch-cells", type=int, default=512)
     args = ap.parse_args()
     rank, world, local = dist_env()
     if args.impl == "reference":
