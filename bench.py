@@ -262,6 +262,7 @@ def run_ours(args, rank, world, local):
         if name == "mixed" and args.no_mixed:
             continue
         s = build(prec)
+        blocks = s.autotune()   # density / force block shapes, outside the timed steps
         s.nve_run(max(args.warmup, 3), dt, record=False)
         s.set_profiling(True)
         s.set_l2_flush(256 << 20)
@@ -282,7 +283,7 @@ def run_ours(args, rank, world, local):
                          ms_integrate=t.ms_integrate, ms_rebuild=t.ms_rebuild,
                          rebuilds=t.rebuilds, launches=t.kernel_launches,
                          clocks=clk.summary(), etot=(ep + ek), nb=sc.nb_entries, sys=s,
-                         graph_rate=graph_rate)
+                         graph_rate=graph_rate, blocks=blocks)
     r = res["fp64"]
     ms_max = r["ms"]
     if dist:
@@ -362,7 +363,8 @@ def run_ours(args, rank, world, local):
         "config": {"workload": WORKLOAD, "precision": "fp64", "atoms": n,
                    "parallelism": "replicas" if world > 1 else "single",
                    "l2": "256 MiB scratch write between timed steps (outside the windows)",
-                   "list_entries": r["nb"], "rebuilds_in_timed_steps": r["rebuilds"]},
+                   "list_entries": r["nb"], "rebuilds_in_timed_steps": r["rebuilds"],
+                   "autotuned_blocks": {"density": r["blocks"][0], "force": r["blocks"][1]}},
         "clocks": r["clocks"],
         "e2e": {"value": e2e, "unit": "atom-steps/s", "h2d_bytes_per_step": 48 * n,
                 "d2h_bytes_per_step": 80 * n, "steps": e2e_steps},
@@ -399,6 +401,7 @@ def run_ours(args, rank, world, local):
                                                  "integrate": m["ms_integrate"] / args.steps,
                                                  "rebuild": m["ms_rebuild"] / args.steps},
                          "rebuilds_in_timed_steps": m["rebuilds"],
+                         "autotuned_blocks": {"density": m["blocks"][0], "force": m["blocks"][1]},
                          "graph_replay_wall": m["graph_rate"],
                          "energy_drift_per_atom": float((m["etot"][-1] - m["etot"][0]) / n),
                          "vs_fp64": prec}

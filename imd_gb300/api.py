@@ -105,6 +105,9 @@ def lib() -> C.CDLL:
         L.imdgpu_batch_advance.argtypes = [vp, C.c_int, _ip, _ip]
         L.imdgpu_batch_rebuilds.argtypes = [vp, C.POINTER(C.c_long)]
         L.imdgpu_batch_set_compaction.argtypes = [vp, C.c_int]
+        L.imdgpu_autotune.argtypes = [vp, _ip, _ip]
+        L.imdgpu_set_blocks.argtypes = [vp, C.c_int, C.c_int]
+        L.imdgpu_batch_set_autotune.argtypes = [vp, C.c_int]
         L.imdgpu_batch_positions.argtypes = [vp, _dp]
         fp = C.POINTER(C.c_float)
         L.imdgpu_ml_nparam.argtypes = []
@@ -342,6 +345,16 @@ class GpuSystem:
                                           _p(g, C.c_float)), "ml_train_step")
         return (loss.value, g) if want_grad else loss.value
 
+    def autotune(self):
+        """Pick the density and force passes' blocks by timing; returns both."""
+        bd = C.c_int(0)
+        bf = C.c_int(0)
+        _check(lib().imdgpu_autotune(self.h, C.byref(bd), C.byref(bf)), "autotune")
+        return bd.value, bf.value
+
+    def set_blocks(self, density: int, force: int) -> None:
+        _check(lib().imdgpu_set_blocks(self.h, int(density), int(force)), "set_blocks")
+
     def timing(self) -> Timing:
         t = Timing()
         _check(lib().imdgpu_get_timing(self.h, C.byref(t)), "get_timing")
@@ -429,6 +442,10 @@ class GpuBatch(GpuSystem):
         x = np.empty((self.n, 3))
         _check(lib().imdgpu_batch_positions(self.h, _p(x)), "batch_positions")
         return np.split(x, np.cumsum(self.natoms)[:-1])
+
+    def set_autotune(self, on: bool) -> None:
+        """Tune the block shape at every imdgpu_batch_begin (default on)."""
+        _check(lib().imdgpu_batch_set_autotune(self.h, int(bool(on))), "batch_set_autotune")
 
     def set_compaction(self, pct: int) -> None:
         """Drop finished cells from the device once the unfinished ones hold

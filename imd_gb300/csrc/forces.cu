@@ -29,7 +29,7 @@ __global__ void k_ghost_pos(SysView v) {
 // ---------------------------------------------------------------------------
 // density pass: loop 1 EAM branch (src/imd_forces_nbl.c:586-611, :907-918)
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(BS_FORCE) k_density64(SysView v, DevTable rho) {
+__global__ void __launch_bounds__(BS_FORCE_MAX) k_density64(SysView v, DevTable rho) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= v.n) return;
   const double4 pi = v.pos[i];
@@ -100,7 +100,7 @@ __global__ void k_ghost_df(SysView v) {
 // reference: -r^2 grad for the pair part, -d.F for the EAM part.
 // ---------------------------------------------------------------------------
 template <bool EAM>
-__global__ void __launch_bounds__(BS_FORCE) k_force64(SysView v, DevTable pair, DevTable rho,
+__global__ void __launch_bounds__(BS_FORCE_MAX) k_force64(SysView v, DevTable pair, DevTable rho,
                                                       double *partial) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   double acc[2] = {0.0, 0.0};  // energy, virial
@@ -162,7 +162,7 @@ __global__ void __launch_bounds__(BS_FORCE) k_force64(SysView v, DevTable pair, 
     atomicAdd(fi + 3, ee);
     if (shortf) flag_short(v, i);
   }
-  block_sum_store<2, BS_FORCE>(acc, partial);
+  block_sum_store_dyn<2, BS_FORCE_MAX>(acc, partial);
 }
 
 // send_forces(add_forces) (src/imd_forces_nbl.c:1997)
@@ -206,7 +206,7 @@ __global__ void k_finalize_forces(const double *pe, int ne, const double *pf, in
 // pairs and formulas as above; only rounding differs (~1e-16 relative).
 // ---------------------------------------------------------------------------
 template <bool NT1, bool CUB>
-__global__ void __launch_bounds__(BS_FORCE) k_density_fast(SysView v, DevTable rho) {
+__global__ void __launch_bounds__(BS_FORCE_MAX) k_density_fast(SysView v, DevTable rho) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= v.n || atom_idle(v, i)) return;
   const double4 pi = v.pos[i];
@@ -248,7 +248,7 @@ __global__ void __launch_bounds__(BS_FORCE) k_density_fast(SysView v, DevTable r
 }
 
 template <bool NT1, bool EAM, bool EPOT, bool SAMEGRID, bool CUB>
-__global__ void __launch_bounds__(BS_FORCE) k_force_fast(SysView v, DevTable pair, DevTable rho,
+__global__ void __launch_bounds__(BS_FORCE_MAX) k_force_fast(SysView v, DevTable pair, DevTable rho,
                                                          double *partial) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   double acc[2] = {0.0, 0.0};  // energy, virial
@@ -330,7 +330,7 @@ __global__ void __launch_bounds__(BS_FORCE) k_force_fast(SysView v, DevTable pai
     acc[1] = vir;
     if (shortf) flag_short(v, i);
   }
-  block_sum_store<2, BS_FORCE>(acc, partial);
+  block_sum_store_dyn<2, BS_FORCE_MAX>(acc, partial);
 }
 
 // embedding with the coefficient-form table
@@ -354,11 +354,11 @@ static void launch_force_fast(int samegrid, int nbf, cudaStream_t st, const SysV
                               const ForceTabs &t, double *pf) {
   const bool cub = (t.pair.mode != TAB_QUADRATIC);
   if (samegrid) {
-    if (cub) k_force_fast<NT1, EAM, EPOT, true, true><<<nbf, BS_FORCE, 0, st>>>(v, t.pair, t.rho, pf);
-    else k_force_fast<NT1, EAM, EPOT, true, false><<<nbf, BS_FORCE, 0, st>>>(v, t.pair, t.rho, pf);
+    if (cub) k_force_fast<NT1, EAM, EPOT, true, true><<<nbf, t.bs, 0, st>>>(v, t.pair, t.rho, pf);
+    else k_force_fast<NT1, EAM, EPOT, true, false><<<nbf, t.bs, 0, st>>>(v, t.pair, t.rho, pf);
   } else {
-    if (cub) k_force_fast<NT1, EAM, EPOT, false, true><<<nbf, BS_FORCE, 0, st>>>(v, t.pair, t.rho, pf);
-    else k_force_fast<NT1, EAM, EPOT, false, false><<<nbf, BS_FORCE, 0, st>>>(v, t.pair, t.rho, pf);
+    if (cub) k_force_fast<NT1, EAM, EPOT, false, true><<<nbf, t.bs, 0, st>>>(v, t.pair, t.rho, pf);
+    else k_force_fast<NT1, EAM, EPOT, false, false><<<nbf, t.bs, 0, st>>>(v, t.pair, t.rho, pf);
   }
 }
 
@@ -374,8 +374,8 @@ static void launch_force_fast2(const ForceTabs &t, int nbf, cudaStream_t st, con
 static void launch_force_any(const ForceTabs &t, int nbf, cudaStream_t st, const SysView &v,
                              double *pf) {
   if (t.exact && t.pair.mode == TAB_QUADRATIC) {
-    if (t.eam) k_force64<true><<<nbf, BS_FORCE, 0, st>>>(v, t.pair, t.rho, pf);
-    else k_force64<false><<<nbf, BS_FORCE, 0, st>>>(v, t.pair, t.rho, pf);
+    if (t.eam) k_force64<true><<<nbf, t.bs, 0, st>>>(v, t.pair, t.rho, pf);
+    else k_force64<false><<<nbf, t.bs, 0, st>>>(v, t.pair, t.rho, pf);
     return;
   }
   if (t.eam) {
@@ -402,17 +402,17 @@ int launch_forces(const SysView &v, const ForceTabs &t, DevScalars *sc, int mixe
   cudaMemsetAsync(v.frc, 0, ext * sizeof(double4), st);
   k_ghost_pos<<<gblocks, BS_VEC, 0, st>>>(v);
   launches++;
-  const int nbf = nblk(v.n, BS_FORCE), nbe = nblk(v.n, BS_VEC);
+  const int nbf = nblk(v.n, t.bs), nbe = nblk(v.n, BS_VEC), nbr = nblk(v.n, t.bs_rho);
   double *pe = v.partial, *pf = v.partial + nbe;
   if (t.eam) {
     cudaMemsetAsync(v.rho, 0, ext * sizeof(double), st);
     if (ev) cudaEventRecord(ev[0], st);
     const bool quad = (t.rho.mode == TAB_QUADRATIC);
-    if (t.exact && quad) k_density64<<<nbf, BS_FORCE, 0, st>>>(v, t.rho);
-    else if (t.nt1 && quad) k_density_fast<true, false><<<nbf, BS_FORCE, 0, st>>>(v, t.rho);
-    else if (t.nt1) k_density_fast<true, true><<<nbf, BS_FORCE, 0, st>>>(v, t.rho);
-    else if (quad) k_density_fast<false, false><<<nbf, BS_FORCE, 0, st>>>(v, t.rho);
-    else k_density_fast<false, true><<<nbf, BS_FORCE, 0, st>>>(v, t.rho);
+    if (t.exact && quad) k_density64<<<nbr, t.bs_rho, 0, st>>>(v, t.rho);
+    else if (t.nt1 && quad) k_density_fast<true, false><<<nbr, t.bs_rho, 0, st>>>(v, t.rho);
+    else if (t.nt1) k_density_fast<true, true><<<nbr, t.bs_rho, 0, st>>>(v, t.rho);
+    else if (quad) k_density_fast<false, false><<<nbr, t.bs_rho, 0, st>>>(v, t.rho);
+    else k_density_fast<false, true><<<nbr, t.bs_rho, 0, st>>>(v, t.rho);
     if (ev) cudaEventRecord(ev[1], st);
     k_fold_rho<<<gblocks, BS_VEC, 0, st>>>(v);
     if (t.exact && t.embed.mode == TAB_QUADRATIC) k_embed<<<nbe, BS_VEC, 0, st>>>(v, t.embed, pe);

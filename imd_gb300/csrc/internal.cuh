@@ -394,4 +394,25 @@ __device__ __forceinline__ void block_sum_store(double (&v)[K], double *out) {
   }
 }
 
+// The same for any block of at most MAXBS threads, a multiple of 32 (the
+// block shape the autotuner picked); deterministic for a given shape.
+template <int K, int MAXBS>
+__device__ __forceinline__ void block_sum_store_dyn(double (&v)[K], double *out) {
+  __shared__ double sh[K][MAXBS / 32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int k = 0; k < K; k++) {
+    double s = warp_sum(v[k]);
+    if (lane == 0) sh[k][w] = s;
+  }
+  __syncthreads();
+  if (threadIdx.x < K) {
+    double s = 0.0;
+#pragma unroll
+    for (int i = 0; i < MAXBS / 32; i++)
+      if (i < nw) s += sh[threadIdx.x][i];
+    out[(size_t)blockIdx.x * K + threadIdx.x] = s;
+  }
+}
+
 }  // namespace imdgpu

@@ -14,6 +14,8 @@ struct ForceTabs {
   int samegrid;  // pair and rho columns share begin / end / step: one index per pair
   int exact;     // IMD's unfused arithmetic (bitwise table values) instead of FMA form
   int epot;      // scatter per-atom energies (POTENG) in the force pass
+  int bs;        // threads per block of the force pass (autotuned, multiple of 32)
+  int bs_rho;    // threads per block of the density pass (autotuned)
 };
 
 // Device-side scalars of one system (results + control).
@@ -50,7 +52,9 @@ struct CgSys {
   int nshort, pad;                                       // line searches ended short, in a row
 };
 
-constexpr int BS_FORCE = 128;
+constexpr int BS_FORCE = 128;      // default block of the pair passes
+constexpr int BS_FORCE_MAX = 128;  // largest block the autotuner may pick (the
+                                   // kernels' launch bound; register use as tuned)
 constexpr int BS_VEC = 256;
 
 // forces.cu

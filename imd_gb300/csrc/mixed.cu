@@ -57,7 +57,7 @@ __device__ __forceinline__ float polyf_g(const DevTable &t, int col, int k, floa
 
 // rho_i = sum_j rho_{it,jt}(r_ij) over the full list (loop 1's eam_r)
 template <bool NT1>
-__global__ void __launch_bounds__(BS_FORCE) k_density_mixed(SysView v, DevTable rho,
+__global__ void __launch_bounds__(BS_FORCE_MAX) k_density_mixed(SysView v, DevTable rho,
                                                             const SplitPos *sp) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= v.n || atom_idle(v, i)) return;
@@ -115,7 +115,7 @@ __global__ void k_ghost_dff(SysView v, float *dff) {
 // forces over the full list: each directed pair adds d*grad to atom i and
 // half of the pair energy and virial
 template <bool NT1, bool EAM>
-__global__ void __launch_bounds__(BS_FORCE) k_force_mixed(SysView v, DevTable pair,
+__global__ void __launch_bounds__(BS_FORCE_MAX) k_force_mixed(SysView v, DevTable pair,
                                                           DevTable rho, const SplitPos *sp,
                                                           const float *dff, int pair_only_epot,
                                                           double *partial) {
@@ -184,7 +184,7 @@ __global__ void __launch_bounds__(BS_FORCE) k_force_mixed(SysView v, DevTable pa
     if (shortf) flag_short(v, i);
   }
   (void)pair_only_epot;
-  block_sum_store<2, BS_FORCE>(acc, partial);
+  block_sum_store_dyn<2, BS_FORCE_MAX>(acc, partial);
 }
 
 __global__ void k_finalize_mixed(const double *pe, int ne, const double *pf, int nf,
@@ -214,19 +214,19 @@ int launch_forces_mixed(const SysView &v, const ForceTabs &t, DevScalars *sc, fl
   cudaMemsetAsync(v.frc, 0, (size_t)v.ncap * sizeof(double4), st);
   k_ghost_pos_launch(v, gblocks, st);
   k_split<<<nblk(ext, BS_VEC), BS_VEC, 0, st>>>(v, sp);
-  const int nbf = nblk(v.n, BS_FORCE), nbe = nblk(v.n, BS_VEC);
+  const int nbf = nblk(v.n, t.bs), nbe = nblk(v.n, BS_VEC), nbr = nblk(v.n, t.bs_rho);
   double *pe = v.partial, *pf = v.partial + nbe;
   int launches = 4;
   if (t.eam) {
     if (ev) cudaEventRecord(ev[0], st);
-    if (t.nt1) k_density_mixed<true><<<nbf, BS_FORCE, 0, st>>>(v, t.rho, sp);
-    else k_density_mixed<false><<<nbf, BS_FORCE, 0, st>>>(v, t.rho, sp);
+    if (t.nt1) k_density_mixed<true><<<nbr, t.bs_rho, 0, st>>>(v, t.rho, sp);
+    else k_density_mixed<false><<<nbr, t.bs_rho, 0, st>>>(v, t.rho, sp);
     if (ev) cudaEventRecord(ev[1], st);
     k_embed_mixed<<<nbe, BS_VEC, 0, st>>>(v, t.embed, dff, pe);
     k_ghost_dff<<<gblocks, BS_VEC, 0, st>>>(v, dff);
     if (ev) cudaEventRecord(ev[2], st);
-    if (t.nt1) k_force_mixed<true, true><<<nbf, BS_FORCE, 0, st>>>(v, t.pair, t.rho, sp, dff, 0, pf);
-    else k_force_mixed<false, true><<<nbf, BS_FORCE, 0, st>>>(v, t.pair, t.rho, sp, dff, 0, pf);
+    if (t.nt1) k_force_mixed<true, true><<<nbf, t.bs, 0, st>>>(v, t.pair, t.rho, sp, dff, 0, pf);
+    else k_force_mixed<false, true><<<nbf, t.bs, 0, st>>>(v, t.pair, t.rho, sp, dff, 0, pf);
     if (ev) cudaEventRecord(ev[3], st);
     launches += 4;
   } else {
@@ -235,8 +235,8 @@ int launch_forces_mixed(const SysView &v, const ForceTabs &t, DevScalars *sc, fl
       cudaEventRecord(ev[1], st);
       cudaEventRecord(ev[2], st);
     }
-    if (t.nt1) k_force_mixed<true, false><<<nbf, BS_FORCE, 0, st>>>(v, t.pair, t.rho, sp, dff, 0, pf);
-    else k_force_mixed<false, false><<<nbf, BS_FORCE, 0, st>>>(v, t.pair, t.rho, sp, dff, 0, pf);
+    if (t.nt1) k_force_mixed<true, false><<<nbf, t.bs, 0, st>>>(v, t.pair, t.rho, sp, dff, 0, pf);
+    else k_force_mixed<false, false><<<nbf, t.bs, 0, st>>>(v, t.pair, t.rho, sp, dff, 0, pf);
     if (ev) cudaEventRecord(ev[3], st);
     launches += 1;
   }

@@ -157,6 +157,11 @@ struct imdgpu_sys {
   std::vector<int> b0_aoff, b0_number, b0_type;
   std::vector<double> b0_boxes, b0_mass;
   int compact_pct = 50;            // compact when active atoms <= this % of the device batch
+  // block shape of the pair passes; autotuned (imdgpu_autotune) per
+  // (atoms, cells, precision), which tuned_key records
+  int bs_force = BS_FORCE, bs_rho = BS_FORCE;
+  std::vector<long> tuned_key;
+  int autotune_batches = 1;        // imdgpu_batch_begin tunes the batch first
   long batch_nbl0 = 0;
 
   // learned start (learn.cu)
@@ -900,6 +905,8 @@ static ForceTabs ftabs(imdgpu_sys *s) {
   t.nt1 = (s->ntypes == 1);
   t.exact = s->exact;
   t.epot = 1;
+  t.bs = s->bs_force;
+  t.bs_rho = s->bs_rho;
   int same = s->have_tab[0] && s->have_tab[1];
   if (same) {
     const HostTable &a = s->htab[0], &b = s->htab[1];
@@ -1381,6 +1388,53 @@ static int calc_forces_sync(imdgpu_sys *s) {
   }
   rc = forces_async(s);
   if (rc) return rc;
+  return read_back(s);
+}
+
+// Autotuner of the pair passes' block shape: with the current list, each
+// candidate block runs the complete force passes once to warm up and three
+// times under CUDA events; the fastest is kept for this (atoms, cells,
+// precision) until the system changes shape.  The forces are then computed
+// once more with the chosen shape.
+static int autotune_forces(imdgpu_sys *s, int force) {
+  const std::vector<long> key = {(long)s->n, (long)s->nsys, (long)s->precision,
+                                 (long)s->interaction, (long)s->exact};
+  if (!force && key == s->tuned_key) return IMDGPU_OK;
+  int rc = calc_forces_sync(s);  // list and geometry current
+  if (rc) return rc;
+  static const int cand[] = {32, 64, 96, 128};
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  const bool mixed = s->precision == IMDGPU_MIXED;
+  // the density block first (the force block at its default), then the force block
+  for (int which = 0; which < 2; which++) {
+    float best_ms = 1e30f;
+    int best = BS_FORCE;
+    for (int c : cand) {
+      (which == 0 ? s->bs_rho : s->bs_force) = c;
+      const SysView v = view(s);
+      const ForceTabs t = ftabs(s);
+      launch_forces(v, t, s->dsc, mixed, s->st);
+      CK(cudaEventRecord(e0, s->st));
+      for (int r = 0; r < 3; r++) launch_forces(v, t, s->dsc, mixed, s->st);
+      CK(cudaEventRecord(e1, s->st));
+      CK(cudaEventSynchronize(e1));
+      CK(cudaGetLastError());
+      float ms = 0.f;
+      CK(cudaEventElapsedTime(&ms, e0, e1));
+      if (ms < best_ms) {
+        best_ms = ms;
+        best = c;
+      }
+    }
+    (which == 0 ? s->bs_rho : s->bs_force) = best;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  s->tuned_key = key;
+  launch_forces(view(s), ftabs(s), s->dsc, mixed, s->st);
+  CK(cudaGetLastError());
   return read_back(s);
 }
 
@@ -2699,6 +2753,11 @@ int imdgpu_batch_begin(imdgpu_sys *s, double fmax, int maxsteps) {
       if ((rc = rebuild_sync(s))) return rc;
     }
   }
+  if (s->autotune_batches) {
+    // the block shape for this batch, then the evaluation state as begun
+    if ((rc = autotune_forces(s, 0))) return rc;
+    CK(cudaMemset(s->d_sys_short, 0, sizeof(int) * ns));
+  }
   if (!s->brun) s->brun = new BatchRun();
   BatchRun &B = *s->brun;
   if (B.gx) cudaGraphExecDestroy(B.gx);
@@ -2722,6 +2781,35 @@ int imdgpu_batch_begin(imdgpu_sys *s, double fmax, int maxsteps) {
   long nbl = 0;
   CK(cudaMemcpy(&nbl, s->dnbl, sizeof(long), cudaMemcpyDeviceToHost));
   s->batch_nbl0 = nbl;
+  return IMDGPU_OK;
+}
+
+// block shapes of the pair passes picked by timing (see autotune_forces)
+int imdgpu_autotune(imdgpu_sys *s, int *block_density, int *block_force) {
+  if (!s) return fail(IMDGPU_ERR_ARG, "null system");
+  int rc = batch_full(s);
+  if (rc) return rc;
+  if ((rc = autotune_forces(s, 1))) return rc;
+  if (block_density) *block_density = s->bs_rho;
+  if (block_force) *block_force = s->bs_force;
+  return IMDGPU_OK;
+}
+
+int imdgpu_set_blocks(imdgpu_sys *s, int block_density, int block_force) {
+  if (!s) return fail(IMDGPU_ERR_ARG, "null system");
+  for (int b : {block_density, block_force})
+    if (b < 32 || b > BS_FORCE_MAX || b % 32)
+      return fail(IMDGPU_ERR_ARG, "blocks must be multiples of 32 in [32, 128]");
+  s->bs_rho = block_density;
+  s->bs_force = block_force;
+  s->tuned_key = {(long)s->n, (long)s->nsys, (long)s->precision, (long)s->interaction,
+                  (long)s->exact};
+  return IMDGPU_OK;
+}
+
+int imdgpu_batch_set_autotune(imdgpu_sys *s, int on) {
+  if (!s) return fail(IMDGPU_ERR_ARG, "null system");
+  s->autotune_batches = on ? 1 : 0;
   return IMDGPU_OK;
 }
 

@@ -232,6 +232,18 @@ int imdgpu_batch_ml_start(imdgpu_sys *sys, int *used, double *e_start, double *e
 int imdgpu_get_pairs(imdgpu_sys *sys, long cap, int *ni, int *nj, int *shift,
                      double *r2, long *count);
 
+/* Autotuner (no counterpart in IMD): the density pass, then the force
+ * pass, run with blocks of 32, 64, 96 and 128 threads on the current list,
+ * timed with CUDA events; the fastest of each is kept for this system until
+ * its size, precision or number of cells changes.  The chosen blocks go to
+ * *block_density and *block_force (either may be NULL).
+ * imdgpu_batch_begin tunes every new batch shape first unless
+ * imdgpu_batch_set_autotune(sys, 0); imdgpu_set_blocks fixes them by hand
+ * (multiples of 32, at most 128). */
+int imdgpu_autotune(imdgpu_sys *sys, int *block_density, int *block_force);
+int imdgpu_set_blocks(imdgpu_sys *sys, int block_density, int block_force);
+int imdgpu_batch_set_autotune(imdgpu_sys *sys, int on);
+
 /* Timing of the dominant kernels of the last nve_run (device ms, CUDA
  * events on the system's stream). */
 typedef struct {

@@ -110,3 +110,31 @@ def test_compaction_keeps_every_cell_result():
     b1.ml_set_weights(np.zeros(learned.NPARAM, np.float32))
     used, e0, e1 = b1.ml_start()
     assert np.allclose(e0, r1["epot"], rtol=1e-11, atol=0)
+
+
+def test_autotune_keeps_results():
+    """The autotuner picks one of its block shapes; forces and energies with
+    the tuned shape equal those of the default shape (only the order of the
+    block sums changes), and a hand-set shape is kept."""
+    from imd_gb300 import api
+    from conftest import golden
+    g = golden("cu_pert")
+    out = {}
+    for mode in ("default", "tuned", "32"):
+        s = api.GpuSystem(1, api.EAM2, api.FP64)
+        s.read_tables(tables("cu"))
+        s.set_box(g["box"], (1, 1, 1), 0.4)
+        s.set_atoms(g["number"], g["type"], g["mass"], g["x"])
+        if mode == "tuned":
+            bd, bf = s.autotune()
+            assert bd in (32, 64, 96, 128) and bf in (32, 64, 96, 128)
+        elif mode == "32":
+            s.set_blocks(32, 64)
+        s.calc_forces(0)
+        out[mode] = (s.get_atoms()["f"], s.scalars().tot_pot_energy)
+        s.close()
+    f0, e0 = out["default"]
+    for mode in ("tuned", "32"):
+        f, e = out[mode]
+        assert np.abs(f - f0).max() <= 1e-12 * np.abs(f0).max()
+        assert abs(e - e0) <= 1e-13 * abs(e0)
