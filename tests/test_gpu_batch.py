@@ -138,3 +138,44 @@ def test_autotune_keeps_results():
         f, e = out[mode]
         assert np.abs(f - f0).max() <= 1e-12 * np.abs(f0).max()
         assert abs(e - e0) <= 1e-13 * abs(e0)
+
+
+def _overlap_cell():
+    """A noisy 4x4x4 Cu cell with one atom pushed to 0.9 A from a neighbour,
+    inside the tables' first point (1.5 A), where the tables clamp."""
+    from imd_gb300 import workloads as wl
+    x, box = wl.fcc(4, 4, 4, 3.615)
+    x = x + 0.02 * np.random.default_rng(1).standard_normal(x.shape)
+    d = x[1] - x[0]
+    x[0] = x[1] - 0.9 * d / np.linalg.norm(d)
+    n = len(x)
+    return wl.System(box, x, np.zeros((n, 3)), np.zeros(n, np.int32), np.full(n, wl.CU.mass),
+                     np.arange(n, dtype=np.int32))
+
+
+def test_short_distance_cell_stops_others_relax():
+    """IMD's CG cannot leave a pair inside the tables' first point (the
+    oracle restatement stays at the same max force, energy creeping up, for
+    as long as it runs); the batch stops that cell with status 4 after five
+    such line searches and relaxes the other cell normally."""
+    import ctypes as C
+    import oracle
+    from imd_gb300 import api
+    from imd_gb300 import workloads as wl
+    from oracle import OracleSystem
+    bad = _overlap_cell()
+    good = wl.defect_cell(np.random.default_rng(14), nmin=300, nmax=600, nlim=(3, 6))
+    b = api.GpuBatch(1, api.EAM2)
+    b.read_tables(tables("cu"))
+    b.set_cells([bad, good])
+    b.relax(1e-4, maxsteps=300)
+    r = b.results()
+    assert r["status"][0] == 4 and r["steps"][0] <= 8, r
+    assert r["status"][1] == 0 and r["fmax"][1] <= 1e-4, r
+    o = OracleSystem(bad.box, bad.x, bad.types, bad.mass, bad.number, 1, tables("cu"), True, 0.4)
+    L = oracle.lib()
+    L.orc_reset_cg(C.byref(o.s))
+    f0 = L.orc_max_atom_force(C.byref(o.s))
+    for k in range(1, 11):
+        L.orc_cg_step(C.byref(o.s), k)
+    assert L.orc_max_atom_force(C.byref(o.s)) > 10.0 and f0 > 10.0
