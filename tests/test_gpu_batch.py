@@ -165,10 +165,10 @@ def test_short_distance_cell_stops_others_relax():
     from oracle import OracleSystem
     bad = _overlap_cell()
     good = wl.defect_cell(np.random.default_rng(14), nmin=300, nmax=600, nlim=(3, 6))
-    b = api.GpuBatch(1, api.EAM2)
+    b = api.GpuBatch(1, api.EAM2, api.FP64, api.SPLINE)
     b.read_tables(tables("cu"))
     b.set_cells([bad, good])
-    b.relax(1e-4, maxsteps=300)
+    b.relax(1e-4, maxsteps=2000)
     r = b.results()
     assert r["status"][0] == 4 and r["steps"][0] <= 8, r
     assert r["status"][1] == 0 and r["fmax"][1] <= 1e-4, r
