@@ -193,37 +193,49 @@ def run_reference(args, rank, world):
     print(json.dumps(line))
 
 
-def run_batch(args, tabs):
+def run_batch(args, tabs, rank=0, world=1, dist=None):
     """Defect CG relaxations/s, plain and from the learned start: the held-out
     cells of the learned-start workload (seed 6), each relaxed by IMD's CG
     to max |F| <= 1e-4 eV/A in one batch; the learned start uses the weights
-    trained by imd_gb300/train_start.py (imd_gb300/data/start_mlp.npz)."""
-    from imd_gb300 import learned
+    trained by imd_gb300/train_start.py (imd_gb300/data/start_mlp.npz).
+    With N ranks the cells are sharded by atom count (no exchange while they
+    relax); the time is the slowest rank's and rank 0 reports."""
+    from imd_gb300 import learned, shard
     from imd_gb300 import workloads as wl
     cells = wl.defect_batch(args.batch_cells, seed=6)
     natoms = np.array([c.n for c in cells])
+    mine = shard.shard_cells(natoms, world)[rank]
     wpath = os.path.join(ROOT, "imd_gb300", "data", "start_mlp.npz")
     w = np.load(wpath)["w"]
     out = {"workload": "%d Sutton-Chen Cu defect cells, %d atoms (%d-%d), 1-4 vacancies or "
                        "<100> dumbbells, +-2%% strain, 0.05 A noise, seed 6; IMD CG to max |F| "
                        "<= 1e-4 eV/A, FP64, spline tables" % (len(cells), natoms.sum(),
                                                               natoms.min(), natoms.max()),
-           "unit": "relaxations/s"}
+           "unit": "relaxations/s", "sharding": "%d ranks, cells split by atom count" % world}
+    res = {}
     for name, weights in (("plain", None), ("learned", w)):
-        r = learned.relax(tabs, cells, weights=weights)
-        out[name] = {"value": r.relaxations_per_s, "seconds": r.seconds,
-                     "converged": int((r.status == 0).sum()),
-                     "converged_per_s": float((r.status == 0).sum() / r.seconds),
-                     "force_calls_per_relaxation": float(r.nfc.mean()),
-                     "rounds": r.rounds, "status_counts": np.bincount(r.status, minlength=5).tolist()}
-        if weights is not None:
-            out[name]["start_used"] = int(r.used.sum())
-        out[name + "_epot"] = r.epot
-        out[name + "_status"] = r.status
-    both = (out["plain_status"] == 0) & (out["learned_status"] == 0)
-    de = np.abs(out["learned_epot"] - out["plain_epot"])[both] / natoms[both]
-    for k in ("plain_epot", "learned_epot", "plain_status", "learned_status"):
-        del out[k]
+        if dist:
+            dist.barrier()
+        r = learned.relax(tabs, [cells[i] for i in mine], weights=weights)
+        sec = shard.max_over_ranks(r.seconds, dist)
+        g = shard.gather_cell_results({"epot": r.epot, "status": r.status, "nfc": r.nfc},
+                                      mine, len(cells), dist)
+        res[name] = (sec, g, r)
+    if rank != 0:
+        return None
+    for name in ("plain", "learned"):
+        sec, g, r = res[name]
+        out[name] = {"value": len(cells) / sec, "seconds": sec,
+                     "converged": int((g["status"] == 0).sum()),
+                     "converged_per_s": float((g["status"] == 0).sum() / sec),
+                     "force_calls_per_relaxation": float(g["nfc"].mean()),
+                     "rounds_rank0": r.rounds,
+                     "status_counts": np.bincount(g["status"], minlength=5).tolist()}
+        if name == "learned":
+            out[name]["start_used_rank0"] = int(r.used.sum())
+    gp, gl = res["plain"][1], res["learned"][1]
+    both = (gp["status"] == 0) & (gl["status"] == 0)
+    de = np.abs(gl["epot"] - gp["epot"])[both] / natoms[both]
     out["speedup_learned_vs_plain"] = out["learned"]["value"] / out["plain"]["value"]
     out["final_energy_diff_ev_per_atom"] = {"max": float(de.max()), "median": float(np.median(de)),
                                             "within_1e-6": int((de <= 1e-6).sum()),
@@ -405,8 +417,10 @@ def run_ours(args, rank, world, local):
                          "graph_replay_wall": m["graph_rate"],
                          "energy_drift_per_atom": float((m["etot"][-1] - m["etot"][0]) / n),
                          "vs_fp64": prec}
-    if not args.no_batch and rank == 0:
-        line["batched_cg"] = run_batch(args, tabs)
+    if not args.no_batch:
+        bc = run_batch(args, tabs, rank, world, dist)
+        if rank == 0:
+            line["batched_cg"] = bc
     if rank == 0 and not args.no_cpu:
         try:
             rate, _ = cpu_sample(tabs, args.cpu_steps, 1)
