@@ -451,6 +451,9 @@ int orc_init(orc_sys_t *s, int n) {
   s->ex = NULL;
   s->etype = s->esrc = s->eowner = NULL;
   s->eshift = s->ef = s->eepot = s->erho = s->edf = NULL;
+  s->do_stress = 0;
+  s->estress = NULL;
+  s->stress = (double *)calloc(6 * (size_t)n, sizeof(double));
   s->tb = NULL;
   s->nb_cap = s->nb_len = 0;
   s->have_valid_nbl = 0;
@@ -469,6 +472,8 @@ int orc_init(orc_sys_t *s, int n) {
 }
 
 void orc_free(orc_sys_t *s) {
+  free(s->estress); free(s->stress);
+  s->estress = s->stress = NULL;
   free(s->number); free(s->type); free(s->mass); free(s->x); free(s->p);
   free(s->f); free(s->epot); free(s->eam_rho); free(s->eam_df);
   free(s->nbl_pos); free(s->old_x); free(s->cg_g); free(s->cg_h);
@@ -583,6 +588,7 @@ static void ensure_ext(orc_sys_t *s, int need) {
   s->eepot = (double *)realloc(s->eepot, sizeof(double) * cap);
   s->erho = (double *)realloc(s->erho, sizeof(double) * cap);
   s->edf = (double *)realloc(s->edf, sizeof(double) * cap);
+  s->estress = (double *)realloc(s->estress, sizeof(double) * 6 * cap);
   s->next_cap = cap;
 }
 
@@ -738,6 +744,21 @@ static void refresh_ghosts(orc_sys_t *s) {
   }
 }
 
+/* STRESS_TENS for one pair (src/imd_forces_nbl.c:558-580, :1284-1303):
+ * with the force halved "to avoid double counting", -d_a f_b goes to both
+ * atoms; components xx yy zz yz zx xy. */
+static void stress_pair(double *pp, double *sj, double dx, double dy, double dz, double fx,
+                        double fy, double fz) {
+  fx *= 0.5;
+  fy *= 0.5;
+  fz *= 0.5;
+  const double v[6] = {dx * fx, dy * fy, dz * fz, dy * fz, dz * fx, dx * fy};
+  for (int c = 0; c < 6; c++) {
+    pp[c] -= v[c];
+    sj[c] -= v[c];
+  }
+}
+
 /* calc_forces (src/imd_forces_nbl.c:281-1999), PAIR + EAM2 */
 int orc_calc_forces(orc_sys_t *s) {
   int n = s->n, nt = s->ntypes, inc = nt * nt;
@@ -753,12 +774,16 @@ int orc_calc_forces(orc_sys_t *s) {
     s->eepot[g] = 0.0;
     s->erho[g] = 0.0;
   }
+  const int st = s->do_stress;  /* do_press_calc */
+  if (st)
+    for (long g = 0; g < 6L * s->next; g++) s->estress[g] = 0.0;
   const double *ex = s->ex;
   /* loop 1: pair + host electron density (:423-981) */
   for (int nn = 0; nn < n; nn++) {
     int i = s->order[nn];
     double d1x = ex[3 * i], d1y = ex[3 * i + 1], d1z = ex[3 * i + 2];
     double ffx = 0, ffy = 0, ffz = 0, ee = 0, eam_r = 0;
+    double pp[6] = {0, 0, 0, 0, 0, 0};
     int it = s->etype[i];
     for (int m = s->tl[nn]; m < s->tl[nn + 1]; m++) {
       int j = s->tb[m];
@@ -781,6 +806,7 @@ int orc_calc_forces(orc_sys_t *s) {
         ee += pot;
         s->eepot[j] += pot;
         s->virial -= r2 * grad;
+        if (st) stress_pair(pp, s->estress + 6 * j, dx, dy, dz, fx, fy, fz);
       }
       if (eam) {
         double rho_h = 0.0;
@@ -803,6 +829,8 @@ int orc_calc_forces(orc_sys_t *s) {
     s->ef[3 * i + 2] += ffz;
     s->eepot[i] += ee;
     if (eam) s->erho[i] += eam_r;
+    if (st)
+      for (int c = 0; c < 6; c++) s->estress[6 * i + c] += pp[c];
   }
   if (eam) {
     /* send_forces(add_rho) (:1076): fold ghosts into sources, reverse order */
@@ -824,6 +852,7 @@ int orc_calc_forces(orc_sys_t *s) {
       int i = s->order[nn];
       double d1x = ex[3 * i], d1y = ex[3 * i + 1], d1z = ex[3 * i + 2];
       double ffx = 0, ffy = 0, ffz = 0;
+      double pp[6] = {0, 0, 0, 0, 0, 0};
       int it = s->etype[i];
       for (int m = s->tl[nn]; m < s->tl[nn + 1]; m++) {
         int j = s->tb[m];
@@ -847,11 +876,14 @@ int orc_calc_forces(orc_sys_t *s) {
           ffy += fy;
           ffz += fz;
           s->virial -= dx * fx + dy * fy + dz * fz;
+          if (st) stress_pair(pp, s->estress + 6 * j, dx, dy, dz, fx, fy, fz);
         }
       }
       s->ef[3 * i] += ffx;
       s->ef[3 * i + 1] += ffy;
       s->ef[3 * i + 2] += ffz;
+      if (st)
+        for (int c = 0; c < 6; c++) s->estress[6 * i + c] += pp[c];
     }
   }
   /* send_forces(add_forces) (:1997) */
@@ -861,6 +893,16 @@ int orc_calc_forces(orc_sys_t *s) {
     s->ef[3 * src + 1] += s->ef[3 * g + 1];
     s->ef[3 * src + 2] += s->ef[3 * g + 2];
     s->eepot[src] += s->eepot[g];
+    if (st)
+      for (int c = 0; c < 6; c++) s->estress[6 * src + c] += s->estress[6 * g + c];
+  }
+  if (st) {
+    /* PRESSTENS of the real atoms; calc_tot_presstens in cell order */
+    for (int c = 0; c < 6; c++) s->tot_stress[c] = 0.0;
+    for (int i = 0; i < n; i++)
+      for (int c = 0; c < 6; c++) s->stress[6 * i + c] = s->estress[6 * i + c];
+    for (int nn = 0; nn < n; nn++)
+      for (int c = 0; c < 6; c++) s->tot_stress[c] += s->stress[6 * s->order[nn] + c];
   }
   for (int i = 0; i < n; i++) {
     s->f[3 * i] = s->ef[3 * i];

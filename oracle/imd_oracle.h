@@ -128,6 +128,12 @@ typedef struct {
   double *old_x, *cg_g, *cg_h;
   double cg_gamma, cg_poteng, old_cg_poteng, old_alphamin;
   long   nactive;
+
+  /* ---- STRESS_TENS (src/imd_forces_nbl.c:548-581, :1275-1318) ---- */
+  int     do_stress;          /* do_press_calc for the next calc_forces */
+  double *estress;            /* 6*next: PRESSTENS xx yy zz yz zx xy */
+  double *stress;             /* 6n, after the ghost fold */
+  double  tot_stress[6];      /* calc_tot_presstens (src/imd_main_3d.c:2069) */
 } orc_sys_t;
 
 /* set defaults; allocate per-atom arrays for n atoms */

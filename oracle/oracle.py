@@ -56,7 +56,9 @@ class Sys(C.Structure):
         ("tot_kin_energy", C.c_double), ("fnorm", C.c_double), ("f_max2", C.c_double),
         ("old_x", _dp), ("cg_g", _dp), ("cg_h", _dp), ("cg_gamma", C.c_double),
         ("cg_poteng", C.c_double), ("old_cg_poteng", C.c_double),
-        ("old_alphamin", C.c_double), ("nactive", C.c_long)]
+        ("old_alphamin", C.c_double), ("nactive", C.c_long),
+        ("do_stress", C.c_int), ("estress", _dp), ("stress", _dp),
+        ("tot_stress", C.c_double * 6)]
 
 
 _lib = None
@@ -207,6 +209,20 @@ class OracleSystem:
     @property
     def df(self):
         return self._arr("eam_df", (self.n,))
+
+    @property
+    def stress(self):
+        """Per-atom PRESSTENS (n, 6: xx yy zz yz zx xy) of the last calc_forces
+        with do_stress set."""
+        return self._arr("stress", (self.n, 6))
+
+    @property
+    def tot_stress(self):
+        return np.array(self.s.tot_stress[:])
+
+    def set_stress(self, on: bool = True) -> None:
+        """do_press_calc: the next calc_forces also accumulates PRESSTENS."""
+        self.s.do_stress = 1 if on else 0
 
     @property
     def epot_total(self):

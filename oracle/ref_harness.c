@@ -93,6 +93,30 @@ static void dump_pairs(const char *fname) {
   fclose(out);
 }
 
+#ifdef STRESS_TENS
+/* per-atom PRESSTENS (xx yy zz yz zx xy) and calc_tot_presstens */
+static void dump_stress(const char *pre) {
+  char fname[600];
+  int k, i;
+  sprintf(fname, "%s.stress", pre);
+  FILE *out = fopen(fname, "w");
+  for (k = 0; k < NCELLS; k++) {
+    cell *p = CELLPTR(k);
+    for (i = 0; i < p->n; i++)
+      fprintf(out, "%ld %.17e %.17e %.17e %.17e %.17e %.17e\n", (long)NUMMER(p, i),
+              PRESSTENS(p, i, xx), PRESSTENS(p, i, yy), PRESSTENS(p, i, zz),
+              PRESSTENS(p, i, yz), PRESSTENS(p, i, zx), PRESSTENS(p, i, xy));
+  }
+  fclose(out);
+  calc_tot_presstens();
+  sprintf(fname, "%s.totstress", pre);
+  out = fopen(fname, "w");
+  fprintf(out, "%.17e %.17e %.17e %.17e %.17e %.17e\n", tot_presstens.xx, tot_presstens.yy,
+          tot_presstens.zz, tot_presstens.yz, tot_presstens.zx, tot_presstens.xy);
+  fclose(out);
+}
+#endif
+
 static double max_atom_force(void) {
   int k, i;
   double m = 0.0;
@@ -130,7 +154,13 @@ int main(int argc, char **argv) {
   dump_state(fname);
 
   if (0 == strcmp(mode, "forces")) {
+#ifdef STRESS_TENS
+    do_press_calc = 1;  /* main_loop sets it on output steps (src/imd_main_3d.c:184) */
+#endif
     calc_forces(0);
+#ifdef STRESS_TENS
+    dump_stress(pre);
+#endif
     sprintf(fname, "%s.forces", pre);
     dump_state(fname);
     sprintf(fname, "%s.pairs", pre);

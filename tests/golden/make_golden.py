@@ -21,6 +21,11 @@ Fixtures (all sorted by atom number):
               table interpolation (targets with `spline`, `4point`)
   defect_cg_spline  a defect cell of the batched-relaxation generator
               (1005 atoms), CG to max |F| <= 1e-4 eV/A with spline tables
+  cu_pert_stress, alloy_pert_stress, lj_pert_stress   the perturbed Cu,
+              Cu/Ni and LJ cases run by the `stress` build (STRESS_TENS):
+              per-atom PRESSTENS and calc_tot_presstens
+
+`python tests/golden/make_golden.py stress` writes the stress fixtures only.
 """
 from __future__ import annotations
 
@@ -257,5 +262,63 @@ def main() -> None:
                                                     "cg_epot", "cg_nfc")})
 
 
+def load_stress(pre: str):
+    a = np.loadtxt(pre + ".stress", ndmin=2)
+    a = a[np.argsort(a[:, 0], kind="stable")]
+    return a[:, 1:7], np.loadtxt(pre + ".totstress")
+
+
+def stress_cases() -> None:
+    """The STRESS_TENS fixtures, on the same inputs as cu_pert, alloy_pert and
+    lj_pert (same generators and seeds)."""
+    subprocess.run(["make", "-s", "-C", ORACLE, "ref"], check=True)
+    tmp = tempfile.mkdtemp(prefix="imdgold_stress")
+    cu = tuple(os.path.join(HERE, "cu" + e) for e in (".pt", ".rho", ".emb"))
+    alloy = tuple(os.path.join(HERE, "cuni" + e) for e in (".pt", ".rho", ".emb"))
+    lj2 = os.path.join(HERE, "lj.pt")
+    cases = []
+    cus = wl.eam_fcc_system(8)
+    cfg = os.path.join(tmp, "cu_pert.cfg")
+    perturbed_config(cus, 0.1, 12, cfg)
+    cases.append(("cu_pert_stress", "nve_nbl_eam_stress", cfg,
+                  dict(core_potential_file=cu[0], **{"atomic_e-density_file": cu[1]},
+                       embedding_energy_file=cu[2], ntypes=1, masses=63.546,
+                       timestep=0.0982266, nbl_margin=0.4, seed=2)))
+    als = wl.eam_fcc_system(6, a0=3.57, species=(wl.CU, wl.NI), type_seed=3)
+    cfg = os.path.join(tmp, "alloy.cfg")
+    perturbed_config(als, 0.08, 13, cfg)
+    cases.append(("alloy_pert_stress", "nve_nbl_eam_stress", cfg,
+                  dict(core_potential_file=alloy[0], **{"atomic_e-density_file": alloy[1]},
+                       embedding_energy_file=alloy[2], ntypes=2, masses=[63.546, 58.69],
+                       timestep=0.0982266, nbl_margin=0.4, seed=2)))
+    lj = wl.lj_fcc_system(10)
+    cfg = os.path.join(tmp, "lj_pert.cfg")
+    perturbed_config(lj, 0.05, 11, cfg)
+    cases.append(("lj_pert_stress", "nve_nbl_stress", cfg,
+                  dict(potfile=lj2, ntypes=1, masses=1.0, timestep=0.005, nbl_margin=0.3,
+                       seed=1)))
+    for name, variant, cfg, kw in cases:
+        p = os.path.join(tmp, name + ".param")
+        tok = dict(coordname=cfg, outfiles=os.path.join(tmp, "o"), ensemble="nve",
+                   pbc_dirs=[1, 1, 1], maxsteps=0, starttemp=0.0, eng_int=0,
+                   checkpt_int=100000000, box_from_header=1)
+        tok.update(kw)
+        wl.write_param(p, **tok)
+        pre = os.path.join(tmp, name)
+        run(variant, p, "forces", pre)
+        st = load_state(pre + ".forces")
+        box, gdim, cellsz = load_box(pre + ".box")
+        tot = np.loadtxt(pre + ".totals")
+        stress, tot_stress = load_stress(pre)
+        d = dict(box=box, gdim=gdim, cellsz=cellsz, epot_total=tot[0], virial=tot[1],
+                 stress=stress, tot_stress=tot_stress, **st)
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **d)
+        print(name, "atoms", len(st["x"]), "tot_stress", tot_stress)
+
+
 if __name__ == "__main__":
-    main()
+    if len(sys.argv) > 1 and sys.argv[1] == "stress":
+        stress_cases()
+    else:
+        main()
+        stress_cases()

@@ -124,3 +124,26 @@ def test_table_reader_quirks():
     pot, grad = t2.pair_int2(0, 1, r2)
     assert np.all(np.isfinite(pot)) and np.all(np.isfinite(grad))
     assert abs(pot[-1]) < 1e-12 * abs(pot[0])
+
+
+STRESS = {"cu_pert_stress": ("cu", True, 1, 0.4), "alloy_pert_stress": ("cuni", True, 2, 0.4),
+          "lj_pert_stress": ("lj", False, 1, 0.3)}
+
+
+@pytest.mark.parametrize("name", list(STRESS))
+def test_stress_matches_reference(name):
+    """STRESS_TENS: per-atom PRESSTENS within 1e-11 of the largest component,
+    the total tensor (calc_tot_presstens) within 1e-12 relative; its trace is
+    the virial."""
+    g = golden(name)
+    tab, eam, nt, skin = STRESS[name]
+    s = OracleSystem(g["box"], g["x"], g["type"], g["mass"], g["number"], nt, tables(tab),
+                     eam, skin)
+    s.set_stress(True)
+    s.calc_forces()
+    scale = np.max(np.abs(g["stress"]))
+    assert np.max(np.abs(s.stress - g["stress"])) <= 1e-11 * scale
+    tot = s.tot_stress
+    assert np.all(np.abs(tot - g["tot_stress"]) <= 1e-12 * np.max(np.abs(g["tot_stress"])))
+    assert abs(tot[:3].sum() - g["virial"]) <= 1e-11 * abs(g["virial"])
+    assert rel_rms(s.f, g["f"]) < 1e-11
