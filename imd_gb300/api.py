@@ -106,6 +106,7 @@ def lib() -> C.CDLL:
         L.imdgpu_batch_rebuilds.argtypes = [vp, C.POINTER(C.c_long)]
         L.imdgpu_batch_set_compaction.argtypes = [vp, C.c_int]
         L.imdgpu_autotune.argtypes = [vp, _ip, _ip]
+        L.imdgpu_calc_stress.argtypes = [vp, _dp, _dp]
         L.imdgpu_set_blocks.argtypes = [vp, C.c_int, C.c_int]
         L.imdgpu_batch_set_autotune.argtypes = [vp, C.c_int]
         L.imdgpu_batch_positions.argtypes = [vp, _dp]
@@ -225,6 +226,16 @@ class GpuSystem:
     def calc_forces(self, steps: int = 0) -> int:
         self.last_rc = _check(lib().imdgpu_calc_forces(self.h, steps), "calc_forces")
         return self.last_rc
+
+    def calc_stress(self):
+        """Forces plus IMD's per-atom stress (STRESS_TENS): returns
+        (presstens (n, 6: xx yy zz yz zx xy), total (6,))."""
+        st = np.empty((self.n, 6))
+        tot = np.empty(6)
+        rc = lib().imdgpu_calc_stress(self.h, _p(st), _p(tot))
+        if rc < 0:
+            _check(rc, "calc_stress")
+        return st, tot
 
     def make_nblist(self) -> None:
         _check(lib().imdgpu_make_nblist(self.h), "make_nblist")

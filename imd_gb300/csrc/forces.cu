@@ -8,6 +8,8 @@
 // F(rho) per atom, then a fused pass that adds the pair force (loop 1's
 // PAIR branch) and the EAM force (loop 2) of each pair with one set of
 // atomics.
+#include <algorithm>
+
 #include "kernels.cuh"
 
 namespace imdgpu {
@@ -347,6 +349,119 @@ __global__ void __launch_bounds__(BS_VEC) k_embed_fast(SysView v, DevTable emb, 
     e[0] = pot;
   }
   block_sum_store<1, BS_VEC>(e, partial);
+}
+
+// ---------------------------------------------------------------------------
+// STRESS_TENS (src/imd_forces_nbl.c:558-580, :1284-1318): for every pair the
+// pair + EAM force f = d grad is halved ("avoid double counting of the
+// virial") and -d_a f_b is added to both atoms; components xx yy zz yz zx xy
+// (sym_tensor).  A pass of its own after the force passes (it reads 2F' of
+// every atom), run on the steps that want pressure (IMD's do_press_calc), so
+// the force pass of the other steps stays as it is.  Ghost sums fold into
+// their owners afterwards (send_forces(add_forces), src/imd_comm_force_3d.c:916).
+// ---------------------------------------------------------------------------
+template <bool NT1, bool EAM, bool SAMEGRID, bool CUB>
+__global__ void __launch_bounds__(BS_FORCE_MAX) k_stress_fast(SysView v, DevTable pair,
+                                                          DevTable rho, double *stress) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= v.n || atom_idle(v, i)) return;
+  const double4 pi = v.pos[i];
+  const int it = NT1 ? 0 : (int)pi.w, nt = v.ntypes;
+  const int nn = v.nnb[i];
+  const double dfi = EAM ? v.df[i] : 0.0;
+  double acc[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+  const uint32_t *__restrict__ nb = v.nbr + i;
+  for (int k = 0; k < nn; k++) {
+    const int j = (int)(__ldg(nb + (size_t)k * v.ncap) & NB_MASK);
+    const double4 pj = ldg4(&v.pos[j]);
+    const double dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
+    const double r2 = fma(dx, dx, fma(dy, dy, dz * dz));
+    const int jt = NT1 ? 0 : (int)pj.w;
+    const int col = NT1 ? 0 : it * nt + jt;
+    double ngrad = 0.0;  // minus grad of the pair: the force on j is d * ngrad
+    bool have = false;
+    int kk = 0;
+    double chi = 0.0;
+    if (le_pos(r2, pair.end[col])) {
+      kk = tab_index_fast(pair, col, r2, chi);
+      ngrad = poly_g<CUB>(cgn_load(pair, col, kk), chi);
+      have = true;
+    }
+    if (EAM) {
+      const int col1 = NT1 ? 0 : jt * nt + it, col2 = col;
+      if (lt_pos(r2, rho.end[col1]) || lt_pos(r2, rho.end[col2])) {
+        double chi1 = chi;
+        int k1 = kk;
+        if (!(SAMEGRID && have)) k1 = tab_index_fast(rho, col1, r2, chi1);
+        const double nris = poly_g<CUB>(cgn_load(rho, col1, k1), chi1);
+        const double dfj = __ldg(&v.df[j]);
+        if (NT1 || col1 == col2) {
+          ngrad = fma(nris, dfi + dfj, ngrad);
+        } else {
+          double chi2 = chi;
+          int k2 = kk;
+          if (!(SAMEGRID && have)) k2 = tab_index_fast(rho, col2, r2, chi2);
+          const double nrjs = poly_g<CUB>(cgn_load(rho, col2, k2), chi2);
+          ngrad = fma(dfi, nrjs, fma(dfj, nris, ngrad));
+        }
+        have = true;
+      }
+    }
+    if (have) {
+      // -d_a (f_b / 2) with f = -d * ngrad on i
+      const double h = 0.5 * ngrad;
+      const double hx = dx * h, hy = dy * h, hz = dz * h;
+      const double c[6] = {dx * hx, dy * hy, dz * hz, dy * hz, dz * hx, dx * hy};
+      double *sj = stress + 6 * (size_t)j;
+#pragma unroll
+      for (int q = 0; q < 6; q++) {
+        acc[q] += c[q];
+        atomicAdd(sj + q, c[q]);
+      }
+    }
+  }
+  double *si = stress + 6 * (size_t)i;
+#pragma unroll
+  for (int q = 0; q < 6; q++) atomicAdd(si + q, acc[q]);
+}
+
+__global__ void k_fold_stress(SysView v, double *stress) {
+  const int ng = v.counters[0];
+  for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < ng; g += gridDim.x * blockDim.x) {
+    const double *sg = stress + 6 * (size_t)(v.n + g);
+    double *so = stress + 6 * (size_t)v.gowner[g];
+#pragma unroll
+    for (int q = 0; q < 6; q++)
+      if (sg[q] != 0.0) atomicAdd(so + q, sg[q]);
+  }
+}
+
+template <bool NT1, bool EAM>
+static void launch_stress2(const ForceTabs &t, const SysView &v, double *stress, cudaStream_t st) {
+  const int nb = (v.n + t.bs - 1) / t.bs;
+  const bool cub = (t.pair.mode != TAB_QUADRATIC);
+  if (t.samegrid) {
+    if (cub) k_stress_fast<NT1, EAM, true, true><<<nb, t.bs, 0, st>>>(v, t.pair, t.rho, stress);
+    else k_stress_fast<NT1, EAM, true, false><<<nb, t.bs, 0, st>>>(v, t.pair, t.rho, stress);
+  } else {
+    if (cub) k_stress_fast<NT1, EAM, false, true><<<nb, t.bs, 0, st>>>(v, t.pair, t.rho, stress);
+    else k_stress_fast<NT1, EAM, false, false><<<nb, t.bs, 0, st>>>(v, t.pair, t.rho, stress);
+  }
+}
+
+int launch_stress(const SysView &v, const ForceTabs &t, double *stress, cudaStream_t st) {
+  const size_t ext = (size_t)v.ncap + v.gcap;
+  cudaMemsetAsync(stress, 0, 6 * ext * sizeof(double), st);
+  if (t.eam) {
+    if (t.nt1) launch_stress2<true, true>(t, v, stress, st);
+    else launch_stress2<false, true>(t, v, stress, st);
+  } else {
+    if (t.nt1) launch_stress2<true, false>(t, v, stress, st);
+    else launch_stress2<false, false>(t, v, stress, st);
+  }
+  const int gblocks = std::max(1, (int)((v.gcap + BS_VEC - 1) / BS_VEC));
+  k_fold_stress<<<gblocks, BS_VEC, 0, st>>>(v, stress);
+  return 2;
 }
 
 template <bool NT1, bool EAM, bool EPOT>

@@ -65,6 +65,10 @@ constexpr int BS_VEC = 256;
 int launch_forces(const SysView &v, const ForceTabs &t, DevScalars *sc, int mixed,
                   cudaStream_t st, cudaEvent_t *ev = nullptr);
 
+// forces.cu: STRESS_TENS per-atom stress (6 per ext atom, xx yy zz yz zx xy)
+// of the current list, after launch_forces; ghosts folded into owners
+int launch_stress(const SysView &v, const ForceTabs &t, double *stress, cudaStream_t st);
+
 // forces.cu: refresh ghost positions (send_cells(copy_cell))
 void k_ghost_pos_launch(const SysView &v, int blocks, cudaStream_t st);
 // mixed.cu: the FP32-force path over the full list

@@ -180,6 +180,10 @@ struct imdgpu_sys {
   int *ml_sel = nullptr;           // per cell: 1 = the prediction is kept
   int ml_save_cap = 0, ml_cell_cap = 0;
 
+  // STRESS_TENS: per ext atom xx yy zz yz zx xy
+  double *d_stress = nullptr;
+  size_t stress_cap = 0;
+
   // CUDA graph of one full chunk of NVE steps, re-captured when buffers move
   cudaGraphExec_t gexec = nullptr;
   std::vector<uintptr_t> gkey;
@@ -786,6 +790,15 @@ __global__ void k_put_state(SysView v, const int *slot_of, const double *x, cons
     b.z = p[3 * o + 2];
     v.mom[s] = b;
   }
+}
+
+// per-atom stress to the caller's order (6 per atom)
+__global__ void k_gather_stress(SysView v, const double *stress, double *out) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= v.n) return;
+  const int o = v.orig[s];
+#pragma unroll
+  for (int q = 0; q < 6; q++) out[6 * (size_t)o + q] = stress[6 * (size_t)s + q];
 }
 
 // batch repacking: slot order -> caller order and back
@@ -1514,6 +1527,7 @@ int imdgpu_destroy(imdgpu_sys *s) {
   dfree(s->ml_pairs); dfree(s->ml_np); dfree(s->ml_dx); dfree(s->ml_target); dfree(s->ml_dldx);
   dfree(s->ml_loss);
   dfree(s->ml_save); dfree(s->ml_ecell); dfree(s->ml_sel);
+  dfree(s->d_stress);
   dfree(s->d_sys_short);
   dfree(s->d_atom_sys); dfree(s->d_aoff); dfree(s->d_sgdim); dfree(s->d_scdim); dfree(s->d_scoff);
   dfree(s->d_sys_done); dfree(s->d_ndone); dfree(s->d_sbox); dfree(s->d_stbox); dfree(s->d_cs);
@@ -1879,6 +1893,38 @@ int imdgpu_calc_forces(imdgpu_sys *s, int steps) {
   if (rc) return rc;
   rc = calc_forces_sync(s);
   if (rc) return rc;
+  return (s->status_host & ST_SHORT) ? IMDGPU_WARN_SHORT : IMDGPU_OK;
+}
+
+// STRESS_TENS with do_press_calc set: calc_forces, then every atom's
+// PRESSTENS (src/imd_forces_nbl.c:558-580, :1284-1318, folded like the
+// forces) and their sum, calc_tot_presstens (src/imd_main_3d.c:2069)
+int imdgpu_calc_stress(imdgpu_sys *s, double *presstens, double *tot) {
+  if (!s) return fail(IMDGPU_ERR_ARG, "null system");
+  if (s->precision != IMDGPU_FP64) return fail(IMDGPU_ERR_STATE, "stress: FP64 precision only");
+  int rc = batch_full(s);
+  if (rc) return rc;
+  if ((rc = calc_forces_sync(s))) return rc;
+  const size_t ext = (size_t)s->ncap + s->gcap;
+  if (s->stress_cap < ext) {
+    dfree(s->d_stress);
+    CK(dalloc(&s->d_stress, 6 * ext));
+    s->stress_cap = ext;
+  }
+  const SysView v = view(s);
+  launch_stress(v, ftabs(s), s->d_stress, s->st);
+  const int n = s->n;
+  k_gather_stress<<<nblk(n, 256), 256, 0, s->st>>>(v, s->d_stress, s->d_out);
+  CK(cudaGetLastError());
+  std::vector<double> h(6 * (size_t)n);
+  CK(cudaMemcpyAsync(h.data(), s->d_out, sizeof(double) * 6 * n, cudaMemcpyDeviceToHost, s->st));
+  CK(cudaStreamSynchronize(s->st));
+  if (presstens) memcpy(presstens, h.data(), sizeof(double) * 6 * n);
+  if (tot) {
+    for (int q = 0; q < 6; q++) tot[q] = 0.0;
+    for (int i = 0; i < n; i++)
+      for (int q = 0; q < 6; q++) tot[q] += h[6 * (size_t)i + q];
+  }
   return (s->status_host & ST_SHORT) ? IMDGPU_WARN_SHORT : IMDGPU_OK;
 }
 

@@ -128,6 +128,14 @@ int imdgpu_get_scalars(imdgpu_sys *sys, imdgpu_scalars *out);
 /* calc_forces (src/imd_forces_nbl.c:281-1999): fix_cells + make_nblist when
  * the list is invalid, then pair / EAM2 forces, energies and virial. */
 int imdgpu_calc_forces(imdgpu_sys *sys, int steps);
+/* calc_forces of a step with do_press_calc set, in the `stress` build
+ * (STRESS_TENS, src/Makefile:1587-1588): forces as imdgpu_calc_forces, and
+ * every atom's PRESSTENS (src/imd_forces_nbl.c:558-580, :1284-1318; ghost
+ * parts folded into their owners as src/imd_comm_force_3d.c:916) into
+ * presstens (6 per atom, caller order: xx yy zz yz zx xy; may be NULL), and
+ * their sum, calc_tot_presstens (src/imd_main_3d.c:2069), into tot (6, may
+ * be NULL).  FP64 precision only. */
+int imdgpu_calc_stress(imdgpu_sys *sys, double *presstens, double *tot);
 /* make_nblist (src/imd_forces_nbl.c:136-273): wrap, bin and rebuild now */
 int imdgpu_make_nblist(imdgpu_sys *sys);
 /* check_nblist (src/imd_forces_nbl.c:2007-2037) */

@@ -310,3 +310,22 @@ def test_spline_cg_relaxation_matches_reference():
     e = s.scalars().tot_pot_energy
     assert abs(e - float(g["cg_epot"])) / len(g["x"]) <= 1e-6
     assert 0.5 * int(g["cg_steps"]) <= steps <= 2 * int(g["cg_steps"]) + 3
+
+
+STRESS = {"cu_pert_stress": ("cu", True, 1, 0.4), "alloy_pert_stress": ("cuni", True, 2, 0.4),
+          "lj_pert_stress": ("lj", False, 1, 0.3)}
+
+
+@pytest.mark.parametrize("name", list(STRESS))
+def test_stress_matches_reference(name):
+    """STRESS_TENS on the device against the reference's `stress` build:
+    per-atom PRESSTENS within 1e-11 of the largest component, the total
+    tensor within 1e-12 relative, forces unchanged."""
+    g = golden(name)
+    tab, eam, nt, skin = STRESS[name]
+    s = gpu_system(g, tab, eam, nt, skin)
+    st, tot = s.calc_stress()
+    scale = np.max(np.abs(g["stress"]))
+    assert np.max(np.abs(st - g["stress"])) <= 1e-11 * scale
+    assert np.all(np.abs(tot - g["tot_stress"]) <= 1e-12 * np.max(np.abs(g["tot_stress"])))
+    assert rel_rms(s.get_atoms()["f"], g["f"]) < 1e-11
