@@ -952,6 +952,75 @@ void orc_move_atoms_nve(orc_sys_t *s) {
   s->f_max2 = fmax2;
 }
 
+/* move_atoms_nvt (src/imd_integrate.c:891-1150), Nose-Hoover thermostat */
+void orc_move_atoms_nvt(orc_sys_t *s) {
+  double e1 = 0.0, e2 = 0.0, fnorm = 0.0, fmax2 = 0.0;
+  double dt = s->timestep;
+  double reibung = 1.0 - s->eta * dt / 2.0;
+  double eins_d_reib = 1.0 / (1.0 + s->eta * dt / 2.0);
+  for (int nn = 0; nn < s->n; nn++) {
+    int i = s->order[nn];
+    double *p = s->p + 3 * i, *f = s->f + 3 * i, *x = s->x + 3 * i;
+    double m = s->mass[i];
+    e1 += (p[0] * p[0] + p[1] * p[1] + p[2] * p[2]) / m;
+    int t = s->type[i];
+    f[0] *= restr(s, t, 0);
+    f[1] *= restr(s, t, 1);
+    f[2] *= restr(s, t, 2);
+    fnorm += f[0] * f[0] + f[1] * f[1] + f[2] * f[2];
+    fmax2 = OMAX(SQR(f[0]), fmax2);
+    fmax2 = OMAX(SQR(f[1]), fmax2);
+    fmax2 = OMAX(SQR(f[2]), fmax2);
+    for (int a = 0; a < 3; a++) p[a] = (p[a] * reibung + dt * f[a]) * eins_d_reib * restr(s, t, a);
+    e2 += (p[0] * p[0] + p[1] * p[1] + p[2] * p[2]) / m;
+    double tmp = dt / m;
+    x[0] += tmp * p[0];
+    x[1] += tmp * p[1];
+    x[2] += tmp * p[2];
+  }
+  s->tot_kin_energy = (e1 + e2) / 4.0;
+  s->fnorm = fnorm;
+  s->f_max2 = fmax2;
+  double ttt = s->nactive * s->temperature;
+  s->eta += dt * (e2 / ttt - 1.0) * s->isq_tau_eta;
+}
+
+/* move_atoms_mik (src/imd_integrate.c:675-873): a momentum that points
+ * against the force is set to zero (microconvergence) */
+void orc_move_atoms_mik(orc_sys_t *s) {
+  double ekin = 0.0, fnorm = 0.0, fmax2 = 0.0;
+  double dt = s->timestep;
+  for (int nn = 0; nn < s->n; nn++) {
+    int i = s->order[nn];
+    double *p = s->p + 3 * i, *f = s->f + 3 * i, *x = s->x + 3 * i;
+    double kin1 = p[0] * p[0] + p[1] * p[1] + p[2] * p[2];
+    int t = s->type[i];
+    f[0] *= restr(s, t, 0);
+    f[1] *= restr(s, t, 1);
+    f[2] *= restr(s, t, 2);
+    fnorm += f[0] * f[0] + f[1] * f[1] + f[2] * f[2];
+    fmax2 = OMAX(SQR(f[0]), fmax2);
+    fmax2 = OMAX(SQR(f[1]), fmax2);
+    fmax2 = OMAX(SQR(f[2]), fmax2);
+    p[0] += dt * f[0];
+    p[1] += dt * f[1];
+    p[2] += dt * f[2];
+    if (0.0 > p[0] * f[0] + p[1] * f[1] + p[2] * f[2]) {
+      p[0] = p[1] = p[2] = 0.0;
+    } else {
+      double tmp = dt / s->mass[i];
+      x[0] += tmp * p[0];
+      x[1] += tmp * p[1];
+      x[2] += tmp * p[2];
+    }
+    double kin2 = p[0] * p[0] + p[1] * p[1] + p[2] * p[2];
+    ekin += (kin1 + kin2) / (4.0 * s->mass[i]);
+  }
+  s->tot_kin_energy = ekin;
+  s->fnorm = fnorm;
+  s->f_max2 = fmax2;
+}
+
 /* check_nblist (src/imd_forces_nbl.c:2007-2037) */
 void orc_check_nblist(orc_sys_t *s) {
   double max1 = 0.0;
@@ -963,6 +1032,21 @@ void orc_check_nblist(orc_sys_t *s) {
     if (r2 > max1) max1 = r2;
   }
   if (max1 > SQR(0.5 * s->nbl_margin)) s->have_valid_nbl = 0;
+}
+
+int orc_md_steps(orc_sys_t *s, int nsteps, int ensemble, double *epot_out,
+                 double *ekin_out, double *extra_out) {
+  for (int st = 0; st < nsteps; st++) {
+    orc_calc_forces(s);
+    if (epot_out) epot_out[st] = s->tot_pot_energy;
+    if (ensemble == 1) orc_move_atoms_nvt(s);
+    else if (ensemble == 2) orc_move_atoms_mik(s);
+    else orc_move_atoms_nve(s);
+    if (ekin_out) ekin_out[st] = s->tot_kin_energy;
+    if (extra_out) extra_out[st] = (ensemble == 1) ? s->eta : s->fnorm;
+    orc_check_nblist(s);
+  }
+  return 0;
 }
 
 int orc_nve_steps(orc_sys_t *s, int nsteps, double *epot_out, double *ekin_out) {

@@ -134,6 +134,9 @@ typedef struct {
   double *estress;            /* 6*next: PRESSTENS xx yy zz yz zx xy */
   double *stress;             /* 6n, after the ghost fold */
   double  tot_stress[6];      /* calc_tot_presstens (src/imd_main_3d.c:2069) */
+
+  /* ---- NVT thermostat (globals eta, isq_tau_eta, temperature) ---- */
+  double  eta, isq_tau_eta, temperature;
 } orc_sys_t;
 
 /* set defaults; allocate per-atom arrays for n atoms */
@@ -152,6 +155,14 @@ void orc_move_atoms_nve(orc_sys_t *s);
 void orc_check_nblist(orc_sys_t *s);
 /* one main_loop NVE step: calc_forces, move_atoms_nve, check_nblist */
 int  orc_nve_steps(orc_sys_t *s, int nsteps, double *epot_out, double *ekin_out);
+/* move_atoms_nvt (src/imd_integrate.c:891-1150, no UNIAX) and move_atoms_mik
+ * (src/imd_integrate.c:675-873) */
+void orc_move_atoms_nvt(orc_sys_t *s);
+void orc_move_atoms_mik(orc_sys_t *s);
+/* main_loop steps with move_atoms of `ensemble` (0 nve, 1 nvt, 2 mik);
+ * per step tot_pot_energy, tot_kin_energy and (nvt) eta / (mik) fnorm */
+int  orc_md_steps(orc_sys_t *s, int nsteps, int ensemble, double *epot_out,
+                  double *ekin_out, double *extra_out);
 /* CG: reset_cg, cg_step (src/imd_cg.c:30-66) */
 int  orc_reset_cg(orc_sys_t *s);
 int  orc_cg_step(orc_sys_t *s, int steps);

@@ -58,7 +58,8 @@ class Sys(C.Structure):
         ("cg_poteng", C.c_double), ("old_cg_poteng", C.c_double),
         ("old_alphamin", C.c_double), ("nactive", C.c_long),
         ("do_stress", C.c_int), ("estress", _dp), ("stress", _dp),
-        ("tot_stress", C.c_double * 6)]
+        ("tot_stress", C.c_double * 6),
+        ("eta", C.c_double), ("isq_tau_eta", C.c_double), ("temperature", C.c_double)]
 
 
 _lib = None
@@ -86,6 +87,7 @@ def lib() -> C.CDLL:
         L.orc_check_nblist.argtypes = [C.POINTER(Sys)]
         L.orc_free.argtypes = [C.POINTER(Sys)]
         L.orc_nve_steps.argtypes = [C.POINTER(Sys), C.c_int, _dp, _dp]
+        L.orc_md_steps.argtypes = [C.POINTER(Sys), C.c_int, C.c_int, _dp, _dp, _dp]
         L.orc_cg_step.argtypes = [C.POINTER(Sys), C.c_int]
         L.orc_cg_relax.argtypes = [C.POINTER(Sys), C.c_double, C.c_int, _dp]
         L.orc_max_atom_force.argtypes = [C.POINTER(Sys)]
@@ -247,6 +249,21 @@ class OracleSystem:
         ek = np.empty(nsteps)
         lib().orc_nve_steps(C.byref(self.s), nsteps, _ptr(ep), _ptr(ek))
         return ep, ek
+
+    def md(self, nsteps: int, ensemble: str = "nve"):
+        """main_loop steps with move_atoms_nve / _nvt / _mik: per step
+        tot_pot_energy, tot_kin_energy and eta (nvt) or fnorm (nve, mik)."""
+        code = {"nve": 0, "nvt": 1, "mik": 2}[ensemble]
+        ep = np.empty(nsteps)
+        ek = np.empty(nsteps)
+        ex = np.empty(nsteps)
+        lib().orc_md_steps(C.byref(self.s), nsteps, code, _ptr(ep), _ptr(ek), _ptr(ex))
+        return ep, ek, ex
+
+    def set_nvt(self, temperature: float, isq_tau_eta: float, eta: float = 0.0) -> None:
+        self.s.temperature = temperature
+        self.s.isq_tau_eta = isq_tau_eta
+        self.s.eta = eta
 
     def cg_relax(self, fmax: float, maxsteps: int = 100000):
         fm = C.c_double(0.0)

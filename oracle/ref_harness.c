@@ -14,6 +14,7 @@
  * and then one of
  *   forces  : calc_forces(0) and dump atoms, totals and the neighbour pairs
  *   nve K   : K main_loop steps calc_forces / move_atoms / check_nblist
+ *             (move_atoms of the parameter file's ensemble: nve, nvt, mik)
  *   cg K F  : reset_cg, then cg_step until max per-atom |F| <= F
  *   time K  : K NVE steps, print cpu seconds
  */
@@ -177,7 +178,14 @@ int main(int argc, char **argv) {
       calc_forces(steps);
       double ep = tot_pot_energy;
       move_atoms();
-      fprintf(out, "%d %.17e %.17e %ld\n", steps, ep, tot_kin_energy, (long)nbl_count);
+      fprintf(out, "%d %.17e %.17e %ld", steps, ep, tot_kin_energy, (long)nbl_count);
+#ifdef NVT
+      fprintf(out, " %.17e", eta);  /* Nose-Hoover variable after the step */
+#endif
+#ifdef FNORM
+      fprintf(out, " %.17e %.17e", fnorm, f_max2);
+#endif
+      fprintf(out, "\n");
       check_nblist();
     }
     clock_t t1 = clock();

@@ -25,7 +25,13 @@ Fixtures (all sorted by atom number):
               Cu/Ni and LJ cases run by the `stress` build (STRESS_TENS):
               per-atom PRESSTENS and calc_tot_presstens
 
-`python tests/golden/make_golden.py stress` writes the stress fixtures only.
+  cu_nvt      Sutton-Chen Cu _fcc 8^3, 300 K, 100 Nose-Hoover NVT steps
+              (tau_eta 10 time units): energies and eta per step
+  cu_mik      cu_pert's configuration quenched by 200 MIK steps: energies,
+              force norms per step, final positions
+
+`python tests/golden/make_golden.py stress` writes the stress fixtures only,
+`... ensembles` the NVT / MIK ones.
 """
 from __future__ import annotations
 
@@ -316,9 +322,59 @@ def stress_cases() -> None:
         print(name, "atoms", len(st["x"]), "tot_stress", tot_stress)
 
 
+def ensemble_cases() -> None:
+    """move_atoms_nvt and move_atoms_mik (src/imd_integrate.c:891, :675) run by
+    the reference's `nvt` and `mik` builds through the same main_loop steps."""
+    subprocess.run(["make", "-s", "-C", ORACLE, "ref"], check=True)
+    tmp = tempfile.mkdtemp(prefix="imdgold_ens")
+    cu = tuple(os.path.join(HERE, "cu" + e) for e in (".pt", ".rho", ".emb"))
+    base = dict(outfiles=os.path.join(tmp, "o"), ntypes=1, masses=63.546,
+                pbc_dirs=[1, 1, 1], timestep=0.0982266, maxsteps=0, seed=2,
+                core_potential_file=cu[0], **{"atomic_e-density_file": cu[1]},
+                embedding_energy_file=cu[2], nbl_margin=0.4, eng_int=0,
+                checkpt_int=100000000)
+    # NVT from IMD's own generator and maxwell at 300 K
+    p = os.path.join(tmp, "cu_nvt.param")
+    wl.write_param(p, coordname="_fcc", box_param=[8, 8, 8], box_unit=3.615,
+                   ensemble="nvt", starttemp=0.0258520, tau_eta=10.0, **base)
+    pre = os.path.join(tmp, "cu_nvt")
+    run("nvt_nbl_eam", p, "nve", pre, 100)
+    st0 = load_state(pre + ".state0")
+    stf = load_state(pre + ".final")
+    steps = np.loadtxt(pre + ".steps")
+    box, gdim, cellsz = load_box(pre + ".box")
+    d = dict(box=box, gdim=gdim, cellsz=cellsz, number=st0["number"], type=st0["type"],
+             mass=st0["mass"], x0=st0["x"], p0=st0["p"], epot=steps[:, 1], ekin=steps[:, 2],
+             nbl_count=steps[:, 3], eta=steps[:, 4], x_final=stf["x"], p_final=stf["p"],
+             dt=0.0982266, skin=0.4, temperature=0.0258520, isq_tau_eta=1.0 / 100.0)
+    np.savez_compressed(os.path.join(HERE, "cu_nvt.npz"), **d)
+    print("cu_nvt eta", steps[[0, -1], 4], "ekin", steps[[0, -1], 2])
+    # MIK quench of cu_pert's configuration
+    cus = wl.eam_fcc_system(8)
+    cfg = os.path.join(tmp, "cu_pert.cfg")
+    perturbed_config(cus, 0.1, 12, cfg)
+    p = os.path.join(tmp, "cu_mik.param")
+    wl.write_param(p, coordname=cfg, box_from_header=1, ensemble="mik", starttemp=0.0, **base)
+    pre = os.path.join(tmp, "cu_mik")
+    run("mik_nbl_eam", p, "nve", pre, 200)
+    st0 = load_state(pre + ".state0")
+    stf = load_state(pre + ".final")
+    steps = np.loadtxt(pre + ".steps")
+    box, gdim, cellsz = load_box(pre + ".box")
+    d = dict(box=box, gdim=gdim, cellsz=cellsz, number=st0["number"], type=st0["type"],
+             mass=st0["mass"], x0=st0["x"], p0=st0["p"], epot=steps[:, 1], ekin=steps[:, 2],
+             nbl_count=steps[:, 3], fnorm=steps[:, 4], f_max2=steps[:, 5],
+             x_final=stf["x"], p_final=stf["p"], dt=0.0982266, skin=0.4)
+    np.savez_compressed(os.path.join(HERE, "cu_mik.npz"), **d)
+    print("cu_mik epot", steps[[0, -1], 1], "fnorm", steps[[0, -1], 4])
+
+
 if __name__ == "__main__":
     if len(sys.argv) > 1 and sys.argv[1] == "stress":
         stress_cases()
+    elif len(sys.argv) > 1 and sys.argv[1] == "ensembles":
+        ensemble_cases()
     else:
         main()
         stress_cases()
+        ensemble_cases()

@@ -147,3 +147,34 @@ def test_stress_matches_reference(name):
     assert np.all(np.abs(tot - g["tot_stress"]) <= 1e-12 * np.max(np.abs(g["tot_stress"])))
     assert abs(tot[:3].sum() - g["virial"]) <= 1e-11 * abs(g["virial"])
     assert rel_rms(s.f, g["f"]) < 1e-11
+
+
+def test_nvt_trajectory_matches_reference():
+    """move_atoms_nvt (Nose-Hoover): same start, 100 steps; energies to 1e-9
+    relative, the thermostat variable eta to 1e-8 relative (1e-12 absolute),
+    the same list rebuilds."""
+    g = golden("cu_nvt")
+    s = OracleSystem(g["box"], g["x0"], g["type"], g["mass"], g["number"], 1, tables("cu"),
+                     True, float(g["skin"]), timestep=float(g["dt"]), p=g["p0"])
+    s.set_nvt(float(g["temperature"]), float(g["isq_tau_eta"]))
+    ep, ek, eta = s.md(len(g["epot"]), "nvt")
+    np.testing.assert_allclose(ep, g["epot"], rtol=1e-9, atol=0)
+    np.testing.assert_allclose(ek, g["ekin"], rtol=1e-8, atol=0)
+    np.testing.assert_allclose(eta, g["eta"], rtol=1e-8, atol=1e-12)
+    assert s.nbl_count == int(g["nbl_count"][-1])
+
+
+def test_mik_quench_matches_reference():
+    """move_atoms_mik: 200 quench steps from a perturbed lattice; energies to
+    1e-9 relative, force norms to 1e-6 relative (a momentum zeroed one step
+    apart would show far above that), final positions to 1e-8 A."""
+    g = golden("cu_mik")
+    s = OracleSystem(g["box"], g["x0"], g["type"], g["mass"], g["number"], 1, tables("cu"),
+                     True, float(g["skin"]), timestep=float(g["dt"]), p=g["p0"])
+    ep, ek, fn = s.md(len(g["epot"]), "mik")
+    np.testing.assert_allclose(ep, g["epot"], rtol=1e-9, atol=0)
+    np.testing.assert_allclose(ek, g["ekin"], rtol=1e-7, atol=1e-12)
+    np.testing.assert_allclose(fn, g["fnorm"], rtol=1e-6, atol=0)
+    d = s.x - g["x_final"]
+    d -= np.round(d @ np.linalg.inv(g["box"])) @ g["box"]
+    assert np.abs(d).max() < 1e-8
