@@ -107,6 +107,10 @@ def lib() -> C.CDLL:
         L.imdgpu_batch_set_compaction.argtypes = [vp, C.c_int]
         L.imdgpu_autotune.argtypes = [vp, _ip, _ip]
         L.imdgpu_calc_stress.argtypes = [vp, _dp, _dp]
+        L.imdgpu_move_atoms_mik.argtypes = [vp, C.c_double]
+        L.imdgpu_move_atoms_nvt.argtypes = [vp, C.c_double]
+        L.imdgpu_set_nvt.argtypes = [vp, C.c_double, C.c_double, C.c_double, C.c_long]
+        L.imdgpu_get_nvt.argtypes = [vp, _dp]
         L.imdgpu_set_blocks.argtypes = [vp, C.c_int, C.c_int]
         L.imdgpu_batch_set_autotune.argtypes = [vp, C.c_int]
         L.imdgpu_batch_positions.argtypes = [vp, _dp]
@@ -254,6 +258,20 @@ class GpuSystem:
 
     def move_atoms_nve(self, timestep: float) -> None:
         _check(lib().imdgpu_move_atoms_nve(self.h, timestep), "move_atoms_nve")
+
+    def move_atoms_mik(self, timestep: float) -> None:
+        _check(lib().imdgpu_move_atoms_mik(self.h, timestep), "move_atoms_mik")
+
+    def set_nvt(self, temperature: float, isq_tau_eta: float, eta: float = 0.0,
+                nactive: int = 0) -> None:
+        _check(lib().imdgpu_set_nvt(self.h, temperature, isq_tau_eta, eta, nactive), "set_nvt")
+
+    def move_atoms_nvt(self, timestep: float) -> float:
+        """One Nose-Hoover step of the atoms; returns eta after it."""
+        _check(lib().imdgpu_move_atoms_nvt(self.h, timestep), "move_atoms_nvt")
+        e = C.c_double(0.0)
+        _check(lib().imdgpu_get_nvt(self.h, C.byref(e)), "get_nvt")
+        return e.value
 
     def nve_run(self, nsteps: int, timestep: float, record: bool = True):
         ep = np.empty(nsteps) if record else None

@@ -180,6 +180,11 @@ struct imdgpu_sys {
   int *ml_sel = nullptr;           // per cell: 1 = the prediction is kept
   int ml_save_cap = 0, ml_cell_cap = 0;
 
+  // NVT thermostat (IMD's globals eta, isq_tau_eta, temperature, nactive)
+  double nvt_eta = 0.0, nvt_isq_tau = 0.0, nvt_temp = 0.0;
+  long nvt_nactive = 0;
+  double *d_e2 = nullptr;
+
   // STRESS_TENS: per ext atom xx yy zz yz zx xy
   double *d_stress = nullptr;
   size_t stress_cap = 0;
@@ -600,6 +605,140 @@ __global__ void k_finalize_nve(const double *partial, int nb, DevScalars *sc, do
       hist[2 * s + 1] = a;
       *istep = s + 1;
     }
+  }
+}
+
+// move_atoms_mik (src/imd_integrate.c:675-873): as move_atoms_nve, but a
+// momentum that ends up against the force is set to zero (microconvergence)
+// and the atom stays; IMD's operation order, unfused
+__global__ void __launch_bounds__(BS_VEC) k_mik(SysView v, double dt, double *partial) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double ek = 0.0, fn = 0.0, fm = 0.0, dm = 0.0;
+  if (i < v.n) {
+    double4 p = v.mom[i], f = v.frc[i], x = v.pos[i];
+    const int t = (int)x.w;
+    const double kin1 = dadd(dadd(dmul(p.x, p.x), dmul(p.y, p.y)), dmul(p.z, p.z));
+    f.x = dmul(f.x, v.restr[3 * t]);
+    f.y = dmul(f.y, v.restr[3 * t + 1]);
+    f.z = dmul(f.z, v.restr[3 * t + 2]);
+    v.frc[i] = f;
+    fn = dadd(dadd(dmul(f.x, f.x), dmul(f.y, f.y)), dmul(f.z, f.z));
+    fm = fmax(fmax(f.x * f.x, f.y * f.y), f.z * f.z);
+    p.x = dadd(p.x, dmul(dt, f.x));
+    p.y = dadd(p.y, dmul(dt, f.y));
+    p.z = dadd(p.z, dmul(dt, f.z));
+    if (0.0 > dadd(dadd(dmul(p.x, f.x), dmul(p.y, f.y)), dmul(p.z, f.z))) {
+      p.x = p.y = p.z = 0.0;
+    } else {
+      const double tmp = dt / p.w;
+      x.x = dadd(x.x, dmul(tmp, p.x));
+      x.y = dadd(x.y, dmul(tmp, p.y));
+      x.z = dadd(x.z, dmul(tmp, p.z));
+    }
+    const double kin2 = dadd(dadd(dmul(p.x, p.x), dmul(p.y, p.y)), dmul(p.z, p.z));
+    ek = dadd(kin1, kin2) / (4.0 * p.w);
+    v.mom[i] = p;
+    v.pos[i] = x;
+    const double4 r = v.ref[i];
+    const double ddx = dsub(x.x, r.x), ddy = dsub(x.y, r.y), ddz = dsub(x.z, r.z);
+    dm = r2_exact(ddx, ddy, ddz);
+  }
+  block_reduce_ssmm<BS_VEC>(ek, fn, fm, dm, partial);
+}
+
+// move_atoms_nvt (src/imd_integrate.c:891-1150, no UNIAX): the Nose-Hoover
+// friction eta enters as reibung = 1 - eta dt / 2 and eins_d_reib =
+// 1 / (1 + eta dt / 2); per block sums of twice the old and the new kinetic
+// energy and of |F|^2, maxima of the force component and of the
+// displacement since the last list build
+__global__ void __launch_bounds__(BS_VEC) k_nvt(SysView v, double dt, double reibung,
+                                                double eins_d_reib, double *partial) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double e1 = 0.0, e2 = 0.0, fn = 0.0, fm = 0.0, dm = 0.0;
+  if (i < v.n) {
+    double4 p = v.mom[i], f = v.frc[i], x = v.pos[i];
+    const int t = (int)x.w;
+    const double m = p.w;
+    e1 = dadd(dadd(dmul(p.x, p.x), dmul(p.y, p.y)), dmul(p.z, p.z)) / m;
+    const double rx = v.restr[3 * t], ry = v.restr[3 * t + 1], rz = v.restr[3 * t + 2];
+    f.x = dmul(f.x, rx);
+    f.y = dmul(f.y, ry);
+    f.z = dmul(f.z, rz);
+    v.frc[i] = f;
+    fn = dadd(dadd(dmul(f.x, f.x), dmul(f.y, f.y)), dmul(f.z, f.z));
+    fm = fmax(fmax(f.x * f.x, f.y * f.y), f.z * f.z);
+    p.x = dmul(dmul(dadd(dmul(p.x, reibung), dmul(dt, f.x)), eins_d_reib), rx);
+    p.y = dmul(dmul(dadd(dmul(p.y, reibung), dmul(dt, f.y)), eins_d_reib), ry);
+    p.z = dmul(dmul(dadd(dmul(p.z, reibung), dmul(dt, f.z)), eins_d_reib), rz);
+    e2 = dadd(dadd(dmul(p.x, p.x), dmul(p.y, p.y)), dmul(p.z, p.z)) / m;
+    const double tmp = dt / m;
+    x.x = dadd(x.x, dmul(tmp, p.x));
+    x.y = dadd(x.y, dmul(tmp, p.y));
+    x.z = dadd(x.z, dmul(tmp, p.z));
+    v.mom[i] = p;
+    v.pos[i] = x;
+    const double4 r = v.ref[i];
+    const double ddx = dsub(x.x, r.x), ddy = dsub(x.y, r.y), ddz = dsub(x.z, r.z);
+    dm = r2_exact(ddx, ddy, ddz);
+  }
+  __shared__ double sh[5][BS_VEC / 32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  e1 = warp_sum(e1);
+  e2 = warp_sum(e2);
+  fn = warp_sum(fn);
+  fm = warp_max(fm);
+  dm = warp_max(dm);
+  if (lane == 0) {
+    sh[0][w] = e1;
+    sh[1][w] = e2;
+    sh[2][w] = fn;
+    sh[3][w] = fm;
+    sh[4][w] = dm;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a = 0, b = 0, c = 0, d = 0, e = 0;
+    for (int k = 0; k < BS_VEC / 32; k++) {
+      a += sh[0][k];
+      b += sh[1][k];
+      c += sh[2][k];
+      d = fmax(d, sh[3][k]);
+      e = fmax(e, sh[4][k]);
+    }
+    double *o = partial + 5 * (size_t)blockIdx.x;
+    o[0] = a;
+    o[1] = b;
+    o[2] = c;
+    o[3] = d;
+    o[4] = e;
+  }
+}
+
+// fixed-order sums of the NVT partials: tot_kin_energy = (E1 + E2) / 4 and,
+// in out2, twice the new kinetic energy for the eta update
+__global__ void k_finalize_nvt(const double *partial, int nb, DevScalars *sc, double skin2,
+                               double *out2) {
+  const int lane = threadIdx.x;
+  double a = 0, b = 0, c = 0, d = 0, e = 0;
+  for (int k = lane; k < nb; k += 32) {
+    a += partial[5 * k];
+    b += partial[5 * k + 1];
+    c += partial[5 * k + 2];
+    d = fmax(d, partial[5 * k + 3]);
+    e = fmax(e, partial[5 * k + 4]);
+  }
+  a = warp_sum(a);
+  b = warp_sum(b);
+  c = warp_sum(c);
+  d = warp_max(d);
+  e = warp_max(e);
+  if (lane == 0) {
+    sc->ekin = (a + b) / 4.0;
+    sc->fnorm = c;
+    sc->fmax2 = d;
+    sc->maxdisp2 = e;
+    if (e > skin2) sc->rebuild = 1;
+    *out2 = b;
   }
 }
 
@@ -1528,6 +1667,7 @@ int imdgpu_destroy(imdgpu_sys *s) {
   dfree(s->ml_loss);
   dfree(s->ml_save); dfree(s->ml_ecell); dfree(s->ml_sel);
   dfree(s->d_stress);
+  dfree(s->d_e2);
   dfree(s->d_sys_short);
   dfree(s->d_atom_sys); dfree(s->d_aoff); dfree(s->d_sgdim); dfree(s->d_scdim); dfree(s->d_scoff);
   dfree(s->d_sys_done); dfree(s->d_ndone); dfree(s->d_sbox); dfree(s->d_stbox); dfree(s->d_cs);
@@ -1908,6 +2048,7 @@ int imdgpu_calc_stress(imdgpu_sys *s, double *presstens, double *tot) {
   const size_t ext = (size_t)s->ncap + s->gcap;
   if (s->stress_cap < ext) {
     dfree(s->d_stress);
+  dfree(s->d_e2);
     CK(dalloc(&s->d_stress, 6 * ext));
     s->stress_cap = ext;
   }
@@ -1976,6 +2117,62 @@ int imdgpu_move_atoms_nve(imdgpu_sys *s, double timestep) {
   k_finalize_nve<<<1, 32, 0, s->st>>>(s->partial, nb, s->dsc, v.skin2, nullptr, nullptr);
   CK(cudaGetLastError());
   return read_back(s);
+}
+
+// move_atoms_mik (src/imd_integrate.c:675-873)
+int imdgpu_move_atoms_mik(imdgpu_sys *s, double timestep) {
+  if (!s || !s->atoms_set) return fail(IMDGPU_ERR_STATE, "atoms not set");
+  if (!s->geom_ready || s->nbcap == 0)
+    return fail(IMDGPU_ERR_STATE, "move_atoms before the first calc_forces");
+  SysView v = view(s);
+  const int nb = nblk(s->n, BS_VEC);
+  k_mik<<<nb, BS_VEC, 0, s->st>>>(v, timestep, s->partial);
+  k_finalize_nve<<<1, 32, 0, s->st>>>(s->partial, nb, s->dsc, v.skin2, nullptr, nullptr);
+  CK(cudaGetLastError());
+  return read_back(s);
+}
+
+// the Nose-Hoover state of move_atoms_nvt; nactive <= 0: three per atom
+int imdgpu_set_nvt(imdgpu_sys *s, double temperature, double isq_tau_eta, double eta,
+                   long nactive) {
+  if (!s || !s->atoms_set) return fail(IMDGPU_ERR_STATE, "atoms not set");
+  if (!(temperature > 0.0) || isq_tau_eta < 0.0)
+    return fail(IMDGPU_ERR_ARG, "nvt: temperature > 0 and isq_tau_eta >= 0");
+  s->nvt_temp = temperature;
+  s->nvt_isq_tau = isq_tau_eta;
+  s->nvt_eta = eta;
+  s->nvt_nactive = nactive > 0 ? nactive : 3L * s->n;
+  return IMDGPU_OK;
+}
+
+int imdgpu_get_nvt(imdgpu_sys *s, double *eta) {
+  if (!s || !eta) return fail(IMDGPU_ERR_ARG, "null");
+  *eta = s->nvt_eta;
+  return IMDGPU_OK;
+}
+
+// move_atoms_nvt (src/imd_integrate.c:891-1150): the atoms on the device,
+// then eta += dt (E_kin_2 / (nactive T) - 1) isq_tau_eta on the host
+int imdgpu_move_atoms_nvt(imdgpu_sys *s, double timestep) {
+  if (!s || !s->atoms_set) return fail(IMDGPU_ERR_STATE, "atoms not set");
+  if (!s->geom_ready || s->nbcap == 0)
+    return fail(IMDGPU_ERR_STATE, "move_atoms before the first calc_forces");
+  if (!(s->nvt_temp > 0.0)) return fail(IMDGPU_ERR_STATE, "imdgpu_set_nvt first");
+  if (!s->d_e2) CK(dalloc(&s->d_e2, 1));
+  SysView v = view(s);
+  const int nb = nblk(s->n, BS_VEC);
+  const double reibung = 1.0 - s->nvt_eta * timestep / 2.0;
+  const double eins_d_reib = 1.0 / (1.0 + s->nvt_eta * timestep / 2.0);
+  k_nvt<<<nb, BS_VEC, 0, s->st>>>(v, timestep, reibung, eins_d_reib, s->partial);
+  k_finalize_nvt<<<1, 32, 0, s->st>>>(s->partial, nb, s->dsc, v.skin2, s->d_e2);
+  CK(cudaGetLastError());
+  double e2 = 0.0;
+  CK(cudaMemcpyAsync(&e2, s->d_e2, sizeof(double), cudaMemcpyDeviceToHost, s->st));
+  int rc = read_back(s);
+  if (rc) return rc;
+  const double ttt = s->nvt_nactive * s->nvt_temp;
+  s->nvt_eta += timestep * (e2 / ttt - 1.0) * s->nvt_isq_tau;
+  return IMDGPU_OK;
 }
 
 // One chunk of NVE steps with guarded device-side rebuilds.  With profiling

@@ -146,6 +146,18 @@ int imdgpu_deallocate_nblist(imdgpu_sys *sys);
 int imdgpu_estimate_nblist_size(imdgpu_sys *sys, long *entries);
 /* move_atoms_nve (src/imd_integrate.c:32-497) */
 int imdgpu_move_atoms_nve(imdgpu_sys *sys, double timestep);
+/* move_atoms_mik (src/imd_integrate.c:675-873): NVE with microconvergence
+ * (a momentum against the force is set to zero) */
+int imdgpu_move_atoms_mik(imdgpu_sys *sys, double timestep);
+/* move_atoms_nvt (src/imd_integrate.c:891-1150): Nose-Hoover NVT.  Its state
+ * is IMD's globals temperature (kT), isq_tau_eta (1/tau_eta^2), eta and
+ * nactive (degrees of freedom; <= 0 means 3 per atom), set once with
+ * imdgpu_set_nvt; each call advances eta as IMD does, imdgpu_get_nvt reads
+ * it. */
+int imdgpu_set_nvt(imdgpu_sys *sys, double temperature, double isq_tau_eta, double eta,
+                   long nactive);
+int imdgpu_get_nvt(imdgpu_sys *sys, double *eta);
+int imdgpu_move_atoms_nvt(imdgpu_sys *sys, double timestep);
 /* nsteps of main_loop (src/imd_main_3d.c:155-870) for ensemble nve:
  * calc_forces, move_atoms_nve, check_nblist, fully on the device.
  * epot/ekin (may be NULL) receive tot_pot_energy and tot_kin_energy of every

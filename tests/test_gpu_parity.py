@@ -329,3 +329,55 @@ def test_stress_matches_reference(name):
     assert np.max(np.abs(st - g["stress"])) <= 1e-11 * scale
     assert np.all(np.abs(tot - g["tot_stress"]) <= 1e-12 * np.max(np.abs(g["tot_stress"])))
     assert rel_rms(s.get_atoms()["f"], g["f"]) < 1e-11
+
+
+def _stepwise(name, move):
+    g = golden(name)
+    gg = dict(g)
+    gg["x"] = g["x0"]
+    s = gpu_system(gg, "cu", 1, 1, float(g["skin"]), p=g["p0"])
+    dt = float(g["dt"])
+    ep, ek, extra = [], [], []
+    for st in range(len(g["epot"])):
+        s.calc_forces(st)
+        ep.append(s.scalars().tot_pot_energy)
+        extra.append(move(s, dt))
+        ek.append(s.scalars().tot_kin_energy)
+        s.check_nblist()
+    return g, s, np.array(ep), np.array(ek), np.array(extra)
+
+
+def test_nvt_matches_reference():
+    """move_atoms_nvt on the device, 100 main_loop steps against the
+    reference's `nvt` build: energies to 1e-9, eta to 1e-8 relative."""
+    g0 = golden("cu_nvt")
+
+    def move(s, dt):
+        if not hasattr(s, "_nvt"):
+            s.set_nvt(float(g0["temperature"]), float(g0["isq_tau_eta"]))
+            s._nvt = True
+        return s.move_atoms_nvt(dt)
+
+    g, s, ep, ek, eta = _stepwise("cu_nvt", move)
+    np.testing.assert_allclose(ep, g["epot"], rtol=1e-9, atol=0)
+    np.testing.assert_allclose(ek, g["ekin"], rtol=1e-8, atol=0)
+    np.testing.assert_allclose(eta, g["eta"], rtol=1e-8, atol=1e-12)
+    assert s.scalars().nbl_count == int(g["nbl_count"][-1])
+
+
+def test_mik_matches_reference():
+    """move_atoms_mik on the device, 200 quench steps against the reference's
+    `mik` build: energies to 1e-9, force norms to 1e-6 relative, final
+    positions to 1e-8 A."""
+    def move(s, dt):
+        s.move_atoms_mik(dt)
+        return s.scalars().fnorm
+
+    g, s, ep, ek, fn = _stepwise("cu_mik", move)
+    np.testing.assert_allclose(ep, g["epot"], rtol=1e-9, atol=0)
+    np.testing.assert_allclose(ek, g["ekin"], rtol=1e-7, atol=1e-12)
+    np.testing.assert_allclose(fn, g["fnorm"], rtol=1e-6, atol=0)
+    x = s.get_atoms()["x"]
+    d = x - g["x_final"]
+    d -= np.round(d @ np.linalg.inv(g["box"])) @ g["box"]
+    assert np.abs(d).max() < 1e-8
