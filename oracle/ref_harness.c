@@ -13,6 +13,8 @@
  *   maxwell (src/imd_main_3d.c:89)
  * and then one of
  *   forces  : calc_forces(0) and dump atoms, totals and the neighbour pairs
+ *   snap K E: K main_loop steps from step 0; every E steps the state before
+ *             the step and after its calc_forces
  *   nve K   : K main_loop steps calc_forces / move_atoms / check_nblist
  *             (move_atoms of the parameter file's ensemble: nve, nvt, mik)
  *   cg K F  : reset_cg, then cg_step until max per-atom |F| <= F
@@ -169,6 +171,32 @@ int main(int argc, char **argv) {
     sprintf(fname, "%s.totals", pre);
     FILE *out = fopen(fname, "w");
     fprintf(out, "%.17e %.17e %ld\n", tot_pot_energy, virial, (long)natoms);
+    fclose(out);
+  } else if (0 == strcmp(mode, "snap")) {
+    /* K main_loop steps; every `every` steps (step 0 included) the state
+     * before the step, and the forces and energy of its calc_forces */
+    int every = (argc > 5) ? atoi(argv[5]) : 100;
+    sprintf(fname, "%s.steps", pre);
+    FILE *out = fopen(fname, "w");
+    for (steps = 0; steps <= nsteps; steps++) {
+      if (steps % every == 0) {
+        sprintf(fname, "%s.pre%05d", pre, steps);
+        dump_state(fname);
+      }
+      calc_forces(steps);
+      if (steps % every == 0) {
+        sprintf(fname, "%s.snap%05d", pre, steps);
+        dump_state(fname);
+      }
+      double ep = tot_pot_energy;
+      if (steps == nsteps) {
+        fprintf(out, "%d %.17e 0 %ld\n", steps, ep, (long)nbl_count);
+        break;
+      }
+      move_atoms();
+      fprintf(out, "%d %.17e %.17e %ld\n", steps, ep, tot_kin_energy, (long)nbl_count);
+      check_nblist();
+    }
     fclose(out);
   } else if (0 == strcmp(mode, "nve") || 0 == strcmp(mode, "time")) {
     sprintf(fname, "%s.steps", pre);

@@ -25,13 +25,16 @@ Fixtures (all sorted by atom number):
               Cu/Ni and LJ cases run by the `stress` build (STRESS_TENS):
               per-atom PRESSTENS and calc_tot_presstens
 
+  lj_nve1000  the LJ set-up of lj_nve run for the full 1000 steps:
+              energies of every step; every 250 steps the positions and
+              momenta before the step and the forces of its calc_forces
   cu_nvt      Sutton-Chen Cu _fcc 8^3, 300 K, 100 Nose-Hoover NVT steps
               (tau_eta 10 time units): energies and eta per step
   cu_mik      cu_pert's configuration quenched by 200 MIK steps: energies,
               force norms per step, final positions
 
 `python tests/golden/make_golden.py stress` writes the stress fixtures only,
-`... ensembles` the NVT / MIK ones.
+`... ensembles` the NVT / MIK ones, `... lj1000` the 1000-step LJ run.
 """
 from __future__ import annotations
 
@@ -369,12 +372,49 @@ def ensemble_cases() -> None:
     print("cu_mik epot", steps[[0, -1], 1], "fnorm", steps[[0, -1], 4])
 
 
+def lj1000_case() -> None:
+    """The plain-method LJ workload (4000 atoms, T* 0.72, dt 0.005, skin 0.3)
+    for all of its 1000 steps, with snapshots every 250 steps."""
+    subprocess.run(["make", "-s", "-C", ORACLE, "ref"], check=True)
+    tmp = tempfile.mkdtemp(prefix="imdgold_lj")
+    lj2 = os.path.join(HERE, "lj.pt")
+    lj = wl.lj_fcc_system(10)
+    p = os.path.join(tmp, "lj.param")
+    wl.write_param(p, coordname="_fcc", outfiles=os.path.join(tmp, "o"), ensemble="nve",
+                   ntypes=1, masses=1.0, pbc_dirs=[1, 1, 1], timestep=0.005, maxsteps=0,
+                   starttemp=0.72, seed=1, potfile=lj2, nbl_margin=0.3, eng_int=0,
+                   checkpt_int=100000000, box_param=[10, 10, 10], box_unit=lj.meta["a0"])
+    pre = os.path.join(tmp, "lj")
+    every = 250
+    run("nve_nbl", p, "snap", pre, 1000, every)
+    steps = np.loadtxt(pre + ".steps")
+    box, gdim, cellsz = load_box(pre + ".box")
+    snaps = list(range(0, 1001, every))
+    x, pp, f, ep = [], [], [], []
+    for k in snaps:
+        a = load_state(pre + ".pre%05d" % k)
+        b = load_state(pre + ".snap%05d" % k)
+        x.append(a["x"])
+        pp.append(a["p"])
+        f.append(b["f"])
+    st0 = load_state(pre + ".pre00000")
+    d = dict(box=box, gdim=gdim, cellsz=cellsz, number=st0["number"], type=st0["type"],
+             mass=st0["mass"], snap_steps=np.array(snaps), snap_x=np.array(x),
+             snap_p=np.array(pp), snap_f=np.array(f), epot=steps[:, 1], ekin=steps[:-1, 2],
+             nbl_count=steps[:, 3], dt=0.005, skin=0.3)
+    np.savez_compressed(os.path.join(HERE, "lj_nve1000.npz"), **d)
+    print("lj_nve1000 steps", len(steps), "rebuilds", steps[-1, 3])
+
+
 if __name__ == "__main__":
     if len(sys.argv) > 1 and sys.argv[1] == "stress":
         stress_cases()
     elif len(sys.argv) > 1 and sys.argv[1] == "ensembles":
         ensemble_cases()
+    elif len(sys.argv) > 1 and sys.argv[1] == "lj1000":
+        lj1000_case()
     else:
         main()
         stress_cases()
         ensemble_cases()
+        lj1000_case()

@@ -178,3 +178,28 @@ def test_mik_quench_matches_reference():
     d = s.x - g["x_final"]
     d -= np.round(d @ np.linalg.inv(g["box"])) @ g["box"]
     assert np.abs(d).max() < 1e-8
+
+
+def test_lj_1000_steps_segmentwise():
+    """The plain-method LJ run over all 1000 steps, step by step: from each
+    of the reference's snapshots (every 250 steps) the oracle reproduces the
+    forces of that step (1e-11 relative RMS) and the energies of the next
+    250 steps (1e-9 relative)."""
+    g = golden("lj_nve1000")
+    snaps = list(g["snap_steps"])
+    for k, st in enumerate(snaps):
+        s = OracleSystem(g["box"], g["snap_x"][k], g["type"], g["mass"], g["number"], 1,
+                         tables("lj"), False, float(g["skin"]), timestep=float(g["dt"]),
+                         p=g["snap_p"][k])
+        s.calc_forces()
+        assert rel_rms(s.f, g["snap_f"][k]) < 1e-11
+        assert abs(s.epot_total - g["epot"][st]) <= 1e-12 * abs(g["epot"][st])
+        if st == snaps[-1]:
+            continue
+        s = OracleSystem(g["box"], g["snap_x"][k], g["type"], g["mass"], g["number"], 1,
+                         tables("lj"), False, float(g["skin"]), timestep=float(g["dt"]),
+                         p=g["snap_p"][k])
+        n = snaps[k + 1] - st
+        ep, ek = s.nve(n)
+        np.testing.assert_allclose(ep, g["epot"][st:st + n], rtol=1e-9, atol=0)
+        np.testing.assert_allclose(ek, g["ekin"][st:st + n], rtol=1e-8, atol=0)
