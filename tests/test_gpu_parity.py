@@ -397,7 +397,10 @@ def test_lj_1000_steps_segmentwise():
         gg["x"] = g["snap_x"][k]
         s = gpu_system(gg, "lj", False, 1, float(g["skin"]), p=g["snap_p"][k])
         s.calc_forces(st)
-        assert rel_rms(s.get_atoms()["f"], g["snap_f"][k]) < 1e-11
+        # step 0 is the perfect lattice, whose forces are rounding noise: the
+        # bar is relative to a force scale of at least 1
+        f, gf = s.get_atoms()["f"], g["snap_f"][k]
+        assert np.sqrt(np.mean((f - gf) ** 2)) < 1e-11 * max(1.0, np.sqrt(np.mean(gf ** 2)))
         assert abs(s.scalars().tot_pot_energy - g["epot"][st]) <= 1e-12 * abs(g["epot"][st])
         if st == snaps[-1]:
             continue
