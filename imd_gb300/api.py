@@ -107,7 +107,6 @@ def lib() -> C.CDLL:
         L.imdgpu_batch_set_compaction.argtypes = [vp, C.c_int]
         L.imdgpu_autotune.argtypes = [vp, _ip, _ip]
         L.imdgpu_calc_stress.argtypes = [vp, _dp, _dp]
-        L.imdgpu_set_mixed_cells.argtypes = [vp, C.c_int]
         L.imdgpu_move_atoms_mik.argtypes = [vp, C.c_double]
         L.imdgpu_move_atoms_nvt.argtypes = [vp, C.c_double]
         L.imdgpu_set_nvt.argtypes = [vp, C.c_double, C.c_double, C.c_double, C.c_long]
@@ -381,10 +380,6 @@ class GpuSystem:
         bf = C.c_int(0)
         _check(lib().imdgpu_autotune(self.h, C.byref(bd), C.byref(bf)), "autotune")
         return bd.value, bf.value
-
-    def set_mixed_cells(self, on: bool) -> None:
-        """Mixed path: cell-pair passes (default) or list passes."""
-        _check(lib().imdgpu_set_mixed_cells(self.h, int(bool(on))), "set_mixed_cells")
 
     def set_blocks(self, density: int, force: int) -> None:
         _check(lib().imdgpu_set_blocks(self.h, int(density), int(force)), "set_blocks")

@@ -16,7 +16,6 @@ struct ForceTabs {
   int epot;      // scatter per-atom energies (POTENG) in the force pass
   int bs;        // threads per block of the force pass (autotuned, multiple of 32)
   int bs_rho;    // threads per block of the density pass (autotuned)
-  int cells;     // mixed path: cell-pair passes instead of list passes
 };
 
 // Device-side scalars of one system (results + control).

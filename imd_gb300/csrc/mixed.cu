@@ -204,187 +204,6 @@ __global__ void k_finalize_mixed(const double *pe, int ne, const double *pf, int
   }
 }
 
-// ---------------------------------------------------------------------------
-// Cell-pair form of the same two passes (single systems).  One block per
-// real cell; its 27 neighbour cells (the full shell, own cell included) are
-// staged one at a time in shared memory and every thread of the block, one
-// per atom of the cell, scans all staged atoms: all lanes read the same
-// staged atom (a shared-memory broadcast), so the per-pair gathers of the
-// list form turn into one coalesced load per staged atom.  The cells are the
-// list's cells (edge >= rc + skin, binned at the last build), so every
-// partner within rc is among the 27 as long as the list would still be
-// valid; the candidates outside rc cost a few FP32 operations each.  Pair
-// arithmetic and accumulation are those of k_density_mixed / k_force_mixed.
-// ---------------------------------------------------------------------------
-constexpr int CELL_BS = 64;   // threads per cell block (a cell of Cu holds ~37 atoms)
-constexpr int CELL_TILE = 64;  // staged atoms per tile
-
-struct CellShell {
-  int start[27], cnt[27];
-};
-
-__device__ __forceinline__ void load_shell(const SysView &v, int r, CellShell &sh) {
-  if (threadIdx.x < 27) {
-    const int c2 = v.hshell[(size_t)27 * r + threadIdx.x];
-    const int s0 = c2 >= 0 ? v.cstart[c2] : 0;
-    const int e = c2 >= 0 ? min(s0 + v.ccount[c2], v.n + v.gcap) : 0;  // ghost overflow: in bounds
-    sh.start[threadIdx.x] = s0;
-    sh.cnt[threadIdx.x] = max(e - s0, 0);
-  }
-}
-
-template <bool NT1>
-__global__ void __launch_bounds__(CELL_BS) k_density_cells(SysView v, DevTable rho,
-                                                           const SplitPos *sp) {
-  __shared__ CellShell sh;
-  __shared__ SplitPos tile[CELL_TILE];
-  __shared__ int tj[CELL_TILE];
-  const int r = blockIdx.x;
-  const int lin = v.rank_lin[r];
-  const int c0 = v.cstart[lin], nc = v.ccount[lin];
-  load_shell(v, r, sh);
-  __syncthreads();
-  for (int ib = 0; ib < nc; ib += CELL_BS) {
-    const int ti = ib + threadIdx.x;
-    const bool act = ti < nc;
-    const int i = c0 + ti;
-    SplitPos a;
-    if (act) a = sp[i];
-    const int it = (NT1 || !act) ? 0 : __float_as_int(a.hi.w), nt = v.ntypes;
-    Acc racc;
-    bool shortf = false;
-    for (int m = 0; m < 27; m++) {
-      const int cnt = sh.cnt[m], s0 = sh.start[m];
-      for (int tb = 0; tb < cnt; tb += CELL_TILE) {
-        const int nt_ = min(CELL_TILE, cnt - tb);
-        __syncthreads();
-        for (int t = threadIdx.x; t < nt_; t += CELL_BS) {
-          tile[t] = ldsp(&sp[s0 + tb + t]);
-          tj[t] = s0 + tb + t;
-        }
-        __syncthreads();
-        if (act) {
-          for (int t = 0; t < nt_; t++) {
-            if (tj[t] == i) continue;
-            const SplitPos b = tile[t];
-            const float dx = (b.hi.x - a.hi.x) + (b.lo.x - a.lo.x);
-            const float dy = (b.hi.y - a.hi.y) + (b.lo.y - a.lo.y);
-            const float dz = (b.hi.z - a.hi.z) + (b.lo.z - a.lo.z);
-            const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-            const int col = NT1 ? 0 : it * nt + __float_as_int(b.hi.w);
-            if (r2 < rho.fend[col]) {
-              float chi;
-              const int kk = tab_index_f(rho, col, r2, chi);
-              racc.add(polyf_v(rho, col, kk, chi));
-              shortf |= r2 < rho.fbegin[col];
-            }
-          }
-        }
-      }
-    }
-    if (act) {
-      v.rho[i] = racc.value();
-      if (shortf) flag_short(v, i);
-    }
-  }
-}
-
-template <bool NT1, bool EAM>
-__global__ void __launch_bounds__(CELL_BS) k_force_cells(SysView v, DevTable pair, DevTable rho,
-                                                         const SplitPos *sp, const float *dff,
-                                                         double *partial) {
-  __shared__ CellShell sh;
-  __shared__ SplitPos tile[CELL_TILE];
-  __shared__ float tdf[CELL_TILE];
-  __shared__ int tj[CELL_TILE];
-  const int r = blockIdx.x;
-  const int lin = v.rank_lin[r];
-  const int c0 = v.cstart[lin], nc = v.ccount[lin];
-  load_shell(v, r, sh);
-  __syncthreads();
-  double acc[2] = {0.0, 0.0};
-  for (int ib = 0; ib < nc; ib += CELL_BS) {
-    const int ti = ib + threadIdx.x;
-    const bool act = ti < nc;
-    const int i = c0 + ti;
-    SplitPos a;
-    if (act) a = sp[i];
-    const int it = (NT1 || !act) ? 0 : __float_as_int(a.hi.w), nt = v.ntypes;
-    const float dfi = (EAM && act) ? dff[i] : 0.f;
-    Acc fx, fy, fz, ee, vir;
-    bool shortf = false;
-    for (int m = 0; m < 27; m++) {
-      const int cnt = sh.cnt[m], s0 = sh.start[m];
-      for (int tb = 0; tb < cnt; tb += CELL_TILE) {
-        const int nt_ = min(CELL_TILE, cnt - tb);
-        __syncthreads();
-        for (int t = threadIdx.x; t < nt_; t += CELL_BS) {
-          tile[t] = ldsp(&sp[s0 + tb + t]);
-          tj[t] = s0 + tb + t;
-          if (EAM) tdf[t] = __ldg(&dff[s0 + tb + t]);
-        }
-        __syncthreads();
-        if (act) {
-          for (int t = 0; t < nt_; t++) {
-            if (tj[t] == i) continue;
-            const SplitPos b = tile[t];
-            const float dx = (b.hi.x - a.hi.x) + (b.lo.x - a.lo.x);
-            const float dy = (b.hi.y - a.hi.y) + (b.lo.y - a.lo.y);
-            const float dz = (b.hi.z - a.hi.z) + (b.lo.z - a.lo.z);
-            const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-            const int jt = NT1 ? 0 : __float_as_int(b.hi.w);
-            const int col = NT1 ? 0 : it * nt + jt;
-            float grad = 0.f;
-            bool have = false;
-            if (r2 <= pair.fend[col]) {
-              float chi;
-              const int kk = tab_index_f(pair, col, r2, chi);
-              ee.add(0.5f * polyf_v(pair, col, kk, chi));
-              grad = polyf_g(pair, col, kk, chi);
-              shortf |= r2 < pair.fbegin[col];
-              have = true;
-            }
-            if (EAM) {
-              const int col1 = NT1 ? 0 : jt * nt + it, col2 = col;
-              if (r2 < rho.fend[col1] || r2 < rho.fend[col2]) {
-                float chi;
-                const int kk = tab_index_f(rho, col1, r2, chi);
-                const float ris = polyf_g(rho, col1, kk, chi);
-                float rjs = ris;
-                if (!NT1 && col1 != col2) {
-                  const int k2 = tab_index_f(rho, col2, r2, chi);
-                  rjs = polyf_g(rho, col2, k2, chi);
-                }
-                grad += 0.5f * (dfi * rjs + tdf[t] * ris);
-                have = true;
-              }
-            }
-            if (have) {
-              fx.add(dx * grad);
-              fy.add(dy * grad);
-              fz.add(dz * grad);
-              vir.add(-0.5f * r2 * grad);
-            }
-          }
-        }
-      }
-    }
-    if (act) {
-      const double e = ee.value();
-      double4 f = v.frc[i];  // .w holds the embedding energy
-      f.x = fx.value();
-      f.y = fy.value();
-      f.z = fz.value();
-      f.w += e;
-      v.frc[i] = f;
-      acc[0] += e;
-      acc[1] += vir.value();
-      if (shortf) flag_short(v, i);
-    }
-  }
-  block_sum_store<2, CELL_BS>(acc, partial);
-}
-
 static inline int nblk(long n, int bs) { return (int)((n + bs - 1) / bs); }
 
 int launch_forces_mixed(const SysView &v, const ForceTabs &t, DevScalars *sc, float *dff,
@@ -395,32 +214,18 @@ int launch_forces_mixed(const SysView &v, const ForceTabs &t, DevScalars *sc, fl
   cudaMemsetAsync(v.frc, 0, (size_t)v.ncap * sizeof(double4), st);
   k_ghost_pos_launch(v, gblocks, st);
   k_split<<<nblk(ext, BS_VEC), BS_VEC, 0, st>>>(v, sp);
-  const int nbe = nblk(v.n, BS_VEC), nbr = nblk(v.n, t.bs_rho);
-  // the cell-pair form for single systems whose per-block partials fit the
-  // partial buffer (two per cell after the embedding's); the list form
-  // otherwise (batches, where finished cells must be skipped atom by atom)
-  const long pcap = 8L * nblk(v.n, 64) + 64;
-  const bool cells = t.cells && v.atom_sys == nullptr && v.nshell == 27 &&
-                     nbe + 2L * v.nreal_cells <= pcap;
-  const int nbf = cells ? v.nreal_cells : nblk(v.n, t.bs);
+  const int nbf = nblk(v.n, t.bs), nbe = nblk(v.n, BS_VEC), nbr = nblk(v.n, t.bs_rho);
   double *pe = v.partial, *pf = v.partial + nbe;
   int launches = 4;
   if (t.eam) {
     if (ev) cudaEventRecord(ev[0], st);
-    if (cells && t.nt1) k_density_cells<true><<<v.nreal_cells, CELL_BS, 0, st>>>(v, t.rho, sp);
-    else if (cells) k_density_cells<false><<<v.nreal_cells, CELL_BS, 0, st>>>(v, t.rho, sp);
-    else if (t.nt1) k_density_mixed<true><<<nbr, t.bs_rho, 0, st>>>(v, t.rho, sp);
+    if (t.nt1) k_density_mixed<true><<<nbr, t.bs_rho, 0, st>>>(v, t.rho, sp);
     else k_density_mixed<false><<<nbr, t.bs_rho, 0, st>>>(v, t.rho, sp);
     if (ev) cudaEventRecord(ev[1], st);
     k_embed_mixed<<<nbe, BS_VEC, 0, st>>>(v, t.embed, dff, pe);
     k_ghost_dff<<<gblocks, BS_VEC, 0, st>>>(v, dff);
     if (ev) cudaEventRecord(ev[2], st);
-    if (cells && t.nt1)
-      k_force_cells<true, true><<<nbf, CELL_BS, 0, st>>>(v, t.pair, t.rho, sp, dff, pf);
-    else if (cells)
-      k_force_cells<false, true><<<nbf, CELL_BS, 0, st>>>(v, t.pair, t.rho, sp, dff, pf);
-    else if (t.nt1)
-      k_force_mixed<true, true><<<nbf, t.bs, 0, st>>>(v, t.pair, t.rho, sp, dff, 0, pf);
+    if (t.nt1) k_force_mixed<true, true><<<nbf, t.bs, 0, st>>>(v, t.pair, t.rho, sp, dff, 0, pf);
     else k_force_mixed<false, true><<<nbf, t.bs, 0, st>>>(v, t.pair, t.rho, sp, dff, 0, pf);
     if (ev) cudaEventRecord(ev[3], st);
     launches += 4;
@@ -430,12 +235,7 @@ int launch_forces_mixed(const SysView &v, const ForceTabs &t, DevScalars *sc, fl
       cudaEventRecord(ev[1], st);
       cudaEventRecord(ev[2], st);
     }
-    if (cells && t.nt1)
-      k_force_cells<true, false><<<nbf, CELL_BS, 0, st>>>(v, t.pair, t.rho, sp, dff, pf);
-    else if (cells)
-      k_force_cells<false, false><<<nbf, CELL_BS, 0, st>>>(v, t.pair, t.rho, sp, dff, pf);
-    else if (t.nt1)
-      k_force_mixed<true, false><<<nbf, t.bs, 0, st>>>(v, t.pair, t.rho, sp, dff, 0, pf);
+    if (t.nt1) k_force_mixed<true, false><<<nbf, t.bs, 0, st>>>(v, t.pair, t.rho, sp, dff, 0, pf);
     else k_force_mixed<false, false><<<nbf, t.bs, 0, st>>>(v, t.pair, t.rho, sp, dff, 0, pf);
     if (ev) cudaEventRecord(ev[3], st);
     launches += 1;

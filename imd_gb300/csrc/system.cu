@@ -160,7 +160,6 @@ struct imdgpu_sys {
   // block shape of the pair passes; autotuned (imdgpu_autotune) per
   // (atoms, cells, precision), which tuned_key records
   int bs_force = BS_FORCE, bs_rho = BS_FORCE;
-  int mixed_cells = 1;             // mixed path: cell-pair passes (1) or list passes (0)
   std::vector<long> tuned_key;
   int autotune_batches = 1;        // imdgpu_batch_begin tunes the batch first
   long batch_nbl0 = 0;
@@ -1060,7 +1059,6 @@ static ForceTabs ftabs(imdgpu_sys *s) {
   t.epot = 1;
   t.bs = s->bs_force;
   t.bs_rho = s->bs_rho;
-  t.cells = s->mixed_cells;
   int same = s->have_tab[0] && s->have_tab[1];
   if (same) {
     const HostTable &a = s->htab[0], &b = s->htab[1];
@@ -3037,13 +3035,6 @@ int imdgpu_autotune(imdgpu_sys *s, int *block_density, int *block_force) {
   if ((rc = autotune_forces(s, 1))) return rc;
   if (block_density) *block_density = s->bs_rho;
   if (block_force) *block_force = s->bs_force;
-  return IMDGPU_OK;
-}
-
-// mixed path: the cell-pair passes (default) or the list passes
-int imdgpu_set_mixed_cells(imdgpu_sys *s, int on) {
-  if (!s) return fail(IMDGPU_ERR_ARG, "null system");
-  s->mixed_cells = on ? 1 : 0;
   return IMDGPU_OK;
 }
 

@@ -263,12 +263,6 @@ int imdgpu_get_pairs(imdgpu_sys *sys, long cap, int *ni, int *nj, int *shift,
 int imdgpu_autotune(imdgpu_sys *sys, int *block_density, int *block_force);
 int imdgpu_set_blocks(imdgpu_sys *sys, int block_density, int block_force);
 int imdgpu_batch_set_autotune(imdgpu_sys *sys, int on);
-/* IMDGPU_MIXED on a single system evaluates its two passes cell by cell:
- * each block stages the 27 neighbour cells of one cell in shared memory and
- * scans them, with the list's cells (edge >= rc + skin, valid while the
- * list is), instead of gathering list partners one by one.  on = 0 selects
- * the list passes (the form batches use).  Same pair arithmetic. */
-int imdgpu_set_mixed_cells(imdgpu_sys *sys, int on);
 
 /* Timing of the dominant kernels of the last nve_run (device ms, CUDA
  * events on the system's stream). */

@@ -420,26 +420,3 @@ def test_lj_1000_steps_segmentwise():
     np.testing.assert_allclose(ep[:250], g["epot"][:250], rtol=1e-9, atol=0)
     assert abs((etot[-1] - etot[0]) - (eref[-1] - eref[0])) / n < 1e-3
     assert (etot.max() - etot.min()) <= 2.0 * (eref.max() - eref.min())
-
-
-@pytest.mark.parametrize("name,tab,nt", [("cu_pert", "cu", 1), ("alloy_pert", "cuni", 2),
-                                         ("lj_pert", "lj", 1)])
-def test_mixed_cell_pairs_equal_list_form(name, tab, nt):
-    """The mixed path's cell-pair passes (shared-memory staging of the 27
-    neighbour cells) and its list passes give the same forces and energies up
-    to FP32 summation order, and both stay within the mixed bar of the
-    reference."""
-    from imd_gb300 import api
-    g = golden(name)
-    eam = tab != "lj"
-    out = {}
-    for cells in (True, False):
-        s = gpu_system(g, tab, eam, nt, 0.4 if eam else 0.3, precision=api.MIXED)
-        s.set_mixed_cells(cells)
-        s.calc_forces(0)
-        out[cells] = (s.get_atoms()["f"], s.scalars().tot_pot_energy, s.scalars().virial)
-    (fc, ec, vc), (fl, el, vl) = out[True], out[False]
-    assert rel_rms(fc, fl) < 1e-6
-    assert abs(ec - el) <= 1e-7 * abs(el)
-    assert abs(vc - vl) <= 1e-6 * abs(vl)
-    assert rel_rms(fc, g["f"]) < 1e-5
