@@ -14,8 +14,9 @@ Prints one JSON line.  `value` is device-timed atom-steps/s with the state
 resident in HBM (CUDA events around every step, an L2-sized scratch write
 between steps outside the timed windows); `e2e` is the same metric through
 the C-ABI with host buffers: every step uploads positions and momenta from
-pinned host memory, runs calc_forces / move_atoms_nve / check_nblist and
-reads positions, momenta, forces and energies back.
+pinned host memory, runs calc_forces / move_atoms_nve / check_nblist (the
+calls IMD's main_loop makes) and reads the new positions and momenta and the
+step's energies back.
 
 The same line carries the FP32-force / FP64-accumulate run of the same
 workload (`mixed`, with its force error against FP64 at the same positions)
@@ -318,12 +319,18 @@ def run_ours(args, rank, world, local):
     except Exception:
         xh, ph, fh, eh = (np.empty((n, 3)), np.empty((n, 3)), np.empty((n, 3)), np.empty(n))
     s.get_state(xh, ph, fh, eh)
+    # one step through the C-ABI with host buffers: the state (positions,
+    # momenta) up, calc_forces / move_atoms_nve / check_nblist, the new state
+    # down and the step's energies (tot_pot_energy, tot_kin_energy) read
+    e_host = []
     for _ in range(3 if e2e_steps else 0):   # warm-up of the host path
         s.put_state(xh, ph)
         s.calc_forces(0)
         s.move_atoms_nve(dt)
         s.check_nblist()
-        s.get_state(xh, ph, fh, eh)
+        s.get_state(xh, ph)
+        sc = s.scalars()
+        e_host.append(sc.tot_pot_energy + sc.tot_kin_energy)
     barrier()
     t0 = time.perf_counter()
     for k in range(e2e_steps):
@@ -331,7 +338,9 @@ def run_ours(args, rank, world, local):
         s.calc_forces(k)
         s.move_atoms_nve(dt)
         s.check_nblist()
-        s.get_state(xh, ph, fh, eh)
+        s.get_state(xh, ph)
+        sc = s.scalars()
+        e_host.append(sc.tot_pot_energy + sc.tot_kin_energy)
     t_e2e = time.perf_counter() - t0
     barrier()
     e2e = n * e2e_steps * world / t_e2e if e2e_steps else None
@@ -379,7 +388,9 @@ def run_ours(args, rank, world, local):
                    "autotuned_blocks": {"density": r["blocks"][0], "force": r["blocks"][1]}},
         "clocks": r["clocks"],
         "e2e": {"value": e2e, "unit": "atom-steps/s", "h2d_bytes_per_step": 48 * n,
-                "d2h_bytes_per_step": 80 * n, "steps": e2e_steps},
+                "d2h_bytes_per_step": 48 * n + 16, "steps": e2e_steps,
+                "per_step": "x, p up; calc_forces, move_atoms_nve, check_nblist; x, p and "
+                            "the energies down"},
         "gpu_launches": int(r["launches"]),
         "roofline": {"bound": "fp64", "kernel": "k_force_fast (EAM2 force pass, half list)",
                      "achieved": force_tflops, "peak": fp64_peak, "unit": "TFLOP/s",
