@@ -1529,18 +1529,27 @@ static int forces_async(imdgpu_sys *s) {
 }
 
 // calc_forces with a synchronous list check
+// The list check needs no round trip: the rebuild kernels run on the device
+// only when check_nblist, the integrator or set_atoms flagged the list, and
+// an overflow of the list or ghost buffers shows in the status word read
+// with the results.  Then the buffers grow in a synchronous rebuild and the
+// forces are computed again (the atoms have not moved).
 static int calc_forces_sync(imdgpu_sys *s) {
   int rc = prepare(s);
   if (rc) return rc;
-  CK(cudaMemcpyAsync(s->hsc, s->dsc, sizeof(DevScalars), cudaMemcpyDeviceToHost, s->st));
-  CK(cudaStreamSynchronize(s->st));
-  if (s->hsc->rebuild) {
-    rc = rebuild_sync(s);
-    if (rc) return rc;
+  CK(cudaMemsetAsync(s->status, 0, sizeof(unsigned), s->st));
+  if ((rc = issue_rebuild(s))) return rc;
+  if ((rc = forces_async(s))) return rc;
+  if ((rc = read_back(s))) return rc;
+  if (s->status_host & ST_CELLOVER)
+    return fail(IMDGPU_ERR_CELL, "more than " + std::to_string(CELLCAP) + " atoms in one cell");
+  if (s->status_host & (ST_NBOVER | ST_GHOSTOVER)) {
+    if ((rc = rebuild_sync(s))) return rc;
+    launch_forces(view(s), ftabs(s), s->dsc, s->precision == IMDGPU_MIXED, s->st);
+    CK(cudaGetLastError());
+    return read_back(s);
   }
-  rc = forces_async(s);
-  if (rc) return rc;
-  return read_back(s);
+  return IMDGPU_OK;
 }
 
 // Autotuner of the pair passes' block shape: with the current list, each
