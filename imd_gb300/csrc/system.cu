@@ -122,6 +122,7 @@ struct imdgpu_sys {
   double *partial = nullptr;
   DevScalars *dsc = nullptr;
   DevScalars *hsc = nullptr;  // pinned mirror
+  bool hsc_valid = false;     // hsc matches the device since the last read_back
   long *dnbl = nullptr;       // device rebuild counter
   double *hist = nullptr;     // per-step (epot, ekin) of nve_run
   int hist_cap = 0;
@@ -1457,11 +1458,10 @@ static int issue_rebuild(imdgpu_sys *s) {
 
 static int read_back(imdgpu_sys *s) {
   CK(cudaMemcpyAsync(s->hsc, s->dsc, sizeof(DevScalars), cudaMemcpyDeviceToHost, s->st));
-  unsigned stt = 0;
   CK(cudaMemcpyAsync(&s->status_host, s->status, sizeof(unsigned), cudaMemcpyDeviceToHost, s->st));
   CK(cudaMemcpyAsync(&s->nbl_count_host, s->dnbl, sizeof(long), cudaMemcpyDeviceToHost, s->st));
   CK(cudaStreamSynchronize(s->st));
-  (void)stt;
+  s->hsc_valid = true;
   return IMDGPU_OK;
 }
 
@@ -1471,6 +1471,7 @@ static int rebuild_sync(imdgpu_sys *s) {
   for (int attempt = 0; attempt < 6; attempt++) {
     int one = 1;
     CK(cudaMemcpyAsync(&s->dsc->rebuild, &one, sizeof(int), cudaMemcpyHostToDevice, s->st));
+  s->hsc_valid = false;
     CK(cudaMemsetAsync(s->status, 0, sizeof(unsigned), s->st));
     int rc = issue_rebuild(s);
     if (rc) return rc;
@@ -1517,6 +1518,7 @@ static int prepare(imdgpu_sys *s) {
     if (rc) return rc;
     int one = 1;
     CK(cudaMemcpy(&s->dsc->rebuild, &one, sizeof(int), cudaMemcpyHostToDevice));
+  s->hsc_valid = false;
   }
   return IMDGPU_OK;
 }
@@ -1538,7 +1540,10 @@ static int calc_forces_sync(imdgpu_sys *s) {
   int rc = prepare(s);
   if (rc) return rc;
   CK(cudaMemsetAsync(s->status, 0, sizeof(unsigned), s->st));
-  if ((rc = issue_rebuild(s))) return rc;
+  // a host mirror read since the flag last changed says whether a rebuild
+  // can be due; the guarded kernels are then not even launched
+  if (!(s->hsc_valid && !s->hsc->rebuild))
+    if ((rc = issue_rebuild(s))) return rc;
   if ((rc = forces_async(s))) return rc;
   if ((rc = read_back(s))) return rc;
   if (s->status_host & ST_CELLOVER)
@@ -1712,6 +1717,7 @@ int imdgpu_set_precision(imdgpu_sys *s, int precision) {
       s->geom_ready = false;
       int one = 1;
       CK(cudaMemcpy(&s->dsc->rebuild, &one, sizeof(int), cudaMemcpyHostToDevice));
+  s->hsc_valid = false;
     }
   }
   return IMDGPU_OK;
@@ -1971,6 +1977,7 @@ int imdgpu_set_atoms(imdgpu_sys *s, int n, const int *number, const int *type,
   s->atoms_set = true;
   int one = 1;
   CK(cudaMemcpy(&s->dsc->rebuild, &one, sizeof(int), cudaMemcpyHostToDevice));
+  s->hsc_valid = false;
   return IMDGPU_OK;
 }
 
@@ -2102,6 +2109,7 @@ int imdgpu_deallocate_nblist(imdgpu_sys *s) {
   if (!s) return fail(IMDGPU_ERR_ARG, "null system");
   int one = 1;
   CK(cudaMemcpy(&s->dsc->rebuild, &one, sizeof(int), cudaMemcpyHostToDevice));
+  s->hsc_valid = false;
   return IMDGPU_OK;
 }
 
@@ -2209,6 +2217,7 @@ static int issue_nve_steps(imdgpu_sys *s, int k, double dt, int *istep, long &la
     if (e) cudaEventRecord(e[6], s->st);
     k_nve<<<nb, BS_VEC, 0, s->st>>>(v, dt, s->partial);
     k_finalize_nve<<<1, 32, 0, s->st>>>(s->partial, nb, s->dsc, v.skin2, s->hist, istep);
+    s->hsc_valid = false;
     launches += 2;
     if (e) cudaEventRecord(e[7], s->st);
     if (s->l2flush_bytes > 0)
@@ -2269,6 +2278,7 @@ static int run_chunk_graph(imdgpu_sys *s, int k, double dt, int *istep, long &la
     s->graph_launches = l;
   }
   CK(cudaGraphLaunch(s->gexec, s->st));
+  s->hsc_valid = false;
   launches += s->graph_launches;
   return IMDGPU_OK;
 }
@@ -2850,6 +2860,7 @@ static int batch_repack(imdgpu_sys *s, const std::vector<char> &keep) {
   CK(cudaMemcpy(s->d_ndone, &nd, sizeof(int), cudaMemcpyHostToDevice));
   int one = 1;
   CK(cudaMemcpy(&s->dsc->rebuild, &one, sizeof(int), cudaMemcpyHostToDevice));
+  s->hsc_valid = false;
   if ((rc = rebuild_sync(s))) return rc;
   {
     int cnt[4];
@@ -2962,6 +2973,7 @@ static void issue_batch_round(imdgpu_sys *s, const CgParams &P) {
   SysView v = view(s);
   ForceTabs ft = ftabs(s);
   ft.epot = 0;
+  s->hsc_valid = false;
   launch_batch_round_pre(v, s->d_cs, s->nsys, P, s->d_sys_done, s->d_sys_short, s->oldx,
                          s->cgg, s->cgh, s->d_maxd, s->d_ndone, s->dsc, v.skin2, s->st);
   issue_rebuild(s);
@@ -2995,6 +3007,7 @@ int imdgpu_batch_begin(imdgpu_sys *s, double fmax, int maxsteps) {
   // first list: synchronous, sizes the buffers (with head-room for relaxation)
   int one = 1;
   CK(cudaMemcpy(&s->dsc->rebuild, &one, sizeof(int), cudaMemcpyHostToDevice));
+  s->hsc_valid = false;
   rc = rebuild_sync(s);
   if (rc) return rc;
   {
@@ -3144,6 +3157,7 @@ int imdgpu_batch_advance(imdgpu_sys *s, int max_rounds, int *ndone_out, int *rou
         B.gkey = key;
       }
       CKR(cudaGraphLaunch(B.gx, s->st));
+      s->hsc_valid = false;
     } else {
       for (int r = 0; r < R; r++) issue_batch_round(s, P);
       CKR(cudaGetLastError());
@@ -3514,6 +3528,7 @@ int imdgpu_batch_ml_start(imdgpu_sys *s, int *used, double *e_start, double *e_p
   CK(cudaMemsetAsync(s->d_sys_short, 0, sizeof(int) * ns, s->st));
   int one = 1;
   CK(cudaMemcpyAsync(&s->dsc->rebuild, &one, sizeof(int), cudaMemcpyHostToDevice, s->st));
+  s->hsc_valid = false;
   if ((rc = calc_forces_sync(s))) return rc;
   v = view(s);
   k_cell_energy<<<ns, 256, 0, s->st>>>(s->frc, s->d_aoff, s->ml_ecell + 1, 2);
@@ -3522,6 +3537,7 @@ int imdgpu_batch_ml_start(imdgpu_sys *s, int *used, double *e_start, double *e_p
   k_restore_by_orig<<<nblk(s->n, 256), 256, 0, s->st>>>(v, s->ml_save, s->ml_sel);
   CK(cudaGetLastError());
   CK(cudaMemcpyAsync(&s->dsc->rebuild, &one, sizeof(int), cudaMemcpyHostToDevice, s->st));
+  s->hsc_valid = false;
   std::vector<double> ec(2 * (size_t)ns);
   std::vector<int> sel(ns);
   CK(cudaMemcpyAsync(ec.data(), s->ml_ecell, sizeof(double) * 2 * ns, cudaMemcpyDeviceToHost, s->st));
