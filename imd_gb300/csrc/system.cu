@@ -123,6 +123,10 @@ struct imdgpu_sys {
   DevScalars *dsc = nullptr;
   DevScalars *hsc = nullptr;  // pinned mirror
   bool hsc_valid = false;     // hsc matches the device since the last read_back
+  // list statistics of imdgpu_get_scalars, recounted after each build
+  long list_stats_build = -1, list_stats_entries = 0;
+  int list_stats_n = -1, list_stats_cap = -1;
+  int list_stats_cnt[4] = {0, 0, 0, 0};
   long *dnbl = nullptr;       // device rebuild counter
   double *hist = nullptr;     // per-step (epot, ekin) of nve_run
   int hist_cap = 0;
@@ -2016,8 +2020,11 @@ int imdgpu_get_scalars(imdgpu_sys *s, imdgpu_scalars *o) {
   if (!s || !o) return fail(IMDGPU_ERR_ARG, "null");
   int rc = read_back(s);
   if (rc) return rc;
-  int cnt[4] = {0, 0, 0, 0};
-  CK(cudaMemcpy(cnt, s->counters, sizeof cnt, cudaMemcpyDeviceToHost));
+  // the list statistics change only with a build: recounted once per build
+  const bool fresh = s->list_stats_build == s->nbl_count_host && s->list_stats_n == s->n &&
+                     s->list_stats_cap == s->nbcap;
+  int *cnt = s->list_stats_cnt;
+  if (!fresh) CK(cudaMemcpy(cnt, s->counters, 4 * sizeof(int), cudaMemcpyDeviceToHost));
   memset(o, 0, sizeof *o);
   o->tot_pot_energy = s->hsc->epot;
   o->virial = s->hsc->virial;
@@ -2032,13 +2039,19 @@ int imdgpu_get_scalars(imdgpu_sys *s, imdgpu_scalars *o) {
   o->nghost = cnt[0];
   o->max_cell_atoms = cnt[2];
   o->short_distance = (s->status_host & ST_SHORT) ? 1 : 0;
-  long total = 0;
-  if (s->atoms_set && s->nbcap > 0) {
-    std::vector<int> nn(s->n);
-    CK(cudaMemcpy(nn.data(), s->nnb, sizeof(int) * s->n, cudaMemcpyDeviceToHost));
-    for (int v : nn) total += v;
+  if (!fresh) {
+    long total = 0;
+    if (s->atoms_set && s->nbcap > 0) {
+      std::vector<int> nn(s->n);
+      CK(cudaMemcpy(nn.data(), s->nnb, sizeof(int) * s->n, cudaMemcpyDeviceToHost));
+      for (int v : nn) total += v;
+    }
+    s->list_stats_entries = total;
+    s->list_stats_build = s->nbl_count_host;
+    s->list_stats_n = s->n;
+    s->list_stats_cap = s->nbcap;
   }
-  o->nb_entries = total;
+  o->nb_entries = s->list_stats_entries;
   return IMDGPU_OK;
 }
 
