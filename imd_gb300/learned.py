@@ -68,10 +68,10 @@ def min_image(d: np.ndarray, box: np.ndarray) -> np.ndarray:
 
 
 def make_batch(tables, cells, precision=api.FP64,
-               interpolation: int = BATCH_INTERPOLATION) -> api.GpuBatch:
+               interpolation: int = BATCH_INTERPOLATION, nbl_margin: float = 0.4) -> api.GpuBatch:
     b = api.GpuBatch(1, api.EAM2, precision, interpolation)
     b.read_tables(tables)
-    b.set_cells(cells)
+    b.set_cells(cells, nbl_margin)
     return b
 
 
@@ -96,12 +96,12 @@ class RelaxResult:
 
 def relax(tables, cells, fmax: float = 1e-4, weights=None, precision=api.FP64,
           keep_positions: bool = False, chunk_rounds: int = 4096,
-          interpolation: int = BATCH_INTERPOLATION) -> RelaxResult:
+          interpolation: int = BATCH_INTERPOLATION, nbl_margin: float = 0.4) -> RelaxResult:
     """Relax every cell with the batched CG, from the learned start when
     `weights` are given.  The wall time covers the learned start (its two
     force calls and the prediction) and the CG, not the upload of the cells.
     Force calls per cell include the learned start's two."""
-    b = make_batch(tables, cells, precision, interpolation)
+    b = make_batch(tables, cells, precision, interpolation, nbl_margin)
     used = e0 = e1 = None
     api.lib()
     b.calc_forces(0)  # first list and geometry outside the timed region
