@@ -1,0 +1,68 @@
+"""The C-ABI from C: tests/c_driver.c includes include/imdgpu.h and links
+libimdgpu.so the way IMD's shim would.  CPU: it compiles and links (every
+symbol it uses resolves).  GPU: it runs, and its energies and forces are
+the oracle's for the same crystal."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, tables
+
+SRC = os.path.join(ROOT, "tests", "c_driver.c")
+
+
+def _build(tmp_path):
+    from imd_gb300 import api
+    api.lib()
+    libdir = os.path.dirname(api.LIBPATH)
+    exe = str(tmp_path / "c_driver")
+    cmd = ["gcc", "-std=c11", "-O2", "-Wall", "-I", os.path.join(ROOT, "include"), SRC,
+           "-o", exe, "-L", libdir, "-limdgpu", "-Wl,-rpath," + libdir]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    return exe
+
+
+def test_c_driver_compiles_and_links(tmp_path):
+    exe = _build(tmp_path)
+    assert os.path.exists(exe)
+
+
+def _crystal(nc):
+    a0 = 3.615
+    basis = np.array([[0, 0, 0], [0.5, 0.5, 0], [0.5, 0, 0.5], [0, 0.5, 0.5]])
+    x = []
+    k = 0
+    for i in range(nc):
+        for j in range(nc):
+            for l in range(nc):
+                for b in range(4):
+                    x.append([(i + basis[b, 0] + 0.25) * a0 + 0.03 * ((k * 7) % 11 - 5) / 5.0,
+                              (j + basis[b, 1] + 0.25) * a0 + 0.03 * ((k * 5) % 13 - 6) / 6.0,
+                              (l + basis[b, 2] + 0.25) * a0 + 0.03 * ((k * 3) % 7 - 3) / 3.0])
+                    k += 1
+    return np.array(x), np.diag([nc * a0] * 3)
+
+
+@pytest.mark.gpu
+def test_c_driver_matches_oracle(tmp_path):
+    from oracle import OracleSystem
+    exe = _build(tmp_path)
+    nc, steps = 6, 20
+    r = subprocess.run([exe, *tables("cu"), str(nc), str(steps)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    v = [float(t) for t in r.stdout.split()]
+    x, box = _crystal(nc)
+    n = len(x)
+    o = OracleSystem(box, x, np.zeros(n, np.int32), np.full(n, 63.546),
+                     np.arange(n, dtype=np.int32), 1, tables("cu"), True, 0.4,
+                     timestep=0.0982266, p=np.zeros((n, 3)))
+    o.calc_forces()
+    assert abs(v[0] - o.epot_total) <= 1e-12 * abs(o.epot_total)
+    assert abs(v[1] - o.virial) <= 1e-12 * abs(o.virial)
+    np.testing.assert_allclose(v[2:5], o.f[0], rtol=1e-10, atol=1e-13)
+    ep, ek = o.nve(steps)
+    assert abs(v[5] - ep[-1]) <= 1e-9 * abs(ep[-1])
+    assert abs(v[6] - ek[-1]) <= 1e-8 * abs(ek[-1])
