@@ -61,7 +61,9 @@ def test_c_driver_matches_oracle(tmp_path):
                      timestep=0.0982266, p=np.zeros((n, 3)))
     o.calc_forces()
     assert abs(v[0] - o.epot_total) <= 1e-12 * abs(o.epot_total)
-    assert abs(v[1] - o.virial) <= 1e-12 * abs(o.virial)
+    # the virial of this nearly relaxed crystal is a small difference of
+    # pair terms of order 1 eV: its bar scales with the atom count
+    assert abs(v[1] - o.virial) <= 1e-12 * max(abs(o.virial), n)
     np.testing.assert_allclose(v[2:5], o.f[0], rtol=1e-10, atol=1e-13)
     ep, ek = o.nve(steps)
     assert abs(v[5] - ep[-1]) <= 1e-9 * abs(ep[-1])
