@@ -194,6 +194,39 @@ def run_reference(args, rank, world):
     print(json.dumps(line))
 
 
+def _cg_cpu_worker(tabs, box, x, mass):
+    """IMD's CG (the C restatement, spline tables) on one cell to max |F| <= 1e-4."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    from oracle import OracleSystem
+    oracle.set_interpolation(oracle.SPLINE)
+    n = len(x)
+    o = OracleSystem(box, x, np.zeros(n, np.int32), mass, np.arange(n, dtype=np.int32), 1,
+                     tabs, True, 0.4)
+    t = time.perf_counter()
+    # bounded: a start that IMD's CG cannot leave (a pair inside the tables'
+    # first point) would otherwise run for its 100000 steps
+    steps, fm = o.cg_relax(1e-4, 3000)
+    return n, int(o.nfc), time.perf_counter() - t, steps >= 0 and fm <= 1e-4
+
+
+def cg_cpu_sample(tabs, cells, count: int):
+    """The reference's CG algorithm on the host cores: the `count` smallest
+    cells of the batch, one process per cell (spawned), relaxed in parallel.
+    Returns (relaxations/s of the sample, atom-force-calls/s per core, cores)."""
+    import multiprocessing as mp
+    order = np.argsort([c.n for c in cells], kind="stable")[:count]
+    jobs = [(tabs, cells[i].box, cells[i].x, cells[i].mass) for i in order]
+    cores = min(count, os.cpu_count() or 1)
+    ctx = mp.get_context("spawn")
+    t0 = time.perf_counter()
+    with ctx.Pool(cores) as pool:
+        res = pool.starmap(_cg_cpu_worker, jobs)
+    wall = time.perf_counter() - t0
+    per_core = float(np.mean([n * nfc / t for n, nfc, t, _ in res]))
+    return len(res) / wall, per_core, cores, res
+
+
 def run_batch(args, tabs, rank=0, world=1, dist=None):
     """Defect CG relaxations/s, plain and from the learned start: the held-out
     cells of the learned-start workload (seed 6), each relaxed by IMD's CG
@@ -238,6 +271,26 @@ def run_batch(args, tabs, rank=0, world=1, dist=None):
     both = (gp["status"] == 0) & (gl["status"] == 0)
     de = np.abs(gl["epot"] - gp["epot"])[both] / natoms[both]
     out["speedup_learned_vs_plain"] = out["learned"]["value"] / out["plain"]["value"]
+    if not args.no_cpu:
+        try:
+            rate, per_core, cores, res = cg_cpu_sample(tabs, cells, 16)
+            # the whole workload on the same cores at the sample's per-core
+            # rate, with the force calls the device's plain run needed
+            work = float((gp["nfc"].astype(np.float64) * natoms).sum())
+            out["cpu_baseline"] = {
+                "value": rate, "unit": "relaxations/s", "cores": cores, "kind": "port",
+                "sample": "the %d smallest of the %d cells (%d-%d atoms), IMD's CG restated in "
+                          "C (oracle/imd_oracle.c), spline tables, one process per cell"
+                          % (len(res), len(cells), min(r[0] for r in res), max(r[0] for r in res)),
+                "atom_force_calls_per_s_per_core": per_core,
+                "converged": int(sum(1 for r in res if r[3])),
+                "estimated_full_workload": {
+                    "value": cores * per_core * len(cells) / work, "unit": "relaxations/s",
+                    "how": "cores x per-core atom-force-calls/s / (atoms x force calls) summed "
+                           "over the %d cells, force calls from the device's plain run"
+                           % len(cells)}}
+        except Exception as e:  # the device measurement stays valid
+            out["cpu_baseline"] = {"value": None, "error": str(e)[:200]}
     out["final_energy_diff_ev_per_atom"] = {"max": float(de.max()), "median": float(np.median(de)),
                                             "within_1e-6": int((de <= 1e-6).sum()),
                                             "compared": int(both.sum())}
