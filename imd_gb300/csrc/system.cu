@@ -1924,6 +1924,13 @@ int imdgpu_set_atoms(imdgpu_sys *s, int n, const int *number, const int *type,
   if (n >= (int)NB_MASK - (1 << 24)) return fail(IMDGPU_ERR_ARG, "too many atoms");
   for (int i = 0; i < n; i++)
     if (type[i] < 0 || type[i] >= s->ntypes) return fail(IMDGPU_ERR_ARG, "type out of range");
+  for (long i = 0; i < 3L * n; i++)
+    if (!std::isfinite(x[i]) || (p && !std::isfinite(p[i])))
+      return fail(IMDGPU_ERR_ARG, "non-finite position or momentum of atom " +
+                                      std::to_string(i / 3));
+  for (int i = 0; i < n; i++)
+    if (!(mass[i] > 0.0) || !std::isfinite(mass[i]))
+      return fail(IMDGPU_ERR_ARG, "mass of atom " + std::to_string(i) + " is not positive");
   if (n != s->n) {
     dfree(s->mom); dfree(s->ref); dfree(s->tpos); dfree(s->tmom); dfree(s->number);
     dfree(s->orig); dfree(s->tnumber); dfree(s->torig); dfree(s->key); dfree(s->local);
@@ -2006,6 +2013,10 @@ int imdgpu_get_atoms(imdgpu_sys *s, double *x, double *p, double *f, double *epo
 
 int imdgpu_put_state(imdgpu_sys *s, const double *x, const double *p) {
   if (!s || !s->atoms_set || !x) return fail(IMDGPU_ERR_STATE, "atoms not set");
+  for (long i = 0; i < 3L * s->n; i++)
+    if (!std::isfinite(x[i]) || (p && !std::isfinite(p[i])))
+      return fail(IMDGPU_ERR_ARG, "non-finite position or momentum of atom " +
+                                      std::to_string(i / 3));
   if (int rcf = batch_full(s)) return rcf;
   const size_t n = s->n;
   CK(cudaMemcpyAsync(s->d_in, x, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, s->st));

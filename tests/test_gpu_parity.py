@@ -183,6 +183,13 @@ def test_bad_inputs_are_errors():
         s.calc_forces(0)
     with pytest.raises(api.IMDGPUError):
         s.set_atoms(g["number"][:10], g["type"][:10] + 3, g["mass"][:10], g["x"][:10])
+    # a NaN in a host buffer (IMD's arrays after a blow-up) is refused before upload
+    x = g["x"][:10].copy()
+    x[3, 1] = np.nan
+    with pytest.raises(api.IMDGPUError):
+        s.set_atoms(g["number"][:10], g["type"][:10], g["mass"][:10], x)
+    with pytest.raises(api.IMDGPUError):
+        s.set_atoms(g["number"][:10], g["type"][:10], np.zeros(10), g["x"][:10])
 
 
 @pytest.mark.parametrize("name", ["cu_pert", "alloy_pert", "lj_pert"])
