@@ -28,7 +28,7 @@ struct DevScalars {
   double fatom2;      // max per-atom |F|^2
   double maxdisp2;    // max |x - x_ref|^2 since the last build
   int rebuild;        // 1: list invalid (check_nblist result)
-  int pad;
+  int badin;          // lowest atom with a non-finite uploaded value (put_state)
 };
 
 // batched CG (batch.cu): vector operation a cell asks for in the next round

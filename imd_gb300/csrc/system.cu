@@ -918,6 +918,19 @@ __global__ void k_scatter_in(SysView v, const double *x, const double *p, const 
   v.orig[o] = o;
 }
 
+// lowest atom (caller's order) whose uploaded position or momentum is not
+// finite; `bad` starts above every atom index
+__global__ void k_check_finite(const double *x, const double *p, int n, int *bad) {
+  const int o = blockIdx.x * blockDim.x + threadIdx.x;
+  if (o >= n) return;
+  bool ok = true;
+  for (int d = 0; d < 3; d++) {
+    ok = ok && isfinite(x[3 * o + d]);
+    if (p) ok = ok && isfinite(p[3 * o + d]);
+  }
+  if (!ok) atomicMin(bad, o);
+}
+
 __global__ void k_put_state(SysView v, const int *slot_of, const double *x, const double *p) {
   const int o = blockIdx.x * blockDim.x + threadIdx.x;
   if (o >= v.n) return;
@@ -2013,14 +2026,22 @@ int imdgpu_get_atoms(imdgpu_sys *s, double *x, double *p, double *f, double *epo
 
 int imdgpu_put_state(imdgpu_sys *s, const double *x, const double *p) {
   if (!s || !s->atoms_set || !x) return fail(IMDGPU_ERR_STATE, "atoms not set");
-  for (long i = 0; i < 3L * s->n; i++)
-    if (!std::isfinite(x[i]) || (p && !std::isfinite(p[i])))
-      return fail(IMDGPU_ERR_ARG, "non-finite position or momentum of atom " +
-                                      std::to_string(i / 3));
   if (int rcf = batch_full(s)) return rcf;
   const size_t n = s->n;
   CK(cudaMemcpyAsync(s->d_in, x, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, s->st));
   if (p) CK(cudaMemcpyAsync(s->d_in + 3 * n, p, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, s->st));
+  // The values are checked where they already are, on the device (a host
+  // pass over 6n doubles cost as much as a quarter of an NVE step); a
+  // non-finite one leaves the device state as it was.
+  int *bad = &s->dsc->badin;
+  CK(cudaMemsetAsync(bad, 0x7f, sizeof(int), s->st));
+  k_check_finite<<<nblk(n, 256), 256, 0, s->st>>>(s->d_in, p ? s->d_in + 3 * n : nullptr, (int)n, bad);
+  CK(cudaGetLastError());
+  int bad_host = 0;
+  CK(cudaMemcpyAsync(&bad_host, bad, sizeof(int), cudaMemcpyDeviceToHost, s->st));
+  CK(cudaStreamSynchronize(s->st));
+  if (bad_host < (int)n)
+    return fail(IMDGPU_ERR_ARG, "non-finite position or momentum of atom " + std::to_string(bad_host));
   SysView v = view(s);
   k_put_state<<<nblk(n, 256), 256, 0, s->st>>>(v, s->slot_of, s->d_in, p ? s->d_in + 3 * n : nullptr);
   CK(cudaGetLastError());

@@ -112,12 +112,15 @@ int imdgpu_set_box(imdgpu_sys *sys, const double *box, const int *pbc, double nb
 /* per-type restriction vectors (src/globals.h:206), 3*ntypes, 1 = free */
 int imdgpu_set_restrictions(imdgpu_sys *sys, const double *restr);
 
-/* Atoms: NUMMER, SORTE, MASSE, ORT (3n), IMPULS (3n, may be NULL). */
+/* Atoms: NUMMER, SORTE, MASSE, ORT (3n), IMPULS (3n, may be NULL).
+ * IMDGPU_ERR_ARG for a non-finite position or momentum or a mass <= 0. */
 int imdgpu_set_atoms(imdgpu_sys *sys, int n, const int *number, const int *type,
                      const double *mass, const double *x, const double *p);
 /* Replace positions and momenta (caller order, 3n each; p may be NULL)
  * without touching the neighbour list: the state IMD's cell arrays hand
- * back to calc_forces each step when they live on the host. */
+ * back to calc_forces each step when they live on the host.  A non-finite
+ * value is IMDGPU_ERR_ARG (checked on the device after the copy) and leaves
+ * the device state as it was. */
 int imdgpu_put_state(imdgpu_sys *sys, const double *x, const double *p);
 /* Copy state back (any pointer may be NULL): x, p, f (3n), epot (n),
  * eam_rho, eam_df (n). */

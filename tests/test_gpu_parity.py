@@ -192,6 +192,35 @@ def test_bad_inputs_are_errors():
         s.set_atoms(g["number"][:10], g["type"][:10], np.zeros(10), g["x"][:10])
 
 
+def test_put_state_refuses_non_finite():
+    """put_state checks the uploaded values on the device: a NaN or an inf
+    momentum is an error naming the lowest bad atom, and the state on the
+    device stays the one before the call."""
+    from imd_gb300 import api
+    g = golden("cu_pert")
+    tab, eam, nt, skin = CASES["cu_pert"]
+    p0 = np.random.default_rng(3).normal(0.0, 0.5, g["x"].shape)
+    s = gpu_system(g, tab, eam, nt, skin, p=p0)
+    s.calc_forces(0)
+    e0 = s.scalars()
+    a0 = s.get_atoms()
+    x, p = g["x"].copy(), p0.copy()
+    p[17, 2] = np.nan
+    p[40, 0] = np.inf
+    with pytest.raises(api.IMDGPUError, match="atom 17"):
+        s.put_state(x, p)
+    x[5, 0] = -np.inf
+    with pytest.raises(api.IMDGPUError, match="atom 5"):
+        s.put_state(x, None)
+    s.calc_forces(1)
+    e1 = s.scalars()
+    # forces are summed with atomics: equal to rounding of the order
+    assert abs(e1.tot_pot_energy - e0.tot_pot_energy) <= 1e-13 * abs(e0.tot_pot_energy)
+    a = s.get_atoms()
+    assert np.array_equal(a["x"], a0["x"]) and np.array_equal(a["p"], a0["p"])
+    assert rel_rms(a["f"], a0["f"]) < 1e-13
+
+
 @pytest.mark.parametrize("name", ["cu_pert", "alloy_pert", "lj_pert"])
 def test_exact_mode_matches_reference(name):
     """IMD's unfused table arithmetic (parity mode) also meets the bars."""
