@@ -1021,6 +1021,131 @@ void orc_move_atoms_mik(orc_sys_t *s) {
   s->f_max2 = fmax2;
 }
 
+/* ------------------------------------------------------------------------ */
+/* GLOK / FIRE (src/imd_main_3d.c:972-1055, src/imd_integrate.c:297-316)     */
+/* ------------------------------------------------------------------------ */
+
+/* INIT values of src/globals.h:580-600 */
+void orc_glok_defaults(orc_glok_t *g) {
+  memset(g, 0, sizeof *g);
+  g->glok_ekin_threshold = 100.0;
+  g->glok_fmaxcrit = 10000.0;
+  g->glok_mixdec = 1.0;
+  g->glok_incfac = 1.02;
+  g->glok_decfac = 0.5;
+  g->glok_minsteps = 5;
+}
+
+/* update_glok (src/imd_main_3d.c:972-1055).  With ADAPTGLOK the loop that
+ * steps the positions back by half a step and zeroes the momenta is the
+ * else branch of `if (glok_int > glok_minsteps) mix = glok_mix;` (the
+ * preprocessor lines at :1030-1035 leave the `else` without a statement of
+ * its own); without ADAPTGLOK it always runs. */
+void orc_update_glok(orc_sys_t *s, orc_glok_t *g, int steps) {
+  const int n = s->n;
+  if (steps == g->steps_min) {
+    g->glok_start = g->steps_min;
+    if (g->mix_on) g->mix = g->glok_mix;
+  }
+  g->glok_int = steps - g->glok_start;
+  if (g->glok_int == 0)
+    for (int i = 0; i < 3 * n; i++) s->p[i] = 0.0;
+  if (g->adapt && g->nPxF >= g->min_nPxF && g->glok_int > g->glok_minsteps) {
+    s->timestep = (s->timestep * g->glok_incfac > g->glok_maxtimestep)
+                      ? g->glok_maxtimestep : s->timestep * g->glok_incfac;
+    if (g->mix_on) g->mix *= g->glok_mixdec;
+  }
+  if (g->mix_on && s->fnorm >= 1e-20) g->mixforcescalefac = sqrt(g->pnorm / s->fnorm);
+  const double nact = g->nactive > 0 ? (double)g->nactive : 3.0 * n;
+  const double ekin = 2 * s->tot_kin_energy / nact;
+  if ((g->PxF < 0.0) || (ekin > g->glok_ekin_threshold) || (sqrt(s->f_max2) >= g->glok_fmaxcrit)) {
+    int back = 1;
+    if (g->adapt) {
+      if (steps > g->glok_minsteps && g->PxF < 0.0) {
+        g->nPxF++;
+        if (s->timestep > g->glok_maxtimestep / 50.0) s->timestep *= g->glok_decfac;
+      }
+      if (g->glok_int > g->glok_minsteps) {
+        g->mix = g->glok_mix;
+        back = 0;
+      }
+    }
+    if (back)
+      for (int nn = 0; nn < n; nn++) {
+        int i = s->order[nn];
+        for (int a = 0; a < 3; a++) {
+          s->x[3 * i + a] -= 0.5 * s->timestep / s->mass[i] * s->p[3 * i + a];
+          s->p[3 * i + a] = 0.0;
+        }
+      }
+    g->glok_start = steps;
+  }
+}
+
+/* move_atoms_nve (src/imd_integrate.c:32-497) with the GLOK and MIX
+ * branches: the global P.F and |P/m|^2 after the momentum update, then the
+ * momenta turned towards the forces by `mix` */
+void orc_move_atoms_glok(orc_sys_t *s, orc_glok_t *g) {
+  double ekin = 0.0, fnorm = 0.0, fmax2 = 0.0, pxf = 0.0, pnorm = 0.0;
+  double dt = s->timestep;
+  for (int nn = 0; nn < s->n; nn++) {
+    int i = s->order[nn];
+    double *p = s->p + 3 * i, *f = s->f + 3 * i, *x = s->x + 3 * i;
+    double m = s->mass[i];
+    double kin1 = p[0] * p[0] + p[1] * p[1] + p[2] * p[2];
+    int t = s->type[i];
+    f[0] *= restr(s, t, 0);
+    f[1] *= restr(s, t, 1);
+    f[2] *= restr(s, t, 2);
+    fnorm += f[0] * f[0] + f[1] * f[1] + f[2] * f[2];
+    fmax2 = OMAX(SQR(f[0]), fmax2);
+    fmax2 = OMAX(SQR(f[1]), fmax2);
+    fmax2 = OMAX(SQR(f[2]), fmax2);
+    p[0] += dt * f[0];
+    p[1] += dt * f[1];
+    p[2] += dt * f[2];
+    pxf += (p[0] * f[0] + p[1] * f[1] + p[2] * f[2]) / m;
+    pnorm += (p[0] * p[0] + p[1] * p[1] + p[2] * p[2]) / m / m;
+    if (g->mix_on)
+      for (int a = 0; a < 3; a++)
+        p[a] = (1.0 - g->mix) * p[a] + g->mix * f[a] * g->mixforcescalefac * m;
+    double kin2 = p[0] * p[0] + p[1] * p[1] + p[2] * p[2];
+    ekin += (kin1 + kin2) / (4 * m);
+    double tmp = dt / m;
+    x[0] += tmp * p[0];
+    x[1] += tmp * p[1];
+    x[2] += tmp * p[2];
+  }
+  s->tot_kin_energy = ekin;
+  s->fnorm = fnorm;
+  s->f_max2 = fmax2;
+  g->pnorm = pnorm;
+  g->PxF = pxf / (sqrt(fnorm) * sqrt(pnorm));
+}
+
+int orc_glok_steps(orc_sys_t *s, orc_glok_t *g, int step0, int nsteps, double *out) {
+  for (int st = 0; st < nsteps; st++) {
+    int rc = orc_calc_forces(s);
+    if (rc < 0) return rc;
+    double ep = s->tot_pot_energy;
+    orc_update_glok(s, g, step0 + st);
+    orc_move_atoms_glok(s, g);
+    if (out) {
+      double *o = out + 8 * (size_t)st;
+      o[0] = ep;
+      o[1] = s->tot_kin_energy;
+      o[2] = s->fnorm;
+      o[3] = s->f_max2;
+      o[4] = s->timestep;
+      o[5] = g->mix;
+      o[6] = g->PxF;
+      o[7] = g->glok_start;
+    }
+    orc_check_nblist(s);
+  }
+  return 0;
+}
+
 /* check_nblist (src/imd_forces_nbl.c:2007-2037) */
 void orc_check_nblist(orc_sys_t *s) {
   double max1 = 0.0;

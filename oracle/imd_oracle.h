@@ -159,6 +159,31 @@ int  orc_nve_steps(orc_sys_t *s, int nsteps, double *epot_out, double *ekin_out)
  * (src/imd_integrate.c:675-873) */
 void orc_move_atoms_nvt(orc_sys_t *s);
 void orc_move_atoms_mik(orc_sys_t *s);
+/* GLOK relaxer, IMD's FIRE (the `glok`, `mix` and `fire` build options):
+ * update_glok (src/imd_main_3d.c:972-1055) before move_atoms_nve with its
+ * GLOK / MIX branches (src/imd_integrate.c:297-316, :485-486).  Parameters
+ * and state are IMD's globals (src/globals.h:425-437, :580-600). */
+typedef struct {
+  int    mix_on, adapt;            /* MIX, ADAPTGLOK (ADAPTGLOK needs MIX) */
+  double glok_ekin_threshold, glok_fmaxcrit;
+  double glok_mix, glok_mixdec;
+  double glok_incfac, glok_decfac, glok_maxtimestep;
+  int    glok_minsteps, min_nPxF;
+  int    steps_min;
+  long   nactive;                  /* <= 0: three per atom */
+  int    glok_start, glok_int, nPxF;
+  double mix, mixforcescalefac, PxF, pnorm;
+} orc_glok_t;
+/* IMD's INIT values of the parameters and the state */
+void orc_glok_defaults(orc_glok_t *g);
+/* update_glok for main_loop step `steps` (s->timestep may change) */
+void orc_update_glok(orc_sys_t *s, orc_glok_t *g, int steps);
+/* move_atoms_nve of the glok ensemble */
+void orc_move_atoms_glok(orc_sys_t *s, orc_glok_t *g);
+/* main_loop steps step0 .. step0+nsteps-1: calc_forces, update_glok,
+ * move_atoms, check_nblist.  Per step 8 values: tot_pot_energy,
+ * tot_kin_energy, fnorm, f_max2, timestep, mix, PxF, glok_start */
+int  orc_glok_steps(orc_sys_t *s, orc_glok_t *g, int step0, int nsteps, double *out);
 /* main_loop steps with move_atoms of `ensemble` (0 nve, 1 nvt, 2 mik);
  * per step tot_pot_energy, tot_kin_energy and (nvt) eta / (mik) fnorm */
 int  orc_md_steps(orc_sys_t *s, int nsteps, int ensemble, double *epot_out,

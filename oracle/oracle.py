@@ -62,6 +62,18 @@ class Sys(C.Structure):
         ("eta", C.c_double), ("isq_tau_eta", C.c_double), ("temperature", C.c_double)]
 
 
+class Glok(C.Structure):
+    """orc_glok_t: parameters and state of the glok ensemble."""
+    _fields_ = [("mix_on", C.c_int), ("adapt", C.c_int), ("glok_ekin_threshold", C.c_double),
+                ("glok_fmaxcrit", C.c_double), ("glok_mix", C.c_double),
+                ("glok_mixdec", C.c_double), ("glok_incfac", C.c_double),
+                ("glok_decfac", C.c_double), ("glok_maxtimestep", C.c_double),
+                ("glok_minsteps", C.c_int), ("min_nPxF", C.c_int), ("steps_min", C.c_int),
+                ("nactive", C.c_long), ("glok_start", C.c_int), ("glok_int", C.c_int),
+                ("nPxF", C.c_int), ("mix", C.c_double), ("mixforcescalefac", C.c_double),
+                ("PxF", C.c_double), ("pnorm", C.c_double)]
+
+
 _lib = None
 
 
@@ -88,6 +100,8 @@ def lib() -> C.CDLL:
         L.orc_free.argtypes = [C.POINTER(Sys)]
         L.orc_nve_steps.argtypes = [C.POINTER(Sys), C.c_int, _dp, _dp]
         L.orc_md_steps.argtypes = [C.POINTER(Sys), C.c_int, C.c_int, _dp, _dp, _dp]
+        L.orc_glok_defaults.argtypes = [C.POINTER(Glok)]
+        L.orc_glok_steps.argtypes = [C.POINTER(Sys), C.POINTER(Glok), C.c_int, C.c_int, _dp]
         L.orc_cg_step.argtypes = [C.POINTER(Sys), C.c_int]
         L.orc_cg_relax.argtypes = [C.POINTER(Sys), C.c_double, C.c_int, _dp]
         L.orc_max_atom_force.argtypes = [C.POINTER(Sys)]
@@ -259,6 +273,24 @@ class OracleSystem:
         ex = np.empty(nsteps)
         lib().orc_md_steps(C.byref(self.s), nsteps, code, _ptr(ep), _ptr(ek), _ptr(ex))
         return ep, ek, ex
+
+    def glok(self, nsteps: int, step0: int = 0, state: Glok = None, **params):
+        """main_loop steps of the glok ensemble (update_glok, move_atoms_nve)
+        from step `step0`.  params: mix_on, adapt and the glok_* values
+        (IMD's defaults otherwise).  Returns (per-step array of tot_pot_energy,
+        tot_kin_energy, fnorm, f_max2, timestep, mix, PxF, glok_start; the
+        state, to continue with)."""
+        L = lib()
+        if state is None:
+            state = Glok()
+            L.orc_glok_defaults(C.byref(state))
+            for k, v in params.items():
+                setattr(state, k, v)
+        out = np.empty((nsteps, 8))
+        rc = L.orc_glok_steps(C.byref(self.s), C.byref(state), step0, nsteps, _ptr(out))
+        if rc < 0:
+            raise RuntimeError("oracle glok steps failed (%d)" % rc)
+        return out, state
 
     def set_nvt(self, temperature: float, isq_tau_eta: float, eta: float = 0.0) -> None:
         self.s.temperature = temperature

@@ -17,6 +17,8 @@
  *             the step and after its calc_forces
  *   nve K   : K main_loop steps calc_forces / move_atoms / check_nblist
  *             (move_atoms of the parameter file's ensemble: nve, nvt, mik)
+ *   glok K  : K main_loop steps of the glok ensemble (update_glok before
+ *             move_atoms) from steps_min
  *   cg K F  : reset_cg, then cg_step until max per-atom |F| <= F
  *   time K  : K NVE steps, print cpu seconds
  */
@@ -224,6 +226,36 @@ int main(int argc, char **argv) {
     sprintf(fname, "%s.final", pre);
     dump_state(fname);
   }
+#ifdef GLOK
+  else if (0 == strcmp(mode, "glok")) {
+    /* K main_loop steps of the glok ensemble from steps_min, in main_loop's
+     * order: calc_forces, update_glok, move_atoms, check_nblist
+     * (src/imd_main_3d.c:66-67, :401, :497-501, :559, :769) */
+    if (glok_start <= steps_min) glok_start = steps_min;
+    sprintf(fname, "%s.steps", pre);
+    FILE *out = fopen(fname, "w");
+    for (steps = steps_min; steps < steps_min + nsteps; steps++) {
+      calc_forces(steps);
+      double ep = tot_pot_energy;
+      update_glok();
+      move_atoms();
+      double mx = 0.0, npxf = 0.0;
+#ifdef MIX
+      mx = mix;
+#endif
+#ifdef ADAPTGLOK
+      npxf = nPxF;
+#endif
+      fprintf(out, "%d %.17e %.17e %ld %.17e %.17e %.17e %.17e %.17e %d %.0f\n", steps, ep,
+              tot_kin_energy, (long)nbl_count, fnorm, f_max2, timestep, mx, PxF, glok_start,
+              npxf);
+      check_nblist();
+    }
+    fclose(out);
+    sprintf(fname, "%s.final", pre);
+    dump_state(fname);
+  }
+#endif
 #ifdef CG
   else if (0 == strcmp(mode, "cg")) {
     double ftol = (argc > 5) ? atof(argv[5]) : 1e-4;

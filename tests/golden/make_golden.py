@@ -32,9 +32,13 @@ Fixtures (all sorted by atom number):
               (tau_eta 10 time units): energies and eta per step
   cu_mik      cu_pert's configuration quenched by 200 MIK steps: energies,
               force norms per step, final positions
+  cu_fire, cu_glok   a perturbed Cu crystal with two vacancies relaxed by
+              the glok ensemble of the `fire` build (300 steps, adaptive time
+              step and mixing) and of the `glok` build (200 steps)
 
 `python tests/golden/make_golden.py stress` writes the stress fixtures only,
-`... ensembles` the NVT / MIK ones, `... lj1000` the 1000-step LJ run.
+`... ensembles` the NVT / MIK ones, `... lj1000` the 1000-step LJ run,
+`... glok` the glok ones.
 """
 from __future__ import annotations
 
@@ -372,6 +376,62 @@ def ensemble_cases() -> None:
     print("cu_mik epot", steps[[0, -1], 1], "fnorm", steps[[0, -1], 4])
 
 
+GLOK_CASES = {
+    # name: (reference build, steps, parameters beyond the ensemble)
+    "cu_fire": ("fire_nbl_eam", 300,
+                dict(glok_mix=0.1, glok_mixdec=0.99, glok_incfac=1.1, glok_decfac=0.5,
+                     glok_maxtimestep=0.5, glok_minsteps=5)),
+    "cu_glok": ("glok_nbl_eam", 200, {}),
+}
+
+
+def glok_cases() -> None:
+    """The glok ensemble (update_glok, src/imd_main_3d.c:972-1055, before
+    move_atoms_nve) of the reference's `fire` and `glok` builds on a
+    perturbed Cu crystal with a vacancy pair: per step the energies, the
+    force norms, the adaptive time step, the mixing factor, P.F and
+    glok_start, and the final state."""
+    subprocess.run(["make", "-s", "-C", ORACLE, "ref"], check=True)
+    tmp = tempfile.mkdtemp(prefix="imdgold_glok")
+    cu = tuple(os.path.join(HERE, "cu" + e) for e in (".pt", ".rho", ".emb"))
+    cus = wl.eam_fcc_system(8)
+    cfg = os.path.join(tmp, "cu_glok.cfg")
+    perturbed_config(cus, 0.15, 21, cfg, remove=[5, 900])
+    for name, (variant, nsteps, extra) in GLOK_CASES.items():
+        p = os.path.join(tmp, name + ".param")
+        wl.write_param(p, coordname=cfg, box_from_header=1, ensemble="glok", starttemp=0.0,
+                       outfiles=os.path.join(tmp, "o"), ntypes=1, masses=63.546,
+                       pbc_dirs=[1, 1, 1], timestep=0.0982266, maxsteps=0, seed=2,
+                       core_potential_file=cu[0], **{"atomic_e-density_file": cu[1]},
+                       embedding_energy_file=cu[2], nbl_margin=0.4, eng_int=0,
+                       checkpt_int=100000000, **extra)
+        pre = os.path.join(tmp, name)
+        run(variant, p, "glok", pre, nsteps)
+        st0 = load_state(pre + ".state0")
+        stf = load_state(pre + ".final")
+        steps = np.loadtxt(pre + ".steps")
+        box, gdim, cellsz = load_box(pre + ".box")
+        prm = dict(GLOK_PARAM_DEFAULTS)
+        prm.update(extra)
+        d = dict(box=box, gdim=gdim, cellsz=cellsz, number=st0["number"], type=st0["type"],
+                 mass=st0["mass"], x0=st0["x"], p0=st0["p"], step=steps[:, 0],
+                 epot=steps[:, 1], ekin=steps[:, 2], nbl_count=steps[:, 3],
+                 fnorm=steps[:, 4], f_max2=steps[:, 5], timestep=steps[:, 6], mix=steps[:, 7],
+                 pxf=steps[:, 8], glok_start=steps[:, 9], npxf=steps[:, 10],
+                 x_final=stf["x"], p_final=stf["p"], dt=0.0982266, skin=0.4,
+                 mix_on=int(variant.startswith("fire")), adapt=int(variant.startswith("fire")),
+                 **{"param_" + k: v for k, v in prm.items()})
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **d)
+        print(name, "epot", steps[[0, -1], 1], "dt", steps[[0, -1], 6],
+              "restarts", len(np.unique(steps[:, 9])), "nPxF", steps[-1, 10])
+
+
+# IMD's INIT values of the glok parameters (src/globals.h:580-600)
+GLOK_PARAM_DEFAULTS = dict(glok_ekin_threshold=100.0, glok_fmaxcrit=10000.0, glok_mix=0.0,
+                           glok_mixdec=1.0, glok_incfac=1.02, glok_decfac=0.5,
+                           glok_maxtimestep=0.0, glok_minsteps=5, min_nPxF=0)
+
+
 def lj1000_case() -> None:
     """The plain-method LJ workload (4000 atoms, T* 0.72, dt 0.005, skin 0.3)
     for all of its 1000 steps, with snapshots every 250 steps."""
@@ -413,8 +473,11 @@ if __name__ == "__main__":
         ensemble_cases()
     elif len(sys.argv) > 1 and sys.argv[1] == "lj1000":
         lj1000_case()
+    elif len(sys.argv) > 1 and sys.argv[1] == "glok":
+        glok_cases()
     else:
         main()
         stress_cases()
         ensemble_cases()
         lj1000_case()
+        glok_cases()

@@ -180,6 +180,42 @@ def test_mik_quench_matches_reference():
     assert np.abs(d).max() < 1e-8
 
 
+def glok_params(g) -> dict:
+    """The glok parameters a golden run used (IMD's names)."""
+    out = {"mix_on": int(g["mix_on"]), "adapt": int(g["adapt"])}
+    for k in g:
+        if k.startswith("param_"):
+            name = k[len("param_"):]
+            out[name] = int(g[k]) if name in ("glok_minsteps", "min_nPxF") else float(g[k])
+    return out
+
+
+@pytest.mark.parametrize("name", ["cu_fire", "cu_glok"])
+def test_glok_matches_reference(name):
+    """update_glok + move_atoms_nve of the `fire` and `glok` builds: the
+    decisions of every step (time step, mixing factor, restarts) identical,
+    energies to 1e-12, P.F to 1e-8 relative, final positions to 1e-12 A."""
+    g = golden(name)
+    s = OracleSystem(g["box"], g["x0"], g["type"], g["mass"], g["number"], 1, tables("cu"),
+                     True, float(g["skin"]), timestep=float(g["dt"]), p=g["p0"])
+    out, st = s.glok(len(g["epot"]), 0, **glok_params(g))
+    np.testing.assert_array_equal(out[:, 4], g["timestep"])
+    np.testing.assert_array_equal(out[:, 5], g["mix"])
+    np.testing.assert_array_equal(out[:, 7], g["glok_start"])
+    assert st.nPxF == int(g["npxf"][-1])
+    np.testing.assert_allclose(out[:, 0], g["epot"], rtol=1e-12, atol=0)
+    np.testing.assert_allclose(out[:, 1], g["ekin"], rtol=1e-10, atol=1e-14)
+    np.testing.assert_allclose(out[:, 2], g["fnorm"], rtol=1e-9, atol=0)
+    np.testing.assert_allclose(out[:, 6], g["pxf"], rtol=1e-8, atol=1e-12)
+    d = s.x - g["x_final"]
+    d -= np.round(d @ np.linalg.inv(g["box"])) @ g["box"]
+    assert np.abs(d).max() < 1e-12
+    # the runs exercise the restarts (and, for fire, the adaptive step)
+    assert len(np.unique(g["glok_start"])) > 3
+    if g["adapt"]:
+        assert g["timestep"].max() > g["timestep"][0] and int(g["npxf"][-1]) > 0
+
+
 def test_lj_1000_steps_segmentwise():
     """The plain-method LJ run over all 1000 steps, step by step: from each
     of the reference's snapshots (every 250 steps) the oracle reproduces the
