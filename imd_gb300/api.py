@@ -36,6 +36,23 @@ class Scalars(C.Structure):
                 ("max_cell_atoms", C.c_int), ("short_distance", C.c_int)]
 
 
+class GlokParams(C.Structure):
+    """imdgpu_glok_params: IMD's glok parameters and build options."""
+    _fields_ = [("mix", C.c_int), ("adapt", C.c_int), ("glok_ekin_threshold", C.c_double),
+                ("glok_fmaxcrit", C.c_double), ("glok_mix", C.c_double),
+                ("glok_mixdec", C.c_double), ("glok_incfac", C.c_double),
+                ("glok_decfac", C.c_double), ("glok_maxtimestep", C.c_double),
+                ("glok_minsteps", C.c_int), ("min_nPxF", C.c_int), ("steps_min", C.c_int),
+                ("nactive", C.c_long)]
+
+
+class GlokState(C.Structure):
+    """imdgpu_glok_state: IMD's globals of the glok ensemble."""
+    _fields_ = [("timestep", C.c_double), ("mix", C.c_double),
+                ("mixforcescalefac", C.c_double), ("PxF", C.c_double), ("pnorm", C.c_double),
+                ("glok_start", C.c_int), ("glok_int", C.c_int), ("nPxF", C.c_int)]
+
+
 class Timing(C.Structure):
     _fields_ = [("ms_total", C.c_double), ("ms_density", C.c_double),
                 ("ms_force", C.c_double), ("ms_integrate", C.c_double),
@@ -111,6 +128,10 @@ def lib() -> C.CDLL:
         L.imdgpu_move_atoms_nvt.argtypes = [vp, C.c_double]
         L.imdgpu_set_nvt.argtypes = [vp, C.c_double, C.c_double, C.c_double, C.c_long]
         L.imdgpu_get_nvt.argtypes = [vp, _dp]
+        L.imdgpu_glok_defaults.argtypes = [C.POINTER(GlokParams)]
+        L.imdgpu_set_glok.argtypes = [vp, C.POINTER(GlokParams), C.c_double]
+        L.imdgpu_move_atoms_glok.argtypes = [vp, C.c_int]
+        L.imdgpu_get_glok.argtypes = [vp, C.POINTER(GlokState)]
         L.imdgpu_set_blocks.argtypes = [vp, C.c_int, C.c_int]
         L.imdgpu_batch_set_autotune.argtypes = [vp, C.c_int]
         L.imdgpu_batch_positions.argtypes = [vp, _dp]
@@ -272,6 +293,29 @@ class GpuSystem:
         e = C.c_double(0.0)
         _check(lib().imdgpu_get_nvt(self.h, C.byref(e)), "get_nvt")
         return e.value
+
+    def set_glok(self, timestep: float, **params) -> None:
+        """Start a glok (FIRE) phase.  params: mix, adapt (the MIX and
+        ADAPTGLOK build options), glok_* and min_nPxF as IMD names them,
+        steps_min, nactive; IMD's defaults for the rest."""
+        prm = GlokParams()
+        _check(lib().imdgpu_glok_defaults(C.byref(prm)), "glok_defaults")
+        for k, v in params.items():
+            if not hasattr(prm, k):
+                raise TypeError("unknown glok parameter %r" % k)
+            setattr(prm, k, v)
+        _check(lib().imdgpu_set_glok(self.h, C.byref(prm), timestep), "set_glok")
+
+    def move_atoms_glok(self, steps: int) -> GlokState:
+        """update_glok for main_loop step `steps`, then move_atoms_nve of
+        the glok ensemble; returns the glok state after it."""
+        _check(lib().imdgpu_move_atoms_glok(self.h, steps), "move_atoms_glok")
+        return self.glok_state()
+
+    def glok_state(self) -> GlokState:
+        st = GlokState()
+        _check(lib().imdgpu_get_glok(self.h, C.byref(st)), "get_glok")
+        return st
 
     def nve_run(self, nsteps: int, timestep: float, record: bool = True):
         ep = np.empty(nsteps) if record else None

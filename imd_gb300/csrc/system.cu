@@ -190,6 +190,14 @@ struct imdgpu_sys {
   long nvt_nactive = 0;
   double *d_e2 = nullptr;
 
+  // glok ensemble: parameters, IMD's globals of update_glok, and the totals
+  // of the last glok move it reads (fnorm, f_max2, tot_kin_energy)
+  imdgpu_glok_params glok_prm{};
+  imdgpu_glok_state glok{};
+  bool glok_set = false;
+  double glok_fnorm = 0.0, glok_fmax2 = 0.0, glok_ekin = 0.0;
+  double *d_glok = nullptr;   // sum P.F/m, sum |P/m|^2 of the last move
+
   // STRESS_TENS: per ext atom xx yy zz yz zx xy
   double *d_stress = nullptr;
   size_t stress_cap = 0;
@@ -744,6 +752,98 @@ __global__ void k_finalize_nvt(const double *partial, int nb, DevScalars *sc, do
     sc->maxdisp2 = e;
     if (e > skin2) sc->rebuild = 1;
     *out2 = b;
+  }
+}
+
+// move_atoms_nve of the glok ensemble (src/imd_integrate.c:32-497 with the
+// GLOK and MIX branches, :297-316), fused with what update_glok did to the
+// atoms just before it (src/imd_main_3d.c:985-995, :1036-1050): `zero`
+// sets the momenta to zero; `back` moves the positions half a step back
+// along the momenta and then zeroes them.  IMD's operation order, unfused.
+// Per block: sums of the kinetic energy, |F|^2, P.F/m and |P/m|^2; maxima
+// of the force component and of the displacement since the last build.
+__global__ void __launch_bounds__(BS_VEC) k_glok(SysView v, double dt, int zero, int back,
+                                                 int mix_on, double omm, double mix,
+                                                 double mfs, double *partial) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double r[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};   // ek fn pf pn | fm dm
+  if (i < v.n) {
+    double4 p = v.mom[i], f = v.frc[i], x = v.pos[i];
+    const int t = (int)x.w;
+    const double m = p.w;
+    if (zero) p.x = p.y = p.z = 0.0;
+    if (back) {
+      const double h = dmul(0.5, dt) / m;
+      x.x = dsub(x.x, dmul(h, p.x));
+      x.y = dsub(x.y, dmul(h, p.y));
+      x.z = dsub(x.z, dmul(h, p.z));
+      p.x = p.y = p.z = 0.0;
+    }
+    const double kin1 = dadd(dadd(dmul(p.x, p.x), dmul(p.y, p.y)), dmul(p.z, p.z));
+    f.x = dmul(f.x, v.restr[3 * t]);
+    f.y = dmul(f.y, v.restr[3 * t + 1]);
+    f.z = dmul(f.z, v.restr[3 * t + 2]);
+    v.frc[i] = f;
+    r[1] = dadd(dadd(dmul(f.x, f.x), dmul(f.y, f.y)), dmul(f.z, f.z));
+    r[4] = fmax(fmax(f.x * f.x, f.y * f.y), f.z * f.z);
+    p.x = dadd(p.x, dmul(dt, f.x));
+    p.y = dadd(p.y, dmul(dt, f.y));
+    p.z = dadd(p.z, dmul(dt, f.z));
+    r[2] = dadd(dadd(dmul(p.x, f.x), dmul(p.y, f.y)), dmul(p.z, f.z)) / m;
+    r[3] = dadd(dadd(dmul(p.x, p.x), dmul(p.y, p.y)), dmul(p.z, p.z)) / m / m;
+    if (mix_on) {
+      p.x = dadd(dmul(omm, p.x), dmul(dmul(dmul(mix, f.x), mfs), m));
+      p.y = dadd(dmul(omm, p.y), dmul(dmul(dmul(mix, f.y), mfs), m));
+      p.z = dadd(dmul(omm, p.z), dmul(dmul(dmul(mix, f.z), mfs), m));
+    }
+    const double kin2 = dadd(dadd(dmul(p.x, p.x), dmul(p.y, p.y)), dmul(p.z, p.z));
+    r[0] = dadd(kin1, kin2) / (4.0 * m);
+    const double tmp = dt / m;
+    x.x = dadd(x.x, dmul(tmp, p.x));
+    x.y = dadd(x.y, dmul(tmp, p.y));
+    x.z = dadd(x.z, dmul(tmp, p.z));
+    v.mom[i] = p;
+    v.pos[i] = x;
+    const double4 rf = v.ref[i];
+    r[5] = r2_exact(dsub(x.x, rf.x), dsub(x.y, rf.y), dsub(x.z, rf.z));
+  }
+  __shared__ double sh[6][BS_VEC / 32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < 6; k++) r[k] = k < 4 ? warp_sum(r[k]) : warp_max(r[k]);
+  if (lane == 0) {
+#pragma unroll
+    for (int k = 0; k < 6; k++) sh[k][w] = r[k];
+  }
+  __syncthreads();
+  if (threadIdx.x < 6) {
+    const int k = threadIdx.x;
+    double a = 0.0;
+    for (int j = 0; j < BS_VEC / 32; j++) a = k < 4 ? a + sh[k][j] : fmax(a, sh[k][j]);
+    partial[6 * (size_t)blockIdx.x + k] = a;
+  }
+}
+
+// fixed-order totals of the glok partials; out2 = sum P.F/m, sum |P/m|^2
+__global__ void k_finalize_glok(const double *partial, int nb, DevScalars *sc, double skin2,
+                                double *out2) {
+  const int lane = threadIdx.x;
+  double r[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+  for (int b = lane; b < nb; b += 32) {
+#pragma unroll
+    for (int k = 0; k < 6; k++)
+      r[k] = k < 4 ? r[k] + partial[6 * (size_t)b + k] : fmax(r[k], partial[6 * (size_t)b + k]);
+  }
+#pragma unroll
+  for (int k = 0; k < 6; k++) r[k] = k < 4 ? warp_sum(r[k]) : warp_max(r[k]);
+  if (lane == 0) {
+    sc->ekin = r[0];
+    sc->fnorm = r[1];
+    sc->fmax2 = r[4];
+    sc->maxdisp2 = r[5];
+    if (r[5] > skin2) sc->rebuild = 1;
+    out2[0] = r[2];
+    out2[1] = r[3];
   }
 }
 
@@ -1699,6 +1799,7 @@ int imdgpu_destroy(imdgpu_sys *s) {
   dfree(s->ml_save); dfree(s->ml_ecell); dfree(s->ml_sel);
   dfree(s->d_stress);
   dfree(s->d_e2);
+  dfree(s->d_glok);
   dfree(s->d_sys_short);
   dfree(s->d_atom_sys); dfree(s->d_aoff); dfree(s->d_sgdim); dfree(s->d_scdim); dfree(s->d_scoff);
   dfree(s->d_sys_done); dfree(s->d_ndone); dfree(s->d_sbox); dfree(s->d_stbox); dfree(s->d_cs);
@@ -2109,7 +2210,6 @@ int imdgpu_calc_stress(imdgpu_sys *s, double *presstens, double *tot) {
   const size_t ext = (size_t)s->ncap + s->gcap;
   if (s->stress_cap < ext) {
     dfree(s->d_stress);
-  dfree(s->d_e2);
     CK(dalloc(&s->d_stress, 6 * ext));
     s->stress_cap = ext;
   }
@@ -2234,6 +2334,103 @@ int imdgpu_move_atoms_nvt(imdgpu_sys *s, double timestep) {
   if (rc) return rc;
   const double ttt = s->nvt_nactive * s->nvt_temp;
   s->nvt_eta += timestep * (e2 / ttt - 1.0) * s->nvt_isq_tau;
+  return IMDGPU_OK;
+}
+
+int imdgpu_glok_defaults(imdgpu_glok_params *prm) {
+  if (!prm) return fail(IMDGPU_ERR_ARG, "null");
+  memset(prm, 0, sizeof *prm);
+  prm->glok_ekin_threshold = 100.0;
+  prm->glok_fmaxcrit = 10000.0;
+  prm->glok_mixdec = 1.0;
+  prm->glok_incfac = 1.02;
+  prm->glok_decfac = 0.5;
+  prm->glok_minsteps = 5;
+  return IMDGPU_OK;
+}
+
+// A new glok phase: IMD's globals as main_loop finds them on its first
+// step (src/globals.h:425-437, :580-600; glok_start clamped to steps_min,
+// src/imd_main_3d.c:66-67).  ADAPTGLOK without MIX does not compile in IMD;
+// an adaptive step with no maximum would set the step to zero there.
+int imdgpu_set_glok(imdgpu_sys *s, const imdgpu_glok_params *prm, double timestep) {
+  if (!s || !s->atoms_set) return fail(IMDGPU_ERR_STATE, "atoms not set");
+  if (!prm || !(timestep > 0.0)) return fail(IMDGPU_ERR_ARG, "glok: parameters and timestep > 0");
+  if (prm->adapt && !prm->mix) return fail(IMDGPU_ERR_ARG, "glok: adapt needs mix (ADAPTGLOK needs MIX)");
+  if (prm->adapt && !(prm->glok_maxtimestep > 0.0))
+    return fail(IMDGPU_ERR_ARG, "glok: adapt needs glok_maxtimestep > 0");
+  s->glok_prm = *prm;
+  s->glok = imdgpu_glok_state{};
+  s->glok.timestep = timestep;
+  s->glok.glok_start = prm->steps_min > 0 ? prm->steps_min : 0;
+  s->glok_fnorm = s->glok_fmax2 = s->glok_ekin = 0.0;
+  s->glok_set = true;
+  return IMDGPU_OK;
+}
+
+int imdgpu_get_glok(imdgpu_sys *s, imdgpu_glok_state *st) {
+  if (!s || !st) return fail(IMDGPU_ERR_ARG, "null");
+  *st = s->glok;
+  return IMDGPU_OK;
+}
+
+// update_glok (src/imd_main_3d.c:972-1055) on the host, then the fused
+// move on the device.  With ADAPTGLOK the half step back is the else branch
+// of `if (glok_int > glok_minsteps) mix = glok_mix;` (the preprocessor lines
+// at :1030-1035 leave that `else` without a statement of its own).
+int imdgpu_move_atoms_glok(imdgpu_sys *s, int steps) {
+  if (!s || !s->atoms_set) return fail(IMDGPU_ERR_STATE, "atoms not set");
+  if (!s->geom_ready || s->nbcap == 0)
+    return fail(IMDGPU_ERR_STATE, "move_atoms before the first calc_forces");
+  if (!s->glok_set) return fail(IMDGPU_ERR_STATE, "imdgpu_set_glok first");
+  const imdgpu_glok_params &P = s->glok_prm;
+  imdgpu_glok_state &G = s->glok;
+  if (steps == P.steps_min) {
+    G.glok_start = P.steps_min;
+    if (P.mix) G.mix = P.glok_mix;
+  }
+  G.glok_int = steps - G.glok_start;
+  const int zero = G.glok_int == 0;
+  if (P.adapt && G.nPxF >= P.min_nPxF && G.glok_int > P.glok_minsteps) {
+    G.timestep = (G.timestep * P.glok_incfac > P.glok_maxtimestep) ? P.glok_maxtimestep
+                                                                   : G.timestep * P.glok_incfac;
+    if (P.mix) G.mix *= P.glok_mixdec;
+  }
+  if (P.mix && s->glok_fnorm >= 1e-20) G.mixforcescalefac = std::sqrt(G.pnorm / s->glok_fnorm);
+  const double nact = P.nactive > 0 ? (double)P.nactive : 3.0 * s->n;
+  const double ekin = 2 * s->glok_ekin / nact;
+  int back = 0;
+  if ((G.PxF < 0.0) || (ekin > P.glok_ekin_threshold) ||
+      (std::sqrt(s->glok_fmax2) >= P.glok_fmaxcrit)) {
+    back = 1;
+    if (P.adapt) {
+      if (steps > P.glok_minsteps && G.PxF < 0.0) {
+        G.nPxF++;
+        if (G.timestep > P.glok_maxtimestep / 50.0) G.timestep *= P.glok_decfac;
+      }
+      if (G.glok_int > P.glok_minsteps) {
+        G.mix = P.glok_mix;
+        back = 0;
+      }
+    }
+    G.glok_start = steps;
+  }
+  if (!s->d_glok) CK(dalloc(&s->d_glok, 2));
+  SysView v = view(s);
+  const int nb = nblk(s->n, BS_VEC);
+  k_glok<<<nb, BS_VEC, 0, s->st>>>(v, G.timestep, zero, back, P.mix ? 1 : 0, 1.0 - G.mix, G.mix,
+                                   G.mixforcescalefac, s->partial);
+  k_finalize_glok<<<1, 32, 0, s->st>>>(s->partial, nb, s->dsc, v.skin2, s->d_glok);
+  CK(cudaGetLastError());
+  double pp[2] = {0.0, 0.0};
+  CK(cudaMemcpyAsync(pp, s->d_glok, sizeof pp, cudaMemcpyDeviceToHost, s->st));
+  int rc = read_back(s);
+  if (rc) return rc;
+  s->glok_fnorm = s->hsc->fnorm;
+  s->glok_fmax2 = s->hsc->fmax2;
+  s->glok_ekin = s->hsc->ekin;
+  G.pnorm = pp[1];
+  G.PxF = pp[0] / (std::sqrt(s->glok_fnorm) * std::sqrt(pp[1]));
   return IMDGPU_OK;
 }
 

@@ -161,6 +161,38 @@ int imdgpu_set_nvt(imdgpu_sys *sys, double temperature, double isq_tau_eta, doub
                    long nactive);
 int imdgpu_get_nvt(imdgpu_sys *sys, double *eta);
 int imdgpu_move_atoms_nvt(imdgpu_sys *sys, double timestep);
+/* The glok ensemble, IMD's FIRE relaxer (build options `glok`, `mix`,
+ * `fire`; src/Makefile:1529-1548).  Parameters as IMD parses them
+ * (src/imd_param.c:1569-1650), defaults from imdgpu_glok_defaults (IMD's
+ * INIT values, src/globals.h:580-600). */
+typedef struct {
+  int mix;                     /* MIX: momenta turned towards the forces */
+  int adapt;                   /* ADAPTGLOK: adaptive time step (needs mix) */
+  double glok_ekin_threshold, glok_fmaxcrit;
+  double glok_mix, glok_mixdec;
+  double glok_incfac, glok_decfac, glok_maxtimestep;
+  int glok_minsteps, min_nPxF;
+  int steps_min;               /* first main_loop step of the phase */
+  long nactive;                /* degrees of freedom; <= 0: 3 per atom */
+} imdgpu_glok_params;
+/* IMD's globals of the glok state after the last call */
+typedef struct {
+  double timestep;             /* the adaptive time step */
+  double mix, mixforcescalefac;
+  double PxF;                  /* P.F / (|F| |P/m|) of the last move */
+  double pnorm;                /* sum |P/m|^2 of the last move */
+  int glok_start, glok_int, nPxF;
+} imdgpu_glok_state;
+int imdgpu_glok_defaults(imdgpu_glok_params *prm);
+/* start a glok phase: parameters, the start time step (IMD's
+ * starttimestep), the state of IMD's globals before the first step */
+int imdgpu_set_glok(imdgpu_sys *sys, const imdgpu_glok_params *prm, double timestep);
+/* update_glok (src/imd_main_3d.c:972-1055) for main_loop step `steps`,
+ * then move_atoms_nve with the GLOK and MIX branches
+ * (src/imd_integrate.c:297-316, :485-486): what main_loop runs between
+ * calc_forces and check_nblist for `ensemble glok` */
+int imdgpu_move_atoms_glok(imdgpu_sys *sys, int steps);
+int imdgpu_get_glok(imdgpu_sys *sys, imdgpu_glok_state *st);
 /* nsteps of main_loop (src/imd_main_3d.c:155-870) for ensemble nve:
  * calc_forces, move_atoms_nve, check_nblist, fully on the device.
  * epot/ekin (may be NULL) receive tot_pot_energy and tot_kin_energy of every

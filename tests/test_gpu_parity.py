@@ -419,6 +419,62 @@ def test_mik_matches_reference():
     assert np.abs(d).max() < 1e-8
 
 
+@pytest.mark.parametrize("name", ["cu_fire", "cu_glok"])
+def test_glok_matches_reference(name):
+    """The glok ensemble (IMD's FIRE) on the device against the reference's
+    `fire` (adaptive step, mixing) and `glok` builds, main_loop step by step:
+    every decision identical (time step, mixing factor, restarts, nPxF),
+    energies to 1e-9, P.F to 1e-6 relative, final positions to 1e-8 A."""
+    g = golden(name)
+    gg = dict(g)
+    gg["x"] = g["x0"]
+    s = gpu_system(gg, "cu", 1, 1, float(g["skin"]), p=g["p0"])
+    prm = {"mix": int(g["mix_on"]), "adapt": int(g["adapt"])}
+    for k in g:
+        if k.startswith("param_"):
+            n = k[len("param_"):]
+            prm[n] = int(g[k]) if n in ("glok_minsteps", "min_nPxF") else float(g[k])
+    s.set_glok(float(g["dt"]), **prm)
+    rows = []
+    for st in range(len(g["epot"])):
+        s.calc_forces(st)
+        ep = s.scalars().tot_pot_energy
+        gs = s.move_atoms_glok(st)
+        sc = s.scalars()
+        rows.append((ep, sc.tot_kin_energy, sc.fnorm, gs.timestep, gs.mix, gs.PxF,
+                     gs.glok_start))
+        s.check_nblist()
+    r = np.array(rows)
+    np.testing.assert_array_equal(r[:, 3], g["timestep"])
+    np.testing.assert_array_equal(r[:, 4], g["mix"])
+    np.testing.assert_array_equal(r[:, 6], g["glok_start"])
+    assert s.glok_state().nPxF == int(g["npxf"][-1])
+    np.testing.assert_allclose(r[:, 0], g["epot"], rtol=1e-9, atol=0)
+    np.testing.assert_allclose(r[:, 1], g["ekin"], rtol=1e-7, atol=1e-12)
+    np.testing.assert_allclose(r[:, 2], g["fnorm"], rtol=1e-6, atol=0)
+    np.testing.assert_allclose(r[:, 5], g["pxf"], rtol=1e-6, atol=1e-9)
+    x = s.get_atoms()["x"]
+    d = x - g["x_final"]
+    d -= np.round(d @ np.linalg.inv(g["box"])) @ g["box"]
+    assert np.abs(d).max() < 1e-8
+
+
+def test_glok_parameters_checked():
+    from imd_gb300 import api
+    g = golden("cu_fire")
+    gg = dict(g)
+    gg["x"] = g["x0"]
+    s = gpu_system(gg, "cu", 1, 1, float(g["skin"]), p=g["p0"])
+    with pytest.raises(api.IMDGPUError):
+        s.move_atoms_glok(0)                       # no set_glok yet
+    with pytest.raises(api.IMDGPUError):
+        s.set_glok(0.1, mix=0, adapt=1, glok_maxtimestep=0.5)   # ADAPTGLOK needs MIX
+    with pytest.raises(api.IMDGPUError):
+        s.set_glok(0.1, mix=1, adapt=1)            # adaptive step without a maximum
+    with pytest.raises(TypeError):
+        s.set_glok(0.1, glok_mixx=0.1)
+
+
 def test_lj_1000_steps_segmentwise():
     """The plain-method LJ workload (4000 atoms, 1000 steps) against the
     reference step by step: from each reference snapshot (every 250 steps)
