@@ -1588,7 +1588,7 @@ static int rebuild_sync(imdgpu_sys *s) {
   for (int attempt = 0; attempt < 6; attempt++) {
     int one = 1;
     CK(cudaMemcpyAsync(&s->dsc->rebuild, &one, sizeof(int), cudaMemcpyHostToDevice, s->st));
-  s->hsc_valid = false;
+    s->hsc_valid = false;
     CK(cudaMemsetAsync(s->status, 0, sizeof(unsigned), s->st));
     int rc = issue_rebuild(s);
     if (rc) return rc;
@@ -1635,7 +1635,7 @@ static int prepare(imdgpu_sys *s) {
     if (rc) return rc;
     int one = 1;
     CK(cudaMemcpy(&s->dsc->rebuild, &one, sizeof(int), cudaMemcpyHostToDevice));
-  s->hsc_valid = false;
+    s->hsc_valid = false;
   }
   return IMDGPU_OK;
 }
@@ -1835,7 +1835,7 @@ int imdgpu_set_precision(imdgpu_sys *s, int precision) {
       s->geom_ready = false;
       int one = 1;
       CK(cudaMemcpy(&s->dsc->rebuild, &one, sizeof(int), cudaMemcpyHostToDevice));
-  s->hsc_valid = false;
+      s->hsc_valid = false;
     }
   }
   return IMDGPU_OK;
