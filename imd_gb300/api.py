@@ -312,6 +312,34 @@ class GpuSystem:
         _check(lib().imdgpu_move_atoms_glok(self.h, steps), "move_atoms_glok")
         return self.glok_state()
 
+    def relax_glok(self, timestep: float, maxsteps: int, fnorm_threshold: float = 0.0,
+                   ekin_threshold: float = 0.0, delta_epot_threshold: float = 0.0,
+                   steps_min: int = 0, **params):
+        """main_loop of `ensemble glok` with IMD's relaxation test: per step
+        calc_forces, update_glok + move_atoms_nve, check_relaxed
+        (src/imd_main_3d.c:1741-1820), check_nblist; the loop ends after the
+        first step that check_relaxed calls relaxed (sqrt(fnorm/nactive),
+        2 E_kin/nactive or the change of E_pot per atom below its
+        threshold).  Returns (steps run, relaxed)."""
+        self.set_glok(timestep, steps_min=steps_min, **params)
+        nact = float(params.get("nactive", 0) or 3 * self.n)
+        old_epot = 0.0
+        for steps in range(steps_min, steps_min + maxsteps):
+            self.calc_forces(steps)
+            self.move_atoms_glok(steps)
+            sc = self.scalars()
+            fnorm2 = np.sqrt(sc.fnorm / nact)
+            ekin = 2 * sc.tot_kin_energy / nact
+            epot = sc.tot_pot_energy / self.n
+            delta_epot = abs(old_epot - epot)
+            relaxed = (ekin < ekin_threshold or fnorm2 < fnorm_threshold
+                       or delta_epot < delta_epot_threshold)
+            old_epot = epot
+            self.check_nblist()
+            if relaxed:
+                return steps - steps_min + 1, True
+        return maxsteps, False
+
     def glok_state(self) -> GlokState:
         st = GlokState()
         _check(lib().imdgpu_get_glok(self.h, C.byref(st)), "get_glok")

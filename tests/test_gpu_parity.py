@@ -459,6 +459,29 @@ def test_glok_matches_reference(name):
     assert np.abs(d).max() < 1e-8
 
 
+def test_glok_relax_stops_where_reference_does():
+    """main_loop of `ensemble glok` with check_relaxed: the run stops at the
+    first step whose sqrt(fnorm/nactive) is below fnorm_threshold, the step
+    the reference's per-step force norms give."""
+    g = golden("cu_fire")
+    gg = dict(g)
+    gg["x"] = g["x0"]
+    n = len(g["x0"])
+    f2 = np.sqrt(g["fnorm"] / (3.0 * n))
+    thr = f2[150] * 1.0001
+    expect = int(np.flatnonzero(f2 < thr)[0]) + 1
+    assert np.all(np.abs(f2[:expect] / thr - 1.0) > 1e-6)   # no decision on a knife edge
+    prm = {"mix": 1, "adapt": 1}
+    for k in g:
+        if k.startswith("param_"):
+            nm = k[len("param_"):]
+            prm[nm] = int(g[k]) if nm in ("glok_minsteps", "min_nPxF") else float(g[k])
+    s = gpu_system(gg, "cu", 1, 1, float(g["skin"]), p=g["p0"])
+    nsteps, relaxed = s.relax_glok(float(g["dt"]), len(g["epot"]), fnorm_threshold=thr, **prm)
+    assert relaxed and nsteps == expect
+    assert s.glok_state().timestep == g["timestep"][expect - 1]
+
+
 def test_glok_parameters_checked():
     from imd_gb300 import api
     g = golden("cu_fire")
