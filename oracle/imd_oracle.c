@@ -496,10 +496,8 @@ static inline double sprod(const double *a, const double *b) {
   return a[0] * b[0] + a[1] * b[1] + a[2] * b[2];
 }
 
-/* make_box (src/imd_geom_3d.c:52-106), init_cells with NBLIST
- * (:113-200; margin added once :122-126) and make_cell_lists with AR
- * (:823-947). */
-int orc_setup_geometry(orc_sys_t *s) {
+/* make_box (src/imd_geom_3d.c:52-80): tbox, volume, squared heights */
+static int make_box(orc_sys_t *s) {
   vec_prod(s->box[1], s->box[2], s->tbox[0]);
   vec_prod(s->box[2], s->box[0], s->tbox[1]);
   vec_prod(s->box[0], s->box[1], s->tbox[2]);
@@ -508,17 +506,27 @@ int orc_setup_geometry(orc_sys_t *s) {
   for (int a = 0; a < 3; a++)
     for (int c = 0; c < 3; c++) s->tbox[a][c] /= s->volume;
   for (int a = 0; a < 3; a++) s->height[a] = 1.0 / sprod(s->tbox[a], s->tbox[a]);
+  return 0;
+}
 
-  s->cellsz = SQR(sqrt((double)s->cellsz) + s->nbl_margin);
+/* init_cells (src/imd_geom_3d.c:113-206) with the NPT tolerance factor tol
+ * (:128-133, 1 otherwise) on the list radius already set, and
+ * make_cell_lists with AR (:823-947); min/max_height (may be NULL) get the
+ * squared heights between which the grid stays (:196-206) */
+static int init_cells(orc_sys_t *s, double tol, double *min_height, double *max_height) {
   for (int a = 0; a < 3; a++) {
-    double scale = sqrt(1.0 * s->cellsz / s->height[a]);
+    double scale = sqrt(tol * s->cellsz / s->height[a]);
     s->gdim[a] = (int)(1.0 / scale);
     if (s->gdim[a] < 1) return 2; /* "global_cell_dim too small" */
     s->cdim[a] = s->gdim[a] + 2;
+    if (min_height) min_height[a] = s->cellsz * SQR(s->gdim[a]);
+    if (max_height) max_height[a] = s->cellsz * SQR(s->gdim[a] + 1) * tol;
   }
   int cx = s->cdim[0], cy = s->cdim[1], cz = s->cdim[2];
   s->nallcells = cx * cy * cz;
   s->nreal_cells = s->gdim[0] * s->gdim[1] * s->gdim[2];
+  free(s->real_cells);
+  free(s->cnbrs);
   s->real_cells = (int *)malloc(sizeof(int) * s->nreal_cells);
   s->cnbrs = (int *)malloc(sizeof(int) * 14 * s->nreal_cells);
   int l = 0;
@@ -549,9 +557,19 @@ int orc_setup_geometry(orc_sys_t *s) {
             }
         l++;
       }
+  free(s->cell_start);
+  free(s->cell_cnt);
   s->cell_start = (int *)calloc(s->nallcells + 1, sizeof(int));
   s->cell_cnt = (int *)calloc(s->nallcells, sizeof(int));
   return 0;
+}
+
+/* make_box, the list margin added once (src/imd_geom_3d.c:122-126), then
+ * init_cells */
+int orc_setup_geometry(orc_sys_t *s) {
+  if (make_box(s)) return 1;
+  s->cellsz = SQR(sqrt((double)s->cellsz) + s->nbl_margin);
+  return init_cells(s, 1.0, NULL, NULL);
 }
 
 /* cell_coord (src/imd_geom_3d.c:1054-1074) */
@@ -1140,6 +1158,138 @@ int orc_glok_steps(orc_sys_t *s, orc_glok_t *g, int step0, int nsteps, double *o
       o[5] = g->mix;
       o[6] = g->PxF;
       o[7] = g->glok_start;
+    }
+    orc_check_nblist(s);
+  }
+  return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* NPT, isotropic (src/imd_integrate.c:1403-1447, :1475-1728)                 */
+/* ------------------------------------------------------------------------ */
+
+void orc_npt_defaults(orc_npt_t *np) {
+  memset(np, 0, sizeof *np);
+  np->cell_size_tolerance = 0.05;   /* src/globals.h:570 */
+}
+
+int orc_npt_begin(orc_sys_t *s, orc_npt_t *np) {
+  if (make_box(s)) return 1;
+  np->volume_init = s->volume;
+  int rc = init_cells(s, SQR(1.0 + np->cell_size_tolerance), np->min_height, np->max_height);
+  s->have_valid_nbl = 0;
+  return rc;
+}
+
+/* The buffer-cell copies of the next calc_forces use the box as it is then
+ * (send_cells, src/imd_comm_force_3d.c:247-358): each ghost's copy vector
+ * is one of 0, +-box_x, +-box_y, +-box_z of the old box, and becomes the
+ * same vector of the new box. */
+static void rescale_ghost_shifts(orc_sys_t *s, double old[3][3]) {
+  for (int g = s->n; g < s->next; g++) {
+    double *v = s->eshift + 3 * g;
+    for (int a = 0; a < 3; a++) {
+      int hit = 0;
+      if (v[0] == old[a][0] && v[1] == old[a][1] && v[2] == old[a][2]) hit = 1;
+      else if (v[0] == -old[a][0] && v[1] == -old[a][1] && v[2] == -old[a][2]) hit = -1;
+      if (hit) {
+        for (int c = 0; c < 3; c++) v[c] = hit > 0 ? s->box[a][c] : -s->box[a][c];
+        break;
+      }
+    }
+  }
+}
+
+int orc_move_atoms_npt_iso(orc_sys_t *s, orc_npt_t *np, int steps) {
+  const int n = s->n;
+  const double dt = s->timestep;
+  const double nact = np->nactive > 0 ? (double)np->nactive : 3.0 * n;
+  double Ekin_new = 0.0, fnorm = 0.0, fmax2 = 0.0;
+  if (steps == np->steps_min) {
+    /* calc_dyn_pressure: twice the kinetic energy, per component */
+    double dx = 0.0, dy = 0.0, dz = 0.0;
+    for (int nn = 0; nn < n; nn++) {
+      int i = s->order[nn];
+      const double *p = s->p + 3 * i;
+      double tmp = 1.0 / s->mass[i];
+      dx += p[0] * p[0] * tmp;
+      dy += p[1] * p[1] * tmp;
+      dz += p[2] * p[2] * tmp;
+    }
+    np->Ekin_old = dx + dy;
+    np->Ekin_old += dz;
+    if (np->isq_tau_xi == 0.0) np->xi = 0.0;
+  }
+  np->pressure = (np->Ekin_old + s->virial) / (3 * s->volume);
+  np->xi_old = np->xi;
+  np->xi += dt * (np->pressure - np->pressure_ext) * s->volume * np->isq_tau_xi / nact;
+  double pfric = 1.0 - (np->xi_old + np->eta) * dt / 2.0;
+  double pifric = 1.0 / (1.0 + (np->xi + np->eta) * dt / 2.0);
+  double rfric = 1.0 + (np->xi) * dt / 2.0;
+  double rifric = 1.0 / (1.0 - (np->xi) * dt / 2.0);
+  for (int nn = 0; nn < n; nn++) {
+    int i = s->order[nn];
+    double *p = s->p + 3 * i, *f = s->f + 3 * i, *x = s->x + 3 * i;
+    fnorm += f[0] * f[0] + f[1] * f[1] + f[2] * f[2];
+    fmax2 = OMAX(SQR(f[0]), fmax2);
+    fmax2 = OMAX(SQR(f[1]), fmax2);
+    fmax2 = OMAX(SQR(f[2]), fmax2);
+    for (int a = 0; a < 3; a++) p[a] = (pfric * p[a] + dt * f[a]) * pifric;
+    Ekin_new += (p[0] * p[0] + p[1] * p[1] + p[2] * p[2]) / s->mass[i];
+    double tmp = dt / s->mass[i];
+    for (int a = 0; a < 3; a++) x[a] = (rfric * x[a] + p[a] * tmp) * rifric;
+  }
+  s->fnorm = fnorm;
+  s->f_max2 = fmax2;
+  s->tot_kin_energy = (np->Ekin_old + Ekin_new) / 4.0;
+  double ttt = nact * np->temperature;
+  np->eta += dt * (Ekin_new / ttt - 1.0) * np->isq_tau_eta;
+  np->Ekin_old = Ekin_new;
+  /* the box */
+  ttt = (1.0 + np->xi * dt / 2.0) / (1.0 - np->xi * dt / 2.0);
+  if (ttt < 0) return -1;   /* "box size has become negative!" */
+  double old[3][3];
+  memcpy(old, s->box, sizeof old);
+  for (int a = 0; a < 3; a++)
+    for (int c = 0; c < 3; c++) s->box[a][c] *= ttt;
+  if (make_box(s)) return -2;
+  if (s->volume > 8 * np->volume_init) return -4;   /* src/imd_geom_3d.c:93-97 */
+  rescale_ghost_shifts(s, old);
+  int out = 0;
+  for (int a = 0; a < 3; a++)
+    if (s->height[a] < np->min_height[a] || s->height[a] > np->max_height[a]) out = 1;
+  if (out) {
+    if (init_cells(s, SQR(1.0 + np->cell_size_tolerance), np->min_height, np->max_height))
+      return -3;
+    s->have_valid_nbl = 0;
+  }
+  if (steps == np->steps_min) {
+    if (np->use_curr_pressure == 1) {
+      np->pressure_ext = np->pressure;
+      np->use_curr_pressure = 0;
+    }
+    np->d_pressure = (np->pressure_end - np->pressure_ext) / (np->steps_max - np->steps_min);
+  }
+  np->pressure_ext += np->d_pressure;
+  return 0;
+}
+
+int orc_npt_steps(orc_sys_t *s, orc_npt_t *np, int step0, int nsteps, double *out) {
+  for (int st = 0; st < nsteps; st++) {
+    int rc = orc_calc_forces(s);
+    if (rc < 0) return rc;
+    double ep = s->tot_pot_energy;
+    if ((rc = orc_move_atoms_npt_iso(s, np, step0 + st))) return rc;
+    if (out) {
+      double *o = out + 8 * (size_t)st;
+      o[0] = ep;
+      o[1] = s->tot_kin_energy;
+      o[2] = np->xi;
+      o[3] = np->eta;
+      o[4] = np->pressure;
+      o[5] = s->volume;
+      o[6] = s->box[0][0];
+      o[7] = np->pressure_ext;
     }
     orc_check_nblist(s);
   }

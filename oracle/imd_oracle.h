@@ -184,6 +184,31 @@ void orc_move_atoms_glok(orc_sys_t *s, orc_glok_t *g);
  * move_atoms, check_nblist.  Per step 8 values: tot_pot_energy,
  * tot_kin_energy, fnorm, f_max2, timestep, mix, PxF, glok_start */
 int  orc_glok_steps(orc_sys_t *s, orc_glok_t *g, int step0, int nsteps, double *out);
+/* NPT with isotropic box scaling, move_atoms_npt_iso (src/imd_integrate.c:
+ * 1475-1728, the `npt_iso` build: Nose-Hoover eta plus the barostat xi.x).
+ * State and parameters are IMD's globals (src/globals.h:405-407, :566-574). */
+typedef struct {
+  double temperature, isq_tau_eta, eta;
+  double isq_tau_xi, xi, xi_old;
+  double pressure_ext, pressure_end, pressure, d_pressure;
+  double Ekin_old;
+  double volume_init;              /* "system seems to explode!" above 8x */
+  double cell_size_tolerance;
+  double min_height[3], max_height[3];
+  int    use_curr_pressure, steps_min, steps_max;
+  long   nactive;                  /* <= 0: three per atom */
+} orc_npt_t;
+void orc_npt_defaults(orc_npt_t *np);
+/* init_cells again with the NPT tolerance (src/imd_geom_3d.c:128-133), as
+ * IMD sets the grid up for an npt ensemble; the list is rebuilt next */
+int  orc_npt_begin(orc_sys_t *s, orc_npt_t *np);
+/* move_atoms_npt_iso for main_loop step `steps`, then make_box on the
+ * scaled box (a new cell grid when a height leaves its bounds) */
+int  orc_move_atoms_npt_iso(orc_sys_t *s, orc_npt_t *np, int steps);
+/* main_loop steps step0 .. step0+nsteps-1: calc_forces, move_atoms_npt_iso,
+ * check_nblist.  Per step 8 values: tot_pot_energy, tot_kin_energy, xi,
+ * eta, pressure, volume, box_x.x, pressure_ext */
+int  orc_npt_steps(orc_sys_t *s, orc_npt_t *np, int step0, int nsteps, double *out);
 /* main_loop steps with move_atoms of `ensemble` (0 nve, 1 nvt, 2 mik);
  * per step tot_pot_energy, tot_kin_energy and (nvt) eta / (mik) fnorm */
 int  orc_md_steps(orc_sys_t *s, int nsteps, int ensemble, double *epot_out,

@@ -74,6 +74,17 @@ class Glok(C.Structure):
                 ("PxF", C.c_double), ("pnorm", C.c_double)]
 
 
+class Npt(C.Structure):
+    """orc_npt_t: parameters and state of ensemble npt_iso."""
+    _fields_ = [("temperature", C.c_double), ("isq_tau_eta", C.c_double), ("eta", C.c_double),
+                ("isq_tau_xi", C.c_double), ("xi", C.c_double), ("xi_old", C.c_double),
+                ("pressure_ext", C.c_double), ("pressure_end", C.c_double),
+                ("pressure", C.c_double), ("d_pressure", C.c_double), ("Ekin_old", C.c_double),
+                ("volume_init", C.c_double), ("cell_size_tolerance", C.c_double), ("min_height", C.c_double * 3),
+                ("max_height", C.c_double * 3), ("use_curr_pressure", C.c_int),
+                ("steps_min", C.c_int), ("steps_max", C.c_int), ("nactive", C.c_long)]
+
+
 _lib = None
 
 
@@ -101,6 +112,9 @@ def lib() -> C.CDLL:
         L.orc_nve_steps.argtypes = [C.POINTER(Sys), C.c_int, _dp, _dp]
         L.orc_md_steps.argtypes = [C.POINTER(Sys), C.c_int, C.c_int, _dp, _dp, _dp]
         L.orc_glok_defaults.argtypes = [C.POINTER(Glok)]
+        L.orc_npt_defaults.argtypes = [C.POINTER(Npt)]
+        L.orc_npt_begin.argtypes = [C.POINTER(Sys), C.POINTER(Npt)]
+        L.orc_npt_steps.argtypes = [C.POINTER(Sys), C.POINTER(Npt), C.c_int, C.c_int, _dp]
         L.orc_glok_steps.argtypes = [C.POINTER(Sys), C.POINTER(Glok), C.c_int, C.c_int, _dp]
         L.orc_cg_step.argtypes = [C.POINTER(Sys), C.c_int]
         L.orc_cg_relax.argtypes = [C.POINTER(Sys), C.c_double, C.c_int, _dp]
@@ -290,6 +304,26 @@ class OracleSystem:
         rc = L.orc_glok_steps(C.byref(self.s), C.byref(state), step0, nsteps, _ptr(out))
         if rc < 0:
             raise RuntimeError("oracle glok steps failed (%d)" % rc)
+        return out, state
+
+    def npt(self, nsteps: int, step0: int = 0, state: Npt = None, **params):
+        """main_loop steps of ensemble npt_iso from step `step0`.  params:
+        the orc_npt_t fields (IMD's names); a new state re-initialises the
+        cell grid with the NPT tolerance as IMD does for this ensemble.
+        Returns (per-step array of tot_pot_energy, tot_kin_energy, xi, eta,
+        pressure, volume, box_x.x, pressure_ext; the state)."""
+        L = lib()
+        if state is None:
+            state = Npt()
+            L.orc_npt_defaults(C.byref(state))
+            for k, v in params.items():
+                setattr(state, k, v)
+            if L.orc_npt_begin(C.byref(self.s), C.byref(state)):
+                raise ValueError("oracle npt grid set-up failed")
+        out = np.empty((nsteps, 8))
+        rc = L.orc_npt_steps(C.byref(self.s), C.byref(state), step0, nsteps, _ptr(out))
+        if rc < 0:
+            raise RuntimeError("oracle npt steps failed (%d)" % rc)
         return out, state
 
     def set_nvt(self, temperature: float, isq_tau_eta: float, eta: float = 0.0) -> None:

@@ -19,6 +19,7 @@
  *             (move_atoms of the parameter file's ensemble: nve, nvt, mik)
  *   glok K  : K main_loop steps of the glok ensemble (update_glok before
  *             move_atoms) from steps_min
+ *   npt K   : K main_loop steps of ensemble npt_iso from steps_min
  *   cg K F  : reset_cg, then cg_step until max per-atom |F| <= F
  *   time K  : K NVE steps, print cpu seconds
  */
@@ -254,6 +255,28 @@ int main(int argc, char **argv) {
     fclose(out);
     sprintf(fname, "%s.final", pre);
     dump_state(fname);
+  }
+#endif
+#ifdef NPT
+  else if (0 == strcmp(mode, "npt")) {
+    /* K main_loop steps of ensemble npt_iso from steps_min: calc_forces,
+     * move_atoms (box scaled inside), check_nblist */
+    sprintf(fname, "%s.steps", pre);
+    FILE *out = fopen(fname, "w");
+    for (steps = steps_min; steps < steps_min + nsteps; steps++) {
+      calc_forces(steps);
+      double ep = tot_pot_energy;
+      move_atoms();
+      fprintf(out, "%d %.17e %.17e %ld %.17e %.17e %.17e %.17e %.17e %.17e\n", steps, ep,
+              tot_kin_energy, (long)nbl_count, xi.x, eta, pressure, volume, box_x.x,
+              pressure_ext.x);
+      check_nblist();
+    }
+    fclose(out);
+    sprintf(fname, "%s.final", pre);
+    dump_state(fname);
+    sprintf(fname, "%s.finalbox", pre);
+    dump_box(fname);
   }
 #endif
 #ifdef CG

@@ -35,10 +35,12 @@ Fixtures (all sorted by atom number):
   cu_fire, cu_glok   a perturbed Cu crystal with two vacancies relaxed by
               the glok ensemble of the `fire` build (300 steps, adaptive time
               step and mixing) and of the `glok` build (200 steps)
+  cu_npt      Cu _fcc 8^3 at 300 K, 200 steps of ensemble npt_iso with the
+              external pressure ramped from 0.01 to 0.005 eV/A^3
 
 `python tests/golden/make_golden.py stress` writes the stress fixtures only,
 `... ensembles` the NVT / MIK ones, `... lj1000` the 1000-step LJ run,
-`... glok` the glok ones.
+`... glok` the glok ones, `... npt` the NPT one.
 """
 from __future__ import annotations
 
@@ -426,6 +428,48 @@ def glok_cases() -> None:
               "restarts", len(np.unique(steps[:, 9])), "nPxF", steps[-1, 10])
 
 
+def npt_case() -> None:
+    """ensemble npt_iso (move_atoms_npt_iso, src/imd_integrate.c:1475-1728)
+    of the reference's `npt_iso` build: Cu _fcc 8^3 at 300 K from IMD's
+    generator and maxwell, external pressure ramped from 0.01 to 0.005
+    eV/A^3 over 200 steps; per step the energies, xi, eta, the pressure,
+    the volume and the box."""
+    subprocess.run(["make", "-s", "-C", ORACLE, "ref"], check=True)
+    tmp = tempfile.mkdtemp(prefix="imdgold_npt")
+    cu = tuple(os.path.join(HERE, "cu" + e) for e in (".pt", ".rho", ".emb"))
+    nsteps = 200
+    prm = dict(temperature=0.0258520, tau_eta=10.0, tau_xi=20.0, pressure_start=0.01,
+               pressure_end=0.005)
+    p = os.path.join(tmp, "cu_npt.param")
+    wl.write_param(p, coordname="_fcc", box_param=[8, 8, 8], box_unit=3.615,
+                   ensemble="npt_iso", starttemp=prm["temperature"], tau_eta=prm["tau_eta"],
+                   tau_xi=prm["tau_xi"], pressure_start=prm["pressure_start"],
+                   pressure_end=prm["pressure_end"], outfiles=os.path.join(tmp, "o"),
+                   ntypes=1, masses=63.546, pbc_dirs=[1, 1, 1], timestep=0.0982266,
+                   maxsteps=nsteps - 1, seed=2, core_potential_file=cu[0],
+                   **{"atomic_e-density_file": cu[1]}, embedding_energy_file=cu[2],
+                   nbl_margin=0.4, eng_int=0, checkpt_int=100000000)
+    pre = os.path.join(tmp, "cu_npt")
+    run("npt_iso_nbl_eam", p, "npt", pre, nsteps)
+    st0 = load_state(pre + ".state0")
+    stf = load_state(pre + ".final")
+    steps = np.loadtxt(pre + ".steps")
+    box, gdim, cellsz = load_box(pre + ".box")
+    boxf, gdimf, _ = load_box(pre + ".finalbox")
+    d = dict(box=box, gdim=gdim, cellsz=cellsz, number=st0["number"], type=st0["type"],
+             mass=st0["mass"], x0=st0["x"], p0=st0["p"], epot=steps[:, 1], ekin=steps[:, 2],
+             nbl_count=steps[:, 3], xi=steps[:, 4], eta=steps[:, 5], pressure=steps[:, 6],
+             volume=steps[:, 7], box_xx=steps[:, 8], pressure_ext=steps[:, 9],
+             x_final=stf["x"], p_final=stf["p"], box_final=boxf, gdim_final=gdimf,
+             dt=0.0982266, skin=0.4, temperature=prm["temperature"],
+             isq_tau_eta=1.0 / prm["tau_eta"] ** 2, isq_tau_xi=1.0 / prm["tau_xi"] ** 2,
+             pressure_start=prm["pressure_start"], pressure_end=prm["pressure_end"],
+             steps_max=nsteps - 1)
+    np.savez_compressed(os.path.join(HERE, "cu_npt.npz"), **d)
+    print("cu_npt volume", steps[[0, -1], 7], "pressure", steps[[0, -1], 6], "gdim", gdim,
+          gdimf, "rebuilds", steps[-1, 3])
+
+
 # IMD's INIT values of the glok parameters (src/globals.h:580-600)
 GLOK_PARAM_DEFAULTS = dict(glok_ekin_threshold=100.0, glok_fmaxcrit=10000.0, glok_mix=0.0,
                            glok_mixdec=1.0, glok_incfac=1.02, glok_decfac=0.5,
@@ -475,9 +519,12 @@ if __name__ == "__main__":
         lj1000_case()
     elif len(sys.argv) > 1 and sys.argv[1] == "glok":
         glok_cases()
+    elif len(sys.argv) > 1 and sys.argv[1] == "npt":
+        npt_case()
     else:
         main()
         stress_cases()
         ensemble_cases()
         lj1000_case()
         glok_cases()
+        npt_case()

@@ -216,6 +216,56 @@ def test_glok_matches_reference(name):
         assert g["timestep"].max() > g["timestep"][0] and int(g["npxf"][-1]) > 0
 
 
+def npt_params(g) -> dict:
+    """The npt_iso parameters of a golden run (IMD's names)."""
+    return dict(temperature=float(g["temperature"]), isq_tau_eta=float(g["isq_tau_eta"]),
+                isq_tau_xi=float(g["isq_tau_xi"]), pressure_ext=float(g["pressure_start"]),
+                pressure_end=float(g["pressure_end"]), steps_min=0,
+                steps_max=int(g["steps_max"]))
+
+
+def test_npt_iso_matches_reference():
+    """move_atoms_npt_iso with the box scaled every step, 200 steps against
+    the reference's `npt_iso` build: energies, xi, eta, the pressure and the
+    box to 1e-12 relative, final positions to 1e-10 A."""
+    g = golden("cu_npt")
+    s = OracleSystem(g["box"], g["x0"], g["type"], g["mass"], g["number"], 1, tables("cu"),
+                     True, float(g["skin"]), timestep=float(g["dt"]), p=g["p0"])
+    out, st = s.npt(len(g["epot"]), 0, **npt_params(g))
+    for j, k in enumerate(["epot", "ekin", "xi", "eta", "pressure", "volume", "box_xx",
+                           "pressure_ext"]):
+        np.testing.assert_allclose(out[:, j], g[k], rtol=1e-12, atol=1e-15, err_msg=k)
+    box = np.array(s.s.box)
+    np.testing.assert_allclose(box, g["box_final"], rtol=1e-12, atol=0)
+    d = s.x - g["x_final"]
+    d -= np.round(d @ np.linalg.inv(box)) @ box
+    assert np.abs(d).max() < 1e-10
+    # the run changes the volume by far more than the tolerance of the bars
+    assert g["volume"][-1] / g["volume"][0] - 1.0 > 5e-3
+
+
+def test_npt_iso_new_cell_grid():
+    """A box that shrinks out of its height bounds gets a new cell grid
+    (make_box calling init_cells, src/imd_geom_3d.c:82-86) and a new list;
+    the forces on the new grid equal those of a fresh system on that box."""
+    g = golden("cu_npt")
+    # a crystal stretched by 9.5 %, pulled further by a negative pressure: its
+    # box grows past the largest height of the 3x3x3 grid within 20 steps
+    s = OracleSystem(g["box"] * 1.095, g["x0"] * 1.095, g["type"], g["mass"], g["number"], 1,
+                     tables("cu"), True, float(g["skin"]), timestep=float(g["dt"]), p=g["p0"])
+    prm = npt_params(g)
+    prm.update(pressure_ext=-0.2, pressure_end=-0.2, isq_tau_xi=1.0 / 25.0, steps_max=19)
+    out, st = s.npt(20, 0, **prm)
+    assert list(s.s.gdim) == [4, 4, 4]               # 3x3x3 at the start
+    s.calc_forces()
+    box = np.array(s.s.box)
+    t = OracleSystem(box, s.x.copy(), g["type"], g["mass"], g["number"], 1, tables("cu"),
+                     True, float(g["skin"]), timestep=float(g["dt"]), p=s.p.copy())
+    t.calc_forces()
+    assert rel_rms(s.f, t.f) < 1e-12
+    assert abs(s.epot_total - t.epot_total) <= 1e-12 * abs(t.epot_total)
+
+
 def test_lj_1000_steps_segmentwise():
     """The plain-method LJ run over all 1000 steps, step by step: from each
     of the reference's snapshots (every 250 steps) the oracle reproduces the
