@@ -53,6 +53,21 @@ class GlokState(C.Structure):
                 ("glok_start", C.c_int), ("glok_int", C.c_int), ("nPxF", C.c_int)]
 
 
+class NptParams(C.Structure):
+    """imdgpu_npt_params: IMD's npt_iso parameters."""
+    _fields_ = [("temperature", C.c_double), ("isq_tau_eta", C.c_double), ("eta", C.c_double),
+                ("isq_tau_xi", C.c_double), ("xi", C.c_double), ("pressure_ext", C.c_double),
+                ("pressure_end", C.c_double), ("use_curr_pressure", C.c_int),
+                ("steps_min", C.c_int), ("steps_max", C.c_int), ("nactive", C.c_long),
+                ("cell_size_tolerance", C.c_double)]
+
+
+class NptState(C.Structure):
+    """imdgpu_npt_state: IMD's globals of ensemble npt_iso."""
+    _fields_ = [("xi", C.c_double), ("eta", C.c_double), ("pressure", C.c_double),
+                ("pressure_ext", C.c_double), ("volume", C.c_double), ("box", C.c_double * 9)]
+
+
 class Timing(C.Structure):
     _fields_ = [("ms_total", C.c_double), ("ms_density", C.c_double),
                 ("ms_force", C.c_double), ("ms_integrate", C.c_double),
@@ -132,6 +147,10 @@ def lib() -> C.CDLL:
         L.imdgpu_set_glok.argtypes = [vp, C.POINTER(GlokParams), C.c_double]
         L.imdgpu_move_atoms_glok.argtypes = [vp, C.c_int]
         L.imdgpu_get_glok.argtypes = [vp, C.POINTER(GlokState)]
+        L.imdgpu_npt_defaults.argtypes = [C.POINTER(NptParams)]
+        L.imdgpu_set_npt.argtypes = [vp, C.POINTER(NptParams)]
+        L.imdgpu_move_atoms_npt_iso.argtypes = [vp, C.c_int, C.c_double]
+        L.imdgpu_get_npt.argtypes = [vp, C.POINTER(NptState)]
         L.imdgpu_set_blocks.argtypes = [vp, C.c_int, C.c_int]
         L.imdgpu_batch_set_autotune.argtypes = [vp, C.c_int]
         L.imdgpu_batch_positions.argtypes = [vp, _dp]
@@ -339,6 +358,30 @@ class GpuSystem:
             if relaxed:
                 return steps - steps_min + 1, True
         return maxsteps, False
+
+    def set_npt(self, **params) -> None:
+        """Start an npt_iso phase.  params: temperature, isq_tau_eta, eta,
+        isq_tau_xi, xi, pressure_ext (IMD's pressure_start), pressure_end,
+        use_curr_pressure, steps_min, steps_max, nactive,
+        cell_size_tolerance; IMD's defaults for the rest."""
+        prm = NptParams()
+        _check(lib().imdgpu_npt_defaults(C.byref(prm)), "npt_defaults")
+        for k, v in params.items():
+            if not hasattr(prm, k):
+                raise TypeError("unknown npt parameter %r" % k)
+            setattr(prm, k, v)
+        _check(lib().imdgpu_set_npt(self.h, C.byref(prm)), "set_npt")
+
+    def move_atoms_npt_iso(self, steps: int, timestep: float) -> NptState:
+        """move_atoms_npt_iso for main_loop step `steps`; returns the NPT
+        state after it (xi, eta, pressure, pressure_ext, volume, box)."""
+        _check(lib().imdgpu_move_atoms_npt_iso(self.h, steps, timestep), "move_atoms_npt_iso")
+        return self.npt_state()
+
+    def npt_state(self) -> NptState:
+        st = NptState()
+        _check(lib().imdgpu_get_npt(self.h, C.byref(st)), "get_npt")
+        return st
 
     def glok_state(self) -> GlokState:
         st = GlokState()

@@ -198,6 +198,16 @@ struct imdgpu_sys {
   double glok_fnorm = 0.0, glok_fmax2 = 0.0, glok_ekin = 0.0;
   double *d_glok = nullptr;   // sum P.F/m, sum |P/m|^2 of the last move
 
+  // npt_iso: parameters, IMD's globals of move_atoms_npt_iso, the grid
+  // tolerance factor of init_cells and the height bounds of the grid
+  imdgpu_npt_params npt_prm{};
+  bool npt_set = false;
+  double npt_xi = 0.0, npt_eta = 0.0, npt_pressure = 0.0, npt_pext = 0.0, npt_dp = 0.0;
+  double npt_ekin_old = 0.0, volume_init = 0.0;
+  double cell_tol2 = 1.0;
+  double min_height[3] = {0.0, 0.0, 0.0}, max_height[3] = {0.0, 0.0, 0.0};
+  double *d_npt = nullptr;    // 3: calc_dyn_pressure sums / twice the new E_kin
+
   // STRESS_TENS: per ext atom xx yy zz yz zx xy
   double *d_stress = nullptr;
   size_t stress_cap = 0;
@@ -847,6 +857,118 @@ __global__ void k_finalize_glok(const double *partial, int nb, DevScalars *sc, d
   }
 }
 
+// calc_dyn_pressure (src/imd_integrate.c:1403-1447): per block the sums of
+// p_a p_a / m over the three components
+__global__ void __launch_bounds__(BS_VEC) k_dyn_press(SysView v, double *partial) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double r[3] = {0.0, 0.0, 0.0};
+  if (i < v.n) {
+    const double4 p = v.mom[i];
+    const double tmp = 1.0 / p.w;
+    r[0] = dmul(dmul(p.x, p.x), tmp);
+    r[1] = dmul(dmul(p.y, p.y), tmp);
+    r[2] = dmul(dmul(p.z, p.z), tmp);
+  }
+  __shared__ double sh[3][BS_VEC / 32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < 3; k++) r[k] = warp_sum(r[k]);
+  if (lane == 0) {
+#pragma unroll
+    for (int k = 0; k < 3; k++) sh[k][w] = r[k];
+  }
+  __syncthreads();
+  if (threadIdx.x < 3) {
+    double a = 0.0;
+    for (int j = 0; j < BS_VEC / 32; j++) a += sh[threadIdx.x][j];
+    partial[3 * (size_t)blockIdx.x + threadIdx.x] = a;
+  }
+}
+__global__ void k_finalize3(const double *partial, int nb, double *out3) {
+  const int lane = threadIdx.x;
+  double r[3] = {0.0, 0.0, 0.0};
+  for (int b = lane; b < nb; b += 32) {
+#pragma unroll
+    for (int k = 0; k < 3; k++) r[k] += partial[3 * (size_t)b + k];
+  }
+#pragma unroll
+  for (int k = 0; k < 3; k++) r[k] = warp_sum(r[k]);
+  if (lane == 0)
+    for (int k = 0; k < 3; k++) out3[k] = r[k];
+}
+
+// move_atoms_npt_iso (src/imd_integrate.c:1475-1728, no UNIAX): momenta
+// (pfric p + dt F) pifric, positions (rfric x + p dt/m) rifric, in IMD's
+// operation order, unfused; no restrictions (IMD applies none here).  Per
+// block: sums of |F|^2 and of twice the new kinetic energy, maxima of the
+// force component and of the displacement (the NVT partial layout, the
+// first slot unused).
+__global__ void __launch_bounds__(BS_VEC) k_npt(SysView v, double dt, double pfric,
+                                                double pifric, double rfric, double rifric,
+                                                double *partial) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double r[5] = {0.0, 0.0, 0.0, 0.0, 0.0};   // - e2 fn | fm dm
+  if (i < v.n) {
+    double4 p = v.mom[i], f = v.frc[i], x = v.pos[i];
+    const double m = p.w;
+    r[2] = dadd(dadd(dmul(f.x, f.x), dmul(f.y, f.y)), dmul(f.z, f.z));
+    r[3] = fmax(fmax(f.x * f.x, f.y * f.y), f.z * f.z);
+    p.x = dmul(dadd(dmul(pfric, p.x), dmul(dt, f.x)), pifric);
+    p.y = dmul(dadd(dmul(pfric, p.y), dmul(dt, f.y)), pifric);
+    p.z = dmul(dadd(dmul(pfric, p.z), dmul(dt, f.z)), pifric);
+    r[1] = dadd(dadd(dmul(p.x, p.x), dmul(p.y, p.y)), dmul(p.z, p.z)) / m;
+    const double tmp = dt / m;
+    x.x = dmul(dadd(dmul(rfric, x.x), dmul(p.x, tmp)), rifric);
+    x.y = dmul(dadd(dmul(rfric, x.y), dmul(p.y, tmp)), rifric);
+    x.z = dmul(dadd(dmul(rfric, x.z), dmul(p.z, tmp)), rifric);
+    v.mom[i] = p;
+    v.pos[i] = x;
+    const double4 rf = v.ref[i];
+    r[4] = r2_exact(dsub(x.x, rf.x), dsub(x.y, rf.y), dsub(x.z, rf.z));
+  }
+  __shared__ double sh[5][BS_VEC / 32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < 5; k++) r[k] = k < 3 ? warp_sum(r[k]) : warp_max(r[k]);
+  if (lane == 0) {
+#pragma unroll
+    for (int k = 0; k < 5; k++) sh[k][w] = r[k];
+  }
+  __syncthreads();
+  if (threadIdx.x < 5) {
+    const int k = threadIdx.x;
+    double a = 0.0;
+    for (int j = 0; j < BS_VEC / 32; j++) a = k < 3 ? a + sh[k][j] : fmax(a, sh[k][j]);
+    partial[5 * (size_t)blockIdx.x + k] = a;
+  }
+}
+
+// totals of the NPT partials: tot_kin_energy = (Ekin_old + Ekin_new) / 4;
+// out = Ekin_new (twice the new kinetic energy)
+__global__ void k_finalize_npt(const double *partial, int nb, DevScalars *sc, double skin2,
+                               double ekin_old, double *out) {
+  const int lane = threadIdx.x;
+  double b = 0, c = 0, d = 0, e = 0;
+  for (int k = lane; k < nb; k += 32) {
+    b += partial[5 * k + 1];
+    c += partial[5 * k + 2];
+    d = fmax(d, partial[5 * k + 3]);
+    e = fmax(e, partial[5 * k + 4]);
+  }
+  b = warp_sum(b);
+  c = warp_sum(c);
+  d = warp_max(d);
+  e = warp_max(e);
+  if (lane == 0) {
+    sc->ekin = (ekin_old + b) / 4.0;
+    sc->fnorm = c;
+    sc->fmax2 = d;
+    sc->maxdisp2 = e;
+    if (e > skin2) sc->rebuild = 1;
+    *out = b;
+  }
+}
+
 // check_nblist alone (CG path)
 __global__ void __launch_bounds__(BS_VEC) k_check(SysView v, double *partial) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1168,6 +1290,7 @@ static SysView view(imdgpu_sys *s) {
 
 static ForceTabs ftabs(imdgpu_sys *s) {
   ForceTabs t;
+  memset(&t, 0, sizeof t);
   t.pair = s->dtab[0];
   t.rho = s->dtab[1];
   t.embed = s->dtab[2];
@@ -1198,7 +1321,8 @@ static uint32_t spread3(uint32_t x) {
 
 // make_box (src/imd_geom_3d.c:52-106), init_cells (:113-200),
 // make_cell_lists (:823-947) and the buffer cells filled by send_cells.
-static int setup_geometry(imdgpu_sys *s) {
+// make_box (src/imd_geom_3d.c:52-80): tbox, volume, squared heights
+static int make_box(imdgpu_sys *s) {
   auto vp = [](const double *u, const double *v, double *w) {
     w[0] = u[1] * v[2] - u[2] * v[1];
     w[1] = u[2] * v[0] - u[0] * v[2];
@@ -1213,19 +1337,30 @@ static int setup_geometry(imdgpu_sys *s) {
   for (int a = 0; a < 3; a++)
     for (int c = 0; c < 3; c++) s->tbox[a][c] /= s->volume;
   for (int a = 0; a < 3; a++) s->height[a] = 1.0 / sp(s->tbox[a], s->tbox[a]);
+  return IMDGPU_OK;
+}
+
+static int setup_geometry(imdgpu_sys *s) {
+  if (int rc = make_box(s)) return rc;
   if (s->list_r2_override > 0)
     s->cellsz = s->list_r2_override;
   else {
     const double r = std::sqrt((double)s->tab_cellsz) + s->nbl_margin;
     s->cellsz = r * r;
   }
+  // init_cells (src/imd_geom_3d.c:128-206): cell_tol2 is (1 + cell_size_tol)^2
+  // for an npt ensemble and 1 otherwise; the heights between which the grid
+  // stays are kept for make_box
   for (int a = 0; a < 3; a++) {
-    const double scale = std::sqrt(1.0 * s->cellsz / s->height[a]);
+    const double scale = std::sqrt(s->cell_tol2 * s->cellsz / s->height[a]);
     s->gdim[a] = (int)(1.0 / scale);
     if (s->gdim[a] < 1)
       return fail(IMDGPU_ERR_GEOM, "global_cell_dim too small, need at least 1");
     if (s->gdim[a] > 1000) return fail(IMDGPU_ERR_GEOM, "more than 1000 cells per dimension");
     s->cdim[a] = s->gdim[a] + 2;
+    const int g = s->gdim[a], g1 = s->gdim[a] + 1;
+    s->min_height[a] = s->cellsz * (g * g);
+    s->max_height[a] = s->cellsz * (g1 * g1) * s->cell_tol2;
   }
   const int gx = s->gdim[0], gy = s->gdim[1], gz = s->gdim[2];
   const int cx = s->cdim[0], cy = s->cdim[1], cz = s->cdim[2];
@@ -1800,6 +1935,7 @@ int imdgpu_destroy(imdgpu_sys *s) {
   dfree(s->d_stress);
   dfree(s->d_e2);
   dfree(s->d_glok);
+  dfree(s->d_npt);
   dfree(s->d_sys_short);
   dfree(s->d_atom_sys); dfree(s->d_aoff); dfree(s->d_sgdim); dfree(s->d_scdim); dfree(s->d_scoff);
   dfree(s->d_sys_done); dfree(s->d_ndone); dfree(s->d_sbox); dfree(s->d_stbox); dfree(s->d_cs);
@@ -2434,6 +2570,127 @@ int imdgpu_move_atoms_glok(imdgpu_sys *s, int steps) {
   return IMDGPU_OK;
 }
 
+int imdgpu_npt_defaults(imdgpu_npt_params *prm) {
+  if (!prm) return fail(IMDGPU_ERR_ARG, "null");
+  memset(prm, 0, sizeof *prm);
+  prm->cell_size_tolerance = 0.05;
+  return IMDGPU_OK;
+}
+
+static void drop_nve_graph(imdgpu_sys *s) {
+  if (s->gexec) cudaGraphExecDestroy(s->gexec);
+  s->gexec = nullptr;
+  s->gkey.clear();
+}
+
+// A new npt_iso phase: IMD's globals xi, eta, pressure_ext as given; the
+// grid is set up again with the NPT tolerance (init_cells,
+// src/imd_geom_3d.c:128-133) at the next calc_forces.
+int imdgpu_set_npt(imdgpu_sys *s, const imdgpu_npt_params *prm) {
+  if (!s || !s->atoms_set) return fail(IMDGPU_ERR_STATE, "atoms not set");
+  if (!prm) return fail(IMDGPU_ERR_ARG, "null");
+  if (s->nsys > 0) return fail(IMDGPU_ERR_STATE, "npt: one system, not a batch");
+  if (s->precision != IMDGPU_FP64) return fail(IMDGPU_ERR_STATE, "npt: FP64 precision only");
+  if (!(prm->temperature > 0.0) || prm->isq_tau_eta < 0.0 || prm->isq_tau_xi < 0.0)
+    return fail(IMDGPU_ERR_ARG, "npt: temperature > 0, isq_tau_eta and isq_tau_xi >= 0");
+  if (prm->steps_max <= prm->steps_min)
+    return fail(IMDGPU_ERR_ARG, "npt: steps_max > steps_min (the pressure ramp divides by it)");
+  if (!(prm->cell_size_tolerance >= 0.0)) return fail(IMDGPU_ERR_ARG, "npt: cell_size_tolerance >= 0");
+  if (int rc = make_box(s)) return rc;
+  s->npt_prm = *prm;
+  s->npt_xi = prm->xi;
+  s->npt_eta = prm->eta;
+  s->npt_pext = prm->pressure_ext;
+  s->npt_pressure = s->npt_dp = s->npt_ekin_old = 0.0;
+  s->volume_init = s->volume;
+  s->cell_tol2 = (1.0 + prm->cell_size_tolerance) * (1.0 + prm->cell_size_tolerance);
+  s->geom_ready = false;
+  s->npt_set = true;
+  return IMDGPU_OK;
+}
+
+int imdgpu_get_npt(imdgpu_sys *s, imdgpu_npt_state *st) {
+  if (!s || !st) return fail(IMDGPU_ERR_ARG, "null");
+  st->xi = s->npt_xi;
+  st->eta = s->npt_eta;
+  st->pressure = s->npt_pressure;
+  st->pressure_ext = s->npt_pext;
+  st->volume = s->volume;
+  for (int a = 0; a < 3; a++)
+    for (int c = 0; c < 3; c++) st->box[3 * a + c] = s->box[a][c];
+  return IMDGPU_OK;
+}
+
+// move_atoms_npt_iso (src/imd_integrate.c:1475-1728): the scalars on the
+// host in IMD's order, the atoms on the device, then the box scaled and
+// make_box (src/imd_geom_3d.c:52-97) with a new grid when a height leaves
+// its bounds.
+int imdgpu_move_atoms_npt_iso(imdgpu_sys *s, int steps, double timestep) {
+  if (!s || !s->atoms_set) return fail(IMDGPU_ERR_STATE, "atoms not set");
+  if (!s->npt_set) return fail(IMDGPU_ERR_STATE, "imdgpu_set_npt first");
+  if (!s->geom_ready || s->nbcap == 0)
+    return fail(IMDGPU_ERR_STATE, "move_atoms before the first calc_forces");
+  if (int rcf = batch_full(s)) return rcf;
+  const imdgpu_npt_params &P = s->npt_prm;
+  const double dt = timestep;
+  const double nact = P.nactive > 0 ? (double)P.nactive : 3.0 * s->n;
+  if (!s->d_npt) CK(dalloc(&s->d_npt, 3));
+  SysView v = view(s);
+  const int nb = nblk(s->n, BS_VEC);
+  if (steps == P.steps_min) {
+    // calc_dyn_pressure: twice the kinetic energy, per component
+    k_dyn_press<<<nb, BS_VEC, 0, s->st>>>(v, s->partial);
+    k_finalize3<<<1, 32, 0, s->st>>>(s->partial, nb, s->d_npt);
+    CK(cudaGetLastError());
+    double d3[3];
+    CK(cudaMemcpyAsync(d3, s->d_npt, sizeof d3, cudaMemcpyDeviceToHost, s->st));
+    CK(cudaStreamSynchronize(s->st));
+    s->npt_ekin_old = d3[0] + d3[1];
+    s->npt_ekin_old += d3[2];
+    if (P.isq_tau_xi == 0.0) s->npt_xi = 0.0;
+  }
+  // the virial of the last calc_forces
+  if (!s->hsc_valid) {
+    if (int rc = read_back(s)) return rc;
+  }
+  s->npt_pressure = (s->npt_ekin_old + s->hsc->virial) / (3 * s->volume);
+  const double xi_old = s->npt_xi;
+  s->npt_xi += dt * (s->npt_pressure - s->npt_pext) * s->volume * P.isq_tau_xi / nact;
+  const double xi = s->npt_xi, eta = s->npt_eta;
+  const double pfric = 1.0 - (xi_old + eta) * dt / 2.0;
+  const double pifric = 1.0 / (1.0 + (xi + eta) * dt / 2.0);
+  const double rfric = 1.0 + (xi) * dt / 2.0;
+  const double rifric = 1.0 / (1.0 - (xi) * dt / 2.0);
+  k_npt<<<nb, BS_VEC, 0, s->st>>>(v, dt, pfric, pifric, rfric, rifric, s->partial);
+  k_finalize_npt<<<1, 32, 0, s->st>>>(s->partial, nb, s->dsc, v.skin2, s->npt_ekin_old, s->d_npt);
+  CK(cudaGetLastError());
+  double ekin_new = 0.0;
+  CK(cudaMemcpyAsync(&ekin_new, s->d_npt, sizeof(double), cudaMemcpyDeviceToHost, s->st));
+  if (int rc = read_back(s)) return rc;
+  const double ttt_eta = nact * P.temperature;
+  s->npt_eta += dt * (ekin_new / ttt_eta - 1.0) * P.isq_tau_eta;
+  s->npt_ekin_old = ekin_new;
+  // the box; ghosts take it from the next launch on
+  const double ttt = (1.0 + xi * dt / 2.0) / (1.0 - xi * dt / 2.0);
+  if (ttt < 0) return fail(IMDGPU_ERR_GEOM, "box size has become negative!");
+  for (int a = 0; a < 3; a++)
+    for (int c = 0; c < 3; c++) s->box[a][c] *= ttt;
+  if (int rc = make_box(s)) return rc;
+  if (s->volume > 8 * s->volume_init) return fail(IMDGPU_ERR_GEOM, "system seems to explode!");
+  drop_nve_graph(s);
+  for (int a = 0; a < 3; a++)
+    if (s->height[a] < s->min_height[a] || s->height[a] > s->max_height[a]) s->geom_ready = false;
+  if (steps == P.steps_min) {
+    if (s->npt_prm.use_curr_pressure == 1) {
+      s->npt_pext = s->npt_pressure;
+      s->npt_prm.use_curr_pressure = 0;
+    }
+    s->npt_dp = (P.pressure_end - s->npt_pext) / (P.steps_max - P.steps_min);
+  }
+  s->npt_pext += s->npt_dp;
+  return IMDGPU_OK;
+}
+
 // One chunk of NVE steps with guarded device-side rebuilds.  With profiling
 // on, 8 events per step bracket the step, the rebuild, the density and force
 // kernels and the integrator; the optional L2 flush runs outside them.
@@ -2486,16 +2743,30 @@ static void accumulate_events(imdgpu_sys *s, int k) {
   }
 }
 
-// key of everything a captured chunk bakes in
+static void append_bytes(std::vector<uintptr_t> &k, const void *p, size_t n) {
+  const size_t at = k.size();
+  k.resize(at + (n + sizeof(uintptr_t) - 1) / sizeof(uintptr_t), 0);
+  memcpy(k.data() + at, p, n);
+}
+
+// key of everything a captured chunk bakes in: the kernel arguments (the
+// system view with its box, grid and buffers, the table set) and the
+// launch options
 static std::vector<uintptr_t> graph_key(imdgpu_sys *s, double dt) {
   double dtv = dt;
   uintptr_t dtb;
   memcpy(&dtb, &dtv, sizeof dtb);
-  return {(uintptr_t)s->pos, (uintptr_t)s->mom, (uintptr_t)s->frc, (uintptr_t)s->nbr,
-          (uintptr_t)s->xl, (uintptr_t)s->hist, (uintptr_t)s->flushbuf, (uintptr_t)s->oldx,
-          (uintptr_t)s->ncap, (uintptr_t)s->gcap, (uintptr_t)s->nbcap,
-          (uintptr_t)s->precision, (uintptr_t)s->exact, (uintptr_t)s->profiling,
-          (uintptr_t)s->l2flush_bytes, (uintptr_t)s->geom_full, (uintptr_t)s->nbuf, dtb};
+  std::vector<uintptr_t> k = {
+      (uintptr_t)s->pos, (uintptr_t)s->mom, (uintptr_t)s->frc, (uintptr_t)s->nbr,
+      (uintptr_t)s->xl, (uintptr_t)s->hist, (uintptr_t)s->flushbuf, (uintptr_t)s->oldx,
+      (uintptr_t)s->ncap, (uintptr_t)s->gcap, (uintptr_t)s->nbcap,
+      (uintptr_t)s->precision, (uintptr_t)s->exact, (uintptr_t)s->profiling,
+      (uintptr_t)s->l2flush_bytes, (uintptr_t)s->geom_full, (uintptr_t)s->nbuf, dtb};
+  const SysView v = view(s);
+  append_bytes(k, &v, sizeof v);
+  const ForceTabs t = ftabs(s);
+  append_bytes(k, &t, sizeof t);
+  return k;
 }
 
 // one full chunk (not the last) through a captured graph

@@ -193,6 +193,33 @@ int imdgpu_set_glok(imdgpu_sys *sys, const imdgpu_glok_params *prm, double times
  * calc_forces and check_nblist for `ensemble glok` */
 int imdgpu_move_atoms_glok(imdgpu_sys *sys, int steps);
 int imdgpu_get_glok(imdgpu_sys *sys, imdgpu_glok_state *st);
+/* NPT with isotropic box scaling, move_atoms_npt_iso
+ * (src/imd_integrate.c:1475-1728, build option `npt_iso`): the Nose-Hoover
+ * eta of NVT plus the barostat xi; the box is scaled after every step, and
+ * the cell grid is set up again when a box height leaves its bounds
+ * (make_box, src/imd_geom_3d.c:82-86).  Parameters as IMD parses them
+ * (src/imd_param.c:2562-2599; defaults src/globals.h:566-574).  FP64,
+ * one system. */
+typedef struct {
+  double temperature, isq_tau_eta, eta;  /* as for imdgpu_set_nvt */
+  double isq_tau_xi, xi;
+  double pressure_ext, pressure_end;     /* pressure_start, pressure_end */
+  int use_curr_pressure;                 /* use_current_pressure */
+  int steps_min, steps_max;              /* the ramp of pressure_ext */
+  long nactive;                          /* <= 0: 3 per atom */
+  double cell_size_tolerance;            /* cell_size_tol */
+} imdgpu_npt_params;
+typedef struct {
+  double xi, eta, pressure, pressure_ext, volume;
+  double box[9];                         /* rows box_x, box_y, box_z */
+} imdgpu_npt_state;
+int imdgpu_npt_defaults(imdgpu_npt_params *prm);
+/* start an npt_iso phase; the cell grid is set up with IMD's NPT
+ * tolerance at the next calc_forces */
+int imdgpu_set_npt(imdgpu_sys *sys, const imdgpu_npt_params *prm);
+/* move_atoms_npt_iso for main_loop step `steps` */
+int imdgpu_move_atoms_npt_iso(imdgpu_sys *sys, int steps, double timestep);
+int imdgpu_get_npt(imdgpu_sys *sys, imdgpu_npt_state *st);
 /* nsteps of main_loop (src/imd_main_3d.c:155-870) for ensemble nve:
  * calc_forces, move_atoms_nve, check_nblist, fully on the device.
  * epot/ekin (may be NULL) receive tot_pot_energy and tot_kin_energy of every

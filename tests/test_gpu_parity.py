@@ -482,6 +482,76 @@ def test_glok_relax_stops_where_reference_does():
     assert s.glok_state().timestep == g["timestep"][expect - 1]
 
 
+def test_npt_iso_matches_reference():
+    """ensemble npt_iso on the device, 200 main_loop steps against the
+    reference's `npt_iso` build (the box scaled every step): energies to
+    1e-9, xi, eta, the pressure and the volume to 1e-8 relative, final box
+    to 1e-10 and positions to 1e-8 A."""
+    g = golden("cu_npt")
+    gg = dict(g)
+    gg["x"] = g["x0"]
+    s = gpu_system(gg, "cu", 1, 1, float(g["skin"]), p=g["p0"])
+    s.set_npt(temperature=float(g["temperature"]), isq_tau_eta=float(g["isq_tau_eta"]),
+              isq_tau_xi=float(g["isq_tau_xi"]), pressure_ext=float(g["pressure_start"]),
+              pressure_end=float(g["pressure_end"]), steps_min=0, steps_max=int(g["steps_max"]))
+    dt = float(g["dt"])
+    rows = []
+    for st in range(len(g["epot"])):
+        s.calc_forces(st)
+        ep = s.scalars().tot_pot_energy
+        ns = s.move_atoms_npt_iso(st, dt)
+        rows.append((ep, s.scalars().tot_kin_energy, ns.xi, ns.eta, ns.pressure, ns.volume,
+                     ns.box[0], ns.pressure_ext))
+        s.check_nblist()
+    r = np.array(rows)
+    np.testing.assert_allclose(r[:, 0], g["epot"], rtol=1e-9, atol=0)
+    np.testing.assert_allclose(r[:, 1], g["ekin"], rtol=1e-8, atol=0)
+    for j, k in ((2, "xi"), (3, "eta"), (4, "pressure")):
+        np.testing.assert_allclose(r[:, j], g[k], rtol=1e-8, atol=1e-12, err_msg=k)
+    np.testing.assert_allclose(r[:, 5], g["volume"], rtol=1e-10, atol=0)
+    np.testing.assert_allclose(r[:, 6], g["box_xx"], rtol=1e-10, atol=0)
+    np.testing.assert_allclose(r[:, 7], g["pressure_ext"], rtol=1e-12, atol=0)
+    box = np.array(s.npt_state().box).reshape(3, 3)
+    np.testing.assert_allclose(box, g["box_final"], rtol=1e-10, atol=1e-12)
+    x = s.get_atoms()["x"]
+    d = x - g["x_final"]
+    d -= np.round(d @ np.linalg.inv(box)) @ box
+    assert np.abs(d).max() < 1e-8
+
+
+def test_npt_iso_new_cell_grid_matches_oracle():
+    """A stretched crystal pulled by a negative pressure: its box grows out
+    of the 3x3x3 grid's height bounds, the device sets up a 4x4x4 grid and a
+    new list, and energies and positions follow the oracle (1e-9)."""
+    from oracle import OracleSystem
+    g = golden("cu_npt")
+    box0, x0 = g["box"] * 1.095, g["x0"] * 1.095
+    prm = dict(temperature=float(g["temperature"]), isq_tau_eta=float(g["isq_tau_eta"]),
+               isq_tau_xi=1.0 / 25.0, pressure_ext=-0.2, pressure_end=-0.2, steps_min=0,
+               steps_max=19)
+    o = OracleSystem(box0, x0, g["type"], g["mass"], g["number"], 1, tables("cu"), True,
+                     float(g["skin"]), timestep=float(g["dt"]), p=g["p0"])
+    out, _ = o.npt(20, 0, **prm)
+    assert list(o.s.gdim) == [4, 4, 4]
+    gg = dict(g)
+    gg["box"], gg["x"] = box0, x0
+    s = gpu_system(gg, "cu", 1, 1, float(g["skin"]), p=g["p0"])
+    s.set_npt(**prm)
+    ep = []
+    for st in range(20):
+        s.calc_forces(st)
+        ep.append(s.scalars().tot_pot_energy)
+        s.move_atoms_npt_iso(st, float(g["dt"]))
+        s.check_nblist()
+    assert list(s.scalars().gdim) == [4, 4, 4]
+    np.testing.assert_allclose(ep, out[:, 0], rtol=1e-9, atol=0)
+    box = np.array(s.npt_state().box).reshape(3, 3)
+    np.testing.assert_allclose(box, np.array(o.s.box), rtol=1e-10, atol=1e-12)
+    d = s.get_atoms()["x"] - o.x
+    d -= np.round(d @ np.linalg.inv(box)) @ box
+    assert np.abs(d).max() < 1e-8
+
+
 def test_glok_parameters_checked():
     from imd_gb300 import api
     g = golden("cu_fire")
