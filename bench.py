@@ -144,26 +144,27 @@ def committed_traffic(kernel: str):
         return None
 
 
-def cpu_sample(tabs, steps: int, cores: int = 1):
-    """The oracle (C restatement of the reference path) on the same workload,
-    `steps` NVE steps, in `cores` independent processes."""
+def cpu_sample(tabs, steps: int, cores: int = 1, warm: int = 1):
+    """The oracle (C restatement of the reference path) on the same workload:
+    `warm` untimed NVE steps (the first list build among them), then `steps`
+    timed ones, in `cores` independent processes."""
     import multiprocessing as mp
     ctx = mp.get_context("spawn")
     with ctx.Pool(cores) as pool:
-        res = pool.starmap(_cpu_worker, [(tabs, steps)] * cores)
+        res = pool.starmap(_cpu_worker, [(tabs, steps, warm)] * cores)
     n = res[0][0]
     rate = sum(n * steps / t for n, t in res)
     return rate, n
 
 
-def _cpu_worker(tabs, steps):
+def _cpu_worker(tabs, steps, warm=1):
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     from imd_gb300 import workloads as wl
     from oracle import OracleSystem
     s = make_state()
     o = OracleSystem(s.box, s.x, s.types, s.mass, s.number, 1, tabs, True, SKIN,
                      timestep=DT_FS * wl.FS, p=s.p)
-    o.nve(1)   # first build outside the timed sample
+    o.nve(max(1, warm))   # the first build and the warm-up outside the timed sample
     t = time.perf_counter()
     o.nve(steps)
     return s.n, time.perf_counter() - t
@@ -177,12 +178,11 @@ def run_reference(args, rank, world):
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "liboracle.so"], check=True)
     cores = os.cpu_count() or 1
     steps = max(1, min(args.steps, 4))
-    # warm-up: one process, W steps (bounded)
-    _ = cpu_sample(tabs, 1, 1)
-    rate, n = cpu_sample(tabs, steps, cores)
+    warm = max(1, min(args.warmup, 3))   # untimed steps in every process, bounded
+    rate, n = cpu_sample(tabs, steps, cores, warm)
     line = {
         "impl": "reference", "metric": METRIC, "value": rate, "unit": "atom-steps/s",
-        "n_gpus": world, "steps": steps, "warmup": 1, "ms_per_step": 1e3 * n / (rate / cores),
+        "n_gpus": world, "steps": steps, "warmup": warm, "ms_per_step": 1e3 * n / (rate / cores),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic", "config": {"workload": WORKLOAD, "sample": "%d NVE steps per core" % steps},
         "cpu_baseline": {"value": rate, "unit": "atom-steps/s", "cores": cores, "kind": "port",
