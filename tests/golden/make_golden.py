@@ -32,9 +32,10 @@ Fixtures (all sorted by atom number):
               (tau_eta 10 time units): energies and eta per step
   cu_mik      cu_pert's configuration quenched by 200 MIK steps: energies,
               force norms per step, final positions
-  cu_fire, cu_glok   a perturbed Cu crystal with two vacancies relaxed by
-              the glok ensemble of the `fire` build (300 steps, adaptive time
-              step and mixing) and of the `glok` build (200 steps)
+  cu_fire, cu_glok, cu_mixglok   a perturbed Cu crystal with two vacancies
+              relaxed by the glok ensemble of the `fire` build (300 steps,
+              adaptive time step and mixing), of the `glok` build and of the
+              `mix glok` build (200 steps each)
   cu_npt      Cu _fcc 8^3 at 300 K, 200 steps of ensemble npt_iso with the
               external pressure ramped from 0.01 to 0.005 eV/A^3
 
@@ -384,6 +385,7 @@ GLOK_CASES = {
                 dict(glok_mix=0.1, glok_mixdec=0.99, glok_incfac=1.1, glok_decfac=0.5,
                      glok_maxtimestep=0.5, glok_minsteps=5)),
     "cu_glok": ("glok_nbl_eam", 200, {}),
+    "cu_mixglok": ("mix_glok_nbl_eam", 200, dict(glok_mix=0.05, glok_ekin_threshold=0.004)),
 }
 
 
@@ -401,9 +403,11 @@ def glok_cases() -> None:
     perturbed_config(cus, 0.15, 21, cfg, remove=[5, 900])
     for name, (variant, nsteps, extra) in GLOK_CASES.items():
         p = os.path.join(tmp, name + ".param")
+        extra = dict(extra)
+        dt = extra.pop("timestep", 0.0982266)
         wl.write_param(p, coordname=cfg, box_from_header=1, ensemble="glok", starttemp=0.0,
                        outfiles=os.path.join(tmp, "o"), ntypes=1, masses=63.546,
-                       pbc_dirs=[1, 1, 1], timestep=0.0982266, maxsteps=0, seed=2,
+                       pbc_dirs=[1, 1, 1], timestep=dt, maxsteps=0, seed=2,
                        core_potential_file=cu[0], **{"atomic_e-density_file": cu[1]},
                        embedding_energy_file=cu[2], nbl_margin=0.4, eng_int=0,
                        checkpt_int=100000000, **extra)
@@ -420,8 +424,9 @@ def glok_cases() -> None:
                  epot=steps[:, 1], ekin=steps[:, 2], nbl_count=steps[:, 3],
                  fnorm=steps[:, 4], f_max2=steps[:, 5], timestep=steps[:, 6], mix=steps[:, 7],
                  pxf=steps[:, 8], glok_start=steps[:, 9], npxf=steps[:, 10],
-                 x_final=stf["x"], p_final=stf["p"], dt=0.0982266, skin=0.4,
-                 mix_on=int(variant.startswith("fire")), adapt=int(variant.startswith("fire")),
+                 x_final=stf["x"], p_final=stf["p"], dt=dt, skin=0.4,
+                 mix_on=int(variant.startswith(("fire", "mix"))),
+                 adapt=int(variant.startswith("fire")),
                  **{"param_" + k: v for k, v in prm.items()})
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **d)
         print(name, "epot", steps[[0, -1], 1], "dt", steps[[0, -1], 6],

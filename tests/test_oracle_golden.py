@@ -190,9 +190,10 @@ def glok_params(g) -> dict:
     return out
 
 
-@pytest.mark.parametrize("name", ["cu_fire", "cu_glok"])
+@pytest.mark.parametrize("name", ["cu_fire", "cu_glok", "cu_mixglok"])
 def test_glok_matches_reference(name):
-    """update_glok + move_atoms_nve of the `fire` and `glok` builds: the
+    """update_glok + move_atoms_nve of the `fire`, `glok` and `mix glok`
+    builds (the last restarting on glok_ekin_threshold): the
     decisions of every step (time step, mixing factor, restarts) identical,
     energies to 1e-12, P.F to 1e-8 relative, final positions to 1e-12 A."""
     g = golden(name)
