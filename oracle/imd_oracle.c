@@ -786,6 +786,7 @@ int orc_calc_forces(orc_sys_t *s) {
 
   s->tot_pot_energy = 0.0;
   s->virial = 0.0;
+  s->vir_axial[0] = s->vir_axial[1] = s->vir_axial[2] = 0.0;
   s->nfc++;
   for (int g = 0; g < s->next; g++) {
     s->ef[3 * g] = s->ef[3 * g + 1] = s->ef[3 * g + 2] = 0.0;
@@ -824,6 +825,9 @@ int orc_calc_forces(orc_sys_t *s) {
         ee += pot;
         s->eepot[j] += pot;
         s->virial -= r2 * grad;
+        s->vir_axial[0] -= dx * fx;
+        s->vir_axial[1] -= dy * fy;
+        s->vir_axial[2] -= dz * fz;
         if (st) stress_pair(pp, s->estress + 6 * j, dx, dy, dz, fx, fy, fz);
       }
       if (eam) {
@@ -894,6 +898,9 @@ int orc_calc_forces(orc_sys_t *s) {
           ffy += fy;
           ffz += fz;
           s->virial -= dx * fx + dy * fy + dz * fz;
+          s->vir_axial[0] -= dx * fx;
+          s->vir_axial[1] -= dy * fy;
+          s->vir_axial[2] -= dz * fz;
           if (st) stress_pair(pp, s->estress + 6 * j, dx, dy, dz, fx, fy, fz);
         }
       }
@@ -1290,6 +1297,133 @@ int orc_npt_steps(orc_sys_t *s, orc_npt_t *np, int step0, int nsteps, double *ou
       o[5] = s->volume;
       o[6] = s->box[0][0];
       o[7] = np->pressure_ext;
+    }
+    orc_check_nblist(s);
+  }
+  return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* NPT, per axis (src/imd_integrate.c:1747-1960)                              */
+/* ------------------------------------------------------------------------ */
+
+void orc_npt_axial_defaults(orc_npt_axial_t *np) {
+  memset(np, 0, sizeof *np);
+  np->cell_size_tolerance = 0.05;
+  np->relax_dirs[0] = np->relax_dirs[1] = np->relax_dirs[2] = 1;   /* einsivektor */
+}
+
+int orc_npt_axial_begin(orc_sys_t *s, orc_npt_axial_t *np) {
+  if (make_box(s)) return 1;
+  np->volume_init = s->volume;
+  int rc = init_cells(s, SQR(1.0 + np->cell_size_tolerance), np->min_height, np->max_height);
+  s->have_valid_nbl = 0;
+  return rc;
+}
+
+int orc_move_atoms_npt_axial(orc_sys_t *s, orc_npt_axial_t *np, int steps) {
+  const int n = s->n;
+  const double dt = s->timestep;
+  const double nact = np->nactive > 0 ? (double)np->nactive : 3.0 * n;
+  double Ekin_new = 0.0, fnorm = 0.0, fmax2 = 0.0;
+  double pfric[3], pifric[3], rfric[3], rifric[3];
+  if (steps == np->steps_min) {
+    /* calc_dyn_pressure (src/imd_integrate.c:1403-1447) */
+    double d[3] = {0.0, 0.0, 0.0};
+    for (int nn = 0; nn < n; nn++) {
+      int i = s->order[nn];
+      const double *p = s->p + 3 * i;
+      double tmp = 1.0 / s->mass[i];
+      for (int a = 0; a < 3; a++) d[a] += p[a] * p[a] * tmp;
+    }
+    for (int a = 0; a < 3; a++) np->dyn_stress[a] = d[a];
+    np->Ekin_old = d[0] + d[1];
+    np->Ekin_old += d[2];
+    if (np->isq_tau_xi == 0.0) np->xi[0] = np->xi[1] = np->xi[2] = 0.0;
+    for (int a = 0; a < 3; a++) np->xi[a] *= np->relax_dirs[a];
+  }
+  for (int a = 0; a < 3; a++) {
+    np->stress[a] = (np->dyn_stress[a] + s->vir_axial[a]) / s->volume;
+    np->dyn_stress[a] = 0.0;
+  }
+  double ttt = dt * s->volume * np->isq_tau_xi / nact;
+  for (int a = 0; a < 3; a++) {
+    np->xi_old[a] = np->xi[a];
+    np->xi[a] += ttt * (np->stress[a] - np->pressure_ext[a]) * np->relax_dirs[a];
+  }
+  for (int a = 0; a < 3; a++) {
+    pfric[a] = 1.0 - (np->xi_old[a] + np->eta) * dt / 2.0;
+    pifric[a] = 1.0 / (1.0 + (np->xi[a] + np->eta) * dt / 2.0);
+    rfric[a] = 1.0 + (np->xi[a]) * dt / 2.0;
+    rifric[a] = 1.0 / (1.0 - (np->xi[a]) * dt / 2.0);
+  }
+  for (int nn = 0; nn < n; nn++) {
+    int i = s->order[nn];
+    double *p = s->p + 3 * i, *f = s->f + 3 * i, *x = s->x + 3 * i;
+    double tmp = 1.0 / s->mass[i];
+    fnorm += f[0] * f[0] + f[1] * f[1] + f[2] * f[2];
+    fmax2 = OMAX(SQR(f[0]), fmax2);
+    fmax2 = OMAX(SQR(f[1]), fmax2);
+    fmax2 = OMAX(SQR(f[2]), fmax2);
+    for (int a = 0; a < 3; a++) p[a] = (pfric[a] * p[a] + dt * f[a]) * pifric[a];
+    int t = s->type[i];
+    for (int a = 0; a < 3; a++) p[a] *= restr(s, t, a);
+    for (int a = 0; a < 3; a++) np->dyn_stress[a] += p[a] * p[a] * tmp;
+    Ekin_new += (p[0] * p[0] + p[1] * p[1] + p[2] * p[2]) * tmp;
+    tmp *= dt;
+    for (int a = 0; a < 3; a++) x[a] = (rfric[a] * x[a] + p[a] * tmp) * rifric[a];
+  }
+  s->fnorm = fnorm;
+  s->f_max2 = fmax2;
+  s->tot_kin_energy = (np->Ekin_old + Ekin_new) / 4.0;
+  ttt = nact * np->temperature;
+  np->eta += dt * (Ekin_new / ttt - 1.0) * np->isq_tau_eta;
+  np->Ekin_old = Ekin_new;
+  /* the box, row a scaled by its own factor */
+  double tvec[3];
+  for (int a = 0; a < 3; a++) tvec[a] = (1.0 + np->xi[a] * dt / 2.0) / (1.0 - np->xi[a] * dt / 2.0);
+  if (tvec[0] < 0 || tvec[1] < 0 || tvec[2] < 0) return -1;   /* "box size has become negative!" */
+  double old[3][3];
+  memcpy(old, s->box, sizeof old);
+  for (int a = 0; a < 3; a++)
+    for (int c = 0; c < 3; c++) s->box[a][c] *= tvec[a];
+  if (make_box(s)) return -2;
+  if (s->volume > 8 * np->volume_init) return -4;
+  rescale_ghost_shifts(s, old);
+  int out = 0;
+  for (int a = 0; a < 3; a++)
+    if (s->height[a] < np->min_height[a] || s->height[a] > np->max_height[a]) out = 1;
+  if (out) {
+    if (init_cells(s, SQR(1.0 + np->cell_size_tolerance), np->min_height, np->max_height))
+      return -3;
+    s->have_valid_nbl = 0;
+  }
+  if (steps == np->steps_min) {
+    if (np->use_curr_pressure == 1) {
+      for (int a = 0; a < 3; a++) np->pressure_ext[a] = np->stress[a];
+      np->use_curr_pressure = 0;
+    }
+    for (int a = 0; a < 3; a++)
+      np->d_pressure[a] = (np->pressure_end[a] - np->pressure_ext[a]) / (np->steps_max - np->steps_min);
+  }
+  for (int a = 0; a < 3; a++) np->pressure_ext[a] += np->d_pressure[a];
+  return 0;
+}
+
+int orc_npt_axial_steps(orc_sys_t *s, orc_npt_axial_t *np, int step0, int nsteps, double *out) {
+  for (int st = 0; st < nsteps; st++) {
+    int rc = orc_calc_forces(s);
+    if (rc < 0) return rc;
+    double ep = s->tot_pot_energy;
+    if ((rc = orc_move_atoms_npt_axial(s, np, step0 + st))) return rc;
+    if (out) {
+      double *o = out + 12 * (size_t)st;
+      o[0] = ep;
+      o[1] = s->tot_kin_energy;
+      for (int a = 0; a < 3; a++) o[2 + a] = np->xi[a];
+      o[5] = np->eta;
+      for (int a = 0; a < 3; a++) o[6 + a] = np->stress[a];
+      for (int a = 0; a < 3; a++) o[9 + a] = s->box[a][a];
     }
     orc_check_nblist(s);
   }

@@ -137,6 +137,10 @@ typedef struct {
 
   /* ---- NVT thermostat (globals eta, isq_tau_eta, temperature) ---- */
   double  eta, isq_tau_eta, temperature;
+
+  /* ---- P_AXIAL (src/imd_forces_nbl.c:548-553, :1275-1278): vir_xx, vir_yy,
+   * vir_zz of the last calc_forces, summed beside the virial ---- */
+  double  vir_axial[3];
 } orc_sys_t;
 
 /* set defaults; allocate per-atom arrays for n atoms */
@@ -209,6 +213,28 @@ int  orc_move_atoms_npt_iso(orc_sys_t *s, orc_npt_t *np, int steps);
  * check_nblist.  Per step 8 values: tot_pot_energy, tot_kin_energy, xi,
  * eta, pressure, volume, box_x.x, pressure_ext */
 int  orc_npt_steps(orc_sys_t *s, orc_npt_t *np, int step0, int nsteps, double *out);
+/* NPT with the box scaled per axis, move_atoms_npt_axial
+ * (src/imd_integrate.c:1747-1960, the `npt_axial` build, which defines
+ * P_AXIAL): per-axis barostats xi driven by the axial stresses
+ * (dyn_stress + vir_xx ...) / volume, momenta restricted per type. */
+typedef struct {
+  double temperature, isq_tau_eta, eta;
+  double isq_tau_xi;
+  double xi[3], xi_old[3];
+  double pressure_ext[3], pressure_end[3], d_pressure[3];
+  double stress[3], dyn_stress[3];
+  double Ekin_old, volume_init, cell_size_tolerance;
+  double min_height[3], max_height[3];
+  int    relax_dirs[3];
+  int    use_curr_pressure, steps_min, steps_max;
+  long   nactive;                  /* <= 0: three per atom */
+} orc_npt_axial_t;
+void orc_npt_axial_defaults(orc_npt_axial_t *np);
+int  orc_npt_axial_begin(orc_sys_t *s, orc_npt_axial_t *np);
+int  orc_move_atoms_npt_axial(orc_sys_t *s, orc_npt_axial_t *np, int steps);
+/* main_loop steps: per step 12 values: tot_pot_energy, tot_kin_energy,
+ * xi (3), eta, stress (3), box_x.x, box_y.y, box_z.z */
+int  orc_npt_axial_steps(orc_sys_t *s, orc_npt_axial_t *np, int step0, int nsteps, double *out);
 /* main_loop steps with move_atoms of `ensemble` (0 nve, 1 nvt, 2 mik);
  * per step tot_pot_energy, tot_kin_energy and (nvt) eta / (mik) fnorm */
 int  orc_md_steps(orc_sys_t *s, int nsteps, int ensemble, double *epot_out,

@@ -59,7 +59,8 @@ class Sys(C.Structure):
         ("old_alphamin", C.c_double), ("nactive", C.c_long),
         ("do_stress", C.c_int), ("estress", _dp), ("stress", _dp),
         ("tot_stress", C.c_double * 6),
-        ("eta", C.c_double), ("isq_tau_eta", C.c_double), ("temperature", C.c_double)]
+        ("eta", C.c_double), ("isq_tau_eta", C.c_double), ("temperature", C.c_double),
+        ("vir_axial", C.c_double * 3)]
 
 
 class Glok(C.Structure):
@@ -83,6 +84,19 @@ class Npt(C.Structure):
                 ("volume_init", C.c_double), ("cell_size_tolerance", C.c_double), ("min_height", C.c_double * 3),
                 ("max_height", C.c_double * 3), ("use_curr_pressure", C.c_int),
                 ("steps_min", C.c_int), ("steps_max", C.c_int), ("nactive", C.c_long)]
+
+
+class NptAxial(C.Structure):
+    """orc_npt_axial_t: parameters and state of ensemble npt_axial."""
+    _d3 = C.c_double * 3
+    _fields_ = [("temperature", C.c_double), ("isq_tau_eta", C.c_double), ("eta", C.c_double),
+                ("isq_tau_xi", C.c_double), ("xi", _d3), ("xi_old", _d3),
+                ("pressure_ext", _d3), ("pressure_end", _d3), ("d_pressure", _d3),
+                ("stress", _d3), ("dyn_stress", _d3), ("Ekin_old", C.c_double),
+                ("volume_init", C.c_double), ("cell_size_tolerance", C.c_double),
+                ("min_height", _d3), ("max_height", _d3), ("relax_dirs", C.c_int * 3),
+                ("use_curr_pressure", C.c_int), ("steps_min", C.c_int), ("steps_max", C.c_int),
+                ("nactive", C.c_long)]
 
 
 _lib = None
@@ -115,6 +129,10 @@ def lib() -> C.CDLL:
         L.orc_npt_defaults.argtypes = [C.POINTER(Npt)]
         L.orc_npt_begin.argtypes = [C.POINTER(Sys), C.POINTER(Npt)]
         L.orc_npt_steps.argtypes = [C.POINTER(Sys), C.POINTER(Npt), C.c_int, C.c_int, _dp]
+        L.orc_npt_axial_defaults.argtypes = [C.POINTER(NptAxial)]
+        L.orc_npt_axial_begin.argtypes = [C.POINTER(Sys), C.POINTER(NptAxial)]
+        L.orc_npt_axial_steps.argtypes = [C.POINTER(Sys), C.POINTER(NptAxial), C.c_int,
+                                          C.c_int, _dp]
         L.orc_glok_steps.argtypes = [C.POINTER(Sys), C.POINTER(Glok), C.c_int, C.c_int, _dp]
         L.orc_cg_step.argtypes = [C.POINTER(Sys), C.c_int]
         L.orc_cg_relax.argtypes = [C.POINTER(Sys), C.c_double, C.c_int, _dp]
@@ -324,6 +342,30 @@ class OracleSystem:
         rc = L.orc_npt_steps(C.byref(self.s), C.byref(state), step0, nsteps, _ptr(out))
         if rc < 0:
             raise RuntimeError("oracle npt steps failed (%d)" % rc)
+        return out, state
+
+    def npt_axial(self, nsteps: int, step0: int = 0, state: NptAxial = None, **params):
+        """main_loop steps of ensemble npt_axial from step `step0`; params as
+        the orc_npt_axial_t fields (3-vectors as sequences).  Returns
+        (per-step array of tot_pot_energy, tot_kin_energy, xi (3), eta,
+        stress (3), box diagonal (3); the state)."""
+        L = lib()
+        if state is None:
+            state = NptAxial()
+            L.orc_npt_axial_defaults(C.byref(state))
+            for k, v in params.items():
+                if isinstance(getattr(state, k), C.Array):
+                    arr = getattr(state, k)
+                    for a in range(3):
+                        arr[a] = v[a]
+                else:
+                    setattr(state, k, v)
+            if L.orc_npt_axial_begin(C.byref(self.s), C.byref(state)):
+                raise ValueError("oracle npt grid set-up failed")
+        out = np.empty((nsteps, 12))
+        rc = L.orc_npt_axial_steps(C.byref(self.s), C.byref(state), step0, nsteps, _ptr(out))
+        if rc < 0:
+            raise RuntimeError("oracle npt_axial steps failed (%d)" % rc)
         return out, state
 
     def set_nvt(self, temperature: float, isq_tau_eta: float, eta: float = 0.0) -> None:

@@ -19,7 +19,8 @@
  *             (move_atoms of the parameter file's ensemble: nve, nvt, mik)
  *   glok K  : K main_loop steps of the glok ensemble (update_glok before
  *             move_atoms) from steps_min
- *   npt K   : K main_loop steps of ensemble npt_iso from steps_min
+ *   npt K   : K main_loop steps of ensemble npt_iso or npt_axial from
+ *             steps_min
  *   cg K F  : reset_cg, then cg_step until max per-atom |F| <= F
  *   time K  : K NVE steps, print cpu seconds
  */
@@ -259,7 +260,7 @@ int main(int argc, char **argv) {
 #endif
 #ifdef NPT
   else if (0 == strcmp(mode, "npt")) {
-    /* K main_loop steps of ensemble npt_iso from steps_min: calc_forces,
+    /* K main_loop steps of ensemble npt_iso / npt_axial from steps_min: calc_forces,
      * move_atoms (box scaled inside), check_nblist */
     sprintf(fname, "%s.steps", pre);
     FILE *out = fopen(fname, "w");
@@ -267,9 +268,15 @@ int main(int argc, char **argv) {
       calc_forces(steps);
       double ep = tot_pot_energy;
       move_atoms();
+#ifdef NPT_axial
+      fprintf(out, "%d %.17e %.17e %ld %.17e %.17e %.17e %.17e %.17e %.17e %.17e %.17e %.17e %.17e\n",
+              steps, ep, tot_kin_energy, (long)nbl_count, xi.x, xi.y, xi.z, eta, stress_x,
+              stress_y, stress_z, box_x.x, box_y.y, box_z.z);
+#else
       fprintf(out, "%d %.17e %.17e %ld %.17e %.17e %.17e %.17e %.17e %.17e\n", steps, ep,
               tot_kin_energy, (long)nbl_count, xi.x, eta, pressure, volume, box_x.x,
               pressure_ext.x);
+#endif
       check_nblist();
     }
     fclose(out);

@@ -38,10 +38,12 @@ Fixtures (all sorted by atom number):
               `mix glok` build (200 steps each)
   cu_npt      Cu _fcc 8^3 at 300 K, 200 steps of ensemble npt_iso with the
               external pressure ramped from 0.01 to 0.005 eV/A^3
+  cu_npt_axial  the same set-up, 200 steps of ensemble npt_axial with a
+              stress per axis and the z axis held
 
 `python tests/golden/make_golden.py stress` writes the stress fixtures only,
 `... ensembles` the NVT / MIK ones, `... lj1000` the 1000-step LJ run,
-`... glok` the glok ones, `... npt` the NPT one.
+`... glok` the glok ones, `... npt` the NPT ones.
 """
 from __future__ import annotations
 
@@ -475,6 +477,49 @@ def npt_case() -> None:
           gdimf, "rebuilds", steps[-1, 3])
 
 
+def npt_axial_case() -> None:
+    """ensemble npt_axial (move_atoms_npt_axial, src/imd_integrate.c:1747-1960)
+    of the reference's `npt_axial` build: the Cu set-up of cu_npt with a
+    different external stress per axis and the z axis held (relax_dirs
+    1 1 0); per step the energies, xi, eta, the axial stresses and the box
+    diagonal."""
+    subprocess.run(["make", "-s", "-C", ORACLE, "ref"], check=True)
+    tmp = tempfile.mkdtemp(prefix="imdgold_npta")
+    cu = tuple(os.path.join(HERE, "cu" + e) for e in (".pt", ".rho", ".emb"))
+    nsteps = 200
+    prm = dict(temperature=0.0258520, tau_eta=10.0, tau_xi=20.0,
+               pressure_start=[0.01, 0.0, -0.005], pressure_end=[0.005, 0.0, -0.005],
+               relax_dirs=[1, 1, 0])
+    p = os.path.join(tmp, "cu_npt_axial.param")
+    wl.write_param(p, coordname="_fcc", box_param=[8, 8, 8], box_unit=3.615,
+                   ensemble="npt_axial", starttemp=prm["temperature"], tau_eta=prm["tau_eta"],
+                   tau_xi=prm["tau_xi"], pressure_start=prm["pressure_start"],
+                   pressure_end=prm["pressure_end"], relax_dirs=prm["relax_dirs"],
+                   outfiles=os.path.join(tmp, "o"), ntypes=1, masses=63.546,
+                   pbc_dirs=[1, 1, 1], timestep=0.0982266, maxsteps=nsteps - 1, seed=2,
+                   core_potential_file=cu[0], **{"atomic_e-density_file": cu[1]},
+                   embedding_energy_file=cu[2], nbl_margin=0.4, eng_int=0,
+                   checkpt_int=100000000)
+    pre = os.path.join(tmp, "cu_npt_axial")
+    run("npt_axial_nbl_eam", p, "npt", pre, nsteps)
+    st0 = load_state(pre + ".state0")
+    stf = load_state(pre + ".final")
+    steps = np.loadtxt(pre + ".steps")
+    box, gdim, cellsz = load_box(pre + ".box")
+    boxf, gdimf, _ = load_box(pre + ".finalbox")
+    d = dict(box=box, gdim=gdim, cellsz=cellsz, number=st0["number"], type=st0["type"],
+             mass=st0["mass"], x0=st0["x"], p0=st0["p"], epot=steps[:, 1], ekin=steps[:, 2],
+             nbl_count=steps[:, 3], xi=steps[:, 4:7], eta=steps[:, 7], stress=steps[:, 8:11],
+             box_diag=steps[:, 11:14], x_final=stf["x"], p_final=stf["p"], box_final=boxf,
+             gdim_final=gdimf, dt=0.0982266, skin=0.4, temperature=prm["temperature"],
+             isq_tau_eta=1.0 / prm["tau_eta"] ** 2, isq_tau_xi=1.0 / prm["tau_xi"] ** 2,
+             pressure_start=np.array(prm["pressure_start"]),
+             pressure_end=np.array(prm["pressure_end"]),
+             relax_dirs=np.array(prm["relax_dirs"], np.int32), steps_max=nsteps - 1)
+    np.savez_compressed(os.path.join(HERE, "cu_npt_axial.npz"), **d)
+    print("cu_npt_axial box", steps[[0, -1], 11:14], "stress", steps[[0, -1], 8:11])
+
+
 # IMD's INIT values of the glok parameters (src/globals.h:580-600)
 GLOK_PARAM_DEFAULTS = dict(glok_ekin_threshold=100.0, glok_fmaxcrit=10000.0, glok_mix=0.0,
                            glok_mixdec=1.0, glok_incfac=1.02, glok_decfac=0.5,
@@ -526,6 +571,7 @@ if __name__ == "__main__":
         glok_cases()
     elif len(sys.argv) > 1 and sys.argv[1] == "npt":
         npt_case()
+        npt_axial_case()
     else:
         main()
         stress_cases()
@@ -533,3 +579,4 @@ if __name__ == "__main__":
         lj1000_case()
         glok_cases()
         npt_case()
+        npt_axial_case()

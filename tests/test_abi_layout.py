@@ -57,6 +57,7 @@ def test_api_structs_match_header(tmp_path):
 def test_oracle_structs_match_header(tmp_path):
     oracle = pytest.importorskip("oracle")
     structs = [("orc_table_t", oracle.Table), ("orc_sys_t", oracle.Sys),
-               ("orc_glok_t", oracle.Glok), ("orc_npt_t", oracle.Npt)]
+               ("orc_glok_t", oracle.Glok), ("orc_npt_t", oracle.Npt),
+               ("orc_npt_axial_t", oracle.NptAxial)]
     got = _c_layout(tmp_path, os.path.join(ROOT, "oracle"), "imd_oracle.h", structs)
     _check(got, structs)

@@ -245,6 +245,36 @@ def test_npt_iso_matches_reference():
     assert g["volume"][-1] / g["volume"][0] - 1.0 > 5e-3
 
 
+def test_npt_axial_matches_reference():
+    """move_atoms_npt_axial (P_AXIAL virial components, a barostat per
+    axis, z held by relax_dirs) against the reference's `npt_axial` build
+    over 200 steps: energies, xi, eta, the axial stresses and the box to
+    1e-12 relative, final positions to 1e-10 A."""
+    g = golden("cu_npt_axial")
+    s = OracleSystem(g["box"], g["x0"], g["type"], g["mass"], g["number"], 1, tables("cu"),
+                     True, float(g["skin"]), timestep=float(g["dt"]), p=g["p0"])
+    out, st = s.npt_axial(len(g["epot"]), 0, temperature=float(g["temperature"]),
+                          isq_tau_eta=float(g["isq_tau_eta"]), isq_tau_xi=float(g["isq_tau_xi"]),
+                          pressure_ext=list(g["pressure_start"]),
+                          pressure_end=list(g["pressure_end"]),
+                          relax_dirs=[int(v) for v in g["relax_dirs"]], steps_min=0,
+                          steps_max=int(g["steps_max"]))
+    np.testing.assert_allclose(out[:, 0], g["epot"], rtol=1e-12, atol=0)
+    np.testing.assert_allclose(out[:, 1], g["ekin"], rtol=1e-12, atol=0)
+    np.testing.assert_allclose(out[:, 2:5], g["xi"], rtol=1e-12, atol=1e-15)
+    np.testing.assert_allclose(out[:, 5], g["eta"], rtol=1e-12, atol=1e-15)
+    np.testing.assert_allclose(out[:, 6:9], g["stress"], rtol=1e-12, atol=1e-15)
+    np.testing.assert_allclose(out[:, 9:12], g["box_diag"], rtol=1e-12, atol=0)
+    box = np.array(s.s.box)
+    np.testing.assert_allclose(box, g["box_final"], rtol=1e-12, atol=0)
+    d = s.x - g["x_final"]
+    d -= np.round(d @ np.linalg.inv(box)) @ box
+    assert np.abs(d).max() < 1e-10
+    # the axes move apart, the held one stays
+    assert g["box_diag"][-1, 2] == g["box_diag"][0, 2]
+    assert abs(g["box_diag"][-1, 1] / g["box_diag"][0, 1] - 1.0) > 5e-3
+
+
 def test_npt_iso_new_cell_grid():
     """A box that shrinks out of its height bounds gets a new cell grid
     (make_box calling init_cells, src/imd_geom_3d.c:82-86) and a new list;
