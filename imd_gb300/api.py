@@ -163,6 +163,7 @@ def lib() -> C.CDLL:
         L.imdgpu_batch_ml_start.argtypes = [vp, _ip, _dp, _dp]
         L.imdgpu_ml_get_adam.argtypes = [vp, fp, fp, _ip]
         L.imdgpu_ml_set_adam.argtypes = [vp, fp, fp, C.c_int]
+        L.imdgpu_ml_set_loss_weights.argtypes = [vp, _dp]
         _lib = L
     return _lib
 
@@ -478,6 +479,14 @@ class GpuSystem:
         dx = np.empty((self.n, 3))
         _check(lib().imdgpu_ml_predict(self.h, _p(dx)), "ml_predict")
         return dx
+
+    def ml_set_loss_weights(self, w=None) -> None:
+        """Per-atom weights of the training loss (caller order); None: all 1."""
+        if w is None:
+            _check(lib().imdgpu_ml_set_loss_weights(self.h, None), "ml_set_loss_weights")
+            return
+        w = _f64(w, (self.n,))
+        _check(lib().imdgpu_ml_set_loss_weights(self.h, _p(w)), "ml_set_loss_weights")
 
     def ml_train_step(self, target, lr: float = 0.0, want_grad: bool = False):
         """Loss (and gradient) for per-atom target displacements; with lr > 0

@@ -92,8 +92,8 @@ void launch_ml_pairs(const SysView &v, MlPair *pairs, int cap, int *count, cudaS
 void launch_ml_forward(const MlPair *pairs, const int *np, const double *rho,
                        const __nv_bfloat16 *wb, const float *wf, float *dxp, int blocks,
                        cudaStream_t st);
-void launch_ml_loss(int n, const float *dxp, const float *target, float *dldx, double *loss,
-                    cudaStream_t st);
+void launch_ml_loss(int n, const float *dxp, const float *target, const float *wt, float *dldx,
+                    double *loss, cudaStream_t st);
 void launch_ml_backward(const MlPair *pairs, const int *np, const double *rho,
                         const __nv_bfloat16 *wb, const float *wf, const float *dldx,
                         float *grad, int blocks, cudaStream_t st);

@@ -271,16 +271,17 @@ __global__ void __launch_bounds__(128) k_ml_forward(const MlPair *pairs, const i
 
 // loss = sum_i |dx_i - t_i|^2 / N; writes dL/d(dx_i) and the block sums of
 // the loss
-__global__ void k_ml_loss(int n, const float *dxp, const float *target, float inv_n,
-                          float *dldx, double *loss) {
+__global__ void k_ml_loss(int n, const float *dxp, const float *target, const float *wt,
+                          float inv_n, float *dldx, double *loss) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   double l = 0.0;
   if (i < n) {
+    const float w = wt ? wt[i] : 1.0f;   // per-atom loss weight (1: the plain mean)
 #pragma unroll
     for (int c = 0; c < 3; c++) {
       const float e = dxp[3 * i + c] - target[3 * i + c];
-      dldx[3 * i + c] = 2.0f * e * inv_n;
-      l += (double)e * e * inv_n;
+      dldx[3 * i + c] = 2.0f * e * inv_n * w;
+      l += (double)e * e * inv_n * w;
     }
   }
   l = warp_sum(l);
@@ -502,9 +503,9 @@ void launch_ml_forward(const MlPair *pairs, const int *np, const double *rho,
                        cudaStream_t st) {
   k_ml_forward<<<blocks, 128, sizeof(MlSmem), st>>>(pairs, np, rho, wb, wf, dxp);
 }
-void launch_ml_loss(int n, const float *dxp, const float *target, float *dldx, double *loss,
-                    cudaStream_t st) {
-  k_ml_loss<<<(n + 255) / 256, 256, 0, st>>>(n, dxp, target, 1.0f / n, dldx, loss);
+void launch_ml_loss(int n, const float *dxp, const float *target, const float *wt, float *dldx,
+                    double *loss, cudaStream_t st) {
+  k_ml_loss<<<(n + 255) / 256, 256, 0, st>>>(n, dxp, target, wt, 1.0f / n, dldx, loss);
 }
 void launch_ml_backward(const MlPair *pairs, const int *np, const double *rho,
                         const __nv_bfloat16 *wb, const float *wf, const float *dldx,

@@ -176,6 +176,8 @@ struct imdgpu_sys {
   int ml_cap = 0;
   int *ml_np = nullptr;
   float *ml_dx = nullptr, *ml_target = nullptr, *ml_dldx = nullptr;
+  float *ml_wt = nullptr;              // per-atom loss weights by slot (training)
+  std::vector<double> ml_wt_host;      // the same in caller order; empty: uniform
   double *ml_loss = nullptr;
   int ml_have = 0;
   int ml_dx_cap = 0;
@@ -1930,6 +1932,7 @@ int imdgpu_destroy(imdgpu_sys *s) {
   dfree(s->slot_of); dfree(s->d_in); dfree(s->d_out); dfree(s->flushbuf); dfree(s->dff);
   dfree(s->ml_w); dfree(s->ml_m); dfree(s->ml_v); dfree(s->ml_grad); dfree(s->ml_wb);
   dfree(s->ml_pairs); dfree(s->ml_np); dfree(s->ml_dx); dfree(s->ml_target); dfree(s->ml_dldx);
+  dfree(s->ml_wt);
   dfree(s->ml_loss);
   dfree(s->ml_save); dfree(s->ml_ecell); dfree(s->ml_sel);
   dfree(s->d_stress);
@@ -2236,6 +2239,7 @@ int imdgpu_set_atoms(imdgpu_sys *s, int n, const int *number, const int *type,
   cudaFree(dt);
   if (dp) cudaFree(dp);
   s->atoms_set = true;
+  s->ml_wt_host.clear();
   int one = 1;
   CK(cudaMemcpy(&s->dsc->rebuild, &one, sizeof(int), cudaMemcpyHostToDevice));
   s->hsc_valid = false;
@@ -3415,6 +3419,7 @@ int imdgpu_batch_set_cells(imdgpu_sys *s, int ncells, const int *natoms, const d
                            const double *x) {
   if (!s || ncells < 1 || !natoms || !boxes || !number || !type || !mass || !x)
     return fail(IMDGPU_ERR_ARG, "bad batch arguments");
+  s->ml_wt_host.clear();
   std::vector<int> aoff(ncells + 1, 0);
   for (int q = 0; q < ncells; q++) {
     if (natoms[q] < 1) return fail(IMDGPU_ERR_ARG, "empty cell in batch");
@@ -3792,6 +3797,11 @@ __global__ void k_gather_target(int n, const int *orig, const double *t, float *
   ts[3 * s + 1] = (float)t[3 * o + 1];
   ts[3 * s + 2] = (float)t[3 * o + 2];
 }
+__global__ void k_gather_weight(int n, const int *orig, const double *w, float *ws) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  ws[s] = (float)w[orig[s]];
+}
 __global__ void k_scatter_dx(int n, const int *orig, const float *dx, double *out) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= n) return;
@@ -3873,9 +3883,11 @@ static int ml_ensure(imdgpu_sys *s) {
     dfree(s->ml_dx);
     dfree(s->ml_target);
     dfree(s->ml_dldx);
+    dfree(s->ml_wt);
     CK(dalloc(&s->ml_dx, 3 * (size_t)s->ncap));
     CK(dalloc(&s->ml_target, 3 * (size_t)s->ncap));
     CK(dalloc(&s->ml_dldx, 3 * (size_t)s->ncap));
+    CK(dalloc(&s->ml_wt, (size_t)s->ncap));
     s->ml_dx_cap = s->ncap;
   }
   return IMDGPU_OK;
@@ -3972,6 +3984,22 @@ int imdgpu_ml_predict(imdgpu_sys *s, double *dx) {
   return IMDGPU_OK;
 }
 
+// Per-atom weights of the training loss (caller order, n; NULL: uniform),
+// kept until the atoms change.  Weighting large displacements lets the
+// model learn the defect cores that set the CG cost.
+int imdgpu_ml_set_loss_weights(imdgpu_sys *s, const double *w) {
+  if (!s || !s->atoms_set) return fail(IMDGPU_ERR_STATE, "atoms not set");
+  if (!w) {
+    s->ml_wt_host.clear();
+    return IMDGPU_OK;
+  }
+  for (int i = 0; i < s->n; i++)
+    if (!(w[i] >= 0.0) || !std::isfinite(w[i]))
+      return fail(IMDGPU_ERR_ARG, "loss weight of atom " + std::to_string(i) + " not finite and >= 0");
+  s->ml_wt_host.assign(w, w + s->n);
+  return IMDGPU_OK;
+}
+
 // loss and parameter gradients for targets (caller order, 3n); with lr > 0
 // also one Adam step (learning rate lr)
 int imdgpu_ml_train_step(imdgpu_sys *s, const double *target, double lr, double *loss,
@@ -3984,9 +4012,16 @@ int imdgpu_ml_train_step(imdgpu_sys *s, const double *target, double lr, double 
   double *d = s->d_out;
   CK(cudaMemcpyAsync(d, target, sizeof(double) * 3 * s->n, cudaMemcpyHostToDevice, s->st));
   k_gather_target<<<nblk(s->n, 256), 256, 0, s->st>>>(s->n, s->orig, d, s->ml_target);
+  const bool weighted = s->ml_wt_host.size() == (size_t)s->n;
+  if (weighted) {
+    CK(cudaMemcpyAsync(d + 3 * s->n, s->ml_wt_host.data(), sizeof(double) * s->n,
+                       cudaMemcpyHostToDevice, s->st));
+    k_gather_weight<<<nblk(s->n, 256), 256, 0, s->st>>>(s->n, s->orig, d + 3 * s->n, s->ml_wt);
+  }
   if ((rc = ml_forward(s))) return rc;
   CK(cudaMemsetAsync(s->ml_loss, 0, sizeof(double), s->st));
-  launch_ml_loss(s->n, s->ml_dx, s->ml_target, s->ml_dldx, s->ml_loss, s->st);
+  launch_ml_loss(s->n, s->ml_dx, s->ml_target, weighted ? s->ml_wt : nullptr, s->ml_dldx,
+                 s->ml_loss, s->st);
   const int np = ml_nparam();
   CK(cudaMemsetAsync(s->ml_grad, 0, sizeof(float) * np, s->st));
   launch_ml_backward(s->ml_pairs, s->ml_np, s->rho, s->ml_wb, s->ml_w, s->ml_dldx, s->ml_grad,

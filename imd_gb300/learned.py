@@ -135,7 +135,12 @@ class Trainer:
     """Adam training of the per-pair MLP on resident groups of cells."""
 
     def __init__(self, tables, cells, disp, batch_cells: int = 64, seed: int = 0,
-                 weights=None, interpolation: int = BATCH_INTERPOLATION):
+                 weights=None, interpolation: int = BATCH_INTERPOLATION,
+                 core_weight: float = 0.0, core_disp: float = 0.2):
+        """core_weight > 0 weights the loss of every atom whose target
+        displacement is at least core_disp (A) by 1 + core_weight: the few
+        defect-core atoms that set the CG cost count as much as the many
+        atoms of the elastic field."""
         self.groups = []
         order = np.arange(len(cells))
         for g0 in range(0, len(cells), batch_cells):
@@ -143,6 +148,9 @@ class Trainer:
             gc = [cells[i] for i in idx]
             b = make_batch(tables, gc, interpolation=interpolation)
             t = np.ascontiguousarray(np.concatenate([disp[i] for i in idx]), np.float64)
+            if core_weight > 0.0:
+                core = np.sqrt(np.sum(t * t, axis=1)) >= core_disp
+                b.ml_set_loss_weights(1.0 + core_weight * core)
             self.groups.append((b, t))
         self.w = init_weights(seed) if weights is None else np.asarray(weights, np.float32)
         self.m = np.zeros(NPARAM, np.float32)

@@ -91,6 +91,9 @@ def main(argv=None):
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--eval-cells", type=int, default=512)
     ap.add_argument("--out", default=DEFAULT_OUT)
+    ap.add_argument("--core-weight", type=float, default=0.0,
+                    help="extra loss weight of atoms displaced by >= --core-disp A")
+    ap.add_argument("--core-disp", type=float, default=0.2)
     a = ap.parse_args(argv)
     tmp = tempfile.mkdtemp(prefix="imdtrain")
     tabs = wl.sutton_chen_tables(os.path.join(tmp, "cu"), [wl.CU])
@@ -101,7 +104,8 @@ def main(argv=None):
     disp = [d for d in disp if d is not None]
     t_data = time.perf_counter() - t0
     t1 = time.perf_counter()
-    tr = learned.Trainer(tabs, train, disp, batch_cells=a.batch_cells, seed=a.seed)
+    tr = learned.Trainer(tabs, train, disp, batch_cells=a.batch_cells, seed=a.seed,
+                         core_weight=a.core_weight, core_disp=a.core_disp)
     loss0 = tr.loss()
     for ep in range(a.epochs):
         m = tr.epoch(a.lr)
@@ -116,6 +120,8 @@ def main(argv=None):
     rec = {"train_cells": a.train_cells, "train_cells_relaxed": len(train),
            "train_atoms": int(sum(c.n for c in train)),
            "epochs": a.epochs, "batch_cells": a.batch_cells, "lr": a.lr, "adam_steps": steps,
+           "core_weight": a.core_weight, "core_disp": a.core_disp,
+           "loss_weighted": a.core_weight > 0.0,
            "loss_initial": loss0, "loss_final": loss1, "loss_zero_prediction": zero,
            "loss_history": tr.history, "seconds_data": t_data, "seconds_train": t_train,
            "relax_batches": relax_stats}

@@ -295,10 +295,13 @@ int imdgpu_ml_get_adam(imdgpu_sys *sys, float *m, float *v, int *step);
 int imdgpu_ml_set_adam(imdgpu_sys *sys, const float *m, const float *v, int step);
 /* dx (3n, caller order) at the current positions */
 int imdgpu_ml_predict(imdgpu_sys *sys, double *dx);
-/* loss = sum_i |dx_i - target_i|^2 / n and its gradient (grad may be NULL);
+/* loss = sum_i w_i |dx_i - target_i|^2 / n and its gradient (grad may be
+ * NULL), w_i = 1 unless imdgpu_ml_set_loss_weights set them;
  * lr > 0: one Adam step (beta 0.9 / 0.999) on the weights */
 int imdgpu_ml_train_step(imdgpu_sys *sys, const double *target, double lr, double *loss,
                          float *grad);
+/* per-atom weights w_i >= 0 of that loss (n, caller order; NULL: all 1) */
+int imdgpu_ml_set_loss_weights(imdgpu_sys *sys, const double *w);
 /* Learned start of a batch (after imdgpu_batch_set_cells and
  * imdgpu_ml_set_weights, before imdgpu_batch_begin): per cell the energy
  * at the current positions (e_start), the energy after adding the predicted
