@@ -5,7 +5,7 @@
  * src/imd_fix_cells_3d.c, src/imd_integrate.c, src/imd_cg.c,
  * src/cg_utils.h).
  *
- * TEST INFRASTRUCTURE ONLY: the checker for the GPU library and the timed
+ * TEST INFRASTRUCTURE ONLY: the reference values for testing the GPU library and the timed
  * CPU baseline.  Never linked into the product.
  *
  * Build with -ffp-contract=off: the reference is compiled without fused

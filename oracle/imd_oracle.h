@@ -1,6 +1,6 @@
 /*
  * imd_oracle.h -- CPU restatement of IMD's force / neighbour-list / NVE / CG
- * hot path, used ONLY as the test checker and as the timed CPU baseline.
+ * hot path, used ONLY as the oracle of the tests and as the timed CPU baseline.
  *
  * This is test infrastructure.  Only tests/, __graft_entry__.smoke() and the
  * cpu_baseline / reference arm of bench.py may load it.  The GPU library in

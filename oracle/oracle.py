@@ -1,7 +1,7 @@
 """ctypes binding of the C oracle (oracle/liboracle.so).
 
 TEST INFRASTRUCTURE: only tests/, __graft_entry__.smoke() and the CPU
-baseline arm of bench.py import this module.  It is the checker, never the
+baseline arm of bench.py import this module.  It is the oracle, never the
 thing measured on the GPU and never called by imd_gb300.
 """
 from __future__ import annotations
