@@ -2495,6 +2495,7 @@ int imdgpu_glok_defaults(imdgpu_glok_params *prm) {
 // an adaptive step with no maximum would set the step to zero there.
 int imdgpu_set_glok(imdgpu_sys *s, const imdgpu_glok_params *prm, double timestep) {
   if (!s || !s->atoms_set) return fail(IMDGPU_ERR_STATE, "atoms not set");
+  if (s->nsys > 0) return fail(IMDGPU_ERR_STATE, "glok: one system, not a batch");
   if (!prm || !(timestep > 0.0)) return fail(IMDGPU_ERR_ARG, "glok: parameters and timestep > 0");
   if (prm->adapt && !prm->mix) return fail(IMDGPU_ERR_ARG, "glok: adapt needs mix (ADAPTGLOK needs MIX)");
   if (prm->adapt && !(prm->glok_maxtimestep > 0.0))
@@ -2594,6 +2595,7 @@ int imdgpu_set_npt(imdgpu_sys *s, const imdgpu_npt_params *prm) {
   if (!s || !s->atoms_set) return fail(IMDGPU_ERR_STATE, "atoms not set");
   if (!prm) return fail(IMDGPU_ERR_ARG, "null");
   if (s->nsys > 0) return fail(IMDGPU_ERR_STATE, "npt: one system, not a batch");
+  if (!s->have_box) return fail(IMDGPU_ERR_STATE, "box not set");
   if (s->precision != IMDGPU_FP64) return fail(IMDGPU_ERR_STATE, "npt: FP64 precision only");
   if (!(prm->temperature > 0.0) || prm->isq_tau_eta < 0.0 || prm->isq_tau_xi < 0.0)
     return fail(IMDGPU_ERR_ARG, "npt: temperature > 0, isq_tau_eta and isq_tau_xi >= 0");
@@ -3420,6 +3422,7 @@ int imdgpu_batch_set_cells(imdgpu_sys *s, int ncells, const int *natoms, const d
   if (!s || ncells < 1 || !natoms || !boxes || !number || !type || !mass || !x)
     return fail(IMDGPU_ERR_ARG, "bad batch arguments");
   s->ml_wt_host.clear();
+  s->glok_set = s->npt_set = false;   // ensembles of one system end here
   std::vector<int> aoff(ncells + 1, 0);
   for (int q = 0; q < ncells; q++) {
     if (natoms[q] < 1) return fail(IMDGPU_ERR_ARG, "empty cell in batch");
