@@ -12,6 +12,7 @@
 // its own device arrays, and the partial sums live in a file-scope
 // __device__ array of fixed size, present on every device that loads the
 // library until the process exits.
+#include <cstdio>
 #include <mutex>
 
 #include "../../include/imdgpu.h"
@@ -23,8 +24,9 @@ constexpr int NA_BS = 256;                        // threads per block
 constexpr int NA_MAX_ATOMS = 1 << 24;             // 16,777,216 atoms per call
 constexpr int NA_MAX_BLOCKS = NA_MAX_ATOMS / NA_BS;
 constexpr int NA_MAX_DEVICES = 64;
-// 4 partials per block + 4 final scalars: 2 MiB + 32 B per device
-constexpr size_t NA_SCRATCH_DOUBLES = 4 * (size_t)NA_MAX_BLOCKS + 4;
+constexpr int NA_SLOTS = 5;                       // partial results per block
+// 5 partials per block + 5 final values: 2.5 MiB + 40 B per device
+constexpr size_t NA_SCRATCH_DOUBLES = NA_SLOTS * (size_t)NA_MAX_BLOCKS + NA_SLOTS;
 
 __device__ __align__(256) double g_nve_scratch[NA_SCRATCH_DOUBLES];
 
@@ -43,14 +45,19 @@ __device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a,
 
 // Same arithmetic as k_nve (src/imd_integrate.c:32-497), on atom-major
 // caller arrays x[3i+c], p[3i+c], f[3i+c]; the masked force is written back
-// as the reference does with KRAFT.
-__global__ void __launch_bounds__(NA_BS) k_nve_noalloc(int n, double *x, double *p, double *f,
-                                                       const double *mass, const int *type,
-                                                       Restr rs, double dt, const double *xref,
-                                                       double *partial) {
+// as the reference does with KRAFT.  The types come straight from the
+// caller's device memory: an atom whose type is outside 0..ntypes-1 is left
+// as it is (its restriction row does not exist) and the lowest such atom
+// index goes to the fifth partial, so that the call can refuse the input.
+__global__ void __launch_bounds__(NA_BS) k_nve_noalloc(int n, int ntypes, double *x, double *p,
+                                                       double *f, const double *mass,
+                                                       const int *type, Restr rs, double dt,
+                                                       const double *xref, double *partial) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   double ek = 0.0, fn = 0.0, fm = 0.0, dm = 0.0;
-  if (i < n) {
+  double bad = (double)n;  // lowest atom with a bad type; n = none
+  if (i < n && (type[i] < 0 || type[i] >= ntypes)) bad = (double)i;
+  else if (i < n) {
     const int t = type[i];
     double px = p[3 * i], py = p[3 * i + 1], pz = p[3 * i + 2];
     double fx = f[3 * i], fy = f[3 * i + 1], fz = f[3 * i + 2];
@@ -85,55 +92,64 @@ __global__ void __launch_bounds__(NA_BS) k_nve_noalloc(int n, double *x, double 
       dm = dadd(dadd(dmul(ddx, ddx), dmul(ddy, ddy)), dmul(ddz, ddz));
     }
   }
-  // every block overwrites its own 4 slots: nothing carries over from an
-  // earlier call
-  __shared__ double sh[4][NA_BS / 32];
+  // every block overwrites its own NA_SLOTS slots: nothing carries over
+  // from an earlier call
+  __shared__ double sh[NA_SLOTS][NA_BS / 32];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   ek = imdgpu::warp_sum(ek);
   fn = imdgpu::warp_sum(fn);
   fm = imdgpu::warp_max(fm);
   dm = imdgpu::warp_max(dm);
+  bad = -imdgpu::warp_max(-bad);
   if (lane == 0) {
     sh[0][w] = ek;
     sh[1][w] = fn;
     sh[2][w] = fm;
     sh[3][w] = dm;
+    sh[4][w] = bad;
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    double a = 0, b = 0, c = 0, d = 0;
+    double a = 0, b = 0, c = 0, d = 0, e = (double)n;
     for (int k = 0; k < NA_BS / 32; k++) {
       a += sh[0][k];
       b += sh[1][k];
       c = fmax(c, sh[2][k]);
       d = fmax(d, sh[3][k]);
+      e = fmin(e, sh[4][k]);
     }
-    partial[4 * blockIdx.x] = a;
-    partial[4 * blockIdx.x + 1] = b;
-    partial[4 * blockIdx.x + 2] = c;
-    partial[4 * blockIdx.x + 3] = d;
+    double *o = partial + NA_SLOTS * (size_t)blockIdx.x;
+    o[0] = a;
+    o[1] = b;
+    o[2] = c;
+    o[3] = d;
+    o[4] = e;
   }
 }
 
-// fixed-order reduction of the nb block partials into out4
-__global__ void k_nve_noalloc_final(const double *partial, int nb, double *out4) {
+// fixed-order reduction of the nb block partials into out (NA_SLOTS values)
+__global__ void k_nve_noalloc_final(const double *partial, int nb, int n, double *out) {
   const int lane = threadIdx.x;
-  double a = 0, b = 0, c = 0, d = 0;
+  double a = 0, b = 0, c = 0, d = 0, e = (double)n;
   for (int k = lane; k < nb; k += 32) {
-    a += partial[4 * k];
-    b += partial[4 * k + 1];
-    c = fmax(c, partial[4 * k + 2]);
-    d = fmax(d, partial[4 * k + 3]);
+    const double *q = partial + NA_SLOTS * (size_t)k;
+    a += q[0];
+    b += q[1];
+    c = fmax(c, q[2]);
+    d = fmax(d, q[3]);
+    e = fmin(e, q[4]);
   }
   a = imdgpu::warp_sum(a);
   b = imdgpu::warp_sum(b);
   c = imdgpu::warp_max(c);
   d = imdgpu::warp_max(d);
+  e = -imdgpu::warp_max(-e);
   if (lane == 0) {
-    out4[0] = a;
-    out4[1] = b;
-    out4[2] = c;
-    out4[3] = d;
+    out[0] = a;
+    out[1] = b;
+    out[2] = c;
+    out[3] = d;
+    out[4] = e;
   }
 }
 
@@ -185,15 +201,26 @@ int imdgpu_move_atoms_nve_noalloc(int n, int ntypes, double *x, double *p, doubl
     for (int k = 0; k < 3 * ntypes; k++) rs.r[k] = restr[k];
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   const int nb = (n + NA_BS - 1) / NA_BS;
-  double *final4 = scratch + 4 * (size_t)NA_MAX_BLOCKS;
-  k_nve_noalloc<<<nb, NA_BS, 0, st>>>(n, x, p, f, mass, type, rs, timestep, x_ref, scratch);
-  k_nve_noalloc_final<<<1, 32, 0, st>>>(scratch, nb, final4);
+  double *fin = scratch + NA_SLOTS * (size_t)NA_MAX_BLOCKS;
+  k_nve_noalloc<<<nb, NA_BS, 0, st>>>(n, ntypes, x, p, f, mass, type, rs, timestep, x_ref,
+                                      scratch);
+  k_nve_noalloc_final<<<1, 32, 0, st>>>(scratch, nb, n, fin);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return na_fail(IMDGPU_ERR_CUDA, cudaGetErrorString(e));
-  e = cudaMemcpyAsync(out, final4, 4 * sizeof(double), cudaMemcpyDeviceToHost, st);
+  double res[NA_SLOTS];
+  e = cudaMemcpyAsync(res, fin, sizeof(res), cudaMemcpyDeviceToHost, st);
   if (e != cudaSuccess) return na_fail(IMDGPU_ERR_CUDA, cudaGetErrorString(e));
   e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return na_fail(IMDGPU_ERR_CUDA, cudaGetErrorString(e));
+  for (int k = 0; k < 4; k++) out[k] = res[k];
+  if (res[4] < (double)n) {
+    char msg[160];
+    snprintf(msg, sizeof msg,
+             "imdgpu_move_atoms_nve_noalloc: atom %ld has a type outside 0..%d; atoms with "
+             "such types were not moved",
+             (long)res[4], ntypes - 1);
+    return na_fail(IMDGPU_ERR_ARG, msg);
+  }
   return IMDGPU_OK;
 }
 

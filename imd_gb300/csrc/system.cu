@@ -2995,10 +2995,6 @@ static int cg_vec(imdgpu_sys *s, int mode, double gamma, double out[4]) {
   return IMDGPU_OK;
 }
 
-struct CgErr {
-  int rc;
-};
-
 // fonedim (src/imd_cg.c:295-307)
 static double fonedim(imdgpu_sys *s, double alpha, int &rc) {
   SysView v = view(s);
@@ -3011,175 +3007,171 @@ static double fonedim(imdgpu_sys *s, double alpha, int &rc) {
   return s->hsc->epot;
 }
 
-#define CGOLD 0.3819660
-#define GOLD 1.618034
-#define TINY 1.0e-20
-#define SHFT(a, b, c, d) \
-  (a) = (b);             \
-  (b) = (c);             \
-  (c) = (d);
-#define SIGN(a, b) ((b) >= 0.0 ? std::fabs(a) : -std::fabs(a))
+// IMD's line search along h for one system: linmin (src/imd_cg.c:96-200)
+// with its bracketing (mnbrak, src/cg_utils.h:119-194) and Brent's
+// minimisation (brent, src/cg_utils.h:34-114).  Every trial step costs one
+// fonedim.  The comparisons and the arithmetic keep IMD's order, so the same
+// trial steps are visited and the trajectory follows the reference's.
+namespace {
 
-// brent (src/cg_utils.h:34-114) as IMD has it: a=ax, b=bx, x=w=v=bx
-static int brent(imdgpu_sys *s, double ax, double bx, double fb, double *alphamin) {
-  double a = ax, b = bx, etemp, fu, fv, fw, fx, p, q, r, tol1, tol2, u, v, w, x, xm;
-  double e = 0.0, d = 0.0;
-  int rc = 0;
-  x = w = v = bx;
-  fw = fv = fx = fb;
-  for (int iter = 1; iter <= s->linmin_maxsteps; iter++) {
-    xm = 0.5 * (a + b);
-    tol1 = s->linmin_tol * std::fabs(x) + s->cg_zeps;
-    tol2 = 2.0 * tol1;
-    if (std::fabs(x - xm) <= (tol2 - 0.5 * (b - a))) {
-      *alphamin = x;
-      return iter;
-    }
-    if (std::fabs(e) > tol1) {
-      r = (x - w) * (fx - fv);
-      q = (x - v) * (fx - fw);
-      p = (x - v) * q - (x - w) * r;
-      q = 2.0 * (q - r);
-      if (q > 0.0) p = -p;
-      q = std::fabs(q);
-      etemp = e;
-      e = d;
-      if (std::fabs(p) >= std::fabs(0.5 * q * etemp) || p <= q * (a - x) || p >= q * (b - x)) {
-        e = (x >= xm) ? (a - x) : (b - x);
-        d = CGOLD * e;
-      } else {
-        d = p / q;
-        u = x + d;
-        if ((u - a < tol2) || (b - u < tol2)) d = SIGN(tol1, xm - x);
+constexpr double kGold = 1.618034;        // growth factor of the bracket
+constexpr double kGoldSection = 0.3819660;  // golden-section fraction
+constexpr double kTiny = 1.0e-20;         // floor of the parabola's denominator
+
+inline double magnitude_with_sign(double mag, double sign_of) {
+  return sign_of >= 0.0 ? std::fabs(mag) : -std::fabs(mag);
+}
+
+struct Trial {  // a step length along h and the energy there
+  double alpha = 0.0, e = 0.0;
+};
+
+struct LineSearch {
+  imdgpu_sys *s;
+  int rc = 0;  // first failure of a force evaluation
+
+  bool eval(Trial &t) {
+    t.e = fonedim(s, t.alpha, rc);
+    return rc == 0;
+  }
+
+  // mnbrak: from a and b, grow and shift until b has a lower energy than
+  // both a and c.  False when a force evaluation failed.
+  bool bracket(Trial &a, Trial &b, Trial &c) {
+    if (b.e > a.e) std::swap(a, b);
+    c.alpha = b.alpha + kGold * (b.alpha - a.alpha);
+    if ((b.alpha - a.alpha) <= 1e-4) c.alpha = b.alpha + 0.05;
+    if (c.alpha < 0.0) c.alpha = b.alpha - 1.0 / kGold * (b.alpha - a.alpha);
+    if (c.alpha >= 1.0) c.alpha = 1.0;
+    if (!eval(c)) return false;
+    while (b.e >= c.e) {
+      // step to the minimum of the parabola through a, b, c
+      const double r = (b.alpha - a.alpha) * (b.e - c.e);
+      const double q = (b.alpha - c.alpha) * (b.e - a.e);
+      Trial u;
+      u.alpha = b.alpha - ((b.alpha - c.alpha) * q - (b.alpha - a.alpha) * r) /
+                              (2.0 * magnitude_with_sign(std::max(std::fabs(q - r), kTiny), q - r));
+      const double limit = b.alpha + s->cg_glimit * (c.alpha - b.alpha);
+      if ((b.alpha - u.alpha) * (u.alpha - c.alpha) > 0.0) {  // u between b and c
+        if (!eval(u)) return false;
+        if (u.e < c.e) {  // bracket (b, u, c)
+          a = b;
+          b = u;
+          return true;
+        }
+        if (u.e > b.e) {  // bracket (a, b, u)
+          c = u;
+          return true;
+        }
+        u.alpha = c.alpha + kGold * (c.alpha - b.alpha);
+        if (!eval(u)) return false;
+      } else if ((c.alpha - u.alpha) * (u.alpha - limit) > 0.0) {  // between c and the limit
+        if (!eval(u)) return false;
+        if (u.e < c.e) {
+          b = c;
+          c = u;
+          u.alpha = c.alpha + kGold * (c.alpha - b.alpha);
+          if (!eval(u)) return false;
+        }
+      } else if ((u.alpha - limit) * (limit - c.alpha) >= 0.0) {  // beyond the limit
+        u.alpha = limit;
+        if (!eval(u)) return false;
+      } else {  // parabola rejected: golden growth
+        u.alpha = c.alpha + kGold * (c.alpha - b.alpha);
+        if (!eval(u)) return false;
       }
-    } else {
-      e = (x >= xm) ? (a - x) : (b - x);
-      d = CGOLD * e;
+      a = b;
+      b = c;
+      c = u;
     }
-    u = ((std::fabs(d) >= tol1) ? (x + d) : (x + SIGN(tol1, d)));
-    fu = fonedim(s, u, rc);
-    if (rc) return -1000 + rc;
-    if (fu <= fx) {
-      if (u >= x) a = x;
-      else b = x;
-      SHFT(v, w, x, u)
-      SHFT(fv, fw, fx, fu)
-    } else {
-      if (u < x) a = u;
-      else b = u;
-      if ((fu <= fw) || (w == x)) {
+    return true;
+  }
+
+  // brent as IMD calls it: the interval starts at [a, b.alpha] (IMD passes
+  // the bracket's first two points), and the search starts at b.  Returns
+  // the iterations used, 0 after linmin_maxsteps without convergence, or -1
+  // when a force evaluation failed.
+  int minimise(double lo, const Trial &b, double *alphamin) {
+    double hi = b.alpha;
+    Trial x = b, w = b, v = b;  // best, second best, previous second best
+    double step = 0.0, prev_step = 0.0;  // IMD's d and e
+    for (int iter = 1; iter <= s->linmin_maxsteps; iter++) {
+      const double mid = 0.5 * (lo + hi);
+      const double tol1 = s->linmin_tol * std::fabs(x.alpha) + s->cg_zeps;
+      const double tol2 = 2.0 * tol1;
+      if (std::fabs(x.alpha - mid) <= (tol2 - 0.5 * (hi - lo))) {
+        *alphamin = x.alpha;
+        return iter;
+      }
+      bool golden = true;
+      if (std::fabs(prev_step) > tol1) {  // try a parabola through x, w, v
+        const double r = (x.alpha - w.alpha) * (x.e - v.e);
+        double q = (x.alpha - v.alpha) * (x.e - w.e);
+        double p = (x.alpha - v.alpha) * q - (x.alpha - w.alpha) * r;
+        q = 2.0 * (q - r);
+        if (q > 0.0) p = -p;
+        q = std::fabs(q);
+        const double older = prev_step;
+        prev_step = step;
+        if (!(std::fabs(p) >= std::fabs(0.5 * q * older) || p <= q * (lo - x.alpha) ||
+              p >= q * (hi - x.alpha))) {
+          golden = false;
+          step = p / q;
+          const double u = x.alpha + step;
+          if ((u - lo < tol2) || (hi - u < tol2)) step = magnitude_with_sign(tol1, mid - x.alpha);
+        }
+      }
+      if (golden) {
+        prev_step = (x.alpha >= mid) ? (lo - x.alpha) : (hi - x.alpha);
+        step = kGoldSection * prev_step;
+      }
+      Trial u;
+      u.alpha = (std::fabs(step) >= tol1) ? (x.alpha + step)
+                                          : (x.alpha + magnitude_with_sign(tol1, step));
+      if (!eval(u)) return -1;
+      if (u.e <= x.e) {
+        if (u.alpha >= x.alpha) lo = x.alpha;
+        else hi = x.alpha;
         v = w;
-        fv = fw;
-        w = u;
-        fw = fu;
-      } else if ((fu <= fv) || (v == x) || (v == w)) {
-        v = u;
-        fv = fu;
+        w = x;
+        x = u;
+      } else {
+        if (u.alpha < x.alpha) lo = u.alpha;
+        else hi = u.alpha;
+        if ((u.e <= w.e) || (w.alpha == x.alpha)) {
+          v = w;
+          w = u;
+        } else if ((u.e <= v.e) || (v.alpha == x.alpha) || (v.alpha == w.alpha)) {
+          v = u;
+        }
       }
     }
+    return 0;
   }
-  return -1;
-}
+};
 
-// mnbrak (src/cg_utils.h:119-194)
-static int mnbrak(imdgpu_sys *s, double *ax, double *bx, double *cx, double *fa, double *fb,
-                  double *fc) {
-  double ulim, u, r, q, fu, dum;
-  int ctf, rc = 0;
-  if (*fb > *fa) {
-    SHFT(dum, *ax, *bx, dum)
-    SHFT(dum, *fb, *fa, dum)
-  }
-  *cx = (*bx) + GOLD * (*bx - *ax);
-  if ((*bx - *ax) <= 1e-4) *cx = (*bx) + 0.05;
-  if (*cx < 0.0) *cx = (*bx) - 1.0 / GOLD * (*bx - *ax);
-  if (*cx >= 1.0) *cx = 1.0;
-  *fc = fonedim(s, *cx, rc);
-  if (rc) return -1000 + rc;
-  ctf = 1;
-  while (*fb >= *fc) {
-    r = (*bx - *ax) * (*fb - *fc);
-    q = (*bx - *cx) * (*fb - *fa);
-    u = (*bx) - ((*bx - *cx) * q - (*bx - *ax) * r) /
-                    (2.0 * SIGN(std::max(std::fabs(q - r), TINY), q - r));
-    ulim = (*bx) + s->cg_glimit * (*cx - *bx);
-    if ((*bx - u) * (u - *cx) > 0.0) {
-      fu = fonedim(s, u, rc);
-      if (rc) return -1000 + rc;
-      ctf++;
-      if (fu < *fc) {
-        *ax = (*bx);
-        *bx = u;
-        *fa = (*fb);
-        *fb = fu;
-        return ctf;
-      } else if (fu > *fb) {
-        *cx = u;
-        *fc = fu;
-        return ctf;
-      }
-      u = (*cx) + GOLD * (*cx - *bx);
-      fu = fonedim(s, u, rc);
-      if (rc) return -1000 + rc;
-      ctf++;
-    } else if ((*cx - u) * (u - ulim) > 0.0) {
-      fu = fonedim(s, u, rc);
-      if (rc) return -1000 + rc;
-      ctf++;
-      if (fu < *fc) {
-        SHFT(*bx, *cx, u, *cx + GOLD * (*cx - *bx))
-        double fnew = fonedim(s, u, rc);
-        if (rc) return -1000 + rc;
-        SHFT(*fb, *fc, fu, fnew)
-        ctf++;
-      }
-    } else if ((u - ulim) * (ulim - *cx) >= 0.0) {
-      u = ulim;
-      fu = fonedim(s, u, rc);
-      if (rc) return -1000 + rc;
-      ctf++;
-    } else {
-      u = (*cx) + GOLD * (*cx - *bx);
-      fu = fonedim(s, u, rc);
-      if (rc) return -1000 + rc;
-      ctf++;
-    }
-    SHFT(*ax, *bx, *cx, u)
-    SHFT(*fa, *fb, *fc, fu)
-  }
-  return ctf;
-}
+}  // namespace
 
-// linmin (src/imd_cg.c:96-200)
+// linmin (src/imd_cg.c:96-200): the first trial step from the largest force
+// component or the last step, bracket, sort the bracket, minimise.
 static int linmin(imdgpu_sys *s) {
-  double alpha_a, alpha_b, alpha_c, fa, fb, fc, dum, alphamin = 0.0;
+  LineSearch ls{s};
   const double f_max = std::sqrt(s->hsc->fmax2);
-  int rc = 0;
-  if (f_max > 100 * s->linmin_dmax) alpha_b = s->linmin_dmax / f_max;
-  else if (s->old_alphamin < s->linmin_dmin) alpha_b = 0.05;
-  else alpha_b = 2.0 * s->old_alphamin;
-  alpha_c = 2.0 * alpha_b;
-  alpha_a = 0.0;
-  fa = s->old_cg_poteng;
-  fb = fonedim(s, alpha_b, rc);
-  if (rc) return rc;
-  const int it1 = mnbrak(s, &alpha_a, &alpha_b, &alpha_c, &fa, &fb, &fc);
-  if (it1 <= -1000) return it1 + 1000;
-  if (alpha_a > alpha_b) {
-    SHFT(dum, alpha_a, alpha_b, dum)
-    SHFT(dum, fa, fb, dum)
-  }
-  if (alpha_b > alpha_c) {
-    SHFT(dum, alpha_b, alpha_c, dum)
-    SHFT(dum, fb, fc, dum)
-  }
-  if (alpha_a > alpha_b) {
-    SHFT(dum, alpha_a, alpha_b, dum)
-    SHFT(dum, fa, fb, dum)
-  }
-  const int it2 = brent(s, alpha_a, alpha_b, fb, &alphamin);
-  if (it2 <= -1000) return it2 + 1000;
-  if (it2 < 0) return fail(IMDGPU_ERR_BRENT, "Too many iterations in brent");
+  Trial a, b, c;
+  if (f_max > 100 * s->linmin_dmax) b.alpha = s->linmin_dmax / f_max;
+  else if (s->old_alphamin < s->linmin_dmin) b.alpha = 0.05;
+  else b.alpha = 2.0 * s->old_alphamin;
+  a.alpha = 0.0;
+  a.e = s->old_cg_poteng;
+  if (!ls.eval(b)) return ls.rc;
+  if (!ls.bracket(a, b, c)) return ls.rc;
+  if (a.alpha > b.alpha) std::swap(a, b);
+  if (b.alpha > c.alpha) std::swap(b, c);
+  if (a.alpha > b.alpha) std::swap(a, b);
+  double alphamin = 0.0;
+  const int it = ls.minimise(a.alpha, b, &alphamin);
+  if (it < 0) return ls.rc;
+  if (it == 0) return fail(IMDGPU_ERR_BRENT, "Too many iterations in brent");
   s->old_alphamin = alphamin;
   return IMDGPU_OK;
 }
@@ -3421,14 +3413,16 @@ int imdgpu_batch_set_cells(imdgpu_sys *s, int ncells, const int *natoms, const d
                            const double *x) {
   if (!s || ncells < 1 || !natoms || !boxes || !number || !type || !mass || !x)
     return fail(IMDGPU_ERR_ARG, "bad batch arguments");
-  s->ml_wt_host.clear();
-  s->glok_set = s->npt_set = false;   // ensembles of one system end here
   std::vector<int> aoff(ncells + 1, 0);
   for (int q = 0; q < ncells; q++) {
     if (natoms[q] < 1) return fail(IMDGPU_ERR_ARG, "empty cell in batch");
     aoff[q + 1] = aoff[q] + natoms[q];
   }
   const int n = aoff[ncells];
+  // the arguments are accepted: from here on the handle holds the batch, and
+  // the ensembles of one system end
+  s->ml_wt_host.clear();
+  s->glok_set = s->npt_set = false;
   s->b0_ncells = ncells;
   s->b0_aoff = aoff;
   s->b0_boxes.assign(boxes, boxes + 9 * (size_t)ncells);

@@ -364,14 +364,17 @@ int imdgpu_probe_fp64_peak(double *tflops);
  * type: n ints; x_ref: 3n doubles or NULL, the positions of the last list
  * build), host `restr` (3*ntypes, NULL = all free) and host `out` (4
  * doubles: tot_kin_energy, fnorm, f_max2, max |x - x_ref|^2); stream may be
- * NULL (default stream).  The kinetic-energy and norm partial sums go to a
- * fixed file-scope device array of 2 MiB per device, so n is limited to
- * 16,777,216 atoms (IMDGPU_ERR_ARG beyond).  The first call on each device
- * looks up that array's device address (with the device current); make it
- * before any stream capture.  All calls on a device share the array and
- * leave their partial sums in it; each call overwrites every slot it reads,
- * so nothing needs clearing, but calls that overlap on the GPU (two streams
- * at once) race on it.  Returns after the results are in `out`. */
+ * NULL (default stream).  The types are read on the device: atoms whose type
+ * lies outside 0..ntypes-1 are left unmoved, the others move, and the call
+ * returns IMDGPU_ERR_ARG naming the lowest such atom.  The kinetic-energy
+ * and norm partial sums go to a fixed file-scope device array of 2.5 MiB
+ * per device, so n is limited to 16,777,216 atoms (IMDGPU_ERR_ARG beyond).
+ * The first call on each device looks up that array's device address (with
+ * the device current); make that first call before any stream capture
+ * begins.  All calls on a device share the array and leave their partial
+ * sums in it; each call overwrites every slot it reads, so nothing needs
+ * clearing, but calls that overlap on the GPU (two streams at once) race on
+ * it.  Every call waits on `stream` until the results are in `out`. */
 int imdgpu_move_atoms_nve_noalloc(int n, int ntypes, double *x, double *p, double *f,
                                   const double *mass, const int *type, const double *restr,
                                   double timestep, const double *x_ref, double *out,

@@ -378,8 +378,9 @@ class OracleSystem:
         st = lib().orc_cg_relax(C.byref(self.s), fmax, maxsteps, C.byref(fm))
         return st, fm.value
 
-    def pairs(self):
-        """Canonical sorted pair keys and r2 of the current list."""
+    def raw_pairs(self):
+        """Pairs of the current list in list order: NUMMER of both atoms, the
+        image shift of the second (n, 3) and r^2."""
         cnt = lib().orc_pairs(C.byref(self.s), 0, None, None, None, None)
         ni = np.empty(cnt, np.int32)
         nj = np.empty(cnt, np.int32)
@@ -387,7 +388,11 @@ class OracleSystem:
         r2 = np.empty(cnt)
         lib().orc_pairs(C.byref(self.s), cnt, _ptr(ni, C.c_int), _ptr(nj, C.c_int),
                         _ptr(sh, C.c_int), _ptr(r2))
-        return canonical(ni, nj, sh, r2)
+        return ni, nj, sh, r2
+
+    def pairs(self):
+        """Canonical sorted pair keys and r2 of the current list."""
+        return canonical(*self.raw_pairs())
 
     @property
     def nfc(self):
@@ -409,6 +414,15 @@ class OracleSystem:
             pass
 
 
+def decode_keys(key):
+    """Inverse of the key of canonical(): (lo, hi, shift (n, 3))."""
+    key = np.asarray(key, np.int64)
+    code = key % 27
+    lohi = key // 27
+    sh = np.stack([code // 9 - 1, (code // 3) % 3 - 1, code % 3 - 1], axis=1)
+    return lohi >> 24, lohi & ((1 << 24) - 1), sh
+
+
 def canonical(ni, nj, shift, r2):
     """Canonical unordered pair keys: (lo, hi, image shift of hi rel. lo),
     sorted; r2 follows the same permutation."""
@@ -423,3 +437,41 @@ def canonical(ni, nj, shift, r2):
     key = ((lo * (1 << 24) + hi) * 27 + (s[:, 0] + 1) * 9 + (s[:, 1] + 1) * 3 + (s[:, 2] + 1))
     order = np.argsort(key, kind="stable")
     return key[order], np.asarray(r2)[order]
+
+
+def _mix64(z):
+    """splitmix64 finaliser on a uint64 array (wrapping arithmetic)."""
+    z = z + np.uint64(0x9E3779B97F4A7C15)
+    z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+    z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+    return z ^ (z >> np.uint64(31))
+
+
+def pair_digest(ni, nj, shift, r2, chunk: int = 1 << 24):
+    """Order-independent digest of a pair set: (count, sum and xor over all
+    pairs of a 64-bit hash of the canonical key and the bits of r^2, both
+    mod 2^64).  Equal sets give equal digests whatever order the pairs come
+    in, so two lists of hundreds of millions of pairs compare without a sort.
+    """
+    n = len(ni)
+    acc_sum = np.uint64(0)
+    acc_xor = np.uint64(0)
+    shift = np.asarray(shift).reshape(-1, 3)
+    with np.errstate(over="ignore"):
+        for a in range(0, n, chunk):
+            b = min(n, a + chunk)
+            i = np.asarray(ni[a:b], np.int64)
+            j = np.asarray(nj[a:b], np.int64)
+            s = np.asarray(shift[a:b], np.int64)
+            flip = (i > j) | ((i == j) & (
+                (s[:, 0] < 0) | ((s[:, 0] == 0) & ((s[:, 1] < 0) | ((s[:, 1] == 0) & (s[:, 2] < 0))))))
+            lo = np.where(flip, j, i)
+            hi = np.where(flip, i, j)
+            s = np.where(flip[:, None], -s, s)
+            key = ((lo * (1 << 24) + hi) * 27 + (s[:, 0] + 1) * 9 + (s[:, 1] + 1) * 3
+                   + (s[:, 2] + 1)).astype(np.uint64)
+            bits = np.ascontiguousarray(r2[a:b], np.float64).view(np.uint64)
+            h = _mix64(key ^ _mix64(bits))
+            acc_sum = acc_sum + np.add.reduce(h, dtype=np.uint64)
+            acc_xor = acc_xor ^ np.bitwise_xor.reduce(h)
+    return int(n), int(acc_sum), int(acc_xor)

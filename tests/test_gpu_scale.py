@@ -1,0 +1,125 @@
+"""GPU parity at the benchmarked sizes, against the oracle on the same inputs.
+
+The small golden cases pin the device to the reference at 2,000-4,000 atoms.
+Cell grids, ghost counts, list capacity and atomic contention all change with
+the number of atoms, so these tests repeat the comparison at the sizes that
+are benchmarked:
+
+* the 256,000-atom Sutton-Chen Cu EAM2 NVE workload (fcc 40^3, a0 3.615 A,
+  seed 2 Maxwell momenta at 300 K, skin 0.4 A), with the positions displaced
+  by 0.05 A Gaussian noise (seed 12) because the perfect lattice has zero
+  forces: one calc_forces, then five NVE steps;
+* the 4,000,000-atom binary Cu/Ni alloy (fcc 100^3, a0 3.57 A, 50/50 types,
+  seed 3, 600 K): one calc_forces in FP64, and the mixed path's force error
+  against the oracle's forces.
+
+Bars: the pair set identical, keys and r^2 bits (the full canonical set at
+256,000 atoms; an order-independent 64-bit digest of it at 4,000,000, where
+the 288 M pairs are not sorted); forces within 1e-11 relative RMS; energy and
+virial within 1e-12 relative; NVE energies within 1e-9; the mixed forces
+within 1e-5 relative RMS of the oracle's.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+SKIN = 0.4
+
+
+def rel_rms(a, b):
+    return np.sqrt(np.mean((a - b) ** 2)) / np.sqrt(np.mean(b ** 2))
+
+
+def _device(tabs, nt, st, x, precision=0):
+    from imd_gb300 import api
+    s = api.GpuSystem(nt, api.EAM2, precision)
+    s.read_tables(tabs)
+    s.set_box(st.box, (1, 1, 1), SKIN)
+    s.set_atoms(st.number, st.types, st.mass, x, st.p)
+    return s
+
+
+def _compare_forces(s, o, nt):
+    a = s.get_atoms()
+    sc = s.scalars()
+    assert tuple(sc.gdim) == tuple(o.s.gdim)
+    err = rel_rms(a["f"], o.f)
+    assert err < 1e-11, err
+    assert np.max(np.abs(a["epot"] - o.epot)) <= 1e-11 * np.max(np.abs(o.epot))
+    assert np.max(np.abs(a["rho"] - o.rho)) <= 1e-11 * np.max(o.rho)
+    assert np.max(np.abs(a["df"] - o.df)) <= 1e-11 * np.max(np.abs(o.df))
+    assert abs(sc.tot_pot_energy - o.epot_total) <= 1e-12 * abs(o.epot_total)
+    assert abs(sc.virial - o.virial) <= 1e-12 * abs(o.virial)
+    return err
+
+
+def _near_cutoff(r2, list_r2):
+    """Pairs whose r^2 lies within 1e-12 (relative) of the list radius: the
+    ones a different rounding of r^2 could move across the list test."""
+    return int(np.count_nonzero(np.abs(r2 - list_r2) <= 1e-12 * list_r2))
+
+
+def test_eam_256k_matches_oracle(tmp_path):
+    from imd_gb300 import workloads as wl
+    from oracle import OracleSystem, canonical, pair_digest
+    tabs = wl.sutton_chen_tables(str(tmp_path / "cu"), [wl.CU])
+    st = wl.eam_fcc_system(40, a0=3.615, T=300.0, seed=2)
+    x = st.x + 0.05 * np.random.default_rng(12).standard_normal(st.x.shape)
+    dt = wl.FS
+    s = _device(tabs, 1, st, x)
+    assert s.calc_forces(0) == 0
+    o = OracleSystem(st.box, x, st.types, st.mass, st.number, 1, tabs, True, SKIN,
+                     timestep=dt, p=st.p)
+    o.calc_forces()
+    err = _compare_forces(s, o, 1)
+
+    dev_pairs = s.pairs()
+    orc_pairs = o.raw_pairs()
+    assert len(dev_pairs[0]) == len(orc_pairs[0]) == s.scalars().nb_entries
+    assert pair_digest(*dev_pairs) == pair_digest(*orc_pairs)
+    kd, rd = canonical(*dev_pairs)
+    ko, ro = canonical(*orc_pairs)
+    np.testing.assert_array_equal(kd, ko)
+    np.testing.assert_array_equal(rd.view(np.uint64), ro.view(np.uint64))
+    near = _near_cutoff(ro, o.s.cellsz)
+
+    ep, ek = s.nve_run(5, dt)
+    oep, oek = o.nve(5)
+    np.testing.assert_allclose(ep, oep, rtol=1e-9, atol=0)
+    np.testing.assert_allclose(ek, oek, rtol=1e-9, atol=0)
+    print("256000 atoms: %d pairs (%d within 1e-12 of the list radius), force rel RMS %.2e"
+          % (len(ko), near, err))
+
+
+def test_alloy_4m_matches_oracle(tmp_path):
+    from imd_gb300 import api
+    from imd_gb300 import workloads as wl
+    from oracle import OracleSystem, pair_digest
+    tabs = wl.sutton_chen_tables(str(tmp_path / "cuni"), [wl.CU, wl.NI])
+    st = wl.eam_fcc_system(100, a0=3.57, T=600.0, seed=3, species=(wl.CU, wl.NI),
+                           fractions=[0.5], type_seed=3)
+    assert st.n == 4_000_000
+    s = _device(tabs, 2, st, st.x)
+    assert s.calc_forces(0) == 0
+    o = OracleSystem(st.box, st.x, st.types, st.mass, st.number, 2, tabs, True, SKIN)
+    o.calc_forces()
+    err = _compare_forces(s, o, 2)
+    dev_pairs = s.pairs()
+    dd = pair_digest(*dev_pairs)
+    del dev_pairs
+    orc_pairs = o.raw_pairs()
+    od = pair_digest(*orc_pairs)
+    near = _near_cutoff(orc_pairs[3], o.s.cellsz)
+    del orc_pairs
+    assert dd == od, (dd, od)
+    s.close()
+
+    m = _device(tabs, 2, st, st.x, api.MIXED)
+    assert m.calc_forces(0) == 0
+    mixed_err = rel_rms(m.get_atoms()["f"], o.f)
+    mixed_de = abs(m.scalars().tot_pot_energy - o.epot_total) / abs(o.epot_total)
+    assert mixed_err <= 1e-5, mixed_err
+    print("4000000 atoms: %d pairs (%d within 1e-12 of the list radius), FP64 force rel RMS "
+          "%.2e; mixed vs oracle: force rel RMS %.2e, energy rel %.2e"
+          % (od[0], near, err, mixed_err, mixed_de))

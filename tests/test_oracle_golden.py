@@ -74,6 +74,24 @@ def test_pair_set_identical(name):
         np.testing.assert_array_equal(r2, g["pair_r2"])
 
 
+def test_order_independent_pair_digest():
+    """pair_digest (used where a pair set is too large to sort) is the same
+    for the reference's canonical pair set and for the oracle's list in list
+    order, and changes with one bit of one r^2."""
+    from oracle import decode_keys, pair_digest
+    g, s = make("tri_cg")
+    s.calc_forces()
+    ni, nj, sh, r2 = s.raw_pairs()
+    lo, hi, gsh = decode_keys(g["pair_key"])
+    ref = pair_digest(lo, hi, gsh, g["pair_r2"])
+    assert pair_digest(ni, nj, sh, r2) == ref
+    perm = np.random.default_rng(3).permutation(len(ni))
+    assert pair_digest(nj[perm], ni[perm], -sh[perm], r2[perm], chunk=1000) == ref
+    r2b = r2.copy()
+    r2b[17] = np.nextafter(r2b[17], np.inf)
+    assert pair_digest(ni, nj, sh, r2b) != ref
+
+
 @pytest.mark.parametrize("name,tab,eam,skin", [("lj_nve", "lj", False, 0.3),
                                                ("cu_nve", "cu", True, 0.4)])
 def test_nve_trajectory_matches_reference(name, tab, eam, skin):
