@@ -777,6 +777,18 @@ static void stress_pair(double *pp, double *sj, double dx, double dy, double dz,
   }
 }
 
+/* Neumaier's compensated summation (a published refinement of Kahan's).
+ * IMD sums the energy and the virial of every pair into one running FP64
+ * total, which loses about (terms x eps) relative: 1e-9 at 4 million atoms.
+ * The compensated totals beside them are accurate to a few ulps and serve as
+ * the reference for summation orders other than IMD's. */
+static inline void csum_add(double acc[2], double v) {
+  double t = acc[0] + v;
+  if (fabs(acc[0]) >= fabs(v)) acc[1] += (acc[0] - t) + v;
+  else acc[1] += (v - t) + acc[0];
+  acc[0] = t;
+}
+
 /* calc_forces (src/imd_forces_nbl.c:281-1999), PAIR + EAM2 */
 int orc_calc_forces(orc_sys_t *s) {
   int n = s->n, nt = s->ntypes, inc = nt * nt;
@@ -787,6 +799,7 @@ int orc_calc_forces(orc_sys_t *s) {
   s->tot_pot_energy = 0.0;
   s->virial = 0.0;
   s->vir_axial[0] = s->vir_axial[1] = s->vir_axial[2] = 0.0;
+  double e_acc[2] = {0.0, 0.0}, v_acc[2] = {0.0, 0.0};
   s->nfc++;
   for (int g = 0; g < s->next; g++) {
     s->ef[3 * g] = s->ef[3 * g + 1] = s->ef[3 * g + 2] = 0.0;
@@ -814,6 +827,7 @@ int orc_calc_forces(orc_sys_t *s) {
         double pot, grad;
         orc_pair_int2(&s->pair, col, inc, r2, &pot, &grad, &s->is_short);
         s->tot_pot_energy += pot;
+        csum_add(e_acc, pot);
         double fx = dx * grad, fy = dy * grad, fz = dz * grad;
         s->ef[3 * j] -= fx;
         s->ef[3 * j + 1] -= fy;
@@ -825,6 +839,7 @@ int orc_calc_forces(orc_sys_t *s) {
         ee += pot;
         s->eepot[j] += pot;
         s->virial -= r2 * grad;
+        csum_add(v_acc, -(r2 * grad));
         s->vir_axial[0] -= dx * fx;
         s->vir_axial[1] -= dy * fy;
         s->vir_axial[2] -= dz * fz;
@@ -866,6 +881,7 @@ int orc_calc_forces(orc_sys_t *s) {
       s->edf[i] = df;
       s->eepot[i] += pot;
       s->tot_pot_energy += pot;
+      csum_add(e_acc, pot);
     }
     /* send_cells(copy_dF) (:1115) */
     for (int g = n; g < s->next; g++) s->edf[g] = s->edf[s->esrc[g]];
@@ -898,6 +914,7 @@ int orc_calc_forces(orc_sys_t *s) {
           ffy += fy;
           ffz += fz;
           s->virial -= dx * fx + dy * fy + dz * fz;
+          csum_add(v_acc, -(dx * fx + dy * fy + dz * fz));
           s->vir_axial[0] -= dx * fx;
           s->vir_axial[1] -= dy * fy;
           s->vir_axial[2] -= dz * fz;
@@ -939,6 +956,8 @@ int orc_calc_forces(orc_sys_t *s) {
       s->eam_df[i] = s->edf[i];
     }
   }
+  s->tot_pot_energy_c = e_acc[0] + e_acc[1];
+  s->virial_c = v_acc[0] + v_acc[1];
   return 0;
 }
 

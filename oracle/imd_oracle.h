@@ -141,6 +141,9 @@ typedef struct {
   /* ---- P_AXIAL (src/imd_forces_nbl.c:548-553, :1275-1278): vir_xx, vir_yy,
    * vir_zz of the last calc_forces, summed beside the virial ---- */
   double  vir_axial[3];
+  /* tot_pot_energy and virial of the last calc_forces by compensated
+   * summation (accurate to a few ulps, unlike IMD's running sums) */
+  double  tot_pot_energy_c, virial_c;
 } orc_sys_t;
 
 /* set defaults; allocate per-atom arrays for n atoms */

@@ -60,7 +60,8 @@ class Sys(C.Structure):
         ("do_stress", C.c_int), ("estress", _dp), ("stress", _dp),
         ("tot_stress", C.c_double * 6),
         ("eta", C.c_double), ("isq_tau_eta", C.c_double), ("temperature", C.c_double),
-        ("vir_axial", C.c_double * 3)]
+        ("vir_axial", C.c_double * 3), ("tot_pot_energy_c", C.c_double),
+        ("virial_c", C.c_double)]
 
 
 class Glok(C.Structure):
@@ -279,6 +280,16 @@ class OracleSystem:
     @property
     def virial(self):
         return self.s.virial
+
+    @property
+    def epot_total_exact(self):
+        """tot_pot_energy by compensated summation (IMD's running sum loses
+        about terms x eps relative at large N)."""
+        return self.s.tot_pot_energy_c
+
+    @property
+    def virial_exact(self):
+        return self.s.virial_c
 
     @property
     def ekin(self):

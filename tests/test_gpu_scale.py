@@ -16,8 +16,10 @@ are benchmarked:
 Bars: the pair set identical, keys and r^2 bits (the full canonical set at
 256,000 atoms; an order-independent 64-bit digest of it at 4,000,000, where
 the 288 M pairs are not sorted); forces within 1e-11 relative RMS; energy and
-virial within 1e-12 relative; NVE energies within 1e-9; the mixed forces
-within 1e-5 relative RMS of the oracle's.
+virial within 1e-12 relative of the oracle's compensated sums (IMD's own
+running sum over every pair carries about pairs x eps relative error: 1e-9 at
+4 M atoms, so the reference's order is not the yardstick there); NVE energies
+within 1e-9; the mixed forces within 1e-5 relative RMS of the oracle's.
 """
 import numpy as np
 import pytest
@@ -49,8 +51,15 @@ def _compare_forces(s, o, nt):
     assert np.max(np.abs(a["epot"] - o.epot)) <= 1e-11 * np.max(np.abs(o.epot))
     assert np.max(np.abs(a["rho"] - o.rho)) <= 1e-11 * np.max(o.rho)
     assert np.max(np.abs(a["df"] - o.df)) <= 1e-11 * np.max(np.abs(o.df))
-    assert abs(sc.tot_pot_energy - o.epot_total) <= 1e-12 * abs(o.epot_total)
-    assert abs(sc.virial - o.virial) <= 1e-12 * abs(o.virial)
+    # totals against the oracle's compensated sums: IMD's own running sum
+    # over every pair loses about (pairs x eps) relative, 1e-9 at 4 M atoms,
+    # while the device sums per atom and then over a fixed tree
+    assert abs(sc.tot_pot_energy - o.epot_total_exact) <= 1e-12 * abs(o.epot_total_exact)
+    assert abs(sc.virial - o.virial_exact) <= 1e-12 * abs(o.virial_exact)
+    imd_order = max(abs(o.epot_total - o.epot_total_exact) / abs(o.epot_total_exact),
+                    abs(o.virial - o.virial_exact) / abs(o.virial_exact))
+    print("IMD-order running sums differ from the compensated ones by %.1e relative"
+          % imd_order)
     return err
 
 
@@ -118,7 +127,7 @@ def test_alloy_4m_matches_oracle(tmp_path):
     m = _device(tabs, 2, st, st.x, api.MIXED)
     assert m.calc_forces(0) == 0
     mixed_err = rel_rms(m.get_atoms()["f"], o.f)
-    mixed_de = abs(m.scalars().tot_pot_energy - o.epot_total) / abs(o.epot_total)
+    mixed_de = abs(m.scalars().tot_pot_energy - o.epot_total_exact) / abs(o.epot_total_exact)
     assert mixed_err <= 1e-5, mixed_err
     print("4000000 atoms: %d pairs (%d within 1e-12 of the list radius), FP64 force rel RMS "
           "%.2e; mixed vs oracle: force rel RMS %.2e, energy rel %.2e"

@@ -53,6 +53,9 @@ def test_forces_match_reference(name):
     assert np.max(np.abs(s.epot - g["epot"])) <= 1e-11 * np.max(np.abs(g["epot"]))
     assert abs(s.epot_total - g["epot_total"]) <= 1e-12 * abs(g["epot_total"])
     assert abs(s.virial - g["virial"]) <= 1e-12 * abs(g["virial"])
+    # the compensated totals sum the same terms
+    assert abs(s.epot_total_exact - g["epot_total"]) <= 1e-12 * abs(g["epot_total"])
+    assert abs(s.virial_exact - g["virial"]) <= 1e-12 * abs(g["virial"])
     if CASES[name][1]:
         assert np.max(np.abs(s.rho - g["rho"])) <= 1e-11 * np.max(g["rho"])
         assert np.max(np.abs(s.df - g["df"])) <= 1e-11 * np.max(np.abs(g["df"]))
