@@ -1,7 +1,8 @@
 /******************************************************************************
 *
-* imd_forces_cuda.c -- IMD's force, neighbour-list and NVE entry points on
-* libimdgpu, the GB300 implementation of that path (IMD make target `cuda`).
+* imd_forces_cuda.c -- IMD's force, neighbour-list, integrator and CG entry
+* points on libimdgpu, the GB300 implementation of that path (IMD make
+* target `cuda`).
 *
 * This file takes the place of src/imd_forces_nbl.c in the link of IMD's
 * serial NBL build.  It defines the symbols that file exports
@@ -10,19 +11,25 @@
 *   check_nblist          :2007
 *   deallocate_nblist     :56
 *   estimate_nblist_size  :74
-* and move_atoms_nve (src/imd_integrate.c:32), the integrator of ensemble
-* nve that main_loop calls through the move_atoms pointer
-* (src/imd_param.c:382).  The cuda target compiles imd_integrate.c with
-* -Dmove_atoms_nve=move_atoms_nve_host, so IMD's own NVE integrator keeps
-* existing under another name and every other IMD source compiles unchanged.
+* and the integrators that main_loop calls through the move_atoms pointer
+* (src/imd_param.c:382-390): move_atoms_nve (src/imd_integrate.c:32),
+* move_atoms_mik (:675) and move_atoms_nvt (:891).  The cuda target
+* compiles imd_integrate.c with -Dmove_atoms_nve=move_atoms_nve_host (and
+* likewise for _mik and _nvt), so IMD's own integrators keep existing under
+* other names and every other IMD source compiles unchanged.  In the CG
+* build (option cg) the target links this file in place of src/imd_cg.c as
+* well: reset_cg and cg_step (src/imd_cg.c:30, :46) run IMD's CG on the
+* device (linmin, mnbrak, brent, cg_calcgamma, set_hg).
 *
 * Who owns the atoms.  From the first calc_forces of a phase on, the library
 * holds positions, momenta and forces on the device; the step runs there
-* (calc_forces, move_atoms_nve, check_nblist), and IMD's cell arrays are
-* stale.  They are brought up to date on the steps where main_loop reads
-* them (src/imd_main_3d.c:690-694, :792-797, :814): checkpoint, distribution
-* and picture steps, the steps where it looks for a write or stop file, every
-* step when a wall-time limit is set, and the last step of the phase.  After
+* (calc_forces or cg_step, move_atoms_*, check_nblist), and IMD's cell
+* arrays are stale.  They are brought up to date on the steps where main_loop
+* reads them (src/imd_main_3d.c:690-694, :760, :792-797, :814): checkpoint,
+* distribution and picture steps, the steps where it looks for a write or
+* stop file, every step when a wall-time limit is set, the step where
+* check_relaxed will find a MIK or CG relaxation done (it writes the relaxed
+* configuration), and the last step of the phase.  After
 * the last step the cell arrays are the authority again: the next phase
 * uploads them (with its box and restrictions) at its first calc_forces.
 *
@@ -219,6 +226,22 @@ static void copy_back_to_cells(void)
   free(x); free(p); free(f); free(e); free(rho); free(df);
 }
 
+#ifdef RELAX
+/* check_relaxed (src/imd_main_3d.c:1741-1770) after this step will find the
+ * system relaxed and write it out: the same test on the same globals, made
+ * before check_relaxed updates old_epot */
+static int will_be_relaxed(void)
+{
+  real fnorm2 = SQRT(fnorm / nactive);
+  real ekin = 2 * tot_kin_energy / nactive;
+  real epot = tot_pot_energy / natoms;
+  real delta_epot = old_epot - epot;
+  if (delta_epot < 0) delta_epot = -delta_epot;
+  return (ekin < ekin_threshold) || (fnorm2 < fnorm_threshold) ||
+         (delta_epot < delta_epot_threshold);
+}
+#endif
+
 /* main_loop reads the cell arrays after the move of this step */
 static int cells_read_after(int st)
 {
@@ -229,7 +252,18 @@ static int cells_read_after(int st)
   if (watch_int > 0 && 0 == st % watch_int) return 1;   /* check_write */
   if (stop_int > 0 && 0 == st % stop_int) return 1;     /* check_stop */
   if (maxwalltime > 0) return 1;                         /* check_walltime */
+#ifdef RELAX
+  if ((ensemble == ENS_MIK || ensemble == ENS_CG) && will_be_relaxed()) return 1;
+#endif
   return 0;
+}
+
+static void after_step(int st)
+{
+  if (cells_read_after(st)) {
+    copy_back_to_cells();
+    if (st >= steps_max) host_owns_atoms = 1;
+  }
 }
 
 static void read_scalars(imdgpu_scalars *sc)
@@ -298,18 +332,91 @@ int estimate_nblist_size(void)
 *  move_atoms_nve (src/imd_integrate.c:32-497), ensemble nve
 ******************************************************************************/
 
-void move_atoms_nve(void)
+static void read_move_scalars(void)
 {
   imdgpu_scalars sc;
-  lib_check(imdgpu_move_atoms_nve(G, timestep), "move_atoms_nve");
   read_scalars(&sc);
   tot_kin_energy = sc.tot_kin_energy;
   fnorm = sc.fnorm;
 #ifdef FNORM
   f_max2 = sc.f_max2;
 #endif
-  if (cells_read_after(steps)) {
-    copy_back_to_cells();
-    if (steps >= steps_max) host_owns_atoms = 1;
-  }
 }
+
+void move_atoms_nve(void)
+{
+  lib_check(imdgpu_move_atoms_nve(G, timestep), "move_atoms_nve");
+  read_move_scalars();
+  after_step(steps);
+}
+
+/******************************************************************************
+*  move_atoms_mik (src/imd_integrate.c:675-873): NVE with microconvergence
+******************************************************************************/
+
+void move_atoms_mik(void)
+{
+#ifdef MIK
+  lib_check(imdgpu_move_atoms_mik(G, timestep), "move_atoms_mik");
+  read_move_scalars();
+  after_step(steps);
+#else
+  error("the chosen ensemble MIK is not supported by this binary");
+#endif
+}
+
+/******************************************************************************
+*  move_atoms_nvt (src/imd_integrate.c:891-1150): Nose-Hoover NVT; eta moves
+*  between IMD's global and the library every step
+******************************************************************************/
+
+void move_atoms_nvt(void)
+{
+#ifdef NVT
+  double e = eta;
+  lib_check(imdgpu_set_nvt(G, temperature, isq_tau_eta, eta, nactive), "imdgpu_set_nvt");
+  lib_check(imdgpu_move_atoms_nvt(G, timestep), "move_atoms_nvt");
+  lib_check(imdgpu_get_nvt(G, &e), "imdgpu_get_nvt");
+  eta = e;
+  read_move_scalars();
+  after_step(steps);
+#else
+  error("the chosen ensemble NVT is not supported by this binary");
+#endif
+}
+
+#ifdef CG
+/******************************************************************************
+*  reset_cg, cg_step (src/imd_cg.c:30-66): IMD's CG with its parameters
+*  (linmin_*, cg_glimit, cg_zeps, cg_fr, cg_reset_int; src/globals.h:711-719)
+******************************************************************************/
+
+static void read_cg_scalars(void)
+{
+  imdgpu_scalars sc;
+  read_scalars(&sc);
+  tot_pot_energy = sc.tot_pot_energy;
+  virial = sc.virial;
+  fnorm = sc.fnorm;
+  f_max2 = sc.f_max2;
+}
+
+void reset_cg(void)
+{
+  if (!G) create_system();
+  if (host_owns_atoms) upload_state();
+  lib_check(imdgpu_set_cg_params(G, linmin_maxsteps, linmin_tol, linmin_dmax, linmin_dmin,
+                                 cg_glimit, cg_zeps, cg_fr, cg_reset_int),
+            "imdgpu_set_cg_params");
+  lib_check(imdgpu_reset_cg(G), "reset_cg");
+  read_cg_scalars();
+}
+
+void cg_step(int st)
+{
+  if (host_owns_atoms) reset_cg();
+  lib_check(imdgpu_cg_step(G, st), "cg_step");
+  read_cg_scalars();
+  after_step(st);
+}
+#endif

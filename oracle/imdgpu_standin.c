@@ -212,3 +212,53 @@ int imdgpu_move_atoms_nve(imdgpu_sys *g, double timestep) {
   orc_move_atoms_nve(&g->s);
   return IMDGPU_OK;
 }
+
+int imdgpu_move_atoms_mik(imdgpu_sys *g, double timestep) {
+  g->s.timestep = timestep;
+  orc_move_atoms_mik(&g->s);
+  return IMDGPU_OK;
+}
+
+int imdgpu_set_nvt(imdgpu_sys *g, double temperature, double isq_tau_eta, double eta,
+                   long nactive) {
+  g->s.temperature = temperature;
+  g->s.isq_tau_eta = isq_tau_eta;
+  g->s.eta = eta;
+  g->s.nactive = nactive > 0 ? nactive : 3L * g->s.n;
+  return IMDGPU_OK;
+}
+
+int imdgpu_get_nvt(imdgpu_sys *g, double *eta) {
+  *eta = g->s.eta;
+  return IMDGPU_OK;
+}
+
+int imdgpu_move_atoms_nvt(imdgpu_sys *g, double timestep) {
+  g->s.timestep = timestep;
+  orc_move_atoms_nvt(&g->s);
+  return IMDGPU_OK;
+}
+
+int imdgpu_set_cg_params(imdgpu_sys *g, int linmin_maxsteps, double linmin_tol,
+                         double linmin_dmax, double linmin_dmin, double cg_glimit,
+                         double cg_zeps, int cg_fr, int cg_reset_int) {
+  orc_sys_t *s = &g->s;
+  s->linmin_maxsteps = linmin_maxsteps;
+  s->linmin_tol = linmin_tol;
+  s->linmin_dmax = linmin_dmax;
+  s->linmin_dmin = linmin_dmin;
+  s->cg_glimit = cg_glimit;
+  s->cg_zeps = cg_zeps;
+  s->cg_fr = cg_fr;
+  s->cg_reset_int = cg_reset_int;
+  return IMDGPU_OK;
+}
+
+int imdgpu_reset_cg(imdgpu_sys *g) {
+  return orc_reset_cg(&g->s) < 0 ? fail(IMDGPU_ERR_STATE, "oracle reset_cg") : IMDGPU_OK;
+}
+
+int imdgpu_cg_step(imdgpu_sys *g, int steps) {
+  return orc_cg_step(&g->s, steps) < 0 ? fail(IMDGPU_ERR_BRENT, "Too many iterations in brent")
+                                       : IMDGPU_OK;
+}
