@@ -53,6 +53,13 @@ DT_FS = 1.0
 SKIN = 0.4
 WORKLOAD = "sutton-chen Cu EAM2 NVE, fcc 40^3 = 256000 atoms, 300 K, dt 1 fs, skin 0.4 A"
 FORCE_BYTES_PER_ATOM = 56.0       # force kernel: read x (24) + 2F' (8), write F (24)
+# mixed force kernel, per full-list entry, loads through L1/TEX: the list
+# word (4), the partner's FP32 (hi, lo) position split (32), the pair table's
+# value and gradient rows (16 + 16), the density gradient row (16), the
+# partner's F' (4)
+MIXED_L1_BYTES_PER_ENTRY = 88.0
+NCU_L1TEX_MIXED_FORCE = 0.696     # l1tex throughput, % of peak (committed ncu profile)
+NCU_FP64_PIPE_FORCE = 0.857       # FP64 pipe busy of k_force_fast (committed ncu profile)
 STEP_BYTES_PER_ATOM = 232.0       # whole NVE EAM step, canonical count
 FLOPS_PER_PAIR = 66.0             # canonical FP64 flops per half-list pair within rc
 FORCE_FLOPS_PER_PAIR = 52.0       # of those in the force pass (all but rho's 14)
@@ -177,17 +184,23 @@ def run_reference(args, rank, world):
     tabs = workload_files(tmp)
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "liboracle.so"], check=True)
     cores = os.cpu_count() or 1
-    steps = max(1, min(args.steps, 4))
-    warm = max(1, min(args.warmup, 3))   # untimed steps in every process, bounded
+    # the same K timed and W untimed steps as the GPU arm, in every process
+    # (a full 256000-atom step takes about 0.6 s on one core)
+    steps = max(1, args.steps)
+    warm = max(1, args.warmup)
     rate, n = cpu_sample(tabs, steps, cores, warm)
+    how = ("%d independent single-core processes, each %d untimed then %d timed NVE steps of "
+           "the full 256000-atom system (oracle/imd_oracle.c, the reference's algorithm "
+           "restated in C); atom-steps/s summed over processes.  IMD's serial build is one "
+           "core; its OpenMP build runs slower on more threads, so independent replicas are "
+           "the host's throughput baseline" % (cores, warm, steps))
     line = {
         "impl": "reference", "metric": METRIC, "value": rate, "unit": "atom-steps/s",
         "n_gpus": world, "steps": steps, "warmup": warm, "ms_per_step": 1e3 * n / (rate / cores),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic", "config": {"workload": WORKLOAD, "sample": "%d NVE steps per core" % steps},
+        "data": "synthetic", "config": {"workload": WORKLOAD, "sample": how},
         "cpu_baseline": {"value": rate, "unit": "atom-steps/s", "cores": cores, "kind": "port",
-                         "sample": "%d independent processes x %d NVE steps of the 256000-atom "
-                                   "system (oracle/imd_oracle.c)" % (cores, steps)},
+                         "sample": how},
         "e2e": {"value": rate, "unit": "atom-steps/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -421,7 +434,17 @@ def run_ours(args, rank, world, local):
     force_ms = r["ms_force"] / args.steps
     pairs_rc = 67.0 * n  # half-list pairs within rc per atom for fcc Cu (6 shells, 134/2)
     force_flops = FORCE_FLOPS_PER_PAIR * pairs_rc
-    fp64_peak = api.probe_fp64_peak()
+    # the FP64 roofline denominator: imdgpu_probe_fp64_peak (kernel
+    # k_fp64_probe: 8 independent FMA chains per thread, 8 blocks of 256
+    # threads per SM, 4096 iterations, one warm-up launch), repeated, the
+    # best run kept, with the SM clock sampled during the repeats
+    with ClockSampler(local) as pclk:
+        probes = [api.probe_fp64_peak() for _ in range(7)]
+    fp64_peak = max(probes)
+    peak_how = {"kernel": "k_fp64_probe: 8 independent FP64 FMA chains per thread, "
+                          "8 x 256-thread blocks per SM, 4096 iterations, after a warm-up launch",
+                "repeats": len(probes), "tflops_each": probes,
+                "kept": "the best", "clocks": pclk.summary()}
     force_tflops = force_flops / (force_ms * 1e-3) / 1e12
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
     hbm_alg = FORCE_BYTES_PER_ATOM * n / (force_ms * 1e-3) / 1e9
@@ -450,9 +473,10 @@ def run_ours(args, rank, world, local):
                      "frac": force_tflops / fp64_peak, "traffic": traffic,
                      "peak_kind": "measured on this device: FP64 FMA chains "
                                   "(imdgpu_probe_fp64_peak); MEASURED_PEAKS.json has no FP64 rate",
+                     "peak_how": peak_how,
                      "flops_per_launch": force_flops,
                      "flops_per_pair": FORCE_FLOPS_PER_PAIR,
-                     "ncu_fp64_pipe_busy": 0.857,
+                     "ncu_fp64_pipe_busy": NCU_FP64_PIPE_FORCE,
                      "hbm": {"achieved": hbm_alg, "peak": hbm_peak, "unit": "GB/s",
                              "frac": hbm_alg / hbm_peak, "peak_kind": peak_kind,
                              "bytes_per_atom": FORCE_BYTES_PER_ATOM,
@@ -470,6 +494,35 @@ def run_ours(args, rank, world, local):
     if "mixed" in res:
         m = res["mixed"]
         mv = n * args.steps * world / (m["ms"] * 1e-3)
+        # roofline of the mixed force pass (k_force_mixed): ncu puts it on
+        # L1/TEX (the partner gathers), with the FP64 pipe idle and DRAM at a
+        # few per cent.  achieved = bytes loaded through L1/TEX per launch
+        # (MIXED_L1_BYTES_PER_ENTRY x full-list entries) / the launch's CUDA
+        # event time; peak = the nominal L1 load width, 128 B per SM per
+        # cycle at the sampled SM clock.  Random 32-byte gathers cost more L1
+        # wavefronts than bytes, so the byte fraction is lower than the
+        # throughput ncu reports (ncu_l1tex_throughput), which is the figure
+        # that binds.
+        mforce_ms = m["ms_force"] / args.steps
+        sm_mhz = (m["clocks"].get("sm_mhz") or 2070.0)
+        l1_peak = 152 * 128.0 * sm_mhz * 1e6 / 1e9
+        l1_bytes = MIXED_L1_BYTES_PER_ENTRY * m["nb"]
+        l1_ach = l1_bytes / (mforce_ms * 1e-3) / 1e9
+        mtraffic = committed_traffic("k_force_mixed")
+        mixed_roof = {"bound": "l1tex", "kernel": "k_force_mixed (EAM2 force pass, full list)",
+                      "achieved": l1_ach, "peak": l1_peak, "unit": "GB/s",
+                      "frac": l1_ach / l1_peak, "traffic": mtraffic,
+                      "peak_kind": "nominal: 128 B per SM per cycle x 152 SMs at the sampled "
+                                   "SM clock",
+                      "bytes_per_launch": l1_bytes, "bytes_per_entry": MIXED_L1_BYTES_PER_ENTRY,
+                      "list_entries": m["nb"],
+                      "ncu_l1tex_throughput": NCU_L1TEX_MIXED_FORCE,
+                      "hbm": {"achieved": FORCE_BYTES_PER_ATOM * n / (mforce_ms * 1e-3) / 1e9,
+                              "peak": hbm_peak, "unit": "GB/s", "peak_kind": peak_kind,
+                              "bytes_per_atom": FORCE_BYTES_PER_ATOM,
+                              "traffic_gbs": (mtraffic / (mforce_ms * 1e-3) / 1e9)
+                              if mtraffic else None}}
+        mixed_roof["hbm"]["frac"] = mixed_roof["hbm"]["achieved"] / hbm_peak
         line["mixed"] = {"value": mv, "unit": "atom-steps/s", "speedup_vs_fp64": mv / value,
                          "ms_per_step": m["ms"] / args.steps,
                          "kernels_ms_per_step": {"density": m["ms_density"] / args.steps,
@@ -480,7 +533,7 @@ def run_ours(args, rank, world, local):
                          "autotuned_blocks": {"density": m["blocks"][0], "force": m["blocks"][1]},
                          "graph_replay_wall": m["graph_rate"],
                          "energy_drift_per_atom": float((m["etot"][-1] - m["etot"][0]) / n),
-                         "vs_fp64": prec}
+                         "vs_fp64": prec, "roofline": mixed_roof, "clocks": m["clocks"]}
     if not args.no_batch:
         bc = run_batch(args, tabs, rank, world, dist)
         if rank == 0:

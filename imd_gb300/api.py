@@ -68,6 +68,23 @@ class NptState(C.Structure):
                 ("pressure_ext", C.c_double), ("volume", C.c_double), ("box", C.c_double * 9)]
 
 
+class NptAxialParams(C.Structure):
+    """imdgpu_npt_axial_params: IMD's npt_axial parameters."""
+    _d3 = C.c_double * 3
+    _fields_ = [("temperature", C.c_double), ("isq_tau_eta", C.c_double), ("eta", C.c_double),
+                ("isq_tau_xi", C.c_double), ("xi", _d3), ("pressure_ext", _d3),
+                ("pressure_end", _d3), ("relax_dirs", C.c_int * 3),
+                ("use_curr_pressure", C.c_int), ("steps_min", C.c_int), ("steps_max", C.c_int),
+                ("nactive", C.c_long), ("cell_size_tolerance", C.c_double)]
+
+
+class NptAxialState(C.Structure):
+    """imdgpu_npt_axial_state: IMD's globals of ensemble npt_axial."""
+    _d3 = C.c_double * 3
+    _fields_ = [("xi", _d3), ("eta", C.c_double), ("stress", _d3), ("pressure_ext", _d3),
+                ("vir_axial", _d3), ("volume", C.c_double), ("box", C.c_double * 9)]
+
+
 class Timing(C.Structure):
     _fields_ = [("ms_total", C.c_double), ("ms_density", C.c_double),
                 ("ms_force", C.c_double), ("ms_integrate", C.c_double),
@@ -151,6 +168,10 @@ def lib() -> C.CDLL:
         L.imdgpu_set_npt.argtypes = [vp, C.POINTER(NptParams)]
         L.imdgpu_move_atoms_npt_iso.argtypes = [vp, C.c_int, C.c_double]
         L.imdgpu_get_npt.argtypes = [vp, C.POINTER(NptState)]
+        L.imdgpu_npt_axial_defaults.argtypes = [C.POINTER(NptAxialParams)]
+        L.imdgpu_set_npt_axial.argtypes = [vp, C.POINTER(NptAxialParams)]
+        L.imdgpu_move_atoms_npt_axial.argtypes = [vp, C.c_int, C.c_double]
+        L.imdgpu_get_npt_axial.argtypes = [vp, C.POINTER(NptAxialState)]
         L.imdgpu_set_blocks.argtypes = [vp, C.c_int, C.c_int]
         L.imdgpu_batch_set_autotune.argtypes = [vp, C.c_int]
         L.imdgpu_batch_positions.argtypes = [vp, _dp]
@@ -382,6 +403,37 @@ class GpuSystem:
     def npt_state(self) -> NptState:
         st = NptState()
         _check(lib().imdgpu_get_npt(self.h, C.byref(st)), "get_npt")
+        return st
+
+    def set_npt_axial(self, **params) -> None:
+        """Start an npt_axial phase.  params: temperature, isq_tau_eta, eta,
+        isq_tau_xi, xi (3), pressure_ext (3, IMD's pressure_start),
+        pressure_end (3), relax_dirs (3), use_curr_pressure, steps_min,
+        steps_max, nactive, cell_size_tolerance; IMD's defaults for the
+        rest."""
+        prm = NptAxialParams()
+        _check(lib().imdgpu_npt_axial_defaults(C.byref(prm)), "npt_axial_defaults")
+        for k, v in params.items():
+            if not hasattr(prm, k):
+                raise TypeError("unknown npt_axial parameter %r" % k)
+            cur = getattr(prm, k)
+            if isinstance(cur, C.Array):
+                for a in range(3):
+                    cur[a] = v[a]
+            else:
+                setattr(prm, k, v)
+        _check(lib().imdgpu_set_npt_axial(self.h, C.byref(prm)), "set_npt_axial")
+
+    def move_atoms_npt_axial(self, steps: int, timestep: float) -> NptAxialState:
+        """move_atoms_npt_axial for main_loop step `steps`; returns the state
+        after it (xi, eta, stress, pressure_ext, vir_axial, volume, box)."""
+        _check(lib().imdgpu_move_atoms_npt_axial(self.h, steps, timestep),
+               "move_atoms_npt_axial")
+        return self.npt_axial_state()
+
+    def npt_axial_state(self) -> NptAxialState:
+        st = NptAxialState()
+        _check(lib().imdgpu_get_npt_axial(self.h, C.byref(st)), "get_npt_axial")
         return st
 
     def glok_state(self) -> GlokState:

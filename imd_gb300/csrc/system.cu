@@ -210,6 +210,18 @@ struct imdgpu_sys {
   double min_height[3] = {0.0, 0.0, 0.0}, max_height[3] = {0.0, 0.0, 0.0};
   double *d_npt = nullptr;    // 3: calc_dyn_pressure sums / twice the new E_kin
 
+  // npt_axial: parameters, IMD's globals of move_atoms_npt_axial (xi, eta,
+  // dyn_stress, stress, pressure_ext, d_pressure per axis) and the P_AXIAL
+  // virial components of the last calc_forces; the grid fields above serve
+  // both NPT ensembles
+  imdgpu_npt_axial_params npta_prm{};
+  bool npta_set = false;
+  double npta_xi[3] = {0.0, 0.0, 0.0}, npta_eta = 0.0, npta_ekin_old = 0.0;
+  double npta_dyn[3] = {0.0, 0.0, 0.0}, npta_stress[3] = {0.0, 0.0, 0.0};
+  double npta_pext[3] = {0.0, 0.0, 0.0}, npta_dp[3] = {0.0, 0.0, 0.0};
+  double vir_axial[3] = {0.0, 0.0, 0.0};
+  double *d_npta = nullptr;   // 7: totals of the last k_npt_axial
+
   // STRESS_TENS: per ext atom xx yy zz yz zx xy
   double *d_stress = nullptr;
   size_t stress_cap = 0;
@@ -968,6 +980,115 @@ __global__ void k_finalize_npt(const double *partial, int nb, DevScalars *sc, do
     sc->maxdisp2 = e;
     if (e > skin2) sc->rebuild = 1;
     *out = b;
+  }
+}
+
+// P_AXIAL (src/imd_forces_nbl.c:548-553, :1275-1278): vir_aa = -sum over
+// pairs of d_a f_a, the pair force and the EAM force alike.  Every pair puts
+// -d_a f_a / 2 on both of its atoms' PRESSTENS (:558-580, :1284-1318), so
+// vir_aa is the sum over the real atoms of the folded per-atom stress
+// diagonal: per block the three sums.
+__global__ void __launch_bounds__(BS_VEC) k_stress_diag(SysView v, const double *stress,
+                                                        double *partial) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double r[3] = {0.0, 0.0, 0.0};
+  if (i < v.n)
+#pragma unroll
+    for (int k = 0; k < 3; k++) r[k] = stress[6 * (size_t)i + k];
+  __shared__ double sh[3][BS_VEC / 32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < 3; k++) r[k] = warp_sum(r[k]);
+  if (lane == 0) {
+#pragma unroll
+    for (int k = 0; k < 3; k++) sh[k][w] = r[k];
+  }
+  __syncthreads();
+  if (threadIdx.x < 3) {
+    double a = 0.0;
+    for (int j = 0; j < BS_VEC / 32; j++) a += sh[threadIdx.x][j];
+    partial[3 * (size_t)blockIdx.x + threadIdx.x] = a;
+  }
+}
+
+// the factors of move_atoms_npt_axial per axis
+struct AxialFric {
+  double pf[3], pif[3], rf[3], rif[3];
+};
+
+// move_atoms_npt_axial (src/imd_integrate.c:1747-1960, no UNIAX): momenta
+// (pfric_a p_a + dt F_a) pifric_a, then masked by the restrictions;
+// positions (rfric_a x_a + p_a dt/m) rifric_a; in IMD's operation order,
+// unfused.  Per block: twice the new kinetic energy, |F|^2, the three
+// dyn_stress sums p_a p_a / m (sums), the largest force component and the
+// largest displacement since the list build (maxima).
+__global__ void __launch_bounds__(BS_VEC) k_npt_axial(SysView v, double dt, AxialFric fr,
+                                                      double *partial) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double r[7] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};  // e2 fn d0 d1 d2 | fm dm
+  if (i < v.n) {
+    double4 p = v.mom[i], x = v.pos[i];
+    const double4 f = v.frc[i];
+    const int t = (int)x.w;
+    double tmp = 1.0 / p.w;
+    r[1] = dadd(dadd(dmul(f.x, f.x), dmul(f.y, f.y)), dmul(f.z, f.z));
+    r[5] = fmax(fmax(f.x * f.x, f.y * f.y), f.z * f.z);
+    p.x = dmul(dadd(dmul(fr.pf[0], p.x), dmul(dt, f.x)), fr.pif[0]);
+    p.y = dmul(dadd(dmul(fr.pf[1], p.y), dmul(dt, f.y)), fr.pif[1]);
+    p.z = dmul(dadd(dmul(fr.pf[2], p.z), dmul(dt, f.z)), fr.pif[2]);
+    p.x = dmul(p.x, v.restr[3 * t]);
+    p.y = dmul(p.y, v.restr[3 * t + 1]);
+    p.z = dmul(p.z, v.restr[3 * t + 2]);
+    r[2] = dmul(dmul(p.x, p.x), tmp);
+    r[3] = dmul(dmul(p.y, p.y), tmp);
+    r[4] = dmul(dmul(p.z, p.z), tmp);
+    r[0] = dmul(dadd(dadd(dmul(p.x, p.x), dmul(p.y, p.y)), dmul(p.z, p.z)), tmp);
+    tmp = dmul(tmp, dt);
+    x.x = dmul(dadd(dmul(fr.rf[0], x.x), dmul(p.x, tmp)), fr.rif[0]);
+    x.y = dmul(dadd(dmul(fr.rf[1], x.y), dmul(p.y, tmp)), fr.rif[1]);
+    x.z = dmul(dadd(dmul(fr.rf[2], x.z), dmul(p.z, tmp)), fr.rif[2]);
+    v.mom[i] = p;
+    v.pos[i] = x;
+    const double4 rf = v.ref[i];
+    r[6] = r2_exact(dsub(x.x, rf.x), dsub(x.y, rf.y), dsub(x.z, rf.z));
+  }
+  __shared__ double sh[7][BS_VEC / 32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < 7; k++) r[k] = k < 5 ? warp_sum(r[k]) : warp_max(r[k]);
+  if (lane == 0) {
+#pragma unroll
+    for (int k = 0; k < 7; k++) sh[k][w] = r[k];
+  }
+  __syncthreads();
+  if (threadIdx.x < 7) {
+    const int k = threadIdx.x;
+    double a = 0.0;
+    for (int j = 0; j < BS_VEC / 32; j++) a = k < 5 ? a + sh[k][j] : fmax(a, sh[k][j]);
+    partial[7 * (size_t)blockIdx.x + k] = a;
+  }
+}
+
+// totals of the npt_axial partials into out (7 values, the layout above);
+// tot_kin_energy = (Ekin_old + Ekin_new) / 4
+__global__ void k_finalize_npta(const double *partial, int nb, DevScalars *sc, double skin2,
+                                double ekin_old, double *out) {
+  const int lane = threadIdx.x;
+  double r[7] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+  for (int b = lane; b < nb; b += 32)
+#pragma unroll
+    for (int k = 0; k < 7; k++)
+      r[k] = k < 5 ? r[k] + partial[7 * (size_t)b + k] : fmax(r[k], partial[7 * (size_t)b + k]);
+#pragma unroll
+  for (int k = 0; k < 7; k++) r[k] = k < 5 ? warp_sum(r[k]) : warp_max(r[k]);
+  if (lane == 0) {
+    sc->ekin = (ekin_old + r[0]) / 4.0;
+    sc->fnorm = r[1];
+    sc->fmax2 = r[5];
+    sc->maxdisp2 = r[6];
+    if (r[6] > skin2) sc->rebuild = 1;
+#pragma unroll
+    for (int k = 0; k < 7; k++) out[k] = r[k];
   }
 }
 
@@ -1939,6 +2060,7 @@ int imdgpu_destroy(imdgpu_sys *s) {
   dfree(s->d_e2);
   dfree(s->d_glok);
   dfree(s->d_npt);
+  dfree(s->d_npta);
   dfree(s->d_sys_short);
   dfree(s->d_atom_sys); dfree(s->d_aoff); dfree(s->d_sgdim); dfree(s->d_scdim); dfree(s->d_scoff);
   dfree(s->d_sys_done); dfree(s->d_ndone); dfree(s->d_sbox); dfree(s->d_stbox); dfree(s->d_cs);
@@ -2328,6 +2450,8 @@ int imdgpu_get_scalars(imdgpu_sys *s, imdgpu_scalars *o) {
   return IMDGPU_OK;
 }
 
+static int axial_virial(imdgpu_sys *s);
+
 int imdgpu_calc_forces(imdgpu_sys *s, int steps) {
   (void)steps;
   if (!s) return fail(IMDGPU_ERR_ARG, "null system");
@@ -2335,6 +2459,7 @@ int imdgpu_calc_forces(imdgpu_sys *s, int steps) {
   if (rc) return rc;
   rc = calc_forces_sync(s);
   if (rc) return rc;
+  if (s->npta_set && (rc = axial_virial(s))) return rc;  // P_AXIAL in the npt_axial build
   return (s->status_host & ST_SHORT) ? IMDGPU_WARN_SHORT : IMDGPU_OK;
 }
 
@@ -2611,6 +2736,7 @@ int imdgpu_set_npt(imdgpu_sys *s, const imdgpu_npt_params *prm) {
   s->volume_init = s->volume;
   s->cell_tol2 = (1.0 + prm->cell_size_tolerance) * (1.0 + prm->cell_size_tolerance);
   s->geom_ready = false;
+  s->npta_set = false;
   s->npt_set = true;
   return IMDGPU_OK;
 }
@@ -2694,6 +2820,172 @@ int imdgpu_move_atoms_npt_iso(imdgpu_sys *s, int steps, double timestep) {
     s->npt_dp = (P.pressure_end - s->npt_pext) / (P.steps_max - P.steps_min);
   }
   s->npt_pext += s->npt_dp;
+  return IMDGPU_OK;
+}
+
+int imdgpu_npt_axial_defaults(imdgpu_npt_axial_params *prm) {
+  if (!prm) return fail(IMDGPU_ERR_ARG, "null");
+  memset(prm, 0, sizeof *prm);
+  prm->cell_size_tolerance = 0.05;
+  for (int a = 0; a < 3; a++) prm->relax_dirs[a] = 1;
+  return IMDGPU_OK;
+}
+
+// A new npt_axial phase: IMD's globals xi, eta and pressure_ext per axis as
+// given; the grid is set up again with the NPT tolerance at the next
+// calc_forces, which from now on also sums the P_AXIAL virial.
+int imdgpu_set_npt_axial(imdgpu_sys *s, const imdgpu_npt_axial_params *prm) {
+  if (!s || !s->atoms_set) return fail(IMDGPU_ERR_STATE, "atoms not set");
+  if (!prm) return fail(IMDGPU_ERR_ARG, "null");
+  if (s->nsys > 0) return fail(IMDGPU_ERR_STATE, "npt_axial: one system, not a batch");
+  if (!s->have_box) return fail(IMDGPU_ERR_STATE, "box not set");
+  if (s->precision != IMDGPU_FP64) return fail(IMDGPU_ERR_STATE, "npt_axial: FP64 precision only");
+  if (!(prm->temperature > 0.0) || prm->isq_tau_eta < 0.0 || prm->isq_tau_xi < 0.0)
+    return fail(IMDGPU_ERR_ARG, "npt_axial: temperature > 0, isq_tau_eta and isq_tau_xi >= 0");
+  if (prm->steps_max <= prm->steps_min)
+    return fail(IMDGPU_ERR_ARG,
+                "npt_axial: steps_max > steps_min (the pressure ramp divides by it)");
+  if (!(prm->cell_size_tolerance >= 0.0))
+    return fail(IMDGPU_ERR_ARG, "npt_axial: cell_size_tolerance >= 0");
+  for (int a = 0; a < 3; a++)
+    if (prm->relax_dirs[a] != 0 && prm->relax_dirs[a] != 1)
+      return fail(IMDGPU_ERR_ARG, "npt_axial: relax_dirs are 0 or 1");
+  if (int rc = make_box(s)) return rc;
+  s->npta_prm = *prm;
+  for (int a = 0; a < 3; a++) {
+    s->npta_xi[a] = prm->xi[a];
+    s->npta_pext[a] = prm->pressure_ext[a];
+    s->npta_dyn[a] = s->npta_stress[a] = s->npta_dp[a] = s->vir_axial[a] = 0.0;
+  }
+  s->npta_eta = prm->eta;
+  s->npta_ekin_old = 0.0;
+  s->volume_init = s->volume;
+  s->cell_tol2 = (1.0 + prm->cell_size_tolerance) * (1.0 + prm->cell_size_tolerance);
+  s->geom_ready = false;
+  s->npt_set = false;
+  s->npta_set = true;
+  return IMDGPU_OK;
+}
+
+int imdgpu_get_npt_axial(imdgpu_sys *s, imdgpu_npt_axial_state *st) {
+  if (!s || !st) return fail(IMDGPU_ERR_ARG, "null");
+  for (int a = 0; a < 3; a++) {
+    st->xi[a] = s->npta_xi[a];
+    st->stress[a] = s->npta_stress[a];
+    st->pressure_ext[a] = s->npta_pext[a];
+    st->vir_axial[a] = s->vir_axial[a];
+  }
+  st->eta = s->npta_eta;
+  st->volume = s->volume;
+  for (int a = 0; a < 3; a++)
+    for (int c = 0; c < 3; c++) st->box[3 * a + c] = s->box[a][c];
+  return IMDGPU_OK;
+}
+
+// vir_xx, vir_yy, vir_zz of the forces just computed: the stress pass over
+// the current list and the sum of its per-atom diagonals (k_stress_diag)
+static int axial_virial(imdgpu_sys *s) {
+  const size_t ext = (size_t)s->ncap + s->gcap;
+  if (s->stress_cap < ext) {
+    dfree(s->d_stress);
+    CK(dalloc(&s->d_stress, 6 * ext));
+    s->stress_cap = ext;
+  }
+  if (!s->d_npt) CK(dalloc(&s->d_npt, 3));
+  const SysView v = view(s);
+  launch_stress(v, ftabs(s), s->d_stress, s->st);
+  const int nb = nblk(s->n, BS_VEC);
+  k_stress_diag<<<nb, BS_VEC, 0, s->st>>>(v, s->d_stress, s->partial);
+  k_finalize3<<<1, 32, 0, s->st>>>(s->partial, nb, s->d_npt);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(s->vir_axial, s->d_npt, 3 * sizeof(double), cudaMemcpyDeviceToHost, s->st));
+  CK(cudaStreamSynchronize(s->st));
+  return IMDGPU_OK;
+}
+
+// move_atoms_npt_axial (src/imd_integrate.c:1747-1960): the scalars on the
+// host in IMD's order, the atoms on the device, then every box row scaled
+// by its own factor and make_box, with a new grid when a height leaves its
+// bounds.
+int imdgpu_move_atoms_npt_axial(imdgpu_sys *s, int steps, double timestep) {
+  if (!s || !s->atoms_set) return fail(IMDGPU_ERR_STATE, "atoms not set");
+  if (!s->npta_set) return fail(IMDGPU_ERR_STATE, "imdgpu_set_npt_axial first");
+  if (!s->geom_ready || s->nbcap == 0)
+    return fail(IMDGPU_ERR_STATE, "move_atoms before the first calc_forces");
+  if (int rcf = batch_full(s)) return rcf;
+  imdgpu_npt_axial_params &P = s->npta_prm;
+  const double dt = timestep;
+  const double nact = P.nactive > 0 ? (double)P.nactive : 3.0 * s->n;
+  if (!s->d_npt) CK(dalloc(&s->d_npt, 3));
+  if (!s->d_npta) CK(dalloc(&s->d_npta, 7));
+  SysView v = view(s);
+  const int nb = nblk(s->n, BS_VEC);
+  double *xi = s->npta_xi;
+  if (steps == P.steps_min) {
+    // calc_dyn_pressure (src/imd_integrate.c:1403-1447)
+    k_dyn_press<<<nb, BS_VEC, 0, s->st>>>(v, s->partial);
+    k_finalize3<<<1, 32, 0, s->st>>>(s->partial, nb, s->d_npt);
+    CK(cudaGetLastError());
+    double d3[3];
+    CK(cudaMemcpyAsync(d3, s->d_npt, sizeof d3, cudaMemcpyDeviceToHost, s->st));
+    CK(cudaStreamSynchronize(s->st));
+    for (int a = 0; a < 3; a++) s->npta_dyn[a] = d3[a];
+    s->npta_ekin_old = d3[0] + d3[1];
+    s->npta_ekin_old += d3[2];
+    if (P.isq_tau_xi == 0.0) xi[0] = xi[1] = xi[2] = 0.0;
+    for (int a = 0; a < 3; a++) xi[a] *= P.relax_dirs[a];
+  }
+  for (int a = 0; a < 3; a++) {
+    s->npta_stress[a] = (s->npta_dyn[a] + s->vir_axial[a]) / s->volume;
+    s->npta_dyn[a] = 0.0;
+  }
+  const double ttt = dt * s->volume * P.isq_tau_xi / nact;
+  double xi_old[3];
+  for (int a = 0; a < 3; a++) {
+    xi_old[a] = xi[a];
+    xi[a] += ttt * (s->npta_stress[a] - s->npta_pext[a]) * P.relax_dirs[a];
+  }
+  AxialFric fr;
+  for (int a = 0; a < 3; a++) {
+    fr.pf[a] = 1.0 - (xi_old[a] + s->npta_eta) * dt / 2.0;
+    fr.pif[a] = 1.0 / (1.0 + (xi[a] + s->npta_eta) * dt / 2.0);
+    fr.rf[a] = 1.0 + (xi[a]) * dt / 2.0;
+    fr.rif[a] = 1.0 / (1.0 - (xi[a]) * dt / 2.0);
+  }
+  k_npt_axial<<<nb, BS_VEC, 0, s->st>>>(v, dt, fr, s->partial);
+  k_finalize_npta<<<1, 32, 0, s->st>>>(s->partial, nb, s->dsc, v.skin2, s->npta_ekin_old,
+                                       s->d_npta);
+  CK(cudaGetLastError());
+  double tot[7];
+  CK(cudaMemcpyAsync(tot, s->d_npta, sizeof tot, cudaMemcpyDeviceToHost, s->st));
+  if (int rc = read_back(s)) return rc;
+  for (int a = 0; a < 3; a++) s->npta_dyn[a] = tot[2 + a];
+  const double ekin_new = tot[0];
+  const double ttt_eta = nact * P.temperature;
+  s->npta_eta += dt * (ekin_new / ttt_eta - 1.0) * P.isq_tau_eta;
+  s->npta_ekin_old = ekin_new;
+  // the box, row a scaled by its own factor; ghosts take it from the next
+  // launch on
+  double tvec[3];
+  for (int a = 0; a < 3; a++) tvec[a] = (1.0 + xi[a] * dt / 2.0) / (1.0 - xi[a] * dt / 2.0);
+  if (tvec[0] < 0 || tvec[1] < 0 || tvec[2] < 0)
+    return fail(IMDGPU_ERR_GEOM, "box size has become negative!");
+  for (int a = 0; a < 3; a++)
+    for (int c = 0; c < 3; c++) s->box[a][c] *= tvec[a];
+  if (int rc = make_box(s)) return rc;
+  if (s->volume > 8 * s->volume_init) return fail(IMDGPU_ERR_GEOM, "system seems to explode!");
+  drop_nve_graph(s);
+  for (int a = 0; a < 3; a++)
+    if (s->height[a] < s->min_height[a] || s->height[a] > s->max_height[a]) s->geom_ready = false;
+  if (steps == P.steps_min) {
+    if (P.use_curr_pressure == 1) {
+      for (int a = 0; a < 3; a++) s->npta_pext[a] = s->npta_stress[a];
+      P.use_curr_pressure = 0;
+    }
+    for (int a = 0; a < 3; a++)
+      s->npta_dp[a] = (P.pressure_end[a] - s->npta_pext[a]) / (P.steps_max - P.steps_min);
+  }
+  for (int a = 0; a < 3; a++) s->npta_pext[a] += s->npta_dp[a];
   return IMDGPU_OK;
 }
 
@@ -3422,7 +3714,7 @@ int imdgpu_batch_set_cells(imdgpu_sys *s, int ncells, const int *natoms, const d
   // the arguments are accepted: from here on the handle holds the batch, and
   // the ensembles of one system end
   s->ml_wt_host.clear();
-  s->glok_set = s->npt_set = false;
+  s->glok_set = s->npt_set = s->npta_set = false;
   s->b0_ncells = ncells;
   s->b0_aoff = aoff;
   s->b0_boxes.assign(boxes, boxes + 9 * (size_t)ncells);

@@ -220,6 +220,40 @@ int imdgpu_set_npt(imdgpu_sys *sys, const imdgpu_npt_params *prm);
 /* move_atoms_npt_iso for main_loop step `steps` */
 int imdgpu_move_atoms_npt_iso(imdgpu_sys *sys, int steps, double timestep);
 int imdgpu_get_npt(imdgpu_sys *sys, imdgpu_npt_state *st);
+/* NPT with a barostat per axis, move_atoms_npt_axial
+ * (src/imd_integrate.c:1747-1960, build option npt_axial, which adds
+ * P_AXIAL): each axis a has its own xi[a], driven by its axial stress
+ * (dyn_stress_a + vir_aa) / volume against pressure_ext[a]; relax_dirs[a] = 0
+ * holds an axis; the momenta are masked by the restrictions after the
+ * update; box row a is scaled by its own factor, with make_box and a new
+ * cell grid as in npt_iso.  While a phase is set, calc_forces also sums
+ * IMD's P_AXIAL virial components vir_xx, vir_yy, vir_zz
+ * (src/imd_forces_nbl.c:548-553, :1275-1278).  Parameters as IMD parses
+ * them (src/imd_param.c:2562-2640).  FP64, one system. */
+typedef struct {
+  double temperature, isq_tau_eta, eta;  /* as for imdgpu_set_nvt */
+  double isq_tau_xi;
+  double xi[3];
+  double pressure_ext[3], pressure_end[3];  /* pressure_start, pressure_end per axis */
+  int relax_dirs[3];                        /* 1: the axis is coupled, 0: held */
+  int use_curr_pressure;
+  int steps_min, steps_max;
+  long nactive;                             /* <= 0: 3 per atom */
+  double cell_size_tolerance;
+} imdgpu_npt_axial_params;
+typedef struct {
+  double xi[3], eta;
+  double stress[3];                      /* IMD's stress_x, stress_y, stress_z */
+  double pressure_ext[3];
+  double vir_axial[3];                   /* vir_xx, vir_yy, vir_zz of the last calc_forces */
+  double volume;
+  double box[9];
+} imdgpu_npt_axial_state;
+int imdgpu_npt_axial_defaults(imdgpu_npt_axial_params *prm);
+int imdgpu_set_npt_axial(imdgpu_sys *sys, const imdgpu_npt_axial_params *prm);
+/* move_atoms_npt_axial for main_loop step `steps` */
+int imdgpu_move_atoms_npt_axial(imdgpu_sys *sys, int steps, double timestep);
+int imdgpu_get_npt_axial(imdgpu_sys *sys, imdgpu_npt_axial_state *st);
 /* nsteps of main_loop (src/imd_main_3d.c:155-870) for ensemble nve:
  * calc_forces, move_atoms_nve, check_nblist, fully on the device.
  * epot/ekin (may be NULL) receive tot_pot_energy and tot_kin_energy of every

@@ -49,7 +49,9 @@ def test_api_structs_match_header(tmp_path):
     from imd_gb300 import api
     structs = [("imdgpu_scalars", api.Scalars), ("imdgpu_timing", api.Timing),
                ("imdgpu_glok_params", api.GlokParams), ("imdgpu_glok_state", api.GlokState),
-               ("imdgpu_npt_params", api.NptParams), ("imdgpu_npt_state", api.NptState)]
+               ("imdgpu_npt_params", api.NptParams), ("imdgpu_npt_state", api.NptState),
+               ("imdgpu_npt_axial_params", api.NptAxialParams),
+               ("imdgpu_npt_axial_state", api.NptAxialState)]
     got = _c_layout(tmp_path, os.path.join(ROOT, "include"), "imdgpu.h", structs)
     _check(got, structs)
 

@@ -419,10 +419,11 @@ def test_mik_matches_reference():
     assert np.abs(d).max() < 1e-8
 
 
-@pytest.mark.parametrize("name", ["cu_fire", "cu_glok"])
+@pytest.mark.parametrize("name", ["cu_fire", "cu_glok", "cu_mixglok"])
 def test_glok_matches_reference(name):
     """The glok ensemble (IMD's FIRE) on the device against the reference's
-    `fire` (adaptive step, mixing) and `glok` builds, main_loop step by step:
+    `fire` (adaptive step, mixing), `glok` and `mix glok` (mixing, fixed
+    step, 28 restarts on glok_ekin_threshold) builds, main_loop step by step:
     every decision identical (time step, mixing factor, restarts, nPxF),
     energies to 1e-9, P.F to 1e-6 relative, final positions to 1e-8 A."""
     g = golden(name)
@@ -517,6 +518,66 @@ def test_npt_iso_matches_reference():
     d = x - g["x_final"]
     d -= np.round(d @ np.linalg.inv(box)) @ box
     assert np.abs(d).max() < 1e-8
+
+
+def test_npt_axial_matches_reference():
+    """ensemble npt_axial on the device (P_AXIAL virial, a barostat per
+    axis, z held by relax_dirs), 200 main_loop steps against the reference's
+    `npt_axial` build: energies to 1e-9, xi, eta and the axial stresses to
+    1e-8 relative, the box diagonal every step and the final box to 1e-10,
+    positions to 1e-8 A."""
+    g = golden("cu_npt_axial")
+    gg = dict(g)
+    gg["x"] = g["x0"]
+    s = gpu_system(gg, "cu", 1, 1, float(g["skin"]), p=g["p0"])
+    s.set_npt_axial(temperature=float(g["temperature"]), isq_tau_eta=float(g["isq_tau_eta"]),
+                    isq_tau_xi=float(g["isq_tau_xi"]), pressure_ext=list(g["pressure_start"]),
+                    pressure_end=list(g["pressure_end"]),
+                    relax_dirs=[int(v) for v in g["relax_dirs"]], steps_min=0,
+                    steps_max=int(g["steps_max"]))
+    dt = float(g["dt"])
+    rows = []
+    for st in range(len(g["epot"])):
+        s.calc_forces(st)
+        ep = s.scalars().tot_pot_energy
+        ns = s.move_atoms_npt_axial(st, dt)
+        rows.append([ep, s.scalars().tot_kin_energy] + list(ns.xi) + [ns.eta]
+                    + list(ns.stress) + [ns.box[0], ns.box[4], ns.box[8]])
+        s.check_nblist()
+    r = np.array(rows)
+    np.testing.assert_allclose(r[:, 0], g["epot"], rtol=1e-9, atol=0)
+    np.testing.assert_allclose(r[:, 1], g["ekin"], rtol=1e-8, atol=0)
+    np.testing.assert_allclose(r[:, 2:5], g["xi"], rtol=1e-8, atol=1e-12)
+    np.testing.assert_allclose(r[:, 5], g["eta"], rtol=1e-8, atol=1e-12)
+    np.testing.assert_allclose(r[:, 6:9], g["stress"], rtol=1e-8, atol=1e-12)
+    np.testing.assert_allclose(r[:, 9:12], g["box_diag"], rtol=1e-10, atol=0)
+    assert np.all(r[:, 4] == 0.0)   # the held axis never moves
+    box = np.array(s.npt_axial_state().box).reshape(3, 3)
+    np.testing.assert_allclose(box, g["box_final"], rtol=1e-10, atol=1e-12)
+    x = s.get_atoms()["x"]
+    d = x - g["x_final"]
+    d -= np.round(d @ np.linalg.inv(box)) @ box
+    assert np.abs(d).max() < 1e-8
+
+
+def test_npt_axial_virial_is_the_oracle_p_axial():
+    """The P_AXIAL components of one calc_forces on the perturbed Cu and
+    Cu/Ni cases: the device's vir_xx, vir_yy, vir_zz against the oracle's
+    running sums (IMD's order) to 1e-11 relative."""
+    from oracle import OracleSystem
+    for name in ("cu_pert", "alloy_pert"):
+        g = golden(name)
+        tab, eam, nt, skin = CASES[name]
+        s = gpu_system(g, tab, eam, nt, skin)
+        s.set_npt_axial(temperature=0.0258520, steps_min=0, steps_max=10)
+        s.calc_forces(0)
+        va = np.array(s.npt_axial_state().vir_axial)
+        o = OracleSystem(g["box"], g["x"], g["type"], g["mass"], g["number"], nt, tables(tab),
+                         bool(eam), skin)
+        o.calc_forces()
+        ref = np.array(o.s.vir_axial[:])
+        np.testing.assert_allclose(va, ref, rtol=1e-11, atol=0, err_msg=name)
+        assert abs(va.sum() - o.virial) <= 1e-11 * abs(o.virial)
 
 
 def test_npt_iso_new_cell_grid_matches_oracle():

@@ -296,6 +296,20 @@ def test_npt_axial_matches_reference():
     assert abs(g["box_diag"][-1, 1] / g["box_diag"][0, 1] - 1.0) > 5e-3
 
 
+@pytest.mark.parametrize("name", ["cu_pert", "alloy_pert", "lj_pert"])
+def test_p_axial_virial_is_the_stress_diagonal(name):
+    """IMD's P_AXIAL sums (vir_xx -= d_x f_x over pairs) equal the diagonal
+    of calc_tot_presstens (every pair puts -d_a f_b / 2 on both atoms'
+    PRESSTENS): the identity the device uses for npt_axial.  Their sum is
+    the virial."""
+    g, s = make(name)
+    s.set_stress(True)
+    s.calc_forces()
+    va = np.array(s.s.vir_axial[:])
+    np.testing.assert_allclose(va, s.tot_stress[:3], rtol=1e-12, atol=0)
+    assert abs(va.sum() - s.virial) <= 1e-12 * abs(s.virial)
+
+
 def test_npt_iso_new_cell_grid():
     """A box that shrinks out of its height bounds gets a new cell grid
     (make_box calling init_cells, src/imd_geom_3d.c:82-86) and a new list;
