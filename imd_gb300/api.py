@@ -114,6 +114,7 @@ def lib() -> C.CDLL:
         L.imdgpu_destroy.argtypes = [vp]
         L.imdgpu_set_precision.argtypes = [vp, C.c_int]
         L.imdgpu_set_exact.argtypes = [vp, C.c_int]
+        L.imdgpu_set_deterministic.argtypes = [vp, C.c_int]
         L.imdgpu_set_graphs.argtypes = [vp, C.c_int]
         L.imdgpu_set_interpolation.argtypes = [vp, C.c_int]
         L.imdgpu_set_table2.argtypes = [vp, C.c_int, C.c_int, C.c_int, _dp]
@@ -284,6 +285,10 @@ class GpuSystem:
     def set_exact(self, on: bool) -> None:
         """IMD's unfused table arithmetic (bitwise table values) on/off."""
         _check(lib().imdgpu_set_exact(self.h, int(on)), "set_exact")
+
+    def set_deterministic(self, on: bool) -> None:
+        """FP64 passes on the full list without atomics: bitwise repeatable."""
+        _check(lib().imdgpu_set_deterministic(self.h, int(on)), "set_deterministic")
 
     def set_precision(self, precision: int) -> None:
         _check(lib().imdgpu_set_precision(self.h, precision), "imdgpu_set_precision")

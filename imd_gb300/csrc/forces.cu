@@ -335,6 +335,139 @@ __global__ void __launch_bounds__(BS_FORCE_MAX) k_force_fast(SysView v, DevTable
   block_sum_store_dyn<2, BS_FORCE_MAX>(acc, partial);
 }
 
+// ---------------------------------------------------------------------------
+// Deterministic FP64 passes (imdgpu_set_deterministic).  The half-list
+// kernels above add the reaction on the second atom of a pair with FP64
+// atomics, so the order of the per-atom sums, and their last bits, change
+// from run to run.  These kernels use the full list instead (every pair in
+// both directions, as the mixed path does): each atom owns its sums.  A quad
+// of four consecutive lanes serves one atom: lane q takes the entries
+// q, q + 4, q + 8, ... of the atom's list in order, and the four partial
+// sums of rho, of the force, the energy and the virial are combined by a
+// fixed shuffle tree, (l0 + l1) + (l2 + l3).  Same pairs, tables and
+// formulas as k_density_fast / k_force_fast; twice the pair arithmetic.
+// ---------------------------------------------------------------------------
+constexpr int DET_Q = 4;  // lanes per atom
+
+__device__ __forceinline__ double quad_sum(double x) {
+  x += __shfl_xor_sync(0xffffffffu, x, 1);
+  return x + __shfl_xor_sync(0xffffffffu, x, 2);
+}
+
+// rho_i = sum_j rho_{it,jt}(r_ij) over the full list (loop 1's eam_r,
+// src/imd_forces_nbl.c:586-611, for the atom that receives)
+template <bool NT1, bool CUB>
+__global__ void __launch_bounds__(BS_FORCE_MAX) k_density_det(SysView v, DevTable rho) {
+  const int gid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = gid / DET_Q, q = gid % DET_Q;
+  const bool live = i < v.n && !atom_idle(v, i);
+  double r = 0.0;
+  bool shortf = false;
+  if (live) {
+    const double4 pi = v.pos[i];
+    const int it = NT1 ? 0 : (int)pi.w, nt = v.ntypes;
+    const int nn = v.nnb[i];
+    const uint32_t *__restrict__ nb = v.nbr + i;
+    for (int k = q; k < nn; k += DET_Q) {
+      const int j = (int)(__ldg(nb + (size_t)k * v.ncap) & NB_MASK);
+      const double4 pj = ldg4(&v.pos[j]);
+      const double dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
+      const double r2 = fma(dx, dx, fma(dy, dy, dz * dz));
+      const int col = NT1 ? 0 : it * nt + (int)pj.w;
+      if (lt_pos(r2, rho.end[col])) {
+        double chi;
+        const int kk = tab_index_fast(rho, col, r2, chi);
+        r += poly_v<CUB>(cv_load(rho, col, kk), chi);
+        shortf |= lt_pos(r2, rho.begin[col]);
+      }
+    }
+  }
+  r = quad_sum(r);
+  if (live && q == 0) v.rho[i] = r;
+  if (live && shortf) flag_short(v, i);
+}
+
+template <bool NT1, bool EAM, bool SAMEGRID, bool CUB>
+__global__ void __launch_bounds__(BS_FORCE_MAX) k_force_det(SysView v, DevTable pair, DevTable rho,
+                                                        double *partial) {
+  const int gid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = gid / DET_Q, q = gid % DET_Q;
+  const bool live = i < v.n && !atom_idle(v, i);
+  // f* = sum of d * (minus the gradient); the atom's force is -f
+  double fx = 0.0, fy = 0.0, fz = 0.0, ee = 0.0, vir = 0.0;
+  bool shortf = false;
+  if (live) {
+    const double4 pi = v.pos[i];
+    const int it = NT1 ? 0 : (int)pi.w, nt = v.ntypes;
+    const int nn = v.nnb[i];
+    const double dfi = EAM ? v.df[i] : 0.0;
+    const uint32_t *__restrict__ nb = v.nbr + i;
+    for (int k = q; k < nn; k += DET_Q) {
+      const int j = (int)(__ldg(nb + (size_t)k * v.ncap) & NB_MASK);
+      const double4 pj = ldg4(&v.pos[j]);
+      const double dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
+      const double r2 = fma(dx, dx, fma(dy, dy, dz * dz));
+      const int jt = NT1 ? 0 : (int)pj.w;
+      const int col = NT1 ? 0 : it * nt + jt;
+      double ngrad = 0.0;
+      bool have = false;
+      int kk = 0;
+      double chi = 0.0;
+      if (le_pos(r2, pair.end[col])) {
+        kk = tab_index_fast(pair, col, r2, chi);
+        ee = fma(0.5, poly_v<CUB>(cv_load(pair, col, kk), chi), ee);
+        ngrad = poly_g<CUB>(cgn_load(pair, col, kk), chi);
+        shortf |= lt_pos(r2, pair.begin[col]);
+        have = true;
+      }
+      if (EAM) {
+        const int col1 = NT1 ? 0 : jt * nt + it, col2 = col;
+        if (lt_pos(r2, rho.end[col1]) || lt_pos(r2, rho.end[col2])) {
+          double chi1 = chi;
+          int k1 = kk;
+          if (!(SAMEGRID && have)) k1 = tab_index_fast(rho, col1, r2, chi1);
+          const double nris = poly_g<CUB>(cgn_load(rho, col1, k1), chi1);
+          const double dfj = __ldg(&v.df[j]);
+          if (NT1 || col1 == col2) {
+            ngrad = fma(nris, dfi + dfj, ngrad);
+          } else {
+            double chi2 = chi;
+            int k2 = kk;
+            if (!(SAMEGRID && have)) k2 = tab_index_fast(rho, col2, r2, chi2);
+            const double nrjs = poly_g<CUB>(cgn_load(rho, col2, k2), chi2);
+            ngrad = fma(dfi, nrjs, fma(dfj, nris, ngrad));
+          }
+          have = true;
+        }
+      }
+      if (have) {
+        fx = fma(dx, ngrad, fx);
+        fy = fma(dy, ngrad, fy);
+        fz = fma(dz, ngrad, fz);
+        vir = fma(r2, ngrad, vir);
+      }
+    }
+  }
+  fx = quad_sum(fx);
+  fy = quad_sum(fy);
+  fz = quad_sum(fz);
+  ee = quad_sum(ee);
+  vir = quad_sum(vir);
+  double acc[2] = {0.0, 0.0};  // energy, virial (each pair counted from both atoms)
+  if (live && q == 0) {
+    double4 f = v.frc[i];  // .w holds the embedding energy
+    f.x = -fx;
+    f.y = -fy;
+    f.z = -fz;
+    f.w += ee;
+    v.frc[i] = f;
+    acc[0] = ee;
+    acc[1] = 0.5 * vir;
+  }
+  if (live && shortf) flag_short(v, i);
+  block_sum_store_dyn<2, BS_FORCE_MAX>(acc, partial);
+}
+
 // embedding with the coefficient-form table
 __global__ void __launch_bounds__(BS_VEC) k_embed_fast(SysView v, DevTable emb, double *partial) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -508,9 +641,63 @@ void k_ghost_pos_launch(const SysView &v, int blocks, cudaStream_t st) {
   k_ghost_pos<<<blocks, BS_VEC, 0, st>>>(v);
 }
 
+template <bool NT1, bool EAM>
+static void launch_force_det(const ForceTabs &t, int nq, cudaStream_t st, const SysView &v,
+                             double *pf) {
+  const bool cub = (t.pair.mode != TAB_QUADRATIC);
+  if (t.samegrid) {
+    if (cub) k_force_det<NT1, EAM, true, true><<<nq, t.bs, 0, st>>>(v, t.pair, t.rho, pf);
+    else k_force_det<NT1, EAM, true, false><<<nq, t.bs, 0, st>>>(v, t.pair, t.rho, pf);
+  } else {
+    if (cub) k_force_det<NT1, EAM, false, true><<<nq, t.bs, 0, st>>>(v, t.pair, t.rho, pf);
+    else k_force_det<NT1, EAM, false, false><<<nq, t.bs, 0, st>>>(v, t.pair, t.rho, pf);
+  }
+}
+
+// the deterministic FP64 sequence: ghosts, density (quads, full list),
+// embedding, 2F' to the ghosts, force (quads, full list), totals; no
+// atomics on per-atom sums and no ghost folds
+static int launch_forces_det(const SysView &v, const ForceTabs &t, DevScalars *sc,
+                             cudaStream_t st, cudaEvent_t *ev) {
+  const int gblocks = nblk(v.gcap, BS_VEC) > 0 ? nblk(v.gcap, BS_VEC) : 1;
+  const size_t ext = (size_t)v.ncap + v.gcap;
+  cudaMemsetAsync(v.frc, 0, ext * sizeof(double4), st);
+  k_ghost_pos<<<gblocks, BS_VEC, 0, st>>>(v);
+  const long lanes = (long)v.n * DET_Q;
+  const int nq = nblk(lanes, t.bs), nqr = nblk(lanes, t.bs_rho), nbe = nblk(v.n, BS_VEC);
+  double *pe = v.partial, *pf = v.partial + nbe;
+  if (t.eam) {
+    if (ev) cudaEventRecord(ev[0], st);
+    const bool cubr = (t.rho.mode != TAB_QUADRATIC);
+    if (t.nt1 && !cubr) k_density_det<true, false><<<nqr, t.bs_rho, 0, st>>>(v, t.rho);
+    else if (t.nt1) k_density_det<true, true><<<nqr, t.bs_rho, 0, st>>>(v, t.rho);
+    else if (!cubr) k_density_det<false, false><<<nqr, t.bs_rho, 0, st>>>(v, t.rho);
+    else k_density_det<false, true><<<nqr, t.bs_rho, 0, st>>>(v, t.rho);
+    if (ev) cudaEventRecord(ev[1], st);
+    k_embed_fast<<<nbe, BS_VEC, 0, st>>>(v, t.embed, pe);
+    k_ghost_df<<<gblocks, BS_VEC, 0, st>>>(v);
+    if (ev) cudaEventRecord(ev[2], st);
+    if (t.nt1) launch_force_det<true, true>(t, nq, st, v, pf);
+    else launch_force_det<false, true>(t, nq, st, v, pf);
+    if (ev) cudaEventRecord(ev[3], st);
+  } else {
+    if (ev) {
+      cudaEventRecord(ev[0], st);
+      cudaEventRecord(ev[1], st);
+      cudaEventRecord(ev[2], st);
+    }
+    if (t.nt1) launch_force_det<true, false>(t, nq, st, v, pf);
+    else launch_force_det<false, false>(t, nq, st, v, pf);
+    if (ev) cudaEventRecord(ev[3], st);
+  }
+  k_finalize_forces<<<1, 32, 0, st>>>(pe, t.eam ? nbe : 0, pf, nq, sc);
+  return t.eam ? 7 : 4;
+}
+
 int launch_forces(const SysView &v, const ForceTabs &t, DevScalars *sc, int mixed,
                   cudaStream_t st, cudaEvent_t *ev) {
   if (mixed) return launch_forces_mixed(v, t, sc, v.dff, st, ev);
+  if (t.det) return launch_forces_det(v, t, sc, st, ev);
   int launches = 0;
   const int gblocks = nblk(v.gcap, BS_VEC) > 0 ? nblk(v.gcap, BS_VEC) : 1;
   const size_t ext = (size_t)v.ncap + v.gcap;

@@ -16,6 +16,7 @@ struct ForceTabs {
   int epot;      // scatter per-atom energies (POTENG) in the force pass
   int bs;        // threads per block of the force pass (autotuned, multiple of 32)
   int bs_rho;    // threads per block of the density pass (autotuned)
+  int det;       // FP64 passes on the full list without atomics (deterministic)
 };
 
 // Device-side scalars of one system (results + control).

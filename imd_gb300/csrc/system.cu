@@ -100,7 +100,8 @@ struct imdgpu_sys {
   int gdim[3] = {0, 0, 0}, cdim[3] = {0, 0, 0};
   int nreal_cells = 0, nall_cells = 0, nbuf = 0;
   bool geom_ready = false;
-  bool geom_full = false;     // full list (mixed precision) instead of IMD's half list
+  bool geom_full = false;     // full list (mixed precision, deterministic FP64) instead of IMD's half list
+  bool deterministic = false; // FP64 passes without atomics (imdgpu_set_deterministic)
   float *dff = nullptr;
   int *d_cell_rank = nullptr, *d_rank_lin = nullptr, *d_hshell = nullptr;
   int *d_bsrc = nullptr, *d_blin = nullptr, *d_bcode = nullptr;
@@ -1423,6 +1424,7 @@ static ForceTabs ftabs(imdgpu_sys *s) {
   t.epot = 1;
   t.bs = s->bs_force;
   t.bs_rho = s->bs_rho;
+  t.det = s->deterministic && s->precision == IMDGPU_FP64;
   int same = s->have_tab[0] && s->have_tab[1];
   if (same) {
     const HostTable &a = s->htab[0], &b = s->htab[1];
@@ -1506,7 +1508,7 @@ static int setup_geometry(imdgpu_sys *s) {
   }
   // half shell (AR order, src/imd_geom_3d.c:895-899) with pbc exclusion, or
   // for the full list all 27 neighbour cells (own cell first)
-  s->geom_full = (s->precision == IMDGPU_MIXED);
+  s->geom_full = (s->precision == IMDGPU_MIXED || s->deterministic);
   const int ns = s->geom_full ? 27 : 14;
   std::vector<int> hshell((size_t)ns * s->nreal_cells, -1);
   std::vector<char> used(s->nall_cells, 0);
@@ -1607,7 +1609,7 @@ static int setup_geometry_batch(imdgpu_sys *s) {
     const double r = std::sqrt((double)s->tab_cellsz) + s->nbl_margin;
     s->cellsz = r * r;
   }
-  s->geom_full = (s->precision == IMDGPU_MIXED);
+  s->geom_full = (s->precision == IMDGPU_MIXED || s->deterministic);
   const int nsh = s->geom_full ? 27 : 14;
   std::vector<double> tb(9 * (size_t)ns);
   std::vector<int> gdim(3 * (size_t)ns), cdim(3 * (size_t)ns), coff(ns + 1, 0), roff(ns + 1, 0);
@@ -2102,6 +2104,28 @@ int imdgpu_set_precision(imdgpu_sys *s, int precision) {
   return IMDGPU_OK;
 }
 
+// Deterministic FP64 force passes: the full list, each atom's sums owned by
+// one quad of lanes, no atomics (forces.cu, k_density_det / k_force_det).
+// Switching rebuilds the list in the other layout at the next use.
+int imdgpu_set_deterministic(imdgpu_sys *s, int on) {
+  if (!s) return fail(IMDGPU_ERR_ARG, "null system");
+  if (s->nsys > 0) return fail(IMDGPU_ERR_STATE, "deterministic mode: one system, not a batch");
+  if (on && s->npta_set)
+    return fail(IMDGPU_ERR_STATE, "deterministic mode: not with npt_axial (its stress pass "
+                                  "uses the half list)");
+  const bool want = on != 0;
+  if (want != s->deterministic) {
+    s->deterministic = want;
+    if (s->geom_ready && s->precision == IMDGPU_FP64) {
+      s->geom_ready = false;
+      int one = 1;
+      CK(cudaMemcpy(&s->dsc->rebuild, &one, sizeof(int), cudaMemcpyHostToDevice));
+      s->hsc_valid = false;
+    }
+  }
+  return IMDGPU_OK;
+}
+
 static int upload_table(imdgpu_sys *s, int which, HostTable &t) {
   const int want = (which == IMDGPU_TAB_EMBED) ? s->ntypes : s->ntypes * s->ntypes;
   if (t.ncols != want)
@@ -2326,7 +2350,9 @@ int imdgpu_set_atoms(imdgpu_sys *s, int n, const int *number, const int *type,
     CK(dalloc(&s->perm, n));
     CK(dalloc(&s->slot_rank, n));
     CK(dalloc(&s->nnb, n));
-    CK(dalloc(&s->partial, 8 * (size_t)nblk(n, 64) + 64));
+    // block partials: the largest user is the deterministic force pass, two
+    // per block of four lanes per atom at 32 lanes per block
+    CK(dalloc(&s->partial, 8 * (size_t)nblk(n, 64) + 2 * (size_t)nblk(4L * n, 32) + 64));
     dfree(s->slot_of);
     dfree(s->d_in);
     dfree(s->d_out);
@@ -2469,6 +2495,8 @@ int imdgpu_calc_forces(imdgpu_sys *s, int steps) {
 int imdgpu_calc_stress(imdgpu_sys *s, double *presstens, double *tot) {
   if (!s) return fail(IMDGPU_ERR_ARG, "null system");
   if (s->precision != IMDGPU_FP64) return fail(IMDGPU_ERR_STATE, "stress: FP64 precision only");
+  if (s->deterministic)
+    return fail(IMDGPU_ERR_STATE, "stress: not in deterministic mode (the pass uses the half list)");
   int rc = batch_full(s);
   if (rc) return rc;
   if ((rc = calc_forces_sync(s))) return rc;
@@ -2840,6 +2868,9 @@ int imdgpu_set_npt_axial(imdgpu_sys *s, const imdgpu_npt_axial_params *prm) {
   if (s->nsys > 0) return fail(IMDGPU_ERR_STATE, "npt_axial: one system, not a batch");
   if (!s->have_box) return fail(IMDGPU_ERR_STATE, "box not set");
   if (s->precision != IMDGPU_FP64) return fail(IMDGPU_ERR_STATE, "npt_axial: FP64 precision only");
+  if (s->deterministic)
+    return fail(IMDGPU_ERR_STATE, "npt_axial: not in deterministic mode (the P_AXIAL stress "
+                                  "pass uses the half list)");
   if (!(prm->temperature > 0.0) || prm->isq_tau_eta < 0.0 || prm->isq_tau_xi < 0.0)
     return fail(IMDGPU_ERR_ARG, "npt_axial: temperature > 0, isq_tau_eta and isq_tau_xi >= 0");
   if (prm->steps_max <= prm->steps_min)
@@ -3715,6 +3746,7 @@ int imdgpu_batch_set_cells(imdgpu_sys *s, int ncells, const int *natoms, const d
   // the ensembles of one system end
   s->ml_wt_host.clear();
   s->glok_set = s->npt_set = s->npta_set = false;
+  s->deterministic = false;
   s->b0_ncells = ncells;
   s->b0_aoff = aoff;
   s->b0_boxes.assign(boxes, boxes + 9 * (size_t)ncells);
@@ -4394,6 +4426,9 @@ extern "C" int imdgpu_get_pairs(imdgpu_sys *s, long cap, int *ni, int *nj, int *
                      long *count) {
   if (!s || !count) return fail(IMDGPU_ERR_ARG, "null");
   if (!s->geom_ready || s->nbcap == 0) return fail(IMDGPU_ERR_STATE, "no list");
+  if (s->geom_full && s->precision == IMDGPU_FP64)
+    return fail(IMDGPU_ERR_STATE, "get_pairs: the deterministic mode holds the full list, not "
+                                  "IMD's half list");
   std::vector<int> nn(s->n);
   CK(cudaMemcpy(nn.data(), s->nnb, sizeof(int) * s->n, cudaMemcpyDeviceToHost));
   std::vector<long> rs(s->n + 1, 0);

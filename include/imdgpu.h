@@ -79,6 +79,15 @@ int imdgpu_destroy(imdgpu_sys *sys);
 int imdgpu_set_exact(imdgpu_sys *sys, int on);
 /* precision may be switched between calls (the list is kept) */
 int imdgpu_set_precision(imdgpu_sys *sys, int precision);
+/* Deterministic reduction mode for parity runs (no counterpart in IMD,
+ * whose serial loops sum in a fixed order, src/imd_forces_nbl.c:907-918).
+ * 1: the FP64 density and force passes run on the full neighbour list, each
+ * atom's sums formed by one quad of lanes in list order and a fixed shuffle
+ * tree, with no atomics, so repeated runs are bitwise equal; about twice the
+ * pair arithmetic of the default half-list passes, whose FP64 atomics make
+ * the last bits vary from run to run.  One system, FP64; imdgpu_calc_stress,
+ * npt_axial and imdgpu_get_pairs need the half list and refuse this mode. */
+int imdgpu_set_deterministic(imdgpu_sys *sys, int on);
 
 /* Upload one pot_table_t (src/types.h:416-428) exactly as IMD holds it
  * after read_pot_table + init_threepoint (src/imd_potential.c:161-282,
