@@ -263,7 +263,7 @@ def run_batch(args, tabs, rank=0, world=1, dist=None):
     for name, weights in (("plain", None), ("learned", w)):
         if dist:
             dist.barrier()
-        r = learned.relax(tabs, [cells[i] for i in mine], weights=weights)
+        r = learned.relax(tabs, [cells[i] for i in mine], weights=weights, trace=True)
         sec = shard.max_over_ranks(r.seconds, dist)
         g = shard.gather_cell_results({"epot": r.epot, "status": r.status, "nfc": r.nfc},
                                       mine, len(cells), dist)
@@ -277,7 +277,8 @@ def run_batch(args, tabs, rank=0, world=1, dist=None):
                      "converged_per_s": float((g["status"] == 0).sum() / sec),
                      "force_calls_per_relaxation": float(g["nfc"].mean()),
                      "rounds_rank0": r.rounds,
-                     "status_counts": np.bincount(g["status"], minlength=5).tolist()}
+                     "status_counts": np.bincount(g["status"], minlength=5).tolist(),
+                     "tail_rank0": r.tail_histogram(len(mine))}
         if name == "learned":
             out[name]["start_used_rank0"] = int(r.used.sum())
     gp, gl = res["plain"][1], res["learned"][1]

@@ -100,7 +100,8 @@ struct SysView {
   const int *cell_rank;     // buffered lin -> Morton rank of real cell (-1 for buffer)
   const int *rank_lin;      // rank -> buffered lin
   const int *hshell;        // nshell buffered lin per real rank (-1 none): half or full shell
-  int nshell;               // 14 (half list, IMD's AR order) or 27 (full list)
+  int nshell;               // 14 (half list, IMD's AR order) or 27 (full or balanced list)
+  int balanced;             // balanced half list: 27 cells, IMD's 14 first (see k_rb_build_half)
   const int *bsrc;          // per buffer cell (enumerated): source real lin
   const int *blin;          // per buffer cell: its lin
   const int *bcode;         // per buffer cell: packed image shift

@@ -101,6 +101,7 @@ struct imdgpu_sys {
   int nreal_cells = 0, nall_cells = 0, nbuf = 0;
   bool geom_ready = false;
   bool geom_full = false;     // full list (mixed precision, deterministic FP64) instead of IMD's half list
+  bool geom_balanced = false; // FP64 half list with balanced orientation (single system)
   bool deterministic = false; // FP64 passes without atomics (imdgpu_set_deterministic)
   float *dff = nullptr;
   int *d_cell_rank = nullptr, *d_rank_lin = nullptr, *d_hshell = nullptr;
@@ -498,6 +499,24 @@ __global__ void k_rb_split(SysView v, DevScalars *sc) {
 // make_nblist (src/imd_forces_nbl.c:136-273): half shell of 14 cells,
 // in-cell partners after i, r^2 < cellsz.  With nshell == 27 the full list
 // (every partner from both sides) for the mixed path.  Stores NBL_POS.
+//
+// Balanced half list (v.balanced, the FP64 default of one system): the same
+// pair set as IMD's, every pair once, with the orientation chosen so that
+// each atom owns about half of its partners.  IMD's half shell hands the
+// first atom of a cell all its in-cell partners and the last none (entries
+// per atom from ~20 to ~130 at 256,000 Cu atoms), and a warp of the pass
+// kernels runs as long as its longest lane.  Here the 27 cells are scanned
+// (IMD's 14 first, then the 13 mirror cells, real cells only); a pair of two
+// real atoms is kept by the atom that the parity rule on their numbers
+// picks (odd sum: the lower number, even sum: the higher), decided alike
+// from both sides; a pair with a ghost is kept as IMD keeps it, from the
+// half-shell side, so the image and the r^2 bits are IMD's.  For two real
+// atoms r^2 is bitwise the same from either side (the difference is negated
+// exactly).
+__device__ __forceinline__ bool owns_pair(int num_i, int num_j) {
+  return ((num_i ^ num_j) & 1) ? (num_i < num_j) : (num_i > num_j);
+}
+
 __global__ void __launch_bounds__(128) k_rb_build_half(SysView v, DevScalars *sc,
                                                         const int *slot_rank) {
   if (!sc->rebuild) return;
@@ -507,7 +526,9 @@ __global__ void __launch_bounds__(128) k_rb_build_half(SysView v, DevScalars *sc
   v.ref[i] = pi;
   const int r = slot_rank[i];
   const int *hs = v.hshell + (size_t)v.nshell * r;
-  const bool full = (v.nshell == 27);
+  const bool bal = v.balanced != 0;
+  const bool full = (v.nshell == 27) && !bal;
+  const int numi = bal ? v.number[i] : 0;
   const SplitPos *sp = reinterpret_cast<const SplitPos *>(v.xl);
   const SplitPos a = sp[i];
   // FP32 distance decides all pairs outside a +-1e-5 band around the list
@@ -519,9 +540,10 @@ __global__ void __launch_bounds__(128) k_rb_build_half(SysView v, DevScalars *sc
     if (c2 < 0) continue;
     const int s = v.cstart[c2];
     const int e = min(s + v.ccount[c2], v.n + v.gcap);  // ghost overflow: stay in bounds
-    const int j0 = (m == 0 && !full) ? i + 1 : s;
+    const int j0 = (m == 0 && !full && !bal) ? i + 1 : s;
     for (int j = j0; j < e; j++) {
-      if (full && j == i) continue;
+      if ((full || bal) && j == i) continue;
+      if (bal && j < v.n && !owns_pair(numi, v.number[j])) continue;
       const SplitPos b = ldsp(&sp[j]);
       const float dx = (b.hi.x - a.hi.x) + (b.lo.x - a.lo.x);
       const float dy = (b.hi.y - a.hi.y) + (b.lo.y - a.lo.y);
@@ -1388,7 +1410,8 @@ static SysView view(imdgpu_sys *s) {
   v.cell_rank = s->d_cell_rank;
   v.rank_lin = s->d_rank_lin;
   v.hshell = s->d_hshell;
-  v.nshell = s->geom_full ? 27 : 14;
+  v.nshell = (s->geom_full || s->geom_balanced) ? 27 : 14;
+  v.balanced = s->geom_balanced ? 1 : 0;
   v.dff = s->dff;
   v.bsrc = s->d_bsrc;
   v.blin = s->d_blin;
@@ -1509,7 +1532,8 @@ static int setup_geometry(imdgpu_sys *s) {
   // half shell (AR order, src/imd_geom_3d.c:895-899) with pbc exclusion, or
   // for the full list all 27 neighbour cells (own cell first)
   s->geom_full = (s->precision == IMDGPU_MIXED || s->deterministic);
-  const int ns = s->geom_full ? 27 : 14;
+  s->geom_balanced = !s->geom_full;
+  const int ns = (s->geom_full || s->geom_balanced) ? 27 : 14;
   std::vector<int> hshell((size_t)ns * s->nreal_cells, -1);
   std::vector<char> used(s->nall_cells, 0);
   for (int r = 0; r < s->nreal_cells; r++) {
@@ -1540,6 +1564,17 @@ static int setup_geometry(imdgpu_sys *s) {
       for (int a = 0; a <= 1; a++)
         for (int b = -a; b <= 1; b++)
           for (int c = (a == 0 ? -b : -a); c <= 1; c++) add(a, b, c);
+    }
+    if (s->geom_balanced) {
+      // the 13 mirror cells, real ones only: their ghosts are never kept
+      for (int a = 0; a <= 1; a++)
+        for (int b = -a; b <= 1; b++)
+          for (int c = (a == 0 ? -b : -a); c <= 1; c++) {
+            if (a == 0 && b == 0 && c == 0) continue;
+            const int qq = ((i - a) * cy + (j - b)) * cz + (k - c);
+            if (cell_rank[qq] >= 0) nq[nn] = qq;
+            nn++;
+          }
     }
   }
   // buffer cells referenced by some half shell
@@ -1610,7 +1645,8 @@ static int setup_geometry_batch(imdgpu_sys *s) {
     s->cellsz = r * r;
   }
   s->geom_full = (s->precision == IMDGPU_MIXED || s->deterministic);
-  const int nsh = s->geom_full ? 27 : 14;
+  s->geom_balanced = !s->geom_full;
+  const int nsh = (s->geom_full || s->geom_balanced) ? 27 : 14;
   std::vector<double> tb(9 * (size_t)ns);
   std::vector<int> gdim(3 * (size_t)ns), cdim(3 * (size_t)ns), coff(ns + 1, 0), roff(ns + 1, 0);
   for (int q = 0; q < ns; q++) {
@@ -1672,6 +1708,18 @@ static int setup_geometry_batch(imdgpu_sys *s) {
         for (int a = 0; a <= 1; a++)
           for (int b = -a; b <= 1; b++)
             for (int c = (a == 0 ? -b : -a); c <= 1; c++) add(a, b, c);
+      }
+      if (s->geom_balanced) {
+        // the 13 mirror cells of the balanced half list, real ones only
+        for (int a = 0; a <= 1; a++)
+          for (int b = -a; b <= 1; b++)
+            for (int c = (a == 0 ? -b : -a); c <= 1; c++) {
+              if (a == 0 && b == 0 && c == 0) continue;
+              const int ri = i - a, rj = j - b, rk = k - c;
+              if (ri >= 1 && ri <= gx && rj >= 1 && rj <= gy && rk >= 1 && rk <= gz)
+                nq[nn] = coff[q] + (ri * cy + rj) * cz + rk;
+              nn++;
+            }
       }
     }
     for (int lin = 0; lin < cx * cy * cz; lin++) {

@@ -88,19 +88,43 @@ class RelaxResult:
     e_start: np.ndarray | None = None
     e_pred: np.ndarray | None = None
     positions: list = field(default_factory=list)
+    # (seconds since the start, rounds so far, cells finished) after every
+    # advance call, when relax() was asked to trace
+    trace: list = field(default_factory=list)
 
     @property
     def relaxations_per_s(self) -> float:
         return len(self.epot) / self.seconds
 
+    def tail_histogram(self, ncells: int, bounds=(8, 32)) -> dict:
+        """Wall time and rounds spent while at most 8, 9-32 and more than 32
+        cells were unfinished (each traced interval counted at the number
+        unfinished when it began)."""
+        edges = sorted(bounds)
+        names = ["unfinished<=%d" % edges[0]] + \
+                ["%d<unfinished<=%d" % (a, b) for a, b in zip(edges, edges[1:])] + \
+                ["unfinished>%d" % edges[-1]]
+        out = {k: {"seconds": 0.0, "rounds": 0} for k in names}
+        t0, r0, left = 0.0, 0, ncells
+        for t, r, done in self.trace:
+            k = sum(left > e for e in edges)
+            out[names[k]]["seconds"] += t - t0
+            out[names[k]]["rounds"] += r - r0
+            t0, r0, left = t, r, ncells - done
+        return out
+
 
 def relax(tables, cells, fmax: float = 1e-4, weights=None, precision=api.FP64,
           keep_positions: bool = False, chunk_rounds: int = 4096,
-          interpolation: int = BATCH_INTERPOLATION, nbl_margin: float = 0.4) -> RelaxResult:
+          interpolation: int = BATCH_INTERPOLATION, nbl_margin: float = 0.4,
+          trace: bool = False) -> RelaxResult:
     """Relax every cell with the batched CG, from the learned start when
     `weights` are given.  The wall time covers the learned start (its two
     force calls and the prediction) and the CG, not the upload of the cells.
-    Force calls per cell include the learned start's two."""
+    Force calls per cell include the learned start's two.  trace: advance
+    64 rounds per call and record the progress after each (RelaxResult.trace)."""
+    if trace:
+        chunk_rounds = 64
     b = make_batch(tables, cells, precision, interpolation, nbl_margin)
     used = e0 = e1 = None
     api.lib()
@@ -111,8 +135,11 @@ def relax(tables, cells, fmax: float = 1e-4, weights=None, precision=api.FP64,
         used, e0, e1 = b.ml_start()
     b.begin(fmax)
     rounds = 0
+    tr = []
     while True:
         nd, rounds = b.advance(chunk_rounds)
+        if trace:
+            tr.append((time.perf_counter() - t0, rounds, nd))
         if nd >= len(cells):
             break
         if rounds > 10_000_000:
@@ -123,7 +150,7 @@ def relax(tables, cells, fmax: float = 1e-4, weights=None, precision=api.FP64,
     pos = b.positions() if keep_positions else []
     b.close()
     return RelaxResult(sec, r["epot"], r["fmax"], nfc, r["steps"], r["status"], rounds,
-                       used, e0, e1, pos)
+                       used, e0, e1, pos, tr)
 
 
 def targets(cells, relaxed_positions) -> list:
