@@ -90,7 +90,10 @@ FMT_HD int fmt_fixed(double v, int prec, int width, char *out) {
       u128 q = p >> sh;
       const u128 rem = p - (q << sh);
       const u128 half = (u128)1 << (sh - 1);
-      if (rem > half || (rem == half && (q & 1u))) q += 1;
+      // half to even on the last printed digit: the fraction's, or with no
+      // decimals the integer part's
+      const bool odd = prec ? (q & 1u) != 0 : (ip & 1u) != 0;
+      if (rem > half || (rem == half && odd)) q += 1;
       fs = (uint64_t)q;
     } else {
       fs = 0;                             // below 2^-75: far under half a unit

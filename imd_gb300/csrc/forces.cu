@@ -640,6 +640,12 @@ static inline int nblk(long n, int bs) { return (int)((n + bs - 1) / bs); }
 void k_ghost_pos_launch(const SysView &v, int blocks, cudaStream_t st) {
   k_ghost_pos<<<blocks, BS_VEC, 0, st>>>(v);
 }
+void fold_rho_launch(const SysView &v, int blocks, cudaStream_t st) {
+  k_fold_rho<<<blocks, BS_VEC, 0, st>>>(v);
+}
+void fold_force_launch(const SysView &v, int blocks, cudaStream_t st) {
+  k_fold_force<<<blocks, BS_VEC, 0, st>>>(v);
+}
 
 template <bool NT1, bool EAM>
 static void launch_force_det(const ForceTabs &t, int nq, cudaStream_t st, const SysView &v,

@@ -72,6 +72,9 @@ int launch_stress(const SysView &v, const ForceTabs &t, double *stress, cudaStre
 
 // forces.cu: refresh ghost positions (send_cells(copy_cell))
 void k_ghost_pos_launch(const SysView &v, int blocks, cudaStream_t st);
+// send_forces(add_rho) and send_forces(add_forces): ghost sums into owners
+void fold_rho_launch(const SysView &v, int blocks, cudaStream_t st);
+void fold_force_launch(const SysView &v, int blocks, cudaStream_t st);
 // mixed.cu: the FP32-force path over the full list
 int launch_forces_mixed(const SysView &v, const ForceTabs &t, DevScalars *sc, float *dff,
                         cudaStream_t st, cudaEvent_t *ev);

@@ -7,11 +7,14 @@
 //     d = (hi_j - hi_i) + (lo_j - lo_i) is accurate to the last FP32 bit of d
 //     itself: the coordinates an FP32 pair sees are relative to the atom,
 //     never absolute box coordinates;
-//   * the list is the FULL list (every pair from both sides), so each thread
-//     owns its atom's sums: no atomics, no ghost fold;
-//   * per-atom sums of rho, force, energy and virial are kept as error-free
-//     (TwoSum) pairs of FP32 values and converted to FP64 once per atom; the
-//     block and device reductions are FP64;
+//   * the list is the balanced half list of the FP64 path (every pair once,
+//     IMD's pair set, k_rb_build_half), so each pair's FP32 arithmetic and
+//     each partner gather happen once;
+//   * the owner's sums of rho, force, energy and virial are kept as
+//     error-free (TwoSum) pairs of FP32 values, converted to FP64 once per
+//     atom; the partner's share of every pair goes in with an FP64 atomic;
+//     ghost sums fold into their owners as in the FP64 path; the block and
+//     device reductions are FP64;
 //   * the embedding function and the integrator stay FP64.
 #include <algorithm>
 
@@ -55,7 +58,8 @@ __device__ __forceinline__ float polyf_g(const DevTable &t, int col, int k, floa
   return fmaf(chi, fmaf(chi, g.z, g.y), g.x);
 }
 
-// rho_i = sum_j rho_{it,jt}(r_ij) over the full list (loop 1's eam_r)
+// loop 1's EAM branch over the half list (src/imd_forces_nbl.c:586-611):
+// rho_{it,jt}(r) to atom i, rho_{jt,it}(r) to atom j
 template <bool NT1>
 __global__ void __launch_bounds__(BS_FORCE_MAX) k_density_mixed(SysView v, DevTable rho,
                                                             const SplitPos *sp) {
@@ -75,15 +79,29 @@ __global__ void __launch_bounds__(BS_FORCE_MAX) k_density_mixed(SysView v, DevTa
     const float dy = (b.hi.y - a.hi.y) + (b.lo.y - a.lo.y);
     const float dz = (b.hi.z - a.hi.z) + (b.lo.z - a.lo.z);
     const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-    const int col = NT1 ? 0 : it * nt + __float_as_int(b.hi.w);
+    const int jt = NT1 ? 0 : __float_as_int(b.hi.w);
+    const int col = NT1 ? 0 : it * nt + jt;
+    float rho_h = 0.f;
     if (r2 < rho.fend[col]) {
       float chi;
       const int kk = tab_index_f(rho, col, r2, chi);
-      r.add(polyf_v(rho, col, kk, chi));
+      rho_h = polyf_v(rho, col, kk, chi);
+      r.add(rho_h);
       shortf |= r2 < rho.fbegin[col];
     }
+    if (NT1 || it == jt) {
+      if (r2 < rho.fend[col]) atomicAdd(&v.rho[j], (double)rho_h);
+    } else {
+      const int col2 = jt * nt + it;
+      if (r2 < rho.fend[col2]) {
+        float chi;
+        const int kk = tab_index_f(rho, col2, r2, chi);
+        atomicAdd(&v.rho[j], (double)polyf_v(rho, col2, kk, chi));
+        shortf |= r2 < rho.fbegin[col2];
+      }
+    }
   }
-  v.rho[i] = r.value();
+  atomicAdd(&v.rho[i], r.value());
   if (shortf) flag_short(v, i);
 }
 
@@ -112,13 +130,15 @@ __global__ void k_ghost_dff(SysView v, float *dff) {
     dff[v.n + g] = dff[v.gowner[g]];
 }
 
-// forces over the full list: each directed pair adds d*grad to atom i and
-// half of the pair energy and virial
-template <bool NT1, bool EAM>
+// forces over the half list: every pair's force d*grad goes to atom i (in
+// its TwoSum sums) and -d*grad to atom j (FP64 atomics); the pair energy
+// and -r^2 grad once per pair.  EPOT: half the pair energy to each atom's
+// POTENG; otherwise, with v.eshare, the whole pair energy to its owner
+// (per-system sums of a batch).
+template <bool NT1, bool EAM, bool EPOT>
 __global__ void __launch_bounds__(BS_FORCE_MAX) k_force_mixed(SysView v, DevTable pair,
                                                           DevTable rho, const SplitPos *sp,
-                                                          const float *dff, int pair_only_epot,
-                                                          double *partial) {
+                                                          const float *dff, double *partial) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   double acc[2] = {0.0, 0.0};
   if (i < v.n && !atom_idle(v, i)) {
@@ -129,7 +149,7 @@ __global__ void __launch_bounds__(BS_FORCE_MAX) k_force_mixed(SysView v, DevTabl
     Acc fx, fy, fz, ee, vir;
     bool shortf = false;
     const uint32_t *__restrict__ nb = v.nbr + i;
-#pragma unroll 4
+#pragma unroll 2
     for (int k = 0; k < nn; k++) {
       const int j = (int)(__ldg(nb + (size_t)k * v.ncap) & NB_MASK);
       const SplitPos b = ldsp(&sp[j]);
@@ -139,12 +159,13 @@ __global__ void __launch_bounds__(BS_FORCE_MAX) k_force_mixed(SysView v, DevTabl
       const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
       const int jt = NT1 ? 0 : __float_as_int(b.hi.w);
       const int col = NT1 ? 0 : it * nt + jt;
-      float grad = 0.f;
+      float grad = 0.f, pot = 0.f;
       bool have = false;
       if (r2 <= pair.fend[col]) {
         float chi;
         const int kk = tab_index_f(pair, col, r2, chi);
-        ee.add(0.5f * polyf_v(pair, col, kk, chi));
+        pot = polyf_v(pair, col, kk, chi);
+        ee.add(pot);
         grad = polyf_g(pair, col, kk, chi);
         shortf |= r2 < pair.fbegin[col];
         have = true;
@@ -166,24 +187,29 @@ __global__ void __launch_bounds__(BS_FORCE_MAX) k_force_mixed(SysView v, DevTabl
         }
       }
       if (have) {
-        fx.add(dx * grad);
-        fy.add(dy * grad);
-        fz.add(dz * grad);
-        vir.add(-0.5f * r2 * grad);
+        const float px = dx * grad, py = dy * grad, pz = dz * grad;
+        fx.add(px);
+        fy.add(py);
+        fz.add(pz);
+        vir.add(-r2 * grad);
+        double *fj = &v.frc[j].x;
+        atomicAdd(fj + 0, -(double)px);
+        atomicAdd(fj + 1, -(double)py);
+        atomicAdd(fj + 2, -(double)pz);
+        if (EPOT) atomicAdd(fj + 3, 0.5 * (double)pot);
       }
     }
     const double e = ee.value();
-    double4 f = v.frc[i];  // .w holds the embedding energy
-    f.x = fx.value();
-    f.y = fy.value();
-    f.z = fz.value();
-    f.w += e;
-    v.frc[i] = f;
+    double *fi = &v.frc[i].x;
+    atomicAdd(fi + 0, fx.value());
+    atomicAdd(fi + 1, fy.value());
+    atomicAdd(fi + 2, fz.value());
+    if (EPOT) atomicAdd(fi + 3, 0.5 * e);
+    else if (v.eshare) atomicAdd(fi + 3, e);
     acc[0] = e;
     acc[1] = vir.value();
     if (shortf) flag_short(v, i);
   }
-  (void)pair_only_epot;
   block_sum_store_dyn<2, BS_FORCE_MAX>(acc, partial);
 }
 
@@ -206,42 +232,52 @@ __global__ void k_finalize_mixed(const double *pe, int ne, const double *pf, int
 
 static inline int nblk(long n, int bs) { return (int)((n + bs - 1) / bs); }
 
+template <bool NT1, bool EAM>
+static void launch_force_mixed2(const ForceTabs &t, int nbf, cudaStream_t st, const SysView &v,
+                                const SplitPos *sp, const float *dff, double *pf) {
+  if (t.epot) k_force_mixed<NT1, EAM, true><<<nbf, t.bs, 0, st>>>(v, t.pair, t.rho, sp, dff, pf);
+  else k_force_mixed<NT1, EAM, false><<<nbf, t.bs, 0, st>>>(v, t.pair, t.rho, sp, dff, pf);
+}
+
 int launch_forces_mixed(const SysView &v, const ForceTabs &t, DevScalars *sc, float *dff,
                         cudaStream_t st, cudaEvent_t *ev) {
   const int gblocks = std::max(1, nblk(v.gcap, BS_VEC));
   const size_t ext = (size_t)v.ncap + v.gcap;
   SplitPos *sp = reinterpret_cast<SplitPos *>(v.xl);
-  cudaMemsetAsync(v.frc, 0, (size_t)v.ncap * sizeof(double4), st);
+  cudaMemsetAsync(v.frc, 0, ext * sizeof(double4), st);
   k_ghost_pos_launch(v, gblocks, st);
   k_split<<<nblk(ext, BS_VEC), BS_VEC, 0, st>>>(v, sp);
   const int nbf = nblk(v.n, t.bs), nbe = nblk(v.n, BS_VEC), nbr = nblk(v.n, t.bs_rho);
   double *pe = v.partial, *pf = v.partial + nbe;
   int launches = 4;
   if (t.eam) {
+    cudaMemsetAsync(v.rho, 0, ext * sizeof(double), st);
     if (ev) cudaEventRecord(ev[0], st);
     if (t.nt1) k_density_mixed<true><<<nbr, t.bs_rho, 0, st>>>(v, t.rho, sp);
     else k_density_mixed<false><<<nbr, t.bs_rho, 0, st>>>(v, t.rho, sp);
     if (ev) cudaEventRecord(ev[1], st);
+    fold_rho_launch(v, gblocks, st);
     k_embed_mixed<<<nbe, BS_VEC, 0, st>>>(v, t.embed, dff, pe);
     k_ghost_dff<<<gblocks, BS_VEC, 0, st>>>(v, dff);
     if (ev) cudaEventRecord(ev[2], st);
-    if (t.nt1) k_force_mixed<true, true><<<nbf, t.bs, 0, st>>>(v, t.pair, t.rho, sp, dff, 0, pf);
-    else k_force_mixed<false, true><<<nbf, t.bs, 0, st>>>(v, t.pair, t.rho, sp, dff, 0, pf);
+    if (t.nt1) launch_force_mixed2<true, true>(t, nbf, st, v, sp, dff, pf);
+    else launch_force_mixed2<false, true>(t, nbf, st, v, sp, dff, pf);
     if (ev) cudaEventRecord(ev[3], st);
-    launches += 4;
+    launches += 5;
   } else {
     if (ev) {
       cudaEventRecord(ev[0], st);
       cudaEventRecord(ev[1], st);
       cudaEventRecord(ev[2], st);
     }
-    if (t.nt1) k_force_mixed<true, false><<<nbf, t.bs, 0, st>>>(v, t.pair, t.rho, sp, dff, 0, pf);
-    else k_force_mixed<false, false><<<nbf, t.bs, 0, st>>>(v, t.pair, t.rho, sp, dff, 0, pf);
+    if (t.nt1) launch_force_mixed2<true, false>(t, nbf, st, v, sp, dff, pf);
+    else launch_force_mixed2<false, false>(t, nbf, st, v, sp, dff, pf);
     if (ev) cudaEventRecord(ev[3], st);
     launches += 1;
   }
+  fold_force_launch(v, gblocks, st);
   k_finalize_mixed<<<1, 32, 0, st>>>(pe, t.eam ? nbe : 0, pf, nbf, sc);
-  return launches + 1;
+  return launches + 2;
 }
 
 }  // namespace imdgpu

@@ -1531,7 +1531,7 @@ static int setup_geometry(imdgpu_sys *s) {
   }
   // half shell (AR order, src/imd_geom_3d.c:895-899) with pbc exclusion, or
   // for the full list all 27 neighbour cells (own cell first)
-  s->geom_full = (s->precision == IMDGPU_MIXED || s->deterministic);
+  s->geom_full = s->deterministic && s->precision == IMDGPU_FP64;
   s->geom_balanced = !s->geom_full;
   const int ns = (s->geom_full || s->geom_balanced) ? 27 : 14;
   std::vector<int> hshell((size_t)ns * s->nreal_cells, -1);
@@ -1644,7 +1644,7 @@ static int setup_geometry_batch(imdgpu_sys *s) {
     const double r = std::sqrt((double)s->tab_cellsz) + s->nbl_margin;
     s->cellsz = r * r;
   }
-  s->geom_full = (s->precision == IMDGPU_MIXED || s->deterministic);
+  s->geom_full = s->deterministic && s->precision == IMDGPU_FP64;
   s->geom_balanced = !s->geom_full;
   const int nsh = (s->geom_full || s->geom_balanced) ? 27 : 14;
   std::vector<double> tb(9 * (size_t)ns);
