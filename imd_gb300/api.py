@@ -115,6 +115,10 @@ def lib() -> C.CDLL:
         L.imdgpu_set_precision.argtypes = [vp, C.c_int]
         L.imdgpu_set_exact.argtypes = [vp, C.c_int]
         L.imdgpu_set_deterministic.argtypes = [vp, C.c_int]
+        L.imdgpu_format_atoms.argtypes = [vp, C.c_int, _ip, C.c_int, C.c_char_p, C.c_long,
+                                          C.POINTER(C.c_long)]
+        L.imdgpu_format_fixed.argtypes = [_dp, C.c_int, C.c_int, C.c_int, C.c_char_p, C.c_long,
+                                          C.POINTER(C.c_long)]
         L.imdgpu_set_graphs.argtypes = [vp, C.c_int]
         L.imdgpu_set_interpolation.argtypes = [vp, C.c_int]
         L.imdgpu_set_table2.argtypes = [vp, C.c_int, C.c_int, C.c_int, _dp]
@@ -285,6 +289,23 @@ class GpuSystem:
     def set_exact(self, on: bool) -> None:
         """IMD's unfused table arithmetic (bitwise table values) on/off."""
         _check(lib().imdgpu_set_exact(self.h, int(on)), "set_exact")
+
+    def format_atoms(self, flags: int, order=None) -> bytes:
+        """IMD's checkpoint atom lines formatted on the device
+        (imdgpu_format_atoms); order: caller indices of the lines."""
+        n = 0
+        op = None
+        if order is not None:
+            o = np.ascontiguousarray(order, np.int32)
+            n = len(o)
+            op = _p(o, C.c_int)
+        ln = C.c_long(0)
+        _check(lib().imdgpu_format_atoms(self.h, flags, op, n, None, 0, C.byref(ln)),
+               "format_atoms")
+        buf = C.create_string_buffer(ln.value + 1)
+        _check(lib().imdgpu_format_atoms(self.h, flags, op, n, buf, ln.value, C.byref(ln)),
+               "format_atoms")
+        return buf.raw[:ln.value]
 
     def set_deterministic(self, on: bool) -> None:
         """FP64 passes on the full list without atomics: bitwise repeatable."""
@@ -661,6 +682,22 @@ class GpuBatch(GpuSystem):
         """Drop finished cells from the device once the unfinished ones hold
         at most pct % of its atoms (0: never)."""
         _check(lib().imdgpu_batch_set_compaction(self.h, int(pct)), "batch_set_compaction")
+
+
+FMT_HPO, FMT_VELOCITY, FMT_EAM_RHO = 1, 2, 4
+
+
+def format_fixed(x, prec: int, width: int = 0) -> bytes:
+    """Each value as printf("%*.*f\\n", width, prec, v), formatted on the
+    device (imdgpu_format_fixed)."""
+    a = np.ascontiguousarray(x, np.float64)
+    ln = C.c_long(0)
+    _check(lib().imdgpu_format_fixed(_p(a), len(a), prec, width, None, 0, C.byref(ln)),
+           "format_fixed")
+    buf = C.create_string_buffer(ln.value + 1)
+    _check(lib().imdgpu_format_fixed(_p(a), len(a), prec, width, buf, ln.value, C.byref(ln)),
+           "format_fixed")
+    return buf.raw[:ln.value]
 
 
 def set_device(device: int) -> None:

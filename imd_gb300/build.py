@@ -22,7 +22,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
            "-Xcompiler", "-ffp-contract=off", "--expt-relaxed-constexpr",
            "-I" + os.path.join(ROOT, "include")]
-SOURCES = ["system.cu", "forces.cu", "mixed.cu", "batch.cu", "learn.cu", "noalloc.cu", "potfile.cpp"]
+SOURCES = ["system.cu", "forces.cu", "mixed.cu", "batch.cu", "learn.cu", "noalloc.cu", "output.cu",
+           "potfile.cpp"]
 
 
 def nvcc() -> str:

@@ -13,6 +13,7 @@
 #pragma once
 
 #include <cstdint>
+#include <cstring>
 
 #ifdef __CUDACC__
 #define FMT_HD __host__ __device__ __forceinline__
@@ -23,6 +24,16 @@
 namespace imdfmt {
 
 typedef unsigned __int128 u128;
+
+FMT_HD uint64_t double_bits(double v) {
+#ifdef __CUDA_ARCH__
+  return (uint64_t)__double_as_longlong(v);
+#else
+  uint64_t b;
+  memcpy(&b, &v, sizeof b);
+  return b;
+#endif
+}
 
 FMT_HD uint64_t pow10u(int p) {
   uint64_t r = 1;
@@ -55,8 +66,7 @@ FMT_HD int pad_left(char *out, int len, int width) {
 // printf("%*.*f", width, prec, v) into out (at most 22 + prec + width
 // bytes, no terminating zero); returns the length, or -1 for |v| >= 2^63
 FMT_HD int fmt_fixed(double v, int prec, int width, char *out) {
-  uint64_t bits;
-  memcpy(&bits, &v, sizeof bits);
+  const uint64_t bits = double_bits(v);
   const bool neg = (bits >> 63) != 0;
   const int ex = (int)((bits >> 52) & 0x7ffu);
   const uint64_t frac_bits = bits & ((1ull << 52) - 1u);

@@ -108,4 +108,17 @@ void launch_ml_to_bf16(const float *w, __nv_bfloat16 *wb, int n, cudaStream_t st
 // system.cu: message returned by imdgpu_last_error()
 void set_last_error(const char *msg);
 
+// output.cu: IMD's checkpoint lines formatted on the device
+struct FormatScratch {
+  long *len = nullptr;   // per line: length, then its offset within its block
+  long *bsum = nullptr;  // per scan block: offset; [nb] the total
+  int *bad = nullptr;    // lowest line that could not be formatted
+  char *text = nullptr;
+  int cap_lines = 0;
+  long cap_bytes = 0;
+};
+int format_atom_lines(const SysView &v, const int *slot_of, const int *order, int n, int flags,
+                      char *buf, long cap, long *len, FormatScratch &fs, cudaStream_t st);
+void free_format_scratch(FormatScratch &fs);
+
 }  // namespace imdgpu

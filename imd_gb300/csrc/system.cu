@@ -224,6 +224,11 @@ struct imdgpu_sys {
   double vir_axial[3] = {0.0, 0.0, 0.0};
   double *d_npta = nullptr;   // 7: totals of the last k_npt_axial
 
+  // device formatting of checkpoint lines (output.cu)
+  FormatScratch fmt;
+  int *d_fmt_order = nullptr;
+  int fmt_order_cap = 0;
+
   // STRESS_TENS: per ext atom xx yy zz yz zx xy
   double *d_stress = nullptr;
   size_t stress_cap = 0;
@@ -2111,6 +2116,8 @@ int imdgpu_destroy(imdgpu_sys *s) {
   dfree(s->d_glok);
   dfree(s->d_npt);
   dfree(s->d_npta);
+  free_format_scratch(s->fmt);
+  dfree(s->d_fmt_order);
   dfree(s->d_sys_short);
   dfree(s->d_atom_sys); dfree(s->d_aoff); dfree(s->d_sgdim); dfree(s->d_scdim); dfree(s->d_scoff);
   dfree(s->d_sys_done); dfree(s->d_ndone); dfree(s->d_sbox); dfree(s->d_stbox); dfree(s->d_cs);
@@ -4469,6 +4476,39 @@ int imdgpu_batch_ml_start(imdgpu_sys *s, int *used, double *e_start, double *e_p
 }
 
 }  // extern "C"
+
+// write_atoms_config's text (src/imd_io_3d.c:696-948) formatted on the
+// device (output.cu), lines in `order` (caller indices) or caller order
+extern "C" int imdgpu_format_atoms(imdgpu_sys *s, int flags, const int *order, int n, char *buf,
+                                   long cap, long *len) {
+  if (!s || !s->atoms_set || !len) return fail(IMDGPU_ERR_ARG, "format_atoms: no atoms / null");
+  if (flags & ~(IMDGPU_FMT_HPO | IMDGPU_FMT_VELOCITY | IMDGPU_FMT_EAM_RHO))
+    return fail(IMDGPU_ERR_ARG, "format_atoms: unknown flags");
+  if (int rc = batch_full(s)) return rc;
+  const int natoms = s->n;
+  const int *d_order = nullptr;
+  if (order) {
+    if (n < 0) return fail(IMDGPU_ERR_ARG, "format_atoms: n < 0");
+    for (int a = 0; a < n; a++)
+      if (order[a] < 0 || order[a] >= natoms)
+        return fail(IMDGPU_ERR_ARG, "format_atoms: order[" + std::to_string(a) +
+                                        "] is not an atom index");
+    if (s->fmt_order_cap < n) {
+      dfree(s->d_fmt_order);
+      s->d_fmt_order = nullptr;
+      CK(dalloc(&s->d_fmt_order, n > 0 ? n : 1));
+      s->fmt_order_cap = n;
+    }
+    if (n > 0)
+      CK(cudaMemcpyAsync(s->d_fmt_order, order, sizeof(int) * (size_t)n, cudaMemcpyHostToDevice,
+                         s->st));
+    d_order = s->d_fmt_order;
+  } else {
+    n = natoms;
+  }
+  const SysView v = view(s);
+  return format_atom_lines(v, s->slot_of, d_order, n, flags, buf, cap, len, s->fmt, s->st);
+}
 
 extern "C" int imdgpu_get_pairs(imdgpu_sys *s, long cap, int *ni, int *nj, int *shift, double *r2,
                      long *count) {

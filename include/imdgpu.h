@@ -354,6 +354,30 @@ int imdgpu_ml_set_loss_weights(imdgpu_sys *sys, const double *w);
  * output pointer may be NULL. */
 int imdgpu_batch_ml_start(imdgpu_sys *sys, int *used, double *e_start, double *e_pred);
 
+/* IMD's checkpoint text formatted on the device: the atom lines of
+ * write_atoms_config (src/imd_io_3d.c:696-948, text branch), byte for byte
+ * what its sprintf calls print, so that writing a checkpoint of a large
+ * system needs neither the state on the host nor 10 printf conversions per
+ * atom there.  Per atom: "%d %d" NUMMER and type, RESOL1 mass, RESOL3
+ * position, RESOL3 velocity (momentum / mass; with IMDGPU_FMT_VELOCITY, as
+ * every ensemble but CG writes it), RESOL1 POTENG of the last calc_forces,
+ * RESOL1 EAM_RHO (with IMDGPU_FMT_EAM_RHO, the EAM2 builds), "\n"; RESOL1
+ * is " %12.16f" with IMDGPU_FMT_HPO (IMD's hpo option) and " %f" without
+ * (:704-711).  order: n caller indices, the order of the lines (IMD writes
+ * cell by cell), or NULL for all atoms in caller order.  *len receives the
+ * size of the text; buf (host) receives it when cap >= *len, so a first call
+ * with cap = 0 sizes it.  A value of magnitude 2^63 or more is
+ * IMDGPU_ERR_ARG. */
+#define IMDGPU_FMT_HPO 1
+#define IMDGPU_FMT_VELOCITY 2
+#define IMDGPU_FMT_EAM_RHO 4
+int imdgpu_format_atoms(imdgpu_sys *sys, int flags, const int *order, int n, char *buf,
+                        long cap, long *len);
+/* The formatter alone: n doubles (host), each as printf("%*.*f\n", width,
+ * prec, x) (prec 0..17, width 0..64), into buf as imdgpu_format_atoms. */
+int imdgpu_format_fixed(const double *x, int n, int prec, int width, char *buf, long cap,
+                        long *len);
+
 /* Neighbour pairs of the current list: NUMMER of both atoms, image shift of
  * the second (3 ints, in box vectors) and r^2 as used for the list test.
  * With cap == 0 only *count is set. */

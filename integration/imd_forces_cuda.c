@@ -385,6 +385,63 @@ void move_atoms_nvt(void)
 #endif
 }
 
+/******************************************************************************
+*  write_atoms_config (src/imd_io_3d.c:696-948): the atom lines of every
+*  configuration IMD writes in text (checkpoints, relaxed configurations),
+*  formatted on the device, byte for byte what IMD's sprintf calls print, in
+*  IMD's cell order.  The cuda target compiles imd_io_3d.c with
+*  -Dwrite_atoms_config=write_atoms_config_host, which keeps IMD's own for
+*  binary output, for virtual types, and for builds that write more fields
+*  than the device formats.
+******************************************************************************/
+
+#if !defined(CNA) && !defined(UNIAX) && !defined(VARCHG) && !defined(EWALD) && \
+    !defined(USEFCS) && !defined(NNBR) && !defined(REFPOS) && !defined(DISLOC) && \
+    !defined(EEAM) && !defined(NORHOH) && !defined(DIPOLE) && !defined(KERMODE) && \
+    !defined(DAMP) && !defined(ADA) && !defined(NYETENSOR) && !defined(LOADBALANCE) && \
+    !defined(VISCOUS) && !defined(TWOD)
+#define DEVICE_FORMATS_CONFIG 1
+#endif
+
+void write_atoms_config_host(FILE *out);
+
+void write_atoms_config(FILE *out)
+{
+#ifdef DEVICE_FORMATS_CONFIG
+  if (G && !host_owns_atoms && !binary_output && vtypes == ntypes) {
+    long n = 0, a = 0, len = 0;
+    int k, i, flags = 0;
+    int *order;
+    char *text;
+    for (k = 0; k < NCELLS; k++) n += CELLPTR(k)->n;
+    order = (int *)malloc((n > 0 ? n : 1) * sizeof(int));
+    if (!order) error("imd_forces_cuda: out of memory");
+    for (k = 0; k < NCELLS; k++) {
+      cell *c = CELLPTR(k);
+      for (i = 0; i < c->n; i++) order[a++] = (int)caller_of(NUMMER(c, i));
+    }
+    if (ensemble != ENS_CG) flags |= IMDGPU_FMT_VELOCITY;
+#ifdef HPO
+    flags |= IMDGPU_FMT_HPO;
+#endif
+#ifdef EAM2
+    flags |= IMDGPU_FMT_EAM_RHO;
+#endif
+    lib_check(imdgpu_format_atoms(G, flags, order, (int)n, NULL, 0, &len), "imdgpu_format_atoms");
+    text = (char *)malloc(len > 0 ? len : 1);
+    if (!text) error("imd_forces_cuda: out of memory");
+    lib_check(imdgpu_format_atoms(G, flags, order, (int)n, text, len, &len),
+              "imdgpu_format_atoms");
+    if (len > 0 && fwrite(text, 1, (size_t)len, out) != (size_t)len)
+      error("imd_forces_cuda: writing a configuration failed");
+    free(text);
+    free(order);
+    return;
+  }
+#endif
+  write_atoms_config_host(out);
+}
+
 #ifdef CG
 /******************************************************************************
 *  reset_cg, cg_step (src/imd_cg.c:30-66): IMD's CG with its parameters

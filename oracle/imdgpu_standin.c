@@ -262,3 +262,32 @@ int imdgpu_cg_step(imdgpu_sys *g, int steps) {
   return orc_cg_step(&g->s, steps) < 0 ? fail(IMDGPU_ERR_BRENT, "Too many iterations in brent")
                                        : IMDGPU_OK;
 }
+
+/* write_atoms_config's text lines (the device formats them in the library),
+ * here by snprintf: the format the library must reproduce */
+int imdgpu_format_atoms(imdgpu_sys *g, int flags, const int *order, int n, char *buf,
+                        long cap, long *len) {
+  orc_sys_t *s = &g->s;
+  const char *f = (flags & IMDGPU_FMT_HPO) ? " %12.16f" : " %f";
+  char line[512];
+  long total = 0;
+  if (!order) n = s->n;
+  for (int a = 0; a < n; a++) {
+    const int i = order ? order[a] : a;
+    int l = snprintf(line, sizeof line, "%d %d", s->number[i], s->type[i]);
+    double vals[9];
+    int nv = 0;
+    vals[nv++] = s->mass[i];
+    for (int c = 0; c < 3; c++) vals[nv++] = s->x[3 * i + c];
+    if (flags & IMDGPU_FMT_VELOCITY)
+      for (int c = 0; c < 3; c++) vals[nv++] = s->p[3 * i + c] / s->mass[i];
+    vals[nv++] = s->epot[i];
+    if (flags & IMDGPU_FMT_EAM_RHO) vals[nv++] = s->eam_rho[i];
+    for (int k = 0; k < nv; k++) l += snprintf(line + l, sizeof line - l, f, vals[k]);
+    l += snprintf(line + l, sizeof line - l, "\n");
+    if (buf && total + l <= cap) memcpy(buf + total, line, l);
+    total += l;
+  }
+  *len = total;
+  return IMDGPU_OK;
+}
