@@ -102,6 +102,9 @@ struct SysView {
   const int *hshell;        // nshell buffered lin per real rank (-1 none): half or full shell
   int nshell;               // 14 (half list, IMD's AR order) or 27 (full or balanced list)
   int balanced;             // balanced half list: 27 cells, IMD's 14 first (see k_rb_build_half)
+  int split;                // mixed: balanced half list at the front of each row (nnb), the
+                            // other partners at its back (nnb2 of them, from nbcap - 1 down)
+  int *nnb2;
   const int *bsrc;          // per buffer cell (enumerated): source real lin
   const int *blin;          // per buffer cell: its lin
   const int *bcode;         // per buffer cell: packed image shift

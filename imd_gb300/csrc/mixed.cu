@@ -7,14 +7,18 @@
 //     d = (hi_j - hi_i) + (lo_j - lo_i) is accurate to the last FP32 bit of d
 //     itself: the coordinates an FP32 pair sees are relative to the atom,
 //     never absolute box coordinates;
-//   * the list is the balanced half list of the FP64 path (every pair once,
-//     IMD's pair set, k_rb_build_half), so each pair's FP32 arithmetic and
-//     each partner gather happen once;
-//   * the owner's sums of rho, force, energy and virial are kept as
-//     error-free (TwoSum) pairs of FP32 values, converted to FP64 once per
-//     atom; the partner's share of every pair goes in with an FP64 atomic;
-//     ghost sums fold into their owners as in the FP64 path; the block and
-//     device reductions are FP64;
+//   * the list is the split list of k_rb_build_half: in every row the
+//     balanced half list (IMD's pair set, every pair once) comes first and
+//     the partners the other atom keeps follow from the back of the row, so
+//     one list serves as a half list and as a full list;
+//   * the density pass walks the half list: each pair's FP32 arithmetic and
+//     partner gather happen once, the partner's rho goes in with an FP64
+//     atomic and ghost rho folds into its owner;
+//   * the force pass walks the full row: each atom owns its sums, with no
+//     atomics and no ghost fold;
+//   * per-atom sums of rho, force, energy and virial are kept as error-free
+//     (TwoSum) pairs of FP32 values and converted to FP64 once per atom; the
+//     block and device reductions are FP64;
 //   * the embedding function and the integrator stay FP64.
 #include <algorithm>
 
@@ -130,12 +134,10 @@ __global__ void k_ghost_dff(SysView v, float *dff) {
     dff[v.n + g] = dff[v.gowner[g]];
 }
 
-// forces over the half list: every pair's force d*grad goes to atom i (in
-// its TwoSum sums) and -d*grad to atom j (FP64 atomics); the pair energy
-// and -r^2 grad once per pair.  EPOT: half the pair energy to each atom's
-// POTENG; otherwise, with v.eshare, the whole pair energy to its owner
-// (per-system sums of a batch).
-template <bool NT1, bool EAM, bool EPOT>
+// forces over the full row (the half list at the front, the other partners
+// at the back): each directed pair adds d*grad to atom i and half of the
+// pair energy and virial
+template <bool NT1, bool EAM>
 __global__ void __launch_bounds__(BS_FORCE_MAX) k_force_mixed(SysView v, DevTable pair,
                                                           DevTable rho, const SplitPos *sp,
                                                           const float *dff, double *partial) {
@@ -144,14 +146,16 @@ __global__ void __launch_bounds__(BS_FORCE_MAX) k_force_mixed(SysView v, DevTabl
   if (i < v.n && !atom_idle(v, i)) {
     const SplitPos a = sp[i];
     const int it = NT1 ? 0 : __float_as_int(a.hi.w), nt = v.ntypes;
-    const int nn = v.nnb[i];
+    const int n1 = v.nnb[i], n2 = v.nnb2[i];
     const float dfi = EAM ? dff[i] : 0.f;
     Acc fx, fy, fz, ee, vir;
     bool shortf = false;
     const uint32_t *__restrict__ nb = v.nbr + i;
-#pragma unroll 2
+    const int nn = n1 + n2, back = v.nbcap - n1 - n2;  // row k >= n1 lives at k + back
+#pragma unroll 4
     for (int k = 0; k < nn; k++) {
-      const int j = (int)(__ldg(nb + (size_t)k * v.ncap) & NB_MASK);
+      const int row = k < n1 ? k : k + back;
+      const int j = (int)(__ldg(nb + (size_t)row * v.ncap) & NB_MASK);
       const SplitPos b = ldsp(&sp[j]);
       const float dx = (b.hi.x - a.hi.x) + (b.lo.x - a.lo.x);
       const float dy = (b.hi.y - a.hi.y) + (b.lo.y - a.lo.y);
@@ -159,13 +163,12 @@ __global__ void __launch_bounds__(BS_FORCE_MAX) k_force_mixed(SysView v, DevTabl
       const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
       const int jt = NT1 ? 0 : __float_as_int(b.hi.w);
       const int col = NT1 ? 0 : it * nt + jt;
-      float grad = 0.f, pot = 0.f;
+      float grad = 0.f;
       bool have = false;
       if (r2 <= pair.fend[col]) {
         float chi;
         const int kk = tab_index_f(pair, col, r2, chi);
-        pot = polyf_v(pair, col, kk, chi);
-        ee.add(pot);
+        ee.add(0.5f * polyf_v(pair, col, kk, chi));
         grad = polyf_g(pair, col, kk, chi);
         shortf |= r2 < pair.fbegin[col];
         have = true;
@@ -187,25 +190,19 @@ __global__ void __launch_bounds__(BS_FORCE_MAX) k_force_mixed(SysView v, DevTabl
         }
       }
       if (have) {
-        const float px = dx * grad, py = dy * grad, pz = dz * grad;
-        fx.add(px);
-        fy.add(py);
-        fz.add(pz);
-        vir.add(-r2 * grad);
-        double *fj = &v.frc[j].x;
-        atomicAdd(fj + 0, -(double)px);
-        atomicAdd(fj + 1, -(double)py);
-        atomicAdd(fj + 2, -(double)pz);
-        if (EPOT) atomicAdd(fj + 3, 0.5 * (double)pot);
+        fx.add(dx * grad);
+        fy.add(dy * grad);
+        fz.add(dz * grad);
+        vir.add(-0.5f * r2 * grad);
       }
     }
     const double e = ee.value();
-    double *fi = &v.frc[i].x;
-    atomicAdd(fi + 0, fx.value());
-    atomicAdd(fi + 1, fy.value());
-    atomicAdd(fi + 2, fz.value());
-    if (EPOT) atomicAdd(fi + 3, 0.5 * e);
-    else if (v.eshare) atomicAdd(fi + 3, e);
+    double4 f = v.frc[i];  // .w holds the embedding energy
+    f.x = fx.value();
+    f.y = fy.value();
+    f.z = fz.value();
+    f.w += e;
+    v.frc[i] = f;
     acc[0] = e;
     acc[1] = vir.value();
     if (shortf) flag_short(v, i);
@@ -235,8 +232,7 @@ static inline int nblk(long n, int bs) { return (int)((n + bs - 1) / bs); }
 template <bool NT1, bool EAM>
 static void launch_force_mixed2(const ForceTabs &t, int nbf, cudaStream_t st, const SysView &v,
                                 const SplitPos *sp, const float *dff, double *pf) {
-  if (t.epot) k_force_mixed<NT1, EAM, true><<<nbf, t.bs, 0, st>>>(v, t.pair, t.rho, sp, dff, pf);
-  else k_force_mixed<NT1, EAM, false><<<nbf, t.bs, 0, st>>>(v, t.pair, t.rho, sp, dff, pf);
+  k_force_mixed<NT1, EAM><<<nbf, t.bs, 0, st>>>(v, t.pair, t.rho, sp, dff, pf);
 }
 
 int launch_forces_mixed(const SysView &v, const ForceTabs &t, DevScalars *sc, float *dff,
@@ -275,9 +271,8 @@ int launch_forces_mixed(const SysView &v, const ForceTabs &t, DevScalars *sc, fl
     if (ev) cudaEventRecord(ev[3], st);
     launches += 1;
   }
-  fold_force_launch(v, gblocks, st);
   k_finalize_mixed<<<1, 32, 0, st>>>(pe, t.eam ? nbe : 0, pf, nbf, sc);
-  return launches + 2;
+  return launches + 1;
 }
 
 }  // namespace imdgpu

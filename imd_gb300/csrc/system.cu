@@ -101,7 +101,9 @@ struct imdgpu_sys {
   int nreal_cells = 0, nall_cells = 0, nbuf = 0;
   bool geom_ready = false;
   bool geom_full = false;     // full list (mixed precision, deterministic FP64) instead of IMD's half list
-  bool geom_balanced = false; // FP64 half list with balanced orientation (single system)
+  bool geom_balanced = false; // half list with balanced orientation (FP64 and mixed)
+  bool geom_split = false;    // mixed: the balanced half list first in every row, the other
+                              // partners at the back (a full list in one)
   bool deterministic = false; // FP64 passes without atomics (imdgpu_set_deterministic)
   float *dff = nullptr;
   int *d_cell_rank = nullptr, *d_rank_lin = nullptr, *d_hshell = nullptr;
@@ -119,6 +121,7 @@ struct imdgpu_sys {
   int *key = nullptr, *local = nullptr, *perm = nullptr, *slot_rank = nullptr;
   uint32_t *nbr = nullptr;
   int *nnb = nullptr;
+  int *nnb2 = nullptr;        // split list: partners at the back of each row
   unsigned *status = nullptr;
   int *counters = nullptr;
   double *partial = nullptr;
@@ -532,8 +535,10 @@ __global__ void __launch_bounds__(128) k_rb_build_half(SysView v, DevScalars *sc
   const int r = slot_rank[i];
   const int *hs = v.hshell + (size_t)v.nshell * r;
   const bool bal = v.balanced != 0;
+  const bool split = v.split != 0;
   const bool full = (v.nshell == 27) && !bal;
   const int numi = bal ? v.number[i] : 0;
+  int cnt2 = 0;  // split list: partners owned by the other atom, from the back
   const SplitPos *sp = reinterpret_cast<const SplitPos *>(v.xl);
   const SplitPos a = sp[i];
   // FP32 distance decides all pairs outside a +-1e-5 band around the list
@@ -548,7 +553,10 @@ __global__ void __launch_bounds__(128) k_rb_build_half(SysView v, DevScalars *sc
     const int j0 = (m == 0 && !full && !bal) ? i + 1 : s;
     for (int j = j0; j < e; j++) {
       if ((full || bal) && j == i) continue;
-      if (bal && j < v.n && !owns_pair(numi, v.number[j])) continue;
+      // the atom that keeps the pair: parity for two real atoms, IMD's half
+      // shell (the first 14 cells) for a ghost
+      const bool owned = !bal || (j < v.n ? owns_pair(numi, v.number[j]) : m < 14);
+      if (!owned && !split) continue;
       const SplitPos b = ldsp(&sp[j]);
       const float dx = (b.hi.x - a.hi.x) + (b.lo.x - a.lo.x);
       const float dy = (b.hi.y - a.hi.y) + (b.lo.y - a.lo.y);
@@ -560,14 +568,22 @@ __global__ void __launch_bounds__(128) k_rb_build_half(SysView v, DevScalars *sc
         in = r2_exact(dsub(pj.x, pi.x), dsub(pj.y, pi.y), dsub(pj.z, pi.z)) < v.cellsz;
       }
       if (in) {
-        if (cnt < v.nbcap) v.nbr[(size_t)cnt * v.ncap + i] = (uint32_t)j | ((uint32_t)m << NB_SHIFT);
-        cnt++;
+        const uint32_t word = (uint32_t)j | ((uint32_t)m << NB_SHIFT);
+        if (owned) {
+          if (cnt + cnt2 < v.nbcap) v.nbr[(size_t)cnt * v.ncap + i] = word;
+          cnt++;
+        } else {
+          if (cnt + cnt2 < v.nbcap) v.nbr[(size_t)(v.nbcap - 1 - cnt2) * v.ncap + i] = word;
+          cnt2++;
+        }
       }
     }
   }
-  v.nnb[i] = min(cnt, v.nbcap);
-  atomicMax(&v.counters[1], cnt);
-  if (cnt > v.nbcap) atomicOr(v.status, ST_NBOVER);
+  const bool over = cnt + cnt2 > v.nbcap;
+  v.nnb[i] = over ? 0 : cnt;
+  if (split) v.nnb2[i] = over ? 0 : cnt2;
+  atomicMax(&v.counters[1], cnt + cnt2);
+  if (over) atomicOr(v.status, ST_NBOVER);
 }
 
 __global__ void k_rb_done(DevScalars *sc, long *nbl) {
@@ -1417,6 +1433,8 @@ static SysView view(imdgpu_sys *s) {
   v.hshell = s->d_hshell;
   v.nshell = (s->geom_full || s->geom_balanced) ? 27 : 14;
   v.balanced = s->geom_balanced ? 1 : 0;
+  v.split = s->geom_split ? 1 : 0;
+  v.nnb2 = s->nnb2;
   v.dff = s->dff;
   v.bsrc = s->d_bsrc;
   v.blin = s->d_blin;
@@ -1538,6 +1556,7 @@ static int setup_geometry(imdgpu_sys *s) {
   // for the full list all 27 neighbour cells (own cell first)
   s->geom_full = s->deterministic && s->precision == IMDGPU_FP64;
   s->geom_balanced = !s->geom_full;
+  s->geom_split = s->geom_balanced && s->precision == IMDGPU_MIXED;
   const int ns = (s->geom_full || s->geom_balanced) ? 27 : 14;
   std::vector<int> hshell((size_t)ns * s->nreal_cells, -1);
   std::vector<char> used(s->nall_cells, 0);
@@ -1576,6 +1595,10 @@ static int setup_geometry(imdgpu_sys *s) {
         for (int b = -a; b <= 1; b++)
           for (int c = (a == 0 ? -b : -a); c <= 1; c++) {
             if (a == 0 && b == 0 && c == 0) continue;
+            if (s->geom_split) {
+              add(-a, -b, -c);  // the split list keeps the other partners too: ghosts as well
+              continue;
+            }
             const int qq = ((i - a) * cy + (j - b)) * cz + (k - c);
             if (cell_rank[qq] >= 0) nq[nn] = qq;
             nn++;
@@ -1651,6 +1674,7 @@ static int setup_geometry_batch(imdgpu_sys *s) {
   }
   s->geom_full = s->deterministic && s->precision == IMDGPU_FP64;
   s->geom_balanced = !s->geom_full;
+  s->geom_split = s->geom_balanced && s->precision == IMDGPU_MIXED;
   const int nsh = (s->geom_full || s->geom_balanced) ? 27 : 14;
   std::vector<double> tb(9 * (size_t)ns);
   std::vector<int> gdim(3 * (size_t)ns), cdim(3 * (size_t)ns), coff(ns + 1, 0), roff(ns + 1, 0);
@@ -1720,6 +1744,10 @@ static int setup_geometry_batch(imdgpu_sys *s) {
           for (int b = -a; b <= 1; b++)
             for (int c = (a == 0 ? -b : -a); c <= 1; c++) {
               if (a == 0 && b == 0 && c == 0) continue;
+              if (s->geom_split) {
+                add(-a, -b, -c);
+                continue;
+              }
               const int ri = i - a, rj = j - b, rk = k - c;
               if (ri >= 1 && ri <= gx && rj >= 1 && rj <= gy && rk >= 1 && rk <= gz)
                 nq[nn] = coff[q] + (ri * cy + rj) * cz + rk;
@@ -1852,7 +1880,7 @@ static void estimate_caps(imdgpu_sys *s, int &nbcap, int &gcap) {
   const double rl = std::sqrt(s->cellsz);
   const double dens = s->n / std::fabs(s->volume);
   const double full = 4.18879 * rl * rl * rl * dens;
-  nbcap = (int)((s->geom_full ? 1.0 : 0.5) * full * 1.6) + 32;
+  nbcap = (int)(((s->geom_full || s->geom_split) ? 1.0 : 0.5) * full * 1.6) + 32;
   const double frac = (double)(s->nall_cells - s->nreal_cells) / s->nreal_cells;
   gcap = (int)(s->n * frac * 1.25) + 1024;
   if (s->nsys > 0) gcap = (int)(s->n * frac * 0.8) + 4096;  // refined by the first build
@@ -2102,7 +2130,7 @@ int imdgpu_destroy(imdgpu_sys *s) {
   dfree(s->rho); dfree(s->df); dfree(s->xl); dfree(s->number); dfree(s->orig);
   dfree(s->tnumber); dfree(s->torig); dfree(s->ecell); dfree(s->gowner); dfree(s->gcode);
   dfree(s->key); dfree(s->local); dfree(s->perm); dfree(s->slot_rank); dfree(s->nbr);
-  dfree(s->nnb); dfree(s->status); dfree(s->counters); dfree(s->partial); dfree(s->dsc);
+  dfree(s->nnb); dfree(s->nnb2); dfree(s->status); dfree(s->counters); dfree(s->partial); dfree(s->dsc);
   dfree(s->dnbl); dfree(s->hist); dfree(s->oldx); dfree(s->cgg); dfree(s->cgh);
   dfree(s->toldx); dfree(s->tcgg); dfree(s->tcgh);
   dfree(s->slot_of); dfree(s->d_in); dfree(s->d_out); dfree(s->flushbuf); dfree(s->dff);
@@ -2388,7 +2416,7 @@ int imdgpu_set_atoms(imdgpu_sys *s, int n, const int *number, const int *type,
   if (n != s->n) {
     dfree(s->mom); dfree(s->ref); dfree(s->tpos); dfree(s->tmom); dfree(s->number);
     dfree(s->orig); dfree(s->tnumber); dfree(s->torig); dfree(s->key); dfree(s->local);
-    dfree(s->perm); dfree(s->slot_rank); dfree(s->nnb); dfree(s->partial); dfree(s->nbr);
+    dfree(s->perm); dfree(s->slot_rank); dfree(s->nnb); dfree(s->nnb2); dfree(s->partial); dfree(s->nbr);
     dfree(s->oldx); dfree(s->cgg); dfree(s->cgh); dfree(s->toldx); dfree(s->tcgg); dfree(s->tcgh);
     s->n = n;
     s->ncap = n;
@@ -2405,6 +2433,8 @@ int imdgpu_set_atoms(imdgpu_sys *s, int n, const int *number, const int *type,
     CK(dalloc(&s->perm, n));
     CK(dalloc(&s->slot_rank, n));
     CK(dalloc(&s->nnb, n));
+    CK(dalloc(&s->nnb2, n));
+    CK(cudaMemset(s->nnb2, 0, sizeof(int) * (size_t)n));
     // block partials: the largest user is the deterministic force pass, two
     // per block of four lanes per atom at 32 lanes per block
     CK(dalloc(&s->partial, 8 * (size_t)nblk(n, 64) + 2 * (size_t)nblk(4L * n, 32) + 64));
