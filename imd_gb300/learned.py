@@ -117,12 +117,15 @@ class RelaxResult:
 def relax(tables, cells, fmax: float = 1e-4, weights=None, precision=api.FP64,
           keep_positions: bool = False, chunk_rounds: int = 4096,
           interpolation: int = BATCH_INTERPOLATION, nbl_margin: float = 0.4,
-          trace: bool = False) -> RelaxResult:
+          trace: bool = False, start_iters: int = 1) -> RelaxResult:
     """Relax every cell with the batched CG, from the learned start when
     `weights` are given.  The wall time covers the learned start (its two
     force calls and the prediction) and the CG, not the upload of the cells.
     Force calls per cell include the learned start's two.  trace: advance
-    64 rounds per call and record the progress after each (RelaxResult.trace)."""
+    64 rounds per call and record the progress after each (RelaxResult.trace).
+    start_iters > 1 applies the learned start again from the positions it
+    chose (features recomputed there), each application kept only where it
+    lowers the cell's energy; two more force calls each."""
     if trace:
         chunk_rounds = 64
     b = make_batch(tables, cells, precision, interpolation, nbl_margin)
@@ -133,6 +136,10 @@ def relax(tables, cells, fmax: float = 1e-4, weights=None, precision=api.FP64,
     if weights is not None:
         b.ml_set_weights(weights)
         used, e0, e1 = b.ml_start()
+        for _ in range(start_iters - 1):
+            u2, _, e2 = b.ml_start()
+            used = np.maximum(used, u2)
+            e1 = np.where(u2 == 1, e2, e1)
     b.begin(fmax)
     rounds = 0
     tr = []
@@ -146,7 +153,7 @@ def relax(tables, cells, fmax: float = 1e-4, weights=None, precision=api.FP64,
             raise RuntimeError("batched CG did not finish")
     sec = time.perf_counter() - t0
     r = b.results()
-    nfc = r["nfc"] + (2 if weights is not None else 0)
+    nfc = r["nfc"] + (2 * start_iters if weights is not None else 0)
     pos = b.positions() if keep_positions else []
     b.close()
     return RelaxResult(sec, r["epot"], r["fmax"], nfc, r["steps"], r["status"], rounds,

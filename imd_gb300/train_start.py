@@ -52,15 +52,15 @@ def relax_targets(tabs, cells, chunk: int = 512):
     return disp, stats
 
 
-def evaluate(tabs, cells, w):
+def evaluate(tabs, cells, w, start_iters: int = 1, plain=None):
     """Held-out cells relaxed plainly and from the learned start."""
-    plain = learned.relax(tabs, cells)
-    ml = learned.relax(tabs, cells, weights=w)
+    plain = plain or learned.relax(tabs, cells)
+    ml = learned.relax(tabs, cells, weights=w, start_iters=start_iters)
     n = np.array([c.n for c in cells])
     both = (plain.status == 0) & (ml.status == 0)
     de = (ml.epot - plain.epot)[both] / n[both]
     return {
-        "cells": len(cells), "atoms": int(n.sum()),
+        "cells": len(cells), "atoms": int(n.sum()), "start_iters": start_iters,
         "plain_seconds": plain.seconds, "learned_seconds": ml.seconds,
         "plain_relaxations_per_s": plain.relaxations_per_s,
         "learned_relaxations_per_s": ml.relaxations_per_s,
@@ -94,6 +94,8 @@ def main(argv=None):
     ap.add_argument("--core-weight", type=float, default=0.0,
                     help="extra loss weight of atoms displaced by >= --core-disp A")
     ap.add_argument("--core-disp", type=float, default=0.2)
+    ap.add_argument("--start-iters", type=int, default=1,
+                    help="also evaluate the learned start applied this many times")
     a = ap.parse_args(argv)
     tmp = tempfile.mkdtemp(prefix="imdtrain")
     tabs = wl.sutton_chen_tables(os.path.join(tmp, "cu"), [wl.CU])
@@ -127,8 +129,12 @@ def main(argv=None):
            "relax_batches": relax_stats}
     if a.eval_cells > 0:
         held = wl.defect_batch(a.eval_cells, seed=6)
-        rec["eval"] = evaluate(tabs, held, w)
+        plain = learned.relax(tabs, held)
+        rec["eval"] = evaluate(tabs, held, w, plain=plain)
         print(json.dumps(rec["eval"]), flush=True)
+        if a.start_iters > 1:
+            rec["eval_iterated"] = evaluate(tabs, held, w, start_iters=a.start_iters, plain=plain)
+            print(json.dumps(rec["eval_iterated"]), flush=True)
     os.makedirs(os.path.dirname(os.path.abspath(a.out)), exist_ok=True)
     np.savez(a.out, w=w, record=json.dumps(rec))
     print("wrote %s (loss %.3e -> %.3e; zero prediction %.3e)" % (a.out, loss0, loss1, zero))
