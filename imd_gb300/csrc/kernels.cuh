@@ -17,6 +17,7 @@ struct ForceTabs {
   int bs;        // threads per block of the force pass (autotuned, multiple of 32)
   int bs_rho;    // threads per block of the density pass (autotuned)
   int det;       // FP64 passes on the full list without atomics (deterministic)
+  const float4 *fused;  // mixed force pass: fused pair/density rows, or null
 };
 
 // Device-side scalars of one system (results + control).

@@ -137,9 +137,10 @@ __global__ void k_ghost_dff(SysView v, float *dff) {
 // forces over the full row (the half list at the front, the other partners
 // at the back): each directed pair adds d*grad to atom i and half of the
 // pair energy and virial
-template <bool NT1, bool EAM>
+template <bool NT1, bool EAM, bool FUSED>
 __global__ void __launch_bounds__(BS_FORCE_MAX) k_force_mixed(SysView v, DevTable pair,
-                                                          DevTable rho, const SplitPos *sp,
+                                                          DevTable rho, const float4 *fused,
+                                                          const SplitPos *sp,
                                                           const float *dff, double *partial) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   double acc[2] = {0.0, 0.0};
@@ -165,7 +166,27 @@ __global__ void __launch_bounds__(BS_FORCE_MAX) k_force_mixed(SysView v, DevTabl
       const int col = NT1 ? 0 : it * nt + jt;
       float grad = 0.f;
       bool have = false;
-      if (r2 <= pair.fend[col]) {
+      if (FUSED) {
+        // one species, quadratic pair and density tables on one grid: one
+        // index and one 32-byte row serve the three lookups below (the
+        // cubic coefficients of a quadratic table are zero and left out)
+        const bool inp = r2 <= pair.fend[0], inr = r2 < rho.fend[0];
+        if (inp || inr) {
+          float chi;
+          const int kk = tab_index_f(pair, 0, r2, chi);
+          const float4 f0 = __ldg(&fused[2 * kk]), f1 = __ldg(&fused[2 * kk + 1]);
+          if (inp) {
+            ee.add(0.5f * fmaf(chi, fmaf(chi, f0.z, f0.y), f0.x));
+            grad = fmaf(chi, f1.x, f0.w);
+            shortf |= r2 < pair.fbegin[0];
+          }
+          if (inr) {
+            const float ris = fmaf(chi, f1.z, f1.y);
+            grad += 0.5f * (dfi * ris + __ldg(&dff[j]) * ris);
+          }
+          have = true;
+        }
+      } else if (r2 <= pair.fend[col]) {
         float chi;
         const int kk = tab_index_f(pair, col, r2, chi);
         ee.add(0.5f * polyf_v(pair, col, kk, chi));
@@ -173,7 +194,7 @@ __global__ void __launch_bounds__(BS_FORCE_MAX) k_force_mixed(SysView v, DevTabl
         shortf |= r2 < pair.fbegin[col];
         have = true;
       }
-      if (EAM) {
+      if (EAM && !FUSED) {
         const int col1 = NT1 ? 0 : jt * nt + it, col2 = col;
         if (r2 < rho.fend[col1] || r2 < rho.fend[col2]) {
           float chi;
@@ -232,7 +253,14 @@ static inline int nblk(long n, int bs) { return (int)((n + bs - 1) / bs); }
 template <bool NT1, bool EAM>
 static void launch_force_mixed2(const ForceTabs &t, int nbf, cudaStream_t st, const SysView &v,
                                 const SplitPos *sp, const float *dff, double *pf) {
-  k_force_mixed<NT1, EAM><<<nbf, t.bs, 0, st>>>(v, t.pair, t.rho, sp, dff, pf);
+  if constexpr (NT1 && EAM) {
+    if (t.fused) {
+      k_force_mixed<true, true, true><<<nbf, t.bs, 0, st>>>(v, t.pair, t.rho, t.fused, sp, dff,
+                                                             pf);
+      return;
+    }
+  }
+  k_force_mixed<NT1, EAM, false><<<nbf, t.bs, 0, st>>>(v, t.pair, t.rho, nullptr, sp, dff, pf);
 }
 
 int launch_forces_mixed(const SysView &v, const ForceTabs &t, DevScalars *sc, float *dff,

@@ -87,6 +87,10 @@ struct imdgpu_sys {
   double4 *dcgn[3] = {nullptr, nullptr, nullptr};
   float4 *dcvf[3] = {nullptr, nullptr, nullptr};
   float4 *dcgf[3] = {nullptr, nullptr, nullptr};
+  // host copies of the FP32 rows, and the fused rows of the mixed force pass
+  // (pair value and gradient, density gradient of one row in 32 bytes)
+  std::vector<float4> hcvf[3], hcgf[3];
+  float4 *dfused = nullptr;
   int exact = 0;
   int interp = 0;  // table interpolation of tables read from now on
   std::vector<double> pending_table2[3];
@@ -515,14 +519,14 @@ __global__ void k_rb_split(SysView v, DevScalars *sc) {
 // per atom from ~20 to ~130 at 256,000 Cu atoms), and a warp of the pass
 // kernels runs as long as its longest lane.  Here the 27 cells are scanned
 // (IMD's 14 first, then the 13 mirror cells, real cells only); a pair of two
-// real atoms is kept by the atom that the parity rule on their numbers
-// picks (odd sum: the lower number, even sum: the higher), decided alike
-// from both sides; a pair with a ghost is kept as IMD keeps it, from the
-// half-shell side, so the image and the r^2 bits are IMD's.  For two real
-// atoms r^2 is bitwise the same from either side (the difference is negated
-// exactly).
-__device__ __forceinline__ bool owns_pair(int num_i, int num_j) {
-  return ((num_i ^ num_j) & 1) ? (num_i < num_j) : (num_i > num_j);
+// real atoms is kept by the atom that the parity rule on their slots picks
+// (odd sum: the lower slot, even sum: the higher), decided alike from both
+// sides and needing no load (the slots are fixed within one build); a pair
+// with a ghost is kept as IMD keeps it, from the half-shell side, so the
+// image and the r^2 bits are IMD's.  For two real atoms r^2 is bitwise the
+// same from either side (the difference is negated exactly).
+__device__ __forceinline__ bool owns_pair(int slot_i, int slot_j) {
+  return ((slot_i ^ slot_j) & 1) ? (slot_i < slot_j) : (slot_i > slot_j);
 }
 
 __global__ void __launch_bounds__(128) k_rb_build_half(SysView v, DevScalars *sc,
@@ -537,7 +541,6 @@ __global__ void __launch_bounds__(128) k_rb_build_half(SysView v, DevScalars *sc
   const bool bal = v.balanced != 0;
   const bool split = v.split != 0;
   const bool full = (v.nshell == 27) && !bal;
-  const int numi = bal ? v.number[i] : 0;
   int cnt2 = 0;  // split list: partners owned by the other atom, from the back
   const SplitPos *sp = reinterpret_cast<const SplitPos *>(v.xl);
   const SplitPos a = sp[i];
@@ -555,7 +558,7 @@ __global__ void __launch_bounds__(128) k_rb_build_half(SysView v, DevScalars *sc
       if ((full || bal) && j == i) continue;
       // the atom that keeps the pair: parity for two real atoms, IMD's half
       // shell (the first 14 cells) for a ghost
-      const bool owned = !bal || (j < v.n ? owns_pair(numi, v.number[j]) : m < 14);
+      const bool owned = !bal || (j < v.n ? owns_pair(i, j) : m < 14);
       if (!owned && !split) continue;
       const SplitPos b = ldsp(&sp[j]);
       const float dx = (b.hi.x - a.hi.x) + (b.lo.x - a.lo.x);
@@ -1471,6 +1474,7 @@ static ForceTabs ftabs(imdgpu_sys *s) {
   t.bs = s->bs_force;
   t.bs_rho = s->bs_rho;
   t.det = s->deterministic && s->precision == IMDGPU_FP64;
+  t.fused = s->dfused;
   int same = s->have_tab[0] && s->have_tab[1];
   if (same) {
     const HostTable &a = s->htab[0], &b = s->htab[1];
@@ -2122,6 +2126,7 @@ int imdgpu_destroy(imdgpu_sys *s) {
     dfree(s->dcgn[k]);
     dfree(s->dcvf[k]);
     dfree(s->dcgf[k]);
+    if (k == 0) dfree(s->dfused);
   }
   dfree(s->d_cell_rank); dfree(s->d_rank_lin); dfree(s->d_hshell); dfree(s->d_bsrc);
   dfree(s->d_blin); dfree(s->d_bcode); dfree(s->d_cstart); dfree(s->d_ccount);
@@ -2206,6 +2211,34 @@ int imdgpu_set_deterministic(imdgpu_sys *s, int on) {
       s->hsc_valid = false;
     }
   }
+  return IMDGPU_OK;
+}
+
+// Fused rows of the mixed force pass, where one species' pair and density
+// tables are quadratic on the same grid: row k holds (A, B, C, G0) of the
+// pair value and gradient and (G1, density G0, density G1, 0), so one index
+// and one 32-byte load serve the three lookups of a pair.  None otherwise.
+static int build_fused(imdgpu_sys *s) {
+  dfree(s->dfused);
+  s->dfused = nullptr;
+  const int P = IMDGPU_TAB_PAIR, R = IMDGPU_TAB_RHO;
+  if (s->ntypes != 1 || s->interaction != IMDGPU_EAM2 || !s->have_tab[P] || !s->have_tab[R])
+    return IMDGPU_OK;
+  const HostTable &a = s->htab[P], &b = s->htab[R];
+  if (a.mode != 0 || b.mode != 0 || a.maxsteps != b.maxsteps || a.begin[0] != b.begin[0] ||
+      a.end[0] != b.end[0] || a.invstep[0] != b.invstep[0])
+    return IMDGPU_OK;
+  const size_t rows = (size_t)a.maxsteps + 2;
+  if (s->hcvf[P].size() != rows || s->hcgf[P].size() != rows || s->hcgf[R].size() != rows)
+    return IMDGPU_OK;
+  std::vector<float4> f(2 * rows);
+  for (size_t k = 0; k < rows; k++) {
+    const float4 pv = s->hcvf[P][k], pg = s->hcgf[P][k], rg = s->hcgf[R][k];
+    f[2 * k] = make_float4(pv.x, pv.y, pv.z, pg.x);
+    f[2 * k + 1] = make_float4(pg.y, rg.x, rg.y, 0.f);
+  }
+  CK(dalloc(&s->dfused, f.size()));
+  CK(cudaMemcpy(s->dfused, f.data(), f.size() * sizeof(float4), cudaMemcpyHostToDevice));
   return IMDGPU_OK;
 }
 
@@ -2323,10 +2356,12 @@ static int upload_table(imdgpu_sys *s, int which, HostTable &t) {
   }
   s->htab[which] = t;
   s->have_tab[which] = true;
+  s->hcvf[which] = cvf;
+  s->hcgf[which] = cgf;
   if (which != IMDGPU_TAB_EMBED)
     for (int c = 0; c < t.ncols; c++) s->tab_cellsz = std::max(s->tab_cellsz, t.end[c]);
   s->geom_ready = false;
-  return IMDGPU_OK;
+  return build_fused(s);
 }
 
 int imdgpu_set_table(imdgpu_sys *s, int which, int ncols, int maxsteps, const double *begin,

@@ -251,6 +251,35 @@ def test_mixed_precision_force_error(name):
     np.testing.assert_allclose(a["epot"], g["epot"], rtol=0, atol=1e-5 * np.max(np.abs(g["epot"])))
 
 
+def test_mixed_fused_rows_match_per_table_lookups(tmp_path):
+    """One species whose pair and density tables are quadratic on one grid
+    (the Sutton-Chen Cu tables) takes the fused-row force pass; the same
+    physics written as two identical species takes the per-table lookups.
+    Both agree to FP32 rounding, and both are within the mixed bar of FP64."""
+    from imd_gb300 import api
+    from imd_gb300 import workloads as wl
+    st = wl.eam_fcc_system(12, a0=3.615, T=300.0, seed=5)
+    x = st.x + 0.05 * np.random.default_rng(6).standard_normal(st.x.shape)
+    one = wl.sutton_chen_tables(str(tmp_path / "one"), [wl.CU])
+    two = wl.sutton_chen_tables(str(tmp_path / "two"), [wl.CU, wl.CU])
+    res = {}
+    for key, tabs, nt, prec in (("fused", one, 1, api.MIXED), ("split", two, 2, api.MIXED),
+                                ("fp64", one, 1, api.FP64)):
+        s = api.GpuSystem(nt, api.EAM2, prec)
+        s.read_tables(tabs)
+        s.set_box(st.box, (1, 1, 1), 0.4)
+        s.set_atoms(st.number, st.types, st.mass, x, st.p)
+        assert s.calc_forces(0) == 0
+        res[key] = (s.get_atoms()["f"], s.scalars().tot_pot_energy)
+        s.close()
+    f64, e64 = res["fp64"]
+    assert rel_rms(res["fused"][0], res["split"][0]) < 1e-6
+    assert abs(res["fused"][1] - res["split"][1]) <= 1e-7 * abs(e64)
+    for key in ("fused", "split"):
+        assert rel_rms(res[key][0], f64) < 1e-5, key
+        assert abs(res[key][1] - e64) <= 1e-6 * abs(e64), key
+
+
 def test_mixed_nve_conserves_energy():
     from imd_gb300 import api
     g = golden("cu_nve")
