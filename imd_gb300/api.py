@@ -120,6 +120,7 @@ def lib() -> C.CDLL:
         L.imdgpu_format_fixed.argtypes = [_dp, C.c_int, C.c_int, C.c_int, C.c_char_p, C.c_long,
                                           C.POINTER(C.c_long)]
         L.imdgpu_set_graphs.argtypes = [vp, C.c_int]
+        L.imdgpu_set_table_staging.argtypes = [vp, C.c_int]
         L.imdgpu_set_interpolation.argtypes = [vp, C.c_int]
         L.imdgpu_set_table2.argtypes = [vp, C.c_int, C.c_int, C.c_int, _dp]
         L.imdgpu_set_table.argtypes = [vp, C.c_int, C.c_int, C.c_int, _dp, _dp, _dp, _dp,
@@ -285,6 +286,11 @@ class GpuSystem:
     def set_graphs(self, on: bool) -> None:
         """Replay NVE chunks from a captured CUDA graph (default on)."""
         _check(lib().imdgpu_set_graphs(self.h, int(on)), "set_graphs")
+
+    def set_table_staging(self, on: bool) -> None:
+        """Mixed force pass: fused table rows staged in shared memory
+        (default on) or read from global memory."""
+        _check(lib().imdgpu_set_table_staging(self.h, int(on)), "set_table_staging")
 
     def set_exact(self, on: bool) -> None:
         """IMD's unfused table arithmetic (bitwise table values) on/off."""

@@ -30,6 +30,7 @@ constexpr unsigned ST_SHORT = 1u;      // r^2 below a table begin
 constexpr unsigned ST_NBOVER = 2u;     // list entries beyond capacity
 constexpr unsigned ST_GHOSTOVER = 4u;  // ghost atoms beyond capacity
 constexpr unsigned ST_CELLOVER = 8u;   // atoms per cell beyond CELLCAP
+constexpr unsigned ST_WAIT = 16u;      // a bounded wait on an asynchronous copy ran out
 
 // One pot_table_t on the device.  `tri` holds, per column and row k, the
 // three table values the quadratic interpolation reads (rows k, k+1, k+2):

@@ -18,6 +18,8 @@ struct ForceTabs {
   int bs_rho;    // threads per block of the density pass (autotuned)
   int det;       // FP64 passes on the full list without atomics (deterministic)
   const float4 *fused;  // mixed force pass: fused pair/density rows, or null
+  unsigned fused_bytes;
+  int stage_grid;       // >0: the force pass stages them in shared memory, this many blocks
 };
 
 // Device-side scalars of one system (results + control).
@@ -74,6 +76,7 @@ int launch_stress(const SysView &v, const ForceTabs &t, double *stress, cudaStre
 // forces.cu: refresh ghost positions (send_cells(copy_cell))
 void k_ghost_pos_launch(const SysView &v, int blocks, cudaStream_t st);
 // send_forces(add_rho) and send_forces(add_forces): ghost sums into owners
+int mixed_staged_grid(unsigned bytes);
 void fold_rho_launch(const SysView &v, int blocks, cudaStream_t st);
 void fold_force_launch(const SysView &v, int blocks, cudaStream_t st);
 // mixed.cu: the FP32-force path over the full list

@@ -134,9 +134,109 @@ __global__ void k_ghost_dff(SysView v, float *dff) {
     dff[v.n + g] = dff[v.gowner[g]];
 }
 
-// forces over the full row (the half list at the front, the other partners
-// at the back): each directed pair adds d*grad to atom i and half of the
-// pair energy and virial
+// where the fused rows are read from
+enum RowSrc { ROWS_NONE = 0, ROWS_GLOBAL = 1, ROWS_SHARED = 2 };
+
+// forces over the full row of atom i (the half list at the front, the other
+// partners at the back): each directed pair adds d*grad to atom i and half
+// of the pair energy and virial
+template <bool NT1, bool EAM, int SRC>
+__device__ __forceinline__ void force_row_mixed(const SysView &v, const DevTable &pair,
+                                                const DevTable &rho, const float4 *rows,
+                                                const SplitPos *__restrict__ sp,
+                                                const float *__restrict__ dff, int i,
+                                                double (&acc)[2]) {
+  const SplitPos a = sp[i];
+  const int it = NT1 ? 0 : __float_as_int(a.hi.w), nt = v.ntypes;
+  const int n1 = v.nnb[i], n2 = v.nnb2[i];
+  const float dfi = EAM ? dff[i] : 0.f;
+  Acc fx, fy, fz, ee, vir;
+  bool shortf = false;
+  const uint32_t *__restrict__ nb = v.nbr + i;
+  const int nn = n1 + n2, back = v.nbcap - n1 - n2;  // row k >= n1 lives at k + back
+#pragma unroll 4
+  for (int k = 0; k < nn; k++) {
+    const int row = k < n1 ? k : k + back;
+    const int j = (int)(__ldg(nb + (size_t)row * v.ncap) & NB_MASK);
+    const SplitPos b = ldsp(&sp[j]);
+    const float dx = (b.hi.x - a.hi.x) + (b.lo.x - a.lo.x);
+    const float dy = (b.hi.y - a.hi.y) + (b.lo.y - a.lo.y);
+    const float dz = (b.hi.z - a.hi.z) + (b.lo.z - a.lo.z);
+    const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+    const int jt = NT1 ? 0 : __float_as_int(b.hi.w);
+    const int col = NT1 ? 0 : it * nt + jt;
+    float grad = 0.f;
+    bool have = false;
+    if (SRC != ROWS_NONE) {
+      // one species, quadratic pair and density tables on one grid: one
+      // index and one 32-byte row serve the three lookups below (the
+      // cubic coefficients of a quadratic table are zero and left out)
+      const bool inp = r2 <= pair.fend[0], inr = r2 < rho.fend[0];
+      if (inp || inr) {
+        float chi;
+        const int kk = tab_index_f(pair, 0, r2, chi);
+        float4 f0, f1;
+        if (SRC == ROWS_SHARED) {
+          f0 = rows[2 * kk];
+          f1 = rows[2 * kk + 1];
+        } else {
+          f0 = __ldg(&rows[2 * kk]);
+          f1 = __ldg(&rows[2 * kk + 1]);
+        }
+        if (inp) {
+          ee.add(0.5f * fmaf(chi, fmaf(chi, f0.z, f0.y), f0.x));
+          grad = fmaf(chi, f1.x, f0.w);
+          shortf |= r2 < pair.fbegin[0];
+        }
+        if (inr) {
+          const float ris = fmaf(chi, f1.z, f1.y);
+          grad += 0.5f * (dfi * ris + __ldg(&dff[j]) * ris);
+        }
+        have = true;
+      }
+    } else if (r2 <= pair.fend[col]) {
+      float chi;
+      const int kk = tab_index_f(pair, col, r2, chi);
+      ee.add(0.5f * polyf_v(pair, col, kk, chi));
+      grad = polyf_g(pair, col, kk, chi);
+      shortf |= r2 < pair.fbegin[col];
+      have = true;
+    }
+    if (EAM && SRC == ROWS_NONE) {
+      const int col1 = NT1 ? 0 : jt * nt + it, col2 = col;
+      if (r2 < rho.fend[col1] || r2 < rho.fend[col2]) {
+        float chi;
+        const int kk = tab_index_f(rho, col1, r2, chi);
+        const float ris = polyf_g(rho, col1, kk, chi);
+        float rjs = ris;
+        if (!NT1 && col1 != col2) {
+          const int k2 = tab_index_f(rho, col2, r2, chi);
+          rjs = polyf_g(rho, col2, k2, chi);
+        }
+        const float dfj = __ldg(&dff[j]);
+        grad += 0.5f * (dfi * rjs + dfj * ris);
+        have = true;
+      }
+    }
+    if (have) {
+      fx.add(dx * grad);
+      fy.add(dy * grad);
+      fz.add(dz * grad);
+      vir.add(-0.5f * r2 * grad);
+    }
+  }
+  const double e = ee.value();
+  double4 f = v.frc[i];  // .w holds the embedding energy
+  f.x = fx.value();
+  f.y = fy.value();
+  f.z = fz.value();
+  f.w += e;
+  v.frc[i] = f;
+  acc[0] += e;
+  acc[1] += vir.value();
+  if (shortf) flag_short(v, i);
+}
+
 template <bool NT1, bool EAM, bool FUSED>
 __global__ void __launch_bounds__(BS_FORCE_MAX) k_force_mixed(SysView v, DevTable pair,
                                                           DevTable rho, const float4 *fused,
@@ -144,91 +244,91 @@ __global__ void __launch_bounds__(BS_FORCE_MAX) k_force_mixed(SysView v, DevTabl
                                                           const float *dff, double *partial) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   double acc[2] = {0.0, 0.0};
-  if (i < v.n && !atom_idle(v, i)) {
-    const SplitPos a = sp[i];
-    const int it = NT1 ? 0 : __float_as_int(a.hi.w), nt = v.ntypes;
-    const int n1 = v.nnb[i], n2 = v.nnb2[i];
-    const float dfi = EAM ? dff[i] : 0.f;
-    Acc fx, fy, fz, ee, vir;
-    bool shortf = false;
-    const uint32_t *__restrict__ nb = v.nbr + i;
-    const int nn = n1 + n2, back = v.nbcap - n1 - n2;  // row k >= n1 lives at k + back
-#pragma unroll 4
-    for (int k = 0; k < nn; k++) {
-      const int row = k < n1 ? k : k + back;
-      const int j = (int)(__ldg(nb + (size_t)row * v.ncap) & NB_MASK);
-      const SplitPos b = ldsp(&sp[j]);
-      const float dx = (b.hi.x - a.hi.x) + (b.lo.x - a.lo.x);
-      const float dy = (b.hi.y - a.hi.y) + (b.lo.y - a.lo.y);
-      const float dz = (b.hi.z - a.hi.z) + (b.lo.z - a.lo.z);
-      const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-      const int jt = NT1 ? 0 : __float_as_int(b.hi.w);
-      const int col = NT1 ? 0 : it * nt + jt;
-      float grad = 0.f;
-      bool have = false;
-      if (FUSED) {
-        // one species, quadratic pair and density tables on one grid: one
-        // index and one 32-byte row serve the three lookups below (the
-        // cubic coefficients of a quadratic table are zero and left out)
-        const bool inp = r2 <= pair.fend[0], inr = r2 < rho.fend[0];
-        if (inp || inr) {
-          float chi;
-          const int kk = tab_index_f(pair, 0, r2, chi);
-          const float4 f0 = __ldg(&fused[2 * kk]), f1 = __ldg(&fused[2 * kk + 1]);
-          if (inp) {
-            ee.add(0.5f * fmaf(chi, fmaf(chi, f0.z, f0.y), f0.x));
-            grad = fmaf(chi, f1.x, f0.w);
-            shortf |= r2 < pair.fbegin[0];
-          }
-          if (inr) {
-            const float ris = fmaf(chi, f1.z, f1.y);
-            grad += 0.5f * (dfi * ris + __ldg(&dff[j]) * ris);
-          }
-          have = true;
-        }
-      } else if (r2 <= pair.fend[col]) {
-        float chi;
-        const int kk = tab_index_f(pair, col, r2, chi);
-        ee.add(0.5f * polyf_v(pair, col, kk, chi));
-        grad = polyf_g(pair, col, kk, chi);
-        shortf |= r2 < pair.fbegin[col];
-        have = true;
-      }
-      if (EAM && !FUSED) {
-        const int col1 = NT1 ? 0 : jt * nt + it, col2 = col;
-        if (r2 < rho.fend[col1] || r2 < rho.fend[col2]) {
-          float chi;
-          const int kk = tab_index_f(rho, col1, r2, chi);
-          const float ris = polyf_g(rho, col1, kk, chi);
-          float rjs = ris;
-          if (!NT1 && col1 != col2) {
-            const int k2 = tab_index_f(rho, col2, r2, chi);
-            rjs = polyf_g(rho, col2, k2, chi);
-          }
-          const float dfj = __ldg(&dff[j]);
-          grad += 0.5f * (dfi * rjs + dfj * ris);
-          have = true;
-        }
-      }
-      if (have) {
-        fx.add(dx * grad);
-        fy.add(dy * grad);
-        fz.add(dz * grad);
-        vir.add(-0.5f * r2 * grad);
-      }
-    }
-    const double e = ee.value();
-    double4 f = v.frc[i];  // .w holds the embedding energy
-    f.x = fx.value();
-    f.y = fy.value();
-    f.z = fz.value();
-    f.w += e;
-    v.frc[i] = f;
-    acc[0] = e;
-    acc[1] = vir.value();
-    if (shortf) flag_short(v, i);
-  }
+  if (i < v.n && !atom_idle(v, i))
+    force_row_mixed<NT1, EAM, FUSED ? ROWS_GLOBAL : ROWS_NONE>(v, pair, rho, fused, sp, dff, i,
+                                                               acc);
   block_sum_store_dyn<2, BS_FORCE_MAX>(acc, partial);
+}
+
+// ---------------------------------------------------------------------------
+// fused rows staged in shared memory
+//
+// One thread of each block issues bulk asynchronous copies (cp.async.bulk,
+// the TMA's untiled form) of the fused rows into dynamic shared memory; they
+// complete on an mbarrier that every thread waits on.  The blocks are
+// resident for the whole pass (STAGE_BLOCKS per SM) and take atoms
+// blockIdx.x * STAGE_BS + t, then every gridDim.x * STAGE_BS further, so the
+// rows are copied once per block rather than once per 128 atoms.
+constexpr int STAGE_BS = 384;
+constexpr unsigned STAGE_CHUNK = 16384;     // bytes per bulk copy
+constexpr int STAGE_WAIT_LIMIT = 1 << 20;   // try_wait rounds before giving up
+
+__device__ __forceinline__ bool mbar_try_wait(unsigned bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity) {
+  for (int it = 0; it < STAGE_WAIT_LIMIT; it++)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+
+// copies `bytes` (a multiple of 16; src 16-byte aligned) into dst; false in
+// every thread if the copy did not complete (ST_WAIT is then set)
+__device__ bool stage_rows(float4 *dst, const float4 *src, unsigned bytes,
+                           unsigned long long *bar, unsigned *status) {
+  const unsigned b = (unsigned)__cvta_generic_to_shared(bar);
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(b) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(b), "r"(bytes)
+                 : "memory");
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    unsigned long long g;
+    asm("cvta.to.global.u64 %0, %1;" : "=l"(g) : "l"(src));
+    for (unsigned o = 0; o < bytes; o += STAGE_CHUNK) {
+      const unsigned sz = min(STAGE_CHUNK, bytes - o);
+      asm volatile(
+          "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, "
+          "[%3];" ::"r"(d + o),
+          "l"(g + o), "r"(sz), "r"(b)
+          : "memory");
+    }
+  }
+  bool ok = mbar_wait(b, 0);
+  if (!ok) {
+    atomicOr(status, ST_WAIT);
+    mbar_wait(b, 0);  // the copies may still land: give them a second bound
+  }
+  return __syncthreads_and(ok) != 0;
+}
+
+__global__ void __launch_bounds__(STAGE_BS) k_force_mixed_staged(SysView v, DevTable pair,
+                                                                DevTable rho,
+                                                                const float4 *fused,
+                                                                unsigned fused_bytes,
+                                                                const SplitPos *sp,
+                                                                const float *dff,
+                                                                double *partial) {
+  extern __shared__ __align__(16) float4 srows[];
+  __shared__ __align__(8) unsigned long long bar;
+  double acc[2] = {0.0, 0.0};
+  if (stage_rows(srows, fused, fused_bytes, &bar, v.status))
+    for (int i = blockIdx.x * STAGE_BS + threadIdx.x; i < v.n; i += gridDim.x * STAGE_BS)
+      if (!atom_idle(v, i))
+        force_row_mixed<true, true, ROWS_SHARED>(v, pair, rho, srows, sp, dff, i, acc);
+  block_sum_store_dyn<2, STAGE_BS>(acc, partial);
 }
 
 __global__ void k_finalize_mixed(const double *pe, int ne, const double *pf, int nf,
@@ -250,13 +350,47 @@ __global__ void k_finalize_mixed(const double *pe, int ne, const double *pf, int
 
 static inline int nblk(long n, int bs) { return (int)((n + bs - 1) / bs); }
 
+// resident blocks of the staged force pass for `bytes` of fused rows on the
+// current device; 0 where fewer than two blocks fit on an SM
+int mixed_staged_grid(unsigned bytes) {
+  int d = 0, nsm = 0, optin = 0, per_sm = 0;
+  if (cudaGetDevice(&d) != cudaSuccess) return 0;
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, d);
+  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, d);
+  if (bytes == 0 || bytes % 16 || (long)bytes + 64 > optin) return 0;
+  // the attribute only grows, so the rows of every live system still fit
+  cudaFuncAttributes fa;
+  if (cudaFuncGetAttributes(&fa, k_force_mixed_staged) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  if (cudaFuncSetAttribute(k_force_mixed_staged, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           std::max((int)bytes, fa.maxDynamicSharedSizeBytes)) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_force_mixed_staged, STAGE_BS,
+                                                    bytes) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return per_sm >= 2 ? nsm * per_sm : 0;
+}
+
+int mixed_force_blocks(const ForceTabs &t, int n) {
+  if (t.fused && t.stage_grid > 0 && t.nt1 && t.eam)
+    return std::min(t.stage_grid, std::max(1, nblk(n, STAGE_BS)));
+  return nblk(n, t.bs);
+}
+
 template <bool NT1, bool EAM>
 static void launch_force_mixed2(const ForceTabs &t, int nbf, cudaStream_t st, const SysView &v,
                                 const SplitPos *sp, const float *dff, double *pf) {
   if constexpr (NT1 && EAM) {
     if (t.fused) {
-      k_force_mixed<true, true, true><<<nbf, t.bs, 0, st>>>(v, t.pair, t.rho, t.fused, sp, dff,
-                                                             pf);
+      if (t.stage_grid > 0)
+        k_force_mixed_staged<<<nbf, STAGE_BS, t.fused_bytes, st>>>(
+            v, t.pair, t.rho, t.fused, t.fused_bytes, sp, dff, pf);
+      else
+        k_force_mixed<true, true, true><<<nbf, t.bs, 0, st>>>(v, t.pair, t.rho, t.fused, sp,
+                                                               dff, pf);
       return;
     }
   }
@@ -271,7 +405,7 @@ int launch_forces_mixed(const SysView &v, const ForceTabs &t, DevScalars *sc, fl
   cudaMemsetAsync(v.frc, 0, ext * sizeof(double4), st);
   k_ghost_pos_launch(v, gblocks, st);
   k_split<<<nblk(ext, BS_VEC), BS_VEC, 0, st>>>(v, sp);
-  const int nbf = nblk(v.n, t.bs), nbe = nblk(v.n, BS_VEC), nbr = nblk(v.n, t.bs_rho);
+  const int nbf = mixed_force_blocks(t, v.n), nbe = nblk(v.n, BS_VEC), nbr = nblk(v.n, t.bs_rho);
   double *pe = v.partial, *pf = v.partial + nbe;
   int launches = 4;
   if (t.eam) {

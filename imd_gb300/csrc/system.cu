@@ -25,6 +25,9 @@ using namespace imdgpu;
 // ---------------------------------------------------------------------------
 static thread_local std::string g_err;
 
+static const char kWaitMsg[] =
+    "a kernel's bounded wait for its shared-memory copy ran out; the results are not valid";
+
 static int fail(int code, const std::string &msg) {
   g_err = msg;
   return code;
@@ -91,6 +94,9 @@ struct imdgpu_sys {
   // (pair value and gradient, density gradient of one row in 32 bytes)
   std::vector<float4> hcvf[3], hcgf[3];
   float4 *dfused = nullptr;
+  unsigned fused_bytes = 0;
+  int fused_grid = 0;    // resident blocks of the staged force pass (0: not stageable)
+  int stage_rows = 1;    // imdgpu_set_table_staging
   int exact = 0;
   int interp = 0;  // table interpolation of tables read from now on
   std::vector<double> pending_table2[3];
@@ -1475,6 +1481,8 @@ static ForceTabs ftabs(imdgpu_sys *s) {
   t.bs_rho = s->bs_rho;
   t.det = s->deterministic && s->precision == IMDGPU_FP64;
   t.fused = s->dfused;
+  t.fused_bytes = s->fused_bytes;
+  t.stage_grid = s->stage_rows ? s->fused_grid : 0;
   int same = s->have_tab[0] && s->have_tab[1];
   if (same) {
     const HostTable &a = s->htab[0], &b = s->htab[1];
@@ -2010,6 +2018,7 @@ static int calc_forces_sync(imdgpu_sys *s) {
   if ((rc = read_back(s))) return rc;
   if (s->status_host & ST_CELLOVER)
     return fail(IMDGPU_ERR_CELL, "more than " + std::to_string(CELLCAP) + " atoms in one cell");
+  if (s->status_host & ST_WAIT) return fail(IMDGPU_ERR_CUDA, kWaitMsg);
   if (s->status_host & (ST_NBOVER | ST_GHOSTOVER)) {
     if ((rc = rebuild_sync(s))) return rc;
     launch_forces(view(s), ftabs(s), s->dsc, s->precision == IMDGPU_MIXED, s->st);
@@ -2221,6 +2230,8 @@ int imdgpu_set_deterministic(imdgpu_sys *s, int on) {
 static int build_fused(imdgpu_sys *s) {
   dfree(s->dfused);
   s->dfused = nullptr;
+  s->fused_bytes = 0;
+  s->fused_grid = 0;
   const int P = IMDGPU_TAB_PAIR, R = IMDGPU_TAB_RHO;
   if (s->ntypes != 1 || s->interaction != IMDGPU_EAM2 || !s->have_tab[P] || !s->have_tab[R])
     return IMDGPU_OK;
@@ -2239,6 +2250,8 @@ static int build_fused(imdgpu_sys *s) {
   }
   CK(dalloc(&s->dfused, f.size()));
   CK(cudaMemcpy(s->dfused, f.data(), f.size() * sizeof(float4), cudaMemcpyHostToDevice));
+  s->fused_bytes = (unsigned)(f.size() * sizeof(float4));
+  s->fused_grid = mixed_staged_grid(s->fused_bytes);
   return IMDGPU_OK;
 }
 
@@ -3245,6 +3258,12 @@ static int run_chunk_graph(imdgpu_sys *s, int k, double dt, int *istep, long &la
   return IMDGPU_OK;
 }
 
+int imdgpu_set_table_staging(imdgpu_sys *s, int on) {
+  if (!s) return fail(IMDGPU_ERR_ARG, "null");
+  s->stage_rows = on ? 1 : 0;
+  return IMDGPU_OK;
+}
+
 int imdgpu_set_graphs(imdgpu_sys *s, int on) {
   if (!s) return fail(IMDGPU_ERR_ARG, "null");
   s->use_graph = on ? 1 : 0;
@@ -3312,6 +3331,10 @@ int imdgpu_nve_run(imdgpu_sys *s, int nsteps, double dt, double *epot, double *e
     CK(cudaStreamSynchronize(s->st));
     if (s->status_host & ST_CELLOVER) {
       rc = fail(IMDGPU_ERR_CELL, "more than " + std::to_string(CELLCAP) + " atoms in one cell");
+      break;
+    }
+    if (s->status_host & ST_WAIT) {
+      rc = fail(IMDGPU_ERR_CUDA, kWaitMsg);
       break;
     }
     if (s->status_host & (ST_NBOVER | ST_GHOSTOVER)) {
@@ -4127,6 +4150,10 @@ int imdgpu_batch_advance(imdgpu_sys *s, int max_rounds, int *ndone_out, int *rou
     CKR(cudaStreamSynchronize(s->st));
     if (s->status_host & ST_CELLOVER) {
       rc = fail(IMDGPU_ERR_CELL, "more than " + std::to_string(CELLCAP) + " atoms in one cell");
+      break;
+    }
+    if (s->status_host & ST_WAIT) {
+      rc = fail(IMDGPU_ERR_CUDA, kWaitMsg);
       break;
     }
     if (s->status_host & (ST_NBOVER | ST_GHOSTOVER)) {

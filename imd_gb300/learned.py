@@ -165,33 +165,59 @@ def targets(cells, relaxed_positions) -> list:
     return [min_image(xr - c.x, np.asarray(c.box)) for c, xr in zip(cells, relaxed_positions)]
 
 
+# above this many training atoms the groups are not kept on the device
+RESIDENT_ATOMS = 24_000_000
+
+
 class Trainer:
-    """Adam training of the per-pair MLP on resident groups of cells."""
+    """Adam training of the per-pair MLP on groups of cells."""
 
     def __init__(self, tables, cells, disp, batch_cells: int = 64, seed: int = 0,
                  weights=None, interpolation: int = BATCH_INTERPOLATION,
-                 core_weight: float = 0.0, core_disp: float = 0.2):
+                 core_weight: float = 0.0, core_disp: float = 0.2, resident=None):
         """core_weight > 0 weights the loss of every atom whose target
         displacement is at least core_disp (A) by 1 + core_weight: the few
         defect-core atoms that set the CG cost count as much as the many
-        atoms of the elastic field."""
+        atoms of the elastic field.  resident: keep every group's batch on
+        the device (default: when the cells hold at most RESIDENT_ATOMS);
+        otherwise each step uploads its group and frees it afterwards."""
+        self.tables, self.interpolation = tables, interpolation
+        self.core_weight, self.core_disp = core_weight, core_disp
+        if resident is None:
+            resident = sum(c.n for c in cells) <= RESIDENT_ATOMS
+        self.resident = resident
         self.groups = []
-        order = np.arange(len(cells))
         for g0 in range(0, len(cells), batch_cells):
-            idx = order[g0:g0 + batch_cells]
-            gc = [cells[i] for i in idx]
-            b = make_batch(tables, gc, interpolation=interpolation)
-            t = np.ascontiguousarray(np.concatenate([disp[i] for i in idx]), np.float64)
-            if core_weight > 0.0:
-                core = np.sqrt(np.sum(t * t, axis=1)) >= core_disp
-                b.ml_set_loss_weights(1.0 + core_weight * core)
-            self.groups.append((b, t))
+            gc = cells[g0:g0 + batch_cells]
+            t = np.ascontiguousarray(np.concatenate(disp[g0:g0 + batch_cells]), np.float64)
+            self.groups.append((self._batch(gc, t) if resident else gc, t))
         self.w = init_weights(seed) if weights is None else np.asarray(weights, np.float32)
         self.m = np.zeros(NPARAM, np.float32)
         self.v = np.zeros(NPARAM, np.float32)
         self.step = 0
         self.rng = np.random.default_rng(seed + 1)
         self.history = []
+
+    def _batch(self, gc, t):
+        b = make_batch(self.tables, gc, interpolation=self.interpolation)
+        if self.core_weight > 0.0:
+            core = np.sqrt(np.sum(t * t, axis=1)) >= self.core_disp
+            b.ml_set_loss_weights(1.0 + self.core_weight * core)
+        return b
+
+    def _step(self, gi, lr):
+        """One Adam step (lr 0: the loss alone) on group gi."""
+        g, t = self.groups[gi]
+        b = g if self.resident else self._batch(g, t)
+        try:
+            self._load(b)
+            loss = b.ml_train_step(t, lr)
+            if lr > 0.0:
+                self._store(b)
+        finally:
+            if not self.resident:
+                b.close()
+        return loss
 
     def _load(self, b):
         b.ml_set_weights(self.w)
@@ -204,32 +230,17 @@ class Trainer:
     def epoch(self, lr: float = 1e-3) -> float:
         """One pass over the groups in random order; mean loss before each
         group's step."""
-        losses = []
-        if len(self.groups) == 1:
-            b, t = self.groups[0]
-            if self.step == 0:
-                self._load(b)
-            losses.append(b.ml_train_step(t, lr))
-            self._store(b)
-        else:
-            for gi in self.rng.permutation(len(self.groups)):
-                b, t = self.groups[gi]
-                self._load(b)
-                losses.append(b.ml_train_step(t, lr))
-                self._store(b)
+        losses = [self._step(gi, lr) for gi in self.rng.permutation(len(self.groups))]
         m = float(np.mean(losses))
         self.history.append(m)
         return m
 
     def loss(self) -> float:
         """Mean loss over all groups at the current weights (no update)."""
-        out = []
-        for b, t in self.groups:
-            b.ml_set_weights(self.w)
-            out.append(b.ml_train_step(t, 0.0))
-        return float(np.mean(out))
+        return float(np.mean([self._step(gi, 0.0) for gi in range(len(self.groups))]))
 
     def close(self):
-        for b, _ in self.groups:
-            b.close()
+        if self.resident:
+            for b, _ in self.groups:
+                b.close()
         self.groups = []

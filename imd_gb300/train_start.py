@@ -2,7 +2,7 @@
 
     python -m imd_gb300.train_start [--train-cells 2048] [--epochs 20]
         [--batch-cells 64] [--lr 1e-3] [--out imd_gb300/data/start_mlp.npz]
-        [--eval-cells 512]
+        [--eval-cells 512] [--relax-chunk 512] [--start-iters 1]
 
 Training cells come from the batched-relaxation generator with seed 5, held-out
 cells with seed 6 (single-species Sutton-Chen Cu, 1-4 vacancies or <100>
@@ -94,6 +94,8 @@ def main(argv=None):
     ap.add_argument("--core-weight", type=float, default=0.0,
                     help="extra loss weight of atoms displaced by >= --core-disp A")
     ap.add_argument("--core-disp", type=float, default=0.2)
+    ap.add_argument("--relax-chunk", type=int, default=512,
+                    help="training cells relaxed per batch when making the targets")
     ap.add_argument("--start-iters", type=int, default=1,
                     help="also evaluate the learned start applied this many times")
     a = ap.parse_args(argv)
@@ -101,7 +103,7 @@ def main(argv=None):
     tabs = wl.sutton_chen_tables(os.path.join(tmp, "cu"), [wl.CU])
     t0 = time.perf_counter()
     train = wl.defect_batch(a.train_cells, seed=5)
-    disp, relax_stats = relax_targets(tabs, train)
+    disp, relax_stats = relax_targets(tabs, train, a.relax_chunk)
     train = [c for c, d in zip(train, disp) if d is not None]
     disp = [d for d in disp if d is not None]
     t_data = time.perf_counter() - t0

@@ -418,6 +418,13 @@ int imdgpu_set_l2_flush(imdgpu_sys *sys, long bytes);
 /* nve_run replays each full chunk of 25 steps from a captured CUDA graph
  * (default 1); 0 issues every launch from the host. */
 int imdgpu_set_graphs(imdgpu_sys *sys, int on);
+/* Mixed precision, one species, pair and density tables quadratic on one
+ * grid: the force pass reads fused rows (pair value and gradient, density
+ * gradient; 32 bytes a row) and, with staging on (default 1) and rows that
+ * fit two blocks per SM, copies them into shared memory once per resident
+ * block (bulk asynchronous copies completing on an mbarrier).  0 reads them
+ * from global memory; the forces are the same bits either way. */
+int imdgpu_set_table_staging(imdgpu_sys *sys, int on);
 /* Measured FP64 FMA throughput of this device (TFLOP/s): a roofline
  * denominator for the FP64 force kernels. */
 int imdgpu_probe_fp64_peak(double *tflops);

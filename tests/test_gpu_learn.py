@@ -58,6 +58,29 @@ def test_training_reduces_loss():
     assert l1 < 0.5 * l0, (l0, l1)
 
 
+def test_streamed_groups_train_like_resident_ones():
+    """Above a size limit the trainer uploads each group for its step and
+    frees it afterwards; the loss history and weights follow the resident
+    trainer's (the backward pass sums with float atomics, so to rounding)."""
+    from imd_gb300 import learned
+    cells = _small_cells(21, 6)
+    disp = [0.01 * np.random.default_rng(k).standard_normal((c.n, 3)) for k, c in
+            enumerate(cells)]
+    out = []
+    for resident in (True, False):
+        tr = learned.Trainer(tables("cu"), cells, disp, batch_cells=2, seed=4, resident=resident)
+        assert tr.resident == resident
+        for _ in range(3):
+            tr.epoch(1e-3)
+        out.append((np.array(tr.history), tr.w.copy(), tr.step, tr.loss()))
+        tr.close()
+    (h0, w0, s0, l0), (h1, w1, s1, l1) = out
+    assert s0 == s1 == 9
+    np.testing.assert_allclose(h1, h0, rtol=1e-4)
+    np.testing.assert_allclose(w1, w0, rtol=1e-3, atol=1e-5)
+    assert abs(l1 - l0) <= 1e-4 * abs(l0)
+
+
 def _small_cells(seed, k, nmin=300, nmax=900):
     from imd_gb300 import workloads as wl
     rng = np.random.default_rng(seed)

@@ -253,9 +253,11 @@ def test_mixed_precision_force_error(name):
 
 def test_mixed_fused_rows_match_per_table_lookups(tmp_path):
     """One species whose pair and density tables are quadratic on one grid
-    (the Sutton-Chen Cu tables) takes the fused-row force pass; the same
-    physics written as two identical species takes the per-table lookups.
-    Both agree to FP32 rounding, and both are within the mixed bar of FP64."""
+    (the Sutton-Chen Cu tables) takes the fused-row force pass, with the rows
+    staged in shared memory or read from global memory (the same bits); the
+    same physics written as two identical species takes the per-table
+    lookups.  All agree to FP32 rounding and are within the mixed bar of
+    FP64."""
     from imd_gb300 import api
     from imd_gb300 import workloads as wl
     st = wl.eam_fcc_system(12, a0=3.615, T=300.0, seed=5)
@@ -263,9 +265,10 @@ def test_mixed_fused_rows_match_per_table_lookups(tmp_path):
     one = wl.sutton_chen_tables(str(tmp_path / "one"), [wl.CU])
     two = wl.sutton_chen_tables(str(tmp_path / "two"), [wl.CU, wl.CU])
     res = {}
-    for key, tabs, nt, prec in (("fused", one, 1, api.MIXED), ("split", two, 2, api.MIXED),
-                                ("fp64", one, 1, api.FP64)):
+    for key, tabs, nt, prec in (("fused", one, 1, api.MIXED), ("global", one, 1, api.MIXED),
+                                ("split", two, 2, api.MIXED), ("fp64", one, 1, api.FP64)):
         s = api.GpuSystem(nt, api.EAM2, prec)
+        s.set_table_staging(key != "global")
         s.read_tables(tabs)
         s.set_box(st.box, (1, 1, 1), 0.4)
         s.set_atoms(st.number, st.types, st.mass, x, st.p)
@@ -273,6 +276,8 @@ def test_mixed_fused_rows_match_per_table_lookups(tmp_path):
         res[key] = (s.get_atoms()["f"], s.scalars().tot_pot_energy)
         s.close()
     f64, e64 = res["fp64"]
+    np.testing.assert_array_equal(res["fused"][0], res["global"][0])
+    assert abs(res["fused"][1] - res["global"][1]) <= 1e-12 * abs(e64)
     assert rel_rms(res["fused"][0], res["split"][0]) < 1e-6
     assert abs(res["fused"][1] - res["split"][1]) <= 1e-7 * abs(e64)
     for key in ("fused", "split"):
