@@ -240,6 +240,27 @@ def cg_cpu_sample(tabs, cells, count: int):
     return len(res) / wall, per_core, cores, res
 
 
+def batch_force_rate(tabs, cells, reps: int = 5) -> dict:
+    """One force call of every atom of the batch at once (every cell
+    unfinished, the list current): device time per atom, the rate the
+    relaxation's rounds are compared with."""
+    from imd_gb300 import learned
+    b = learned.make_batch(tabs, cells)
+    b.calc_forces(0)
+    b.calc_forces(0)
+    t = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        b.calc_forces(0)  # synchronous: results read back
+        t.append(time.perf_counter() - t0)
+    b.close()
+    n = sum(c.n for c in cells)
+    best = min(t)
+    return {"atoms": n, "ms": 1e3 * best, "ns_per_atom": 1e9 * best / n,
+            "how": "calc_forces of the whole batch, best of %d, wall clock around the "
+                   "synchronous call" % reps}
+
+
 def run_batch(args, tabs, rank=0, world=1, dist=None):
     """Defect CG relaxations/s, plain and from the learned start: the held-out
     cells of the learned-start workload (seed 6), each relaxed by IMD's CG
@@ -259,14 +280,20 @@ def run_batch(args, tabs, rank=0, world=1, dist=None):
                        "<= 1e-4 eV/A, FP64, spline tables" % (len(cells), natoms.sum(),
                                                               natoms.min(), natoms.max()),
            "unit": "relaxations/s", "sharding": "%d ranks, cells split by atom count" % world}
+    cells4 = wl.defect_batch(args.batch_cells, seed=4)
+    natoms4 = np.array([c.n for c in cells4])
+    mine4 = shard.shard_cells(natoms4, world)[rank]
     res = {}
-    for name, weights in (("plain", None), ("learned", w)):
+    runs = [("plain", cells, mine, None), ("learned", cells, mine, w)]
+    if not args.no_seed4:
+        runs.append(("seed4", cells4, mine4, None))
+    for name, cs, mi, weights in runs:
         if dist:
             dist.barrier()
-        r = learned.relax(tabs, [cells[i] for i in mine], weights=weights, trace=True)
+        r = learned.relax(tabs, [cs[i] for i in mi], weights=weights, trace=True)
         sec = shard.max_over_ranks(r.seconds, dist)
         g = shard.gather_cell_results({"epot": r.epot, "status": r.status, "nfc": r.nfc},
-                                      mine, len(cells), dist)
+                                      mi, len(cs), dist)
         res[name] = (sec, g, r)
     if rank != 0:
         return None
@@ -278,9 +305,19 @@ def run_batch(args, tabs, rank=0, world=1, dist=None):
                      "force_calls_per_relaxation": float(g["nfc"].mean()),
                      "rounds_rank0": r.rounds,
                      "status_counts": np.bincount(g["status"], minlength=5).tolist(),
-                     "tail_rank0": r.tail_histogram(len(mine))}
+                     "tail_rank0": r.tail_histogram(len(mine), int(natoms[mine].sum()))}
         if name == "learned":
             out[name]["start_used_rank0"] = int(r.used.sum())
+    out["full_batch_force_call"] = batch_force_rate(tabs, [cells[i] for i in mine])
+    if "seed4" in res:
+        sec, g, r = res["seed4"]
+        out["plain_seed4"] = {
+            "workload": "the batching workload's own cells: seed 4, %d cells, %d atoms, "
+                        "spline tables" % (len(cells4), natoms4.sum()),
+            "value": len(cells4) / sec, "seconds": sec,
+            "converged": int((g["status"] == 0).sum()),
+            "force_calls_per_relaxation": float(g["nfc"].mean()), "rounds_rank0": r.rounds,
+            "status_counts": np.bincount(g["status"], minlength=5).tolist()}
     gp, gl = res["plain"][1], res["learned"][1]
     both = (gp["status"] == 0) & (gl["status"] == 0)
     de = np.abs(gl["epot"] - gp["epot"])[both] / natoms[both]
@@ -566,6 +603,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--batch-cells", type=int, default=512)
+    ap.add_argument("--no-seed4", action="store_true",
+                    help="skip the plain relaxation of the seed-4 batching cells")
     args = ap.parse_args()
     rank, world, local = dist_env()
     if args.impl == "reference":

@@ -159,6 +159,7 @@ def lib() -> C.CDLL:
         L.imdgpu_batch_begin.argtypes = [vp, C.c_double, C.c_int]
         L.imdgpu_batch_advance.argtypes = [vp, C.c_int, _ip, _ip]
         L.imdgpu_batch_rebuilds.argtypes = [vp, C.POINTER(C.c_long)]
+        L.imdgpu_batch_progress.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(C.c_long)]
         L.imdgpu_batch_set_compaction.argtypes = [vp, C.c_int]
         L.imdgpu_autotune.argtypes = [vp, _ip, _ip]
         L.imdgpu_calc_stress.argtypes = [vp, _dp, _dp]
@@ -662,6 +663,13 @@ class GpuBatch(GpuSystem):
         n = C.c_long(0)
         _check(lib().imdgpu_batch_rebuilds(self.h, C.byref(n)), "batch_rebuilds")
         return n.value
+
+    def progress(self):
+        """(cells finished, atoms of the unfinished cells)."""
+        nd = C.c_int(0)
+        a = C.c_long(0)
+        _check(lib().imdgpu_batch_progress(self.h, C.byref(nd), C.byref(a)), "batch_progress")
+        return nd.value, a.value
 
     def results(self):
         k = self.ncells

@@ -4224,6 +4224,21 @@ int imdgpu_batch_rebuilds(imdgpu_sys *s, long *n) {
   return IMDGPU_OK;
 }
 
+int imdgpu_batch_progress(imdgpu_sys *s, int *ndone, long *active_atoms) {
+  if (!s || !s->brun) return fail(IMDGPU_ERR_STATE, "imdgpu_batch_begin first");
+  std::vector<int> dn(s->nsys);
+  CK(cudaMemcpy(dn.data(), s->d_sys_done, sizeof(int) * s->nsys, cudaMemcpyDeviceToHost));
+  long active = 0;
+  int nd = s->brun->ndone_base;
+  for (int c = 0; c < s->nsys; c++) {
+    if (dn[c]) nd++;
+    else active += s->h_aoff[c + 1] - s->h_aoff[c];
+  }
+  if (ndone) *ndone = nd;
+  if (active_atoms) *active_atoms = active;
+  return IMDGPU_OK;
+}
+
 // per-cell results: energy, max |F|, CG steps, force calls, status
 // (0 converged, 1 not converged within maxsteps or the rounds, 2 brent
 // failed, 3 control, 4 short distance)

@@ -88,29 +88,36 @@ class RelaxResult:
     e_start: np.ndarray | None = None
     e_pred: np.ndarray | None = None
     positions: list = field(default_factory=list)
-    # (seconds since the start, rounds so far, cells finished) after every
-    # advance call, when relax() was asked to trace
+    # (seconds since the start, rounds so far, cells finished, atoms of the
+    # unfinished cells) after every advance call, when relax() was asked to
+    # trace
     trace: list = field(default_factory=list)
 
     @property
     def relaxations_per_s(self) -> float:
         return len(self.epot) / self.seconds
 
-    def tail_histogram(self, ncells: int, bounds=(8, 32)) -> dict:
-        """Wall time and rounds spent while at most 8, 9-32 and more than 32
-        cells were unfinished (each traced interval counted at the number
-        unfinished when it began)."""
+    def tail_histogram(self, ncells: int, natoms: int, bounds=(8, 32)) -> dict:
+        """Wall time, rounds and atom-rounds (one force call of one atom)
+        spent while at most 8, 9-32 and more than 32 cells were unfinished;
+        each traced interval counts at the cells unfinished when it began and
+        at the mean of the unfinished atoms at its two ends."""
         edges = sorted(bounds)
         names = ["unfinished<=%d" % edges[0]] + \
                 ["%d<unfinished<=%d" % (a, b) for a, b in zip(edges, edges[1:])] + \
                 ["unfinished>%d" % edges[-1]]
-        out = {k: {"seconds": 0.0, "rounds": 0} for k in names}
-        t0, r0, left = 0.0, 0, ncells
-        for t, r, done in self.trace:
+        out = {k: {"seconds": 0.0, "rounds": 0, "atom_rounds": 0.0} for k in names}
+        t0, r0, left, a0 = 0.0, 0, ncells, natoms
+        for t, r, done, active in self.trace:
             k = sum(left > e for e in edges)
             out[names[k]]["seconds"] += t - t0
             out[names[k]]["rounds"] += r - r0
-            t0, r0, left = t, r, ncells - done
+            out[names[k]]["atom_rounds"] += 0.5 * (a0 + active) * (r - r0)
+            t0, r0, left, a0 = t, r, ncells - done, active
+        for v in out.values():
+            v["ms_per_round"] = 1e3 * v["seconds"] / v["rounds"] if v["rounds"] else None
+            v["ns_per_atom_round"] = 1e9 * v["seconds"] / v["atom_rounds"] \
+                if v["atom_rounds"] else None
         return out
 
 
@@ -146,7 +153,7 @@ def relax(tables, cells, fmax: float = 1e-4, weights=None, precision=api.FP64,
     while True:
         nd, rounds = b.advance(chunk_rounds)
         if trace:
-            tr.append((time.perf_counter() - t0, rounds, nd))
+            tr.append((time.perf_counter() - t0, rounds, nd, b.progress()[1]))
         if nd >= len(cells):
             break
         if rounds > 10_000_000:

@@ -312,6 +312,9 @@ int imdgpu_batch_set_compaction(imdgpu_sys *sys, int pct);
 int imdgpu_batch_positions(imdgpu_sys *sys, double *x);
 /* neighbour-list rebuilds since imdgpu_batch_begin */
 int imdgpu_batch_rebuilds(imdgpu_sys *sys, long *n);
+/* cells finished since imdgpu_batch_begin and the atoms of the unfinished
+ * ones (either pointer may be NULL) */
+int imdgpu_batch_progress(imdgpu_sys *sys, int *ndone, long *active_atoms);
 /* per cell: final energy, max |F|, CG steps, force calls (nfc), status
  * (0 converged, 1 not converged within maxsteps or the rounds, 2 "Too many
  * iterations in brent", 3 line-search control failure, 4 five line
