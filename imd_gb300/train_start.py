@@ -91,8 +91,10 @@ def main(argv=None):
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--eval-cells", type=int, default=512)
     ap.add_argument("--out", default=DEFAULT_OUT)
-    ap.add_argument("--core-weight", type=float, default=0.0,
-                    help="extra loss weight of atoms displaced by >= --core-disp A")
+    ap.add_argument("--core-weight", default="0",
+                    help="extra loss weight of atoms displaced by >= --core-disp A; a comma "
+                         "list trains one model per weight on the same targets, each written "
+                         "to --out with _cw<weight> before the extension")
     ap.add_argument("--core-disp", type=float, default=0.2)
     ap.add_argument("--relax-chunk", type=int, default=512,
                     help="training cells relaxed per batch when making the targets")
@@ -107,16 +109,31 @@ def main(argv=None):
     train = [c for c, d in zip(train, disp) if d is not None]
     disp = [d for d in disp if d is not None]
     t_data = time.perf_counter() - t0
+    weights = [float(v) for v in str(a.core_weight).split(",")]
+    held = plain = None
+    if a.eval_cells > 0:
+        held = wl.defect_batch(a.eval_cells, seed=6)
+        plain = learned.relax(tabs, held)
+    for cw in weights:
+        out = a.out
+        if len(weights) > 1:
+            root, ext = os.path.splitext(a.out)
+            out = "%s_cw%g%s" % (root, cw, ext)
+        train_one(a, tabs, train, disp, cw, t_data, relax_stats, held, plain, out)
+
+
+def train_one(a, tabs, train, disp, core_weight, t_data, relax_stats, held, plain, out):
     t1 = time.perf_counter()
     tr = learned.Trainer(tabs, train, disp, batch_cells=a.batch_cells, seed=a.seed,
-                         core_weight=a.core_weight, core_disp=a.core_disp)
+                         core_weight=core_weight, core_disp=a.core_disp)
     loss0 = tr.loss()
     for ep in range(a.epochs):
         m = tr.epoch(a.lr)
-        print("epoch %d: mean loss %.6e" % (ep + 1, m), flush=True)
+        print("core weight %g, epoch %d: mean loss %.6e" % (core_weight, ep + 1, m), flush=True)
     loss1 = tr.loss()
     w = tr.w.copy()
     steps = tr.step
+    resident = tr.resident
     tr.close()
     t_train = time.perf_counter() - t1
     # the same loss with zero displacement: mean |target|^2 per atom
@@ -124,22 +141,22 @@ def main(argv=None):
     rec = {"train_cells": a.train_cells, "train_cells_relaxed": len(train),
            "train_atoms": int(sum(c.n for c in train)),
            "epochs": a.epochs, "batch_cells": a.batch_cells, "lr": a.lr, "adam_steps": steps,
-           "core_weight": a.core_weight, "core_disp": a.core_disp,
-           "loss_weighted": a.core_weight > 0.0,
+           "groups_resident": resident,
+           "core_weight": core_weight, "core_disp": a.core_disp,
+           "loss_weighted": core_weight > 0.0,
            "loss_initial": loss0, "loss_final": loss1, "loss_zero_prediction": zero,
            "loss_history": tr.history, "seconds_data": t_data, "seconds_train": t_train,
            "relax_batches": relax_stats}
-    if a.eval_cells > 0:
-        held = wl.defect_batch(a.eval_cells, seed=6)
-        plain = learned.relax(tabs, held)
+    if held is not None:
         rec["eval"] = evaluate(tabs, held, w, plain=plain)
         print(json.dumps(rec["eval"]), flush=True)
         if a.start_iters > 1:
             rec["eval_iterated"] = evaluate(tabs, held, w, start_iters=a.start_iters, plain=plain)
             print(json.dumps(rec["eval_iterated"]), flush=True)
-    os.makedirs(os.path.dirname(os.path.abspath(a.out)), exist_ok=True)
-    np.savez(a.out, w=w, record=json.dumps(rec))
-    print("wrote %s (loss %.3e -> %.3e; zero prediction %.3e)" % (a.out, loss0, loss1, zero))
+    os.makedirs(os.path.dirname(os.path.abspath(out)), exist_ok=True)
+    np.savez(out, w=w, record=json.dumps(rec))
+    print("wrote %s (loss %.3e -> %.3e; zero prediction %.3e)" % (out, loss0, loss1, zero),
+          flush=True)
 
 
 if __name__ == "__main__":
