@@ -53,13 +53,13 @@ DT_FS = 1.0
 SKIN = 0.4
 WORKLOAD = "sutton-chen Cu EAM2 NVE, fcc 40^3 = 256000 atoms, 300 K, dt 1 fs, skin 0.4 A"
 FORCE_BYTES_PER_ATOM = 56.0       # force kernel: read x (24) + 2F' (8), write F (24)
-# mixed force kernel, per full-list entry, loads through L1/TEX: the list
-# word (4), the partner's FP32 (hi, lo) position split (32), the pair table's
-# value and gradient rows (16 + 16), the density gradient row (16), the
-# partner's F' (4)
-MIXED_L1_BYTES_PER_ENTRY = 88.0
-NCU_L1TEX_MIXED_FORCE = 0.696     # l1tex throughput, % of peak (committed ncu profile)
-NCU_FP64_PIPE_FORCE = 0.857       # FP64 pipe busy of k_force_fast (committed ncu profile)
+# mixed force kernel (k_force_mixed_staged), per full-list entry, loads on
+# the L1/shared-memory data path: the list word (4), the partner's FP32
+# (hi, lo) position split (32), the fused pair/density row (32, from shared
+# memory), the partner's F' (4)
+MIXED_L1_BYTES_PER_ENTRY = 72.0
+NCU_L1TEX_MIXED_FORCE = 0.628     # l1tex throughput, % of peak (committed ncu profile)
+NCU_FP64_PIPE_FORCE = 0.835       # FP64 pipe busy of k_force_fast (committed ncu profile)
 STEP_BYTES_PER_ATOM = 232.0       # whole NVE EAM step, canonical count
 FLOPS_PER_PAIR = 66.0             # canonical FP64 flops per half-list pair within rc
 FORCE_FLOPS_PER_PAIR = 52.0       # of those in the force pass (all but rho's 14)
@@ -532,7 +532,7 @@ def run_ours(args, rank, world, local):
     if "mixed" in res:
         m = res["mixed"]
         mv = n * args.steps * world / (m["ms"] * 1e-3)
-        # roofline of the mixed force pass (k_force_mixed): ncu puts it on
+        # roofline of the mixed force pass (k_force_mixed_staged): ncu puts it on
         # L1/TEX (the partner gathers), with the FP64 pipe idle and DRAM at a
         # few per cent.  achieved = bytes loaded through L1/TEX per launch
         # (MIXED_L1_BYTES_PER_ENTRY x full-list entries) / the launch's CUDA
@@ -547,7 +547,9 @@ def run_ours(args, rank, world, local):
         l1_bytes = MIXED_L1_BYTES_PER_ENTRY * m["nb"]
         l1_ach = l1_bytes / (mforce_ms * 1e-3) / 1e9
         mtraffic = committed_traffic("k_force_mixed")
-        mixed_roof = {"bound": "l1tex", "kernel": "k_force_mixed (EAM2 force pass, full list)",
+        mixed_roof = {"bound": "l1tex",
+                      "kernel": "k_force_mixed_staged (EAM2 force pass, full rows, fused table "
+                                "rows in shared memory)",
                       "achieved": l1_ach, "peak": l1_peak, "unit": "GB/s",
                       "frac": l1_ach / l1_peak, "traffic": mtraffic,
                       "peak_kind": "nominal: 128 B per SM per cycle x 152 SMs at the sampled "

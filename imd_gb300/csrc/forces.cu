@@ -186,18 +186,16 @@ __global__ void k_fold_force(SysView v) {
 // 8 scalars, src/imd_forces_nbl.c:1975-1994, on one device)
 __global__ void k_finalize_forces(const double *pe, int ne, const double *pf, int nf,
                                   DevScalars *sc) {
-  const int lane = threadIdx.x;
-  double e = 0.0, w = 0.0;
-  for (int b = lane; b < ne; b += 32) e += pe[b];
-  for (int b = lane; b < nf; b += 32) {
-    e += pf[2 * b];
-    w += pf[2 * b + 1];
+  double v[2] = {0.0, 0.0};
+  for (int b = threadIdx.x; b < ne; b += FIN_BS) v[0] += pe[b];
+  for (int b = threadIdx.x; b < nf; b += FIN_BS) {
+    v[0] += pf[2 * b];
+    v[1] += pf[2 * b + 1];
   }
-  e = warp_sum(e);
-  w = warp_sum(w);
-  if (lane == 0) {
-    sc->epot = e;
-    sc->virial = w;
+  fin_block<2, 0u>(v);
+  if (threadIdx.x == 0) {
+    sc->epot = v[0];
+    sc->virial = v[1];
   }
 }
 
@@ -696,7 +694,7 @@ static int launch_forces_det(const SysView &v, const ForceTabs &t, DevScalars *s
     else launch_force_det<false, false>(t, nq, st, v, pf);
     if (ev) cudaEventRecord(ev[3], st);
   }
-  k_finalize_forces<<<1, 32, 0, st>>>(pe, t.eam ? nbe : 0, pf, nq, sc);
+  k_finalize_forces<<<1, FIN_BS, 0, st>>>(pe, t.eam ? nbe : 0, pf, nq, sc);
   return t.eam ? 7 : 4;
 }
 
@@ -741,7 +739,7 @@ int launch_forces(const SysView &v, const ForceTabs &t, DevScalars *sc, int mixe
     launches += 1;
   }
   k_fold_force<<<gblocks, BS_VEC, 0, st>>>(v);
-  k_finalize_forces<<<1, 32, 0, st>>>(pe, t.eam ? nbe : 0, pf, nbf, sc);
+  k_finalize_forces<<<1, FIN_BS, 0, st>>>(pe, t.eam ? nbe : 0, pf, nbf, sc);
   launches += 2;
   return launches;
 }

@@ -420,4 +420,27 @@ __device__ __forceinline__ void block_sum_store_dyn(double (&v)[K], double *out)
   }
 }
 
+// The per-block partials of a pass reduced by one block of FIN_BS threads:
+// each thread folds a strided share, then warps and the block combine in a
+// fixed order (sums, or maxima where bit k of MAXMASK is set); thread 0
+// holds the totals.  Many independent loads in flight instead of one warp
+// walking every partial.
+constexpr int FIN_BS = 1024;
+template <int K, unsigned MAXMASK>
+__device__ __forceinline__ void fin_block(double (&v)[K]) {
+  __shared__ double sh[K][FIN_BS / 32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < K; k++) {
+    v[k] = ((MAXMASK >> k) & 1u) ? warp_max(v[k]) : warp_sum(v[k]);
+    if (lane == 0) sh[k][w] = v[k];
+  }
+  __syncthreads();
+  if (w == 0) {
+#pragma unroll
+    for (int k = 0; k < K; k++)
+      v[k] = ((MAXMASK >> k) & 1u) ? warp_max(sh[k][lane]) : warp_sum(sh[k][lane]);
+  }
+}
+
 }  // namespace imdgpu

@@ -333,18 +333,16 @@ __global__ void __launch_bounds__(STAGE_BS) k_force_mixed_staged(SysView v, DevT
 
 __global__ void k_finalize_mixed(const double *pe, int ne, const double *pf, int nf,
                                  DevScalars *sc) {
-  const int lane = threadIdx.x;
-  double e = 0.0, w = 0.0;
-  for (int b = lane; b < ne; b += 32) e += pe[b];
-  for (int b = lane; b < nf; b += 32) {
-    e += pf[2 * b];
-    w += pf[2 * b + 1];
+  double v[2] = {0.0, 0.0};
+  for (int b = threadIdx.x; b < ne; b += FIN_BS) v[0] += pe[b];
+  for (int b = threadIdx.x; b < nf; b += FIN_BS) {
+    v[0] += pf[2 * b];
+    v[1] += pf[2 * b + 1];
   }
-  e = warp_sum(e);
-  w = warp_sum(w);
-  if (lane == 0) {
-    sc->epot = e;
-    sc->virial = w;
+  fin_block<2, 0u>(v);
+  if (threadIdx.x == 0) {
+    sc->epot = v[0];
+    sc->virial = v[1];
   }
 }
 
@@ -433,7 +431,7 @@ int launch_forces_mixed(const SysView &v, const ForceTabs &t, DevScalars *sc, fl
     if (ev) cudaEventRecord(ev[3], st);
     launches += 1;
   }
-  k_finalize_mixed<<<1, 32, 0, st>>>(pe, t.eam ? nbe : 0, pf, nbf, sc);
+  k_finalize_mixed<<<1, FIN_BS, 0, st>>>(pe, t.eam ? nbe : 0, pf, nbf, sc);
   return launches + 1;
 }
 

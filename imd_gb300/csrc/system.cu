@@ -97,6 +97,9 @@ struct imdgpu_sys {
   unsigned fused_bytes = 0;
   int fused_grid = 0;    // resident blocks of the staged force pass (0: not stageable)
   int stage_rows = 1;    // imdgpu_set_table_staging
+  // every atom of type t has mass type_mass[t] (set_atoms checks)
+  double type_mass[MAXT] = {0, 0, 0, 0};
+  int type_mass_uniform = 0;
   int exact = 0;
   int interp = 0;  // table interpolation of tables read from now on
   std::vector<double> pending_table2[3];
@@ -638,7 +641,18 @@ __device__ __forceinline__ void block_reduce_ssmm(double a, double b, double c, 
   }
 }
 
-__global__ void __launch_bounds__(BS_VEC) k_nve(SysView v, double dt, double *partial) {
+// per type, where every atom of a type has the same mass m: timestep / m
+// rounded on the host (the bits of the per-atom division) and 1 / (4 m), so
+// the update needs no FP64 division, the costliest operation of the step on
+// this device's FP64 pipe
+struct NveMass {
+  double dt_over_m[MAXT];
+  double inv_4m[MAXT];
+  int uniform;
+};
+
+__global__ void __launch_bounds__(BS_VEC) k_nve(SysView v, double dt, NveMass nm,
+                                                double *partial) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   double ek = 0.0, fn = 0.0, fm = 0.0, dm = 0.0;
   if (i < v.n) {
@@ -655,8 +669,14 @@ __global__ void __launch_bounds__(BS_VEC) k_nve(SysView v, double dt, double *pa
     p.y = dadd(p.y, dmul(dt, f.y));
     p.z = dadd(p.z, dmul(dt, f.z));
     const double kin2 = dadd(dadd(dmul(p.x, p.x), dmul(p.y, p.y)), dmul(p.z, p.z));
-    ek = dadd(kin1, kin2) / (4.0 * p.w);
-    const double tmp = dt / p.w;
+    double tmp;
+    if (nm.uniform) {
+      ek = dmul(dadd(kin1, kin2), nm.inv_4m[t]);
+      tmp = nm.dt_over_m[t];
+    } else {
+      ek = dadd(kin1, kin2) / (4.0 * p.w);
+      tmp = dt / p.w;
+    }
     x.x = dadd(x.x, dmul(tmp, p.x));
     x.y = dadd(x.y, dmul(tmp, p.y));
     x.z = dadd(x.z, dmul(tmp, p.z));
@@ -671,19 +691,16 @@ __global__ void __launch_bounds__(BS_VEC) k_nve(SysView v, double dt, double *pa
 
 __global__ void k_finalize_nve(const double *partial, int nb, DevScalars *sc, double skin2,
                                double *hist, int *istep) {
-  const int lane = threadIdx.x;
-  double a = 0, b = 0, c = 0, d = 0;
-  for (int k = lane; k < nb; k += 32) {
-    a += partial[4 * k];
-    b += partial[4 * k + 1];
-    c = fmax(c, partial[4 * k + 2]);
-    d = fmax(d, partial[4 * k + 3]);
+  double v[4] = {0.0, 0.0, 0.0, 0.0};
+  for (int k = threadIdx.x; k < nb; k += FIN_BS) {
+    v[0] += partial[4 * k];
+    v[1] += partial[4 * k + 1];
+    v[2] = fmax(v[2], partial[4 * k + 2]);
+    v[3] = fmax(v[3], partial[4 * k + 3]);
   }
-  a = warp_sum(a);
-  b = warp_sum(b);
-  c = warp_max(c);
-  d = warp_max(d);
-  if (lane == 0) {
+  fin_block<4, 0xCu>(v);
+  const double a = v[0], b = v[1], c = v[2], d = v[3];
+  if (threadIdx.x == 0) {
     sc->ekin = a;
     sc->fnorm = b;
     sc->fmax2 = c;
@@ -2505,6 +2522,19 @@ int imdgpu_set_atoms(imdgpu_sys *s, int n, const int *number, const int *type,
   CK(dalloc(&dt, n));
   if (p) CK(dalloc(&dp, 3 * (size_t)n));
   CK(cudaMemcpy(dx, x, sizeof(double) * 3 * n, cudaMemcpyHostToDevice));
+  {
+    int seen[MAXT] = {0, 0, 0, 0};
+    s->type_mass_uniform = 1;
+    for (int i = 0; i < n && s->type_mass_uniform; i++) {
+      const int t = type[i];
+      if (!seen[t]) {
+        seen[t] = 1;
+        s->type_mass[t] = mass[i];
+      } else if (mass[i] != s->type_mass[t]) {
+        s->type_mass_uniform = 0;
+      }
+    }
+  }
   CK(cudaMemcpy(dm, mass, sizeof(double) * n, cudaMemcpyHostToDevice));
   CK(cudaMemcpy(dn, number, sizeof(int) * n, cudaMemcpyHostToDevice));
   CK(cudaMemcpy(dt, type, sizeof(int) * n, cudaMemcpyHostToDevice));
@@ -2695,14 +2725,25 @@ int imdgpu_estimate_nblist_size(imdgpu_sys *s, long *entries) {
   return IMDGPU_OK;
 }
 
+static NveMass nve_mass(const imdgpu_sys *s, double dt) {
+  NveMass nm;
+  memset(&nm, 0, sizeof nm);
+  nm.uniform = s->type_mass_uniform;
+  for (int t = 0; t < s->ntypes && nm.uniform; t++) {
+    nm.dt_over_m[t] = dt / s->type_mass[t];
+    nm.inv_4m[t] = 1.0 / (4.0 * s->type_mass[t]);
+  }
+  return nm;
+}
+
 int imdgpu_move_atoms_nve(imdgpu_sys *s, double timestep) {
   if (!s || !s->atoms_set) return fail(IMDGPU_ERR_STATE, "atoms not set");
   if (!s->geom_ready || s->nbcap == 0)
     return fail(IMDGPU_ERR_STATE, "move_atoms before the first calc_forces");
   SysView v = view(s);
   const int nb = nblk(s->n, BS_VEC);
-  k_nve<<<nb, BS_VEC, 0, s->st>>>(v, timestep, s->partial);
-  k_finalize_nve<<<1, 32, 0, s->st>>>(s->partial, nb, s->dsc, v.skin2, nullptr, nullptr);
+  k_nve<<<nb, BS_VEC, 0, s->st>>>(v, timestep, nve_mass(s, timestep), s->partial);
+  k_finalize_nve<<<1, FIN_BS, 0, s->st>>>(s->partial, nb, s->dsc, v.skin2, nullptr, nullptr);
   CK(cudaGetLastError());
   return read_back(s);
 }
@@ -2715,7 +2756,7 @@ int imdgpu_move_atoms_mik(imdgpu_sys *s, double timestep) {
   SysView v = view(s);
   const int nb = nblk(s->n, BS_VEC);
   k_mik<<<nb, BS_VEC, 0, s->st>>>(v, timestep, s->partial);
-  k_finalize_nve<<<1, 32, 0, s->st>>>(s->partial, nb, s->dsc, v.skin2, nullptr, nullptr);
+  k_finalize_nve<<<1, FIN_BS, 0, s->st>>>(s->partial, nb, s->dsc, v.skin2, nullptr, nullptr);
   CK(cudaGetLastError());
   return read_back(s);
 }
@@ -3176,8 +3217,8 @@ static int issue_nve_steps(imdgpu_sys *s, int k, double dt, int *istep, long &la
     launches += launch_forces(v, ft, s->dsc, s->precision == IMDGPU_MIXED, s->st,
                               e ? e + 2 : nullptr);
     if (e) cudaEventRecord(e[6], s->st);
-    k_nve<<<nb, BS_VEC, 0, s->st>>>(v, dt, s->partial);
-    k_finalize_nve<<<1, 32, 0, s->st>>>(s->partial, nb, s->dsc, v.skin2, s->hist, istep);
+    k_nve<<<nb, BS_VEC, 0, s->st>>>(v, dt, nve_mass(s, dt), s->partial);
+    k_finalize_nve<<<1, FIN_BS, 0, s->st>>>(s->partial, nb, s->dsc, v.skin2, s->hist, istep);
     s->hsc_valid = false;
     launches += 2;
     if (e) cudaEventRecord(e[7], s->st);
@@ -3706,6 +3747,7 @@ static int batch_load(imdgpu_sys *s, int ncells, const int *natoms, const double
   }
   s->nsys = ncells;
   s->h_aoff = aoff;
+  s->type_mass_uniform = 0;  // batches keep the per-atom division
   s->h_boxes.assign(boxes, boxes + 9 * (size_t)ncells);
   s->have_box = true;
   s->geom_ready = false;
