@@ -700,7 +700,7 @@ static int launch_forces_det(const SysView &v, const ForceTabs &t, DevScalars *s
 
 int launch_forces(const SysView &v, const ForceTabs &t, DevScalars *sc, int mixed,
                   cudaStream_t st, cudaEvent_t *ev) {
-  if (mixed) return launch_forces_mixed(v, t, sc, v.dff, st, ev);
+  if (mixed) return launch_forces_mixed(v, t, sc, st, ev);
   if (t.det) return launch_forces_det(v, t, sc, st, ev);
   int launches = 0;
   const int gblocks = nblk(v.gcap, BS_VEC) > 0 ? nblk(v.gcap, BS_VEC) : 1;

@@ -90,7 +90,6 @@ struct SysView {
   double4 *pos, *mom, *frc, *ref;
   double *rho, *df;
   float4 *xl;               // mixed: per atom FP32 (hi, lo) split of the position
-  float *dff;               // mixed: 2F' in FP32 (ext)
   int *number, *orig;
   int *ecell;               // buffered cell id of every ext atom
   int *gowner;              // ghost -> owning real slot

@@ -80,8 +80,8 @@ int mixed_staged_grid(unsigned bytes);
 void fold_rho_launch(const SysView &v, int blocks, cudaStream_t st);
 void fold_force_launch(const SysView &v, int blocks, cudaStream_t st);
 // mixed.cu: the FP32-force path over the full list
-int launch_forces_mixed(const SysView &v, const ForceTabs &t, DevScalars *sc, float *dff,
-                        cudaStream_t st, cudaEvent_t *ev);
+int launch_forces_mixed(const SysView &v, const ForceTabs &t, DevScalars *sc, cudaStream_t st,
+                        cudaEvent_t *ev);
 
 // batch.cu
 void launch_batch_round_pre(const SysView &v, CgSys *cs, int nsys, const CgParams &P,

@@ -110,7 +110,7 @@ __global__ void __launch_bounds__(BS_FORCE_MAX) k_density_mixed(SysView v, DevTa
 }
 
 // embedding in FP64 (per atom), F' also as FP32 for the pair kernel
-__global__ void __launch_bounds__(BS_VEC) k_embed_mixed(SysView v, DevTable emb, float *dff,
+__global__ void __launch_bounds__(BS_VEC) k_embed_mixed(SysView v, DevTable emb, SplitPos *sp,
                                                         double *partial) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   double e[1] = {0.0};
@@ -121,17 +121,17 @@ __global__ void __launch_bounds__(BS_VEC) k_embed_mixed(SysView v, DevTable emb,
     const double pot = poly_v<true>(cv_load(emb, t, k), chi);
     const double df = poly_g<true>(cg_load(emb, t, k), chi);
     v.df[i] = df;
-    dff[i] = (float)df;
+    sp[i].lo.w = (float)df;  // F' in FP32 travels with the position split
     v.frc[i].w = pot;
     e[0] = pot;
   }
   block_sum_store<1, BS_VEC>(e, partial);
 }
 
-__global__ void k_ghost_dff(SysView v, float *dff) {
+__global__ void k_ghost_dff(SysView v, SplitPos *sp) {
   const int ng = v.counters[0];
   for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < ng; g += gridDim.x * blockDim.x)
-    dff[v.n + g] = dff[v.gowner[g]];
+    sp[v.n + g].lo.w = sp[v.gowner[g]].lo.w;
 }
 
 // where the fused rows are read from
@@ -143,13 +143,12 @@ enum RowSrc { ROWS_NONE = 0, ROWS_GLOBAL = 1, ROWS_SHARED = 2 };
 template <bool NT1, bool EAM, int SRC>
 __device__ __forceinline__ void force_row_mixed(const SysView &v, const DevTable &pair,
                                                 const DevTable &rho, const float4 *rows,
-                                                const SplitPos *__restrict__ sp,
-                                                const float *__restrict__ dff, int i,
+                                                const SplitPos *__restrict__ sp, int i,
                                                 double (&acc)[2]) {
   const SplitPos a = sp[i];
   const int it = NT1 ? 0 : __float_as_int(a.hi.w), nt = v.ntypes;
   const int n1 = v.nnb[i], n2 = v.nnb2[i];
-  const float dfi = EAM ? dff[i] : 0.f;
+  const float dfi = EAM ? a.lo.w : 0.f;
   Acc fx, fy, fz, ee, vir;
   bool shortf = false;
   const uint32_t *__restrict__ nb = v.nbr + i;
@@ -190,7 +189,7 @@ __device__ __forceinline__ void force_row_mixed(const SysView &v, const DevTable
         }
         if (inr) {
           const float ris = fmaf(chi, f1.z, f1.y);
-          grad += 0.5f * (dfi * ris + __ldg(&dff[j]) * ris);
+          grad += 0.5f * (dfi * ris + b.lo.w * ris);
         }
         have = true;
       }
@@ -213,7 +212,7 @@ __device__ __forceinline__ void force_row_mixed(const SysView &v, const DevTable
           const int k2 = tab_index_f(rho, col2, r2, chi);
           rjs = polyf_g(rho, col2, k2, chi);
         }
-        const float dfj = __ldg(&dff[j]);
+        const float dfj = b.lo.w;
         grad += 0.5f * (dfi * rjs + dfj * ris);
         have = true;
       }
@@ -241,12 +240,11 @@ template <bool NT1, bool EAM, bool FUSED>
 __global__ void __launch_bounds__(BS_FORCE_MAX) k_force_mixed(SysView v, DevTable pair,
                                                           DevTable rho, const float4 *fused,
                                                           const SplitPos *sp,
-                                                          const float *dff, double *partial) {
+                                                          double *partial) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   double acc[2] = {0.0, 0.0};
   if (i < v.n && !atom_idle(v, i))
-    force_row_mixed<NT1, EAM, FUSED ? ROWS_GLOBAL : ROWS_NONE>(v, pair, rho, fused, sp, dff, i,
-                                                               acc);
+    force_row_mixed<NT1, EAM, FUSED ? ROWS_GLOBAL : ROWS_NONE>(v, pair, rho, fused, sp, i, acc);
   block_sum_store_dyn<2, BS_FORCE_MAX>(acc, partial);
 }
 
@@ -319,7 +317,6 @@ __global__ void __launch_bounds__(STAGE_BS) k_force_mixed_staged(SysView v, DevT
                                                                 const float4 *fused,
                                                                 unsigned fused_bytes,
                                                                 const SplitPos *sp,
-                                                                const float *dff,
                                                                 double *partial) {
   extern __shared__ __align__(16) float4 srows[];
   __shared__ __align__(8) unsigned long long bar;
@@ -327,7 +324,7 @@ __global__ void __launch_bounds__(STAGE_BS) k_force_mixed_staged(SysView v, DevT
   if (stage_rows(srows, fused, fused_bytes, &bar, v.status))
     for (int i = blockIdx.x * STAGE_BS + threadIdx.x; i < v.n; i += gridDim.x * STAGE_BS)
       if (!atom_idle(v, i))
-        force_row_mixed<true, true, ROWS_SHARED>(v, pair, rho, srows, sp, dff, i, acc);
+        force_row_mixed<true, true, ROWS_SHARED>(v, pair, rho, srows, sp, i, acc);
   block_sum_store_dyn<2, STAGE_BS>(acc, partial);
 }
 
@@ -380,23 +377,22 @@ int mixed_force_blocks(const ForceTabs &t, int n) {
 
 template <bool NT1, bool EAM>
 static void launch_force_mixed2(const ForceTabs &t, int nbf, cudaStream_t st, const SysView &v,
-                                const SplitPos *sp, const float *dff, double *pf) {
+                                const SplitPos *sp, double *pf) {
   if constexpr (NT1 && EAM) {
     if (t.fused) {
       if (t.stage_grid > 0)
         k_force_mixed_staged<<<nbf, STAGE_BS, t.fused_bytes, st>>>(
-            v, t.pair, t.rho, t.fused, t.fused_bytes, sp, dff, pf);
+            v, t.pair, t.rho, t.fused, t.fused_bytes, sp, pf);
       else
-        k_force_mixed<true, true, true><<<nbf, t.bs, 0, st>>>(v, t.pair, t.rho, t.fused, sp,
-                                                               dff, pf);
+        k_force_mixed<true, true, true><<<nbf, t.bs, 0, st>>>(v, t.pair, t.rho, t.fused, sp, pf);
       return;
     }
   }
-  k_force_mixed<NT1, EAM, false><<<nbf, t.bs, 0, st>>>(v, t.pair, t.rho, nullptr, sp, dff, pf);
+  k_force_mixed<NT1, EAM, false><<<nbf, t.bs, 0, st>>>(v, t.pair, t.rho, nullptr, sp, pf);
 }
 
-int launch_forces_mixed(const SysView &v, const ForceTabs &t, DevScalars *sc, float *dff,
-                        cudaStream_t st, cudaEvent_t *ev) {
+int launch_forces_mixed(const SysView &v, const ForceTabs &t, DevScalars *sc, cudaStream_t st,
+                        cudaEvent_t *ev) {
   const int gblocks = std::max(1, nblk(v.gcap, BS_VEC));
   const size_t ext = (size_t)v.ncap + v.gcap;
   SplitPos *sp = reinterpret_cast<SplitPos *>(v.xl);
@@ -413,11 +409,11 @@ int launch_forces_mixed(const SysView &v, const ForceTabs &t, DevScalars *sc, fl
     else k_density_mixed<false><<<nbr, t.bs_rho, 0, st>>>(v, t.rho, sp);
     if (ev) cudaEventRecord(ev[1], st);
     fold_rho_launch(v, gblocks, st);
-    k_embed_mixed<<<nbe, BS_VEC, 0, st>>>(v, t.embed, dff, pe);
-    k_ghost_dff<<<gblocks, BS_VEC, 0, st>>>(v, dff);
+    k_embed_mixed<<<nbe, BS_VEC, 0, st>>>(v, t.embed, sp, pe);
+    k_ghost_dff<<<gblocks, BS_VEC, 0, st>>>(v, sp);
     if (ev) cudaEventRecord(ev[2], st);
-    if (t.nt1) launch_force_mixed2<true, true>(t, nbf, st, v, sp, dff, pf);
-    else launch_force_mixed2<false, true>(t, nbf, st, v, sp, dff, pf);
+    if (t.nt1) launch_force_mixed2<true, true>(t, nbf, st, v, sp, pf);
+    else launch_force_mixed2<false, true>(t, nbf, st, v, sp, pf);
     if (ev) cudaEventRecord(ev[3], st);
     launches += 5;
   } else {
@@ -426,8 +422,8 @@ int launch_forces_mixed(const SysView &v, const ForceTabs &t, DevScalars *sc, fl
       cudaEventRecord(ev[1], st);
       cudaEventRecord(ev[2], st);
     }
-    if (t.nt1) launch_force_mixed2<true, false>(t, nbf, st, v, sp, dff, pf);
-    else launch_force_mixed2<false, false>(t, nbf, st, v, sp, dff, pf);
+    if (t.nt1) launch_force_mixed2<true, false>(t, nbf, st, v, sp, pf);
+    else launch_force_mixed2<false, false>(t, nbf, st, v, sp, pf);
     if (ev) cudaEventRecord(ev[3], st);
     launches += 1;
   }

@@ -118,7 +118,6 @@ struct imdgpu_sys {
   bool geom_split = false;    // mixed: the balanced half list first in every row, the other
                               // partners at the back (a full list in one)
   bool deterministic = false; // FP64 passes without atomics (imdgpu_set_deterministic)
-  float *dff = nullptr;
   int *d_cell_rank = nullptr, *d_rank_lin = nullptr, *d_hshell = nullptr;
   int *d_bsrc = nullptr, *d_blin = nullptr, *d_bcode = nullptr;
   int *d_cstart = nullptr, *d_ccount = nullptr;
@@ -1461,7 +1460,6 @@ static SysView view(imdgpu_sys *s) {
   v.balanced = s->geom_balanced ? 1 : 0;
   v.split = s->geom_split ? 1 : 0;
   v.nnb2 = s->nnb2;
-  v.dff = s->dff;
   v.bsrc = s->d_bsrc;
   v.blin = s->d_blin;
   v.bcode = s->d_bcode;
@@ -1868,8 +1866,6 @@ static int alloc_ext(imdgpu_sys *s, int gcap) {
   dfree(s->ecell);
   dfree(s->gowner);
   dfree(s->gcode);
-  dfree(s->dff);
-  CK(dalloc(&s->dff, ext));
   CK(dalloc(&s->pos, ext));
   CK(dalloc(&s->frc, ext));
   CK(dalloc(&s->rho, ext));
@@ -2164,7 +2160,7 @@ int imdgpu_destroy(imdgpu_sys *s) {
   dfree(s->nnb); dfree(s->nnb2); dfree(s->status); dfree(s->counters); dfree(s->partial); dfree(s->dsc);
   dfree(s->dnbl); dfree(s->hist); dfree(s->oldx); dfree(s->cgg); dfree(s->cgh);
   dfree(s->toldx); dfree(s->tcgg); dfree(s->tcgh);
-  dfree(s->slot_of); dfree(s->d_in); dfree(s->d_out); dfree(s->flushbuf); dfree(s->dff);
+  dfree(s->slot_of); dfree(s->d_in); dfree(s->d_out); dfree(s->flushbuf);
   dfree(s->ml_w); dfree(s->ml_m); dfree(s->ml_v); dfree(s->ml_grad); dfree(s->ml_wb);
   dfree(s->ml_pairs); dfree(s->ml_np); dfree(s->ml_dx); dfree(s->ml_target); dfree(s->ml_dldx);
   dfree(s->ml_wt);
