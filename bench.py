@@ -423,27 +423,19 @@ def run_ours(args, rank, world, local):
     except Exception:
         xh, ph, fh, eh = (np.empty((n, 3)), np.empty((n, 3)), np.empty((n, 3)), np.empty(n))
     s.get_state(xh, ph, fh, eh)
-    # one step through the C-ABI with host buffers: the state (positions,
-    # momenta) up, calc_forces / move_atoms_nve / check_nblist, the new state
-    # down and the step's energies (tot_pot_energy, tot_kin_energy) read
+    # one step through the C-ABI with host buffers (imdgpu_nve_step_host):
+    # the state (positions, momenta) up from pinned memory, calc_forces,
+    # move_atoms_nve with check_nblist's test, the new state down and the
+    # step's energies (tot_pot_energy, tot_kin_energy) read; one call and one
+    # synchronisation a step
     e_host = []
     for _ in range(3 if e2e_steps else 0):   # warm-up of the host path
-        s.put_state(xh, ph)
-        s.calc_forces(0)
-        s.move_atoms_nve(dt)
-        s.check_nblist()
-        s.get_state(xh, ph)
-        sc = s.scalars()
+        sc = s.nve_step_host(xh, ph, dt, xh, ph)
         e_host.append(sc.tot_pot_energy + sc.tot_kin_energy)
     barrier()
     t0 = time.perf_counter()
     for k in range(e2e_steps):
-        s.put_state(xh, ph)
-        s.calc_forces(k)
-        s.move_atoms_nve(dt)
-        s.check_nblist()
-        s.get_state(xh, ph)
-        sc = s.scalars()
+        sc = s.nve_step_host(xh, ph, dt, xh, ph)
         e_host.append(sc.tot_pot_energy + sc.tot_kin_energy)
     t_e2e = time.perf_counter() - t0
     barrier()
@@ -503,8 +495,9 @@ def run_ours(args, rank, world, local):
         "clocks": r["clocks"],
         "e2e": {"value": e2e, "unit": "atom-steps/s", "h2d_bytes_per_step": 48 * n,
                 "d2h_bytes_per_step": 48 * n + 16, "steps": e2e_steps,
-                "per_step": "x, p up; calc_forces, move_atoms_nve, check_nblist; x, p and "
-                            "the energies down"},
+                "per_step": "imdgpu_nve_step_host: x, p up from pinned host memory; "
+                            "calc_forces, move_atoms_nve with check_nblist's test; x, p and "
+                            "the energies down; one synchronisation"},
         "gpu_launches": int(r["launches"]),
         "roofline": {"bound": "fp64", "kernel": "k_force_fast (EAM2 force pass, half list)",
                      "achieved": force_tflops, "peak": fp64_peak, "unit": "TFLOP/s",

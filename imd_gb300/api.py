@@ -149,6 +149,8 @@ def lib() -> C.CDLL:
         L.imdgpu_set_profiling.argtypes = [vp, C.c_int]
         L.imdgpu_device_count.argtypes = [_ip]
         L.imdgpu_put_state.argtypes = [vp, _dp, _dp]
+        L.imdgpu_nve_step_host.argtypes = [vp, _dp, _dp, C.c_double, _dp, _dp,
+                                           C.POINTER(Scalars)]
         L.imdgpu_set_l2_flush.argtypes = [vp, C.c_long]
         L.imdgpu_probe_fp64_peak.argtypes = [_dp]
         L.imdgpu_set_device.argtypes = [C.c_int]
@@ -272,6 +274,16 @@ class GpuSystem:
         """Positions / momenta in caller order; x, p should be C-contiguous
         float64 (pinned host memory gives direct DMA)."""
         _check(lib().imdgpu_put_state(self.h, _p(x), _p(p)), "put_state")
+
+    def nve_step_host(self, x, p, timestep: float, x_out=None, p_out=None) -> Scalars:
+        """One NVE step with the state on the host (imdgpu_nve_step_host):
+        x, p up, calc_forces, move_atoms_nve with the list check, the new x, p
+        into x_out / p_out (may be x, p) and the step's scalars; one
+        synchronisation.  C-contiguous float64 arrays, pinned for direct DMA."""
+        sc = Scalars()
+        _check(lib().imdgpu_nve_step_host(self.h, _p(x), _p(p), float(timestep), _p(x_out),
+                                          _p(p_out), C.byref(sc)), "nve_step_host")
+        return sc
 
     def get_state(self, x=None, p=None, f=None, epot=None) -> None:
         """Fill the given preallocated (n,3)/(n,) float64 arrays."""

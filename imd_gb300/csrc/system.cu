@@ -650,8 +650,15 @@ struct NveMass {
   int uniform;
 };
 
+// skip: a device flag (the lowest non-finite input atom, n or more when
+// none); when it names an atom no atom moves and the block's partials are
+// zero.  Null on every path but the host-buffer step.
 __global__ void __launch_bounds__(BS_VEC) k_nve(SysView v, double dt, NveMass nm,
-                                                double *partial) {
+                                                double *partial, const int *skip = nullptr) {
+  if (skip && *skip < v.n) {
+    if (threadIdx.x < 4) partial[4 * blockIdx.x + threadIdx.x] = 0.0;
+    return;
+  }
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   double ek = 0.0, fn = 0.0, fm = 0.0, dm = 0.0;
   if (i < v.n) {
@@ -1345,9 +1352,10 @@ __global__ void k_check_finite(const double *x, const double *p, int n, int *bad
   if (!ok) atomicMin(bad, o);
 }
 
-__global__ void k_put_state(SysView v, const int *slot_of, const double *x, const double *p) {
+__global__ void k_put_state(SysView v, const int *slot_of, const double *x, const double *p,
+                            const int *skip = nullptr) {
   const int o = blockIdx.x * blockDim.x + threadIdx.x;
-  if (o >= v.n) return;
+  if (o >= v.n || (skip && *skip < v.n)) return;
   const int s = slot_of[o];
   double4 a = v.pos[s];
   a.x = x[3 * o];
@@ -2596,10 +2604,17 @@ int imdgpu_put_state(imdgpu_sys *s, const double *x, const double *p) {
   return IMDGPU_OK;
 }
 
+static int fill_scalars(imdgpu_sys *s, imdgpu_scalars *o);
+
 int imdgpu_get_scalars(imdgpu_sys *s, imdgpu_scalars *o) {
   if (!s || !o) return fail(IMDGPU_ERR_ARG, "null");
   int rc = read_back(s);
   if (rc) return rc;
+  return fill_scalars(s, o);
+}
+
+// the scalars of the host mirror read last, and the list statistics
+static int fill_scalars(imdgpu_sys *s, imdgpu_scalars *o) {
   // the list statistics change only with a build: recounted once per build
   const bool fresh = s->list_stats_build == s->nbl_count_host && s->list_stats_n == s->n &&
                      s->list_stats_cap == s->nbcap;
@@ -2636,6 +2651,65 @@ int imdgpu_get_scalars(imdgpu_sys *s, imdgpu_scalars *o) {
 }
 
 static int axial_virial(imdgpu_sys *s);
+static NveMass nve_mass(const imdgpu_sys *s, double dt);
+
+// One main_loop NVE step for a caller whose state lives on the host: the
+// positions and momenta up, calc_forces, move_atoms_nve (check_nblist's
+// displacement test is part of its reduction), the new positions and
+// momenta down, and the scalars; one synchronisation.  The input is checked
+// on the device: a non-finite value moves no atom and is IMDGPU_ERR_ARG.
+// An overflow of the list or ghost buffers redoes the step from the copied
+// input with grown buffers.
+int imdgpu_nve_step_host(imdgpu_sys *s, const double *x, const double *p, double timestep,
+                         double *x_out, double *p_out, imdgpu_scalars *out) {
+  if (!s || !x || !p) return fail(IMDGPU_ERR_ARG, "null state");
+  if (s->nsys > 0) return fail(IMDGPU_ERR_STATE, "a batch of cells has no NVE step");
+  int rc = prepare(s);
+  if (rc) return rc;
+  const size_t n = s->n;
+  const double *din_x = s->d_in, *din_p = s->d_in + 3 * n;
+  CK(cudaMemcpyAsync(s->d_in, x, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, s->st));
+  CK(cudaMemcpyAsync(s->d_in + 3 * n, p, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, s->st));
+  int *bad = &s->dsc->badin;
+  CK(cudaMemsetAsync(bad, 0x7f, sizeof(int), s->st));
+  k_check_finite<<<nblk(n, 256), 256, 0, s->st>>>(din_x, din_p, (int)n, bad);
+  SysView v = view(s);
+  k_put_state<<<nblk(n, 256), 256, 0, s->st>>>(v, s->slot_of, din_x, din_p, bad);
+  const int nb = nblk(n, BS_VEC);
+  for (int attempt = 0; attempt < 2; attempt++) {
+    CK(cudaMemsetAsync(s->status, 0, sizeof(unsigned), s->st));
+    if (attempt == 0) {
+      if (!(s->hsc_valid && !s->hsc->rebuild))
+        if ((rc = issue_rebuild(s))) return rc;
+    } else {
+      // the list overflowed: the step again from its input, grown buffers
+      k_put_state<<<nblk(n, 256), 256, 0, s->st>>>(view(s), s->slot_of, din_x, din_p, bad);
+      if ((rc = rebuild_sync(s))) return rc;
+      v = view(s);
+    }
+    if ((rc = forces_async(s))) return rc;
+    k_nve<<<nb, BS_VEC, 0, s->st>>>(v, timestep, nve_mass(s, timestep), s->partial, bad);
+    k_finalize_nve<<<1, FIN_BS, 0, s->st>>>(s->partial, nb, s->dsc, v.skin2, nullptr, nullptr);
+    s->hsc_valid = false;
+    double *ox = s->d_out, *op = s->d_out + 3 * n;
+    k_gather_out<<<nblk(n, 256), 256, 0, s->st>>>(v, x_out ? ox : nullptr, p_out ? op : nullptr,
+                                                 nullptr, nullptr, nullptr, nullptr);
+    CK(cudaGetLastError());
+    if (x_out) CK(cudaMemcpyAsync(x_out, ox, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, s->st));
+    if (p_out) CK(cudaMemcpyAsync(p_out, op, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, s->st));
+    if ((rc = read_back(s))) return rc;  // the one synchronisation
+    if (s->hsc->badin < (int)n)
+      return fail(IMDGPU_ERR_ARG, "non-finite position or momentum of atom " +
+                                      std::to_string(s->hsc->badin));
+    if (s->status_host & ST_CELLOVER)
+      return fail(IMDGPU_ERR_CELL, "more than " + std::to_string(CELLCAP) + " atoms in one cell");
+    if (s->status_host & ST_WAIT) return fail(IMDGPU_ERR_CUDA, kWaitMsg);
+    if (!(s->status_host & (ST_NBOVER | ST_GHOSTOVER))) break;
+    if (attempt == 1) return fail(IMDGPU_ERR_NOMEM, "list overflow persists");
+  }
+  if (out && (rc = fill_scalars(s, out))) return rc;
+  return (s->status_host & ST_SHORT) ? IMDGPU_WARN_SHORT : IMDGPU_OK;
+}
 
 int imdgpu_calc_forces(imdgpu_sys *s, int steps) {
   (void)steps;

@@ -136,6 +136,14 @@ int imdgpu_put_state(imdgpu_sys *sys, const double *x, const double *p);
 int imdgpu_get_atoms(imdgpu_sys *sys, double *x, double *p, double *f, double *epot,
                      double *eam_rho, double *eam_df);
 int imdgpu_get_scalars(imdgpu_sys *sys, imdgpu_scalars *out);
+/* One NVE step of main_loop for a caller whose state lives on the host:
+ * x and p (caller order, 3n each) up, calc_forces, move_atoms_nve with
+ * check_nblist's displacement test, the new x and p down to x_out / p_out
+ * (either may be NULL; they may be x and p themselves) and the scalars to
+ * *out (may be NULL), with one synchronisation.  A non-finite input is
+ * IMDGPU_ERR_ARG and moves no atom. */
+int imdgpu_nve_step_host(imdgpu_sys *sys, const double *x, const double *p, double timestep,
+                         double *x_out, double *p_out, imdgpu_scalars *out);
 
 /* calc_forces (src/imd_forces_nbl.c:281-1999): fix_cells + make_nblist when
  * the list is invalid, then pair / EAM2 forces, energies and virial. */

@@ -1,0 +1,73 @@
+"""imdgpu_nve_step_host: one NVE step of main_loop with the state on the host.
+
+The fused call must leave exactly what the separate C-ABI calls leave
+(put_state, calc_forces, move_atoms_nve, check_nblist, get_atoms): the same
+positions and momenta bit for bit and the same energies, over 40 steps of the
+Cu NVE golden run (rebuilds included), in place or into separate buffers.  A
+non-finite input is an error and moves no atom.
+"""
+import numpy as np
+import pytest
+
+from conftest import golden, tables
+
+pytestmark = pytest.mark.gpu
+
+
+def _system():
+    from imd_gb300 import api
+    g = golden("cu_nve")
+    s = api.GpuSystem(1, api.EAM2, api.FP64)
+    s.read_tables(tables("cu"))
+    s.set_box(g["box"], (1, 1, 1), 0.4)
+    s.set_atoms(g["number"], g["type"], g["mass"], g["x0"], g["p0"])
+    return s, g
+
+
+def test_fused_step_equals_separate_calls():
+    a, g = _system()
+    b, _ = _system()
+    dt = float(g["dt"])
+    xa = np.ascontiguousarray(g["x0"], np.float64).copy()
+    pa = np.ascontiguousarray(g["p0"], np.float64).copy()
+    xb, pb = xa.copy(), pa.copy()
+    xo, po = np.empty_like(xb), np.empty_like(pb)
+    rebuilds = set()
+    for k in range(40):
+        a.put_state(xa, pa)
+        a.calc_forces(k)
+        a.move_atoms_nve(dt)
+        a.check_nblist()
+        a.get_state(xa, pa)
+        sa = a.scalars()
+        if k % 2:
+            sb = b.nve_step_host(xb, pb, dt, xb, pb)          # in place
+        else:
+            sb = b.nve_step_host(xb, pb, dt, xo, po)
+            xb, pb = xo.copy(), po.copy()
+        np.testing.assert_array_equal(xb, xa)
+        np.testing.assert_array_equal(pb, pa)
+        assert sb.tot_pot_energy == sa.tot_pot_energy
+        assert sb.tot_kin_energy == sa.tot_kin_energy
+        assert sb.nbl_count == sa.nbl_count
+        rebuilds.add(sb.nbl_count)
+    assert len(rebuilds) > 1   # the run crossed at least one list rebuild
+
+
+def test_fused_step_refuses_non_finite_input():
+    from imd_gb300 import api
+    s, g = _system()
+    dt = float(g["dt"])
+    x = np.ascontiguousarray(g["x0"], np.float64).copy()
+    p = np.ascontiguousarray(g["p0"], np.float64).copy()
+    s.nve_step_host(x, p, dt, x, p)
+    before = s.get_atoms()
+    bad = x.copy()
+    bad[7, 1] = np.nan
+    with pytest.raises(api.IMDGPUError, match="atom 7"):
+        s.nve_step_host(bad, p, dt, None, None)
+    after = s.get_atoms()
+    np.testing.assert_array_equal(after["x"], before["x"])
+    np.testing.assert_array_equal(after["p"], before["p"])
+    # and the next good step goes on from where the system was
+    s.nve_step_host(x, p, dt, x, p)
