@@ -183,6 +183,7 @@ def lib() -> C.CDLL:
         L.imdgpu_get_npt_axial.argtypes = [vp, C.POINTER(NptAxialState)]
         L.imdgpu_set_blocks.argtypes = [vp, C.c_int, C.c_int]
         L.imdgpu_batch_set_autotune.argtypes = [vp, C.c_int]
+        L.imdgpu_batch_set_engine.argtypes = [vp, C.c_int]
         L.imdgpu_batch_positions.argtypes = [vp, _dp]
         fp = C.POINTER(C.c_float)
         L.imdgpu_ml_nparam.argtypes = []
@@ -699,6 +700,11 @@ class GpuBatch(GpuSystem):
         x = np.empty((self.n, 3))
         _check(lib().imdgpu_batch_positions(self.h, _p(x)), "batch_positions")
         return np.split(x, np.cumsum(self.natoms)[:-1])
+
+    def set_engine(self, on: bool) -> None:
+        """A round's CG work in one persistent kernel (default on) or in four
+        kernels (imdgpu_batch_set_engine)."""
+        _check(lib().imdgpu_batch_set_engine(self.h, int(bool(on))), "batch_set_engine")
 
     def set_autotune(self, on: bool) -> None:
         """Tune the block shape at every imdgpu_batch_begin (default on)."""

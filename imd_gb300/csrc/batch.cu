@@ -14,6 +14,8 @@
 //      single-system path; pairs never cross cells)
 //   -> per-cell reductions (energy, |F|^2, max |F|, g.g and F.(F-g)).
 // The host replays a captured CUDA graph of rounds until every cell is done.
+#include <algorithm>
+
 #include "kernels.cuh"
 
 namespace imdgpu {
@@ -397,7 +399,167 @@ __global__ void __launch_bounds__(256) k_bt_reduce(SysView v, const int *aoff, C
   }
 }
 
+// ---------------------------------------------------------------------------
+// The persistent CG engine.  One launch per round replaces the control,
+// vector, flag and reduction kernels: resident blocks of BS_ENGINE threads
+// take cells from a queue, largest first, and carry each cell through
+//   (1) the sums of its last force evaluation (k_bt_reduce's, same order),
+//   (2) its control (cg_machine, on thread 0),
+//   (3) the move / set_hg / reset of its atoms (k_bt_vec's),
+//   (4) its largest displacement since the list build, and the batch's
+//       rebuild flag when it passes skin/2 (k_bt_flag's test).
+// A cell's atoms are read once for (1) and once for (3) by the same block, so
+// the forces, g and h of (1) are still in L1/L2 for (3).  The force passes
+// stay separate kernels: they need every cell's list and run at their own
+// tuned shapes.
+constexpr int BS_ENGINE = 256;  // k_bt_reduce's block: the same summation order
+
+__global__ void __launch_bounds__(BS_ENGINE) k_bt_engine(
+    SysView v, const int *aoff, const int *order, CgSys *cs, int nsys, CgParams P,
+    int *sys_done, int *sys_short, double4 *oldx, double4 *g, double4 *h,
+    unsigned long long *maxd, int *ndone, int *queue, DevScalars *sc, double skin2) {
+  __shared__ double sh[6][BS_ENGINE / 32];
+  __shared__ CgSys S;
+  __shared__ int cell, active;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (;;) {
+    if (threadIdx.x == 0) {
+      const int c = atomicAdd(queue, 1);
+      cell = c < nsys ? order[c] : -1;
+      active = cell >= 0 && !sys_done[cell];
+      if (active) S = cs[cell];
+    }
+    __syncthreads();
+    const int s = cell;
+    if (s < 0) break;
+    if (active) {
+      const int a0 = aoff[s], a1 = aoff[s + 1];
+      if (S.eval) {  // (1) k_bt_reduce's sums of the last evaluation
+        double e = 0, fn = 0, fm = 0, fa = 0, gg = 0, dgg = 0;
+        for (int i = a0 + threadIdx.x; i < a1; i += BS_ENGINE) {
+          const double4 f = v.frc[i];
+          const double4 gi = g[i];
+          const double ff = f.x * f.x + f.y * f.y + f.z * f.z;
+          e += f.w;
+          fn += ff;
+          fm = fmax(fm, fmax(fmax(f.x * f.x, f.y * f.y), f.z * f.z));
+          fa = fmax(fa, ff);
+          gg += gi.x * gi.x + gi.y * gi.y + gi.z * gi.z;
+          dgg += P.cg_fr ? ff : f.x * (f.x - gi.x) + f.y * (f.y - gi.y) + f.z * (f.z - gi.z);
+        }
+        e = warp_sum(e);
+        fn = warp_sum(fn);
+        fm = warp_max(fm);
+        fa = warp_max(fa);
+        gg = warp_sum(gg);
+        dgg = warp_sum(dgg);
+        if (lane == 0) {
+          sh[0][w] = e; sh[1][w] = fn; sh[2][w] = fm; sh[3][w] = fa; sh[4][w] = gg; sh[5][w] = dgg;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+          double r[6] = {0, 0, 0, 0, 0, 0};
+          for (int k = 0; k < BS_ENGINE / 32; k++) {
+            r[0] += sh[0][k];
+            r[1] += sh[1][k];
+            r[2] = fmax(r[2], sh[2][k]);
+            r[3] = fmax(r[3], sh[3][k]);
+            r[4] += sh[4][k];
+            r[5] += sh[5][k];
+          }
+          S.E = r[0];
+          S.fnorm = r[1];
+          S.fmax2 = r[2];
+          S.fatom2 = r[3];
+          S.gg = r[4];
+          S.dgg = r[5];
+          S.nfc++;
+        }
+      }
+      if (threadIdx.x == 0) {  // (2) k_bt_control's step
+        const bool short_last = sys_short[s] != 0;
+        sys_short[s] = 0;
+        if (S.pc != PC_DONE) cg_machine(S, P, short_last);
+        const int done = (S.pc == PC_DONE);
+        if (done) {
+          atomicAdd(ndone, 1);
+          sys_done[s] = 1;
+        }
+        S.eval = !done;  // the coming force pass evaluates every unfinished cell
+        cs[s] = S;
+      }
+      __syncthreads();
+      // (3) k_bt_vec's update and (4) the displacement of every atom
+      const int op = S.op;
+      double dmax = 0.0;
+      if (op != OP_IDLE) {
+        const double alpha = S.alpha, gm = S.gamma;
+        for (int i = a0 + threadIdx.x; i < a1; i += BS_ENGINE) {
+          double4 x = v.pos[i];
+          if (op != OP_NONE) {
+            double4 ox = oldx[i], hh = h[i];
+            if (op == OP_RESET_MOVE || op == OP_SETHG_MOVE) {
+              const double4 f = v.frc[i];
+              ox = make_double4(x.x, x.y, x.z, 0.0);
+              if (op == OP_RESET_MOVE) {
+                hh = f;
+              } else {
+                hh.x = f.x + gm * hh.x;
+                hh.y = f.y + gm * hh.y;
+                hh.z = f.z + gm * hh.z;
+              }
+              g[i] = f;
+              h[i] = hh;
+              oldx[i] = ox;
+            }
+            x.x = ox.x + alpha * hh.x;
+            x.y = ox.y + alpha * hh.y;
+            x.z = ox.z + alpha * hh.z;
+            v.pos[i] = x;
+          }
+          const double4 r = v.ref[i];
+          const double dx = x.x - r.x, dy = x.y - r.y, dz = x.z - r.z;
+          dmax = fmax(dmax, dx * dx + dy * dy + dz * dz);
+        }
+      }
+      dmax = warp_max(dmax);
+      if (lane == 0) sh[0][w] = dmax;
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        double d = 0.0;
+        for (int k = 0; k < BS_ENGINE / 32; k++) d = fmax(d, sh[0][k]);
+        maxd[s] = (unsigned long long)__double_as_longlong(d);
+        if (!sys_done[s] && d > skin2) atomicExch(&sc->rebuild, 1);
+      }
+    }
+    __syncthreads();  // cell, active and S are rewritten for the next cell
+  }
+}
+
 static inline int nblk(long n, int bs) { return (int)((n + bs - 1) / bs); }
+
+int batch_engine_grid() {
+  int d = 0, nsm = 0, per_sm = 0;
+  if (cudaGetDevice(&d) != cudaSuccess) return 0;
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, d);
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bt_engine, BS_ENGINE, 0) !=
+      cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return nsm * std::max(1, per_sm);
+}
+
+void launch_batch_engine(const SysView &v, const int *aoff, const int *order, CgSys *cs,
+                         int nsys, const CgParams &P, int *sys_done, int *sys_short,
+                         double4 *oldx, double4 *g, double4 *h, unsigned long long *maxd,
+                         int *ndone, int *queue, DevScalars *sc, double skin2, int grid,
+                         cudaStream_t st) {
+  cudaMemsetAsync(queue, 0, sizeof(int), st);
+  k_bt_engine<<<std::max(1, std::min(grid, nsys)), BS_ENGINE, 0, st>>>(
+      v, aoff, order, cs, nsys, P, sys_done, sys_short, oldx, g, h, maxd, ndone, queue, sc,
+      skin2);
+}
 
 void launch_batch_round_pre(const SysView &v, CgSys *cs, int nsys, const CgParams &P,
                             int *sys_done, int *sys_short, double4 *oldx, double4 *g,

@@ -53,7 +53,8 @@ struct CgSys {
   double ax, bx, cx, fa, fb, fc, u, fu, ulim;            // mnbrak
   double a, b, x, w, v, fx, fw, fv, e, d;                // brent
   int pc, op, pending, steps, nfc, status, iter, ctf;
-  int nshort, pad;                                       // line searches ended short, in a row
+  int nshort;                                            // line searches ended short, in a row
+  int eval;  // the last force pass evaluated this cell: its sums are still to be taken
 };
 
 constexpr int BS_FORCE = 128;      // default block of the pair passes
@@ -91,6 +92,15 @@ void launch_batch_round_pre(const SysView &v, CgSys *cs, int nsys, const CgParam
                             double skin2, cudaStream_t st);
 void launch_batch_round_post(const SysView &v, const int *aoff, CgSys *cs, int nsys,
                              const double4 *g, int cg_fr, cudaStream_t st);
+// the persistent CG engine of a round (sums of the last evaluation, control,
+// vector update, displacement test), in place of the pre and post kernels;
+// `order`: cells largest first, `queue`: a work counter the launch zeroes
+void launch_batch_engine(const SysView &v, const int *aoff, const int *order, CgSys *cs,
+                         int nsys, const CgParams &P, int *sys_done, int *sys_short,
+                         double4 *oldx, double4 *g, double4 *h, unsigned long long *maxd,
+                         int *ndone, int *queue, DevScalars *sc, double skin2, int grid,
+                         cudaStream_t st);
+int batch_engine_grid();
 
 // learn.cu
 struct MlPair;

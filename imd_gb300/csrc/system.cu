@@ -172,6 +172,9 @@ struct imdgpu_sys {
   double *d_sbox = nullptr, *d_stbox = nullptr;
   CgSys *d_cs = nullptr;
   unsigned long long *d_maxd = nullptr;
+  int *d_order = nullptr, *d_queue = nullptr;  // cells largest first; the engine's work counter
+  int bt_engine = 1;                           // rounds through k_bt_engine (imdgpu_batch_set_engine)
+  int engine_grid = 0;
   std::vector<int> h_sgdim;
   BatchRun *brun = nullptr;
   // the cells as imdgpu_batch_set_cells received them (batch repacking)
@@ -1856,6 +1859,19 @@ static int setup_geometry_batch(imdgpu_sys *s) {
   CK(cudaMemcpy(s->d_scdim, cdim.data(), sizeof(int) * cdim.size(), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(s->d_scoff, coff.data(), sizeof(int) * ns, cudaMemcpyHostToDevice));
   CK(cudaMemcpy(s->d_aoff, s->h_aoff.data(), sizeof(int) * (ns + 1), cudaMemcpyHostToDevice));
+  {
+    // the CG engine's queue order: cells largest first, ties by index
+    std::vector<int> ord(ns);
+    for (int q = 0; q < ns; q++) ord[q] = q;
+    std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) {
+      return s->h_aoff[a + 1] - s->h_aoff[a] > s->h_aoff[b + 1] - s->h_aoff[b];
+    });
+    dfree(s->d_order);
+    dfree(s->d_queue);
+    CK(dalloc(&s->d_order, ns));
+    CK(dalloc(&s->d_queue, 1));
+    CK(cudaMemcpy(s->d_order, ord.data(), sizeof(int) * ns, cudaMemcpyHostToDevice));
+  }
   CK(cudaMemcpy(s->d_sbox, s->h_boxes.data(), sizeof(double) * 9 * ns, cudaMemcpyHostToDevice));
   CK(cudaMemcpy(s->d_stbox, tb.data(), sizeof(double) * 9 * ns, cudaMemcpyHostToDevice));
   CK(cudaMemset(s->d_ccount, 0, sizeof(int) * s->nall_cells));
@@ -2183,6 +2199,7 @@ int imdgpu_destroy(imdgpu_sys *s) {
   dfree(s->d_fmt_order);
   dfree(s->d_sys_short);
   dfree(s->d_atom_sys); dfree(s->d_aoff); dfree(s->d_sgdim); dfree(s->d_scdim); dfree(s->d_scoff);
+  dfree(s->d_order); dfree(s->d_queue);
   dfree(s->d_sys_done); dfree(s->d_ndone); dfree(s->d_sbox); dfree(s->d_stbox); dfree(s->d_cs);
   dfree(s->d_maxd);
   for (auto e : s->sev) cudaEventDestroy(e);
@@ -4068,6 +4085,15 @@ static void issue_batch_round(imdgpu_sys *s, const CgParams &P) {
   ForceTabs ft = ftabs(s);
   ft.epot = 0;
   s->hsc_valid = false;
+  if (s->bt_engine) {
+    if (!s->engine_grid) s->engine_grid = batch_engine_grid();
+    launch_batch_engine(v, s->d_aoff, s->d_order, s->d_cs, s->nsys, P, s->d_sys_done,
+                        s->d_sys_short, s->oldx, s->cgg, s->cgh, s->d_maxd, s->d_ndone,
+                        s->d_queue, s->dsc, v.skin2, s->engine_grid, s->st);
+    issue_rebuild(s);
+    launch_forces(v, ft, s->dsc, s->precision == IMDGPU_MIXED, s->st);
+    return;
+  }
   launch_batch_round_pre(v, s->d_cs, s->nsys, P, s->d_sys_done, s->d_sys_short, s->oldx,
                          s->cgg, s->cgh, s->d_maxd, s->d_ndone, s->dsc, v.skin2, s->st);
   issue_rebuild(s);
@@ -4166,6 +4192,12 @@ int imdgpu_set_blocks(imdgpu_sys *s, int block_density, int block_force) {
   return IMDGPU_OK;
 }
 
+int imdgpu_batch_set_engine(imdgpu_sys *s, int on) {
+  if (!s) return fail(IMDGPU_ERR_ARG, "null system");
+  s->bt_engine = on ? 1 : 0;
+  return IMDGPU_OK;
+}
+
 int imdgpu_batch_set_autotune(imdgpu_sys *s, int on) {
   if (!s) return fail(IMDGPU_ERR_ARG, "null system");
   s->autotune_batches = on ? 1 : 0;
@@ -4229,7 +4261,8 @@ int imdgpu_batch_advance(imdgpu_sys *s, int max_rounds, int *ndone_out, int *rou
     std::vector<uintptr_t> key = {(uintptr_t)s->pos, (uintptr_t)s->nbr, (uintptr_t)s->xl,
                                   (uintptr_t)s->nbcap, (uintptr_t)s->gcap,
                                   (uintptr_t)s->precision, (uintptr_t)s->exact,
-                                  (uintptr_t)s->n, (uintptr_t)s->nsys, (uintptr_t)s->d_cs};
+                                  (uintptr_t)s->n, (uintptr_t)s->nsys, (uintptr_t)s->d_cs,
+                                  (uintptr_t)s->bt_engine, (uintptr_t)s->d_order};
     if (s->use_graph) {
       if (!B.gx || key != B.gkey) {
         if (B.gx) cudaGraphExecDestroy(B.gx);

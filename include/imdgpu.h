@@ -406,6 +406,12 @@ int imdgpu_get_pairs(imdgpu_sys *sys, long cap, int *ni, int *nj, int *shift,
 int imdgpu_autotune(imdgpu_sys *sys, int *block_density, int *block_force);
 int imdgpu_set_blocks(imdgpu_sys *sys, int block_density, int block_force);
 int imdgpu_batch_set_autotune(imdgpu_sys *sys, int on);
+/* A batch round's CG work (the sums of the last evaluation, the control of
+ * every cell, the move and set_hg of its atoms, the list displacement test)
+ * runs in one persistent kernel whose resident blocks take cells largest
+ * first (default 1); 0 runs it as four kernels.  The results are the same
+ * bits either way. */
+int imdgpu_batch_set_engine(imdgpu_sys *sys, int on);
 
 /* Timing of the dominant kernels of the last nve_run (device ms, CUDA
  * events on the system's stream). */
