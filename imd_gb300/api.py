@@ -121,6 +121,7 @@ def lib() -> C.CDLL:
                                           C.POINTER(C.c_long)]
         L.imdgpu_set_graphs.argtypes = [vp, C.c_int]
         L.imdgpu_set_table_staging.argtypes = [vp, C.c_int]
+        L.imdgpu_set_pair_cache.argtypes = [vp, C.c_int]
         L.imdgpu_set_interpolation.argtypes = [vp, C.c_int]
         L.imdgpu_set_table2.argtypes = [vp, C.c_int, C.c_int, C.c_int, _dp]
         L.imdgpu_set_table.argtypes = [vp, C.c_int, C.c_int, C.c_int, _dp, _dp, _dp, _dp,
@@ -300,6 +301,11 @@ class GpuSystem:
     def set_graphs(self, on: bool) -> None:
         """Replay NVE chunks from a captured CUDA graph (default on)."""
         _check(lib().imdgpu_set_graphs(self.h, int(on)), "set_graphs")
+
+    def set_pair_cache(self, on: bool) -> None:
+        """FP64 one-species EAM2 on one table grid: the density pass caches
+        every pair's table terms for the force pass (default on)."""
+        _check(lib().imdgpu_set_pair_cache(self.h, int(on)), "set_pair_cache")
 
     def set_table_staging(self, on: bool) -> None:
         """Mixed force pass: fused table rows staged in shared memory

@@ -334,6 +334,121 @@ __global__ void __launch_bounds__(BS_FORCE_MAX) k_force_fast(SysView v, DevTable
 }
 
 // ---------------------------------------------------------------------------
+// Pair cache (imdgpu_set_pair_cache): one species, EAM2, pair and density
+// tables on one grid.  The density pass computes r^2 and the table index of
+// every half-list pair anyway; it also evaluates the pair's table terms the
+// force pass needs and stores them per list entry, column-major like the
+// list (entry k of atom i at k * ncap + i): r^2, the pair term of -grad
+// (phi' from cgn), -rho'/2 and phi, or r^2 = -1 beyond both cutoffs.  The
+// force pass streams them and gathers only the partner's position and F'.
+// Both passes are bound by the FP64 pipe with DRAM nearly idle, so 32 bytes
+// written and read per entry buy back the r^2, index and table arithmetic
+// of the second pass.  Formulas and order are k_density_fast's and
+// k_force_fast's: the forces are the same bits.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void st_stream(double4 *p, const double4 c) {
+  double2 *q = reinterpret_cast<double2 *>(p);
+  __stcs(q, make_double2(c.x, c.y));
+  __stcs(q + 1, make_double2(c.z, c.w));
+}
+__device__ __forceinline__ double4 ld_stream(const double4 *p) {
+  const double2 *q = reinterpret_cast<const double2 *>(p);
+  const double2 a = __ldcs(q), b = __ldcs(q + 1);
+  return make_double4(a.x, a.y, b.x, b.y);
+}
+
+template <bool CUB>
+__global__ void __launch_bounds__(BS_FORCE_MAX) k_density_cache(SysView v, DevTable pair,
+                                                            DevTable rho) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= v.n || atom_idle(v, i)) return;
+  const double4 pi = v.pos[i];
+  const int nn = v.nnb[i];
+  bool shortf = false;
+  double eam_r = 0.0;
+  const uint32_t *__restrict__ nb = v.nbr + i;
+  double4 *__restrict__ pc = v.pcache + i;
+#pragma unroll 2
+  for (int k = 0; k < nn; k++) {
+    const int j = (int)(__ldg(nb + (size_t)k * v.ncap) & NB_MASK);
+    const double4 pj = ldg4(&v.pos[j]);
+    const double dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
+    const double r2 = fma(dx, dx, fma(dy, dy, dz * dz));
+    double4 c = make_double4(-1.0, 0.0, 0.0, 0.0);
+    const bool inp = le_pos(r2, pair.end[0]), inr = lt_pos(r2, rho.end[0]);
+    if (inp || inr) {
+      double chi;
+      const int kk = tab_index_fast(pair, 0, r2, chi);  // rho's index too: one grid
+      c.x = r2;
+      if (inp) {
+        c.w = poly_v<CUB>(cv_load(pair, 0, kk), chi);
+        c.y = poly_g<CUB>(cgn_load(pair, 0, kk), chi);
+      }
+      if (inr) {
+        const double rho_h = poly_v<CUB>(cv_load(rho, 0, kk), chi);
+        eam_r += rho_h;
+        atomicAdd(&v.rho[j], rho_h);
+        c.z = poly_g<CUB>(cgn_load(rho, 0, kk), chi);  // rho.cgn holds -rho'/2
+      }
+      shortf |= lt_pos(r2, pair.begin[0]);
+    }
+    st_stream(pc + (size_t)k * v.ncap, c);
+  }
+  atomicAdd(&v.rho[i], eam_r);
+  if (shortf) flag_short(v, i);
+}
+
+template <bool EPOT>
+__global__ void __launch_bounds__(BS_FORCE_MAX) k_force_cache(SysView v, double *partial) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double acc[2] = {0.0, 0.0};  // energy, virial
+  if (i < v.n && !atom_idle(v, i)) {
+    const double4 pi = v.pos[i];
+    const int nn = v.nnb[i];
+    const double dfi = v.df[i];
+    double fnx = 0.0, fny = 0.0, fnz = 0.0, ee = 0.0, esum = 0.0, vir = 0.0;
+    const uint32_t *__restrict__ nb = v.nbr + i;
+    const double4 *__restrict__ pc = v.pcache + i;
+#pragma unroll 2
+    for (int k = 0; k < nn; k++) {
+      const double4 c = ld_stream(pc + (size_t)k * v.ncap);
+      if (c.x < 0.0) continue;  // beyond both cutoffs
+      const int j = (int)(__ldg(nb + (size_t)k * v.ncap) & NB_MASK);
+      const double4 pj = ldg4(&v.pos[j]);
+      const double dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
+      const double dfj = __ldg(&v.df[j]);
+      // c.z = 0 outside rho's cutoff and c.y = 0 outside phi's: the fma
+      // then returns the other term exactly, as the two branches would
+      const double ngrad = fma(c.z, dfi + dfj, c.y);
+      esum += c.w;
+      const double fx = dx * ngrad, fy = dy * ngrad, fz = dz * ngrad;
+      double *fj = &v.frc[j].x;
+      atomicAdd(fj + 0, fx);
+      atomicAdd(fj + 1, fy);
+      atomicAdd(fj + 2, fz);
+      if (EPOT) {
+        const double ehalf = 0.5 * c.w;
+        ee += ehalf;
+        atomicAdd(fj + 3, ehalf);
+      }
+      fnx += fx;
+      fny += fy;
+      fnz += fz;
+      vir = fma(c.x, ngrad, vir);
+    }
+    double *fi = &v.frc[i].x;
+    atomicAdd(fi + 0, -fnx);
+    atomicAdd(fi + 1, -fny);
+    atomicAdd(fi + 2, -fnz);
+    if (EPOT) atomicAdd(fi + 3, ee);
+    if (!EPOT && v.eshare) atomicAdd(fi + 3, esum);
+    acc[0] = esum;
+    acc[1] = vir;
+  }
+  block_sum_store_dyn<2, BS_FORCE_MAX>(acc, partial);
+}
+
+// ---------------------------------------------------------------------------
 // Deterministic FP64 passes (imdgpu_set_deterministic).  The half-list
 // kernels above add the reaction on the second atom of a pair with FP64
 // atomics, so the order of the per-atom sums, and their last bits, change
@@ -714,7 +829,9 @@ int launch_forces(const SysView &v, const ForceTabs &t, DevScalars *sc, int mixe
     cudaMemsetAsync(v.rho, 0, ext * sizeof(double), st);
     if (ev) cudaEventRecord(ev[0], st);
     const bool quad = (t.rho.mode == TAB_QUADRATIC);
-    if (t.exact && quad) k_density64<<<nbr, t.bs_rho, 0, st>>>(v, t.rho);
+    if (t.cache && quad) k_density_cache<false><<<nbr, t.bs_rho, 0, st>>>(v, t.pair, t.rho);
+    else if (t.cache) k_density_cache<true><<<nbr, t.bs_rho, 0, st>>>(v, t.pair, t.rho);
+    else if (t.exact && quad) k_density64<<<nbr, t.bs_rho, 0, st>>>(v, t.rho);
     else if (t.nt1 && quad) k_density_fast<true, false><<<nbr, t.bs_rho, 0, st>>>(v, t.rho);
     else if (t.nt1) k_density_fast<true, true><<<nbr, t.bs_rho, 0, st>>>(v, t.rho);
     else if (quad) k_density_fast<false, false><<<nbr, t.bs_rho, 0, st>>>(v, t.rho);
@@ -725,7 +842,9 @@ int launch_forces(const SysView &v, const ForceTabs &t, DevScalars *sc, int mixe
     else k_embed_fast<<<nbe, BS_VEC, 0, st>>>(v, t.embed, pe);
     k_ghost_df<<<gblocks, BS_VEC, 0, st>>>(v);
     if (ev) cudaEventRecord(ev[2], st);
-    launch_force_any(t, nbf, st, v, pf);
+    if (t.cache && t.epot) k_force_cache<true><<<nbf, t.bs, 0, st>>>(v, pf);
+    else if (t.cache) k_force_cache<false><<<nbf, t.bs, 0, st>>>(v, pf);
+    else launch_force_any(t, nbf, st, v, pf);
     if (ev) cudaEventRecord(ev[3], st);
     launches += 5;
   } else {

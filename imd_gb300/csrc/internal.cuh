@@ -95,6 +95,7 @@ struct SysView {
   int *gowner;              // ghost -> owning real slot
   int *gcode;               // ghost -> packed image shift (sx+1) + 3(sy+1) + 9(sz+1)
   uint32_t *nbr;            // ELL list
+  double4 *pcache;          // per list entry (same layout): r^2, -grad of phi, -rho'/2, phi
   int *nnb;                 // entries per atom
   int *cstart, *ccount;     // per buffered cell: first ext index, atoms
   const int *cell_rank;     // buffered lin -> Morton rank of real cell (-1 for buffer)

@@ -20,6 +20,7 @@ struct ForceTabs {
   const float4 *fused;  // mixed force pass: fused pair/density rows, or null
   unsigned fused_bytes;
   int stage_grid;       // >0: the force pass stages them in shared memory, this many blocks
+  int cache;            // FP64: the density pass caches per-entry pair terms for the force pass
 };
 
 // Device-side scalars of one system (results + control).

@@ -173,6 +173,9 @@ struct imdgpu_sys {
   CgSys *d_cs = nullptr;
   unsigned long long *d_maxd = nullptr;
   int *d_order = nullptr, *d_queue = nullptr;  // cells largest first; the engine's work counter
+  double4 *pcache = nullptr;                   // per list entry: the density pass's pair terms
+  size_t pcache_entries = 0;
+  int pair_cache = 1;                          // imdgpu_set_pair_cache
   int bt_engine = 1;                           // rounds through k_bt_engine (imdgpu_batch_set_engine)
   int engine_grid = 0;
   std::vector<int> h_sgdim;
@@ -1433,6 +1436,7 @@ static SysView view(imdgpu_sys *s) {
   v.gcap = s->gcap;
   v.ntypes = s->ntypes;
   v.nbcap = s->nbcap;
+  v.pcache = s->pcache;
   v.nreal_cells = s->nreal_cells;
   v.nall_cells = s->nall_cells;
   for (int a = 0; a < 3; a++) {
@@ -1493,6 +1497,23 @@ static SysView view(imdgpu_sys *s) {
   return v;
 }
 
+// pair and density tables on one grid (every column pair)
+static bool same_grid(const imdgpu_sys *s) {
+  if (!(s->have_tab[0] && s->have_tab[1])) return false;
+  const HostTable &a = s->htab[0], &b = s->htab[1];
+  for (int c = 0; c < a.ncols; c++)
+    for (int d = 0; d < b.ncols; d++)
+      if (!(a.begin[c] == b.begin[d] && a.end[c] == b.end[d] && a.invstep[c] == b.invstep[d]))
+        return false;
+  return true;
+}
+
+// the FP64 passes share per-entry pair terms (k_density_cache, k_force_cache)
+static bool cache_wanted(const imdgpu_sys *s) {
+  return s->pair_cache && s->precision == IMDGPU_FP64 && !s->deterministic && !s->exact &&
+         s->interaction == IMDGPU_EAM2 && s->ntypes == 1 && same_grid(s);
+}
+
 static ForceTabs ftabs(imdgpu_sys *s) {
   ForceTabs t;
   memset(&t, 0, sizeof t);
@@ -1509,14 +1530,8 @@ static ForceTabs ftabs(imdgpu_sys *s) {
   t.fused = s->dfused;
   t.fused_bytes = s->fused_bytes;
   t.stage_grid = s->stage_rows ? s->fused_grid : 0;
-  int same = s->have_tab[0] && s->have_tab[1];
-  if (same) {
-    const HostTable &a = s->htab[0], &b = s->htab[1];
-    for (int c = 0; c < a.ncols && same; c++)
-      for (int d = 0; d < b.ncols && same; d++)
-        same = (a.begin[c] == b.begin[d] && a.end[c] == b.end[d] && a.invstep[c] == b.invstep[d]);
-  }
-  t.samegrid = same;
+  t.samegrid = same_grid(s);
+  t.cache = cache_wanted(s) && s->pcache && s->pcache_entries == (size_t)s->nbcap * s->ncap;
   return t;
 }
 
@@ -1909,6 +1924,18 @@ static int alloc_list(imdgpu_sys *s, int nbcap) {
   dfree(s->nbr);
   CK(dalloc(&s->nbr, (size_t)nbcap * s->ncap));
   s->nbcap = nbcap;
+  dfree(s->pcache);
+  s->pcache = nullptr;
+  s->pcache_entries = 0;
+  if (cache_wanted(s)) {
+    // best effort: without room the passes run without the cache
+    if (dalloc(&s->pcache, (size_t)nbcap * s->ncap) == cudaSuccess) {
+      s->pcache_entries = (size_t)nbcap * s->ncap;
+    } else {
+      cudaGetLastError();
+      s->pcache = nullptr;
+    }
+  }
   return IMDGPU_OK;
 }
 
@@ -2199,7 +2226,7 @@ int imdgpu_destroy(imdgpu_sys *s) {
   dfree(s->d_fmt_order);
   dfree(s->d_sys_short);
   dfree(s->d_atom_sys); dfree(s->d_aoff); dfree(s->d_sgdim); dfree(s->d_scdim); dfree(s->d_scoff);
-  dfree(s->d_order); dfree(s->d_queue);
+  dfree(s->d_order); dfree(s->d_queue); dfree(s->pcache);
   dfree(s->d_sys_done); dfree(s->d_ndone); dfree(s->d_sbox); dfree(s->d_stbox); dfree(s->d_cs);
   dfree(s->d_maxd);
   for (auto e : s->sev) cudaEventDestroy(e);
@@ -3386,6 +3413,15 @@ static int run_chunk_graph(imdgpu_sys *s, int k, double dt, int *istep, long &la
   return IMDGPU_OK;
 }
 
+int imdgpu_set_pair_cache(imdgpu_sys *s, int on) {
+  if (!s) return fail(IMDGPU_ERR_ARG, "null");
+  if (s->pair_cache != (on ? 1 : 0)) {
+    s->pair_cache = on ? 1 : 0;
+    s->geom_ready = false;  // the cache is allocated with the list
+  }
+  return IMDGPU_OK;
+}
+
 int imdgpu_set_table_staging(imdgpu_sys *s, int on) {
   if (!s) return fail(IMDGPU_ERR_ARG, "null");
   s->stage_rows = on ? 1 : 0;
@@ -3466,7 +3502,8 @@ int imdgpu_nve_run(imdgpu_sys *s, int nsteps, double dt, double *epot, double *e
       break;
     }
     if (s->status_host & (ST_NBOVER | ST_GHOSTOVER)) {
-      // restore the chunk's start, grow and redo it
+      // restore the chunk's start, grow and redo it; eight overflows of one
+      // chunk in a row mean the growth does not converge
       if (++replays > 8) {
         rc = fail(IMDGPU_ERR_NOMEM, "list overflow persists");
         break;
@@ -3482,7 +3519,7 @@ int imdgpu_nve_run(imdgpu_sys *s, int nsteps, double dt, double *epot, double *e
         if (rc) break;
       }
       if (s->status_host & ST_NBOVER) {
-        rc = alloc_list(s, (int)(cnt[1] * 1.2) + 8);
+        rc = alloc_list(s, (int)(cnt[1] * 1.25) + 8);
         if (rc) break;
       }
       CK(cudaMemcpyAsync(s->pos, s->tpos, sizeof(double4) * s->n, cudaMemcpyDeviceToDevice, s->st));
@@ -3495,6 +3532,7 @@ int imdgpu_nve_run(imdgpu_sys *s, int nsteps, double dt, double *epot, double *e
     if (prof) accumulate_events(s, k);
     launches += chunk_launches;
     done += k;
+    replays = 0;
   }
   CK(cudaEventRecord(s->ev[1], s->st));
   CK(cudaStreamSynchronize(s->st));
@@ -4302,6 +4340,8 @@ int imdgpu_batch_advance(imdgpu_sys *s, int max_rounds, int *ndone_out, int *rou
       break;
     }
     if (s->status_host & (ST_NBOVER | ST_GHOSTOVER)) {
+      // eight overflows of one chunk of rounds in a row: the growth does not
+      // converge (the count resets with every chunk that completes)
       if (++replays > 8) {
         rc = fail(IMDGPU_ERR_NOMEM, "list overflow persists in batch relaxation");
         break;
@@ -4311,7 +4351,7 @@ int imdgpu_batch_advance(imdgpu_sys *s, int max_rounds, int *ndone_out, int *rou
       if (s->status_host & ST_GHOSTOVER)
         if ((rc = alloc_ext(s, (int)(cnt[3] * 1.25) + 4096))) break;
       if (s->status_host & ST_NBOVER)
-        if ((rc = alloc_list(s, (int)(cnt[1] * 1.2) + 8))) break;
+        if ((rc = alloc_list(s, (int)(cnt[1] * 1.25) + 8))) break;
       double4 *back[6] = {s->pos, s->mom, s->oldx, s->cgg, s->cgh, s->frc};
       for (int k = 0; k < 6; k++)
         CKR(cudaMemcpy(back[k], b4[k], sizeof(double4) * n, cudaMemcpyDeviceToDevice));
@@ -4327,6 +4367,7 @@ int imdgpu_batch_advance(imdgpu_sys *s, int max_rounds, int *ndone_out, int *rou
     B.ndone = B.ndone_base + nd;
     B.rounds += R;
     done_rounds += R;
+    replays = 0;
     // compaction: the unfinished cells alone, once they hold few enough atoms
     if (s->compact_pct > 0 && nd > 0 && nd < ns) {
       std::vector<int> dn(ns);

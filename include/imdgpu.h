@@ -442,6 +442,13 @@ int imdgpu_set_graphs(imdgpu_sys *sys, int on);
  * block (bulk asynchronous copies completing on an mbarrier).  0 reads them
  * from global memory; the forces are the same bits either way. */
 int imdgpu_set_table_staging(imdgpu_sys *sys, int on);
+/* FP64, one species, EAM2 with pair and density tables on one grid: the
+ * density pass, which finds r^2 and the table index of every pair anyway,
+ * stores the pair's table terms per list entry (32 bytes) and the force pass
+ * reads them instead of computing them again (default 1; trades FP64
+ * arithmetic, the bound of these passes, for memory traffic).  The forces
+ * are the same bits either way. */
+int imdgpu_set_pair_cache(imdgpu_sys *sys, int on);
 /* Measured FP64 FMA throughput of this device (TFLOP/s): a roofline
  * denominator for the FP64 force kernels. */
 int imdgpu_probe_fp64_peak(double *tflops);

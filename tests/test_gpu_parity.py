@@ -285,6 +285,41 @@ def test_mixed_fused_rows_match_per_table_lookups(tmp_path):
         assert abs(res[key][1] - e64) <= 1e-6 * abs(e64), key
 
 
+def test_pair_cache_matches_recomputed_terms(tmp_path):
+    """FP64 Sutton-Chen Cu (one species, pair and density tables on one
+    grid): the force pass reading the density pass's cached pair terms gives
+    the forces of the pass that computes them again (FP64 atomics change the
+    last bits from run to run, hence 1e-14), the same energies and, over 30
+    NVE steps with rebuilds, the same trajectory."""
+    from imd_gb300 import api
+    from imd_gb300 import workloads as wl
+    st = wl.eam_fcc_system(12, a0=3.615, T=300.0, seed=7)
+    x = st.x + 0.05 * np.random.default_rng(8).standard_normal(st.x.shape)
+    tabs = wl.sutton_chen_tables(str(tmp_path / "cu"), [wl.CU])
+    res = {}
+    for cache in (True, False):
+        s = api.GpuSystem(1, api.EAM2, api.FP64)
+        s.set_pair_cache(cache)
+        s.read_tables(tabs)
+        s.set_box(st.box, (1, 1, 1), 0.4)
+        s.set_atoms(st.number, st.types, st.mass, x, st.p)
+        assert s.calc_forces(0) == 0
+        a = s.get_atoms()
+        sc = s.scalars()
+        ep, ek = s.nve_run(30, wl.FS)
+        res[cache] = (a, sc.tot_pot_energy, sc.virial, ep, ek, s.get_atoms()["x"],
+                      s.scalars().nbl_count)
+        s.close()
+    (a1, e1, w1, ep1, ek1, x1, n1), (a0, e0, w0, ep0, ek0, x0, n0) = res[True], res[False]
+    assert rel_rms(a1["f"], a0["f"]) < 1e-14
+    np.testing.assert_allclose(a1["epot"], a0["epot"], rtol=1e-13, atol=0)
+    assert abs(e1 - e0) <= 1e-13 * abs(e0) and abs(w1 - w0) <= 1e-13 * abs(w0)
+    np.testing.assert_allclose(ep1, ep0, rtol=1e-12)
+    np.testing.assert_allclose(ek1, ek0, rtol=1e-12)
+    np.testing.assert_allclose(x1, x0, rtol=0, atol=1e-11)
+    assert n1 == n0 and n1 > 1
+
+
 def test_mixed_nve_conserves_energy():
     from imd_gb300 import api
     g = golden("cu_nve")
