@@ -53,6 +53,7 @@ DT_FS = 1.0
 SKIN = 0.4
 WORKLOAD = "sutton-chen Cu EAM2 NVE, fcc 40^3 = 256000 atoms, 300 K, dt 1 fs, skin 0.4 A"
 FORCE_BYTES_PER_ATOM = 56.0       # force kernel: read x (24) + 2F' (8), write F (24)
+PAIR_BYTES_PER_ATOM = 88.0        # both pair passes: x (24) in, rho (8) out; x, 2F' in, F out
 # mixed force kernel (k_force_mixed_staged), per full-list entry, loads on
 # the L1/shared-memory data path: the list word (4), the partner's FP32
 # (hi, lo) position split (32), the fused pair/density row (32, from shared
@@ -62,7 +63,6 @@ NCU_L1TEX_MIXED_FORCE = 0.628     # l1tex throughput, % of peak (committed ncu p
 NCU_FP64_PIPE_FORCE = 0.835       # FP64 pipe busy of k_force_fast (committed ncu profile)
 STEP_BYTES_PER_ATOM = 232.0       # whole NVE EAM step, canonical count
 FLOPS_PER_PAIR = 66.0             # canonical FP64 flops per half-list pair within rc
-FORCE_FLOPS_PER_PAIR = 52.0       # of those in the force pass (all but rho's 14)
 
 
 def dist_env():
@@ -303,7 +303,7 @@ def run_batch(args, tabs, rank=0, world=1, dist=None):
                      "converged": int((g["status"] == 0).sum()),
                      "converged_per_s": float((g["status"] == 0).sum() / sec),
                      "force_calls_per_relaxation": float(g["nfc"].mean()),
-                     "rounds_rank0": r.rounds,
+                     "rounds_rank0": r.rounds, "rebuilds_rank0": r.rebuilds,
                      "status_counts": np.bincount(g["status"], minlength=5).tolist(),
                      "tail_rank0": r.tail_histogram(len(mine), int(natoms[mine].sum()))}
         if name == "learned":
@@ -457,13 +457,18 @@ def run_ours(args, rank, world, local):
                 "energy_rel_error": float(abs(emx - e64) / abs(e64)),
                 "positions": "the 256000-atom system after the FP64 run (300 K)"}
 
-    # ---- roofline of the dominant kernel (EAM force pass, k_force_fast) ----
-    # The FP64 kernels are bound by the FP64 pipe (ncu: 86% busy, DRAM 1-3%),
-    # so the roofline is FP64 TFLOP/s against this device's measured FP64 FMA
-    # rate; the HBM figures are given beside it.
+    # ---- roofline of the dominant kernels: the two EAM pair passes ----
+    # The density and force passes are bound by the FP64 pipe (ncu: 83%
+    # busy, DRAM a few per cent), so the roofline is FP64 TFLOP/s against
+    # this device's measured FP64 FMA rate, the HBM figures beside it.  With
+    # the pair cache the density pass evaluates the table terms the force
+    # pass reads back, so the two are one unit: achieved = the canonical 66
+    # flops per half-list pair within rc / the two passes' CUDA-event time.
     force_ms = r["ms_force"] / args.steps
+    dens_ms = r["ms_density"] / args.steps
+    pair_ms = force_ms + dens_ms
     pairs_rc = 67.0 * n  # half-list pairs within rc per atom for fcc Cu (6 shells, 134/2)
-    force_flops = FORCE_FLOPS_PER_PAIR * pairs_rc
+    pair_flops = FLOPS_PER_PAIR * pairs_rc
     # the FP64 roofline denominator: imdgpu_probe_fp64_peak (kernel
     # k_fp64_probe: 8 independent FMA chains per thread, 8 blocks of 256
     # threads per SM, 4096 iterations, one warm-up launch), repeated, the
@@ -475,10 +480,11 @@ def run_ours(args, rank, world, local):
                           "8 x 256-thread blocks per SM, 4096 iterations, after a warm-up launch",
                 "repeats": len(probes), "tflops_each": probes,
                 "kept": "the best", "clocks": pclk.summary()}
-    force_tflops = force_flops / (force_ms * 1e-3) / 1e12
+    pair_tflops = pair_flops / (pair_ms * 1e-3) / 1e12
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
-    hbm_alg = FORCE_BYTES_PER_ATOM * n / (force_ms * 1e-3) / 1e9
-    traffic = committed_traffic("k_force_fast")
+    hbm_alg = PAIR_BYTES_PER_ATOM * n / (pair_ms * 1e-3) / 1e9
+    td, tf = committed_traffic("k_density_cache"), committed_traffic("k_force_cache")
+    traffic = (td + tf) if (td is not None and tf is not None) else None
     step_ms = r["ms"] / args.steps
     fp64_achieved = FLOPS_PER_PAIR * pairs_rc / (step_ms * 1e-3) / 1e12
 
@@ -499,19 +505,22 @@ def run_ours(args, rank, world, local):
                             "calc_forces, move_atoms_nve with check_nblist's test; x, p and "
                             "the energies down; one synchronisation"},
         "gpu_launches": int(r["launches"]),
-        "roofline": {"bound": "fp64", "kernel": "k_force_fast (EAM2 force pass, half list)",
-                     "achieved": force_tflops, "peak": fp64_peak, "unit": "TFLOP/s",
-                     "frac": force_tflops / fp64_peak, "traffic": traffic,
+        "roofline": {"bound": "fp64",
+                     "kernel": "k_density_cache + k_force_cache (the EAM2 pair passes, balanced "
+                               "half list, per-entry pair cache)",
+                     "achieved": pair_tflops, "peak": fp64_peak, "unit": "TFLOP/s",
+                     "frac": pair_tflops / fp64_peak, "traffic": traffic,
                      "peak_kind": "measured on this device: FP64 FMA chains "
                                   "(imdgpu_probe_fp64_peak); MEASURED_PEAKS.json has no FP64 rate",
                      "peak_how": peak_how,
-                     "flops_per_launch": force_flops,
-                     "flops_per_pair": FORCE_FLOPS_PER_PAIR,
+                     "flops_per_launch": pair_flops,
+                     "flops_per_pair": FLOPS_PER_PAIR,
+                     "ms_density": dens_ms, "ms_force": force_ms,
                      "ncu_fp64_pipe_busy": NCU_FP64_PIPE_FORCE,
                      "hbm": {"achieved": hbm_alg, "peak": hbm_peak, "unit": "GB/s",
                              "frac": hbm_alg / hbm_peak, "peak_kind": peak_kind,
-                             "bytes_per_atom": FORCE_BYTES_PER_ATOM,
-                             "traffic_gbs": (traffic / (force_ms * 1e-3) / 1e9) if traffic else None},
+                             "bytes_per_atom": PAIR_BYTES_PER_ATOM,
+                             "traffic_gbs": (traffic / (pair_ms * 1e-3) / 1e9) if traffic else None},
                      "step_fp64": {"achieved_tflops": fp64_achieved,
                                    "frac": fp64_achieved / fp64_peak,
                                    "flops_per_step": FLOPS_PER_PAIR * pairs_rc}},

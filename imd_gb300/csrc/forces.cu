@@ -344,7 +344,7 @@ __global__ void __launch_bounds__(BS_FORCE_MAX) k_force_fast(SysView v, DevTable
 // Both passes are bound by the FP64 pipe with DRAM nearly idle, so 32 bytes
 // written and read per entry buy back the r^2, index and table arithmetic
 // of the second pass.  Formulas and order are k_density_fast's and
-// k_force_fast's: the forces are the same bits.
+// k_force_fast's, so every pair term is the same bits.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ void st_stream(double4 *p, const double4 c) {
   double2 *q = reinterpret_cast<double2 *>(p);

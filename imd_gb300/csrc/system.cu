@@ -550,6 +550,11 @@ __global__ void __launch_bounds__(128) k_rb_build_half(SysView v, DevScalars *sc
   if (i >= v.n) return;
   const double4 pi = v.pos[i];
   v.ref[i] = pi;
+  if (atom_idle(v, i)) {  // a finished cell of a batch: no partners (pairs stay in a cell)
+    v.nnb[i] = 0;
+    if (v.split) v.nnb2[i] = 0;
+    return;
+  }
   const int r = slot_rank[i];
   const int *hs = v.hshell + (size_t)v.nshell * r;
   const bool bal = v.balanced != 0;

@@ -92,6 +92,7 @@ class RelaxResult:
     # unfinished cells) after every advance call, when relax() was asked to
     # trace
     trace: list = field(default_factory=list)
+    rebuilds: int = 0   # neighbour-list rebuilds of the batch during the relaxation
 
     @property
     def relaxations_per_s(self) -> float:
@@ -162,9 +163,10 @@ def relax(tables, cells, fmax: float = 1e-4, weights=None, precision=api.FP64,
     r = b.results()
     nfc = r["nfc"] + (2 * start_iters if weights is not None else 0)
     pos = b.positions() if keep_positions else []
+    nreb = b.rebuilds()
     b.close()
     return RelaxResult(sec, r["epot"], r["fmax"], nfc, r["steps"], r["status"], rounds,
-                       used, e0, e1, pos, tr)
+                       used, e0, e1, pos, tr, nreb)
 
 
 def targets(cells, relaxed_positions) -> list:

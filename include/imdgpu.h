@@ -409,8 +409,7 @@ int imdgpu_batch_set_autotune(imdgpu_sys *sys, int on);
 /* A batch round's CG work (the sums of the last evaluation, the control of
  * every cell, the move and set_hg of its atoms, the list displacement test)
  * runs in one persistent kernel whose resident blocks take cells largest
- * first (default 1); 0 runs it as four kernels.  The results are the same
- * bits either way. */
+ * first (default 1); 0 runs it as four kernels, with the same arithmetic. */
 int imdgpu_batch_set_engine(imdgpu_sys *sys, int on);
 
 /* Timing of the dominant kernels of the last nve_run (device ms, CUDA
@@ -440,14 +439,14 @@ int imdgpu_set_graphs(imdgpu_sys *sys, int on);
  * gradient; 32 bytes a row) and, with staging on (default 1) and rows that
  * fit two blocks per SM, copies them into shared memory once per resident
  * block (bulk asynchronous copies completing on an mbarrier).  0 reads them
- * from global memory; the forces are the same bits either way. */
+ * from global memory, with the same arithmetic. */
 int imdgpu_set_table_staging(imdgpu_sys *sys, int on);
 /* FP64, one species, EAM2 with pair and density tables on one grid: the
  * density pass, which finds r^2 and the table index of every pair anyway,
  * stores the pair's table terms per list entry (32 bytes) and the force pass
  * reads them instead of computing them again (default 1; trades FP64
  * arithmetic, the bound of these passes, for memory traffic).  The forces
- * are the same bits either way. */
+ * have the same per-pair terms either way. */
 int imdgpu_set_pair_cache(imdgpu_sys *sys, int on);
 /* Measured FP64 FMA throughput of this device (TFLOP/s): a roofline
  * denominator for the FP64 force kernels. */
