@@ -357,11 +357,30 @@ __device__ __forceinline__ double4 ld_stream(const double4 *p) {
   return make_double4(a.x, a.y, b.x, b.y);
 }
 
-template <bool CUB>
+// LPA lanes serve one atom (the autotuner's tile dimension: 1, 2 or 4):
+// lane q takes the entries q, q + LPA, ... of the atom's list and the lanes'
+// sums meet in a shuffle tree of the lane group.  More lanes per atom give
+// more warps when few atoms are active (the end of a batched relaxation).
+template <int LPA>
+__device__ __forceinline__ unsigned lane_group_mask() {
+  if (LPA == 1) return 1u << (threadIdx.x & 31);
+  const unsigned g = (1u << LPA) - 1u;
+  return g << ((threadIdx.x & 31) & ~(LPA - 1));
+}
+template <int LPA>
+__device__ __forceinline__ double group_sum(double x, unsigned mask) {
+#pragma unroll
+  for (int o = 1; o < LPA; o <<= 1) x += __shfl_xor_sync(mask, x, o);
+  return x;
+}
+
+template <bool CUB, int LPA>
 __global__ void __launch_bounds__(BS_FORCE_MAX) k_density_cache(SysView v, DevTable pair,
                                                             DevTable rho) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= v.n || atom_idle(v, i)) return;
+  const long gid = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = (int)(gid / LPA), q = (int)(gid % LPA);
+  if (i >= v.n || atom_idle(v, i)) return;  // the whole lane group alike
+  const unsigned mask = lane_group_mask<LPA>();
   const double4 pi = v.pos[i];
   const int nn = v.nnb[i];
   bool shortf = false;
@@ -369,7 +388,7 @@ __global__ void __launch_bounds__(BS_FORCE_MAX) k_density_cache(SysView v, DevTa
   const uint32_t *__restrict__ nb = v.nbr + i;
   double4 *__restrict__ pc = v.pcache + i;
 #pragma unroll 2
-  for (int k = 0; k < nn; k++) {
+  for (int k = q; k < nn; k += LPA) {
     const int j = (int)(__ldg(nb + (size_t)k * v.ncap) & NB_MASK);
     const double4 pj = ldg4(&v.pos[j]);
     const double dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
@@ -394,15 +413,18 @@ __global__ void __launch_bounds__(BS_FORCE_MAX) k_density_cache(SysView v, DevTa
     }
     st_stream(pc + (size_t)k * v.ncap, c);
   }
-  atomicAdd(&v.rho[i], eam_r);
+  eam_r = group_sum<LPA>(eam_r, mask);
+  if (q == 0) atomicAdd(&v.rho[i], eam_r);
   if (shortf) flag_short(v, i);
 }
 
-template <bool EPOT>
+template <bool EPOT, int LPA>
 __global__ void __launch_bounds__(BS_FORCE_MAX) k_force_cache(SysView v, double *partial) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const long gid = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = (int)(gid / LPA), q = (int)(gid % LPA);
   double acc[2] = {0.0, 0.0};  // energy, virial
-  if (i < v.n && !atom_idle(v, i)) {
+  if (i < v.n && !atom_idle(v, i)) {  // the whole lane group alike
+    const unsigned mask = lane_group_mask<LPA>();
     const double4 pi = v.pos[i];
     const int nn = v.nnb[i];
     const double dfi = v.df[i];
@@ -410,7 +432,7 @@ __global__ void __launch_bounds__(BS_FORCE_MAX) k_force_cache(SysView v, double 
     const uint32_t *__restrict__ nb = v.nbr + i;
     const double4 *__restrict__ pc = v.pcache + i;
 #pragma unroll 2
-    for (int k = 0; k < nn; k++) {
+    for (int k = q; k < nn; k += LPA) {
       const double4 c = ld_stream(pc + (size_t)k * v.ncap);
       if (c.x < 0.0) continue;  // beyond both cutoffs
       const int j = (int)(__ldg(nb + (size_t)k * v.ncap) & NB_MASK);
@@ -436,16 +458,48 @@ __global__ void __launch_bounds__(BS_FORCE_MAX) k_force_cache(SysView v, double 
       fnz += fz;
       vir = fma(c.x, ngrad, vir);
     }
-    double *fi = &v.frc[i].x;
-    atomicAdd(fi + 0, -fnx);
-    atomicAdd(fi + 1, -fny);
-    atomicAdd(fi + 2, -fnz);
-    if (EPOT) atomicAdd(fi + 3, ee);
-    if (!EPOT && v.eshare) atomicAdd(fi + 3, esum);
-    acc[0] = esum;
-    acc[1] = vir;
+    fnx = group_sum<LPA>(fnx, mask);
+    fny = group_sum<LPA>(fny, mask);
+    fnz = group_sum<LPA>(fnz, mask);
+    esum = group_sum<LPA>(esum, mask);
+    vir = group_sum<LPA>(vir, mask);
+    if (EPOT) ee = group_sum<LPA>(ee, mask);
+    if (q == 0) {
+      double *fi = &v.frc[i].x;
+      atomicAdd(fi + 0, -fnx);
+      atomicAdd(fi + 1, -fny);
+      atomicAdd(fi + 2, -fnz);
+      if (EPOT) atomicAdd(fi + 3, ee);
+      if (!EPOT && v.eshare) atomicAdd(fi + 3, esum);
+      acc[0] = esum;
+      acc[1] = vir;
+    }
   }
   block_sum_store_dyn<2, BS_FORCE_MAX>(acc, partial);
+}
+
+template <int LPA>
+static void launch_cache_passes(const ForceTabs &t, const SysView &v, int which, double *pf,
+                                cudaStream_t st) {
+  const long threads = (long)v.n * LPA;
+  if (which == 0) {
+    const int nb = (int)((threads + t.bs_rho - 1) / t.bs_rho);
+    if (t.rho.mode == TAB_QUADRATIC)
+      k_density_cache<false, LPA><<<nb, t.bs_rho, 0, st>>>(v, t.pair, t.rho);
+    else
+      k_density_cache<true, LPA><<<nb, t.bs_rho, 0, st>>>(v, t.pair, t.rho);
+  } else {
+    const int nb = (int)((threads + t.bs - 1) / t.bs);
+    if (t.epot) k_force_cache<true, LPA><<<nb, t.bs, 0, st>>>(v, pf);
+    else k_force_cache<false, LPA><<<nb, t.bs, 0, st>>>(v, pf);
+  }
+}
+// which: 0 the density pass, 1 the force pass
+static void launch_cache(const ForceTabs &t, const SysView &v, int which, double *pf,
+                         cudaStream_t st) {
+  if (t.lpa == 4) launch_cache_passes<4>(t, v, which, pf, st);
+  else if (t.lpa == 2) launch_cache_passes<2>(t, v, which, pf, st);
+  else launch_cache_passes<1>(t, v, which, pf, st);
 }
 
 // ---------------------------------------------------------------------------
@@ -823,14 +877,14 @@ int launch_forces(const SysView &v, const ForceTabs &t, DevScalars *sc, int mixe
   cudaMemsetAsync(v.frc, 0, ext * sizeof(double4), st);
   k_ghost_pos<<<gblocks, BS_VEC, 0, st>>>(v);
   launches++;
-  const int nbf = nblk(v.n, t.bs), nbe = nblk(v.n, BS_VEC), nbr = nblk(v.n, t.bs_rho);
+  const int lpa = t.cache ? t.lpa : 1;
+  const int nbf = nblk((long)v.n * lpa, t.bs), nbe = nblk(v.n, BS_VEC), nbr = nblk(v.n, t.bs_rho);
   double *pe = v.partial, *pf = v.partial + nbe;
   if (t.eam) {
     cudaMemsetAsync(v.rho, 0, ext * sizeof(double), st);
     if (ev) cudaEventRecord(ev[0], st);
     const bool quad = (t.rho.mode == TAB_QUADRATIC);
-    if (t.cache && quad) k_density_cache<false><<<nbr, t.bs_rho, 0, st>>>(v, t.pair, t.rho);
-    else if (t.cache) k_density_cache<true><<<nbr, t.bs_rho, 0, st>>>(v, t.pair, t.rho);
+    if (t.cache) launch_cache(t, v, 0, nullptr, st);
     else if (t.exact && quad) k_density64<<<nbr, t.bs_rho, 0, st>>>(v, t.rho);
     else if (t.nt1 && quad) k_density_fast<true, false><<<nbr, t.bs_rho, 0, st>>>(v, t.rho);
     else if (t.nt1) k_density_fast<true, true><<<nbr, t.bs_rho, 0, st>>>(v, t.rho);
@@ -842,8 +896,7 @@ int launch_forces(const SysView &v, const ForceTabs &t, DevScalars *sc, int mixe
     else k_embed_fast<<<nbe, BS_VEC, 0, st>>>(v, t.embed, pe);
     k_ghost_df<<<gblocks, BS_VEC, 0, st>>>(v);
     if (ev) cudaEventRecord(ev[2], st);
-    if (t.cache && t.epot) k_force_cache<true><<<nbf, t.bs, 0, st>>>(v, pf);
-    else if (t.cache) k_force_cache<false><<<nbf, t.bs, 0, st>>>(v, pf);
+    if (t.cache) launch_cache(t, v, 1, pf, st);
     else launch_force_any(t, nbf, st, v, pf);
     if (ev) cudaEventRecord(ev[3], st);
     launches += 5;

@@ -21,6 +21,7 @@ struct ForceTabs {
   unsigned fused_bytes;
   int stage_grid;       // >0: the force pass stages them in shared memory, this many blocks
   int cache;            // FP64: the density pass caches per-entry pair terms for the force pass
+  int lpa;              // lanes per atom of the cached passes (1, 2, 4)
 };
 
 // Device-side scalars of one system (results + control).

@@ -176,6 +176,7 @@ struct imdgpu_sys {
   double4 *pcache = nullptr;                   // per list entry: the density pass's pair terms
   size_t pcache_entries = 0;
   int pair_cache = 1;                          // imdgpu_set_pair_cache
+  int lpa = 1;                                 // lanes per atom of the cached passes (tuned)
   int bt_engine = 1;                           // rounds through k_bt_engine (imdgpu_batch_set_engine)
   int engine_grid = 0;
   std::vector<int> h_sgdim;
@@ -1537,6 +1538,7 @@ static ForceTabs ftabs(imdgpu_sys *s) {
   t.stage_grid = s->stage_rows ? s->fused_grid : 0;
   t.samegrid = same_grid(s);
   t.cache = cache_wanted(s) && s->pcache && s->pcache_entries == (size_t)s->nbcap * s->ncap;
+  t.lpa = s->lpa;
   return t;
 }
 
@@ -2102,7 +2104,7 @@ static int calc_forces_sync(imdgpu_sys *s) {
 // times under CUDA events; the fastest is kept for this (atoms, cells,
 // precision) until the system changes shape.  The forces are then computed
 // once more with the chosen shape.
-static int autotune_forces(imdgpu_sys *s, int force) {
+static int autotune_forces(imdgpu_sys *s, int force, bool tile_only = false) {
   const std::vector<long> key = {(long)s->n, (long)s->nsys, (long)s->precision,
                                  (long)s->interaction, (long)s->exact};
   if (!force && key == s->tuned_key) return IMDGPU_OK;
@@ -2114,7 +2116,7 @@ static int autotune_forces(imdgpu_sys *s, int force) {
   CK(cudaEventCreate(&e1));
   const bool mixed = s->precision == IMDGPU_MIXED;
   // the density block first (the force block at its default), then the force block
-  for (int which = 0; which < 2; which++) {
+  for (int which = 0; which < (tile_only ? 0 : 2); which++) {
     float best_ms = 1e30f;
     int best = BS_FORCE;
     for (int c : cand) {
@@ -2135,6 +2137,29 @@ static int autotune_forces(imdgpu_sys *s, int force) {
       }
     }
     (which == 0 ? s->bs_rho : s->bs_force) = best;
+  }
+  // the tile of the cached FP64 passes: lanes per atom, at the chosen blocks
+  if (ftabs(s).cache) {
+    float best_ms = 1e30f;
+    int best = 1;
+    for (int l : {1, 2, 4}) {
+      s->lpa = l;
+      const SysView v = view(s);
+      const ForceTabs t = ftabs(s);
+      launch_forces(v, t, s->dsc, mixed, s->st);
+      CK(cudaEventRecord(e0, s->st));
+      for (int r = 0; r < 3; r++) launch_forces(v, t, s->dsc, mixed, s->st);
+      CK(cudaEventRecord(e1, s->st));
+      CK(cudaEventSynchronize(e1));
+      CK(cudaGetLastError());
+      float ms = 0.f;
+      CK(cudaEventElapsedTime(&ms, e0, e1));
+      if (ms < best_ms) {
+        best_ms = ms;
+        best = l;
+      }
+    }
+    s->lpa = best;
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
@@ -4305,7 +4330,9 @@ int imdgpu_batch_advance(imdgpu_sys *s, int max_rounds, int *ndone_out, int *rou
                                   (uintptr_t)s->nbcap, (uintptr_t)s->gcap,
                                   (uintptr_t)s->precision, (uintptr_t)s->exact,
                                   (uintptr_t)s->n, (uintptr_t)s->nsys, (uintptr_t)s->d_cs,
-                                  (uintptr_t)s->bt_engine, (uintptr_t)s->d_order};
+                                  (uintptr_t)s->bt_engine, (uintptr_t)s->d_order,
+                                  (uintptr_t)s->pcache, (uintptr_t)s->lpa,
+                                  (uintptr_t)s->bs_rho, (uintptr_t)s->bs_force};
     if (s->use_graph) {
       if (!B.gx || key != B.gkey) {
         if (B.gx) cudaGraphExecDestroy(B.gx);
@@ -4347,12 +4374,17 @@ int imdgpu_batch_advance(imdgpu_sys *s, int max_rounds, int *ndone_out, int *rou
     if (s->status_host & (ST_NBOVER | ST_GHOSTOVER)) {
       // eight overflows of one chunk of rounds in a row: the growth does not
       // converge (the count resets with every chunk that completes)
-      if (++replays > 8) {
-        rc = fail(IMDGPU_ERR_NOMEM, "list overflow persists in batch relaxation");
-        break;
-      }
       int cnt[4];
       CKR(cudaMemcpy(cnt, s->counters, sizeof cnt, cudaMemcpyDeviceToHost));
+      if (++replays > 8) {
+        rc = fail(IMDGPU_ERR_NOMEM,
+                  "list overflow persists in batch relaxation (status " +
+                      std::to_string(s->status_host) + ", entries " + std::to_string(cnt[1]) +
+                      " of " + std::to_string(s->nbcap) + ", ghosts " + std::to_string(cnt[3]) +
+                      " of " + std::to_string(s->gcap) + ", round " +
+                      std::to_string(B.rounds) + ")");
+        break;
+      }
       if (s->status_host & ST_GHOSTOVER)
         if ((rc = alloc_ext(s, (int)(cnt[3] * 1.25) + 4096))) break;
       if (s->status_host & ST_NBOVER)
@@ -4385,6 +4417,8 @@ int imdgpu_batch_advance(imdgpu_sys *s, int max_rounds, int *ndone_out, int *rou
         for (int c = 0; c < ns; c++)
           if (!dn[c]) keep[B.cell_of[c]] = 1;
         if ((rc = batch_repack(s, keep))) break;
+        // fewer atoms: the lanes per atom of the pair passes again
+        if (s->autotune_batches && (rc = autotune_forces(s, 0, true))) break;
       }
     }
   }
