@@ -122,6 +122,9 @@ struct imdgpu_sys {
   int *d_bsrc = nullptr, *d_blin = nullptr, *d_bcode = nullptr;
   int *d_cstart = nullptr, *d_ccount = nullptr;
   int *d_rcount = nullptr, *d_rstart = nullptr, *d_gstart = nullptr;
+  // batches: per system, its first real bin and first buffer cell (ns + 1
+  // each), its ghost count and first ghost (scratch of the scans)
+  int *d_roff = nullptr, *d_boff = nullptr, *d_gtot = nullptr, *d_gbase = nullptr;
 
   int n = 0, ncap = 0, gcap = 0, nbcap = 0;
   double4 *pos = nullptr, *mom = nullptr, *frc = nullptr, *ref = nullptr;
@@ -494,6 +497,99 @@ __global__ void k_rb_ghost_scan(SysView v, DevScalars *sc, int *gstart) {
       atomicOr(v.status, ST_GHOSTOVER);
       v.counters[3] = carry;
     }
+  }
+}
+
+// Batches: the same scans per system, one block each, instead of one block
+// over every cell of the batch (a rebuild of a 2 M-atom batch has ~54 000
+// real bins and ~100 000 buffer cells).  A system's atoms fill exactly its
+// own bins, so its bins start at its first slot; its ghosts start after the
+// ghosts of the systems before it (the totals scanned by one block).  The
+// layout is the one-block scans' to the bit.
+__global__ void k_rb_scan_cells_sys(SysView v, DevScalars *sc, const int *roff, const int *aoff,
+                                    const int *rcount, int *rstart) {
+  if (!sc->rebuild) return;
+  const int q = blockIdx.x;
+  const int r0 = roff[q], nr = roff[q + 1] - r0;
+  __shared__ int total;
+  block_exclusive_scan<1024>(rcount + r0, rstart + r0, nr, &total);
+  __syncthreads();
+  const int a0 = aoff[q];
+  int mx = 0;
+  for (int t = threadIdx.x; t < nr; t += blockDim.x) {
+    const int r = r0 + t;
+    const int st = rstart[r] + a0;
+    rstart[r] = st;
+    const int lin = v.rank_lin[r];
+    v.cstart[lin] = st;
+    v.ccount[lin] = rcount[r];
+    mx = max(mx, rcount[r]);
+  }
+  atomicMax(&v.counters[2], mx);
+  if (mx > CELLCAP) atomicOr(v.status, ST_CELLOVER);
+}
+
+__global__ void k_rb_ghost_count_sys(SysView v, DevScalars *sc, const int *boff, int *gtot) {
+  if (!sc->rebuild) return;
+  const int q = blockIdx.x;
+  int c = 0;
+  for (int b = boff[q] + threadIdx.x; b < boff[q + 1]; b += blockDim.x) c += v.ccount[v.bsrc[b]];
+  __shared__ int sh[32];
+  c = __reduce_add_sync(0xffffffffu, c);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = c;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    int x = (threadIdx.x < (blockDim.x >> 5)) ? sh[threadIdx.x] : 0;
+    x = __reduce_add_sync(0xffffffffu, x);
+    if (threadIdx.x == 0) gtot[q] = x;
+  }
+}
+
+__global__ void k_rb_ghost_base(SysView v, DevScalars *sc, const int *gtot, int *gbase,
+                                int nsys) {
+  if (!sc->rebuild) return;
+  __shared__ int total;
+  block_exclusive_scan<1024>(gtot, gbase, nsys, &total);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    v.counters[0] = min(total, v.gcap);
+    if (total > v.gcap) {
+      atomicOr(v.status, ST_GHOSTOVER);
+      v.counters[3] = total;
+    }
+  }
+}
+
+__global__ void k_rb_ghost_scan_sys(SysView v, DevScalars *sc, const int *boff,
+                                    const int *gbase, int *gstart) {
+  if (!sc->rebuild) return;
+  const int q = blockIdx.x;
+  const int b0 = boff[q], nb = boff[q + 1] - b0;
+  __shared__ int sh[1024];
+  __shared__ int carry;
+  if (threadIdx.x == 0) carry = gbase[q];
+  __syncthreads();
+  for (int base = 0; base < nb; base += 1024) {
+    const int b = b0 + base + threadIdx.x;
+    const bool in = base + (int)threadIdx.x < nb;
+    const int x = in ? v.ccount[v.bsrc[b]] : 0;
+    sh[threadIdx.x] = x;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1) {
+      const int t = (threadIdx.x >= (unsigned)o) ? sh[threadIdx.x - o] : 0;
+      __syncthreads();
+      sh[threadIdx.x] += t;
+      __syncthreads();
+    }
+    if (in) {
+      const int st = carry + sh[threadIdx.x] - x;
+      gstart[b] = st;
+      v.cstart[v.blin[b]] = v.n + st;
+      v.ccount[v.blin[b]] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x == 1023) carry += sh[1023];
+    __syncthreads();
   }
 }
 
@@ -1762,7 +1858,7 @@ static int setup_geometry_batch(imdgpu_sys *s) {
   s->nreal_cells = roff[ns];
   std::vector<int> cell_rank(s->nall_cells, -1), rank_lin(s->nreal_cells);
   std::vector<int> hshell((size_t)nsh * s->nreal_cells, -1);
-  std::vector<int> bsrc, blin, bcode;
+  std::vector<int> bsrc, blin, bcode, boff(ns + 1, 0);
   for (int q = 0; q < ns; q++) {
     const int gx = gdim[3 * q], gy = gdim[3 * q + 1], gz = gdim[3 * q + 2];
     const int cx = cdim[3 * q], cy = cdim[3 * q + 1], cz = cdim[3 * q + 2];
@@ -1826,6 +1922,7 @@ static int setup_geometry_batch(imdgpu_sys *s) {
       bsrc.push_back(coff[q] + (ri * cy + rj) * cz + rk);
       bcode.push_back((sx + 1) + 3 * (sy + 1) + 9 * (sz + 1));
     }
+    boff[q + 1] = (int)blin.size();
   }
   s->nbuf = (int)blin.size();
   for (int a = 0; a < 3; a++) {
@@ -1881,6 +1978,16 @@ static int setup_geometry_batch(imdgpu_sys *s) {
   CK(cudaMemcpy(s->d_scdim, cdim.data(), sizeof(int) * cdim.size(), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(s->d_scoff, coff.data(), sizeof(int) * ns, cudaMemcpyHostToDevice));
   CK(cudaMemcpy(s->d_aoff, s->h_aoff.data(), sizeof(int) * (ns + 1), cudaMemcpyHostToDevice));
+  dfree(s->d_roff);
+  dfree(s->d_boff);
+  dfree(s->d_gtot);
+  dfree(s->d_gbase);
+  CK(dalloc(&s->d_roff, ns + 1));
+  CK(dalloc(&s->d_boff, ns + 1));
+  CK(dalloc(&s->d_gtot, ns));
+  CK(dalloc(&s->d_gbase, ns));
+  CK(cudaMemcpy(s->d_roff, roff.data(), sizeof(int) * (ns + 1), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(s->d_boff, boff.data(), sizeof(int) * (ns + 1), cudaMemcpyHostToDevice));
   {
     // the CG engine's queue order: cells largest first, ties by index
     std::vector<int> ord(ns);
@@ -1979,7 +2086,11 @@ static int issue_rebuild(imdgpu_sys *s) {
   k_rb_zero<<<std::max(1, nblk(std::max(s->nall_cells, s->nreal_cells), 256)), 256, 0, st>>>(
       v, sc, s->d_rcount);
   k_rb_wrap_bin<<<nb, BS_VEC, 0, st>>>(v, sc, s->key, s->local, s->d_rcount);
-  k_rb_scan_cells<<<1, 1024, 0, st>>>(v, sc, s->d_rcount, s->d_rstart);
+  if (s->nsys > 0)
+    k_rb_scan_cells_sys<<<s->nsys, 1024, 0, st>>>(v, sc, s->d_roff, s->d_aoff, s->d_rcount,
+                                                  s->d_rstart);
+  else
+    k_rb_scan_cells<<<1, 1024, 0, st>>>(v, sc, s->d_rcount, s->d_rstart);
   k_rb_scatter<<<nb, BS_VEC, 0, st>>>(v, sc, s->key, s->local, s->d_rstart, s->perm);
   k_rb_sort_cells<<<nblk(s->nreal_cells, 4), 128, 0, st>>>(v, sc, s->perm, s->d_rstart, s->d_rcount);
   k_rb_permute<<<nb, BS_VEC, 0, st>>>(v, sc, s->perm, s->key, s->tpos, s->tmom, s->tnumber,
@@ -1988,7 +2099,13 @@ static int issue_rebuild(imdgpu_sys *s) {
   k_rb_copyback<<<nb, BS_VEC, 0, st>>>(v, sc, s->tpos, s->tmom, s->tnumber, s->torig,
                                        s->slot_rank, cg ? s->oldx : nullptr, s->cgg, s->cgh,
                                        s->toldx, s->tcgg, s->tcgh, s->slot_of);
-  k_rb_ghost_scan<<<1, 1024, 0, st>>>(v, sc, s->d_gstart);
+  if (s->nsys > 0) {
+    k_rb_ghost_count_sys<<<s->nsys, 256, 0, st>>>(v, sc, s->d_boff, s->d_gtot);
+    k_rb_ghost_base<<<1, 1024, 0, st>>>(v, sc, s->d_gtot, s->d_gbase, s->nsys);
+    k_rb_ghost_scan_sys<<<s->nsys, 1024, 0, st>>>(v, sc, s->d_boff, s->d_gbase, s->d_gstart);
+  } else {
+    k_rb_ghost_scan<<<1, 1024, 0, st>>>(v, sc, s->d_gstart);
+  }
   if (s->nbuf) k_rb_ghost_fill<<<s->nbuf, 64, 0, st>>>(v, sc, s->d_gstart);
   k_rb_split<<<std::max(1, nblk((long)s->n + s->gcap, BS_VEC)), BS_VEC, 0, st>>>(v, sc);
   k_rb_build_half<<<nblk(s->n, 128), 128, 0, st>>>(v, sc, s->slot_rank);
@@ -2234,6 +2351,7 @@ int imdgpu_destroy(imdgpu_sys *s) {
   dfree(s->d_cell_rank); dfree(s->d_rank_lin); dfree(s->d_hshell); dfree(s->d_bsrc);
   dfree(s->d_blin); dfree(s->d_bcode); dfree(s->d_cstart); dfree(s->d_ccount);
   dfree(s->d_rcount); dfree(s->d_rstart); dfree(s->d_gstart);
+  dfree(s->d_roff); dfree(s->d_boff); dfree(s->d_gtot); dfree(s->d_gbase);
   dfree(s->pos); dfree(s->mom); dfree(s->frc); dfree(s->ref); dfree(s->tpos); dfree(s->tmom);
   dfree(s->rho); dfree(s->df); dfree(s->xl); dfree(s->number); dfree(s->orig);
   dfree(s->tnumber); dfree(s->torig); dfree(s->ecell); dfree(s->gowner); dfree(s->gcode);
