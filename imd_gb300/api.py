@@ -185,6 +185,7 @@ def lib() -> C.CDLL:
         L.imdgpu_set_blocks.argtypes = [vp, C.c_int, C.c_int]
         L.imdgpu_batch_set_autotune.argtypes = [vp, C.c_int]
         L.imdgpu_batch_set_engine.argtypes = [vp, C.c_int]
+        L.imdgpu_batch_set_partial_rebuild.argtypes = [vp, C.c_int]
         L.imdgpu_batch_positions.argtypes = [vp, _dp]
         fp = C.POINTER(C.c_float)
         L.imdgpu_ml_nparam.argtypes = []
@@ -711,6 +712,12 @@ class GpuBatch(GpuSystem):
         """A round's CG work in one persistent kernel (default on) or in four
         kernels (imdgpu_batch_set_engine)."""
         _check(lib().imdgpu_batch_set_engine(self.h, int(bool(on))), "batch_set_engine")
+
+    def set_partial_rebuild(self, on: bool) -> None:
+        """Rebuild the lists of the cells that moved only, each cell with a
+        fixed ghost range (imdgpu_batch_set_partial_rebuild)."""
+        _check(lib().imdgpu_batch_set_partial_rebuild(self.h, int(bool(on))),
+               "batch_set_partial_rebuild")
 
     def set_autotune(self, on: bool) -> None:
         """Tune the block shape at every imdgpu_batch_begin (default on)."""

@@ -338,13 +338,20 @@ __global__ void __launch_bounds__(BS_VEC) k_bt_vec(SysView v, const CgSys *cs, d
 }
 
 // any unfinished cell beyond skin/2 -> rebuild the list of the batch
+// with per-system rebuilds (sys_rb) only the cells that moved are flagged
 __global__ void k_bt_flag(const unsigned long long *maxd, const int *sys_done, int nsys,
-                          double skin2, DevScalars *sc) {
+                          double skin2, DevScalars *sc, int *sys_rb) {
   int need = 0;
   for (int s = threadIdx.x; s < nsys; s += blockDim.x)
-    if (!sys_done[s] && __longlong_as_double((long long)maxd[s]) > skin2) need = 1;
+    if (!sys_done[s] && __longlong_as_double((long long)maxd[s]) > skin2) {
+      need = 1;
+      if (sys_rb) sys_rb[s] = 1;
+    }
   need = __syncthreads_or(need);
-  if (threadIdx.x == 0 && need) sc->rebuild = 1;
+  if (threadIdx.x == 0 && need) {
+    if (sys_rb) atomicOr(&sc->rebuild, RB_FLAGGED);
+    else sc->rebuild = RB_ALL;
+  }
 }
 
 // per-cell sums in a fixed order: energy (per-atom shares in frc.w),
@@ -529,7 +536,14 @@ __global__ void __launch_bounds__(BS_ENGINE) k_bt_engine(
         double d = 0.0;
         for (int k = 0; k < BS_ENGINE / 32; k++) d = fmax(d, sh[0][k]);
         maxd[s] = (unsigned long long)__double_as_longlong(d);
-        if (!sys_done[s] && d > skin2) atomicExch(&sc->rebuild, 1);
+        if (!sys_done[s] && d > skin2) {
+          if (v.sys_rb) {
+            v.sys_rb[s] = 1;
+            atomicOr(&sc->rebuild, RB_FLAGGED);
+          } else {
+            atomicExch(&sc->rebuild, RB_ALL);
+          }
+        }
       }
     }
     __syncthreads();  // cell, active and S are rewritten for the next cell
@@ -567,7 +581,7 @@ void launch_batch_round_pre(const SysView &v, CgSys *cs, int nsys, const CgParam
                             double skin2, cudaStream_t st) {
   k_bt_control<<<nblk(nsys, 128), 128, 0, st>>>(cs, nsys, P, sys_done, sys_short, maxd, ndone);
   k_bt_vec<<<nblk(v.n, BS_VEC), BS_VEC, 0, st>>>(v, cs, oldx, g, h, maxd);
-  k_bt_flag<<<1, 1024, 0, st>>>(maxd, sys_done, nsys, skin2, sc);
+  k_bt_flag<<<1, 1024, 0, st>>>(maxd, sys_done, nsys, skin2, sc, v.sys_rb);
 }
 
 void launch_batch_round_post(const SysView &v, const int *aoff, CgSys *cs, int nsys,

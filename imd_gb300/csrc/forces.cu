@@ -24,6 +24,7 @@ __global__ void k_ghost_pos(SysView v) {
   for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < ng; g += gridDim.x * blockDim.x)
   {
     const int o = v.gowner[g];
+    if (o < 0) continue;  // an unused slot of a system's ghost range
     v.pos[v.n + g] = ghost_image(v, v.pos[o], v.gcode[g], sys_of(v, o));
   }
 }
@@ -67,7 +68,7 @@ __global__ void __launch_bounds__(BS_FORCE_MAX) k_density64(SysView v, DevTable 
 __global__ void k_fold_rho(SysView v) {
   const int ng = v.counters[0];
   for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < ng; g += gridDim.x * blockDim.x) {
-    const double r = v.rho[v.n + g];
+    const double r = v.rho[v.n + g];  // zero in unused slots
     if (r != 0.0) atomicAdd(&v.rho[v.gowner[g]], r);
   }
 }
@@ -91,8 +92,10 @@ __global__ void __launch_bounds__(BS_VEC) k_embed(SysView v, DevTable emb, doubl
 // send_cells(copy_dF) (src/imd_forces_nbl.c:1115)
 __global__ void k_ghost_df(SysView v) {
   const int ng = v.counters[0];
-  for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < ng; g += gridDim.x * blockDim.x)
-    v.df[v.n + g] = v.df[v.gowner[g]];
+  for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < ng; g += gridDim.x * blockDim.x) {
+    const int o = v.gowner[g];
+    if (o >= 0) v.df[v.n + g] = v.df[o];
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -728,6 +731,7 @@ __global__ void __launch_bounds__(BS_FORCE_MAX) k_stress_fast(SysView v, DevTabl
 __global__ void k_fold_stress(SysView v, double *stress) {
   const int ng = v.counters[0];
   for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < ng; g += gridDim.x * blockDim.x) {
+    if (v.gowner[g] < 0) continue;  // an unused slot of a system's ghost range
     const double *sg = stress + 6 * (size_t)(v.n + g);
     double *so = stress + 6 * (size_t)v.gowner[g];
 #pragma unroll

@@ -125,11 +125,26 @@ struct SysView {
   double4 *wrap_oldx;          // batch CG: old_x moved with the wrap of x
   int *sys_short;              // batch: per-system flag, a pair below a table begin
   int eshare;                  // force pass adds each atom's own pair energies to frc.w
+  // per-system rebuilds (batch, imdgpu_batch_set_partial_rebuild): the flag
+  // of each system that moved past skin/2, each system's fixed ghost range
+  // [goff[q], goff[q + 1]) (unused slots have gowner -1), the system of each
+  // real bin, of each buffer cell, and each system's first buffered cell
+  int *sys_rb;
+  const int *goff, *rank_sys, *buf_sys, *coff;
 };
+
+// sc->rebuild: bit 0 rebuild everything, bit 1 rebuild the systems whose
+// sys_rb flag is set
+constexpr int RB_ALL = 1, RB_FLAGGED = 2;
 
 // atoms of finished cells of a batch are skipped by the force passes
 __device__ __forceinline__ bool atom_idle(const SysView &v, int i) {
   return v.sys_done && v.sys_done[v.atom_sys[i]];
+}
+
+// a rebuild in progress covers system q (flag: the value of sc->rebuild)
+__device__ __forceinline__ bool rb_covers(const SysView &v, int flag, int q) {
+  return (flag & RB_ALL) || !v.sys_rb || v.sys_rb[q];
 }
 
 // a pair of atom i closer than a table's first point (IMD's "Short

@@ -131,7 +131,7 @@ __global__ void __launch_bounds__(BS_VEC) k_embed_mixed(SysView v, DevTable emb,
 __global__ void k_ghost_dff(SysView v, SplitPos *sp) {
   const int ng = v.counters[0];
   for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < ng; g += gridDim.x * blockDim.x)
-    sp[v.n + g].lo.w = sp[v.gowner[g]].lo.w;
+    if (v.gowner[g] >= 0) sp[v.n + g].lo.w = sp[v.gowner[g]].lo.w;
 }
 
 // where the fused rows are read from

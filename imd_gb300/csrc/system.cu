@@ -125,6 +125,11 @@ struct imdgpu_sys {
   // batches: per system, its first real bin and first buffer cell (ns + 1
   // each), its ghost count and first ghost (scratch of the scans)
   int *d_roff = nullptr, *d_boff = nullptr, *d_gtot = nullptr, *d_gbase = nullptr;
+  // per-system rebuilds (imdgpu_batch_set_partial_rebuild): flags, fixed
+  // ghost ranges, the system of every real bin and buffer cell
+  int percell_rb = 0;
+  int *d_sys_rb = nullptr, *d_goff = nullptr, *d_rank_sys = nullptr, *d_buf_sys = nullptr;
+  std::vector<int> h_goff;
 
   int n = 0, ncap = 0, gcap = 0, nbcap = 0;
   double4 *pos = nullptr, *mom = nullptr, *frc = nullptr, *ref = nullptr;
@@ -285,24 +290,31 @@ static int batch_full(imdgpu_sys *s);
 namespace imdgpu {
 
 __global__ void k_rb_zero(SysView v, DevScalars *sc, int *rcount) {
-  if (!sc->rebuild) return;
+  const int flag = sc->rebuild;
+  if (!flag) return;
   for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < v.nreal_cells; r += gridDim.x * blockDim.x)
-    rcount[r] = 0;
-  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < v.nall_cells; c += gridDim.x * blockDim.x)
-    v.ccount[c] = 0;
+    if (!v.rank_sys || rb_covers(v, flag, v.rank_sys[r])) rcount[r] = 0;
+  // a partial rebuild rewrites the counts of its systems' real and buffer
+  // cells in the scans and keeps the others
+  if (flag & RB_ALL || !v.sys_rb)
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < v.nall_cells; c += gridDim.x * blockDim.x)
+      v.ccount[c] = 0;
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     v.counters[1] = 0;
     v.counters[2] = 0;
+    if (v.goff) v.counters[0] = v.gcap;  // fixed ghost ranges: every slot, unused ones marked
   }
 }
 
 // do_boundaries (src/imd_main_3d.c:1972-2010) + cell_coord
 // (src/imd_geom_3d.c:1054-1074)
 __global__ void k_rb_wrap_bin(SysView v, DevScalars *sc, int *key, int *local, int *rcount) {
-  if (!sc->rebuild) return;
+  const int flag = sc->rebuild;
+  if (!flag) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= v.n) return;
   const int sy = sys_of(v, i);
+  if (!rb_covers(v, flag, sy)) return;
   double4 p = v.pos[i];
   double sh[3] = {0.0, 0.0, 0.0};  // lattice shift applied (also to CG's old_x in a batch)
 #pragma unroll
@@ -391,9 +403,10 @@ __global__ void k_rb_scan_cells(SysView v, DevScalars *sc, const int *rcount, in
 
 __global__ void k_rb_scatter(SysView v, DevScalars *sc, const int *key, const int *local,
                              const int *rstart, int *perm) {
-  if (!sc->rebuild) return;
+  const int flag = sc->rebuild;
+  if (!flag) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= v.n) return;
+  if (i >= v.n || !rb_covers(v, flag, sys_of(v, i))) return;
   perm[rstart[key[i]] + local[i]] = i;
 }
 
@@ -407,6 +420,7 @@ __global__ void k_rb_sort_cells(SysView v, DevScalars *sc, int *perm, const int 
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int r = blockIdx.x * 4 + w;
   if (r >= v.nreal_cells) return;
+  if (v.rank_sys && !rb_covers(v, sc->rebuild, v.rank_sys[r])) return;  // the whole warp
   const int s = rstart[r];
   const int c = min(rcount[r], CELLCAP);
   for (int t = lane; t < c; t += 32) {
@@ -426,9 +440,10 @@ __global__ void k_rb_permute(SysView v, DevScalars *sc, const int *perm, const i
                              double4 *tpos, double4 *tmom, int *tnumber, int *torig,
                              int *slot_rank, const double4 *oldx, const double4 *cgg,
                              const double4 *cgh, double4 *toldx, double4 *tcgg, double4 *tcgh) {
-  if (!sc->rebuild) return;
+  const int flag = sc->rebuild;
+  if (!flag) return;
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= v.n) return;
+  if (s >= v.n || !rb_covers(v, flag, sys_of(v, s))) return;  // slots stay in their system
   const int i = perm[s];
   tpos[s] = v.pos[i];
   tmom[s] = v.mom[i];
@@ -447,9 +462,10 @@ __global__ void k_rb_copyback(SysView v, DevScalars *sc, const double4 *tpos,
                               const int *slot_rank, double4 *oldx, double4 *cgg, double4 *cgh,
                               const double4 *toldx, const double4 *tcgg, const double4 *tcgh,
                               int *slot_of) {
-  if (!sc->rebuild) return;
+  const int flag = sc->rebuild;
+  if (!flag) return;
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= v.n) return;
+  if (s >= v.n || !rb_covers(v, flag, sys_of(v, s))) return;
   v.pos[s] = tpos[s];
   v.mom[s] = tmom[s];
   v.number[s] = tnumber[s];
@@ -508,8 +524,8 @@ __global__ void k_rb_ghost_scan(SysView v, DevScalars *sc, int *gstart) {
 // layout is the one-block scans' to the bit.
 __global__ void k_rb_scan_cells_sys(SysView v, DevScalars *sc, const int *roff, const int *aoff,
                                     const int *rcount, int *rstart) {
-  if (!sc->rebuild) return;
   const int q = blockIdx.x;
+  if (!sc->rebuild || !rb_covers(v, sc->rebuild, q)) return;
   const int r0 = roff[q], nr = roff[q + 1] - r0;
   __shared__ int total;
   block_exclusive_scan<1024>(rcount + r0, rstart + r0, nr, &total);
@@ -530,8 +546,8 @@ __global__ void k_rb_scan_cells_sys(SysView v, DevScalars *sc, const int *roff, 
 }
 
 __global__ void k_rb_ghost_count_sys(SysView v, DevScalars *sc, const int *boff, int *gtot) {
-  if (!sc->rebuild) return;
   const int q = blockIdx.x;
+  if (!sc->rebuild || !rb_covers(v, sc->rebuild, q)) return;
   int c = 0;
   for (int b = boff[q] + threadIdx.x; b < boff[q + 1]; b += blockDim.x) c += v.ccount[v.bsrc[b]];
   __shared__ int sh[32];
@@ -562,12 +578,15 @@ __global__ void k_rb_ghost_base(SysView v, DevScalars *sc, const int *gtot, int 
 
 __global__ void k_rb_ghost_scan_sys(SysView v, DevScalars *sc, const int *boff,
                                     const int *gbase, int *gstart) {
-  if (!sc->rebuild) return;
   const int q = blockIdx.x;
+  if (!sc->rebuild || !rb_covers(v, sc->rebuild, q)) return;
   const int b0 = boff[q], nb = boff[q + 1] - b0;
+  // fixed ghost ranges: the system's own range; otherwise after the systems
+  // before it
+  const int base = v.goff ? v.goff[q] : gbase[q];
   __shared__ int sh[1024];
   __shared__ int carry;
-  if (threadIdx.x == 0) carry = gbase[q];
+  if (threadIdx.x == 0) carry = base;
   __syncthreads();
   for (int base = 0; base < nb; base += 1024) {
     const int b = b0 + base + threadIdx.x;
@@ -591,18 +610,30 @@ __global__ void k_rb_ghost_scan_sys(SysView v, DevScalars *sc, const int *boff,
     if (threadIdx.x == 1023) carry += sh[1023];
     __syncthreads();
   }
+  if (v.goff) {
+    const int end = v.goff[q + 1];
+    if (carry > end) {
+      if (threadIdx.x == 0) atomicOr(v.status, ST_GHOSTOVER);
+    } else {
+      for (int g = carry + threadIdx.x; g < end; g += blockDim.x) v.gowner[g] = -1;
+    }
+  }
 }
 
 __global__ void k_rb_ghost_fill(SysView v, DevScalars *sc, const int *gstart) {
-  if (!sc->rebuild) return;
+  const int flag = sc->rebuild;
+  if (!flag) return;
   const int b = blockIdx.x;
   if (b >= v.nbuf) return;
+  const int q = v.buf_sys ? v.buf_sys[b] : 0;
+  if (!rb_covers(v, flag, q)) return;
+  const int gend = v.goff ? v.goff[q + 1] : v.gcap;  // overflow: stay in the range
   const int src = v.bsrc[b];
   const int s0 = v.cstart[src], cnt = v.ccount[src];
   const int g0 = gstart[b], code = v.bcode[b], lin = v.blin[b];
   for (int t = threadIdx.x; t < cnt; t += blockDim.x) {
     const int g = g0 + t;
-    if (g >= v.gcap) break;
+    if (g >= gend) break;
     const int owner = s0 + t;
     v.gowner[g] = owner;
     v.gcode[g] = code;
@@ -642,9 +673,10 @@ __device__ __forceinline__ bool owns_pair(int slot_i, int slot_j) {
 
 __global__ void __launch_bounds__(128) k_rb_build_half(SysView v, DevScalars *sc,
                                                         const int *slot_rank) {
-  if (!sc->rebuild) return;
+  const int flag = sc->rebuild;
+  if (!flag) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= v.n) return;
+  if (i >= v.n || !rb_covers(v, flag, sys_of(v, i))) return;  // other systems keep their lists
   const double4 pi = v.pos[i];
   v.ref[i] = pi;
   if (atom_idle(v, i)) {  // a finished cell of a batch: no partners (pairs stay in a cell)
@@ -705,8 +737,11 @@ __global__ void __launch_bounds__(128) k_rb_build_half(SysView v, DevScalars *sc
   if (over) atomicOr(v.status, ST_NBOVER);
 }
 
-__global__ void k_rb_done(DevScalars *sc, long *nbl) {
-  if (sc->rebuild) {
+__global__ void k_rb_done(DevScalars *sc, long *nbl, int *sys_rb, int nsys) {
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; sys_rb && q < nsys;
+       q += gridDim.x * blockDim.x)
+    sys_rb[q] = 0;
+  if (blockIdx.x == 0 && threadIdx.x == 0 && sc->rebuild) {
     sc->rebuild = 0;
     sc->maxdisp2 = 0.0;
     (*nbl)++;
@@ -1539,6 +1574,14 @@ static SysView view(imdgpu_sys *s) {
   v.ntypes = s->ntypes;
   v.nbcap = s->nbcap;
   v.pcache = s->pcache;
+  if (s->nsys > 0) {
+    v.rank_sys = s->d_rank_sys;
+    v.buf_sys = s->d_buf_sys;
+    if (s->percell_rb && s->d_goff) {
+      v.sys_rb = s->d_sys_rb;
+      v.goff = s->d_goff;
+    }
+  }
   v.nreal_cells = s->nreal_cells;
   v.nall_cells = s->nall_cells;
   for (int a = 0; a < 3; a++) {
@@ -1989,6 +2032,36 @@ static int setup_geometry_batch(imdgpu_sys *s) {
   CK(cudaMemcpy(s->d_roff, roff.data(), sizeof(int) * (ns + 1), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(s->d_boff, boff.data(), sizeof(int) * (ns + 1), cudaMemcpyHostToDevice));
   {
+    std::vector<int> rsys(s->nreal_cells), bsys(std::max(1, s->nbuf), 0);
+    for (int q = 0; q < ns; q++) {
+      for (int r = roff[q]; r < roff[q + 1]; r++) rsys[r] = q;
+      for (int b = boff[q]; b < boff[q + 1]; b++) bsys[b] = q;
+    }
+    dfree(s->d_rank_sys);
+    dfree(s->d_buf_sys);
+    dfree(s->d_sys_rb);
+    dfree(s->d_goff);
+    CK(dalloc(&s->d_rank_sys, rsys.size()));
+    CK(dalloc(&s->d_buf_sys, bsys.size()));
+    CK(cudaMemcpy(s->d_rank_sys, rsys.data(), sizeof(int) * rsys.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(s->d_buf_sys, bsys.data(), sizeof(int) * bsys.size(), cudaMemcpyHostToDevice));
+    s->h_goff.clear();
+    if (s->percell_rb) {
+      // each system's ghost range: its buffer cells times its atoms per real
+      // bin, with a quarter of head-room (grown on overflow)
+      s->h_goff.assign(ns + 1, 0);
+      for (int q = 0; q < ns; q++) {
+        const double per_bin = (double)(s->h_aoff[q + 1] - s->h_aoff[q]) / (roff[q + 1] - roff[q]);
+        const int cap = (int)((boff[q + 1] - boff[q]) * per_bin * 1.25) + 64;
+        s->h_goff[q + 1] = s->h_goff[q] + cap;
+      }
+      CK(dalloc(&s->d_goff, ns + 1));
+      CK(dalloc(&s->d_sys_rb, ns));
+      CK(cudaMemcpy(s->d_goff, s->h_goff.data(), sizeof(int) * (ns + 1), cudaMemcpyHostToDevice));
+      CK(cudaMemset(s->d_sys_rb, 0, sizeof(int) * ns));
+    }
+  }
+  {
     // the CG engine's queue order: cells largest first, ties by index
     std::vector<int> ord(ns);
     for (int q = 0; q < ns; q++) ord[q] = q;
@@ -2074,6 +2147,7 @@ static void estimate_caps(imdgpu_sys *s, int &nbcap, int &gcap) {
   const double frac = (double)(s->nall_cells - s->nreal_cells) / s->nreal_cells;
   gcap = (int)(s->n * frac * 1.25) + 1024;
   if (s->nsys > 0) gcap = (int)(s->n * frac * 0.8) + 4096;  // refined by the first build
+  if (s->nsys > 0 && !s->h_goff.empty()) gcap = s->h_goff.back();  // fixed per-system ranges
 }
 
 // issue the guarded rebuild sequence (no host synchronisation)
@@ -2101,7 +2175,7 @@ static int issue_rebuild(imdgpu_sys *s) {
                                        s->toldx, s->tcgg, s->tcgh, s->slot_of);
   if (s->nsys > 0) {
     k_rb_ghost_count_sys<<<s->nsys, 256, 0, st>>>(v, sc, s->d_boff, s->d_gtot);
-    k_rb_ghost_base<<<1, 1024, 0, st>>>(v, sc, s->d_gtot, s->d_gbase, s->nsys);
+    if (!v.goff) k_rb_ghost_base<<<1, 1024, 0, st>>>(v, sc, s->d_gtot, s->d_gbase, s->nsys);
     k_rb_ghost_scan_sys<<<s->nsys, 1024, 0, st>>>(v, sc, s->d_boff, s->d_gbase, s->d_gstart);
   } else {
     k_rb_ghost_scan<<<1, 1024, 0, st>>>(v, sc, s->d_gstart);
@@ -2109,7 +2183,7 @@ static int issue_rebuild(imdgpu_sys *s) {
   if (s->nbuf) k_rb_ghost_fill<<<s->nbuf, 64, 0, st>>>(v, sc, s->d_gstart);
   k_rb_split<<<std::max(1, nblk((long)s->n + s->gcap, BS_VEC)), BS_VEC, 0, st>>>(v, sc);
   k_rb_build_half<<<nblk(s->n, 128), 128, 0, st>>>(v, sc, s->slot_rank);
-  k_rb_done<<<1, 1, 0, st>>>(sc, s->dnbl);
+  k_rb_done<<<std::max(1, nblk(s->nsys, 256)), 256, 0, st>>>(sc, s->dnbl, v.sys_rb, s->nsys);
   CK(cudaGetLastError());
   return IMDGPU_OK;
 }
@@ -2121,6 +2195,27 @@ static int read_back(imdgpu_sys *s) {
   CK(cudaStreamSynchronize(s->st));
   s->hsc_valid = true;
   return IMDGPU_OK;
+}
+
+// More ghost room after an overflow: with fixed per-system ranges every
+// system whose ghosts passed its range gets a quarter more than it needed;
+// otherwise the one range grows to a quarter above the count.
+static int grow_ghosts(imdgpu_sys *s, int need, int margin) {
+  if (s->nsys > 0 && !s->h_goff.empty()) {
+    const int ns = s->nsys;
+    std::vector<int> used(ns);
+    CK(cudaMemcpy(used.data(), s->d_gtot, sizeof(int) * ns, cudaMemcpyDeviceToHost));
+    std::vector<int> g(ns + 1, 0);
+    for (int q = 0; q < ns; q++) {
+      int cap = s->h_goff[q + 1] - s->h_goff[q];
+      if (used[q] > cap) cap = (int)(used[q] * 1.25) + 64;
+      g[q + 1] = g[q] + cap;
+    }
+    s->h_goff = g;
+    CK(cudaMemcpy(s->d_goff, g.data(), sizeof(int) * (ns + 1), cudaMemcpyHostToDevice));
+    return alloc_ext(s, g[ns]);
+  }
+  return alloc_ext(s, (int)(need * 1.25) + margin);
 }
 
 // A synchronous rebuild with capacity growth: used for explicit builds and
@@ -2143,7 +2238,7 @@ static int rebuild_sync(imdgpu_sys *s) {
     if (!(stt & (ST_NBOVER | ST_GHOSTOVER))) return IMDGPU_OK;
     if (stt & ST_GHOSTOVER) {
       // positions were permuted already; ghosts only need the larger buffers
-      rc = alloc_ext(s, (int)(cnt[3] * 1.25) + 1024);
+      rc = grow_ghosts(s, cnt[3], 1024);
       if (rc) return rc;
       // the real-atom part of pos lives in the ext array: re-upload via tpos
       CK(cudaMemcpyAsync(s->pos, s->tpos, sizeof(double4) * s->n, cudaMemcpyDeviceToDevice, s->st));
@@ -2352,6 +2447,7 @@ int imdgpu_destroy(imdgpu_sys *s) {
   dfree(s->d_blin); dfree(s->d_bcode); dfree(s->d_cstart); dfree(s->d_ccount);
   dfree(s->d_rcount); dfree(s->d_rstart); dfree(s->d_gstart);
   dfree(s->d_roff); dfree(s->d_boff); dfree(s->d_gtot); dfree(s->d_gbase);
+  dfree(s->d_sys_rb); dfree(s->d_goff); dfree(s->d_rank_sys); dfree(s->d_buf_sys);
   dfree(s->pos); dfree(s->mom); dfree(s->frc); dfree(s->ref); dfree(s->tpos); dfree(s->tmom);
   dfree(s->rho); dfree(s->df); dfree(s->xl); dfree(s->number); dfree(s->orig);
   dfree(s->tnumber); dfree(s->torig); dfree(s->ecell); dfree(s->gowner); dfree(s->gcode);
@@ -4378,6 +4474,15 @@ int imdgpu_set_blocks(imdgpu_sys *s, int block_density, int block_force) {
   return IMDGPU_OK;
 }
 
+int imdgpu_batch_set_partial_rebuild(imdgpu_sys *s, int on) {
+  if (!s) return fail(IMDGPU_ERR_ARG, "null system");
+  if (s->percell_rb != (on ? 1 : 0)) {
+    s->percell_rb = on ? 1 : 0;
+    s->geom_ready = false;  // the ghost layout changes
+  }
+  return IMDGPU_OK;
+}
+
 int imdgpu_batch_set_engine(imdgpu_sys *s, int on) {
   if (!s) return fail(IMDGPU_ERR_ARG, "null system");
   s->bt_engine = on ? 1 : 0;
@@ -4450,7 +4555,9 @@ int imdgpu_batch_advance(imdgpu_sys *s, int max_rounds, int *ndone_out, int *rou
                                   (uintptr_t)s->n, (uintptr_t)s->nsys, (uintptr_t)s->d_cs,
                                   (uintptr_t)s->bt_engine, (uintptr_t)s->d_order,
                                   (uintptr_t)s->pcache, (uintptr_t)s->lpa,
-                                  (uintptr_t)s->bs_rho, (uintptr_t)s->bs_force};
+                                  (uintptr_t)s->bs_rho, (uintptr_t)s->bs_force,
+                                  (uintptr_t)s->percell_rb, (uintptr_t)s->d_goff,
+                                  (uintptr_t)s->gcap};
     if (s->use_graph) {
       if (!B.gx || key != B.gkey) {
         if (B.gx) cudaGraphExecDestroy(B.gx);
@@ -4504,7 +4611,7 @@ int imdgpu_batch_advance(imdgpu_sys *s, int max_rounds, int *ndone_out, int *rou
         break;
       }
       if (s->status_host & ST_GHOSTOVER)
-        if ((rc = alloc_ext(s, (int)(cnt[3] * 1.25) + 4096))) break;
+        if ((rc = grow_ghosts(s, cnt[3], 4096))) break;
       if (s->status_host & ST_NBOVER)
         if ((rc = alloc_list(s, (int)(cnt[1] * 1.25) + 8))) break;
       double4 *back[6] = {s->pos, s->mom, s->oldx, s->cgg, s->cgh, s->frc};

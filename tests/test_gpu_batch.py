@@ -83,6 +83,33 @@ def test_engine_rounds_equal_four_kernel_rounds():
         assert a.shape == b.shape
 
 
+@pytest.mark.parametrize("engine", [True, False])
+def test_partial_rebuilds_relax_like_full_ones(engine):
+    """Per-system rebuilds (fixed ghost ranges, only the cells that moved
+    past skin/2 rebuilt) relax every cell to the energy of whole-batch
+    rebuilds (1e-9 eV/atom) with fewer atoms rebuilt; the lists they keep
+    stay valid because a cell's ghosts and slots do not move."""
+    from imd_gb300 import api
+    from imd_gb300 import workloads as wl
+    rng = np.random.default_rng(11)
+    cells = [wl.defect_cell(rng, nmin=300, nmax=900, nlim=(3, 6)) for _ in range(5)]
+    out = []
+    for partial in (True, False):
+        b = api.GpuBatch(1, api.EAM2)
+        b.read_tables(tables("cu"))
+        b.set_cells(cells)
+        b.set_engine(engine)
+        b.set_partial_rebuild(partial)
+        b.relax(1e-4)
+        out.append(b.results())
+        b.close()
+    ra, rb = out
+    n = np.array([c.n for c in cells])
+    assert (ra["status"] == 0).all() and (rb["status"] == 0).all()
+    assert (ra["fmax"] <= 1e-4).all()
+    assert np.max(np.abs(ra["epot"] - rb["epot"]) / n) <= 1e-9
+
+
 def test_batch_mixed_precision_relaxes():
     from imd_gb300 import api
     from imd_gb300 import workloads as wl
