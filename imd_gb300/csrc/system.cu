@@ -147,6 +147,12 @@ struct imdgpu_sys {
   double *partial = nullptr;
   DevScalars *dsc = nullptr;
   DevScalars *hsc = nullptr;  // pinned mirror
+  // imdgpu_nve_step_host replayed as a CUDA graph: pinned status and build
+  // count, the graph and its key (the caller's buffers among it)
+  unsigned *hstep_status = nullptr;
+  long *hstep_nbl = nullptr;
+  cudaGraphExec_t step_gx = nullptr;
+  std::vector<uintptr_t> step_key;
   bool hsc_valid = false;     // hsc matches the device since the last read_back
   // list statistics of imdgpu_get_scalars, recounted after each build
   long list_stats_build = -1, list_stats_entries = 0;
@@ -2417,7 +2423,9 @@ int imdgpu_create(imdgpu_sys **out, int ntypes, int interaction, int precision) 
   }
   if (dalloc(&s->dsc, 1) != cudaSuccess || dalloc(&s->status, 1) != cudaSuccess ||
       dalloc(&s->counters, 8) != cudaSuccess || dalloc(&s->dnbl, 1) != cudaSuccess ||
-      cudaMallocHost((void **)&s->hsc, sizeof(DevScalars)) != cudaSuccess) {
+      cudaMallocHost((void **)&s->hsc, sizeof(DevScalars)) != cudaSuccess ||
+      cudaMallocHost((void **)&s->hstep_status, sizeof(unsigned)) != cudaSuccess ||
+      cudaMallocHost((void **)&s->hstep_nbl, sizeof(long)) != cudaSuccess) {
     imdgpu_destroy(s);
     return fail(IMDGPU_ERR_NOMEM, "cannot allocate system scalars");
   }
@@ -2475,11 +2483,14 @@ int imdgpu_destroy(imdgpu_sys *s) {
   dfree(s->d_maxd);
   for (auto e : s->sev) cudaEventDestroy(e);
   if (s->gexec) cudaGraphExecDestroy(s->gexec);
+  if (s->step_gx) cudaGraphExecDestroy(s->step_gx);
   if (s->brun) {
     if (s->brun->gx) cudaGraphExecDestroy(s->brun->gx);
     delete s->brun;
   }
   if (s->hsc) cudaFreeHost(s->hsc);
+  if (s->hstep_status) cudaFreeHost(s->hstep_status);
+  if (s->hstep_nbl) cudaFreeHost(s->hstep_nbl);
   if (s->ev_made)
     for (int k = 0; k < 8; k++) cudaEventDestroy(s->ev[k]);
   if (s->st) cudaStreamDestroy(s->st);
@@ -2948,12 +2959,23 @@ static NveMass nve_mass(const imdgpu_sys *s, double dt);
 // on the device: a non-finite value moves no atom and is IMDGPU_ERR_ARG.
 // An overflow of the list or ghost buffers redoes the step from the copied
 // input with grown buffers.
-int imdgpu_nve_step_host(imdgpu_sys *s, const double *x, const double *p, double timestep,
-                         double *x_out, double *p_out, imdgpu_scalars *out) {
-  if (!s || !x || !p) return fail(IMDGPU_ERR_ARG, "null state");
-  if (s->nsys > 0) return fail(IMDGPU_ERR_STATE, "a batch of cells has no NVE step");
-  int rc = prepare(s);
-  if (rc) return rc;
+static std::vector<uintptr_t> graph_key(imdgpu_sys *s, double dt);
+
+static bool pinned(const void *p) {
+  if (!p) return true;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeHost;
+}
+
+// the host step's sequence: the state up and checked, the guarded rebuild,
+// the forces, move_atoms_nve with the displacement test, the state and the
+// scalars down
+static int issue_host_step(imdgpu_sys *s, const double *x, const double *p, double dt,
+                           double *x_out, double *p_out) {
   const size_t n = s->n;
   const double *din_x = s->d_in, *din_p = s->d_in + 3 * n;
   CK(cudaMemcpyAsync(s->d_in, x, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, s->st));
@@ -2963,8 +2985,92 @@ int imdgpu_nve_step_host(imdgpu_sys *s, const double *x, const double *p, double
   k_check_finite<<<nblk(n, 256), 256, 0, s->st>>>(din_x, din_p, (int)n, bad);
   SysView v = view(s);
   k_put_state<<<nblk(n, 256), 256, 0, s->st>>>(v, s->slot_of, din_x, din_p, bad);
+  CK(cudaMemsetAsync(s->status, 0, sizeof(unsigned), s->st));
+  int rc = issue_rebuild(s);
+  if (rc) return rc;
+  launch_forces(v, ftabs(s), s->dsc, s->precision == IMDGPU_MIXED, s->st);
   const int nb = nblk(n, BS_VEC);
-  for (int attempt = 0; attempt < 2; attempt++) {
+  k_nve<<<nb, BS_VEC, 0, s->st>>>(v, dt, nve_mass(s, dt), s->partial, bad);
+  k_finalize_nve<<<1, FIN_BS, 0, s->st>>>(s->partial, nb, s->dsc, v.skin2, nullptr, nullptr);
+  double *ox = s->d_out, *op = s->d_out + 3 * n;
+  k_gather_out<<<nblk(n, 256), 256, 0, s->st>>>(v, x_out ? ox : nullptr, p_out ? op : nullptr,
+                                               nullptr, nullptr, nullptr, nullptr);
+  if (x_out) CK(cudaMemcpyAsync(x_out, ox, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, s->st));
+  if (p_out) CK(cudaMemcpyAsync(p_out, op, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, s->st));
+  CK(cudaMemcpyAsync(s->hsc, s->dsc, sizeof(DevScalars), cudaMemcpyDeviceToHost, s->st));
+  CK(cudaMemcpyAsync(s->hstep_status, s->status, sizeof(unsigned), cudaMemcpyDeviceToHost, s->st));
+  CK(cudaMemcpyAsync(s->hstep_nbl, s->dnbl, sizeof(long), cudaMemcpyDeviceToHost, s->st));
+  return IMDGPU_OK;
+}
+
+// the same step from a captured graph, kept while the buffers and the
+// system's shape stay the same; pinned host buffers only
+static int host_step_graph(imdgpu_sys *s, const double *x, const double *p, double dt,
+                           double *x_out, double *p_out) {
+  std::vector<uintptr_t> key = graph_key(s, dt);
+  for (const void *q : {(const void *)x, (const void *)p, (const void *)x_out, (const void *)p_out})
+    key.push_back((uintptr_t)q);
+  key.push_back((uintptr_t)s->n);
+  if (!s->step_gx || key != s->step_key) {
+    if (s->step_gx) cudaGraphExecDestroy(s->step_gx);
+    s->step_gx = nullptr;
+    cudaGraph_t g;
+    CK(cudaStreamBeginCapture(s->st, cudaStreamCaptureModeThreadLocal));
+    const int rc = issue_host_step(s, x, p, dt, x_out, p_out);
+    const cudaError_t e = cudaStreamEndCapture(s->st, &g);
+    if (rc) return rc;
+    if (e != cudaSuccess) return fail(IMDGPU_ERR_CUDA, std::string("step capture: ") + cudaGetErrorString(e));
+    const cudaError_t ei = cudaGraphInstantiate(&s->step_gx, g, 0);
+    cudaGraphDestroy(g);
+    if (ei != cudaSuccess) return fail(IMDGPU_ERR_CUDA, std::string("step instantiate: ") + cudaGetErrorString(ei));
+    s->step_key = key;
+  }
+  CK(cudaGraphLaunch(s->step_gx, s->st));
+  return IMDGPU_OK;
+}
+
+int imdgpu_nve_step_host(imdgpu_sys *s, const double *x, const double *p, double timestep,
+                         double *x_out, double *p_out, imdgpu_scalars *out) {
+  if (!s || !x || !p) return fail(IMDGPU_ERR_ARG, "null state");
+  if (s->nsys > 0) return fail(IMDGPU_ERR_STATE, "a batch of cells has no NVE step");
+  int rc = prepare(s);
+  if (rc) return rc;
+  const size_t n = s->n;
+  int first = 0;
+  if (s->use_graph && pinned(x) && pinned(p) && pinned(x_out) && pinned(p_out)) {
+    if ((rc = host_step_graph(s, x, p, timestep, x_out, p_out))) return rc;
+    CK(cudaStreamSynchronize(s->st));  // the one synchronisation
+    s->status_host = *s->hstep_status;
+    s->nbl_count_host = *s->hstep_nbl;
+    s->hsc_valid = true;
+    s->nfc++;
+    const bool over = s->status_host & (ST_NBOVER | ST_GHOSTOVER);
+    if (s->hsc->badin < (int)n)
+      return fail(IMDGPU_ERR_ARG, "non-finite position or momentum of atom " +
+                                      std::to_string(s->hsc->badin));
+    if (s->status_host & ST_CELLOVER)
+      return fail(IMDGPU_ERR_CELL, "more than " + std::to_string(CELLCAP) + " atoms in one cell");
+    if (s->status_host & ST_WAIT) return fail(IMDGPU_ERR_CUDA, kWaitMsg);
+    if (!over) {
+      if (out && (rc = fill_scalars(s, out))) return rc;
+      return (s->status_host & ST_SHORT) ? IMDGPU_WARN_SHORT : IMDGPU_OK;
+    }
+    // an overflow: the step again below from the input still on the device
+    // (x may be x_out and hold the discarded result), with grown buffers
+    first = 1;
+  }
+  const double *din_x = s->d_in, *din_p = s->d_in + 3 * n;
+  int *bad = &s->dsc->badin;
+  SysView v = view(s);
+  if (!first) {
+    CK(cudaMemcpyAsync(s->d_in, x, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, s->st));
+    CK(cudaMemcpyAsync(s->d_in + 3 * n, p, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, s->st));
+    CK(cudaMemsetAsync(bad, 0x7f, sizeof(int), s->st));
+    k_check_finite<<<nblk(n, 256), 256, 0, s->st>>>(din_x, din_p, (int)n, bad);
+    k_put_state<<<nblk(n, 256), 256, 0, s->st>>>(v, s->slot_of, din_x, din_p, bad);
+  }
+  const int nb = nblk(n, BS_VEC);
+  for (int attempt = first; attempt < 2; attempt++) {
     CK(cudaMemsetAsync(s->status, 0, sizeof(unsigned), s->st));
     if (attempt == 0) {
       if (!(s->hsc_valid && !s->hsc->rebuild))

@@ -28,8 +28,17 @@ def _system(deterministic=False):
     return s, g
 
 
-@pytest.mark.parametrize("deterministic", [True, False])
-def test_fused_step_equals_separate_calls(deterministic):
+def _buffers(shape, pinned):
+    """Host arrays, page-locked when asked (the captured-graph path of the
+    call needs pinned buffers; pageable ones take the direct launches)."""
+    if not pinned:
+        return np.empty(shape)
+    torch = pytest.importorskip("torch")
+    return torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()
+
+
+@pytest.mark.parametrize("deterministic,pinned", [(True, False), (True, True), (False, True)])
+def test_fused_step_equals_separate_calls(deterministic, pinned):
     a, g = _system(deterministic)
     b, _ = _system(deterministic)
     same = np.testing.assert_array_equal if deterministic else \
@@ -37,8 +46,9 @@ def test_fused_step_equals_separate_calls(deterministic):
     dt = float(g["dt"])
     xa = np.ascontiguousarray(g["x0"], np.float64).copy()
     pa = np.ascontiguousarray(g["p0"], np.float64).copy()
-    xb, pb = xa.copy(), pa.copy()
-    xo, po = np.empty_like(xb), np.empty_like(pb)
+    xb, pb = _buffers(xa.shape, pinned), _buffers(pa.shape, pinned)
+    xb[:], pb[:] = xa, pa
+    xo, po = _buffers(xb.shape, pinned), _buffers(pb.shape, pinned)
     rebuilds = set()
     for k in range(40):
         a.put_state(xa, pa)
@@ -51,7 +61,7 @@ def test_fused_step_equals_separate_calls(deterministic):
             sb = b.nve_step_host(xb, pb, dt, xb, pb)          # in place
         else:
             sb = b.nve_step_host(xb, pb, dt, xo, po)
-            xb, pb = xo.copy(), po.copy()
+            xb[:], pb[:] = xo, po
         same(xb, xa)
         same(pb, pa)
         same(np.array([sb.tot_pot_energy, sb.tot_kin_energy]),
