@@ -129,6 +129,7 @@ struct imdgpu_sys {
   // ghost ranges, the system of every real bin and buffer cell
   int percell_rb = 0;
   int *d_sys_rb = nullptr, *d_goff = nullptr, *d_rank_sys = nullptr, *d_buf_sys = nullptr;
+  int *d_gmax = nullptr;  // per system, the most ghosts any build needed
   std::vector<int> h_goff;
 
   int n = 0, ncap = 0, gcap = 0, nbcap = 0;
@@ -305,8 +306,10 @@ __global__ void k_rb_zero(SysView v, DevScalars *sc, int *rcount) {
   if (flag & RB_ALL || !v.sys_rb)
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < v.nall_cells; c += gridDim.x * blockDim.x)
       v.ccount[c] = 0;
+  // counters[1] (most entries of an atom) is a running maximum over builds:
+  // a chunk of steps or rounds may rebuild again after the build that
+  // overflowed, and the host sizes the list from the largest count seen
   if (blockIdx.x == 0 && threadIdx.x == 0) {
-    v.counters[1] = 0;
     v.counters[2] = 0;
     if (v.goff) v.counters[0] = v.gcap;  // fixed ghost ranges: every slot, unused ones marked
   }
@@ -517,7 +520,7 @@ __global__ void k_rb_ghost_scan(SysView v, DevScalars *sc, int *gstart) {
     v.counters[0] = min(carry, v.gcap);
     if (carry > v.gcap) {
       atomicOr(v.status, ST_GHOSTOVER);
-      v.counters[3] = carry;
+      atomicMax(&v.counters[3], carry);  // the largest need since the host last grew
     }
   }
 }
@@ -551,7 +554,8 @@ __global__ void k_rb_scan_cells_sys(SysView v, DevScalars *sc, const int *roff, 
   if (mx > CELLCAP) atomicOr(v.status, ST_CELLOVER);
 }
 
-__global__ void k_rb_ghost_count_sys(SysView v, DevScalars *sc, const int *boff, int *gtot) {
+__global__ void k_rb_ghost_count_sys(SysView v, DevScalars *sc, const int *boff, int *gtot,
+                                     int *gmax) {
   const int q = blockIdx.x;
   if (!sc->rebuild || !rb_covers(v, sc->rebuild, q)) return;
   int c = 0;
@@ -563,7 +567,10 @@ __global__ void k_rb_ghost_count_sys(SysView v, DevScalars *sc, const int *boff,
   if (threadIdx.x < 32) {
     int x = (threadIdx.x < (blockDim.x >> 5)) ? sh[threadIdx.x] : 0;
     x = __reduce_add_sync(0xffffffffu, x);
-    if (threadIdx.x == 0) gtot[q] = x;
+    if (threadIdx.x == 0) {
+      gtot[q] = x;
+      if (gmax) gmax[q] = max(gmax[q], x);  // the largest need since the host last grew
+    }
   }
 }
 
@@ -577,7 +584,7 @@ __global__ void k_rb_ghost_base(SysView v, DevScalars *sc, const int *gtot, int 
     v.counters[0] = min(total, v.gcap);
     if (total > v.gcap) {
       atomicOr(v.status, ST_GHOSTOVER);
-      v.counters[3] = total;
+      atomicMax(&v.counters[3], total);
     }
   }
 }
@@ -2047,6 +2054,7 @@ static int setup_geometry_batch(imdgpu_sys *s) {
     dfree(s->d_buf_sys);
     dfree(s->d_sys_rb);
     dfree(s->d_goff);
+    dfree(s->d_gmax);
     CK(dalloc(&s->d_rank_sys, rsys.size()));
     CK(dalloc(&s->d_buf_sys, bsys.size()));
     CK(cudaMemcpy(s->d_rank_sys, rsys.data(), sizeof(int) * rsys.size(), cudaMemcpyHostToDevice));
@@ -2063,6 +2071,8 @@ static int setup_geometry_batch(imdgpu_sys *s) {
       }
       CK(dalloc(&s->d_goff, ns + 1));
       CK(dalloc(&s->d_sys_rb, ns));
+      CK(dalloc(&s->d_gmax, ns));
+      CK(cudaMemset(s->d_gmax, 0, sizeof(int) * ns));
       CK(cudaMemcpy(s->d_goff, s->h_goff.data(), sizeof(int) * (ns + 1), cudaMemcpyHostToDevice));
       CK(cudaMemset(s->d_sys_rb, 0, sizeof(int) * ns));
     }
@@ -2180,7 +2190,7 @@ static int issue_rebuild(imdgpu_sys *s) {
                                        s->slot_rank, cg ? s->oldx : nullptr, s->cgg, s->cgh,
                                        s->toldx, s->tcgg, s->tcgh, s->slot_of);
   if (s->nsys > 0) {
-    k_rb_ghost_count_sys<<<s->nsys, 256, 0, st>>>(v, sc, s->d_boff, s->d_gtot);
+    k_rb_ghost_count_sys<<<s->nsys, 256, 0, st>>>(v, sc, s->d_boff, s->d_gtot, s->d_gmax);
     if (!v.goff) k_rb_ghost_base<<<1, 1024, 0, st>>>(v, sc, s->d_gtot, s->d_gbase, s->nsys);
     k_rb_ghost_scan_sys<<<s->nsys, 1024, 0, st>>>(v, sc, s->d_boff, s->d_gbase, s->d_gstart);
   } else {
@@ -2210,7 +2220,7 @@ static int grow_ghosts(imdgpu_sys *s, int need, int margin) {
   if (s->nsys > 0 && !s->h_goff.empty()) {
     const int ns = s->nsys;
     std::vector<int> used(ns);
-    CK(cudaMemcpy(used.data(), s->d_gtot, sizeof(int) * ns, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(used.data(), s->d_gmax, sizeof(int) * ns, cudaMemcpyDeviceToHost));
     std::vector<int> g(ns + 1, 0);
     for (int q = 0; q < ns; q++) {
       int cap = s->h_goff[q + 1] - s->h_goff[q];
@@ -2456,6 +2466,7 @@ int imdgpu_destroy(imdgpu_sys *s) {
   dfree(s->d_rcount); dfree(s->d_rstart); dfree(s->d_gstart);
   dfree(s->d_roff); dfree(s->d_boff); dfree(s->d_gtot); dfree(s->d_gbase);
   dfree(s->d_sys_rb); dfree(s->d_goff); dfree(s->d_rank_sys); dfree(s->d_buf_sys);
+  dfree(s->d_gmax);
   dfree(s->pos); dfree(s->mom); dfree(s->frc); dfree(s->ref); dfree(s->tpos); dfree(s->tmom);
   dfree(s->rho); dfree(s->df); dfree(s->xl); dfree(s->number); dfree(s->orig);
   dfree(s->tnumber); dfree(s->torig); dfree(s->ecell); dfree(s->gowner); dfree(s->gcode);

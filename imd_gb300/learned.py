@@ -209,6 +209,9 @@ class Trainer:
 
     def _batch(self, gc, t):
         b = make_batch(self.tables, gc, interpolation=self.interpolation)
+        # training needs rho and the pairs, not fast forces: no 32-byte
+        # per-entry pair cache beside every resident group's list
+        b.set_pair_cache(False)
         if self.core_weight > 0.0:
             core = np.sqrt(np.sum(t * t, axis=1)) >= self.core_disp
             b.ml_set_loss_weights(1.0 + self.core_weight * core)
