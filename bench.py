@@ -60,7 +60,8 @@ PAIR_BYTES_PER_ATOM = 88.0        # both pair passes: x (24) in, rho (8) out; x,
 # memory), the partner's F' (4)
 MIXED_L1_BYTES_PER_ENTRY = 72.0
 NCU_L1TEX_MIXED_FORCE = 0.628     # l1tex throughput, % of peak (committed ncu profile)
-NCU_FP64_PIPE_FORCE = 0.835       # FP64 pipe busy of k_force_fast (committed ncu profile)
+NCU_FP64_PIPE_FORCE = 0.786       # FP64 pipe busy of k_force_cache (committed ncu profile)
+NCU_FP64_PIPE_DENSITY = 0.848     # FP64 pipe busy of k_density_cache (committed ncu profile)
 STEP_BYTES_PER_ATOM = 232.0       # whole NVE EAM step, canonical count
 FLOPS_PER_PAIR = 66.0             # canonical FP64 flops per half-list pair within rc
 
@@ -516,7 +517,8 @@ def run_ours(args, rank, world, local):
                      "flops_per_launch": pair_flops,
                      "flops_per_pair": FLOPS_PER_PAIR,
                      "ms_density": dens_ms, "ms_force": force_ms,
-                     "ncu_fp64_pipe_busy": NCU_FP64_PIPE_FORCE,
+                     "ncu_fp64_pipe_busy": {"k_density_cache": NCU_FP64_PIPE_DENSITY,
+                                            "k_force_cache": NCU_FP64_PIPE_FORCE},
                      "hbm": {"achieved": hbm_alg, "peak": hbm_peak, "unit": "GB/s",
                              "frac": hbm_alg / hbm_peak, "peak_kind": peak_kind,
                              "bytes_per_atom": PAIR_BYTES_PER_ATOM,

@@ -5099,8 +5099,12 @@ int imdgpu_batch_ml_start(imdgpu_sys *s, int *used, double *e_start, double *e_p
   int rc = batch_full(s);
   if (rc) return rc;
   if (s->brun) {
-    // a batch relaxation was begun on these cells: they may be marked done
+    // a batch relaxation was begun on these cells: they may be marked done,
+    // and the list builds skipped finished cells, so every list is rebuilt
     CK(cudaMemset(s->d_sys_done, 0, sizeof(int) * s->nsys));
+    int one = RB_ALL;
+    CK(cudaMemcpy(&s->dsc->rebuild, &one, sizeof(int), cudaMemcpyHostToDevice));
+    s->hsc_valid = false;
   }
   rc = ml_prepare_pairs(s);  // forces, rho and the list at the start positions
   if (rc) return rc;

@@ -87,12 +87,15 @@ def test_engine_rounds_equal_four_kernel_rounds():
 def test_partial_rebuilds_relax_like_full_ones(engine):
     """Per-system rebuilds (fixed ghost ranges, only the cells that moved
     past skin/2 rebuilt) relax every cell to the energy of whole-batch
-    rebuilds (1e-9 eV/atom) with fewer atoms rebuilt; the lists they keep
-    stay valid because a cell's ghosts and slots do not move."""
+    rebuilds (1e-8 eV/atom, the bar of the compaction test: the force
+    passes' FP64 atomics let two runs' CG paths part in the last bits); the
+    lists they keep stay valid because a cell's ghosts and slots do not
+    move.  The final positions' energies are checked against the oracle."""
     from imd_gb300 import api
     from imd_gb300 import workloads as wl
     rng = np.random.default_rng(11)
     cells = [wl.defect_cell(rng, nmin=300, nmax=900, nlim=(3, 6)) for _ in range(5)]
+    from oracle import OracleSystem
     out = []
     for partial in (True, False):
         b = api.GpuBatch(1, api.EAM2)
@@ -102,12 +105,19 @@ def test_partial_rebuilds_relax_like_full_ones(engine):
         b.set_partial_rebuild(partial)
         b.relax(1e-4)
         out.append(b.results())
+        if partial:
+            xs = b.positions()
         b.close()
     ra, rb = out
+    for k, c in enumerate(cells):  # the reported energy is the final positions' energy
+        o = OracleSystem(c.box, xs[k], c.types, c.mass, c.number, 1, tables("cu"), True, 0.4)
+        o.calc_forces()
+        assert abs(o.epot_total - ra["epot"][k]) <= 1e-10 * abs(o.epot_total), k
     n = np.array([c.n for c in cells])
-    assert (ra["status"] == 0).all() and (rb["status"] == 0).all()
+    assert (ra["status"] == 0).all(), ra["status"]
+    assert (rb["status"] == 0).all(), rb["status"]
     assert (ra["fmax"] <= 1e-4).all()
-    assert np.max(np.abs(ra["epot"] - rb["epot"]) / n) <= 1e-9
+    assert np.max(np.abs(ra["epot"] - rb["epot"]) / n) <= 1e-8
 
 
 def test_batch_mixed_precision_relaxes():
