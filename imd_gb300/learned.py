@@ -10,9 +10,10 @@ the host-side sequencing only:
    its cell's box;
 2. training: Adam on the per-pair MLP (imdgpu_ml_train_step: the project's
    own forward, backward and Adam kernels), one step per group of
-   `batch_cells` cells; each group stays resident as one GpuBatch with its
-   atoms at the unrelaxed positions, and the model's weights and Adam state
-   move between the groups' handles;
+   `batch_cells` cells; each group is one GpuBatch with its atoms at the
+   unrelaxed positions, kept on the device when the training set is small
+   enough and uploaded for its step otherwise, and the model's weights and
+   Adam state move between the groups' handles;
 3. use: imdgpu_batch_ml_start moves every cell to its predicted start where
    that lowers the cell's energy, and the plain batched CG finishes every
    cell to the same force tolerance.
@@ -261,7 +262,7 @@ class Trainer:
 def main(argv=None):
     """python -m imd_gb300.learned [--cells 512] [--seed 6] [--rounds 0]
     [--weights imd_gb300/data/start_mlp.npz] [--engine 1] [--pair-cache 1]
-    [--partial-rebuild 0]
+    [--partial-rebuild 1]
 
     Relax a batch of the defect-cell workload (Sutton-Chen Cu, spline tables)
     with the batched CG, from the learned start when --weights is given, and
@@ -280,7 +281,7 @@ def main(argv=None):
     ap.add_argument("--weights", default=None)
     ap.add_argument("--engine", type=int, default=1)
     ap.add_argument("--pair-cache", type=int, default=1)
-    ap.add_argument("--partial-rebuild", type=int, default=0)
+    ap.add_argument("--partial-rebuild", type=int, default=1)
     a = ap.parse_args(argv)
     tabs = wl.sutton_chen_tables(os.path.join(tempfile.mkdtemp(prefix="imdrelax"), "cu"),
                                  [wl.CU])

@@ -411,7 +411,7 @@ int imdgpu_batch_set_autotune(imdgpu_sys *sys, int on);
  * runs in one persistent kernel whose resident blocks take cells largest
  * first (default 1); 0 runs it as four kernels, with the same arithmetic. */
 int imdgpu_batch_set_engine(imdgpu_sys *sys, int on);
-/* Per-system rebuilds (default 0): every cell of the batch gets a fixed
+/* Per-system rebuilds (default 1): every cell of the batch gets a fixed
  * ghost range with head-room, and a round rebuilds the lists of the cells
  * that moved past skin/2 only, instead of the whole batch. */
 int imdgpu_batch_set_partial_rebuild(imdgpu_sys *sys, int on);
