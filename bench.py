@@ -381,6 +381,7 @@ def run_ours(args, rank, world, local):
             continue
         s = build(prec)
         blocks = s.autotune()   # density / force block shapes, outside the timed steps
+        blocks = (blocks[0], blocks[1], s.tile())  # and the lanes per atom
         s.nve_run(max(args.warmup, 3), dt, record=False)
         s.set_profiling(True)
         s.set_l2_flush(256 << 20)
@@ -498,7 +499,8 @@ def run_ours(args, rank, world, local):
                    "parallelism": "replicas" if world > 1 else "single",
                    "l2": "256 MiB scratch write between timed steps (outside the windows)",
                    "list_entries": r["nb"], "rebuilds_in_timed_steps": r["rebuilds"],
-                   "autotuned_blocks": {"density": r["blocks"][0], "force": r["blocks"][1]}},
+                   "autotuned_blocks": {"density": r["blocks"][0], "force": r["blocks"][1],
+                                        "lanes_per_atom": r["blocks"][2]}},
         "clocks": r["clocks"],
         "e2e": {"value": e2e, "unit": "atom-steps/s", "h2d_bytes_per_step": 48 * n,
                 "d2h_bytes_per_step": 48 * n + 16, "steps": e2e_steps,
@@ -574,7 +576,8 @@ def run_ours(args, rank, world, local):
                                                  "integrate": m["ms_integrate"] / args.steps,
                                                  "rebuild": m["ms_rebuild"] / args.steps},
                          "rebuilds_in_timed_steps": m["rebuilds"],
-                         "autotuned_blocks": {"density": m["blocks"][0], "force": m["blocks"][1]},
+                         "autotuned_blocks": {"density": m["blocks"][0], "force": m["blocks"][1],
+                                              "lanes_per_atom": m["blocks"][2]},
                          "graph_replay_wall": m["graph_rate"],
                          "energy_drift_per_atom": float((m["etot"][-1] - m["etot"][0]) / n),
                          "vs_fp64": prec, "roofline": mixed_roof, "clocks": m["clocks"]}

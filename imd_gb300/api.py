@@ -121,6 +121,7 @@ def lib() -> C.CDLL:
                                           C.POINTER(C.c_long)]
         L.imdgpu_set_graphs.argtypes = [vp, C.c_int]
         L.imdgpu_set_table_staging.argtypes = [vp, C.c_int]
+        L.imdgpu_get_tile.argtypes = [vp, C.POINTER(C.c_int)]
         L.imdgpu_set_pair_cache.argtypes = [vp, C.c_int]
         L.imdgpu_set_interpolation.argtypes = [vp, C.c_int]
         L.imdgpu_set_table2.argtypes = [vp, C.c_int, C.c_int, C.c_int, _dp]
@@ -609,6 +610,12 @@ class GpuSystem:
         bf = C.c_int(0)
         _check(lib().imdgpu_autotune(self.h, C.byref(bd), C.byref(bf)), "autotune")
         return bd.value, bf.value
+
+    def tile(self) -> int:
+        """Lanes per atom the autotuner chose (imdgpu_get_tile)."""
+        t = C.c_int(0)
+        _check(lib().imdgpu_get_tile(self.h, C.byref(t)), "get_tile")
+        return t.value
 
     def set_blocks(self, density: int, force: int) -> None:
         _check(lib().imdgpu_set_blocks(self.h, int(density), int(force)), "set_blocks")

@@ -22,6 +22,7 @@ struct ForceTabs {
   int stage_grid;       // >0: the force pass stages them in shared memory, this many blocks
   int cache;            // FP64: the density pass caches per-entry pair terms for the force pass
   int lpa;              // lanes per atom of the cached passes (1, 2, 4)
+  int mixed_lpa;        // lanes per atom of the mixed density pass (1, 2, 4; one species)
 };
 
 // Device-side scalars of one system (results + control).

@@ -64,11 +64,14 @@ __device__ __forceinline__ float polyf_g(const DevTable &t, int col, int k, floa
 
 // loop 1's EAM branch over the half list (src/imd_forces_nbl.c:586-611):
 // rho_{it,jt}(r) to atom i, rho_{jt,it}(r) to atom j
-template <bool NT1>
+template <bool NT1, int LPA>
 __global__ void __launch_bounds__(BS_FORCE_MAX) k_density_mixed(SysView v, DevTable rho,
                                                             const SplitPos *sp) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= v.n || atom_idle(v, i)) return;
+  // LPA lanes per atom (the autotuner's tile): lane q takes the entries
+  // q, q + LPA, ... and the lanes' FP64 sums meet in a shuffle tree
+  const long gid = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = (int)(gid / LPA), q = (int)(gid % LPA);
+  if (i >= v.n || atom_idle(v, i)) return;  // the whole lane group alike
   const SplitPos a = sp[i];
   const int it = NT1 ? 0 : __float_as_int(a.hi.w), nt = v.ntypes;
   const int nn = v.nnb[i];
@@ -76,7 +79,7 @@ __global__ void __launch_bounds__(BS_FORCE_MAX) k_density_mixed(SysView v, DevTa
   bool shortf = false;
   const uint32_t *__restrict__ nb = v.nbr + i;
 #pragma unroll 4
-  for (int k = 0; k < nn; k++) {
+  for (int k = q; k < nn; k += LPA) {
     const int j = (int)(__ldg(nb + (size_t)k * v.ncap) & NB_MASK);
     const SplitPos b = ldsp(&sp[j]);
     const float dx = (b.hi.x - a.hi.x) + (b.lo.x - a.lo.x);
@@ -105,7 +108,13 @@ __global__ void __launch_bounds__(BS_FORCE_MAX) k_density_mixed(SysView v, DevTa
       }
     }
   }
-  atomicAdd(&v.rho[i], r.value());
+  double ri = r.value();
+  if (LPA > 1) {
+    const unsigned g = ((1u << LPA) - 1u) << ((threadIdx.x & 31) & ~(LPA - 1));
+#pragma unroll
+    for (int o = 1; o < LPA; o <<= 1) ri += __shfl_xor_sync(g, ri, o);
+  }
+  if (q == 0) atomicAdd(&v.rho[i], ri);
   if (shortf) flag_short(v, i);
 }
 
@@ -405,8 +414,12 @@ int launch_forces_mixed(const SysView &v, const ForceTabs &t, DevScalars *sc, cu
   if (t.eam) {
     cudaMemsetAsync(v.rho, 0, ext * sizeof(double), st);
     if (ev) cudaEventRecord(ev[0], st);
-    if (t.nt1) k_density_mixed<true><<<nbr, t.bs_rho, 0, st>>>(v, t.rho, sp);
-    else k_density_mixed<false><<<nbr, t.bs_rho, 0, st>>>(v, t.rho, sp);
+    const int lpa = t.mixed_lpa;
+    const int nbl = nblk((long)v.n * lpa, t.bs_rho);
+    if (t.nt1 && lpa == 4) k_density_mixed<true, 4><<<nbl, t.bs_rho, 0, st>>>(v, t.rho, sp);
+    else if (t.nt1 && lpa == 2) k_density_mixed<true, 2><<<nbl, t.bs_rho, 0, st>>>(v, t.rho, sp);
+    else if (t.nt1) k_density_mixed<true, 1><<<nbr, t.bs_rho, 0, st>>>(v, t.rho, sp);
+    else k_density_mixed<false, 1><<<nbr, t.bs_rho, 0, st>>>(v, t.rho, sp);
     if (ev) cudaEventRecord(ev[1], st);
     fold_rho_launch(v, gblocks, st);
     k_embed_mixed<<<nbe, BS_VEC, 0, st>>>(v, t.embed, sp, pe);

@@ -1691,6 +1691,7 @@ static ForceTabs ftabs(imdgpu_sys *s) {
   t.samegrid = same_grid(s);
   t.cache = cache_wanted(s) && s->pcache && s->pcache_entries == (size_t)s->nbcap * s->ncap;
   t.lpa = s->lpa;
+  t.mixed_lpa = (s->precision == IMDGPU_MIXED && s->ntypes == 1) ? s->lpa : 1;
   return t;
 }
 
@@ -2366,8 +2367,9 @@ static int autotune_forces(imdgpu_sys *s, int force, bool tile_only = false) {
     }
     (which == 0 ? s->bs_rho : s->bs_force) = best;
   }
-  // the tile of the cached FP64 passes: lanes per atom, at the chosen blocks
-  if (ftabs(s).cache) {
+  // the tile: lanes per atom of the cached FP64 passes or of the mixed
+  // density pass, at the chosen blocks
+  if (ftabs(s).cache || (mixed && s->ntypes == 1)) {
     float best_ms = 1e30f;
     int best = 1;
     for (int l : {1, 2, 4}) {
@@ -4576,6 +4578,12 @@ int imdgpu_autotune(imdgpu_sys *s, int *block_density, int *block_force) {
   if ((rc = autotune_forces(s, 1))) return rc;
   if (block_density) *block_density = s->bs_rho;
   if (block_force) *block_force = s->bs_force;
+  return IMDGPU_OK;
+}
+
+int imdgpu_get_tile(imdgpu_sys *s, int *lanes_per_atom) {
+  if (!s || !lanes_per_atom) return fail(IMDGPU_ERR_ARG, "null");
+  *lanes_per_atom = s->lpa;
   return IMDGPU_OK;
 }
 

@@ -405,6 +405,10 @@ int imdgpu_get_pairs(imdgpu_sys *sys, long cap, int *ni, int *nj, int *shift,
  * (multiples of 32, at most 128). */
 int imdgpu_autotune(imdgpu_sys *sys, int *block_density, int *block_force);
 int imdgpu_set_blocks(imdgpu_sys *sys, int block_density, int block_force);
+/* The tile the autotuner chose besides the blocks: lanes per atom (1, 2 or
+ * 4) of the FP64 pair passes with the pair cache and of the mixed density
+ * pass of one species. */
+int imdgpu_get_tile(imdgpu_sys *sys, int *lanes_per_atom);
 int imdgpu_batch_set_autotune(imdgpu_sys *sys, int on);
 /* A batch round's CG work (the sums of the last evaluation, the control of
  * every cell, the move and set_hg of its atoms, the list displacement test)
