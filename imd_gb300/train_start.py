@@ -2,7 +2,7 @@
 
     python -m imd_gb300.train_start [--train-cells 2048] [--epochs 20]
         [--batch-cells 64] [--lr 1e-3] [--out imd_gb300/data/start_mlp.npz]
-        [--eval-cells 512] [--relax-chunk 512] [--start-iters 1]
+        [--eval-cells 512] [--relax-chunk 512] [--start-iters 1] [--max-mean-disp2 0]
 
 Training cells come from the batched-relaxation generator with seed 5, held-out
 cells with seed 6 (single-species Sutton-Chen Cu, 1-4 vacancies or <100>
@@ -35,18 +35,30 @@ from imd_gb300 import learned, workloads as wl  # noqa: E402
 DEFAULT_OUT = os.path.join(HERE, "data", "start_mlp.npz")
 
 
-def relax_targets(tabs, cells, chunk: int = 512):
-    """Plain batched CG of `cells` in batches of `chunk`; displacement targets."""
+def relax_targets(tabs, cells, chunk: int = 512, max_mean_disp2: float = 0.0):
+    """Plain batched CG of `cells` in batches of `chunk`; displacement targets.
+    A cell whose mean squared displacement exceeds max_mean_disp2 (A^2; 0:
+    no limit) gives no target; every batch's record names its cells with the
+    largest targets (index, atoms, mean |d|^2, max |d|, |mean d|, force calls)."""
     disp, stats = [], []
     for c0 in range(0, len(cells), chunk):
         part = cells[c0:c0 + chunk]
         r = learned.relax(tabs, part, keep_positions=True)
         # cells that did not relax (status != 0) give no target
         d = learned.targets(part, r.positions)
-        disp += [d[k] if r.status[k] == 0 else None for k in range(len(part))]
+        m2 = np.array([float(np.mean(np.sum(x * x, axis=1))) for x in d])
+        keep = (r.status == 0) & ((m2 <= max_mean_disp2) if max_mean_disp2 > 0 else True)
+        disp += [d[k] if keep[k] else None for k in range(len(part))]
+        top = np.argsort(-np.where(r.status == 0, m2, -1.0))[:8]
         stats.append({"cells": len(part), "seconds": r.seconds, "rounds": r.rounds,
                       "nfc_mean": float(r.nfc.mean()),
-                      "status": np.bincount(r.status, minlength=5).tolist()})
+                      "status": np.bincount(r.status, minlength=5).tolist(),
+                      "mean_disp2_cells": float(m2[r.status == 0].mean()),
+                      "dropped_large": int(((r.status == 0) & ~keep).sum()),
+                      "largest": [[int(c0 + k), int(part[k].n), float(m2[k]),
+                                   float(np.sqrt(np.max(np.sum(d[k] ** 2, axis=1)))),
+                                   float(np.linalg.norm(d[k].mean(axis=0))), int(r.nfc[k])]
+                                  for k in top]})
         print("relaxed %d/%d cells: %.1f s, %d rounds, %.0f force calls per cell"
               % (c0 + len(part), len(cells), r.seconds, r.rounds, r.nfc.mean()), flush=True)
     return disp, stats
@@ -98,6 +110,8 @@ def main(argv=None):
     ap.add_argument("--core-disp", type=float, default=0.2)
     ap.add_argument("--relax-chunk", type=int, default=512,
                     help="training cells relaxed per batch when making the targets")
+    ap.add_argument("--max-mean-disp2", type=float, default=0.0,
+                    help="drop cells whose mean squared target exceeds this (A^2; 0: keep all)")
     ap.add_argument("--start-iters", type=int, default=1,
                     help="also evaluate the learned start applied this many times")
     a = ap.parse_args(argv)
@@ -105,7 +119,7 @@ def main(argv=None):
     tabs = wl.sutton_chen_tables(os.path.join(tmp, "cu"), [wl.CU])
     t0 = time.perf_counter()
     train = wl.defect_batch(a.train_cells, seed=5)
-    disp, relax_stats = relax_targets(tabs, train, a.relax_chunk)
+    disp, relax_stats = relax_targets(tabs, train, a.relax_chunk, a.max_mean_disp2)
     train = [c for c, d in zip(train, disp) if d is not None]
     disp = [d for d in disp if d is not None]
     t_data = time.perf_counter() - t0
