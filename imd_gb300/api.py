@@ -187,6 +187,8 @@ def lib() -> C.CDLL:
         L.imdgpu_batch_set_autotune.argtypes = [vp, C.c_int]
         L.imdgpu_batch_set_engine.argtypes = [vp, C.c_int]
         L.imdgpu_batch_set_partial_rebuild.argtypes = [vp, C.c_int]
+        L.imdgpu_batch_set_list_headroom.argtypes = [vp, C.c_double]
+        L.imdgpu_batch_replays.argtypes = [vp, C.POINTER(C.c_long)]
         L.imdgpu_batch_positions.argtypes = [vp, _dp]
         fp = C.POINTER(C.c_float)
         L.imdgpu_ml_nparam.argtypes = []
@@ -719,6 +721,17 @@ class GpuBatch(GpuSystem):
         """A round's CG work in one persistent kernel (default on) or in four
         kernels (imdgpu_batch_set_engine)."""
         _check(lib().imdgpu_batch_set_engine(self.h, int(bool(on))), "batch_set_engine")
+
+    def set_list_headroom(self, factor: float) -> None:
+        """List capacity over the largest count at a build (default 1.3)."""
+        _check(lib().imdgpu_batch_set_list_headroom(self.h, float(factor)),
+               "batch_set_list_headroom")
+
+    def replays(self) -> int:
+        """Chunks of rounds replayed after an overflow since begin()."""
+        n = C.c_long(0)
+        _check(lib().imdgpu_batch_replays(self.h, C.byref(n)), "batch_replays")
+        return n.value
 
     def set_partial_rebuild(self, on: bool) -> None:
         """Rebuild the lists of the cells that moved only, each cell with a

@@ -70,6 +70,7 @@ struct BatchRun {
   std::vector<char> have_final;
   std::vector<double> final_x;       // 3 per atom of imdgpu_batch_set_cells
   int ndone_base = 0;                // finished cells no longer on the device
+  long replays = 0;                  // chunks of rounds replayed after a list or ghost overflow
   int compactions = 0;
 };
 
@@ -188,6 +189,7 @@ struct imdgpu_sys {
   CgSys *d_cs = nullptr;
   unsigned long long *d_maxd = nullptr;
   int *d_order = nullptr, *d_queue = nullptr;  // cells largest first; the engine's work counter
+  double list_headroom = 1.3;  // batch list capacity over the largest count at a build
   double4 *pcache = nullptr;                   // per list entry: the density pass's pair terms
   size_t pcache_entries = 0;
   int pair_cache = 1;                          // imdgpu_set_pair_cache
@@ -4372,8 +4374,9 @@ static int batch_repack(imdgpu_sys *s, const std::vector<char> &keep) {
   {
     int cnt[4];
     CK(cudaMemcpy(cnt, s->counters, sizeof cnt, cudaMemcpyDeviceToHost));
-    if (s->nbcap < (int)(cnt[1] * 1.3) + 8) {
-      if ((rc = alloc_list(s, (int)(cnt[1] * 1.3) + 8))) return rc;
+    const int want = (int)(cnt[1] * s->list_headroom) + 8;
+    if (s->nbcap < want) {
+      if ((rc = alloc_list(s, want))) return rc;
       if ((rc = rebuild_sync(s))) return rc;
     }
   }
@@ -4534,8 +4537,9 @@ int imdgpu_batch_begin(imdgpu_sys *s, double fmax, int maxsteps) {
   {
     int cnt[4];
     CK(cudaMemcpy(cnt, s->counters, sizeof cnt, cudaMemcpyDeviceToHost));
-    if (s->nbcap < (int)(cnt[1] * 1.3) + 8) {
-      if ((rc = alloc_list(s, (int)(cnt[1] * 1.3) + 8))) return rc;
+    const int want = (int)(cnt[1] * s->list_headroom) + 8;
+    if (s->nbcap < want) {
+      if ((rc = alloc_list(s, want))) return rc;
       if ((rc = rebuild_sync(s))) return rc;
     }
   }
@@ -4605,6 +4609,19 @@ int imdgpu_batch_set_partial_rebuild(imdgpu_sys *s, int on) {
     s->percell_rb = on ? 1 : 0;
     s->geom_ready = false;  // the ghost layout changes
   }
+  return IMDGPU_OK;
+}
+
+int imdgpu_batch_set_list_headroom(imdgpu_sys *s, double factor) {
+  if (!s) return fail(IMDGPU_ERR_ARG, "null system");
+  if (!(factor >= 1.0 && factor <= 4.0)) return fail(IMDGPU_ERR_ARG, "headroom outside [1, 4]");
+  s->list_headroom = factor;
+  return IMDGPU_OK;
+}
+
+int imdgpu_batch_replays(imdgpu_sys *s, long *n) {
+  if (!s || !n) return fail(IMDGPU_ERR_ARG, "null");
+  *n = s->brun ? s->brun->replays : 0;
   return IMDGPU_OK;
 }
 
@@ -4722,6 +4739,7 @@ int imdgpu_batch_advance(imdgpu_sys *s, int max_rounds, int *ndone_out, int *rou
       break;
     }
     if (s->status_host & (ST_NBOVER | ST_GHOSTOVER)) {
+      B.replays++;
       // eight overflows of one chunk of rounds in a row: the growth does not
       // converge (the count resets with every chunk that completes)
       int cnt[4];
@@ -4749,6 +4767,12 @@ int imdgpu_batch_advance(imdgpu_sys *s, int max_rounds, int *ndone_out, int *rou
       CKR(cudaMemcpy(s->d_ndone, bnd, sizeof(int), cudaMemcpyDeviceToDevice));
       CKR(cudaMemcpy(s->d_cs, bcs, sizeof(CgSys) * ns, cudaMemcpyDeviceToDevice));
       if ((rc = rebuild_sync(s))) break;
+      // the build moved positions, momenta and the CG vectors to new slots;
+      // the last forces, which the next round's sums and set_hg / reset read,
+      // follow them there: snapshot slot -> caller index -> new slot
+      k_gather4<<<nblk(n, 256), 256, 0, s->st>>>(b4[5], borig, (int)n, b4[0]);
+      k_scatter4<<<nblk(n, 256), 256, 0, s->st>>>(b4[0], s->slot_of, (int)n, s->frc);
+      CKR(cudaGetLastError());
       continue;
     }
     B.ndone = B.ndone_base + nd;

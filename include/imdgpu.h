@@ -419,6 +419,13 @@ int imdgpu_batch_set_engine(imdgpu_sys *sys, int on);
  * ghost range with head-room, and a round rebuilds the lists of the cells
  * that moved past skin/2 only, instead of the whole batch. */
 int imdgpu_batch_set_partial_rebuild(imdgpu_sys *sys, int on);
+/* List capacity of a batch at imdgpu_batch_begin and after a compaction:
+ * factor x the most entries an atom has (default 1.3, within [1, 4]).  A
+ * chunk of rounds that overflows the list or the ghosts is replayed from
+ * its start with grown buffers; imdgpu_batch_replays counts those replays
+ * since imdgpu_batch_begin. */
+int imdgpu_batch_set_list_headroom(imdgpu_sys *sys, double factor);
+int imdgpu_batch_replays(imdgpu_sys *sys, long *n);
 
 /* Timing of the dominant kernels of the last nve_run (device ms, CUDA
  * events on the system's stream). */

@@ -124,6 +124,37 @@ def test_partial_rebuilds_relax_like_full_ones(engine):
     assert np.max(np.abs(ra["epot"] - rb["epot"])[both] / n[both]) <= 1e-8
 
 
+def test_overflow_replays_keep_the_relaxation():
+    """A list with no head-room overflows as the cells relax; each overflow
+    replays its chunk of rounds from the snapshot with a grown list.  The
+    replayed rounds must continue the same relaxation: the last forces,
+    which the next round's CG sums and directions read, move with the atoms
+    to their new slots.  Every cell ends at the energy of a run without
+    replays (1e-8 eV/atom) and no atom ends far from where it started."""
+    from imd_gb300 import api, learned
+    from imd_gb300 import workloads as wl
+    rng = np.random.default_rng(17)
+    cells = [wl.defect_cell(rng, nmin=300, nmax=1200, nlim=(3, 7)) for _ in range(8)]
+    out = []
+    for headroom in (1.0, 1.3):
+        b = api.GpuBatch(1, api.EAM2)
+        b.read_tables(tables("cu"))
+        b.set_cells(cells)
+        b.set_list_headroom(headroom)
+        b.relax(1e-4, max_rounds=100_000)
+        out.append((b.results(), b.positions(), b.replays()))
+        b.close()
+    (ra, xa, na), (rb, xb, nb) = out
+    assert na > 0, "no overflow was replayed"
+    n = np.array([c.n for c in cells])
+    both = (ra["status"] == 0) & (rb["status"] == 0)
+    assert both.sum() >= len(cells) - 1, (ra["status"], rb["status"])
+    assert np.max(np.abs(ra["epot"] - rb["epot"])[both] / n[both]) <= 1e-8
+    for c, x in zip(cells, xa):
+        d = learned.min_image(x - c.x, np.asarray(c.box))
+        assert np.max(np.sqrt(np.sum(d * d, axis=1))) < 6.0
+
+
 def test_batch_mixed_precision_relaxes():
     from imd_gb300 import api
     from imd_gb300 import workloads as wl
