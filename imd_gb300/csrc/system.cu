@@ -128,7 +128,7 @@ struct imdgpu_sys {
   int *d_roff = nullptr, *d_boff = nullptr, *d_gtot = nullptr, *d_gbase = nullptr;
   // per-system rebuilds (imdgpu_batch_set_partial_rebuild): flags, fixed
   // ghost ranges, the system of every real bin and buffer cell
-  int percell_rb = 1;
+  int percell_rb = 0;
   int *d_sys_rb = nullptr, *d_goff = nullptr, *d_rank_sys = nullptr, *d_buf_sys = nullptr;
   int *d_gmax = nullptr;  // per system, the most ghosts any build needed
   std::vector<int> h_goff;

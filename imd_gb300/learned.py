@@ -262,7 +262,7 @@ class Trainer:
 def main(argv=None):
     """python -m imd_gb300.learned [--cells 512] [--seed 6] [--rounds 0]
     [--weights imd_gb300/data/start_mlp.npz] [--engine 1] [--pair-cache 1]
-    [--partial-rebuild 1]
+    [--partial-rebuild 0]
 
     Relax a batch of the defect-cell workload (Sutton-Chen Cu, spline tables)
     with the batched CG, from the learned start when --weights is given, and
@@ -281,7 +281,7 @@ def main(argv=None):
     ap.add_argument("--weights", default=None)
     ap.add_argument("--engine", type=int, default=1)
     ap.add_argument("--pair-cache", type=int, default=1)
-    ap.add_argument("--partial-rebuild", type=int, default=1)
+    ap.add_argument("--partial-rebuild", type=int, default=0)
     a = ap.parse_args(argv)
     tabs = wl.sutton_chen_tables(os.path.join(tempfile.mkdtemp(prefix="imdrelax"), "cu"),
                                  [wl.CU])

@@ -415,9 +415,12 @@ int imdgpu_batch_set_autotune(imdgpu_sys *sys, int on);
  * runs in one persistent kernel whose resident blocks take cells largest
  * first (default 1); 0 runs it as four kernels, with the same arithmetic. */
 int imdgpu_batch_set_engine(imdgpu_sys *sys, int on);
-/* Per-system rebuilds (default 1): every cell of the batch gets a fixed
+/* Per-system rebuilds (default 0): every cell of the batch gets a fixed
  * ghost range with head-room, and a round rebuilds the lists of the cells
- * that moved past skin/2 only, instead of the whole batch. */
+ * that moved past skin/2 only, instead of the whole batch.  Known defect:
+ * after a chunk of rounds is replayed following an overflow, part of the
+ * cells continue with their atoms' CG vectors out of step with the atoms;
+ * they relax to the right energies with the atoms relabelled. */
 int imdgpu_batch_set_partial_rebuild(imdgpu_sys *sys, int on);
 /* List capacity of a batch at imdgpu_batch_begin and after a compaction:
  * factor x the most entries an atom has (default 1.3, within [1, 4]).  A
