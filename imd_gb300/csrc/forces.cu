@@ -68,8 +68,12 @@ __global__ void __launch_bounds__(BS_FORCE_MAX) k_density64(SysView v, DevTable 
 __global__ void k_fold_rho(SysView v) {
   const int ng = v.counters[0];
   for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < ng; g += gridDim.x * blockDim.x) {
-    const double r = v.rho[v.n + g];  // zero in unused slots
-    if (r != 0.0) atomicAdd(&v.rho[v.gowner[g]], r);
+    // an unused slot of a system's ghost range is normally zero, but the
+    // lists of a system that overflowed its range reach into the next
+    // range's unused slots until the overflow is replayed: skip them
+    const int o = v.gowner[g];
+    const double r = v.rho[v.n + g];
+    if (r != 0.0 && o >= 0) atomicAdd(&v.rho[o], r);
   }
 }
 
@@ -175,8 +179,9 @@ __global__ void k_fold_force(SysView v) {
   const int ng = v.counters[0];
   for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < ng; g += gridDim.x * blockDim.x) {
     const double4 f = v.frc[v.n + g];
-    if (f.x != 0.0 || f.y != 0.0 || f.z != 0.0 || f.w != 0.0) {
-      double *o = &v.frc[v.gowner[g]].x;
+    const int own = v.gowner[g];  // -1: an unused slot (see k_fold_rho)
+    if (own >= 0 && (f.x != 0.0 || f.y != 0.0 || f.z != 0.0 || f.w != 0.0)) {
+      double *o = &v.frc[own].x;
       atomicAdd(o + 0, f.x);
       atomicAdd(o + 1, f.y);
       atomicAdd(o + 2, f.z);

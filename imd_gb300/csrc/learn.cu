@@ -55,6 +55,7 @@ __global__ void k_ml_pairs(SysView v, MlPair *pairs, int cap, int *count) {
     const float r2 = dx * dx + dy * dy + dz * dz;
     if (r2 >= ML_RC * ML_RC) continue;
     const int jo = (j >= v.n) ? v.gowner[j - v.n] : j;
+    if (jo < 0) continue;  // an unused ghost slot (only after a range overflow)
     const int at = atomicAdd(count, 2);
     if (at + 1 < cap) {
       pairs[at] = MlPair{i, dx, dy, dz};
