@@ -189,6 +189,7 @@ def lib() -> C.CDLL:
         L.imdgpu_batch_set_partial_rebuild.argtypes = [vp, C.c_int]
         L.imdgpu_batch_set_list_headroom.argtypes = [vp, C.c_double]
         L.imdgpu_batch_replays.argtypes = [vp, C.POINTER(C.c_long)]
+        L.imdgpu_batch_inject_replays.argtypes = [vp, C.c_int, C.c_int]
         L.imdgpu_batch_positions.argtypes = [vp, _dp]
         fp = C.POINTER(C.c_float)
         L.imdgpu_ml_nparam.argtypes = []
@@ -732,6 +733,13 @@ class GpuBatch(GpuSystem):
         n = C.c_long(0)
         _check(lib().imdgpu_batch_replays(self.h, C.byref(n)), "batch_replays")
         return n.value
+
+    def inject_replays(self, every: int, count: int) -> None:
+        """Test hook: after every `every` completed chunks the next chunk is
+        replayed from its snapshot as after an overflow, `count` times in all
+        (imdgpu_batch_inject_replays; call after begin())."""
+        _check(lib().imdgpu_batch_inject_replays(self.h, int(every), int(count)),
+               "batch_inject_replays")
 
     def set_partial_rebuild(self, on: bool) -> None:
         """Rebuild the lists of the cells that moved only, each cell with a

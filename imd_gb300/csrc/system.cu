@@ -54,6 +54,24 @@ static void dfree(T *&p) {
   p = nullptr;
 }
 
+// Transfers and fills on a system's stream.  The stream is created
+// non-blocking, so the legacy default stream (plain cudaMemcpy, cudaMemset)
+// is not ordered with the kernels on it: a device-to-device copy or a fill
+// issued there returns before it has run, and a kernel issued next on the
+// stream may read the memory while it is being written (the snapshot a
+// batch restores after an overflow, read by the rebuild that follows it).
+// These run after everything issued on the stream before them and return
+// when the work is done, like the blocking calls they replace.
+static cudaError_t scopy(cudaStream_t st, void *dst, const void *src, size_t bytes,
+                         cudaMemcpyKind kind) {
+  const cudaError_t e = cudaMemcpyAsync(dst, src, bytes, kind, st);
+  return e != cudaSuccess ? e : cudaStreamSynchronize(st);
+}
+static cudaError_t sset(cudaStream_t st, void *p, int value, size_t bytes) {
+  const cudaError_t e = cudaMemsetAsync(p, value, bytes, st);
+  return e != cudaSuccess ? e : cudaStreamSynchronize(st);
+}
+
 // state of a batched relaxation in progress
 struct BatchRun {
   CgParams P;
@@ -72,6 +90,9 @@ struct BatchRun {
   int ndone_base = 0;                // finished cells no longer on the device
   long replays = 0;                  // chunks of rounds replayed after a list or ghost overflow
   int compactions = 0;
+  // replays forced from the host (imdgpu_batch_inject_replays): after every
+  // inject_every completed chunks the next one is replayed, inject_left times
+  int inject_every = 0, inject_left = 0, inject_ok = 0;
 };
 
 // ---------------------------------------------------------------------------
@@ -1856,16 +1877,16 @@ static int setup_geometry(imdgpu_sys *s) {
   CK(dalloc(&s->d_rcount, s->nreal_cells));
   CK(dalloc(&s->d_rstart, s->nreal_cells));
   CK(dalloc(&s->d_gstart, s->nbuf));
-  CK(cudaMemcpy(s->d_cell_rank, cell_rank.data(), sizeof(int) * s->nall_cells, cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(s->d_rank_lin, rank_lin.data(), sizeof(int) * s->nreal_cells, cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(s->d_hshell, hshell.data(), sizeof(int) * hshell.size(), cudaMemcpyHostToDevice));
+  CK(scopy(s->st, s->d_cell_rank, cell_rank.data(), sizeof(int) * s->nall_cells, cudaMemcpyHostToDevice));
+  CK(scopy(s->st, s->d_rank_lin, rank_lin.data(), sizeof(int) * s->nreal_cells, cudaMemcpyHostToDevice));
+  CK(scopy(s->st, s->d_hshell, hshell.data(), sizeof(int) * hshell.size(), cudaMemcpyHostToDevice));
   if (s->nbuf) {
-    CK(cudaMemcpy(s->d_bsrc, bsrc.data(), sizeof(int) * s->nbuf, cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(s->d_blin, blin.data(), sizeof(int) * s->nbuf, cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(s->d_bcode, bcode.data(), sizeof(int) * s->nbuf, cudaMemcpyHostToDevice));
+    CK(scopy(s->st, s->d_bsrc, bsrc.data(), sizeof(int) * s->nbuf, cudaMemcpyHostToDevice));
+    CK(scopy(s->st, s->d_blin, blin.data(), sizeof(int) * s->nbuf, cudaMemcpyHostToDevice));
+    CK(scopy(s->st, s->d_bcode, bcode.data(), sizeof(int) * s->nbuf, cudaMemcpyHostToDevice));
   }
-  CK(cudaMemset(s->d_ccount, 0, sizeof(int) * s->nall_cells));
-  CK(cudaMemset(s->d_cstart, 0, sizeof(int) * s->nall_cells));
+  CK(sset(s->st, s->d_ccount, 0, sizeof(int) * s->nall_cells));
+  CK(sset(s->st, s->d_cstart, 0, sizeof(int) * s->nall_cells));
   s->geom_ready = true;
   return IMDGPU_OK;
 }
@@ -2025,18 +2046,18 @@ static int setup_geometry_batch(imdgpu_sys *s) {
   CK(dalloc(&s->d_aoff, ns + 1));
   CK(dalloc(&s->d_sbox, 9 * (size_t)ns));
   CK(dalloc(&s->d_stbox, 9 * (size_t)ns));
-  CK(cudaMemcpy(s->d_cell_rank, cell_rank.data(), sizeof(int) * cell_rank.size(), cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(s->d_rank_lin, rank_lin.data(), sizeof(int) * rank_lin.size(), cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(s->d_hshell, hshell.data(), sizeof(int) * hshell.size(), cudaMemcpyHostToDevice));
+  CK(scopy(s->st, s->d_cell_rank, cell_rank.data(), sizeof(int) * cell_rank.size(), cudaMemcpyHostToDevice));
+  CK(scopy(s->st, s->d_rank_lin, rank_lin.data(), sizeof(int) * rank_lin.size(), cudaMemcpyHostToDevice));
+  CK(scopy(s->st, s->d_hshell, hshell.data(), sizeof(int) * hshell.size(), cudaMemcpyHostToDevice));
   if (s->nbuf) {
-    CK(cudaMemcpy(s->d_bsrc, bsrc.data(), sizeof(int) * s->nbuf, cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(s->d_blin, blin.data(), sizeof(int) * s->nbuf, cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(s->d_bcode, bcode.data(), sizeof(int) * s->nbuf, cudaMemcpyHostToDevice));
+    CK(scopy(s->st, s->d_bsrc, bsrc.data(), sizeof(int) * s->nbuf, cudaMemcpyHostToDevice));
+    CK(scopy(s->st, s->d_blin, blin.data(), sizeof(int) * s->nbuf, cudaMemcpyHostToDevice));
+    CK(scopy(s->st, s->d_bcode, bcode.data(), sizeof(int) * s->nbuf, cudaMemcpyHostToDevice));
   }
-  CK(cudaMemcpy(s->d_sgdim, gdim.data(), sizeof(int) * gdim.size(), cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(s->d_scdim, cdim.data(), sizeof(int) * cdim.size(), cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(s->d_scoff, coff.data(), sizeof(int) * ns, cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(s->d_aoff, s->h_aoff.data(), sizeof(int) * (ns + 1), cudaMemcpyHostToDevice));
+  CK(scopy(s->st, s->d_sgdim, gdim.data(), sizeof(int) * gdim.size(), cudaMemcpyHostToDevice));
+  CK(scopy(s->st, s->d_scdim, cdim.data(), sizeof(int) * cdim.size(), cudaMemcpyHostToDevice));
+  CK(scopy(s->st, s->d_scoff, coff.data(), sizeof(int) * ns, cudaMemcpyHostToDevice));
+  CK(scopy(s->st, s->d_aoff, s->h_aoff.data(), sizeof(int) * (ns + 1), cudaMemcpyHostToDevice));
   dfree(s->d_roff);
   dfree(s->d_boff);
   dfree(s->d_gtot);
@@ -2045,8 +2066,8 @@ static int setup_geometry_batch(imdgpu_sys *s) {
   CK(dalloc(&s->d_boff, ns + 1));
   CK(dalloc(&s->d_gtot, ns));
   CK(dalloc(&s->d_gbase, ns));
-  CK(cudaMemcpy(s->d_roff, roff.data(), sizeof(int) * (ns + 1), cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(s->d_boff, boff.data(), sizeof(int) * (ns + 1), cudaMemcpyHostToDevice));
+  CK(scopy(s->st, s->d_roff, roff.data(), sizeof(int) * (ns + 1), cudaMemcpyHostToDevice));
+  CK(scopy(s->st, s->d_boff, boff.data(), sizeof(int) * (ns + 1), cudaMemcpyHostToDevice));
   {
     std::vector<int> rsys(s->nreal_cells), bsys(std::max(1, s->nbuf), 0);
     for (int q = 0; q < ns; q++) {
@@ -2060,8 +2081,8 @@ static int setup_geometry_batch(imdgpu_sys *s) {
     dfree(s->d_gmax);
     CK(dalloc(&s->d_rank_sys, rsys.size()));
     CK(dalloc(&s->d_buf_sys, bsys.size()));
-    CK(cudaMemcpy(s->d_rank_sys, rsys.data(), sizeof(int) * rsys.size(), cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(s->d_buf_sys, bsys.data(), sizeof(int) * bsys.size(), cudaMemcpyHostToDevice));
+    CK(scopy(s->st, s->d_rank_sys, rsys.data(), sizeof(int) * rsys.size(), cudaMemcpyHostToDevice));
+    CK(scopy(s->st, s->d_buf_sys, bsys.data(), sizeof(int) * bsys.size(), cudaMemcpyHostToDevice));
     s->h_goff.clear();
     if (s->percell_rb) {
       // each system's ghost range: its buffer cells times its atoms per real
@@ -2075,9 +2096,9 @@ static int setup_geometry_batch(imdgpu_sys *s) {
       CK(dalloc(&s->d_goff, ns + 1));
       CK(dalloc(&s->d_sys_rb, ns));
       CK(dalloc(&s->d_gmax, ns));
-      CK(cudaMemset(s->d_gmax, 0, sizeof(int) * ns));
-      CK(cudaMemcpy(s->d_goff, s->h_goff.data(), sizeof(int) * (ns + 1), cudaMemcpyHostToDevice));
-      CK(cudaMemset(s->d_sys_rb, 0, sizeof(int) * ns));
+      CK(sset(s->st, s->d_gmax, 0, sizeof(int) * ns));
+      CK(scopy(s->st, s->d_goff, s->h_goff.data(), sizeof(int) * (ns + 1), cudaMemcpyHostToDevice));
+      CK(sset(s->st, s->d_sys_rb, 0, sizeof(int) * ns));
     }
   }
   {
@@ -2091,12 +2112,12 @@ static int setup_geometry_batch(imdgpu_sys *s) {
     dfree(s->d_queue);
     CK(dalloc(&s->d_order, ns));
     CK(dalloc(&s->d_queue, 1));
-    CK(cudaMemcpy(s->d_order, ord.data(), sizeof(int) * ns, cudaMemcpyHostToDevice));
+    CK(scopy(s->st, s->d_order, ord.data(), sizeof(int) * ns, cudaMemcpyHostToDevice));
   }
-  CK(cudaMemcpy(s->d_sbox, s->h_boxes.data(), sizeof(double) * 9 * ns, cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(s->d_stbox, tb.data(), sizeof(double) * 9 * ns, cudaMemcpyHostToDevice));
-  CK(cudaMemset(s->d_ccount, 0, sizeof(int) * s->nall_cells));
-  CK(cudaMemset(s->d_cstart, 0, sizeof(int) * s->nall_cells));
+  CK(scopy(s->st, s->d_sbox, s->h_boxes.data(), sizeof(double) * 9 * ns, cudaMemcpyHostToDevice));
+  CK(scopy(s->st, s->d_stbox, tb.data(), sizeof(double) * 9 * ns, cudaMemcpyHostToDevice));
+  CK(sset(s->st, s->d_ccount, 0, sizeof(int) * s->nall_cells));
+  CK(sset(s->st, s->d_cstart, 0, sizeof(int) * s->nall_cells));
   s->geom_ready = true;
   return IMDGPU_OK;
 }
@@ -2119,9 +2140,9 @@ static int alloc_ext(imdgpu_sys *s, int gcap) {
   CK(dalloc(&s->ecell, ext));
   CK(dalloc(&s->gowner, (size_t)gcap));
   CK(dalloc(&s->gcode, (size_t)gcap));
-  CK(cudaMemset(s->frc, 0, ext * sizeof(double4)));
-  CK(cudaMemset(s->rho, 0, ext * sizeof(double)));
-  CK(cudaMemset(s->df, 0, ext * sizeof(double)));
+  CK(sset(s->st, s->frc, 0, ext * sizeof(double4)));
+  CK(sset(s->st, s->rho, 0, ext * sizeof(double)));
+  CK(sset(s->st, s->df, 0, ext * sizeof(double)));
   s->gcap = gcap;
   return IMDGPU_OK;
 }
@@ -2223,7 +2244,7 @@ static int grow_ghosts(imdgpu_sys *s, int need, int margin) {
   if (s->nsys > 0 && !s->h_goff.empty()) {
     const int ns = s->nsys;
     std::vector<int> used(ns);
-    CK(cudaMemcpy(used.data(), s->d_gmax, sizeof(int) * ns, cudaMemcpyDeviceToHost));
+    CK(scopy(s->st, used.data(), s->d_gmax, sizeof(int) * ns, cudaMemcpyDeviceToHost));
     std::vector<int> g(ns + 1, 0);
     for (int q = 0; q < ns; q++) {
       int cap = s->h_goff[q + 1] - s->h_goff[q];
@@ -2231,7 +2252,7 @@ static int grow_ghosts(imdgpu_sys *s, int need, int margin) {
       g[q + 1] = g[q] + cap;
     }
     s->h_goff = g;
-    CK(cudaMemcpy(s->d_goff, g.data(), sizeof(int) * (ns + 1), cudaMemcpyHostToDevice));
+    CK(scopy(s->st, s->d_goff, g.data(), sizeof(int) * (ns + 1), cudaMemcpyHostToDevice));
     return alloc_ext(s, g[ns]);
   }
   return alloc_ext(s, (int)(need * 1.25) + margin);
@@ -2282,14 +2303,14 @@ static int prepare(imdgpu_sys *s) {
     int nbcap, gcap;
     estimate_caps(s, nbcap, gcap);
     // keep the real-atom part of pos across the (re)allocation of ext arrays
-    CK(cudaMemcpy(s->tpos, s->pos, sizeof(double4) * s->n, cudaMemcpyDeviceToDevice));
+    CK(scopy(s->st, s->tpos, s->pos, sizeof(double4) * s->n, cudaMemcpyDeviceToDevice));
     rc = alloc_ext(s, gcap);
     if (rc) return rc;
-    CK(cudaMemcpy(s->pos, s->tpos, sizeof(double4) * s->n, cudaMemcpyDeviceToDevice));
+    CK(scopy(s->st, s->pos, s->tpos, sizeof(double4) * s->n, cudaMemcpyDeviceToDevice));
     rc = alloc_list(s, nbcap);
     if (rc) return rc;
     int one = 1;
-    CK(cudaMemcpy(&s->dsc->rebuild, &one, sizeof(int), cudaMemcpyHostToDevice));
+    CK(scopy(s->st, &s->dsc->rebuild, &one, sizeof(int), cudaMemcpyHostToDevice));
     s->hsc_valid = false;
   }
   return IMDGPU_OK;
@@ -2443,10 +2464,10 @@ int imdgpu_create(imdgpu_sys **out, int ntypes, int interaction, int precision) 
     imdgpu_destroy(s);
     return fail(IMDGPU_ERR_NOMEM, "cannot allocate system scalars");
   }
-  cudaMemset(s->dsc, 0, sizeof(DevScalars));
-  cudaMemset(s->status, 0, sizeof(unsigned));
-  cudaMemset(s->counters, 0, 8 * sizeof(int));
-  cudaMemset(s->dnbl, 0, sizeof(long));
+  sset(s->st, s->dsc, 0, sizeof(DevScalars));
+  sset(s->st, s->status, 0, sizeof(unsigned));
+  sset(s->st, s->counters, 0, 8 * sizeof(int));
+  sset(s->st, s->dnbl, 0, sizeof(long));
   memset(s->hsc, 0, sizeof(DevScalars));
   *out = s;
   return IMDGPU_OK;
@@ -2529,7 +2550,7 @@ int imdgpu_set_precision(imdgpu_sys *s, int precision) {
       // the two paths use different lists (half vs full): rebuild on next use
       s->geom_ready = false;
       int one = 1;
-      CK(cudaMemcpy(&s->dsc->rebuild, &one, sizeof(int), cudaMemcpyHostToDevice));
+      CK(scopy(s->st, &s->dsc->rebuild, &one, sizeof(int), cudaMemcpyHostToDevice));
       s->hsc_valid = false;
     }
   }
@@ -2551,7 +2572,7 @@ int imdgpu_set_deterministic(imdgpu_sys *s, int on) {
     if (s->geom_ready && s->precision == IMDGPU_FP64) {
       s->geom_ready = false;
       int one = 1;
-      CK(cudaMemcpy(&s->dsc->rebuild, &one, sizeof(int), cudaMemcpyHostToDevice));
+      CK(scopy(s->st, &s->dsc->rebuild, &one, sizeof(int), cudaMemcpyHostToDevice));
       s->hsc_valid = false;
     }
   }
@@ -2584,7 +2605,7 @@ static int build_fused(imdgpu_sys *s) {
     f[2 * k + 1] = make_float4(pg.y, rg.x, rg.y, 0.f);
   }
   CK(dalloc(&s->dfused, f.size()));
-  CK(cudaMemcpy(s->dfused, f.data(), f.size() * sizeof(float4), cudaMemcpyHostToDevice));
+  CK(scopy(s->st, s->dfused, f.data(), f.size() * sizeof(float4), cudaMemcpyHostToDevice));
   s->fused_bytes = (unsigned)(f.size() * sizeof(float4));
   s->fused_grid = mixed_staged_grid(s->fused_bytes);
   return IMDGPU_OK;
@@ -2674,13 +2695,13 @@ static int upload_table(imdgpu_sys *s, int which, HostTable &t) {
   CK(dalloc(&s->dcgn[which], cgn.size()));
   CK(dalloc(&s->dcvf[which], cvf.size()));
   CK(dalloc(&s->dcgf[which], cgf.size()));
-  CK(cudaMemcpy(s->dtri[which], tri.data(), tri.size() * sizeof(double4), cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(s->dtrif[which], trif.data(), trif.size() * sizeof(float4), cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(s->dcv[which], cv.data(), cv.size() * sizeof(double4), cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(s->dcg[which], cg.data(), cg.size() * sizeof(double4), cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(s->dcgn[which], cgn.data(), cgn.size() * sizeof(double4), cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(s->dcvf[which], cvf.data(), cvf.size() * sizeof(float4), cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(s->dcgf[which], cgf.data(), cgf.size() * sizeof(float4), cudaMemcpyHostToDevice));
+  CK(scopy(s->st, s->dtri[which], tri.data(), tri.size() * sizeof(double4), cudaMemcpyHostToDevice));
+  CK(scopy(s->st, s->dtrif[which], trif.data(), trif.size() * sizeof(float4), cudaMemcpyHostToDevice));
+  CK(scopy(s->st, s->dcv[which], cv.data(), cv.size() * sizeof(double4), cudaMemcpyHostToDevice));
+  CK(scopy(s->st, s->dcg[which], cg.data(), cg.size() * sizeof(double4), cudaMemcpyHostToDevice));
+  CK(scopy(s->st, s->dcgn[which], cgn.data(), cgn.size() * sizeof(double4), cudaMemcpyHostToDevice));
+  CK(scopy(s->st, s->dcvf[which], cvf.data(), cvf.size() * sizeof(float4), cudaMemcpyHostToDevice));
+  CK(scopy(s->st, s->dcgf[which], cgf.data(), cgf.size() * sizeof(float4), cudaMemcpyHostToDevice));
   DevTable &d = s->dtab[which];
   memset(&d, 0, sizeof d);
   d.ncols = t.ncols;
@@ -2817,7 +2838,7 @@ int imdgpu_set_atoms(imdgpu_sys *s, int n, const int *number, const int *type,
     CK(dalloc(&s->slot_rank, n));
     CK(dalloc(&s->nnb, n));
     CK(dalloc(&s->nnb2, n));
-    CK(cudaMemset(s->nnb2, 0, sizeof(int) * (size_t)n));
+    CK(sset(s->st, s->nnb2, 0, sizeof(int) * (size_t)n));
     // block partials: the largest user is the deterministic force pass, two
     // per block of four lanes per atom at 32 lanes per block
     CK(dalloc(&s->partial, 8 * (size_t)nblk(n, 64) + 2 * (size_t)nblk(4L * n, 32) + 64));
@@ -2839,7 +2860,7 @@ int imdgpu_set_atoms(imdgpu_sys *s, int n, const int *number, const int *type,
   CK(dalloc(&dn, n));
   CK(dalloc(&dt, n));
   if (p) CK(dalloc(&dp, 3 * (size_t)n));
-  CK(cudaMemcpy(dx, x, sizeof(double) * 3 * n, cudaMemcpyHostToDevice));
+  CK(scopy(s->st, dx, x, sizeof(double) * 3 * n, cudaMemcpyHostToDevice));
   {
     int seen[MAXT] = {0, 0, 0, 0};
     s->type_mass_uniform = 1;
@@ -2853,10 +2874,10 @@ int imdgpu_set_atoms(imdgpu_sys *s, int n, const int *number, const int *type,
       }
     }
   }
-  CK(cudaMemcpy(dm, mass, sizeof(double) * n, cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(dn, number, sizeof(int) * n, cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(dt, type, sizeof(int) * n, cudaMemcpyHostToDevice));
-  if (p) CK(cudaMemcpy(dp, p, sizeof(double) * 3 * n, cudaMemcpyHostToDevice));
+  CK(scopy(s->st, dm, mass, sizeof(double) * n, cudaMemcpyHostToDevice));
+  CK(scopy(s->st, dn, number, sizeof(int) * n, cudaMemcpyHostToDevice));
+  CK(scopy(s->st, dt, type, sizeof(int) * n, cudaMemcpyHostToDevice));
+  if (p) CK(scopy(s->st, dp, p, sizeof(double) * 3 * n, cudaMemcpyHostToDevice));
   SysView v = view(s);
   k_scatter_in<<<nblk(n, 256), 256, 0, s->st>>>(v, dx, dp, dn, dt, dm);
   k_iota<<<nblk(n, 256), 256, 0, s->st>>>(s->slot_of, n);
@@ -2870,7 +2891,7 @@ int imdgpu_set_atoms(imdgpu_sys *s, int n, const int *number, const int *type,
   s->atoms_set = true;
   s->ml_wt_host.clear();
   int one = 1;
-  CK(cudaMemcpy(&s->dsc->rebuild, &one, sizeof(int), cudaMemcpyHostToDevice));
+  CK(scopy(s->st, &s->dsc->rebuild, &one, sizeof(int), cudaMemcpyHostToDevice));
   s->hsc_valid = false;
   return IMDGPU_OK;
 }
@@ -2933,7 +2954,7 @@ static int fill_scalars(imdgpu_sys *s, imdgpu_scalars *o) {
   const bool fresh = s->list_stats_build == s->nbl_count_host && s->list_stats_n == s->n &&
                      s->list_stats_cap == s->nbcap;
   int *cnt = s->list_stats_cnt;
-  if (!fresh) CK(cudaMemcpy(cnt, s->counters, 4 * sizeof(int), cudaMemcpyDeviceToHost));
+  if (!fresh) CK(scopy(s->st, cnt, s->counters, 4 * sizeof(int), cudaMemcpyDeviceToHost));
   memset(o, 0, sizeof *o);
   o->tot_pot_energy = s->hsc->epot;
   o->virial = s->hsc->virial;
@@ -2952,7 +2973,7 @@ static int fill_scalars(imdgpu_sys *s, imdgpu_scalars *o) {
     long total = 0;
     if (s->atoms_set && s->nbcap > 0) {
       std::vector<int> nn(s->n);
-      CK(cudaMemcpy(nn.data(), s->nnb, sizeof(int) * s->n, cudaMemcpyDeviceToHost));
+      CK(scopy(s->st, nn.data(), s->nnb, sizeof(int) * s->n, cudaMemcpyDeviceToHost));
       for (int v : nn) total += v;
     }
     s->list_stats_entries = total;
@@ -3188,7 +3209,7 @@ int imdgpu_check_nblist(imdgpu_sys *s) {
 int imdgpu_deallocate_nblist(imdgpu_sys *s) {
   if (!s) return fail(IMDGPU_ERR_ARG, "null system");
   int one = 1;
-  CK(cudaMemcpy(&s->dsc->rebuild, &one, sizeof(int), cudaMemcpyHostToDevice));
+  CK(scopy(s->st, &s->dsc->rebuild, &one, sizeof(int), cudaMemcpyHostToDevice));
   s->hsc_valid = false;
   return IMDGPU_OK;
 }
@@ -3828,7 +3849,7 @@ int imdgpu_nve_run(imdgpu_sys *s, int nsteps, double dt, double *epot, double *e
   }
   if (s->l2flush_bytes > 0 && !s->flushbuf) CK(dalloc(&s->flushbuf, (size_t)s->l2flush_bytes));
   long nbl0 = 0;
-  CK(cudaMemcpy(&nbl0, s->dnbl, sizeof(long), cudaMemcpyDeviceToHost));
+  CK(scopy(s->st, &nbl0, s->dnbl, sizeof(long), cudaMemcpyDeviceToHost));
   s->timing = imdgpu_timing();
   // snapshot for replay after an overflow
   double4 *bpos = nullptr, *bmom = nullptr;
@@ -3878,7 +3899,7 @@ int imdgpu_nve_run(imdgpu_sys *s, int nsteps, double dt, double *epot, double *e
       CK(cudaMemcpyAsync(s->orig, borig, sizeof(int) * s->n, cudaMemcpyDeviceToDevice, s->st));
       CK(cudaMemcpyAsync(s->tpos, bpos, sizeof(double4) * s->n, cudaMemcpyDeviceToDevice, s->st));
       int cnt[4];
-      CK(cudaMemcpy(cnt, s->counters, sizeof cnt, cudaMemcpyDeviceToHost));
+      CK(scopy(s->st, cnt, s->counters, sizeof cnt, cudaMemcpyDeviceToHost));
       if (s->status_host & ST_GHOSTOVER) {
         rc = alloc_ext(s, (int)(cnt[3] * 1.25) + 1024);
         if (rc) break;
@@ -3915,7 +3936,7 @@ int imdgpu_nve_run(imdgpu_sys *s, int nsteps, double dt, double *epot, double *e
   s->timing.kernel_launches = launches;
   s->nfc += nsteps;
   std::vector<double> h(2 * (size_t)nsteps);
-  if (nsteps) CK(cudaMemcpy(h.data(), s->hist, sizeof(double) * 2 * nsteps, cudaMemcpyDeviceToHost));
+  if (nsteps) CK(scopy(s->st, h.data(), s->hist, sizeof(double) * 2 * nsteps, cudaMemcpyDeviceToHost));
   for (int k = 0; k < nsteps; k++) {
     if (epot) epot[k] = h[2 * k];
     if (ekin) ekin[k] = h[2 * k + 1];
@@ -4255,13 +4276,13 @@ static int batch_load(imdgpu_sys *s, int ncells, const int *natoms, const double
   dfree(s->d_sys_short);
   CK(dalloc(&s->d_atom_sys, asys.size()));
   CK(dalloc(&s->d_sys_short, ncells));
-  CK(cudaMemset(s->d_sys_short, 0, sizeof(int) * ncells));
+  CK(sset(s->st, s->d_sys_short, 0, sizeof(int) * ncells));
   CK(dalloc(&s->d_sys_done, ncells));
   CK(dalloc(&s->d_ndone, 1));
   CK(dalloc(&s->d_cs, ncells));
   CK(dalloc(&s->d_maxd, ncells));
-  CK(cudaMemcpy(s->d_atom_sys, asys.data(), sizeof(int) * asys.size(), cudaMemcpyHostToDevice));
-  CK(cudaMemset(s->d_sys_done, 0, sizeof(int) * ncells));
+  CK(scopy(s->st, s->d_atom_sys, asys.data(), sizeof(int) * asys.size(), cudaMemcpyHostToDevice));
+  CK(sset(s->st, s->d_sys_done, 0, sizeof(int) * ncells));
   return IMDGPU_OK;
 }
 
@@ -4279,8 +4300,8 @@ static int batch_repack(imdgpu_sys *s, const std::vector<char> &keep) {
   std::vector<CgSys> cs(ns);
   std::vector<int> done(ns);
   CK(cudaStreamSynchronize(s->st));
-  CK(cudaMemcpy(cs.data(), s->d_cs, sizeof(CgSys) * ns, cudaMemcpyDeviceToHost));
-  CK(cudaMemcpy(done.data(), s->d_sys_done, sizeof(int) * ns, cudaMemcpyDeviceToHost));
+  CK(scopy(s->st, cs.data(), s->d_cs, sizeof(CgSys) * ns, cudaMemcpyDeviceToHost));
+  CK(scopy(s->st, done.data(), s->d_sys_done, sizeof(int) * ns, cudaMemcpyDeviceToHost));
   // pos, old_x, g, h, forces of every atom, by its index in the device batch
   std::vector<double4> hv[5];
   {
@@ -4359,21 +4380,21 @@ static int batch_repack(imdgpu_sys *s, const std::vector<char> &keep) {
   if ((rc = ensure_cg(s))) return rc;
   const int nn = s->n;
   // before the first build the device slot of every atom is its index
-  CK(cudaMemcpy(s->oldx, nv[0].data(), sizeof(double4) * nn, cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(s->cgg, nv[1].data(), sizeof(double4) * nn, cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(s->cgh, nv[2].data(), sizeof(double4) * nn, cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(s->d_cs, ncs.data(), sizeof(CgSys) * nc, cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(s->d_sys_done, ndone.data(), sizeof(int) * nc, cudaMemcpyHostToDevice));
+  CK(scopy(s->st, s->oldx, nv[0].data(), sizeof(double4) * nn, cudaMemcpyHostToDevice));
+  CK(scopy(s->st, s->cgg, nv[1].data(), sizeof(double4) * nn, cudaMemcpyHostToDevice));
+  CK(scopy(s->st, s->cgh, nv[2].data(), sizeof(double4) * nn, cudaMemcpyHostToDevice));
+  CK(scopy(s->st, s->d_cs, ncs.data(), sizeof(CgSys) * nc, cudaMemcpyHostToDevice));
+  CK(scopy(s->st, s->d_sys_done, ndone.data(), sizeof(int) * nc, cudaMemcpyHostToDevice));
   int nd = 0;
   for (int v : ndone) nd += v;
-  CK(cudaMemcpy(s->d_ndone, &nd, sizeof(int), cudaMemcpyHostToDevice));
+  CK(scopy(s->st, s->d_ndone, &nd, sizeof(int), cudaMemcpyHostToDevice));
   int one = 1;
-  CK(cudaMemcpy(&s->dsc->rebuild, &one, sizeof(int), cudaMemcpyHostToDevice));
+  CK(scopy(s->st, &s->dsc->rebuild, &one, sizeof(int), cudaMemcpyHostToDevice));
   s->hsc_valid = false;
   if ((rc = rebuild_sync(s))) return rc;
   {
     int cnt[4];
-    CK(cudaMemcpy(cnt, s->counters, sizeof cnt, cudaMemcpyDeviceToHost));
+    CK(scopy(s->st, cnt, s->counters, sizeof cnt, cudaMemcpyDeviceToHost));
     const int want = (int)(cnt[1] * s->list_headroom) + 8;
     if (s->nbcap < want) {
       if ((rc = alloc_list(s, want))) return rc;
@@ -4385,7 +4406,7 @@ static int batch_repack(imdgpu_sys *s, const std::vector<char> &keep) {
   {
     double4 *tmp = nullptr;
     CK(dalloc(&tmp, nn));
-    CK(cudaMemcpy(tmp, nv[3].data(), sizeof(double4) * nn, cudaMemcpyHostToDevice));
+    CK(scopy(s->st, tmp, nv[3].data(), sizeof(double4) * nn, cudaMemcpyHostToDevice));
     k_scatter4<<<nblk(nn, 256), 256, 0, s->st>>>(tmp, s->slot_of, nn, s->frc);
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(s->st));
@@ -4521,22 +4542,22 @@ int imdgpu_batch_begin(imdgpu_sys *s, double fmax, int maxsteps) {
     c.op = OP_NONE;
     c.old_alphamin = 0.1;  // static in linmin, src/imd_cg.c:99
   }
-  CK(cudaMemcpy(s->d_cs, init.data(), sizeof(CgSys) * ns, cudaMemcpyHostToDevice));
-  CK(cudaMemset(s->d_sys_done, 0, sizeof(int) * ns));
-  CK(cudaMemset(s->d_sys_short, 0, sizeof(int) * ns));
-  CK(cudaMemset(s->d_ndone, 0, sizeof(int)));
-  CK(cudaMemset(s->cgg, 0, sizeof(double4) * s->ncap));
-  CK(cudaMemset(s->cgh, 0, sizeof(double4) * s->ncap));
-  CK(cudaMemset(s->oldx, 0, sizeof(double4) * s->ncap));
+  CK(scopy(s->st, s->d_cs, init.data(), sizeof(CgSys) * ns, cudaMemcpyHostToDevice));
+  CK(sset(s->st, s->d_sys_done, 0, sizeof(int) * ns));
+  CK(sset(s->st, s->d_sys_short, 0, sizeof(int) * ns));
+  CK(sset(s->st, s->d_ndone, 0, sizeof(int)));
+  CK(sset(s->st, s->cgg, 0, sizeof(double4) * s->ncap));
+  CK(sset(s->st, s->cgh, 0, sizeof(double4) * s->ncap));
+  CK(sset(s->st, s->oldx, 0, sizeof(double4) * s->ncap));
   // first list: synchronous, sizes the buffers (with head-room for relaxation)
   int one = 1;
-  CK(cudaMemcpy(&s->dsc->rebuild, &one, sizeof(int), cudaMemcpyHostToDevice));
+  CK(scopy(s->st, &s->dsc->rebuild, &one, sizeof(int), cudaMemcpyHostToDevice));
   s->hsc_valid = false;
   rc = rebuild_sync(s);
   if (rc) return rc;
   {
     int cnt[4];
-    CK(cudaMemcpy(cnt, s->counters, sizeof cnt, cudaMemcpyDeviceToHost));
+    CK(scopy(s->st, cnt, s->counters, sizeof cnt, cudaMemcpyDeviceToHost));
     const int want = (int)(cnt[1] * s->list_headroom) + 8;
     if (s->nbcap < want) {
       if ((rc = alloc_list(s, want))) return rc;
@@ -4546,7 +4567,7 @@ int imdgpu_batch_begin(imdgpu_sys *s, double fmax, int maxsteps) {
   if (s->autotune_batches) {
     // the block shape for this batch, then the evaluation state as begun
     if ((rc = autotune_forces(s, 0))) return rc;
-    CK(cudaMemset(s->d_sys_short, 0, sizeof(int) * ns));
+    CK(sset(s->st, s->d_sys_short, 0, sizeof(int) * ns));
   }
   if (!s->brun) s->brun = new BatchRun();
   BatchRun &B = *s->brun;
@@ -4569,7 +4590,7 @@ int imdgpu_batch_begin(imdgpu_sys *s, double fmax, int maxsteps) {
   B.have_final.assign(ns, 0);
   B.final_x.assign(3 * (size_t)s->n, 0.0);
   long nbl = 0;
-  CK(cudaMemcpy(&nbl, s->dnbl, sizeof(long), cudaMemcpyDeviceToHost));
+  CK(scopy(s->st, &nbl, s->dnbl, sizeof(long), cudaMemcpyDeviceToHost));
   s->batch_nbl0 = nbl;
   return IMDGPU_OK;
 }
@@ -4616,6 +4637,15 @@ int imdgpu_batch_set_list_headroom(imdgpu_sys *s, double factor) {
   if (!s) return fail(IMDGPU_ERR_ARG, "null system");
   if (!(factor >= 1.0 && factor <= 4.0)) return fail(IMDGPU_ERR_ARG, "headroom outside [1, 4]");
   s->list_headroom = factor;
+  return IMDGPU_OK;
+}
+
+int imdgpu_batch_inject_replays(imdgpu_sys *s, int every, int count) {
+  if (!s || !s->brun) return fail(IMDGPU_ERR_STATE, "imdgpu_batch_begin first");
+  if (every < 0 || count < 0) return fail(IMDGPU_ERR_ARG, "negative replay spacing or count");
+  s->brun->inject_every = every;
+  s->brun->inject_left = count;
+  s->brun->inject_ok = 0;
   return IMDGPU_OK;
 }
 
@@ -4738,12 +4768,18 @@ int imdgpu_batch_advance(imdgpu_sys *s, int max_rounds, int *ndone_out, int *rou
       rc = fail(IMDGPU_ERR_CUDA, kWaitMsg);
       break;
     }
-    if (s->status_host & (ST_NBOVER | ST_GHOSTOVER)) {
+    const bool overflow = (s->status_host & (ST_NBOVER | ST_GHOSTOVER)) != 0;
+    const bool inject = !overflow && B.inject_left > 0 && B.inject_ok >= B.inject_every;
+    if (inject) {
+      B.inject_left--;
+      B.inject_ok = 0;
+    }
+    if (overflow || inject) {
       B.replays++;
       // eight overflows of one chunk of rounds in a row: the growth does not
       // converge (the count resets with every chunk that completes)
       int cnt[4];
-      CKR(cudaMemcpy(cnt, s->counters, sizeof cnt, cudaMemcpyDeviceToHost));
+      CKR(scopy(s->st, cnt, s->counters, sizeof cnt, cudaMemcpyDeviceToHost));
       if (++replays > 8) {
         rc = fail(IMDGPU_ERR_NOMEM,
                   "list overflow persists in batch relaxation (status " +
@@ -4759,13 +4795,13 @@ int imdgpu_batch_advance(imdgpu_sys *s, int max_rounds, int *ndone_out, int *rou
         if ((rc = alloc_list(s, (int)(cnt[1] * 1.25) + 8))) break;
       double4 *back[6] = {s->pos, s->mom, s->oldx, s->cgg, s->cgh, s->frc};
       for (int k = 0; k < 6; k++)
-        CKR(cudaMemcpy(back[k], b4[k], sizeof(double4) * n, cudaMemcpyDeviceToDevice));
-      CKR(cudaMemcpy(s->number, bnum, sizeof(int) * n, cudaMemcpyDeviceToDevice));
-      CKR(cudaMemcpy(s->orig, borig, sizeof(int) * n, cudaMemcpyDeviceToDevice));
-      CKR(cudaMemcpy(s->d_sys_done, bdone, sizeof(int) * ns, cudaMemcpyDeviceToDevice));
-      CKR(cudaMemcpy(s->d_sys_short, bshort, sizeof(int) * ns, cudaMemcpyDeviceToDevice));
-      CKR(cudaMemcpy(s->d_ndone, bnd, sizeof(int), cudaMemcpyDeviceToDevice));
-      CKR(cudaMemcpy(s->d_cs, bcs, sizeof(CgSys) * ns, cudaMemcpyDeviceToDevice));
+        CKR(scopy(s->st, back[k], b4[k], sizeof(double4) * n, cudaMemcpyDeviceToDevice));
+      CKR(scopy(s->st, s->number, bnum, sizeof(int) * n, cudaMemcpyDeviceToDevice));
+      CKR(scopy(s->st, s->orig, borig, sizeof(int) * n, cudaMemcpyDeviceToDevice));
+      CKR(scopy(s->st, s->d_sys_done, bdone, sizeof(int) * ns, cudaMemcpyDeviceToDevice));
+      CKR(scopy(s->st, s->d_sys_short, bshort, sizeof(int) * ns, cudaMemcpyDeviceToDevice));
+      CKR(scopy(s->st, s->d_ndone, bnd, sizeof(int), cudaMemcpyDeviceToDevice));
+      CKR(scopy(s->st, s->d_cs, bcs, sizeof(CgSys) * ns, cudaMemcpyDeviceToDevice));
       if ((rc = rebuild_sync(s))) break;
       // the build moved positions, momenta and the CG vectors to new slots;
       // the last forces, which the next round's sums and set_hg / reset read,
@@ -4779,10 +4815,11 @@ int imdgpu_batch_advance(imdgpu_sys *s, int max_rounds, int *ndone_out, int *rou
     B.rounds += R;
     done_rounds += R;
     replays = 0;
+    B.inject_ok++;
     // compaction: the unfinished cells alone, once they hold few enough atoms
     if (s->compact_pct > 0 && nd > 0 && nd < ns) {
       std::vector<int> dn(ns);
-      CKR(cudaMemcpy(dn.data(), s->d_sys_done, sizeof(int) * ns, cudaMemcpyDeviceToHost));
+      CKR(scopy(s->st, dn.data(), s->d_sys_done, sizeof(int) * ns, cudaMemcpyDeviceToHost));
       long active = 0;
       for (int c = 0; c < ns; c++)
         if (!dn[c]) active += s->h_aoff[c + 1] - s->h_aoff[c];
@@ -4818,7 +4855,7 @@ int imdgpu_batch_relax(imdgpu_sys *s, double fmax, int maxsteps, int max_rounds,
 int imdgpu_batch_rebuilds(imdgpu_sys *s, long *n) {
   if (!s || !n) return fail(IMDGPU_ERR_ARG, "null");
   long nbl = 0;
-  CK(cudaMemcpy(&nbl, s->dnbl, sizeof(long), cudaMemcpyDeviceToHost));
+  CK(scopy(s->st, &nbl, s->dnbl, sizeof(long), cudaMemcpyDeviceToHost));
   *n = nbl - s->batch_nbl0;
   return IMDGPU_OK;
 }
@@ -4826,7 +4863,7 @@ int imdgpu_batch_rebuilds(imdgpu_sys *s, long *n) {
 int imdgpu_batch_progress(imdgpu_sys *s, int *ndone, long *active_atoms) {
   if (!s || !s->brun) return fail(IMDGPU_ERR_STATE, "imdgpu_batch_begin first");
   std::vector<int> dn(s->nsys);
-  CK(cudaMemcpy(dn.data(), s->d_sys_done, sizeof(int) * s->nsys, cudaMemcpyDeviceToHost));
+  CK(scopy(s->st, dn.data(), s->d_sys_done, sizeof(int) * s->nsys, cudaMemcpyDeviceToHost));
   long active = 0;
   int nd = s->brun->ndone_base;
   for (int c = 0; c < s->nsys; c++) {
@@ -4845,7 +4882,7 @@ int imdgpu_batch_results(imdgpu_sys *s, double *epot, double *fmax_out, int *ste
                          int *status) {
   if (!s || s->nsys < 1) return fail(IMDGPU_ERR_STATE, "no batch");
   std::vector<CgSys> cs(s->nsys);
-  CK(cudaMemcpy(cs.data(), s->d_cs, sizeof(CgSys) * s->nsys, cudaMemcpyDeviceToHost));
+  CK(scopy(s->st, cs.data(), s->d_cs, sizeof(CgSys) * s->nsys, cudaMemcpyDeviceToHost));
   // per cell of imdgpu_batch_set_cells: on the device, or finished and
   // compacted away
   std::vector<CgSys> all;
@@ -4957,9 +4994,9 @@ static int ml_ensure(imdgpu_sys *s) {
     CK(dalloc(&s->ml_wb, np));
     CK(dalloc(&s->ml_np, 1));
     CK(dalloc(&s->ml_loss, 1));
-    CK(cudaMemset(s->ml_w, 0, sizeof(float) * np));
-    CK(cudaMemset(s->ml_m, 0, sizeof(float) * np));
-    CK(cudaMemset(s->ml_v, 0, sizeof(float) * np));
+    CK(sset(s->st, s->ml_w, 0, sizeof(float) * np));
+    CK(sset(s->st, s->ml_m, 0, sizeof(float) * np));
+    CK(sset(s->st, s->ml_v, 0, sizeof(float) * np));
   }
   if (s->ml_dx_cap < s->ncap) {
     dfree(s->ml_dx);
@@ -4983,7 +5020,7 @@ static int ml_prepare_pairs(imdgpu_sys *s) {
   long entries = 0;
   {
     std::vector<int> nn(s->n);
-    CK(cudaMemcpy(nn.data(), s->nnb, sizeof(int) * s->n, cudaMemcpyDeviceToHost));
+    CK(scopy(s->st, nn.data(), s->nnb, sizeof(int) * s->n, cudaMemcpyDeviceToHost));
     for (int v : nn) entries += v;
   }
   const long need = 2 * entries + 64;
@@ -5016,9 +5053,9 @@ int imdgpu_ml_set_weights(imdgpu_sys *s, const float *w, int n) {
   if (!s->atoms_set) return fail(IMDGPU_ERR_STATE, "atoms not set");
   int rc = ml_ensure(s);
   if (rc) return rc;
-  CK(cudaMemcpy(s->ml_w, w, sizeof(float) * n, cudaMemcpyHostToDevice));
-  CK(cudaMemset(s->ml_m, 0, sizeof(float) * n));
-  CK(cudaMemset(s->ml_v, 0, sizeof(float) * n));
+  CK(scopy(s->st, s->ml_w, w, sizeof(float) * n, cudaMemcpyHostToDevice));
+  CK(sset(s->st, s->ml_m, 0, sizeof(float) * n));
+  CK(sset(s->st, s->ml_v, 0, sizeof(float) * n));
   launch_ml_to_bf16(s->ml_w, s->ml_wb, n, s->st);
   CK(cudaStreamSynchronize(s->st));
   s->ml_have = 1;
@@ -5028,15 +5065,15 @@ int imdgpu_ml_set_weights(imdgpu_sys *s, const float *w, int n) {
 
 int imdgpu_ml_get_weights(imdgpu_sys *s, float *w, int n) {
   if (!s || !w || n != ml_nparam() || !s->ml_w) return fail(IMDGPU_ERR_ARG, "weights: not set");
-  CK(cudaMemcpy(w, s->ml_w, sizeof(float) * n, cudaMemcpyDeviceToHost));
+  CK(scopy(s->st, w, s->ml_w, sizeof(float) * n, cudaMemcpyDeviceToHost));
   return IMDGPU_OK;
 }
 
 int imdgpu_ml_get_adam(imdgpu_sys *s, float *m, float *v, int *step) {
   if (!s || !s->ml_have) return fail(IMDGPU_ERR_STATE, "no weights");
   const int np = ml_nparam();
-  if (m) CK(cudaMemcpy(m, s->ml_m, sizeof(float) * np, cudaMemcpyDeviceToHost));
-  if (v) CK(cudaMemcpy(v, s->ml_v, sizeof(float) * np, cudaMemcpyDeviceToHost));
+  if (m) CK(scopy(s->st, m, s->ml_m, sizeof(float) * np, cudaMemcpyDeviceToHost));
+  if (v) CK(scopy(s->st, v, s->ml_v, sizeof(float) * np, cudaMemcpyDeviceToHost));
   if (step) *step = s->ml_adam_step;
   return IMDGPU_OK;
 }
@@ -5045,8 +5082,8 @@ int imdgpu_ml_set_adam(imdgpu_sys *s, const float *m, const float *v, int step) 
   if (!s || !s->ml_have) return fail(IMDGPU_ERR_STATE, "no weights");
   if (!m || !v || step < 0) return fail(IMDGPU_ERR_ARG, "adam state");
   const int np = ml_nparam();
-  CK(cudaMemcpy(s->ml_m, m, sizeof(float) * np, cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(s->ml_v, v, sizeof(float) * np, cudaMemcpyHostToDevice));
+  CK(scopy(s->st, s->ml_m, m, sizeof(float) * np, cudaMemcpyHostToDevice));
+  CK(scopy(s->st, s->ml_v, v, sizeof(float) * np, cudaMemcpyHostToDevice));
   s->ml_adam_step = step;
   return IMDGPU_OK;
 }
@@ -5133,9 +5170,9 @@ int imdgpu_batch_ml_start(imdgpu_sys *s, int *used, double *e_start, double *e_p
   if (s->brun) {
     // a batch relaxation was begun on these cells: they may be marked done,
     // and the list builds skipped finished cells, so every list is rebuilt
-    CK(cudaMemset(s->d_sys_done, 0, sizeof(int) * s->nsys));
+    CK(sset(s->st, s->d_sys_done, 0, sizeof(int) * s->nsys));
     int one = RB_ALL;
-    CK(cudaMemcpy(&s->dsc->rebuild, &one, sizeof(int), cudaMemcpyHostToDevice));
+    CK(scopy(s->st, &s->dsc->rebuild, &one, sizeof(int), cudaMemcpyHostToDevice));
     s->hsc_valid = false;
   }
   rc = ml_prepare_pairs(s);  // forces, rho and the list at the start positions
@@ -5228,7 +5265,7 @@ extern "C" int imdgpu_get_pairs(imdgpu_sys *s, long cap, int *ni, int *nj, int *
     return fail(IMDGPU_ERR_STATE, "get_pairs: the deterministic mode holds the full list, not "
                                   "IMD's half list");
   std::vector<int> nn(s->n);
-  CK(cudaMemcpy(nn.data(), s->nnb, sizeof(int) * s->n, cudaMemcpyDeviceToHost));
+  CK(scopy(s->st, nn.data(), s->nnb, sizeof(int) * s->n, cudaMemcpyDeviceToHost));
   std::vector<long> rs(s->n + 1, 0);
   for (int i = 0; i < s->n; i++) rs[i + 1] = rs[i] + nn[i];
   *count = rs[s->n];
@@ -5243,15 +5280,15 @@ extern "C" int imdgpu_get_pairs(imdgpu_sys *s, long cap, int *ni, int *nj, int *
   CK(dalloc(&dnj, m));
   CK(dalloc(&dsh, 3 * m));
   CK(dalloc(&dr2, m));
-  CK(cudaMemcpy(drs, rs.data(), sizeof(long) * (s->n + 1), cudaMemcpyHostToDevice));
+  CK(scopy(s->st, drs, rs.data(), sizeof(long) * (s->n + 1), cudaMemcpyHostToDevice));
   SysView v = view(s);
   k_pairs<<<nblk(s->n, 128), 128, 0, s->st>>>(v, drs, dni, dnj, dsh, dr2);
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(s->st));
-  if (ni) CK(cudaMemcpy(ni, dni, sizeof(int) * m, cudaMemcpyDeviceToHost));
-  if (nj) CK(cudaMemcpy(nj, dnj, sizeof(int) * m, cudaMemcpyDeviceToHost));
-  if (shift) CK(cudaMemcpy(shift, dsh, sizeof(int) * 3 * m, cudaMemcpyDeviceToHost));
-  if (r2) CK(cudaMemcpy(r2, dr2, sizeof(double) * m, cudaMemcpyDeviceToHost));
+  if (ni) CK(scopy(s->st, ni, dni, sizeof(int) * m, cudaMemcpyDeviceToHost));
+  if (nj) CK(scopy(s->st, nj, dnj, sizeof(int) * m, cudaMemcpyDeviceToHost));
+  if (shift) CK(scopy(s->st, shift, dsh, sizeof(int) * 3 * m, cudaMemcpyDeviceToHost));
+  if (r2) CK(scopy(s->st, r2, dr2, sizeof(double) * m, cudaMemcpyDeviceToHost));
   dfree(drs);
   dfree(dni);
   dfree(dnj);

@@ -417,10 +417,7 @@ int imdgpu_batch_set_autotune(imdgpu_sys *sys, int on);
 int imdgpu_batch_set_engine(imdgpu_sys *sys, int on);
 /* Per-system rebuilds (default 0): every cell of the batch gets a fixed
  * ghost range with head-room, and a round rebuilds the lists of the cells
- * that moved past skin/2 only, instead of the whole batch.  Known defect:
- * after a chunk of rounds is replayed following an overflow, part of the
- * cells continue with their atoms' CG vectors out of step with the atoms;
- * they relax to the right energies with the atoms relabelled. */
+ * that moved past skin/2 only, instead of the whole batch. */
 int imdgpu_batch_set_partial_rebuild(imdgpu_sys *sys, int on);
 /* List capacity of a batch at imdgpu_batch_begin and after a compaction:
  * factor x the most entries an atom has (default 1.3, within [1, 4]).  A
@@ -429,6 +426,12 @@ int imdgpu_batch_set_partial_rebuild(imdgpu_sys *sys, int on);
  * since imdgpu_batch_begin. */
 int imdgpu_batch_set_list_headroom(imdgpu_sys *sys, double factor);
 int imdgpu_batch_replays(imdgpu_sys *sys, long *n);
+/* Test hook for the replay path, no counterpart in the reference: after
+ * every `every` completed chunks of imdgpu_batch_advance, the next chunk is
+ * replayed from its snapshot as if it had overflowed (without growing a
+ * buffer), `count` times in all; call after imdgpu_batch_begin.  The
+ * replays are counted by imdgpu_batch_replays. */
+int imdgpu_batch_inject_replays(imdgpu_sys *sys, int every, int count);
 
 /* Timing of the dominant kernels of the last nve_run (device ms, CUDA
  * events on the system's stream). */
