@@ -488,11 +488,12 @@ int imdgpu_probe_fp64_peak(double *tflops);
  * and norm partial sums go to a fixed file-scope device array of 2.5 MiB
  * per device, so n is limited to 16,777,216 atoms (IMDGPU_ERR_ARG beyond).
  * The first call on each device looks up that array's device address (with
- * the device current); make that first call before any stream capture
- * begins.  All calls on a device share the array and leave their partial
- * sums in it; each call overwrites every slot it reads, so nothing needs
- * clearing, but calls that overlap on the GPU (two streams at once) race on
- * it.  Every call waits on `stream` until the results are in `out`. */
+ * the device current).  All calls on a device share the array and leave
+ * their partial sums in it; each call overwrites every slot it reads, so
+ * nothing needs clearing, but calls that overlap on the GPU (two streams at
+ * once) race on it.  Every call copies its results to the host `out` and
+ * waits on `stream` until they are there, so no call can be captured into a
+ * CUDA graph. */
 int imdgpu_move_atoms_nve_noalloc(int n, int ntypes, double *x, double *p, double *f,
                                   const double *mass, const int *type, const double *restr,
                                   double timestep, const double *x_ref, double *out,
