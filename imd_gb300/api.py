@@ -15,7 +15,9 @@ import os
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIBPATH = os.path.join(HERE, "libimdgpu.so")
+# IMDGPU_LIB names another build of the library, e.g. the bounds-checked
+# libimdgpu_check.so (python -m imd_gb300.build --check)
+LIBPATH = os.environ.get("IMDGPU_LIB") or os.path.join(HERE, "libimdgpu.so")
 
 PAIR, EAM2 = 0, 1
 QUADRATIC, FOURPOINT, SPLINE = 0, 1, 2
@@ -104,6 +106,8 @@ def lib() -> C.CDLL:
     global _lib
     if _lib is None:
         if not os.path.exists(LIBPATH):
+            if os.environ.get("IMDGPU_LIB"):
+                raise IMDGPUError("IMDGPU_LIB names a missing library: " + LIBPATH)
             from . import build
             build.build()
         L = C.CDLL(LIBPATH)
@@ -190,6 +194,7 @@ def lib() -> C.CDLL:
         L.imdgpu_batch_set_list_headroom.argtypes = [vp, C.c_double]
         L.imdgpu_batch_replays.argtypes = [vp, C.POINTER(C.c_long)]
         L.imdgpu_batch_inject_replays.argtypes = [vp, C.c_int, C.c_int]
+        L.imdgpu_check_sites.argtypes = [vp, _ip, _ip]
         L.imdgpu_batch_positions.argtypes = [vp, _dp]
         fp = C.POINTER(C.c_float)
         L.imdgpu_ml_nparam.argtypes = []
@@ -627,6 +632,13 @@ class GpuSystem:
         t = Timing()
         _check(lib().imdgpu_get_timing(self.h, C.byref(t)), "get_timing")
         return t
+
+    def check_sites(self):
+        """(checked, sites): whether the loaded library is the bounds-checked
+        build, and the mask of the checks that failed (imdgpu_check_sites)."""
+        c, m = C.c_int(0), C.c_int(0)
+        _check(lib().imdgpu_check_sites(self.h, C.byref(c), C.byref(m)), "check_sites")
+        return bool(c.value), m.value
 
     def close(self) -> None:
         if getattr(self, "h", None):

@@ -25,6 +25,7 @@ __global__ void k_ghost_pos(SysView v) {
   {
     const int o = v.gowner[g];
     if (o < 0) continue;  // an unused slot of a system's ghost range
+    if (!in_bounds(v, o, v.n, CK_OWNER)) continue;
     v.pos[v.n + g] = ghost_image(v, v.pos[o], v.gcode[g], sys_of(v, o));
   }
 }
@@ -43,6 +44,7 @@ __global__ void __launch_bounds__(BS_FORCE_MAX) k_density64(SysView v, DevTable 
   const uint32_t *nb = v.nbr + i;
   for (int k = 0; k < nn; k++) {
     const int j = (int)(__ldg(nb + (size_t)k * v.ncap) & NB_MASK);
+    if (!in_bounds(v, j, (long)v.n + v.gcap, CK_PARTNER)) continue;
     const double4 pj = ldg4(&v.pos[j]);
     const double dx = dsub(pj.x, pi.x), dy = dsub(pj.y, pi.y), dz = dsub(pj.z, pi.z);
     const double r2 = r2_exact(dx, dy, dz);
@@ -73,7 +75,7 @@ __global__ void k_fold_rho(SysView v) {
     // range's unused slots until the overflow is replayed: skip them
     const int o = v.gowner[g];
     const double r = v.rho[v.n + g];
-    if (r != 0.0 && o >= 0) atomicAdd(&v.rho[o], r);
+    if (r != 0.0 && o >= 0 && in_bounds(v, o, v.n, CK_OWNER)) atomicAdd(&v.rho[o], r);
   }
 }
 
@@ -98,7 +100,7 @@ __global__ void k_ghost_df(SysView v) {
   const int ng = v.counters[0];
   for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < ng; g += gridDim.x * blockDim.x) {
     const int o = v.gowner[g];
-    if (o >= 0) v.df[v.n + g] = v.df[o];
+    if (o >= 0 && in_bounds(v, o, v.n, CK_OWNER)) v.df[v.n + g] = v.df[o];
   }
 }
 
@@ -123,6 +125,7 @@ __global__ void __launch_bounds__(BS_FORCE_MAX) k_force64(SysView v, DevTable pa
     const uint32_t *nb = v.nbr + i;
     for (int k = 0; k < nn; k++) {
       const int j = (int)(__ldg(nb + (size_t)k * v.ncap) & NB_MASK);
+      if (!in_bounds(v, j, (long)v.n + v.gcap, CK_PARTNER)) continue;
       const double4 pj = ldg4(&v.pos[j]);
       const double dx = dsub(pj.x, pi.x), dy = dsub(pj.y, pi.y), dz = dsub(pj.z, pi.z);
       const double r2 = r2_exact(dx, dy, dz);
@@ -180,7 +183,8 @@ __global__ void k_fold_force(SysView v) {
   for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < ng; g += gridDim.x * blockDim.x) {
     const double4 f = v.frc[v.n + g];
     const int own = v.gowner[g];  // -1: an unused slot (see k_fold_rho)
-    if (own >= 0 && (f.x != 0.0 || f.y != 0.0 || f.z != 0.0 || f.w != 0.0)) {
+    if (own >= 0 && (f.x != 0.0 || f.y != 0.0 || f.z != 0.0 || f.w != 0.0) &&
+        in_bounds(v, own, v.n, CK_OWNER)) {
       double *o = &v.frc[own].x;
       atomicAdd(o + 0, f.x);
       atomicAdd(o + 1, f.y);
@@ -226,6 +230,7 @@ __global__ void __launch_bounds__(BS_FORCE_MAX) k_density_fast(SysView v, DevTab
 #pragma unroll 2
   for (int k = 0; k < nn; k++) {
     const int j = (int)(__ldg(nb + (size_t)k * v.ncap) & NB_MASK);
+    if (!in_bounds(v, j, (long)v.n + v.gcap, CK_PARTNER)) continue;
     const double4 pj = ldg4(&v.pos[j]);
     const double dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
     const double r2 = fma(dx, dx, fma(dy, dy, dz * dz));
@@ -272,6 +277,7 @@ __global__ void __launch_bounds__(BS_FORCE_MAX) k_force_fast(SysView v, DevTable
 #pragma unroll 2
     for (int k = 0; k < nn; k++) {
       const int j = (int)(__ldg(nb + (size_t)k * v.ncap) & NB_MASK);
+      if (!in_bounds(v, j, (long)v.n + v.gcap, CK_PARTNER)) continue;
       const double4 pj = ldg4(&v.pos[j]);
       const double dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
       const double r2 = fma(dx, dx, fma(dy, dy, dz * dz));
@@ -398,6 +404,7 @@ __global__ void __launch_bounds__(BS_FORCE_MAX) k_density_cache(SysView v, DevTa
 #pragma unroll 2
   for (int k = q; k < nn; k += LPA) {
     const int j = (int)(__ldg(nb + (size_t)k * v.ncap) & NB_MASK);
+    if (!in_bounds(v, j, (long)v.n + v.gcap, CK_PARTNER)) continue;
     const double4 pj = ldg4(&v.pos[j]);
     const double dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
     const double r2 = fma(dx, dx, fma(dy, dy, dz * dz));
@@ -444,6 +451,7 @@ __global__ void __launch_bounds__(BS_FORCE_MAX) k_force_cache(SysView v, double 
       const double4 c = ld_stream(pc + (size_t)k * v.ncap);
       if (c.x < 0.0) continue;  // beyond both cutoffs
       const int j = (int)(__ldg(nb + (size_t)k * v.ncap) & NB_MASK);
+      if (!in_bounds(v, j, (long)v.n + v.gcap, CK_PARTNER)) continue;
       const double4 pj = ldg4(&v.pos[j]);
       const double dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
       const double dfj = __ldg(&v.df[j]);
@@ -545,6 +553,7 @@ __global__ void __launch_bounds__(BS_FORCE_MAX) k_density_det(SysView v, DevTabl
     const uint32_t *__restrict__ nb = v.nbr + i;
     for (int k = q; k < nn; k += DET_Q) {
       const int j = (int)(__ldg(nb + (size_t)k * v.ncap) & NB_MASK);
+      if (!in_bounds(v, j, (long)v.n + v.gcap, CK_PARTNER)) continue;
       const double4 pj = ldg4(&v.pos[j]);
       const double dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
       const double r2 = fma(dx, dx, fma(dy, dy, dz * dz));
@@ -579,6 +588,7 @@ __global__ void __launch_bounds__(BS_FORCE_MAX) k_force_det(SysView v, DevTable 
     const uint32_t *__restrict__ nb = v.nbr + i;
     for (int k = q; k < nn; k += DET_Q) {
       const int j = (int)(__ldg(nb + (size_t)k * v.ncap) & NB_MASK);
+      if (!in_bounds(v, j, (long)v.n + v.gcap, CK_PARTNER)) continue;
       const double4 pj = ldg4(&v.pos[j]);
       const double dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
       const double r2 = fma(dx, dx, fma(dy, dy, dz * dz));
@@ -681,6 +691,7 @@ __global__ void __launch_bounds__(BS_FORCE_MAX) k_stress_fast(SysView v, DevTabl
   const uint32_t *__restrict__ nb = v.nbr + i;
   for (int k = 0; k < nn; k++) {
     const int j = (int)(__ldg(nb + (size_t)k * v.ncap) & NB_MASK);
+    if (!in_bounds(v, j, (long)v.n + v.gcap, CK_PARTNER)) continue;
     const double4 pj = ldg4(&v.pos[j]);
     const double dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
     const double r2 = fma(dx, dx, fma(dy, dy, dz * dz));
@@ -736,9 +747,11 @@ __global__ void __launch_bounds__(BS_FORCE_MAX) k_stress_fast(SysView v, DevTabl
 __global__ void k_fold_stress(SysView v, double *stress) {
   const int ng = v.counters[0];
   for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < ng; g += gridDim.x * blockDim.x) {
-    if (v.gowner[g] < 0) continue;  // an unused slot of a system's ghost range
+    const int o = v.gowner[g];
+    if (o < 0) continue;  // an unused slot of a system's ghost range
+    if (!in_bounds(v, o, v.n, CK_OWNER)) continue;
     const double *sg = stress + 6 * (size_t)(v.n + g);
-    double *so = stress + 6 * (size_t)v.gowner[g];
+    double *so = stress + 6 * (size_t)o;
 #pragma unroll
     for (int q = 0; q < 6; q++)
       if (sg[q] != 0.0) atomicAdd(so + q, sg[q]);

@@ -31,6 +31,30 @@ constexpr unsigned ST_NBOVER = 2u;     // list entries beyond capacity
 constexpr unsigned ST_GHOSTOVER = 4u;  // ghost atoms beyond capacity
 constexpr unsigned ST_CELLOVER = 8u;   // atoms per cell beyond CELLCAP
 constexpr unsigned ST_WAIT = 16u;      // a bounded wait on an asynchronous copy ran out
+constexpr unsigned ST_BOUNDS = 32u;    // bounds-checked build: an index failed its check
+
+// ---------------------------------------------------------------------------
+// Bounds-checked build (-DIMDGPU_CHECK, not the default).  The indices the
+// kernels take from device data (list partners, ghost owners, table rows,
+// cell bins, permutation slots) are checked before use.  A failed check sets
+// ST_BOUNDS in the status word and the site's bit in counters[CK_SITES],
+// which nothing clears while the system lives (imdgpu_check_sites reads it),
+// and the access is skipped, or the index clamped where the kernel needs
+// one.  Without the macro every check is the constant true and compiles away.
+// ---------------------------------------------------------------------------
+constexpr int CK_PARTNER = 1;  // a list partner outside the real and ghost slots
+constexpr int CK_OWNER = 2;    // a ghost's owner outside the real atoms
+constexpr int CK_ROW = 4;      // a table row or column outside the table
+constexpr int CK_BIN = 8;      // an atom's bin outside the cell grid
+constexpr int CK_SLOT = 16;    // a permutation slot or caller index outside the atoms
+constexpr int CK_SITES = 4;    // the counters slot of the failed sites
+
+#ifdef IMDGPU_CHECK
+static __device__ __noinline__ void check_failed(unsigned *status, int *counters, int site) {
+  atomicOr(status, ST_BOUNDS);
+  atomicOr(&counters[CK_SITES], site);
+}
+#endif
 
 // One pot_table_t on the device.  `tri` holds, per column and row k, the
 // three table values the quadratic interpolation reads (rows k, k+1, k+2):
@@ -67,7 +91,23 @@ struct DevTable {
   float fbegin[MAXCOL];
   float fend[MAXCOL];
   float finv[MAXCOL];
+#ifdef IMDGPU_CHECK
+  unsigned *chk_status;     // the system's status word and counters
+  int *chk_counters;
+#endif
 };
+
+// element of column col, row k of a table array; a checked build confirms
+// both and reads row 0 of column 0 in place of a bad one
+__device__ __forceinline__ size_t row_of(const DevTable &t, int col, int k) {
+#ifdef IMDGPU_CHECK
+  if (col < 0 || col >= t.ncols || k < 0 || k >= t.rows) {
+    check_failed(t.chk_status, t.chk_counters, CK_ROW);
+    return 0;
+  }
+#endif
+  return (size_t)col * t.rows + k;
+}
 
 // Everything a kernel of one system needs, passed by value.
 struct SysView {
@@ -132,6 +172,19 @@ struct SysView {
   int *sys_rb;
   const int *goff, *rank_sys, *buf_sys, *coff;
 };
+
+// idx within [0, lim): always true without -DIMDGPU_CHECK; a checked build
+// records a failure (see CK_PARTNER ...)
+__device__ __forceinline__ bool in_bounds(const SysView &v, long idx, long lim, int site) {
+#ifdef IMDGPU_CHECK
+  if (idx >= 0 && idx < lim) return true;
+  check_failed(v.status, v.counters, site);
+  return false;
+#else
+  (void)v, (void)idx, (void)lim, (void)site;
+  return true;
+#endif
+}
 
 // sc->rebuild: bit 0 rebuild everything, bit 1 rebuild the systems whose
 // sys_rb flag is set
@@ -223,7 +276,7 @@ __device__ __forceinline__ double4 ldg4(const double4 *p) {
 }
 
 __device__ __forceinline__ double4 tab_load(const DevTable &t, int col, int k) {
-  return ldg4(&t.tri[(size_t)col * t.rows + k]);
+  return ldg4(&t.tri[row_of(t, col, k)]);
 }
 
 __device__ __forceinline__ void pair_int2(const DevTable &t, int col, double r2, double &pot,
@@ -285,13 +338,13 @@ __device__ __forceinline__ int tab_index_fast(const DevTable &t, int col, double
   return k;
 }
 __device__ __forceinline__ double4 cv_load(const DevTable &t, int col, int k) {
-  return ldg4(&t.cv[(size_t)col * t.rows + k]);
+  return ldg4(&t.cv[row_of(t, col, k)]);
 }
 __device__ __forceinline__ double4 cg_load(const DevTable &t, int col, int k) {
-  return ldg4(&t.cg[(size_t)col * t.rows + k]);
+  return ldg4(&t.cg[row_of(t, col, k)]);
 }
 __device__ __forceinline__ double4 cgn_load(const DevTable &t, int col, int k) {
-  return ldg4(&t.cgn[(size_t)col * t.rows + k]);
+  return ldg4(&t.cgn[row_of(t, col, k)]);
 }
 // CUB: cubic rows (4-point / spline); quadratic rows skip the zero terms
 template <bool CUB = false>

@@ -50,12 +50,14 @@ __global__ void k_ml_pairs(SysView v, MlPair *pairs, int cap, int *count) {
   const int nn = v.nnb[i];
   for (int k = 0; k < nn; k++) {
     const int j = (int)(v.nbr[(size_t)k * v.ncap + i] & NB_MASK);
+    if (!in_bounds(v, j, (long)v.n + v.gcap, CK_PARTNER)) continue;
     const double4 pj = v.pos[j];
     const float dx = (float)(pj.x - pi.x), dy = (float)(pj.y - pi.y), dz = (float)(pj.z - pi.z);
     const float r2 = dx * dx + dy * dy + dz * dz;
     if (r2 >= ML_RC * ML_RC) continue;
     const int jo = (j >= v.n) ? v.gowner[j - v.n] : j;
     if (jo < 0) continue;  // an unused ghost slot (only after a range overflow)
+    if (!in_bounds(v, jo, v.n, CK_OWNER)) continue;
     const int at = atomicAdd(count, 2);
     if (at + 1 < cap) {
       pairs[at] = MlPair{i, dx, dy, dz};

@@ -54,11 +54,11 @@ __device__ __forceinline__ int tab_index_f(const DevTable &t, int col, float r2,
   return k;
 }
 __device__ __forceinline__ float polyf_v(const DevTable &t, int col, int k, float chi) {
-  const float4 c = __ldg(&t.cvf[(size_t)col * t.rows + k]);
+  const float4 c = __ldg(&t.cvf[row_of(t, col, k)]);
   return fmaf(chi, fmaf(chi, fmaf(chi, c.w, c.z), c.y), c.x);
 }
 __device__ __forceinline__ float polyf_g(const DevTable &t, int col, int k, float chi) {
-  const float4 g = __ldg(&t.cgf[(size_t)col * t.rows + k]);
+  const float4 g = __ldg(&t.cgf[row_of(t, col, k)]);
   return fmaf(chi, fmaf(chi, g.z, g.y), g.x);
 }
 
@@ -81,6 +81,7 @@ __global__ void __launch_bounds__(BS_FORCE_MAX) k_density_mixed(SysView v, DevTa
 #pragma unroll 4
   for (int k = q; k < nn; k += LPA) {
     const int j = (int)(__ldg(nb + (size_t)k * v.ncap) & NB_MASK);
+    if (!in_bounds(v, j, (long)v.n + v.gcap, CK_PARTNER)) continue;
     const SplitPos b = ldsp(&sp[j]);
     const float dx = (b.hi.x - a.hi.x) + (b.lo.x - a.lo.x);
     const float dy = (b.hi.y - a.hi.y) + (b.lo.y - a.lo.y);
@@ -139,8 +140,10 @@ __global__ void __launch_bounds__(BS_VEC) k_embed_mixed(SysView v, DevTable emb,
 
 __global__ void k_ghost_dff(SysView v, SplitPos *sp) {
   const int ng = v.counters[0];
-  for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < ng; g += gridDim.x * blockDim.x)
-    if (v.gowner[g] >= 0) sp[v.n + g].lo.w = sp[v.gowner[g]].lo.w;
+  for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < ng; g += gridDim.x * blockDim.x) {
+    const int o = v.gowner[g];
+    if (o >= 0 && in_bounds(v, o, v.n, CK_OWNER)) sp[v.n + g].lo.w = sp[o].lo.w;
+  }
 }
 
 // where the fused rows are read from
@@ -166,6 +169,7 @@ __device__ __forceinline__ void force_row_mixed(const SysView &v, const DevTable
   for (int k = 0; k < nn; k++) {
     const int row = k < n1 ? k : k + back;
     const int j = (int)(__ldg(nb + (size_t)row * v.ncap) & NB_MASK);
+    if (!in_bounds(v, j, (long)v.n + v.gcap, CK_PARTNER)) continue;
     const SplitPos b = ldsp(&sp[j]);
     const float dx = (b.hi.x - a.hi.x) + (b.lo.x - a.lo.x);
     const float dy = (b.hi.y - a.hi.y) + (b.lo.y - a.lo.y);
@@ -182,7 +186,7 @@ __device__ __forceinline__ void force_row_mixed(const SysView &v, const DevTable
       const bool inp = r2 <= pair.fend[0], inr = r2 < rho.fend[0];
       if (inp || inr) {
         float chi;
-        const int kk = tab_index_f(pair, 0, r2, chi);
+        const int kk = (int)row_of(pair, 0, tab_index_f(pair, 0, r2, chi));
         float4 f0, f1;
         if (SRC == ROWS_SHARED) {
           f0 = rows[2 * kk];

@@ -386,7 +386,8 @@ __global__ void k_rb_wrap_bin(SysView v, DevScalars *sc, int *key, int *local, i
     c[a] = q;
   }
   const int lin = (v.scoff ? v.scoff[sy] : 0) + ((c[0] + 1) * cd[1] + (c[1] + 1)) * cd[2] + (c[2] + 1);
-  const int r = v.cell_rank[lin];
+  int r = v.cell_rank[lin];
+  if (!in_bounds(v, r, v.nreal_cells, CK_BIN)) r = 0;
   key[i] = r;
   local[i] = atomicAdd(&rcount[r], 1);
 }
@@ -439,7 +440,9 @@ __global__ void k_rb_scatter(SysView v, DevScalars *sc, const int *key, const in
   if (!flag) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= v.n || !rb_covers(v, flag, sys_of(v, i))) return;
-  perm[rstart[key[i]] + local[i]] = i;
+  const int slot = rstart[key[i]] + local[i];
+  if (!in_bounds(v, slot, v.n, CK_SLOT)) return;
+  perm[slot] = i;
 }
 
 // order the atoms of each cell by number (a deterministic layout); one warp
@@ -455,6 +458,7 @@ __global__ void k_rb_sort_cells(SysView v, DevScalars *sc, int *perm, const int 
   if (v.rank_sys && !rb_covers(v, sc->rebuild, v.rank_sys[r])) return;  // the whole warp
   const int s = rstart[r];
   const int c = min(rcount[r], CELLCAP);
+  if (c > 0 && (!in_bounds(v, s, v.n, CK_SLOT) || !in_bounds(v, s + c - 1, v.n, CK_SLOT))) return;
   for (int t = lane; t < c; t += 32) {
     sp[w][t] = perm[s + t];
     sn[w][t] = v.number[sp[w][t]];
@@ -476,7 +480,8 @@ __global__ void k_rb_permute(SysView v, DevScalars *sc, const int *perm, const i
   if (!flag) return;
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= v.n || !rb_covers(v, flag, sys_of(v, s))) return;  // slots stay in their system
-  const int i = perm[s];
+  int i = perm[s];
+  if (!in_bounds(v, i, v.n, CK_SLOT)) i = s;
   tpos[s] = v.pos[i];
   tmom[s] = v.mom[i];
   tnumber[s] = v.number[i];
@@ -502,7 +507,7 @@ __global__ void k_rb_copyback(SysView v, DevScalars *sc, const double4 *tpos,
   v.mom[s] = tmom[s];
   v.number[s] = tnumber[s];
   v.orig[s] = torig[s];
-  slot_of[torig[s]] = s;
+  if (in_bounds(v, torig[s], v.n, CK_SLOT)) slot_of[torig[s]] = s;
   v.ecell[s] = v.rank_lin[slot_rank[s]];
   if (oldx) {
     oldx[s] = toldx[s];
@@ -671,6 +676,7 @@ __global__ void k_rb_ghost_fill(SysView v, DevScalars *sc, const int *gstart) {
     const int g = g0 + t;
     if (g >= gend) break;
     const int owner = s0 + t;
+    if (!in_bounds(v, owner, v.n, CK_OWNER)) break;
     v.gowner[g] = owner;
     v.gcode[g] = code;
     v.ecell[v.n + g] = lin;
@@ -1461,7 +1467,8 @@ __global__ void k_pairs(SysView v, const long *rowstart, int *ni, int *nj, int *
   const double4 pi = v.pos[i];
   long o = rowstart[i];
   for (int k = 0; k < v.nnb[i]; k++, o++) {
-    const int j = (int)(v.nbr[(size_t)k * v.ncap + i] & NB_MASK);
+    int j = (int)(v.nbr[(size_t)k * v.ncap + i] & NB_MASK);
+    if (!in_bounds(v, j, (long)v.n + v.gcap, CK_PARTNER)) j = i;  // every output row is written
     const double4 pj = v.pos[j];
     r2out[o] = r2_exact(dsub(pj.x, pi.x), dsub(pj.y, pi.y), dsub(pj.z, pi.z));
     ni[o] = v.number[i];
@@ -1469,6 +1476,7 @@ __global__ void k_pairs(SysView v, const long *rowstart, int *ni, int *nj, int *
     if (j >= v.n) {
       code = v.gcode[j - v.n];
       owner = v.gowner[j - v.n];
+      if (!in_bounds(v, owner, v.n, CK_OWNER)) owner = i;
     }
     nj[o] = v.number[owner];
     shift[3 * o] = code % 3 - 1;
@@ -1482,6 +1490,7 @@ __global__ void k_gather_out(SysView v, double *x, double *p, double *f, double 
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= v.n) return;
   const int o = v.orig[s];
+  if (!in_bounds(v, o, v.n, CK_SLOT)) return;
   if (x) {
     const double4 a = v.pos[s];
     x[3 * o] = a.x;
@@ -1536,6 +1545,7 @@ __global__ void k_put_state(SysView v, const int *slot_of, const double *x, cons
   const int o = blockIdx.x * blockDim.x + threadIdx.x;
   if (o >= v.n || (skip && *skip < v.n)) return;
   const int s = slot_of[o];
+  if (!in_bounds(v, s, v.n, CK_SLOT)) return;
   double4 a = v.pos[s];
   a.x = x[3 * o];
   a.y = x[3 * o + 1];
@@ -2228,13 +2238,29 @@ static int issue_rebuild(imdgpu_sys *s) {
   return IMDGPU_OK;
 }
 
+// A checked build (-DIMDGPU_CHECK) turns a failed bounds check into an error
+// of the call that read the status word; the sites as imdgpu_check_sites
+// reports them.  Always IMDGPU_OK in the default build.
+static int bounds_status(imdgpu_sys *s) {
+#ifdef IMDGPU_CHECK
+  if (s->status_host & ST_BOUNDS) {
+    int sites = 0;
+    CK(scopy(s->st, &sites, s->counters + CK_SITES, sizeof sites, cudaMemcpyDeviceToHost));
+    return fail(IMDGPU_ERR_CUDA, "bounds check failed (sites " + std::to_string(sites) + ")");
+  }
+#else
+  (void)s;
+#endif
+  return IMDGPU_OK;
+}
+
 static int read_back(imdgpu_sys *s) {
   CK(cudaMemcpyAsync(s->hsc, s->dsc, sizeof(DevScalars), cudaMemcpyDeviceToHost, s->st));
   CK(cudaMemcpyAsync(&s->status_host, s->status, sizeof(unsigned), cudaMemcpyDeviceToHost, s->st));
   CK(cudaMemcpyAsync(&s->nbl_count_host, s->dnbl, sizeof(long), cudaMemcpyDeviceToHost, s->st));
   CK(cudaStreamSynchronize(s->st));
   s->hsc_valid = true;
-  return IMDGPU_OK;
+  return bounds_status(s);
 }
 
 // More ghost room after an overflow: with fixed per-system ranges every
@@ -2428,7 +2454,25 @@ static int autotune_forces(imdgpu_sys *s, int force, bool tile_only = false) {
 extern "C" {
 
 const char *imdgpu_last_error(void) { return g_err.c_str(); }
-const char *imdgpu_version(void) { return "imdgpu 1.0 (sm_103a)"; }
+const char *imdgpu_version(void) {
+#ifdef IMDGPU_CHECK
+  return "imdgpu 1.0 (sm_103a, bounds-checked)";
+#else
+  return "imdgpu 1.0 (sm_103a)";
+#endif
+}
+
+int imdgpu_check_sites(imdgpu_sys *s, int *checked, int *sites) {
+  if (!s || !checked || !sites) return fail(IMDGPU_ERR_ARG, "null");
+#ifdef IMDGPU_CHECK
+  *checked = 1;
+  CK(scopy(s->st, sites, s->counters + CK_SITES, sizeof(int), cudaMemcpyDeviceToHost));
+#else
+  *checked = 0;
+  *sites = 0;
+#endif
+  return IMDGPU_OK;
+}
 
 int imdgpu_device_count(int *count) {
   CK(cudaGetDeviceCount(count));
@@ -2704,6 +2748,10 @@ static int upload_table(imdgpu_sys *s, int which, HostTable &t) {
   CK(scopy(s->st, s->dcgf[which], cgf.data(), cgf.size() * sizeof(float4), cudaMemcpyHostToDevice));
   DevTable &d = s->dtab[which];
   memset(&d, 0, sizeof d);
+#ifdef IMDGPU_CHECK
+  d.chk_status = s->status;
+  d.chk_counters = s->counters;
+#endif
   d.ncols = t.ncols;
   d.rows = rows;
   d.mode = t.mode;
@@ -3087,6 +3135,7 @@ int imdgpu_nve_step_host(imdgpu_sys *s, const double *x, const double *p, double
     if (s->status_host & ST_CELLOVER)
       return fail(IMDGPU_ERR_CELL, "more than " + std::to_string(CELLCAP) + " atoms in one cell");
     if (s->status_host & ST_WAIT) return fail(IMDGPU_ERR_CUDA, kWaitMsg);
+    if ((rc = bounds_status(s))) return rc;
     if (!over) {
       if (out && (rc = fill_scalars(s, out))) return rc;
       return (s->status_host & ST_SHORT) ? IMDGPU_WARN_SHORT : IMDGPU_OK;
@@ -3887,6 +3936,7 @@ int imdgpu_nve_run(imdgpu_sys *s, int nsteps, double dt, double *epot, double *e
       rc = fail(IMDGPU_ERR_CUDA, kWaitMsg);
       break;
     }
+    if ((rc = bounds_status(s))) break;
     if (s->status_host & (ST_NBOVER | ST_GHOSTOVER)) {
       // restore the chunk's start, grow and redo it; eight overflows of one
       // chunk in a row mean the growth does not converge
@@ -4768,6 +4818,7 @@ int imdgpu_batch_advance(imdgpu_sys *s, int max_rounds, int *ndone_out, int *rou
       rc = fail(IMDGPU_ERR_CUDA, kWaitMsg);
       break;
     }
+    if ((rc = bounds_status(s))) break;
     const bool overflow = (s->status_host & (ST_NBOVER | ST_GHOSTOVER)) != 0;
     const bool inject = !overflow && B.inject_left > 0 && B.inject_ok >= B.inject_every;
     if (inject) {

@@ -473,6 +473,19 @@ int imdgpu_set_pair_cache(imdgpu_sys *sys, int on);
  * denominator for the FP64 force kernels. */
 int imdgpu_probe_fp64_peak(double *tflops);
 
+/* Bounds-checked build (compiled with -DIMDGPU_CHECK; `python -m
+ * imd_gb300.build --check` writes imd_gb300/libimdgpu_check.so).  No
+ * counterpart in the reference.  The kernels check the indices they take
+ * from device data before using them; imdgpu_check_sites returns the checks
+ * that failed since the system was created, as a mask: 1 a list partner
+ * outside the real and ghost slots, 2 a ghost's owner outside the real
+ * atoms, 4 a table row or column outside its table, 8 an atom's bin outside
+ * the cell grid, 16 a permutation slot or caller index outside the atoms.
+ * A failed check also sets flag 32 of the status word, and the access is
+ * skipped or its index clamped.  *checked is 0 (and *sites 0) in the
+ * default build, which has no checks. */
+int imdgpu_check_sites(imdgpu_sys *sys, int *checked, int *sites);
+
 /* move_atoms_nve for callers that cannot allocate device memory.  No
  * counterpart in the reference: IMD allocates everything itself.  Meant for
  * host programs whose device memory all comes from their own pool or arena,
