@@ -4771,15 +4771,17 @@ int imdgpu_batch_advance(imdgpu_sys *s, int max_rounds, int *ndone_out, int *rou
     CKR(cudaMemcpyAsync(bnd, s->d_ndone, sizeof(int), cudaMemcpyDeviceToDevice, s->st));
     CKR(cudaMemcpyAsync(bcs, s->d_cs, sizeof(CgSys) * ns, cudaMemcpyDeviceToDevice, s->st));
     CKR(cudaMemsetAsync(s->status, 0, sizeof(unsigned), s->st));
-    std::vector<uintptr_t> key = {(uintptr_t)s->pos, (uintptr_t)s->nbr, (uintptr_t)s->xl,
-                                  (uintptr_t)s->nbcap, (uintptr_t)s->gcap,
-                                  (uintptr_t)s->precision, (uintptr_t)s->exact,
-                                  (uintptr_t)s->n, (uintptr_t)s->nsys, (uintptr_t)s->d_cs,
-                                  (uintptr_t)s->bt_engine, (uintptr_t)s->d_order,
-                                  (uintptr_t)s->pcache, (uintptr_t)s->lpa,
-                                  (uintptr_t)s->bs_rho, (uintptr_t)s->bs_force,
-                                  (uintptr_t)s->percell_rb, (uintptr_t)s->d_goff,
-                                  (uintptr_t)s->gcap};
+    // the graph holds every pointer and size its kernels were given: the
+    // whole kernel view and force tables (as the NVE graphs), and the CG
+    // engine's own arrays
+    if (s->bt_engine && !s->engine_grid) s->engine_grid = batch_engine_grid();
+    std::vector<uintptr_t> key = graph_key(s, 0.0);
+    for (uintptr_t u : {(uintptr_t)s->nsys, (uintptr_t)s->d_cs, (uintptr_t)s->bt_engine,
+                        (uintptr_t)s->engine_grid, (uintptr_t)s->d_order, (uintptr_t)s->d_aoff,
+                        (uintptr_t)s->d_sys_done, (uintptr_t)s->d_sys_short, (uintptr_t)s->cgg,
+                        (uintptr_t)s->cgh, (uintptr_t)s->d_maxd, (uintptr_t)s->d_ndone,
+                        (uintptr_t)s->d_queue, (uintptr_t)s->dsc})
+      key.push_back(u);
     if (s->use_graph) {
       if (!B.gx || key != B.gkey) {
         if (B.gx) cudaGraphExecDestroy(B.gx);
