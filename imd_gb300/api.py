@@ -195,6 +195,7 @@ def lib() -> C.CDLL:
         L.imdgpu_batch_replays.argtypes = [vp, C.POINTER(C.c_long)]
         L.imdgpu_batch_inject_replays.argtypes = [vp, C.c_int, C.c_int]
         L.imdgpu_check_sites.argtypes = [vp, _ip, _ip]
+        L.imdgpu_ml_set_tensor_cores.argtypes = [vp, C.c_int]
         L.imdgpu_batch_positions.argtypes = [vp, _dp]
         fp = C.POINTER(C.c_float)
         L.imdgpu_ml_nparam.argtypes = []
@@ -563,6 +564,11 @@ class GpuSystem:
         return ni, nj, sh, r2
 
     # --- learned start ---------------------------------------------------------
+    def ml_set_tensor_cores(self, on: bool) -> None:
+        """Forward pass on tcgen05 instead of mma.sync
+        (imdgpu_ml_set_tensor_cores)."""
+        _check(lib().imdgpu_ml_set_tensor_cores(self.h, int(bool(on))), "ml_set_tensor_cores")
+
     def ml_set_weights(self, w) -> None:
         w = np.ascontiguousarray(w, np.float32)
         _check(lib().imdgpu_ml_set_weights(self.h, _p(w, C.c_float), len(w)), "ml_set_weights")

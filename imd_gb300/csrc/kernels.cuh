@@ -115,6 +115,9 @@ void launch_ml_forward(const MlPair *pairs, const int *np, const double *rho,
                        cudaStream_t st);
 void launch_ml_loss(int n, const float *dxp, const float *target, const float *wt, float *dldx,
                     double *loss, cudaStream_t st);
+void launch_ml_forward_tc(const MlPair *pairs, const int *np, const double *rho,
+                          const __nv_bfloat16 *wb, const float *wf, float *dxp, unsigned *status,
+                          int blocks, cudaStream_t st);
 void launch_ml_backward(const MlPair *pairs, const int *np, const double *rho,
                         const __nv_bfloat16 *wb, const float *wf, const float *dldx,
                         float *grad, int blocks, cudaStream_t st);

@@ -11,7 +11,8 @@
 // layer are FP32.  The backward kernel recomputes the forward pass of its
 // tile and accumulates weight gradients per block in FP32 before one atomic
 // add per weight; Adam updates FP32 master weights and refreshes the BF16
-// copies.
+// copies.  k_ml_forward_tc is the forward pass on tcgen05 with tensor-memory
+// accumulators, opt-in per system.
 #include <cuda_bf16.h>
 
 #include "kernels.cuh"
@@ -272,6 +273,281 @@ __global__ void __launch_bounds__(128) k_ml_forward(const MlPair *pairs, const i
   }
 }
 
+// ---------------------------------------------------------------------------
+// The forward pass on the fifth-generation tensor cores (tcgen05); opt-in
+// per system (imdgpu_ml_set_tensor_cores), the mma.sync kernel above is the
+// default.  One CTA of 128 threads takes 128 pairs per tile:
+// - the tile's features (A: 128 x 32) and the weights (B: W1 64 x 32 and
+//   W2 64 x 64, [out][in]) sit in shared memory as 8-row x 16-byte core
+//   matrices, K-major, without swizzle;
+// - one thread issues tcgen05.mma (M 128, N 64, K 16; BF16 in, FP32
+//   accumulate) into tensor memory: 128 lanes (one pair each) x 128
+//   columns, layer 1 in columns 0-63 and layer 2 in 64-127, and commits to
+//   an mbarrier that the CTA waits on (bounded);
+// - each warp reads its 32 lanes with tcgen05.ld, one pair per thread;
+//   layer 1's epilogue (bias, SiLU, BF16) writes the A operand of layer 2;
+// - layer 3 (64 -> 1) and the scatter of w_ij * unit(r_ij) stay on the CUDA
+//   cores, one pair per thread, with no shuffles.
+// A wait that runs out sets ST_WAIT in the status word; the CTA then stops,
+// waits once more (bounded) for its products and frees its tensor memory.
+// ---------------------------------------------------------------------------
+constexpr int TC_M = 128;                  // pairs per tile = TMEM lanes
+constexpr uint32_t TC_COLS = 128;          // TMEM columns of a CTA
+constexpr uint32_t TC_WAIT_LIMIT = 1u << 22;
+constexpr int TC_SMEM = 56 * 1024;         // at most 4 CTAs (512 TMEM columns) per SM
+
+// byte offset of element (r, k) of an R x K BF16 operand stored as 8 x 8
+// core matrices (8 rows of 16 bytes): the K / 8 core matrices of an 8-row
+// group side by side (leading byte offset 128 along K), the groups one
+// after another (stride byte offset K / 8 * 128)
+__device__ __forceinline__ int core_off(int r, int k, int K) {
+  return ((r >> 3) * (K >> 3) + (k >> 3)) * 128 + (r & 7) * 16 + (k & 7) * 2;
+}
+
+struct TcSmem {
+  alignas(1024) __nv_bfloat16 X[TC_M * ML_K1];
+  alignas(1024) __nv_bfloat16 H1[TC_M * ML_H];
+  alignas(1024) __nv_bfloat16 W1[ML_H * ML_K1];
+  alignas(1024) __nv_bfloat16 W2[ML_H * ML_H];
+  float b1[ML_H], b2[ML_H], W3[ML_H];
+  float b3;
+  float ux[TC_M], uy[TC_M], uz[TC_M];
+  int ip[TC_M];
+  alignas(8) unsigned long long mbar;
+  uint32_t tmem;
+};
+static_assert(sizeof(TcSmem) + 1024 <= TC_SMEM, "tcgen05 MLP shared memory");
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+// shared-memory matrix descriptor: start address, leading and stride byte
+// offsets (16-byte units, 14 bits each), descriptor version 1 (bits 46-47),
+// base offset 0, no swizzle (bits 61-63 = 0)
+__device__ __forceinline__ uint64_t tc_sdesc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+         ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+// kind::f16 instruction descriptor: D FP32 (bits 4-5 = 1), A and B BF16
+// (bits 7-9 and 10-12 = 1), both K-major (bits 15, 16 = 0), N / 8 from bit
+// 17, M / 16 from bit 24
+__host__ __device__ constexpr uint32_t tc_idesc(int M, int N) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) |
+         ((uint32_t)(M >> 4) << 24);
+}
+static_assert(tc_idesc(128, 64) == 0x08100490u, "instruction descriptor");
+
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+// generic-proxy writes to shared memory made visible to the tensor core
+__device__ __forceinline__ void fence_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void tc_mma(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc,
+                                       uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d),
+      "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+__device__ __forceinline__ void tc_commit(uint32_t mbar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar)
+      : "memory");
+}
+// 16 consecutive FP32 columns of this thread's lane; the load and its wait
+// in one statement, so no use of the registers comes before the wait
+__device__ __forceinline__ void tc_ld16(uint32_t taddr, float (&v)[16]) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
+      "%14,%15}, [%16];\n\ttcgen05.wait::ld.sync.aligned;"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+        "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr)
+      : "memory");
+#pragma unroll
+  for (int q = 0; q < 16; q++) v[q] = __uint_as_float(r[q]);
+}
+__device__ __forceinline__ bool tc_mbar_try(uint32_t mbar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}\n"
+      : "=r"(ok)
+      : "r"(mbar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ bool tc_mbar_wait(uint32_t mbar, uint32_t parity) {
+  for (uint32_t it = 0; it < TC_WAIT_LIMIT; it++)
+    if (tc_mbar_try(mbar, parity)) return true;
+  return false;
+}
+
+__global__ void __launch_bounds__(128) k_ml_forward_tc(const MlPair *pairs, const int *npairs,
+                                                       const double *rho,
+                                                       const __nv_bfloat16 *wb, const float *wf,
+                                                       float *dxp, unsigned *status) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  TcSmem &S = *reinterpret_cast<TcSmem *>(smraw + ((1024u - (smem_u32(smraw) & 1023u)) & 1023u));
+  const int tid = threadIdx.x, warp = tid >> 5;
+  for (int e = tid; e < ML_H * ML_K1; e += blockDim.x)
+    *reinterpret_cast<__nv_bfloat16 *>(reinterpret_cast<char *>(S.W1) +
+                                       core_off(e / ML_K1, e % ML_K1, ML_K1)) = wb[OFF_W1 + e];
+  for (int e = tid; e < ML_H * ML_H; e += blockDim.x)
+    *reinterpret_cast<__nv_bfloat16 *>(reinterpret_cast<char *>(S.W2) +
+                                       core_off(e / ML_H, e % ML_H, ML_H)) = wb[OFF_W2 + e];
+  for (int k = tid; k < ML_H; k += blockDim.x) {
+    S.b1[k] = wf[OFF_B1 + k];
+    S.b2[k] = wf[OFF_B2 + k];
+    S.W3[k] = __bfloat162float(wb[OFF_W3 + k]);
+  }
+  const uint32_t mbar = smem_u32(&S.mbar);
+  if (tid == 0) {
+    S.b3 = wf[OFF_B3];
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(&S.tmem)),
+                 "r"(TC_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = S.tmem;
+  const uint32_t lane_base = tmem + ((uint32_t)(32 * warp) << 16);  // this warp's 32 lanes
+  const uint32_t idesc = tc_idesc(TC_M, ML_H);
+  const uint32_t xa = smem_u32(S.X), ha = smem_u32(S.H1);
+  const uint32_t w1a = smem_u32(S.W1), w2a = smem_u32(S.W2);
+  const int np = *npairs;
+  uint32_t parity = 0;
+  bool failed = false;
+  for (int p0 = blockIdx.x * TC_M; p0 < np; p0 += gridDim.x * TC_M) {
+    {  // features of pair p0 + tid (row tid of A), as ml_features
+      const int p = p0 + tid;
+      float f[ML_K1];
+#pragma unroll
+      for (int k = 0; k < ML_K1; k++) f[k] = 0.f;
+      float ux = 0.f, uy = 0.f, uz = 0.f;
+      int i = -1;
+      if (p < np) {
+        const MlPair P = pairs[p];
+        const float r = sqrtf(P.dx * P.dx + P.dy * P.dy + P.dz * P.dz);
+        const float ir = 1.0f / r;
+        ux = P.dx * ir;
+        uy = P.dy * ir;
+        uz = P.dz * ir;
+        i = P.i;
+#pragma unroll
+        for (int k = 0; k < 16; k++) {
+          const float c = 2.0f + k * (3.5f / 15.0f);
+          const float t = (r - c) * (1.0f / 0.25f);
+          f[k] = __expf(-0.5f * t * t);
+        }
+        f[16] = (float)rho[i] * 0.01f;
+      }
+#pragma unroll
+      for (int k8 = 0; k8 < ML_K1; k8 += 8) {
+        const uint4 q = make_uint4(pack2(f[k8], f[k8 + 1]), pack2(f[k8 + 2], f[k8 + 3]),
+                                   pack2(f[k8 + 4], f[k8 + 5]), pack2(f[k8 + 6], f[k8 + 7]));
+        *reinterpret_cast<uint4 *>(reinterpret_cast<char *>(S.X) + core_off(tid, k8, ML_K1)) = q;
+      }
+      S.ux[tid] = ux;
+      S.uy[tid] = uy;
+      S.uz[tid] = uz;
+      S.ip[tid] = i;
+    }
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (tid == 0) {  // layer 1: D[0, 64) = X W1^T over K = 32
+#pragma unroll
+      for (int k = 0; k < ML_K1 / 16; k++)
+        tc_mma(tmem, tc_sdesc(xa + 256 * k, 128, ML_K1 / 8 * 128),
+               tc_sdesc(w1a + 256 * k, 128, ML_K1 / 8 * 128), idesc, k > 0);
+      tc_commit(mbar);
+    }
+    failed = !tc_mbar_wait(mbar, parity);
+    parity ^= 1u;
+    if (__syncthreads_or(failed)) {
+      failed = true;
+      break;
+    }
+    tc_fence_after();
+#pragma unroll
+    for (int c0 = 0; c0 < ML_H; c0 += 16) {  // bias, SiLU, BF16 -> row tid of H1
+      float d[16];
+      tc_ld16(lane_base + c0, d);
+#pragma unroll
+      for (int h = 0; h < 16; h += 8) {
+        float a[8];
+#pragma unroll
+        for (int q = 0; q < 8; q++) a[q] = silu(d[h + q] + S.b1[c0 + h + q]);
+        const uint4 q = make_uint4(pack2(a[0], a[1]), pack2(a[2], a[3]), pack2(a[4], a[5]),
+                                   pack2(a[6], a[7]));
+        *reinterpret_cast<uint4 *>(reinterpret_cast<char *>(S.H1) + core_off(tid, c0 + h, ML_H)) =
+            q;
+      }
+    }
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (tid == 0) {  // layer 2: D[64, 128) = H1 W2^T over K = 64
+#pragma unroll
+      for (int k = 0; k < ML_H / 16; k++)
+        tc_mma(tmem + ML_H, tc_sdesc(ha + 256 * k, 128, ML_H / 8 * 128),
+               tc_sdesc(w2a + 256 * k, 128, ML_H / 8 * 128), idesc, k > 0);
+      tc_commit(mbar);
+    }
+    failed = !tc_mbar_wait(mbar, parity);
+    parity ^= 1u;
+    if (__syncthreads_or(failed)) {
+      failed = true;
+      break;
+    }
+    tc_fence_after();
+    float w = S.b3;  // layer 3 on this thread's pair
+#pragma unroll
+    for (int c0 = 0; c0 < ML_H; c0 += 16) {
+      float d[16];
+      tc_ld16(lane_base + ML_H + c0, d);
+#pragma unroll
+      for (int q = 0; q < 16; q++) w += silu(d[q] + S.b2[c0 + q]) * S.W3[c0 + q];
+    }
+    const int i = S.ip[tid];
+    if (i >= 0) {
+      atomicAdd(&dxp[3 * i], w * S.ux[tid]);
+      atomicAdd(&dxp[3 * i + 1], w * S.uy[tid]);
+      atomicAdd(&dxp[3 * i + 2], w * S.uz[tid]);
+    }
+  }
+  if (failed) {  // the products of the last commit, once more before the memory goes
+    if (tid == 0) atomicOr(status, ST_WAIT);
+    tc_mbar_wait(mbar, parity ^ 1u);
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(TC_COLS)
+                 : "memory");
+  }
+}
+
 // loss = sum_i |dx_i - t_i|^2 / N; writes dL/d(dx_i) and the block sums of
 // the loss
 __global__ void k_ml_loss(int n, const float *dxp, const float *target, const float *wt,
@@ -505,6 +781,16 @@ void launch_ml_forward(const MlPair *pairs, const int *np, const double *rho,
                        const __nv_bfloat16 *wb, const float *wf, float *dxp, int blocks,
                        cudaStream_t st) {
   k_ml_forward<<<blocks, 128, sizeof(MlSmem), st>>>(pairs, np, rho, wb, wf, dxp);
+}
+void launch_ml_forward_tc(const MlPair *pairs, const int *np, const double *rho,
+                          const __nv_bfloat16 *wb, const float *wf, float *dxp, unsigned *status,
+                          int blocks, cudaStream_t st) {
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_ml_forward_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM);
+    attr = true;
+  }
+  k_ml_forward_tc<<<blocks, 128, TC_SMEM, st>>>(pairs, np, rho, wb, wf, dxp, status);
 }
 void launch_ml_loss(int n, const float *dxp, const float *target, const float *wt, float *dldx,
                     double *loss, cudaStream_t st) {

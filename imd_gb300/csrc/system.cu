@@ -239,6 +239,7 @@ struct imdgpu_sys {
   int *ml_np = nullptr;
   float *ml_dx = nullptr, *ml_target = nullptr, *ml_dldx = nullptr;
   float *ml_wt = nullptr;              // per-atom loss weights by slot (training)
+  int ml_tc = 0;                       // forward pass on tcgen05 (imdgpu_ml_set_tensor_cores)
   std::vector<double> ml_wt_host;      // the same in caller order; empty: uniform
   double *ml_loss = nullptr;
   int ml_have = 0;
@@ -5092,6 +5093,17 @@ static int ml_blocks() { return 152 * 8; }
 
 static int ml_forward(imdgpu_sys *s) {
   CK(cudaMemsetAsync(s->ml_dx, 0, sizeof(float) * 3 * s->n, s->st));
+  if (s->ml_tc) {
+    // four CTAs of 128 TMEM columns per SM; a wait that ran out sets ST_WAIT
+    CK(cudaMemsetAsync(s->status, 0, sizeof(unsigned), s->st));
+    launch_ml_forward_tc(s->ml_pairs, s->ml_np, s->rho, s->ml_wb, s->ml_w, s->ml_dx, s->status,
+                         152 * 4, s->st);
+    CK(cudaGetLastError());
+    unsigned st = 0;
+    CK(scopy(s->st, &st, s->status, sizeof st, cudaMemcpyDeviceToHost));
+    if (st & ST_WAIT) return fail(IMDGPU_ERR_CUDA, kWaitMsg);
+    return IMDGPU_OK;
+  }
   launch_ml_forward(s->ml_pairs, s->ml_np, s->rho, s->ml_wb, s->ml_w, s->ml_dx, ml_blocks(), s->st);
   CK(cudaGetLastError());
   return IMDGPU_OK;
@@ -5100,6 +5112,12 @@ static int ml_forward(imdgpu_sys *s) {
 extern "C" {
 
 int imdgpu_ml_nparam(void) { return ml_nparam(); }
+
+int imdgpu_ml_set_tensor_cores(imdgpu_sys *s, int on) {
+  if (!s) return fail(IMDGPU_ERR_ARG, "null system");
+  s->ml_tc = on ? 1 : 0;
+  return IMDGPU_OK;
+}
 
 int imdgpu_ml_set_weights(imdgpu_sys *s, const float *w, int n) {
   if (!s || !w || n != ml_nparam()) return fail(IMDGPU_ERR_ARG, "weights: wrong size");

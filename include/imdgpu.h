@@ -340,6 +340,10 @@ int imdgpu_batch_results(imdgpu_sys *sys, double *epot, double *fmax, int *steps
  * array of imdgpu_ml_nparam() values (W1[64][32] with inputs >= 17 zero,
  * b1[64], W2[64][64], b2[64], W3[64], b3). */
 int imdgpu_ml_nparam(void);
+/* The forward pass on the fifth-generation tensor cores (tcgen05.mma into
+ * tensor memory, 128 pairs per CTA) instead of mma.sync (default 0).  The
+ * backward pass stays on mma.sync.  Not yet run on a GPU: off by default. */
+int imdgpu_ml_set_tensor_cores(imdgpu_sys *sys, int on);
 int imdgpu_ml_set_weights(imdgpu_sys *sys, const float *w, int n);
 int imdgpu_ml_get_weights(imdgpu_sys *sys, float *w, int n);
 /* Adam first and second moments (imdgpu_ml_nparam() floats each) and step

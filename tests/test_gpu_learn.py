@@ -1,6 +1,8 @@
 """Learned start: the hand-written BF16 tensor-core forward and backward
 kernels of the per-pair MLP against the numpy oracle (same BF16 rounding
 points), and Adam training on the GPU reducing the loss."""
+import os
+
 import numpy as np
 import pytest
 
@@ -40,6 +42,31 @@ def test_mlp_forward_and_gradients_match_oracle():
     assert rel(grad_g, grad_o) < 1e-2
     for lo, hi in ((M.OFF_W1, M.OFF_B1), (M.OFF_W2, M.OFF_B2), (M.OFF_W3, M.OFF_B3)):
         assert rel(grad_g[lo:hi], grad_o[lo:hi]) < 2e-2
+
+
+@pytest.mark.skipif(os.environ.get("IMDGPU_TRY_TCGEN05") != "1",
+                    reason="the tcgen05 forward pass has not run on a GPU yet; "
+                           "IMDGPU_TRY_TCGEN05=1 runs it")
+def test_tcgen05_forward_matches_mma_sync_and_oracle():
+    """The forward pass on tcgen05 (tensor memory, 128 pairs per CTA)
+    against the mma.sync forward on the same pairs and weights, and against
+    the oracle (the bar of the mma.sync test).  Both paths multiply the same
+    BF16 operands in FP32; only the order of the FP32 sums differs."""
+    import mlp_oracle as M
+    g = golden("cu_pert")
+    s = _system(g)
+    w = M.init_weights(3)
+    s.ml_set_weights(w)
+    s.calc_forces(0)
+    dx_sync = s.ml_predict()
+    s.ml_set_tensor_cores(True)
+    dx_tc = s.ml_predict()
+    s.ml_set_tensor_cores(False)
+    assert np.all(np.isfinite(dx_tc))
+    assert rel(dx_tc, dx_sync) < 1e-4, rel(dx_tc, dx_sync)
+    pi, d = M.pairs_min_image(g["x"], g["box"])
+    _, _, dx_o = M.loss_and_grad(w, pi, d, g["rho"], np.zeros_like(dx_sync))
+    assert rel(dx_tc, dx_o) < 2e-3
 
 
 def test_training_reduces_loss():
