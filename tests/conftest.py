@@ -14,6 +14,13 @@ for p in (ROOT, os.path.join(ROOT, "oracle")):
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300) and the built extension")
+    config.addinivalue_line("markers", "late: a path whose first GPU run this is; runs last")
+
+
+def pytest_collection_modifyitems(config, items):
+    # tests marked late go after the others (stable order otherwise), so
+    # that under -x a failure there hides no other result
+    items.sort(key=lambda it: it.get_closest_marker("late") is not None)
 
 
 def golden(name):

@@ -30,6 +30,7 @@ RUN = [
 ]
 
 
+@pytest.mark.late
 def test_parity_and_batch_tests_pass_in_the_checked_build():
     from imd_gb300 import build
     lib = build.build(check=True)
