@@ -280,7 +280,9 @@ def run_batch(args, tabs, rank=0, world=1, dist=None):
                        "<100> dumbbells, +-2%% strain, 0.05 A noise, seed 6; IMD CG to max |F| "
                        "<= 1e-4 eV/A, FP64, spline tables" % (len(cells), natoms.sum(),
                                                               natoms.min(), natoms.max()),
-           "unit": "relaxations/s", "sharding": "%d ranks, cells split by atom count" % world}
+           "unit": "relaxations/s", "sharding": "%d ranks, cells split by atom count" % world,
+           "list_rebuilds": "whole batch: a round rebuilds every cell's list once any cell "
+                            "moved past skin/2 (the library default; per-system rebuilds off)"}
     cells4 = wl.defect_batch(args.batch_cells, seed=4)
     natoms4 = np.array([c.n for c in cells4])
     mine4 = shard.shard_cells(natoms4, world)[rank]
